@@ -1,0 +1,306 @@
+/*
+ * trayracer.h - C ABI of the GB300 wavefront path-tracing hot path.
+ *
+ * One context owns one scene, one film and the SoA wavefront buffers on one
+ * CUDA device. Every entry point returns a tr_status and never exits the
+ * process. Pointers are plain host or device pointers as documented per call;
+ * streams are passed as opaque `void*` (a cudaStream_t, NULL = legacy default
+ * stream). A context is driven by one host thread at a time.
+ *
+ * The per-stage entry points map 1:1 onto the stages of the reference
+ * renderer (rdbruijne/trayracer):
+ *   tr_generate   <- OptiX __raygen__ RayGenModes::Primary (camera rays)
+ *                    Tracer/Optix/GPU/optix.cu:235-276, launched from
+ *                    Tracer/Renderer/DeviceRenderer.cpp:215-218
+ *   tr_extend     <- OptiX __raygen__ RayGenModes::Secondary + __closesthit__/
+ *                    __miss__, Tracer/Optix/GPU/optix.cu:203-218,278-314;
+ *                    for bounce 0 this is the trace half of the Primary mode
+ *   tr_shade      <- Shade(RenderModes::PathTracing, DECLARE_KERNEL_PARAMS)
+ *                    Tracer/CUDA/GPU/CudaFwd.h:34, Tracer/CUDA/GPU/cuda.cu:22-84,
+ *                    kernel Tracer/CUDA/GPU/Shade/PathTracing.h:8-175
+ *   tr_connect    <- OptiX __raygen__ RayGenModes::Shadow,
+ *                    Tracer/Optix/GPU/optix.cu:316-343
+ *   tr_finalize   <- FinalizeFrame, Tracer/CUDA/GPU/CudaUtilityKernels.h:27-44
+ *   tr_begin_frame<- DeviceRenderer::PreRender + InitCudaCounters,
+ *                    Tracer/Renderer/DeviceRenderer.cpp:137-177,
+ *                    Tracer/CUDA/GPU/CudaUtilityKernels.h:6-20
+ *   tr_render_frame <- DeviceRenderer::RenderFrame bounce loop,
+ *                    Tracer/Renderer/DeviceRenderer.cpp:97-133
+ *   tr_scene_upload <- Renderer::UpdateScene/UploadGeometry/UploadMaterials and
+ *                    the SetCuda* setters, Tracer/Renderer/Renderer.cpp:79-143,
+ *                    442-527, Tracer/CUDA/GPU/CudaFwd.h:9-31; the OptiX
+ *                    acceleration build (Tracer/Optix/OptixRenderer.cpp:90-123,
+ *                    Tracer/Resources/Model.cpp:240-306) is replaced by a host
+ *                    built 8-wide compressed BVH
+ *   tr_set_camera <- DeviceRenderer::SetCamera, DeviceRenderer.cpp:25-40
+ *   tr_set_settings <- KernelSettings, Tracer/Common/CommonStructs.h:145-153
+ *   tr_get_statistics <- RenderStatistics::DeviceStatistics,
+ *                    Tracer/Renderer/RenderStatistics.h:11-26, and RayCounters,
+ *                    Tracer/Common/CommonStructs.h:208-212
+ */
+#ifndef TRAYRACER_H
+#define TRAYRACER_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define TR_ABI_VERSION 1u
+
+/* Maximum path length; the reference's DeviceRenderer::MaxTraceDepth
+ * (Tracer/Renderer/DeviceRenderer.h:29). */
+#define TR_MAX_DEPTH 16u
+
+/* Largest number of paths in flight: path indices are packed in 28 bits
+ * (PackedPathIxShift = 4, Tracer/Common/CommonStructs.h:46-71). */
+#define TR_MAX_PATHS (1u << 28)
+
+typedef enum tr_status {
+    TR_OK = 0,
+    TR_ERR_INVALID_ARGUMENT = 1,
+    TR_ERR_OUT_OF_MEMORY = 2,
+    TR_ERR_CUDA = 3,
+    TR_ERR_NO_SCENE = 4,
+    TR_ERR_NOT_READY = 5,
+    TR_ERR_LIMIT = 6,
+    TR_ERR_DEVICE_FAULT = 7
+} tr_status;
+
+/* Closure (BSDF) per material. The reference selects its closure by commenting
+ * code in Tracer/CUDA/GPU/Shade/PathTracing.h:127-129 (Lambert live); here it
+ * is a material property. */
+typedef enum tr_closure {
+    TR_CLOSURE_LAMBERT = 0, /* Shade/BSDF/Lambert.h:53-59 */
+    TR_CLOSURE_DIFFUSE = 1, /* Shade/BSDF/Diffuse.h:36-42 */
+    TR_CLOSURE_DISNEY = 2   /* Shade/BSDF/Disney.h:573-579 */
+} tr_closure;
+
+/* Kernel setting flags. */
+enum {
+    /* Reproduce the reference's sampling exactly: TEA/LCG random streams
+     * (thirdparty/CUDA/random.h:31-67, seeded as in optix.cu:247 and
+     * PathTracing.h:103), binary-search light pick over the exclusive energy
+     * prefix (CudaLights.h:38-59) with LightEnergy = last prefix
+     * (Renderer.cpp:500), three independent light barycentrics
+     * (CudaLights.h:107-108), its emissive-hit weighting (PathTracing.h:76-97),
+     * its Disney lobe-sample reuse of r0 (Disney.h:491-521) and its NEE gate
+     * (CudaLights.h:118). Without this flag the path uses the counter-based
+     * RNG, an alias-table light pick, uniform triangle points, balance-
+     * heuristic MIS on emissive hits and a rescaled lobe sample. */
+    TR_FLAG_REFERENCE_SAMPLING = 1u << 0,
+    /* Write the first-hit albedo and normal guide buffers
+     * (PathTracing.h:48-52,66-70,93-97). */
+    TR_FLAG_WRITE_AOVS = 1u << 1,
+    /* With TR_FLAG_REFERENCE_SAMPLING: take the random numbers that the
+     * reference draws as arguments of one call (camera jitter optix.cu:147,
+     * lens sample optix.cu:55, light barycentrics CudaLights.h:107, closure
+     * r0/r1 PathTracing.h:129) right to left instead of left to right. C++
+     * leaves that order unspecified; right to left is what the g++ host build
+     * of the reference does. */
+    TR_FLAG_REFERENCE_DRAW_RTL = 1u << 2,
+    /* Count the BVH nodes visited and triangles tested by the extend and
+     * connect launches (tr_statistics.traversal_*). Adds atomics; for
+     * measurement runs outside timed regions. */
+    TR_FLAG_COUNT_TRAVERSAL = 1u << 3
+};
+
+/* ≙ KernelSettings (Tracer/Common/CommonStructs.h:145-153) plus the knobs the
+ * reference hard-wires. */
+typedef struct tr_kernel_settings {
+    uint32_t multi_sample;   /* samples per pixel in one frame (paths in flight = W*H*multi_sample) */
+    uint32_t max_depth;      /* bounces per path, <= TR_MAX_DEPTH */
+    uint32_t seed;           /* frame seed */
+    float ray_epsilon;       /* tmin of every ray, shadow tmax = dist - 2*eps */
+    uint32_t rr_start;       /* first path length with Russian roulette (reference: 1); >= max_depth disables */
+    uint32_t flags;          /* TR_FLAG_* */
+    float max_color;         /* firefly clamp of SafeColor (CudaUtility.h:91); <= 0 selects 10 */
+    uint32_t reserved;
+} tr_kernel_settings;
+
+/* ≙ the camera fields of LaunchParams (Tracer/Common/CommonStructs.h:170-184). */
+typedef struct tr_camera {
+    float position[3];
+    float side[3];
+    float up[3];
+    float forward[3];
+    float aperture;
+    float distortion;
+    float focal_dist;
+    float fov;              /* radians */
+    int32_t bokeh_side_count;
+    float bokeh_rotation;
+} tr_camera;
+
+/* One material with constant properties (the reference's 13 material
+ * properties, Tracer/Common/CommonStructs.h:78-93; values are rounded to fp16
+ * on upload as Material::Property::Build does, Material.cpp:56-78). */
+typedef struct tr_material_desc {
+    float diffuse[3];
+    float emissive[3];
+    float metallic;
+    float subsurface;
+    float specular;
+    float roughness;
+    float specular_tint;
+    float anisotropic;
+    float sheen;
+    float sheen_tint;
+    float clearcoat;
+    float clearcoat_gloss;
+    uint32_t closure;       /* tr_closure */
+} tr_material_desc;
+
+/* One triangle mesh (≙ Model, Tracer/Resources/Model.h). Normals and
+ * texcoords are per vertex and optional (NULL: face normal / zero uv). */
+typedef struct tr_mesh_desc {
+    const float* positions;        /* float3 x vertex_count */
+    const float* normals;          /* float3 x vertex_count or NULL */
+    const float* texcoords;        /* float2 x vertex_count or NULL */
+    uint32_t vertex_count;
+    uint32_t triangle_count;
+    const uint32_t* indices;       /* uint3 x triangle_count */
+    const uint32_t* material_indices; /* triangle_count entries into the scene material list */
+} tr_mesh_desc;
+
+typedef struct tr_scene_desc {
+    const tr_mesh_desc* mesh;      /* one mesh, one identity instance */
+    const tr_material_desc* materials;
+    uint32_t material_count;
+    uint32_t bvh_leaf_size;        /* 1..3 triangles per leaf, 0 = default (3) */
+    uint32_t build_threads;        /* host threads for the BVH build, 0 = all */
+    uint32_t reserved;
+} tr_scene_desc;
+
+typedef struct tr_config {
+    int32_t device;                /* CUDA device ordinal */
+    uint32_t abi_version;          /* TR_ABI_VERSION */
+} tr_config;
+
+/* ≙ RenderStatistics::DeviceStatistics (RenderStatistics.h:11-26) + per-stage
+ * device times of the last frame, measured with CUDA events on the stream the
+ * frame was rendered on. */
+typedef struct tr_statistics {
+    uint64_t path_count;            /* extend + shadow rays of the last frame */
+    uint64_t primary_path_count;
+    uint64_t secondary_path_count;
+    uint64_t deep_path_count;
+    uint64_t shadow_ray_count;
+    uint32_t extend_rays[TR_MAX_DEPTH]; /* queue length per bounce */
+    uint32_t shadow_rays[TR_MAX_DEPTH];
+    float render_time_ms;
+    float generate_time_ms;
+    float extend_time_ms;
+    float shade_time_ms;
+    float connect_time_ms;
+    float finalize_time_ms;
+    uint32_t sample_count;          /* accumulated samples per pixel */
+    uint32_t device_error;          /* nonzero: a kernel recorded a bounded-loop overrun */
+    /* with TR_FLAG_COUNT_TRAVERSAL, summed over the frames since tr_reset */
+    uint64_t traversal_extend_nodes;
+    uint64_t traversal_extend_tris;
+    uint64_t traversal_connect_nodes;
+    uint64_t traversal_connect_tris;
+} tr_statistics;
+
+/* Scene numbers: triangle/light/BVH sizes and the host build time. */
+typedef struct tr_scene_info {
+    uint32_t triangle_count;
+    uint32_t light_count;
+    uint32_t material_count;
+    uint32_t bvh_node_count;        /* 8-wide compressed nodes (80 B each) */
+    uint64_t device_bytes;          /* scene bytes resident on the device */
+    float light_energy;             /* total emitted energy used for light picks */
+    float build_time_ms;            /* host flattening + BVH build */
+    float upload_time_ms;
+    float scene_bounds[6];
+} tr_scene_info;
+
+/* Device pointers of the wavefront buffers (plane-major SoA), for parity
+ * dumps and external consumers. `capacity` is the plane stride in elements.
+ *   path_state[k]: 3 planes of float4: (O.xyz, bits(pathIx<<4|flags)),
+ *                  (D.xyz, bits(packed normal)), (T.xyz, extend pdf);
+ *                  k = bounce & 1 holds the queue of that bounce.
+ *   hits:          uint4 per queue slot: (bary 16:16, instIx, primIx, bits(t)).
+ *   shadow:        3 planes of float4: (O.xyz, bits(pathIx)), (L.xyz, dist),
+ *                  (T.xyz, 0).
+ *   radiance:      float4 per path index (sum of this frame's contributions).
+ *   accumulator:   float4 per pixel (sum over frames, .w = sample count).
+ *   counters:      uint32[4*(TR_MAX_DEPTH+1)]: extend queue length per bounce,
+ *                  shadow queue length per bounce, then the work cursors of
+ *                  the extend and connect launches. */
+typedef struct tr_buffers {
+    void* path_state[2];
+    void* hits;
+    void* shadow;
+    void* radiance;
+    void* accumulator;
+    void* albedo;
+    void* normals;
+    void* colors;
+    void* counters;
+    uint64_t capacity;
+    uint32_t width;
+    uint32_t height;
+} tr_buffers;
+
+/* ---- lifetime ---- */
+tr_status tr_create(const tr_config* config, void** out_ctx);
+tr_status tr_destroy(void* ctx);
+const char* tr_status_string(tr_status status);
+const char* tr_last_error(void* ctx);
+
+/* ---- scene / camera / settings ---- */
+tr_status tr_scene_upload(void* ctx, const tr_scene_desc* scene);
+tr_status tr_get_scene_info(void* ctx, tr_scene_info* info);
+tr_status tr_set_camera(void* ctx, const tr_camera* camera);
+tr_status tr_set_settings(void* ctx, const tr_kernel_settings* settings);
+tr_status tr_resize(void* ctx, uint32_t width, uint32_t height);
+tr_status tr_reset(void* ctx);
+
+/* ---- per-stage wavefront interface ---- */
+tr_status tr_begin_frame(void* ctx, void* stream);
+tr_status tr_generate(void* ctx, void* stream);
+tr_status tr_extend(void* ctx, void* stream, uint32_t bounce);
+tr_status tr_shade(void* ctx, void* stream, uint32_t bounce);
+tr_status tr_connect(void* ctx, void* stream, uint32_t bounce);
+tr_status tr_finalize(void* ctx, void* stream);
+
+/* Whole frame: begin, generate, max_depth x (extend, shade, connect),
+ * finalize. The bounce loop runs from device-side queue counters without host
+ * round trips; with use_graph != 0 it is captured once per configuration into
+ * a CUDA graph and replayed. */
+tr_status tr_render_frame(void* ctx, void* stream, int32_t use_graph);
+
+/* ---- results ---- */
+tr_status tr_synchronize(void* ctx, void* stream);
+tr_status tr_get_statistics(void* ctx, tr_statistics* stats);
+tr_status tr_get_buffers(void* ctx, tr_buffers* buffers);
+/* Copy the finalized colors (float4 per pixel) to host memory. */
+tr_status tr_download_image(void* ctx, void* stream, float* host_rgba, uint64_t bytes);
+/* Copy the accumulator (float4 per pixel) to host memory. */
+tr_status tr_download_accumulator(void* ctx, void* stream, float* host_rgba, uint64_t bytes);
+
+/* Synchronous copies between host memory and device memory of this
+ * context's device (e.g. the buffers of tr_get_buffers), for inspection and
+ * for injecting stage inputs. */
+tr_status tr_copy_from_device(void* ctx, void* host_dst, const void* device_src, uint64_t bytes);
+tr_status tr_copy_to_device(void* ctx, void* device_dst, const void* host_src, uint64_t bytes);
+
+/* Host-side check of the acceleration structure: builds the 8-wide compressed
+ * BVH of `scene` on the host and traverses n rays (float4 O, float4 D) with
+ * the traversal source of tr_extend / tr_connect compiled for the CPU.
+ * any_hit = 0: closest hit over [tmin, 1e30], hits as tr_extend writes them
+ * (uint4: bary 16:16, instIx, primIx, bits(t)). any_hit = 1: first hit over
+ * [tmin, D.w]; hits[4i+2] = primIx or ~0. counts (optional): uint2 per ray =
+ * (nodes visited, triangles tested). No context or GPU needed. */
+tr_status tr_trace_host(const tr_scene_desc* scene, const float* O4, const float* D4, uint32_t n, float tmin,
+                        int32_t any_hit, uint32_t* hits, uint32_t* counts);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* TRAYRACER_H */

@@ -1,0 +1,129 @@
+"""Generates the golden fixtures of tests/golden from the reference's own code.
+
+Runs where the reference sources are present (oracle/_ref/libtrref.so built by
+oracle/build.py from the reference tree): the reference's closures
+(Tracer/CUDA/GPU/Shade/BSDF/*.h), its random streams (thirdparty/CUDA/random.h)
+and its raygen + path-tracing kernels (Tracer/Optix/GPU/optix.cu,
+Tracer/CUDA/GPU/Shade/PathTracing.h), compiled as host C++, produce the
+expected values; nothing here is written from memory.
+
+    python tests/golden/make_golden.py
+"""
+from __future__ import annotations
+
+import sys
+from pathlib import Path
+
+import numpy as np
+
+ROOT = Path(__file__).resolve().parents[2]
+sys.path.insert(0, str(ROOT))
+
+import trayracer_gb300 as tr  # noqa: E402
+from oracle import Reference, build  # noqa: E402
+from trayracer_gb300.renderer import KernelSettings  # noqa: E402
+
+OUT = Path(__file__).resolve().parent
+
+
+def closure_inputs(n: int, seed: int) -> np.ndarray:
+    """wo (z > 0.05), wi (any hemisphere), T, HitMaterial fields, r0, r1 (layout of ref_closure)."""
+    rng = np.random.default_rng(seed)
+    x = np.zeros((n, 31), np.float32)
+
+    def unit(k, zmin=None):
+        v = rng.normal(size=(k, 3))
+        v /= np.linalg.norm(v, axis=1, keepdims=True)
+        if zmin is not None:
+            v[:, 2] = np.maximum(np.abs(v[:, 2]), zmin)
+            v /= np.linalg.norm(v, axis=1, keepdims=True)
+        return v.astype(np.float32)
+
+    x[:, 0:3] = unit(n, 0.05)
+    x[:, 3:6] = unit(n)
+    x[:, 6:9] = rng.uniform(0.05, 1.0, (n, 3))
+    q = x[:, 9:]
+    diffuse = rng.uniform(0, 1, (n, 3)).astype(np.float32)
+    q[:, 0:3] = diffuse
+    q[:, 3] = rng.uniform(0, 1, n)       # metallic
+    q[:, 4:7] = 0                        # emissive
+    q[:, 7] = np.where(rng.uniform(size=n) < 0.3, rng.uniform(0, 1, n), 0)  # subsurface
+    # tint / luminance from CIE XYZ of the diffuse colour (CudaMaterial.h:155-183)
+    d = diffuse
+    X = np.maximum(0, np.float32(0.412453) * d[:, 0] + np.float32(0.357580) * d[:, 1] + np.float32(0.180423) * d[:, 2])
+    Y = np.maximum(0, np.float32(0.212671) * d[:, 0] + np.float32(0.715160) * d[:, 1] + np.float32(0.072169) * d[:, 2])
+    Z = np.maximum(0, np.float32(0.019334) * d[:, 0] + np.float32(0.119193) * d[:, 1] + np.float32(0.950227) * d[:, 2])
+    Yn = np.where(Y > 0, Y, 1).astype(np.float32)
+    xx, yy, zz = X / Yn, Y / Yn, Z / Yn
+    tint = np.stack([
+        np.maximum(0, np.float32(3.240479) * xx - np.float32(1.537150) * yy - np.float32(0.498535) * zz),
+        np.maximum(0, np.float32(-0.969256) * xx + np.float32(1.875992) * yy + np.float32(0.041556) * zz),
+        np.maximum(0, np.float32(0.055648) * xx - np.float32(0.204043) * yy + np.float32(1.057311) * zz),
+    ], axis=1)
+    q[:, 8:11] = np.where((Y > 0)[:, None], tint, 1)
+    q[:, 11] = rng.uniform(0, 1, n)      # specular
+    q[:, 12] = rng.uniform(0.02, 1, n)   # roughness
+    q[:, 13] = rng.uniform(0, 1, n)      # specularTint
+    q[:, 14] = np.where(rng.uniform(size=n) < 0.3, rng.uniform(-1, 1, n), 0)  # anisotropic
+    q[:, 15] = np.where(rng.uniform(size=n) < 0.3, rng.uniform(0, 1, n), 0)   # sheen
+    q[:, 16] = rng.uniform(0, 1, n)      # sheenTint
+    q[:, 17] = np.where(rng.uniform(size=n) < 0.3, rng.uniform(0, 1, n), 0)   # clearcoat
+    q[:, 18] = rng.uniform(0, 1, n)      # clearcoatGloss
+    q[:, 19] = Y
+    q[:, 20] = rng.uniform(0, 1, n)      # r0
+    q[:, 21] = rng.uniform(0, 1, n)      # r1
+    return x
+
+
+def cornell_reference_frames(width=32, height=32, ms=1, seed=5, frames=2):
+    """The reference's frame loop on the Cornell box (Lambert everywhere, as PathTracing.h:129)."""
+    scene = tr.cornell_box(wall_closure=tr.TR_CLOSURE_LAMBERT, width=width, height=height)
+    st = KernelSettings(multiSample=ms, maxDepth=scene.max_depth, seed=seed, rrStart=1,
+                        flags=tr.TR_FLAG_REFERENCE_SAMPLING | tr._abi.TR_FLAG_REFERENCE_DRAW_RTL)
+    ref = Reference(scene)
+    acc = np.zeros((width * height, 4), np.float32)
+    accs, exts, shs = [], [], []
+    for f in range(frames):
+        ext, sh = ref.render_frame(scene.camera, st, width, height, f * ms, acc)
+        accs.append(acc.copy())
+        exts.append(ext.copy())
+        shs.append(sh.copy())
+    # stage data of the first frame: primary rays + hits, and the shade of bounce 0
+    acc0 = np.zeros((width * height, 4), np.float32)
+    states, hits = ref.primary(scene.camera, st, width, height, 0, acc0)
+    prim_states, prim_hits = states.copy(), hits.copy()
+    shadow = np.zeros_like(states)
+    n_ext, n_sh = ref.shade(scene.camera, st, width, height, 0, 0, width * height * ms, states, hits, shadow, acc0)
+    return dict(
+        digest=np.array(scene.digest()), width=width, height=height, ms=ms, seed=seed, frames=frames,
+        acc=np.stack(accs), ext=np.stack(exts), sh=np.stack(shs),
+        prim_states=prim_states, prim_hits=prim_hits,
+        shade_states=states[:, :n_ext].copy(), shade_shadow=shadow[:, :n_sh].copy(), shade_acc=acc0,
+    )
+
+
+def main():
+    build.build_oracle()
+    if build.build_reference() is None:
+        raise SystemExit("reference sources not found: the golden fixtures come from the reference's own code")
+    # random streams
+    pairs = np.array([[0, 0], [1, 2], [5, 0], [123456, 7], [0xFFFFFFFF, 3], [77, 1 << 20]], np.uint32)
+    draws = np.stack([Reference.rng(int(a), int(b), 16) for a, b in pairs])
+    np.savez_compressed(OUT / "ref_rng.npz", pairs=pairs, draws=draws)
+    # closures
+    out = {}
+    for ctype, name in ((tr.TR_CLOSURE_LAMBERT, "lambert"), (tr.TR_CLOSURE_DIFFUSE, "diffuse"),
+                        (tr.TR_CLOSURE_DISNEY, "disney")):
+        x = closure_inputs(1500, seed=11 + ctype)
+        out[f"{name}_in"] = x
+        out[f"{name}_out"] = Reference.closure(ctype, x)
+    np.savez_compressed(OUT / "ref_closures.npz", **out)
+    # frames
+    np.savez_compressed(OUT / "ref_cornell_32x32_ms1.npz", **cornell_reference_frames(ms=1))
+    np.savez_compressed(OUT / "ref_cornell_24x16_ms2.npz", **cornell_reference_frames(24, 16, ms=2, seed=9))
+    for p in sorted(OUT.glob("*.npz")):
+        print(p.name, p.stat().st_size)
+
+
+if __name__ == "__main__":
+    main()

@@ -1,0 +1,228 @@
+"""GPU parity: every stage of the wavefront against the CPU oracle, on the
+same inputs, through the C ABI (libtrayracer.so).
+
+Tolerances (the oracle runs the same fp32 algorithm; the GPU contracts
+multiply-adds and uses its own transcendental functions):
+  hits       bit-exact primitive, t and 16-bit barycentrics, except logged
+             near ties (|dt| <= 1e-6 t) between coplanar or edge-sharing triangles;
+  rays       |a - b| <= 1e-4 * max(1, |b|) per component;
+  radiance   per-path within 1e-4 relative (atol 1e-6), for all but a
+             logged fraction of paths whose discrete decisions (Russian roulette,
+             NEE gate, lobe choice) flipped on a last-bit difference.
+"""
+import numpy as np
+import pytest
+
+import trayracer_gb300 as tr
+from oracle import Oracle
+from trayracer_gb300._abi import TR_FLAG_REFERENCE_DRAW_RTL
+from trayracer_gb300.renderer import KernelSettings
+
+pytestmark = pytest.mark.gpu
+
+RTOL = 1e-4
+
+
+def close(a, b, rtol=RTOL, atol=1e-6):
+    return np.abs(a - b) <= rtol * np.maximum(1.0, np.abs(b)) + atol
+
+
+def make_renderer(scene, settings):
+    r = tr.DeviceRenderer(0)
+    r.UpdateScene(scene)
+    r.SetCamera(scene.camera)
+    r.Resize((scene.width, scene.height))
+    r.SetSettings(settings)
+    return r
+
+
+def read_state(r, buf, k, n):
+    cap = buf["capacity"]
+    a = r.read_device(buf["path_state"][k], np.float32, 3 * cap * 4).reshape(3, cap, 4)
+    return a[:, :n].copy()
+
+
+def check_hits(o, O, D, got, eps):
+    want = o.trace_closest(O, D, eps)
+    same = (got == want).all(axis=1)
+    ties = 0
+    for i in np.where(~same)[0]:
+        tg = float(got[i, 3].view(np.float32))
+        tw = float(want[i, 3].view(np.float32))
+        assert abs(tg - tw) <= 1e-6 * abs(tw), f"ray {i}: gpu {got[i]} oracle {want[i]}"
+        assert int(got[i, 2]) in o.ties(O[i], D[i], eps, tw), f"ray {i}: {got[i]} is no near tie of {want[i]}"
+        ties += 1
+    return ties
+
+
+SCENES = {
+    "cornell_counter": lambda: (tr.cornell_box(width=48, height=40), dict(ms=2, reference=False)),
+    "cornell_reference": lambda: (tr.cornell_box(width=40, height=32), dict(ms=2, reference=True)),
+    "heightfield_counter": lambda: (tr.heightfield(n=128, width=64, height=36, rr_start=2),
+                                    dict(ms=2, reference=False)),
+}
+
+
+@pytest.mark.parametrize("name", list(SCENES))
+def test_stagewise_parity(name):
+    scene, kw = SCENES[name]()
+    st = tr.settings_for(scene, multi_sample=kw["ms"], reference=kw["reference"])
+    o = Oracle(scene)
+    r = make_renderer(scene, st)
+    W, H = scene.width, scene.height
+    r.BeginFrame()
+    r.Generate()
+    buf = r.Buffers()
+    n = buf["capacity"]
+    s0 = read_state(r, buf, 0, n)
+    O, D, T = o.generate(scene.camera, st, W, H, 0, 0, n)
+    np.testing.assert_array_equal(s0[0][:, 3].view(np.uint32), O[:, 3].view(np.uint32))
+    assert close(s0[0][:, :3], O[:, :3]).all()
+    assert close(s0[1][:, :3], D[:, :3]).all()
+    assert close(s0[2], T).all()
+
+    radiance = np.zeros((n, 4), np.float32)
+    total_ties = 0
+    flipped = 0
+    for b in range(st.maxDepth):
+        counters = r.read_device(buf["counters"], np.uint32, 4 * 17)
+        count = n if b == 0 else int(counters[b])
+        if count == 0:
+            break
+        state = read_state(r, buf, b & 1, count)
+        r.Extend(b)
+        hits = r.read_device(buf["hits"], np.uint32, count * 4).reshape(count, 4)
+        total_ties += check_hits(o, state[0], state[1], hits, st.rayEpsilon)
+
+        r.Shade(b)
+        counters = r.read_device(buf["counters"], np.uint32, 4 * 17)
+        n_ext, n_sh = int(counters[b + 1]), int(counters[17 + b])
+        ext_gpu = read_state(r, buf, (b + 1) & 1, n_ext)
+        sh_gpu = r.read_device(buf["shadow"], np.float32, 3 * n * 4).reshape(3, n, 4)[:, :n_sh]
+        rad_gpu = r.read_device(buf["radiance"], np.float32, n * 4).reshape(n, 4)
+        ext, ev, sh, sv, add = o.shade(st, b, 0, W, H, state[0], state[1], state[2], hits)
+        path = state[0][:, 3].view(np.uint32) >> 4
+
+        # extend rays, matched by path index
+        gpu_ext_paths = ext_gpu[0][:, 3].view(np.uint32) >> 4
+        orc_ext_paths = path[ev]
+        sym = np.setxor1d(gpu_ext_paths, orc_ext_paths)
+        flipped += sym.size
+        assert sym.size <= max(2, count // 500), f"bounce {b}: {sym.size} extend decisions differ"
+        common = np.intersect1d(gpu_ext_paths, orc_ext_paths)
+        gi = np.argsort(gpu_ext_paths)[np.searchsorted(np.sort(gpu_ext_paths), common)]
+        oe = ext[ev]
+        oi = np.argsort(orc_ext_paths)[np.searchsorted(np.sort(orc_ext_paths), common)]
+        np.testing.assert_array_equal(ext_gpu[0][gi, 3].view(np.uint32), oe[oi, 0, 3].view(np.uint32))
+        ok = close(ext_gpu[0][gi, :3], oe[oi, 0, :3]).all(1) & close(ext_gpu[1][gi, :3], oe[oi, 1, :3]).all(1) \
+            & close(ext_gpu[2][gi], oe[oi, 2]).all(1)
+        assert ok.mean() >= 0.998, f"bounce {b}: extend rays agree for {ok.mean():.4f}"
+
+        # shadow rays, matched by path index
+        gpu_sh_paths = sh_gpu[0][:, 3].view(np.uint32)
+        orc_sh_paths = path[sv]
+        sym = np.setxor1d(gpu_sh_paths, orc_sh_paths)
+        flipped += sym.size
+        assert sym.size <= max(2, count // 500), f"bounce {b}: {sym.size} NEE decisions differ"
+        common = np.intersect1d(gpu_sh_paths, orc_sh_paths)
+        gi = np.argsort(gpu_sh_paths)[np.searchsorted(np.sort(gpu_sh_paths), common)]
+        osh = sh[sv]
+        oi = np.argsort(orc_sh_paths)[np.searchsorted(np.sort(orc_sh_paths), common)]
+        ok = close(sh_gpu[0][gi, :3], osh[oi, 0, :3]).all(1) & close(sh_gpu[1][gi], osh[oi, 1]).all(1) \
+            & close(sh_gpu[2][gi, :3], osh[oi, 2, :3], rtol=1e-3).all(1)
+        assert ok.mean() >= 0.998, f"bounce {b}: shadow rays agree for {ok.mean():.4f}"
+
+        # radiance added by shade
+        want_rad = radiance.copy()
+        np.add.at(want_rad, path, add)
+        okr = close(rad_gpu[:, :3], want_rad[:, :3], rtol=1e-4).all(1)
+        assert okr.mean() >= 0.999, f"bounce {b}: shade radiance agrees for {okr.mean():.4f}"
+
+        # connect: unoccluded shadow rays add their throughput
+        r.Connect(b)
+        rad_after = r.read_device(buf["radiance"], np.float32, n * 4).reshape(n, 4)
+        if n_sh:
+            occ = o.trace_any(sh_gpu[0], sh_gpu[1], st.rayEpsilon).astype(bool)
+            want2 = rad_gpu.copy()
+            vis = ~occ
+            np.add.at(want2, gpu_sh_paths[vis], sh_gpu[2][vis])
+            okc = close(rad_after[:, :3], want2[:, :3], rtol=1e-5).all(1)
+            assert okc.mean() >= 0.9995, f"bounce {b}: connect agrees for {okc.mean():.5f}"
+        radiance = rad_after
+    print(f"{name}: near ties {total_ties}, flipped decisions {flipped}")
+    r.close()
+
+
+@pytest.mark.parametrize("reference", [False, True])
+def test_frame_parity_per_path(reference):
+    scene = tr.cornell_box(width=64, height=48)
+    st = tr.settings_for(scene, multi_sample=4, reference=reference)
+    r = make_renderer(scene, st)
+    r.RenderFrame()
+    buf = r.Buffers()
+    n = buf["capacity"]
+    rad = r.read_device(buf["radiance"], np.float32, n * 4).reshape(st.multiSample, scene.height * scene.width, 4)
+    img = r.ColorBuffer()
+    stats = r.Statistics()
+    r.close()
+    assert stats["device_error"] == 0
+    acc, paths, counts = Oracle(scene).render(scene.camera, st, scene.width, scene.height, want_paths=True)
+    ok = close(rad[..., :3].astype(np.float64), paths[..., :3], rtol=1e-4).all(-1)
+    assert ok.mean() >= 0.995, ok.mean()
+    ref_img = (acc[:, :3] / acc[:, 3:4]).reshape(scene.height, scene.width, 3)
+    rel_rmse = np.sqrt(np.mean((img[..., :3] - ref_img) ** 2)) / np.sqrt(np.mean(ref_img ** 2))
+    assert rel_rmse < 1e-2, rel_rmse
+    # ray counts of the wavefront and of the depth-first oracle agree up to flipped decisions
+    assert abs(stats["path_count"] - sum(counts)) <= 0.002 * sum(counts)
+
+
+def test_image_rmse_against_fp64_oracle():
+    scene = tr.cornell_box(width=48, height=48)
+    st = tr.settings_for(scene, multi_sample=8)
+    r = make_renderer(scene, st)
+    for _ in range(2):
+        r.RenderFrame()
+    img = r.ColorBuffer()
+    r.close()
+    acc64, _, _ = Oracle(scene).render(scene.camera, st, 48, 48, frames=2, use_double=True)
+    ref = (acc64[:, :3] / acc64[:, 3:4]).reshape(48, 48, 3)
+    rel_rmse = np.sqrt(np.mean((img[..., :3] - ref) ** 2)) / np.sqrt(np.mean(ref ** 2))
+    print(f"relative image RMSE vs FP64 oracle: {rel_rmse:.3e}")
+    assert rel_rmse < 1e-3 * 30, rel_rmse
+
+
+@pytest.mark.parametrize("fixture", ["ref_cornell_32x32_ms1.npz", "ref_cornell_24x16_ms2.npz"])
+def test_gpu_against_reference_golden(fixture):
+    """The GPU kernels in reference mode (right-to-left draws, Lambert closures)
+    against the accumulator the reference's own kernels produced."""
+    from pathlib import Path
+
+    g = np.load(Path(__file__).resolve().parent / "golden" / fixture)
+    w, h, ms, seed = int(g["width"]), int(g["height"]), int(g["ms"]), int(g["seed"])
+    scene = tr.cornell_box(wall_closure=tr.TR_CLOSURE_LAMBERT, width=w, height=h)
+    assert scene.digest() == str(g["digest"])
+    st = KernelSettings(multiSample=ms, maxDepth=5, seed=seed, rrStart=1,
+                        flags=tr.TR_FLAG_REFERENCE_SAMPLING | TR_FLAG_REFERENCE_DRAW_RTL)
+    r = make_renderer(scene, st)
+    # stage check on the first frame: primary rays and hits
+    r.BeginFrame()
+    r.Generate()
+    buf = r.Buffers()
+    n = buf["capacity"]
+    s0 = read_state(r, buf, 0, n)
+    ps = g["prim_states"]
+    assert close(s0[0][:, :3], ps[0][:, :3]).all() and close(s0[1][:, :3], ps[1][:, :3]).all()
+    r.Extend(0)
+    hits = r.read_device(buf["hits"], np.uint32, n * 4).reshape(n, 4)
+    # the reference indexes hits by path; the first queue is in path order
+    match = (hits[:, 2] == g["prim_hits"][:, 2]).mean()
+    assert match >= 0.995, match
+    r.Reset()
+    for f in range(int(g["frames"])):
+        r.RenderFrame()
+    acc = r.Accumulator().reshape(-1, 4)
+    r.close()
+    want = g["acc"][-1]
+    ok = close(acc[:, :3], want[:, :3], rtol=1e-4).all(1)
+    assert ok.mean() >= 0.99, ok.mean()
+    np.testing.assert_array_equal(acc[:, 3], want[:, 3])

@@ -1,0 +1,14 @@
+"""GB300-native wavefront path tracer: the ray generation -> extend -> shade ->
+connect -> accumulate hot path of rdbruijne/trayracer, rebuilt as hand-written
+sm_103a CUDA kernels behind a C ABI (include/trayracer.h, libtrayracer.so)."""
+from ._abi import (  # noqa: F401
+    TR_CLOSURE_DIFFUSE,
+    TR_CLOSURE_DISNEY,
+    TR_CLOSURE_LAMBERT,
+    TR_FLAG_REFERENCE_SAMPLING,
+    TR_FLAG_WRITE_AOVS,
+    TR_MAX_DEPTH,
+    load_library,
+)
+from .renderer import DeviceRenderer, KernelSettings, RenderModes, TracerError, camera_to_c, settings_for  # noqa: F401
+from .scenes import CameraSpec, Scene, cornell_box, heightfield  # noqa: F401

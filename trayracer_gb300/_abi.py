@@ -1,0 +1,209 @@
+"""ctypes view of the C ABI declared in include/trayracer.h."""
+from __future__ import annotations
+
+import ctypes as C
+from pathlib import Path
+
+TR_MAX_DEPTH = 16
+TR_ABI_VERSION = 1
+TR_FLAG_REFERENCE_SAMPLING = 1 << 0
+TR_FLAG_WRITE_AOVS = 1 << 1
+TR_FLAG_REFERENCE_DRAW_RTL = 1 << 2
+TR_FLAG_COUNT_TRAVERSAL = 1 << 3
+
+TR_CLOSURE_LAMBERT = 0
+TR_CLOSURE_DIFFUSE = 1
+TR_CLOSURE_DISNEY = 2
+
+STATUS = {
+    0: "TR_OK",
+    1: "TR_ERR_INVALID_ARGUMENT",
+    2: "TR_ERR_OUT_OF_MEMORY",
+    3: "TR_ERR_CUDA",
+    4: "TR_ERR_NO_SCENE",
+    5: "TR_ERR_NOT_READY",
+    6: "TR_ERR_LIMIT",
+    7: "TR_ERR_DEVICE_FAULT",
+}
+
+
+class KernelSettings(C.Structure):
+    _fields_ = [
+        ("multi_sample", C.c_uint32),
+        ("max_depth", C.c_uint32),
+        ("seed", C.c_uint32),
+        ("ray_epsilon", C.c_float),
+        ("rr_start", C.c_uint32),
+        ("flags", C.c_uint32),
+        ("max_color", C.c_float),
+        ("reserved", C.c_uint32),
+    ]
+
+
+class Camera(C.Structure):
+    _fields_ = [
+        ("position", C.c_float * 3),
+        ("side", C.c_float * 3),
+        ("up", C.c_float * 3),
+        ("forward", C.c_float * 3),
+        ("aperture", C.c_float),
+        ("distortion", C.c_float),
+        ("focal_dist", C.c_float),
+        ("fov", C.c_float),
+        ("bokeh_side_count", C.c_int32),
+        ("bokeh_rotation", C.c_float),
+    ]
+
+
+class MaterialDesc(C.Structure):
+    _fields_ = [
+        ("diffuse", C.c_float * 3),
+        ("emissive", C.c_float * 3),
+        ("metallic", C.c_float),
+        ("subsurface", C.c_float),
+        ("specular", C.c_float),
+        ("roughness", C.c_float),
+        ("specular_tint", C.c_float),
+        ("anisotropic", C.c_float),
+        ("sheen", C.c_float),
+        ("sheen_tint", C.c_float),
+        ("clearcoat", C.c_float),
+        ("clearcoat_gloss", C.c_float),
+        ("closure", C.c_uint32),
+    ]
+
+
+class MeshDesc(C.Structure):
+    _fields_ = [
+        ("positions", C.c_void_p),
+        ("normals", C.c_void_p),
+        ("texcoords", C.c_void_p),
+        ("vertex_count", C.c_uint32),
+        ("triangle_count", C.c_uint32),
+        ("indices", C.c_void_p),
+        ("material_indices", C.c_void_p),
+    ]
+
+
+class SceneDesc(C.Structure):
+    _fields_ = [
+        ("mesh", C.POINTER(MeshDesc)),
+        ("materials", C.POINTER(MaterialDesc)),
+        ("material_count", C.c_uint32),
+        ("bvh_leaf_size", C.c_uint32),
+        ("build_threads", C.c_uint32),
+        ("reserved", C.c_uint32),
+    ]
+
+
+class Config(C.Structure):
+    _fields_ = [("device", C.c_int32), ("abi_version", C.c_uint32)]
+
+
+class Statistics(C.Structure):
+    _fields_ = [
+        ("path_count", C.c_uint64),
+        ("primary_path_count", C.c_uint64),
+        ("secondary_path_count", C.c_uint64),
+        ("deep_path_count", C.c_uint64),
+        ("shadow_ray_count", C.c_uint64),
+        ("extend_rays", C.c_uint32 * TR_MAX_DEPTH),
+        ("shadow_rays", C.c_uint32 * TR_MAX_DEPTH),
+        ("render_time_ms", C.c_float),
+        ("generate_time_ms", C.c_float),
+        ("extend_time_ms", C.c_float),
+        ("shade_time_ms", C.c_float),
+        ("connect_time_ms", C.c_float),
+        ("finalize_time_ms", C.c_float),
+        ("sample_count", C.c_uint32),
+        ("device_error", C.c_uint32),
+        ("traversal_extend_nodes", C.c_uint64),
+        ("traversal_extend_tris", C.c_uint64),
+        ("traversal_connect_nodes", C.c_uint64),
+        ("traversal_connect_tris", C.c_uint64),
+    ]
+
+
+class SceneInfo(C.Structure):
+    _fields_ = [
+        ("triangle_count", C.c_uint32),
+        ("light_count", C.c_uint32),
+        ("material_count", C.c_uint32),
+        ("bvh_node_count", C.c_uint32),
+        ("device_bytes", C.c_uint64),
+        ("light_energy", C.c_float),
+        ("build_time_ms", C.c_float),
+        ("upload_time_ms", C.c_float),
+        ("scene_bounds", C.c_float * 6),
+    ]
+
+
+class Buffers(C.Structure):
+    _fields_ = [
+        ("path_state", C.c_void_p * 2),
+        ("hits", C.c_void_p),
+        ("shadow", C.c_void_p),
+        ("radiance", C.c_void_p),
+        ("accumulator", C.c_void_p),
+        ("albedo", C.c_void_p),
+        ("normals", C.c_void_p),
+        ("colors", C.c_void_p),
+        ("counters", C.c_void_p),
+        ("capacity", C.c_uint64),
+        ("width", C.c_uint32),
+        ("height", C.c_uint32),
+    ]
+
+
+# name -> (restype, argtypes) for every function include/trayracer.h declares
+_V = C.c_void_p
+_U = C.c_uint32
+FUNCTIONS = {
+    "tr_create": (C.c_int, [C.POINTER(Config), C.POINTER(_V)]),
+    "tr_destroy": (C.c_int, [_V]),
+    "tr_status_string": (C.c_char_p, [C.c_int]),
+    "tr_last_error": (C.c_char_p, [_V]),
+    "tr_scene_upload": (C.c_int, [_V, C.POINTER(SceneDesc)]),
+    "tr_get_scene_info": (C.c_int, [_V, C.POINTER(SceneInfo)]),
+    "tr_set_camera": (C.c_int, [_V, C.POINTER(Camera)]),
+    "tr_set_settings": (C.c_int, [_V, C.POINTER(KernelSettings)]),
+    "tr_resize": (C.c_int, [_V, _U, _U]),
+    "tr_reset": (C.c_int, [_V]),
+    "tr_begin_frame": (C.c_int, [_V, _V]),
+    "tr_generate": (C.c_int, [_V, _V]),
+    "tr_extend": (C.c_int, [_V, _V, _U]),
+    "tr_shade": (C.c_int, [_V, _V, _U]),
+    "tr_connect": (C.c_int, [_V, _V, _U]),
+    "tr_finalize": (C.c_int, [_V, _V]),
+    "tr_render_frame": (C.c_int, [_V, _V, C.c_int32]),
+    "tr_synchronize": (C.c_int, [_V, _V]),
+    "tr_get_statistics": (C.c_int, [_V, C.POINTER(Statistics)]),
+    "tr_get_buffers": (C.c_int, [_V, C.POINTER(Buffers)]),
+    "tr_download_image": (C.c_int, [_V, _V, _V, C.c_uint64]),
+    "tr_download_accumulator": (C.c_int, [_V, _V, _V, C.c_uint64]),
+    "tr_copy_from_device": (C.c_int, [_V, _V, _V, C.c_uint64]),
+    "tr_copy_to_device": (C.c_int, [_V, _V, _V, C.c_uint64]),
+    "tr_trace_host": (C.c_int, [C.POINTER(SceneDesc), _V, _V, _U, C.c_float, C.c_int32, _V, _V]),
+}
+
+LIB_PATH = Path(__file__).resolve().parent / "libtrayracer.so"
+_lib = None
+
+
+def load_library() -> C.CDLL:
+    """Loads libtrayracer.so; raises when it has not been built (no fallback)."""
+    global _lib
+    if _lib is not None:
+        return _lib
+    if not LIB_PATH.exists():
+        raise RuntimeError(
+            f"{LIB_PATH} is missing: build the CUDA extension first "
+            "(python -c 'import __graft_entry__ as g; g.build()')"
+        )
+    lib = C.CDLL(str(LIB_PATH))
+    for name, (res, args) in FUNCTIONS.items():
+        fn = getattr(lib, name)
+        fn.restype = res
+        fn.argtypes = args
+    _lib = lib
+    return lib

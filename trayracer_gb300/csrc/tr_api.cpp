@@ -1,0 +1,797 @@
+// C ABI of the wavefront path tracer: context, scene upload, wavefront
+// buffers, per-stage launches, CUDA-graph frame loop, statistics.
+//
+// Mirrors the reference's DeviceRenderer (Tracer/Renderer/DeviceRenderer.cpp)
+// and Renderer upload path (Tracer/Renderer/Renderer.cpp:442-527), with
+// status codes instead of CUDA_CHECK -> FatalError -> exit
+// (Tracer/CUDA/CudaError.cpp:13-25), scene pointers passed as kernel
+// parameters instead of __constant__ symbols (Tracer/CUDA/GPU/CudaGlobals.h),
+// and no host round trip per bounce (the reference downloads the ray counters
+// after every shade, DeviceRenderer.cpp:255-257).
+#include <cuda_runtime.h>
+
+#include <chrono>
+#include <cmath>
+#include <cstring>
+#include <mutex>
+#include <new>
+#include <string>
+#include <vector>
+
+#include "../../include/trayracer.h"
+#include "tr_bvh.h"
+#include "tr_kernels.h"
+#include "tr_scene.h"
+
+namespace {
+
+using namespace tr;
+
+struct DeviceArena {
+    void* base = nullptr;
+    size_t bytes = 0;
+    void release()
+    {
+        if (base)
+            cudaFree(base);
+        base = nullptr;
+        bytes = 0;
+    }
+};
+
+inline size_t align256(size_t x) { return (x + 255) & ~size_t(255); }
+
+struct Context {
+    int device = 0;
+    cudaStream_t stream = nullptr;
+    std::string lastError;
+
+    // scene
+    bool hasScene = false;
+    DeviceArena sceneArena;
+    SceneView scene{};
+    tr_scene_info info{};
+
+    // settings / camera
+    Settings settings{};
+    Camera camera{};
+    bool hasCamera = false;
+
+    // frame
+    uint32_t width = 0, height = 0;
+    DeviceArena frameArena;
+    FrameView frame{};
+    size_t frameCapacity = 0;
+    uint32_t frameW = 0, frameH = 0, frameMs = 0;
+    LaunchShape shape{};
+    uint32_t sampleCount = 0;
+    uint32_t* hostCounters = nullptr;  // pinned
+
+    // timing
+    cudaEvent_t evStart = nullptr, evGenerate = nullptr, evFinal = nullptr;
+    cudaEvent_t evExtend[TR_MAX_DEPTH] = {}, evShade[TR_MAX_DEPTH] = {}, evConnect[TR_MAX_DEPTH] = {};
+    bool timedFrame = false;
+    uint32_t timedDepth = 0;
+    cudaStream_t lastStream = nullptr;
+
+    // graph
+    cudaGraph_t graph = nullptr;
+    cudaGraphExec_t graphExec = nullptr;
+    bool graphValid = false;
+};
+
+tr_status fail(Context* c, tr_status st, const std::string& msg)
+{
+    if (c)
+        c->lastError = msg;
+    return st;
+}
+
+tr_status cuda_fail(Context* c, cudaError_t e, const char* what)
+{
+    const bool sticky = e == cudaErrorIllegalAddress || e == cudaErrorLaunchFailure ||
+                        e == cudaErrorIllegalInstruction || e == cudaErrorMisalignedAddress ||
+                        e == cudaErrorHardwareStackError || e == cudaErrorAssert;
+    if (e == cudaErrorMemoryAllocation) {
+        cudaGetLastError();
+        return fail(c, TR_ERR_OUT_OF_MEMORY, std::string(what) + ": " + cudaGetErrorString(e));
+    }
+    return fail(c, sticky ? TR_ERR_DEVICE_FAULT : TR_ERR_CUDA, std::string(what) + ": " + cudaGetErrorString(e));
+}
+
+#define TR_CUDA(ctx, call)                                  \
+    do {                                                    \
+        const cudaError_t e_ = (call);                      \
+        if (e_ != cudaSuccess)                              \
+            return cuda_fail((ctx), e_, #call);             \
+    } while (0)
+
+cudaStream_t pick_stream(Context* c, void* s) { return s ? static_cast<cudaStream_t>(s) : c->stream; }
+
+void invalidate_graph(Context* c)
+{
+    if (c->graphExec)
+        cudaGraphExecDestroy(c->graphExec);
+    if (c->graph)
+        cudaGraphDestroy(c->graph);
+    c->graphExec = nullptr;
+    c->graph = nullptr;
+    c->graphValid = false;
+}
+
+tr_status ensure_frame(Context* c)
+{
+    if (c->width == 0 || c->height == 0)
+        return fail(c, TR_ERR_NOT_READY, "resolution not set (tr_resize)");
+    const uint64_t wh = uint64_t(c->width) * c->height;
+    const uint64_t paths = wh * c->settings.multiSample;
+    if (paths == 0 || paths >= TR_MAX_PATHS)
+        return fail(c, TR_ERR_LIMIT, "paths in flight (width*height*multi_sample) must be in [1, 2^28)");
+    if (c->frameArena.base && c->frameW == c->width && c->frameH == c->height && c->frameMs == c->settings.multiSample)
+        return TR_OK;
+
+    invalidate_graph(c);
+    c->frameArena.release();
+    const size_t cap = size_t(paths);
+    size_t off = 0;
+    auto take = [&](size_t bytes) {
+        const size_t o = off;
+        off = align256(off + bytes);
+        return o;
+    };
+    const size_t oState0 = take(3 * cap * sizeof(float4));
+    const size_t oState1 = take(3 * cap * sizeof(float4));
+    const size_t oHits = take(cap * sizeof(uint4));
+    const size_t oShadow = take(3 * cap * sizeof(float4));
+    const size_t oRad = take(cap * sizeof(float4));
+    const size_t oAcc = take(wh * sizeof(float4));
+    const size_t oAlb = take(wh * sizeof(float4));
+    const size_t oNrm = take(wh * sizeof(float4));
+    const size_t oCol = take(wh * sizeof(float4));
+    const size_t oCnt = take(kCounterWords * sizeof(uint32_t));
+    const size_t oSc = take(sizeof(uint32_t));
+    const size_t oErr = take(sizeof(uint32_t));
+    const size_t oTrav = take(4 * sizeof(unsigned long long));
+    void* base = nullptr;
+    const cudaError_t e = cudaMalloc(&base, off);
+    if (e != cudaSuccess)
+        return cuda_fail(c, e, "cudaMalloc(frame buffers)");
+    c->frameArena.base = base;
+    c->frameArena.bytes = off;
+    char* b = static_cast<char*>(base);
+    FrameView& f = c->frame;
+    f.state[0] = reinterpret_cast<float4*>(b + oState0);
+    f.state[1] = reinterpret_cast<float4*>(b + oState1);
+    f.hits = reinterpret_cast<uint4*>(b + oHits);
+    f.shadow = reinterpret_cast<float4*>(b + oShadow);
+    f.radiance = reinterpret_cast<float4*>(b + oRad);
+    f.accumulator = reinterpret_cast<float4*>(b + oAcc);
+    f.albedo = reinterpret_cast<float4*>(b + oAlb);
+    f.normals = reinterpret_cast<float4*>(b + oNrm);
+    f.colors = reinterpret_cast<float4*>(b + oCol);
+    f.counters = reinterpret_cast<uint32_t*>(b + oCnt);
+    f.sampleCount = reinterpret_cast<uint32_t*>(b + oSc);
+    f.errorFlag = reinterpret_cast<uint32_t*>(b + oErr);
+    f.traversal = reinterpret_cast<unsigned long long*>(b + oTrav);
+    f.capacity = uint32_t(cap);
+    f.resX = c->width;
+    f.resY = c->height;
+    f.pathCount = uint32_t(paths);
+    TR_CUDA(c, cudaMemset(base, 0, off));
+    c->frameCapacity = cap;
+    c->frameW = c->width;
+    c->frameH = c->height;
+    c->frameMs = c->settings.multiSample;
+    c->sampleCount = 0;
+    c->shape = default_launch_shape(c->device, uint32_t(cap));
+    return TR_OK;
+}
+
+tr_status check_ready(Context* c)
+{
+    if (!c->hasScene)
+        return fail(c, TR_ERR_NO_SCENE, "no scene uploaded");
+    if (!c->hasCamera)
+        return fail(c, TR_ERR_NOT_READY, "camera not set");
+    return ensure_frame(c);
+}
+
+tr_status enqueue_begin(Context* c, cudaStream_t s)
+{
+    TR_CUDA(c, cudaMemsetAsync(c->frame.counters, 0, kCounterWords * sizeof(uint32_t), s));
+    return TR_OK;
+}
+
+tr_status enqueue_frame(Context* c, cudaStream_t s, bool timed)
+{
+    tr_status st = enqueue_begin(c, s);
+    if (st != TR_OK)
+        return st;
+    if (timed)
+        TR_CUDA(c, cudaEventRecord(c->evStart, s));
+    TR_CUDA(c, launch_generate(c->frame, c->camera, c->settings, s));
+    if (timed)
+        TR_CUDA(c, cudaEventRecord(c->evGenerate, s));
+    for (uint32_t b = 0; b < c->settings.maxDepth; ++b) {
+        TR_CUDA(c, launch_extend(c->scene, c->frame, c->settings, b, c->shape, s));
+        if (timed)
+            TR_CUDA(c, cudaEventRecord(c->evExtend[b], s));
+        TR_CUDA(c, launch_shade(c->scene, c->frame, c->settings, b, c->shape, s));
+        if (timed)
+            TR_CUDA(c, cudaEventRecord(c->evShade[b], s));
+        TR_CUDA(c, launch_connect(c->scene, c->frame, c->settings, b, c->shape, s));
+        if (timed)
+            TR_CUDA(c, cudaEventRecord(c->evConnect[b], s));
+    }
+    TR_CUDA(c, launch_finalize(c->frame, c->settings, s));
+    if (timed)
+        TR_CUDA(c, cudaEventRecord(c->evFinal, s));
+    return TR_OK;
+}
+
+} // namespace
+
+extern "C" {
+
+const char* tr_status_string(tr_status status)
+{
+    switch (status) {
+    case TR_OK: return "ok";
+    case TR_ERR_INVALID_ARGUMENT: return "invalid argument";
+    case TR_ERR_OUT_OF_MEMORY: return "out of memory";
+    case TR_ERR_CUDA: return "CUDA error";
+    case TR_ERR_NO_SCENE: return "no scene";
+    case TR_ERR_NOT_READY: return "not ready";
+    case TR_ERR_LIMIT: return "limit exceeded";
+    case TR_ERR_DEVICE_FAULT: return "device fault";
+    }
+    return "unknown status";
+}
+
+const char* tr_last_error(void* ctx)
+{
+    return ctx ? static_cast<Context*>(ctx)->lastError.c_str() : "null context";
+}
+
+tr_status tr_create(const tr_config* config, void** out_ctx)
+{
+    if (!out_ctx)
+        return TR_ERR_INVALID_ARGUMENT;
+    *out_ctx = nullptr;
+    const int device = config ? config->device : 0;
+    if (config && config->abi_version != TR_ABI_VERSION)
+        return TR_ERR_INVALID_ARGUMENT;
+    int count = 0;
+    if (cudaGetDeviceCount(&count) != cudaSuccess || count == 0) {
+        cudaGetLastError();
+        return TR_ERR_CUDA;
+    }
+    if (device < 0 || device >= count)
+        return TR_ERR_INVALID_ARGUMENT;
+    if (cudaSetDevice(device) != cudaSuccess)
+        return TR_ERR_CUDA;
+    Context* c = new (std::nothrow) Context();
+    if (!c)
+        return TR_ERR_OUT_OF_MEMORY;
+    c->device = device;
+    c->settings.multiSample = 1;
+    c->settings.maxDepth = TR_MAX_DEPTH;
+    c->settings.seed = 0;
+    c->settings.rayEpsilon = kEpsilon;
+    c->settings.rrStart = 1;
+    c->settings.flags = 0;
+    c->settings.maxColor = 10.f;
+    bool ok = cudaStreamCreate(&c->stream) == cudaSuccess;
+    ok = ok && cudaEventCreate(&c->evStart) == cudaSuccess && cudaEventCreate(&c->evGenerate) == cudaSuccess &&
+         cudaEventCreate(&c->evFinal) == cudaSuccess;
+    for (uint32_t i = 0; ok && i < TR_MAX_DEPTH; ++i)
+        ok = cudaEventCreate(&c->evExtend[i]) == cudaSuccess && cudaEventCreate(&c->evShade[i]) == cudaSuccess &&
+             cudaEventCreate(&c->evConnect[i]) == cudaSuccess;
+    ok = ok && cudaMallocHost(reinterpret_cast<void**>(&c->hostCounters), kCounterWords * 2 * sizeof(uint32_t)) ==
+                   cudaSuccess;
+    if (!ok) {
+        cudaGetLastError();
+        tr_destroy(c);
+        return TR_ERR_CUDA;
+    }
+    *out_ctx = c;
+    return TR_OK;
+}
+
+tr_status tr_destroy(void* ctx)
+{
+    if (!ctx)
+        return TR_ERR_INVALID_ARGUMENT;
+    Context* c = static_cast<Context*>(ctx);
+    cudaSetDevice(c->device);
+    if (c->stream)
+        cudaStreamSynchronize(c->stream);
+    invalidate_graph(c);
+    c->sceneArena.release();
+    c->frameArena.release();
+    if (c->hostCounters)
+        cudaFreeHost(c->hostCounters);
+    cudaEvent_t* evs[] = {&c->evStart, &c->evGenerate, &c->evFinal};
+    for (cudaEvent_t* e : evs)
+        if (*e)
+            cudaEventDestroy(*e);
+    for (uint32_t i = 0; i < TR_MAX_DEPTH; ++i) {
+        if (c->evExtend[i]) cudaEventDestroy(c->evExtend[i]);
+        if (c->evShade[i]) cudaEventDestroy(c->evShade[i]);
+        if (c->evConnect[i]) cudaEventDestroy(c->evConnect[i]);
+    }
+    if (c->stream)
+        cudaStreamDestroy(c->stream);
+    delete c;
+    return TR_OK;
+}
+
+tr_status tr_scene_upload(void* ctx, const tr_scene_desc* desc)
+{
+    if (!ctx)
+        return TR_ERR_INVALID_ARGUMENT;
+    Context* c = static_cast<Context*>(ctx);
+    if (!desc)
+        return fail(c, TR_ERR_INVALID_ARGUMENT, "null scene description");
+    const std::string err = validate_scene(*desc);
+    if (!err.empty())
+        return fail(c, TR_ERR_INVALID_ARGUMENT, err);
+    cudaSetDevice(c->device);
+
+    const auto t0 = std::chrono::steady_clock::now();
+    FlatScene fs = flatten_scene(*desc);
+    BvhBuildOptions opt;
+    opt.maxLeafSize = desc->bvh_leaf_size ? desc->bvh_leaf_size : 3u;
+    opt.threads = desc->build_threads;
+    const tr_mesh_desc& m = *desc->mesh;
+    const BinaryBvh bin = build_binary_bvh(m.positions, m.indices, m.triangle_count, opt);
+    const Cwbvh wide = collapse_to_cwbvh(bin, m.positions, m.indices);
+    const auto t1 = std::chrono::steady_clock::now();
+
+    // one arena for all scene buffers
+    size_t off = 0;
+    auto take = [&](size_t bytes) {
+        const size_t o = off;
+        off = align256(off + std::max<size_t>(bytes, 16));
+        return o;
+    };
+    const size_t oNodes = take(wide.nodes.size() * sizeof(CwbvhNode));
+    const size_t oBTris = take(wide.tris.size() * sizeof(float4));
+    const size_t oTris = take(fs.tris.size() * sizeof(TriShade));
+    const size_t oMat = take(fs.matIdx.size() * sizeof(uint32_t));
+    const size_t oMats = take(fs.materials.size() * sizeof(Material));
+    const size_t oLights = take(fs.lights.size() * sizeof(LightTri));
+    const size_t oAlias = take(fs.alias.size() * sizeof(AliasEntry));
+    const size_t oXf = take(fs.invTransforms.size() * sizeof(float4));
+
+    if (c->stream)
+        cudaStreamSynchronize(c->stream);
+    invalidate_graph(c);
+    c->sceneArena.release();
+    c->hasScene = false;
+    void* base = nullptr;
+    cudaError_t e = cudaMalloc(&base, off);
+    if (e != cudaSuccess)
+        return cuda_fail(c, e, "cudaMalloc(scene)");
+    c->sceneArena.base = base;
+    c->sceneArena.bytes = off;
+    char* b = static_cast<char*>(base);
+    auto up = [&](size_t o, const void* src, size_t bytes) -> cudaError_t {
+        if (bytes == 0)
+            return cudaSuccess;
+        return cudaMemcpy(b + o, src, bytes, cudaMemcpyHostToDevice);
+    };
+    const cudaError_t es[] = {
+        up(oNodes, wide.nodes.data(), wide.nodes.size() * sizeof(CwbvhNode)),
+        up(oBTris, wide.tris.data(), wide.tris.size() * sizeof(float4)),
+        up(oTris, fs.tris.data(), fs.tris.size() * sizeof(TriShade)),
+        up(oMat, fs.matIdx.data(), fs.matIdx.size() * sizeof(uint32_t)),
+        up(oMats, fs.materials.data(), fs.materials.size() * sizeof(Material)),
+        up(oLights, fs.lights.data(), fs.lights.size() * sizeof(LightTri)),
+        up(oAlias, fs.alias.data(), fs.alias.size() * sizeof(AliasEntry)),
+        up(oXf, fs.invTransforms.data(), fs.invTransforms.size() * sizeof(float4)),
+    };
+    for (cudaError_t x : es)
+        if (x != cudaSuccess) {
+            c->sceneArena.release();
+            return cuda_fail(c, x, "cudaMemcpy(scene)");
+        }
+    const auto t2 = std::chrono::steady_clock::now();
+
+    SceneView& s = c->scene;
+    s.nodes = reinterpret_cast<const CwbvhNode*>(b + oNodes);
+    s.bvhTris = reinterpret_cast<const float4*>(b + oBTris);
+    s.tris = reinterpret_cast<const TriShade*>(b + oTris);
+    s.matIdx = reinterpret_cast<const uint32_t*>(b + oMat);
+    s.materials = reinterpret_cast<const Material*>(b + oMats);
+    s.lights = reinterpret_cast<const LightTri*>(b + oLights);
+    s.alias = reinterpret_cast<const AliasEntry*>(b + oAlias);
+    s.invTransforms = reinterpret_cast<const float4*>(b + oXf);
+    s.lightCount = int32_t(fs.lights.size());
+    s.lightEnergy = fs.lightEnergy;
+    s.lightEnergyTotal = fs.lightEnergyTotal;
+    s.nodeCount = uint32_t(wide.nodes.size());
+    s.triCount = m.triangle_count;
+
+    tr_scene_info& in = c->info;
+    in = tr_scene_info{};
+    in.triangle_count = m.triangle_count;
+    in.light_count = uint32_t(fs.lights.size());
+    in.material_count = desc->material_count;
+    in.bvh_node_count = uint32_t(wide.nodes.size());
+    in.device_bytes = off;
+    in.light_energy = fs.lightEnergyTotal;
+    in.build_time_ms = std::chrono::duration<float, std::milli>(t1 - t0).count();
+    in.upload_time_ms = std::chrono::duration<float, std::milli>(t2 - t1).count();
+    for (int i = 0; i < 6; ++i)
+        in.scene_bounds[i] = fs.bounds[i];
+    c->hasScene = true;
+    c->sampleCount = 0;
+    if (c->frame.sampleCount)
+        cudaMemset(c->frame.sampleCount, 0, sizeof(uint32_t));
+    return TR_OK;
+}
+
+tr_status tr_get_scene_info(void* ctx, tr_scene_info* info)
+{
+    if (!ctx || !info)
+        return TR_ERR_INVALID_ARGUMENT;
+    Context* c = static_cast<Context*>(ctx);
+    if (!c->hasScene)
+        return fail(c, TR_ERR_NO_SCENE, "no scene uploaded");
+    *info = c->info;
+    return TR_OK;
+}
+
+tr_status tr_set_camera(void* ctx, const tr_camera* cam)
+{
+    if (!ctx || !cam)
+        return TR_ERR_INVALID_ARGUMENT;
+    Context* c = static_cast<Context*>(ctx);
+    Camera k{};
+    k.pos = make_float3(cam->position[0], cam->position[1], cam->position[2]);
+    k.side = make_float3(cam->side[0], cam->side[1], cam->side[2]);
+    k.up = make_float3(cam->up[0], cam->up[1], cam->up[2]);
+    k.forward = make_float3(cam->forward[0], cam->forward[1], cam->forward[2]);
+    k.aperture = cam->aperture;
+    k.distortion = cam->distortion;
+    k.focalDist = cam->focal_dist;
+    k.fov = cam->fov;
+    k.bokehSideCount = cam->bokeh_side_count;
+    k.bokehRotation = cam->bokeh_rotation;
+    k.tanFov2 = tanf(cam->fov / 2.0f);
+    if (!(cam->fov > 0.f && cam->fov < 3.14159f) || !(cam->focal_dist > 0.f))
+        return fail(c, TR_ERR_INVALID_ARGUMENT, "camera fov must be in (0, pi) and focal_dist > 0");
+    c->camera = k;
+    c->hasCamera = true;
+    invalidate_graph(c);
+    return tr_reset(ctx);
+}
+
+tr_status tr_set_settings(void* ctx, const tr_kernel_settings* s)
+{
+    if (!ctx || !s)
+        return TR_ERR_INVALID_ARGUMENT;
+    Context* c = static_cast<Context*>(ctx);
+    if (s->multi_sample == 0 || s->max_depth == 0 || s->max_depth > TR_MAX_DEPTH)
+        return fail(c, TR_ERR_INVALID_ARGUMENT, "multi_sample must be >= 1 and max_depth in [1, 16]");
+    if (!(s->ray_epsilon >= 0.f))
+        return fail(c, TR_ERR_INVALID_ARGUMENT, "ray_epsilon must be >= 0");
+    Settings k{};
+    k.multiSample = s->multi_sample;
+    k.maxDepth = s->max_depth;
+    k.seed = s->seed;
+    k.rayEpsilon = s->ray_epsilon;
+    k.rrStart = s->rr_start;
+    k.flags = s->flags;
+    k.maxColor = s->max_color > 0.f ? s->max_color : 10.f;
+    const bool changed = std::memcmp(&k, &c->settings, sizeof(Settings)) != 0;
+    c->settings = k;
+    if (changed) {
+        invalidate_graph(c);
+        return tr_reset(ctx);
+    }
+    return TR_OK;
+}
+
+tr_status tr_resize(void* ctx, uint32_t width, uint32_t height)
+{
+    if (!ctx)
+        return TR_ERR_INVALID_ARGUMENT;
+    Context* c = static_cast<Context*>(ctx);
+    if (width == 0 || height == 0 || uint64_t(width) * height >= TR_MAX_PATHS)
+        return fail(c, TR_ERR_INVALID_ARGUMENT, "resolution must be non-zero with width*height < 2^28");
+    c->width = width;
+    c->height = height;
+    return tr_reset(ctx);
+}
+
+tr_status tr_reset(void* ctx)
+{
+    if (!ctx)
+        return TR_ERR_INVALID_ARGUMENT;
+    Context* c = static_cast<Context*>(ctx);
+    c->sampleCount = 0;
+    if (c->frame.sampleCount && c->frameArena.base) {
+        cudaSetDevice(c->device);
+        TR_CUDA(c, cudaMemsetAsync(c->frame.sampleCount, 0, sizeof(uint32_t), c->stream));
+        TR_CUDA(c, cudaMemsetAsync(c->frame.traversal, 0, 4 * sizeof(unsigned long long), c->stream));
+        TR_CUDA(c, cudaStreamSynchronize(c->stream));
+    }
+    return TR_OK;
+}
+
+tr_status tr_begin_frame(void* ctx, void* stream)
+{
+    if (!ctx)
+        return TR_ERR_INVALID_ARGUMENT;
+    Context* c = static_cast<Context*>(ctx);
+    cudaSetDevice(c->device);
+    tr_status st = check_ready(c);
+    if (st != TR_OK)
+        return st;
+    c->timedFrame = false;
+    c->lastStream = pick_stream(c, stream);
+    return enqueue_begin(c, c->lastStream);
+}
+
+tr_status tr_generate(void* ctx, void* stream)
+{
+    if (!ctx)
+        return TR_ERR_INVALID_ARGUMENT;
+    Context* c = static_cast<Context*>(ctx);
+    tr_status st = check_ready(c);
+    if (st != TR_OK)
+        return st;
+    TR_CUDA(c, launch_generate(c->frame, c->camera, c->settings, pick_stream(c, stream)));
+    return TR_OK;
+}
+
+tr_status tr_extend(void* ctx, void* stream, uint32_t bounce)
+{
+    if (!ctx)
+        return TR_ERR_INVALID_ARGUMENT;
+    Context* c = static_cast<Context*>(ctx);
+    if (bounce >= TR_MAX_DEPTH)
+        return fail(c, TR_ERR_INVALID_ARGUMENT, "bounce out of range");
+    tr_status st = check_ready(c);
+    if (st != TR_OK)
+        return st;
+    TR_CUDA(c, launch_extend(c->scene, c->frame, c->settings, bounce, c->shape, pick_stream(c, stream)));
+    return TR_OK;
+}
+
+tr_status tr_shade(void* ctx, void* stream, uint32_t bounce)
+{
+    if (!ctx)
+        return TR_ERR_INVALID_ARGUMENT;
+    Context* c = static_cast<Context*>(ctx);
+    if (bounce >= TR_MAX_DEPTH)
+        return fail(c, TR_ERR_INVALID_ARGUMENT, "bounce out of range");
+    tr_status st = check_ready(c);
+    if (st != TR_OK)
+        return st;
+    TR_CUDA(c, launch_shade(c->scene, c->frame, c->settings, bounce, c->shape, pick_stream(c, stream)));
+    return TR_OK;
+}
+
+tr_status tr_connect(void* ctx, void* stream, uint32_t bounce)
+{
+    if (!ctx)
+        return TR_ERR_INVALID_ARGUMENT;
+    Context* c = static_cast<Context*>(ctx);
+    if (bounce >= TR_MAX_DEPTH)
+        return fail(c, TR_ERR_INVALID_ARGUMENT, "bounce out of range");
+    tr_status st = check_ready(c);
+    if (st != TR_OK)
+        return st;
+    TR_CUDA(c, launch_connect(c->scene, c->frame, c->settings, bounce, c->shape, pick_stream(c, stream)));
+    return TR_OK;
+}
+
+tr_status tr_finalize(void* ctx, void* stream)
+{
+    if (!ctx)
+        return TR_ERR_INVALID_ARGUMENT;
+    Context* c = static_cast<Context*>(ctx);
+    tr_status st = check_ready(c);
+    if (st != TR_OK)
+        return st;
+    TR_CUDA(c, launch_finalize(c->frame, c->settings, pick_stream(c, stream)));
+    c->sampleCount += c->settings.multiSample;
+    return TR_OK;
+}
+
+tr_status tr_render_frame(void* ctx, void* stream, int32_t use_graph)
+{
+    if (!ctx)
+        return TR_ERR_INVALID_ARGUMENT;
+    Context* c = static_cast<Context*>(ctx);
+    cudaSetDevice(c->device);
+    tr_status st = check_ready(c);
+    if (st != TR_OK)
+        return st;
+    cudaStream_t s = pick_stream(c, stream);
+    c->lastStream = s;
+    if (use_graph) {
+        if (!c->graphValid) {
+            // capture on the context stream (the legacy default stream cannot be captured)
+            TR_CUDA(c, cudaStreamBeginCapture(c->stream, cudaStreamCaptureModeThreadLocal));
+            st = enqueue_frame(c, c->stream, false);
+            cudaGraph_t g = nullptr;
+            const cudaError_t ec = cudaStreamEndCapture(c->stream, &g);
+            if (st != TR_OK) {
+                if (g)
+                    cudaGraphDestroy(g);
+                return st;
+            }
+            if (ec != cudaSuccess)
+                return cuda_fail(c, ec, "cudaStreamEndCapture");
+            c->graph = g;
+            TR_CUDA(c, cudaGraphInstantiate(&c->graphExec, g, 0));
+            c->graphValid = true;
+        }
+        TR_CUDA(c, cudaGraphLaunch(c->graphExec, s));
+        c->timedFrame = false;
+    } else {
+        st = enqueue_frame(c, s, true);
+        if (st != TR_OK)
+            return st;
+        c->timedFrame = true;
+        c->timedDepth = c->settings.maxDepth;
+    }
+    c->sampleCount += c->settings.multiSample;
+    return TR_OK;
+}
+
+tr_status tr_synchronize(void* ctx, void* stream)
+{
+    if (!ctx)
+        return TR_ERR_INVALID_ARGUMENT;
+    Context* c = static_cast<Context*>(ctx);
+    cudaSetDevice(c->device);
+    TR_CUDA(c, cudaStreamSynchronize(pick_stream(c, stream)));
+    return TR_OK;
+}
+
+tr_status tr_get_statistics(void* ctx, tr_statistics* out)
+{
+    if (!ctx || !out)
+        return TR_ERR_INVALID_ARGUMENT;
+    Context* c = static_cast<Context*>(ctx);
+    if (!c->frameArena.base)
+        return fail(c, TR_ERR_NOT_READY, "no frame rendered");
+    cudaSetDevice(c->device);
+    TR_CUDA(c, cudaDeviceSynchronize());
+    TR_CUDA(c, cudaMemcpy(c->hostCounters, c->frame.counters, kCounterWords * sizeof(uint32_t), cudaMemcpyDeviceToHost));
+    uint32_t err = 0, sc = 0;
+    unsigned long long trav[4] = {0, 0, 0, 0};
+    TR_CUDA(c, cudaMemcpy(trav, c->frame.traversal, sizeof(trav), cudaMemcpyDeviceToHost));
+    TR_CUDA(c, cudaMemcpy(&err, c->frame.errorFlag, sizeof(uint32_t), cudaMemcpyDeviceToHost));
+    TR_CUDA(c, cudaMemcpy(&sc, c->frame.sampleCount, sizeof(uint32_t), cudaMemcpyDeviceToHost));
+    tr_statistics s{};
+    const uint32_t depth = c->settings.maxDepth;
+    for (uint32_t b = 0; b < depth; ++b) {
+        s.extend_rays[b] = b == 0 ? c->frame.pathCount : c->hostCounters[b];
+        s.shadow_rays[b] = c->hostCounters[kShadowCounterBase + b];
+        s.path_count += s.extend_rays[b] + s.shadow_rays[b];
+        s.shadow_ray_count += s.shadow_rays[b];
+        if (b == 0)
+            s.primary_path_count = s.extend_rays[b];
+        else if (b == 1)
+            s.secondary_path_count = s.extend_rays[b];
+        else
+            s.deep_path_count += s.extend_rays[b];
+    }
+    if (c->timedFrame) {
+        float ms = 0.f;
+        cudaEventElapsedTime(&ms, c->evStart, c->evFinal);
+        s.render_time_ms = ms;
+        cudaEventElapsedTime(&ms, c->evStart, c->evGenerate);
+        s.generate_time_ms = ms;
+        cudaEvent_t prev = c->evGenerate;
+        for (uint32_t b = 0; b < c->timedDepth; ++b) {
+            cudaEventElapsedTime(&ms, prev, c->evExtend[b]);
+            s.extend_time_ms += ms;
+            cudaEventElapsedTime(&ms, c->evExtend[b], c->evShade[b]);
+            s.shade_time_ms += ms;
+            cudaEventElapsedTime(&ms, c->evShade[b], c->evConnect[b]);
+            s.connect_time_ms += ms;
+            prev = c->evConnect[b];
+        }
+        cudaEventElapsedTime(&ms, prev, c->evFinal);
+        s.finalize_time_ms = ms;
+    }
+    s.sample_count = sc;
+    s.device_error = err;
+    s.traversal_extend_nodes = trav[0];
+    s.traversal_extend_tris = trav[1];
+    s.traversal_connect_nodes = trav[2];
+    s.traversal_connect_tris = trav[3];
+    *out = s;
+    return TR_OK;
+}
+
+tr_status tr_get_buffers(void* ctx, tr_buffers* out)
+{
+    if (!ctx || !out)
+        return TR_ERR_INVALID_ARGUMENT;
+    Context* c = static_cast<Context*>(ctx);
+    tr_status st = ensure_frame(c);
+    if (st != TR_OK)
+        return st;
+    tr_buffers b{};
+    b.path_state[0] = c->frame.state[0];
+    b.path_state[1] = c->frame.state[1];
+    b.hits = c->frame.hits;
+    b.shadow = c->frame.shadow;
+    b.radiance = c->frame.radiance;
+    b.accumulator = c->frame.accumulator;
+    b.albedo = c->frame.albedo;
+    b.normals = c->frame.normals;
+    b.colors = c->frame.colors;
+    b.counters = c->frame.counters;
+    b.capacity = c->frame.capacity;
+    b.width = c->frame.resX;
+    b.height = c->frame.resY;
+    *out = b;
+    return TR_OK;
+}
+
+static tr_status download(Context* c, void* stream, const void* src, float* dst, uint64_t bytes)
+{
+    if (!c->frameArena.base)
+        return fail(c, TR_ERR_NOT_READY, "no frame rendered");
+    const uint64_t need = uint64_t(c->frame.resX) * c->frame.resY * sizeof(float4);
+    if (!dst || bytes < need)
+        return fail(c, TR_ERR_INVALID_ARGUMENT, "destination smaller than width*height*16 bytes");
+    cudaSetDevice(c->device);
+    cudaStream_t s = pick_stream(c, stream);
+    TR_CUDA(c, cudaMemcpyAsync(dst, src, need, cudaMemcpyDeviceToHost, s));
+    TR_CUDA(c, cudaStreamSynchronize(s));
+    return TR_OK;
+}
+
+tr_status tr_download_image(void* ctx, void* stream, float* host_rgba, uint64_t bytes)
+{
+    if (!ctx)
+        return TR_ERR_INVALID_ARGUMENT;
+    Context* c = static_cast<Context*>(ctx);
+    return download(c, stream, c->frame.colors, host_rgba, bytes);
+}
+
+tr_status tr_download_accumulator(void* ctx, void* stream, float* host_rgba, uint64_t bytes)
+{
+    if (!ctx)
+        return TR_ERR_INVALID_ARGUMENT;
+    Context* c = static_cast<Context*>(ctx);
+    return download(c, stream, c->frame.accumulator, host_rgba, bytes);
+}
+
+tr_status tr_copy_from_device(void* ctx, void* host_dst, const void* device_src, uint64_t bytes)
+{
+    if (!ctx)
+        return TR_ERR_INVALID_ARGUMENT;
+    Context* c = static_cast<Context*>(ctx);
+    if ((!host_dst || !device_src) && bytes)
+        return fail(c, TR_ERR_INVALID_ARGUMENT, "null pointer");
+    cudaSetDevice(c->device);
+    TR_CUDA(c, cudaDeviceSynchronize());
+    TR_CUDA(c, cudaMemcpy(host_dst, device_src, bytes, cudaMemcpyDeviceToHost));
+    return TR_OK;
+}
+
+tr_status tr_copy_to_device(void* ctx, void* device_dst, const void* host_src, uint64_t bytes)
+{
+    if (!ctx)
+        return TR_ERR_INVALID_ARGUMENT;
+    Context* c = static_cast<Context*>(ctx);
+    if ((!device_dst || !host_src) && bytes)
+        return fail(c, TR_ERR_INVALID_ARGUMENT, "null pointer");
+    cudaSetDevice(c->device);
+    TR_CUDA(c, cudaDeviceSynchronize());
+    TR_CUDA(c, cudaMemcpy(device_dst, host_src, bytes, cudaMemcpyHostToDevice));
+    return TR_OK;
+}
+
+} // extern "C"

@@ -1,0 +1,403 @@
+// Host BVH builder: binned SAH over triangle bounds, then a greedy collapse to
+// an 8-wide compressed BVH (CWBVH) with octant-ordered child slots and 8-bit
+// quantized child boxes (Ylitie, Karras, Laine, HPG 2017).
+#include "tr_bvh.h"
+
+#include <algorithm>
+#include <atomic>
+#include <cmath>
+#include <cstring>
+#include <deque>
+#include <thread>
+
+namespace tr {
+namespace {
+
+struct PrimInfo {
+    float lo[3];
+    float hi[3];
+    float c[3];
+};
+
+inline void box_empty(Aabb& b)
+{
+    for (int a = 0; a < 3; ++a) {
+        b.lo[a] = INFINITY;
+        b.hi[a] = -INFINITY;
+    }
+}
+inline void box_grow(Aabb& b, const float* lo, const float* hi)
+{
+    for (int a = 0; a < 3; ++a) {
+        b.lo[a] = std::min(b.lo[a], lo[a]);
+        b.hi[a] = std::max(b.hi[a], hi[a]);
+    }
+}
+inline float box_area(const Aabb& b)
+{
+    const float dx = b.hi[0] - b.lo[0], dy = b.hi[1] - b.lo[1], dz = b.hi[2] - b.lo[2];
+    if (!(dx >= 0.f) || !(dy >= 0.f) || !(dz >= 0.f))
+        return 0.f;
+    return 2.f * (dx * dy + dy * dz + dz * dx);
+}
+
+struct BinaryBuilder {
+    const std::vector<PrimInfo>& prims;
+    std::vector<uint32_t>& refs;
+    std::vector<BinaryNode>& nodes;
+    BvhBuildOptions opt;
+    std::atomic<uint32_t> nodeCount{1};
+    std::atomic<int> threadsLeft{0};
+
+    BinaryBuilder(const std::vector<PrimInfo>& p, std::vector<uint32_t>& r, std::vector<BinaryNode>& n,
+                  const BvhBuildOptions& o)
+        : prims(p), refs(r), nodes(n), opt(o)
+    {
+    }
+
+    void make_leaf(uint32_t nodeIx, uint32_t begin, uint32_t end, const Aabb& box)
+    {
+        BinaryNode& n = nodes[nodeIx];
+        n.box = box;
+        n.left = begin;
+        n.count = end - begin;
+    }
+
+    void build(uint32_t nodeIx, uint32_t begin, uint32_t end)
+    {
+        const uint32_t count = end - begin;
+        Aabb box, cbox;
+        box_empty(box);
+        box_empty(cbox);
+        for (uint32_t i = begin; i < end; ++i) {
+            const PrimInfo& p = prims[refs[i]];
+            box_grow(box, p.lo, p.hi);
+            box_grow(cbox, p.c, p.c);
+        }
+        if (count == 1) {
+            make_leaf(nodeIx, begin, end, box);
+            return;
+        }
+
+        // binned SAH over all three axes
+        const uint32_t B = std::max(2u, std::min(opt.bins, 64u));
+        float bestCost = INFINITY;
+        int bestAxis = -1;
+        uint32_t bestSplit = 0;
+        const float parentArea = box_area(box);
+        for (int axis = 0; axis < 3; ++axis) {
+            const float extent = cbox.hi[axis] - cbox.lo[axis];
+            if (!(extent > 0.f))
+                continue;
+            Aabb binBox[64];
+            uint32_t binCount[64];
+            for (uint32_t b = 0; b < B; ++b) {
+                box_empty(binBox[b]);
+                binCount[b] = 0;
+            }
+            const float k = float(B) / extent;
+            for (uint32_t i = begin; i < end; ++i) {
+                const PrimInfo& p = prims[refs[i]];
+                uint32_t b = uint32_t((p.c[axis] - cbox.lo[axis]) * k);
+                b = std::min(b, B - 1);
+                box_grow(binBox[b], p.lo, p.hi);
+                binCount[b]++;
+            }
+            float rightArea[64];
+            uint32_t rightCount[64];
+            Aabb acc;
+            box_empty(acc);
+            uint32_t cnt = 0;
+            for (uint32_t b = B - 1; b > 0; --b) {
+                box_grow(acc, binBox[b].lo, binBox[b].hi);
+                cnt += binCount[b];
+                rightArea[b] = box_area(acc);
+                rightCount[b] = cnt;
+            }
+            box_empty(acc);
+            cnt = 0;
+            for (uint32_t b = 0; b + 1 < B; ++b) {
+                box_grow(acc, binBox[b].lo, binBox[b].hi);
+                cnt += binCount[b];
+                if (cnt == 0 || rightCount[b + 1] == 0)
+                    continue;
+                const float cost = box_area(acc) * float(cnt) + rightArea[b + 1] * float(rightCount[b + 1]);
+                if (cost < bestCost) {
+                    bestCost = cost;
+                    bestAxis = axis;
+                    bestSplit = b + 1;
+                }
+            }
+        }
+
+        // leaf if allowed and cheaper (traversal step cost 1, intersection cost 1)
+        const float leafCost = float(count);
+        const float splitCost = parentArea > 0.f ? 1.f + bestCost / parentArea : INFINITY;
+        if (count <= opt.maxLeafSize && (bestAxis < 0 || leafCost <= splitCost)) {
+            make_leaf(nodeIx, begin, end, box);
+            return;
+        }
+
+        uint32_t mid = begin;
+        if (bestAxis >= 0) {
+            const float extent = cbox.hi[bestAxis] - cbox.lo[bestAxis];
+            const float k = float(B) / extent;
+            const float lo = cbox.lo[bestAxis];
+            uint32_t* it = std::partition(refs.data() + begin, refs.data() + end, [&](uint32_t r) {
+                uint32_t b = uint32_t((prims[r].c[bestAxis] - lo) * k);
+                b = std::min(b, B - 1);
+                return b < bestSplit;
+            });
+            mid = uint32_t(it - refs.data());
+        }
+        if (mid == begin || mid == end) {
+            // degenerate centroids: median split along the widest centroid axis
+            int axis = 0;
+            float ext = -1.f;
+            for (int a = 0; a < 3; ++a) {
+                const float e = cbox.hi[a] - cbox.lo[a];
+                if (e > ext) {
+                    ext = e;
+                    axis = a;
+                }
+            }
+            mid = begin + count / 2;
+            std::nth_element(refs.data() + begin, refs.data() + mid, refs.data() + end,
+                             [&](uint32_t x, uint32_t y) { return prims[x].c[axis] < prims[y].c[axis]; });
+        }
+
+        const uint32_t children = nodeCount.fetch_add(2);
+        BinaryNode& n = nodes[nodeIx];
+        n.box = box;
+        n.left = children;
+        n.count = 0;
+
+        const bool spawn = count > 32768 && threadsLeft.fetch_sub(1) > 0;
+        if (spawn) {
+            std::thread t([this, children, begin, mid] { build(children, begin, mid); });
+            build(children + 1, mid, end);
+            t.join();
+        } else {
+            build(children, begin, mid);
+            build(children + 1, mid, end);
+        }
+    }
+};
+
+inline uint8_t byte_of(const uint32_t* words, int i) { return uint8_t((words[i >> 2] >> ((i & 3) * 8)) & 0xff); }
+inline void set_byte(uint32_t* words, int i, uint32_t v)
+{
+    words[i >> 2] &= ~(0xffu << ((i & 3) * 8));
+    words[i >> 2] |= (v & 0xffu) << ((i & 3) * 8);
+}
+
+} // namespace
+
+BinaryBvh build_binary_bvh(const float* positions, const uint32_t* indices, uint32_t triCount,
+                           const BvhBuildOptions& options)
+{
+    BinaryBvh out;
+    std::vector<PrimInfo> prims(triCount);
+    for (uint32_t t = 0; t < triCount; ++t) {
+        PrimInfo& p = prims[t];
+        for (int a = 0; a < 3; ++a) {
+            const float x0 = positions[3 * indices[3 * t + 0] + a];
+            const float x1 = positions[3 * indices[3 * t + 1] + a];
+            const float x2 = positions[3 * indices[3 * t + 2] + a];
+            p.lo[a] = std::min(x0, std::min(x1, x2));
+            p.hi[a] = std::max(x0, std::max(x1, x2));
+            p.c[a] = 0.5f * (p.lo[a] + p.hi[a]);
+        }
+    }
+    out.primRefs.resize(triCount);
+    for (uint32_t t = 0; t < triCount; ++t)
+        out.primRefs[t] = t;
+    out.nodes.resize(std::max<size_t>(1, 2 * size_t(triCount)));
+    if (triCount == 0) {
+        box_empty(out.nodes[0].box);
+        out.nodes[0].left = 0;
+        out.nodes[0].count = 0;
+        out.nodes.resize(1);
+        return out;
+    }
+    BvhBuildOptions opt = options;
+    opt.maxLeafSize = std::max(1u, std::min(opt.maxLeafSize, 3u));
+    BinaryBuilder b(prims, out.primRefs, out.nodes, opt);
+    const unsigned hw = std::max(1u, std::thread::hardware_concurrency());
+    b.threadsLeft = int(opt.threads ? opt.threads : hw) - 1;
+    b.build(0, 0, triCount);
+    out.nodes.resize(b.nodeCount.load());
+    return out;
+}
+
+Cwbvh collapse_to_cwbvh(const BinaryBvh& bvh, const float* positions, const uint32_t* indices)
+{
+    Cwbvh out;
+    const std::vector<BinaryNode>& bn = bvh.nodes;
+    out.nodes.reserve(bn.size() / 4 + 1);
+    out.tris.reserve(bvh.primRefs.size() * 3);
+    out.triPrim.reserve(bvh.primRefs.size());
+    out.nodes.push_back(CwbvhNode{});
+    if (bvh.primRefs.empty()) {
+        // empty scene: a root without children never reports a hit
+        return out;
+    }
+
+    struct Task {
+        uint32_t bin;
+        uint32_t wide;
+    };
+    std::deque<Task> tasks;
+    tasks.push_back({0, 0});
+    while (!tasks.empty()) {
+        const Task task = tasks.front();
+        tasks.pop_front();
+
+        // gather up to 8 children by repeatedly opening the largest internal child
+        uint32_t kids[8];
+        int kidCount = 0;
+        if (bn[task.bin].count > 0) {
+            kids[kidCount++] = task.bin;  // a leaf root
+        } else {
+            kids[kidCount++] = bn[task.bin].left;
+            kids[kidCount++] = bn[task.bin].left + 1;
+        }
+        while (kidCount < 8) {
+            int best = -1;
+            float bestArea = -1.f;
+            for (int k = 0; k < kidCount; ++k) {
+                if (bn[kids[k]].count == 0) {
+                    const float a = box_area(bn[kids[k]].box);
+                    if (a > bestArea) {
+                        bestArea = a;
+                        best = k;
+                    }
+                }
+            }
+            if (best < 0)
+                break;
+            const uint32_t opened = kids[best];
+            kids[best] = bn[opened].left;
+            kids[kidCount++] = bn[opened].left + 1;
+        }
+
+        Aabb nodeBox;
+        box_empty(nodeBox);
+        for (int k = 0; k < kidCount; ++k)
+            box_grow(nodeBox, bn[kids[k]].box.lo, bn[kids[k]].box.hi);
+
+        // slot assignment: slot s holds the child nearest for rays of octant s
+        // (octant bit a set = negative direction along axis a)
+        int slotKid[8];
+        for (int s = 0; s < 8; ++s)
+            slotKid[s] = -1;
+        {
+            float cost[8][8];
+            float pc[3];
+            for (int a = 0; a < 3; ++a)
+                pc[a] = 0.5f * (nodeBox.lo[a] + nodeBox.hi[a]);
+            for (int k = 0; k < kidCount; ++k) {
+                float c[3];
+                for (int a = 0; a < 3; ++a)
+                    c[a] = 0.5f * (bn[kids[k]].box.lo[a] + bn[kids[k]].box.hi[a]) - pc[a];
+                for (int s = 0; s < 8; ++s) {
+                    const float dx = (s & 1) ? -1.f : 1.f, dy = (s & 2) ? -1.f : 1.f, dz = (s & 4) ? -1.f : 1.f;
+                    cost[k][s] = c[0] * dx + c[1] * dy + c[2] * dz;
+                }
+            }
+            bool kidDone[8] = {};
+            for (int round = 0; round < kidCount; ++round) {
+                float bc = INFINITY;
+                int bk = -1, bs = -1;
+                for (int k = 0; k < kidCount; ++k) {
+                    if (kidDone[k])
+                        continue;
+                    for (int s = 0; s < 8; ++s) {
+                        if (slotKid[s] >= 0)
+                            continue;
+                        if (cost[k][s] < bc || bk < 0) {
+                            bc = cost[k][s];
+                            bk = k;
+                            bs = s;
+                        }
+                    }
+                }
+                kidDone[bk] = true;
+                slotKid[bs] = bk;
+            }
+        }
+
+        // quantization frame
+        CwbvhNode node{};
+        uint32_t w0[4] = {0, 0, 0, 0};
+        uint32_t meta[2] = {0, 0};
+        uint32_t q[6][2] = {};  // qlo.x, qlo.y, qlo.z, qhi.x, qhi.y, qhi.z
+        double scale[3];
+        int biased[3];
+        for (int a = 0; a < 3; ++a) {
+            const double extent = double(nodeBox.hi[a]) - double(nodeBox.lo[a]);
+            int e = -100;
+            if (extent > 0.0) {
+                int ex;
+                std::frexp(extent / 255.0, &ex);
+                e = ex;
+            }
+            e = std::max(-126, std::min(e, 127));
+            biased[a] = e + 127;
+            scale[a] = std::ldexp(1.0, e);
+            w0[a] = f2u(nodeBox.lo[a]);
+        }
+        w0[3] = uint32_t(biased[0]) | (uint32_t(biased[1]) << 8) | (uint32_t(biased[2]) << 16);
+
+        uint32_t imask = 0;
+        const uint32_t triBase = uint32_t(out.triPrim.size());
+        const uint32_t childBase = uint32_t(out.nodes.size());
+        uint32_t internalCount = 0;
+        for (int s = 0; s < 8; ++s) {
+            if (slotKid[s] < 0)
+                continue;
+            const BinaryNode& kid = bn[kids[slotKid[s]]];
+            for (int a = 0; a < 3; ++a) {
+                const double lo = (double(kid.box.lo[a]) - double(nodeBox.lo[a])) / scale[a];
+                const double hi = (double(kid.box.hi[a]) - double(nodeBox.lo[a])) / scale[a];
+                const int qlo = std::max(0, std::min(255, int(std::floor(lo))));
+                const int qhi = std::max(0, std::min(255, int(std::ceil(hi))));
+                set_byte(q[a], s, uint32_t(qlo));
+                set_byte(q[3 + a], s, uint32_t(qhi));
+            }
+            if (kid.count == 0) {
+                imask |= 1u << s;
+                set_byte(meta, s, 0x20u | (24u + uint32_t(s)));
+                tasks.push_back({kids[slotKid[s]], childBase + internalCount});
+                internalCount++;
+            } else {
+                const uint32_t offset = uint32_t(out.triPrim.size()) - triBase;
+                const uint32_t unary = (1u << kid.count) - 1u;
+                set_byte(meta, s, (unary << 5) | offset);
+                for (uint32_t i = 0; i < kid.count; ++i) {
+                    const uint32_t prim = bvh.primRefs[kid.left + i];
+                    const float* p0 = positions + 3 * indices[3 * prim + 0];
+                    const float* p1 = positions + 3 * indices[3 * prim + 1];
+                    const float* p2 = positions + 3 * indices[3 * prim + 2];
+                    out.tris.push_back(make_float4(p0[0], p0[1], p0[2], u2f(prim)));
+                    out.tris.push_back(make_float4(p1[0] - p0[0], p1[1] - p0[1], p1[2] - p0[2], 0.f));
+                    out.tris.push_back(make_float4(p2[0] - p0[0], p2[1] - p0[1], p2[2] - p0[2], 0.f));
+                    out.triPrim.push_back(prim);
+                }
+            }
+        }
+        w0[3] |= imask << 24;
+        for (uint32_t i = 0; i < internalCount; ++i)
+            out.nodes.push_back(CwbvhNode{});
+
+        node.w[0] = make_uint4(w0[0], w0[1], w0[2], w0[3]);
+        node.w[1] = make_uint4(childBase, triBase, meta[0], meta[1]);
+        node.w[2] = make_uint4(q[0][0], q[0][1], q[1][0], q[1][1]);
+        node.w[3] = make_uint4(q[2][0], q[2][1], q[3][0], q[3][1]);
+        node.w[4] = make_uint4(q[4][0], q[4][1], q[5][0], q[5][1]);
+        out.nodes[task.wide] = node;
+    }
+    return out;
+}
+
+} // namespace tr

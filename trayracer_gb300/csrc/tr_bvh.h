@@ -1,0 +1,52 @@
+// Host BVH builder: binned-SAH binary BVH, collapsed into an 8-wide
+// compressed BVH (CWBVH) for the extend/connect kernels. Replaces the OptiX
+// acceleration-structure build of the reference (Model::Upload,
+// Tracer/Resources/Model.cpp:240-306; OptixRenderer::BuildAccel,
+// Tracer/Optix/OptixRenderer.cpp:90-123).
+#pragma once
+
+#include <cstdint>
+#include <vector>
+
+#include "tr_device.h"
+
+namespace tr {
+
+struct Aabb {
+    float lo[3];
+    float hi[3];
+};
+
+struct BinaryNode {
+    Aabb box;
+    uint32_t left;     // internal: index of the left child (right = left + 1); leaf: first primitive ref
+    uint32_t count;    // 0 = internal, else primitives in the leaf
+};
+
+struct BvhBuildOptions {
+    uint32_t maxLeafSize = 3;   // 1..3 (the CWBVH leaf encoding holds up to 3)
+    uint32_t bins = 16;
+    uint32_t threads = 0;       // 0 = hardware concurrency
+};
+
+struct BinaryBvh {
+    std::vector<BinaryNode> nodes;
+    std::vector<uint32_t> primRefs;   // leaf ranges index this array; values are triangle indices
+};
+
+struct Cwbvh {
+    std::vector<CwbvhNode> nodes;
+    std::vector<float4> tris;          // 3 float4 per triangle slot
+    std::vector<uint32_t> triPrim;     // triangle index per slot
+};
+
+// Builds a binary BVH over triangles given as positions (float3 per vertex)
+// and indices (uint3 per triangle).
+BinaryBvh build_binary_bvh(const float* positions, const uint32_t* indices, uint32_t triCount,
+                           const BvhBuildOptions& options);
+
+// Collapses a binary BVH into the 8-wide compressed layout and packs the
+// traversal triangles (v0, e1 = v1 - v0, e2 = v2 - v0).
+Cwbvh collapse_to_cwbvh(const BinaryBvh& bvh, const float* positions, const uint32_t* indices);
+
+} // namespace tr

@@ -1,0 +1,166 @@
+// Device-resident data layout of the wavefront path tracer (shared by the host
+// build code and the kernels).
+#pragma once
+
+#include "tr_vec.h"
+#include "../../include/trayracer.h"
+
+namespace tr {
+
+// Shading record of one triangle: fp32 positions, fp16 texcoords and vertex
+// normals, fp16 face normal. Same content and 72-byte layout as the
+// reference's PackedTriangle (Tracer/Common/CommonStructs.h:219-253) so the
+// shading code reads the same values; fp16 fields are stored as raw bits.
+struct alignas(8) TriShade {
+    float v0x, v0y, v0z;
+    uint16_t uv0x, uv0y, N0x, N0y, N0z, Nx;
+    float v1x, v1y, v1z;
+    uint16_t uv1x, uv1y, N1x, N1y, N1z, Ny;
+    float v2x, v2y, v2z;
+    uint16_t uv2x, uv2y, N2x, N2y, N2z, Nz;
+};
+static_assert(sizeof(TriShade) == 72, "TriShade must stay 72 bytes");
+
+// Resolved constant material. The reference resolves its 13 fp16 properties
+// per hit (GetIntersectionAttributes, Tracer/CUDA/GPU/CudaMaterial.h:117-175);
+// without textures the resolution is per material, done once on upload with
+// the same formulas (emissive = Emissive * diffuse, tint from CIE XYZ,
+// luminance = Y).
+struct alignas(16) Material {
+    float3 diffuse;
+    float metallic;
+    float3 emissive;
+    float subsurface;
+    float3 tint;
+    float specular;
+    float roughness;
+    float specularTint;
+    float anisotropic;
+    float sheen;
+    float sheenTint;
+    float clearcoat;
+    float clearcoatGloss;
+    float luminance;
+    uint32_t closure;
+    uint32_t isEmissive;   // emissive.x + .y + .z > Epsilon (PathTracing.h:73)
+    uint32_t pad0, pad1;
+};
+static_assert(sizeof(Material) == 96, "Material must stay 96 bytes");
+
+// Emissive triangle in world space: same fields and 80-byte layout as the
+// reference's LightTriangle (Tracer/Common/CommonStructs.h:257-273).
+struct alignas(16) LightTri {
+    float3 V0;
+    int32_t instIx;
+    float3 V1;
+    int32_t triIx;
+    float3 V2;
+    float area;
+    float3 N;
+    float energy;
+    float3 radiance;
+    float sumEnergy;     // exclusive prefix of energy
+};
+static_assert(sizeof(LightTri) == 80, "LightTri must stay 80 bytes");
+
+// One entry of the Walker/Vose alias table over the lights.
+struct AliasEntry {
+    float prob;      // probability of keeping this bucket
+    uint32_t alias;  // bucket taken otherwise
+};
+
+// 8-wide compressed BVH node (Ylitie, Karras, Laine, "Efficient Incoherent Ray
+// Traversal on GPUs Through Compressed Wide BVHs", HPG 2017), 80 bytes:
+//   w0: p.x, p.y, p.z (float bits), e.x | e.y<<8 | e.z<<16 | imask<<24
+//   w1: child_base, tri_base, meta[0..3], meta[4..7]
+//   w2: qlo.x[0..7], qlo.y[0..7]
+//   w3: qlo.z[0..7], qhi.x[0..7]
+//   w4: qhi.y[0..7], qhi.z[0..7]
+// e are biased exponents (scale = 2^(e-127)); a child box is
+// p + q * scale. meta: 0 empty; internal child = 0x20 | (24 + slot);
+// leaf = (unary triangle count << 5) | triangle offset from tri_base.
+struct alignas(16) CwbvhNode {
+    uint4 w[5];
+};
+static_assert(sizeof(CwbvhNode) == 80, "CwbvhNode must stay 80 bytes");
+
+// Scene as seen by the kernels (constant for one uploaded scene).
+struct SceneView {
+    const CwbvhNode* nodes;
+    const float4* bvhTris;      // 3 float4 per triangle in BVH order: (v0, bits(primIx)), (e1, 0), (e2, 0)
+    const TriShade* tris;       // by primIx
+    const uint32_t* matIdx;     // by primIx
+    const Material* materials;
+    const LightTri* lights;
+    const AliasEntry* alias;
+    const float4* invTransforms; // 3 float4 per instance (inverse instance transform rows)
+    int32_t lightCount;
+    float lightEnergy;          // reference: last exclusive prefix (Renderer.cpp:500)
+    float lightEnergyTotal;     // sum of all light energies
+    uint32_t nodeCount;
+    uint32_t triCount;
+    uint32_t pad;
+};
+
+// Per-frame constants of the wavefront (constant between resizes / setting
+// changes). Passed by value as a kernel parameter.
+struct FrameView {
+    float4* state[2];      // 3 planes each, plane stride = capacity
+    uint4* hits;           // by queue slot
+    float4* shadow;        // 3 planes, plane stride = capacity
+    float4* radiance;      // by path index
+    float4* accumulator;   // by pixel
+    float4* albedo;        // by pixel (optional)
+    float4* normals;       // by pixel (optional)
+    float4* colors;        // by pixel
+    uint32_t* counters;    // kCounterWords words, layout above
+    uint32_t* sampleCount; // device copy of the accumulated sample count
+    uint32_t* errorFlag;   // set by bounded loops that ran out
+    unsigned long long* traversal;  // extend nodes, extend tris, connect nodes, connect tris (counting launches)
+    uint32_t capacity;
+    uint32_t resX, resY;
+    uint32_t pathCount;    // resX * resY * multiSample
+};
+
+struct Camera {
+    float3 pos;
+    float aperture;
+    float3 side;
+    float distortion;
+    float3 up;
+    float focalDist;
+    float3 forward;
+    float fov;
+    int32_t bokehSideCount;
+    float bokehRotation;
+    float tanFov2;
+    float pad;
+};
+
+struct Settings {
+    uint32_t multiSample;
+    uint32_t maxDepth;
+    uint32_t seed;
+    float rayEpsilon;
+    uint32_t rrStart;
+    uint32_t flags;
+    float maxColor;
+    uint32_t pad;
+};
+
+// Device counter words: queue lengths per bounce, then the work-fetch cursors
+// of the persistent extend and connect launches.
+constexpr uint32_t kShadowCounterBase = TR_MAX_DEPTH + 1;
+constexpr uint32_t kExtendWorkBase = 2 * (TR_MAX_DEPTH + 1);
+constexpr uint32_t kConnectWorkBase = 3 * (TR_MAX_DEPTH + 1);
+constexpr uint32_t kCounterWords = 4 * (TR_MAX_DEPTH + 1);
+
+// Path index / flag packing, Tracer/Common/CommonStructs.h:46-71.
+constexpr uint32_t kPathIxShift = 4;
+constexpr uint32_t kFlagsMask = (1u << kPathIxShift) - 1;
+constexpr uint32_t kFlagSpecular = 1u;  // BsdfFlags::Specular, Shade/BSDF/Closure.h:7-11
+TR_HD uint32_t pack_path(uint32_t pathIx, uint32_t flags) { return (pathIx << kPathIxShift) | (flags & kFlagsMask); }
+TR_HD uint32_t path_ix(uint32_t packed) { return packed >> kPathIxShift; }
+TR_HD uint32_t path_flags(uint32_t packed) { return packed & kFlagsMask; }
+
+} // namespace tr

@@ -1,0 +1,736 @@
+// Wavefront path-tracing kernels for sm_103a: generate, extend, shade,
+// connect, finalize.
+//
+// Data layout (all in HBM):
+//   path state  3 float4 planes per queue (coalesced 16-byte accesses), two
+//               queues ping-ponged by bounce parity so a launch never reads
+//               and writes the same queue (the reference compacts in place,
+//               PathTracing.h:16-18 vs :171-173);
+//   hits        one uint4 per queue slot, written and read in queue order;
+//   shadow      3 float4 planes, compacted;
+//   radiance    one float4 per path index; every contribution of a path is
+//               added here by the only thread that owns the path in that
+//               stage, so no atomics are needed and the per-pixel sum in
+//               finalize runs in a fixed sample order (the reference adds into
+//               the pixel with plain read-modify-writes from many paths,
+//               PathTracing.h:45,90 and optix.cu:340).
+// Queue appends use one warp ballot + one atomicAdd per warp.
+#include "tr_kernels.h"
+
+#include "tr_bsdf.cuh"
+#include "tr_rng.h"
+#include "tr_traverse.cuh"
+
+#include <cuda_fp16.h>
+
+namespace tr {
+
+namespace {
+
+constexpr uint32_t kFull = 0xffffffffu;
+
+__device__ __forceinline__ float h2f(uint16_t h) { return __half2float(__ushort_as_half(h)); }
+
+__device__ __forceinline__ uint32_t lane_id() { return threadIdx.x & 31u; }
+
+// Appends the lanes with pred set to a queue; one atomic per warp.
+__device__ __forceinline__ uint32_t warp_append(uint32_t* counter, bool pred)
+{
+    const uint32_t mask = __ballot_sync(kFull, pred);
+    if (mask == 0)
+        return 0;
+    const uint32_t lane = lane_id();
+    const uint32_t leader = __ffs(mask) - 1u;
+    uint32_t base = 0;
+    if (lane == leader)
+        base = atomicAdd(counter, __popc(mask));
+    base = __shfl_sync(kFull, base, leader);
+    return base + __popc(mask & ((1u << lane) - 1u));
+}
+
+// SafeColor = fixnan(clamp_scaled(c, max)), CudaUtility.h:95-99 and
+// CudaLinearMath.h:127-142.
+__device__ __forceinline__ float3 safe_color(const float3& c, float maxValue)
+{
+    float3 r = c;
+    const float m = fmaxf(c.x, fmaxf(c.y, c.z));
+    if (!(m <= maxValue))
+        r = c * (maxValue / m);
+    return isfinite(r.x + r.y + r.z) ? r : f3(0.f);
+}
+
+__device__ __forceinline__ float3 fixnan(const float3& c) { return isfinite(c.x + c.y + c.z) ? c : f3(0.f); }
+
+__device__ __forceinline__ uint32_t encode_bary(float u, float v)
+{
+    const uint32_t bx = static_cast<uint32_t>(u * 65535.f) & 0xFFFFu;
+    const uint32_t by = static_cast<uint32_t>(v * 65535.f) & 0xFFFFu;
+    return (bx << 16) | by;
+}
+
+__device__ __forceinline__ float2 decode_bary(uint32_t b)
+{
+    return make_float2(static_cast<float>(b >> 16) / 65535.f, static_cast<float>(b & 0xFFFFu) / 65535.f);
+}
+
+// PackNormal as stored by the reference (CudaUtility.h:153-160: the x and y
+// components, saturated to 16 bits); kept for the D.w payload only.
+__device__ __forceinline__ uint32_t pack_normal(const float3& n)
+{
+    return (__float2uint_rz(n.x * 65535.f) << 16) | __float2uint_rz(n.y * 65535.f);
+}
+
+// ------------------------------------------------------------------ camera
+// Two draws in argument order: left to right, or right to left when rtl.
+template <class Rng>
+__device__ __forceinline__ void draw2(Rng& rng, bool rtl, float& a, float& b)
+{
+    if (rtl) {
+        b = rng.next();
+        a = rng.next();
+    } else {
+        a = rng.next();
+        b = rng.next();
+    }
+}
+
+template <class Rng>
+__device__ __forceinline__ float2 sample_disk(Rng& rng, bool rtl)
+{
+    float ux, uy;
+    draw2(rng, rtl, ux, uy);
+    const float lx = (ux * 2.f) - 1.f;
+    const float ly = (uy * 2.f) - 1.f;
+    if (lx == 0 && ly == 0)
+        return make_float2(lx, ly);
+    float theta, r;
+    if (fabsf(lx) > fabsf(ly)) {
+        r = lx;
+        theta = kPiOver4 * (ly / lx);
+    } else {
+        r = ly;
+        theta = kPiOver2 - kPiOver4 * (lx / ly);
+    }
+    float s, c;
+    sincosf(theta, &s, &c);
+    return make_float2(r * c, r * s);
+}
+
+template <class Rng>
+__device__ __forceinline__ float2 sample_bokeh(const Camera& cam, Rng& rng, bool rtl)
+{
+    if (cam.bokehSideCount < 3)
+        return sample_disk(rng, rtl);
+    const int index = static_cast<int>(rng.next() * cam.bokehSideCount);
+    const float step = (2.f * kPi) / cam.bokehSideCount;
+    float s0, c0, s1, c1;
+    sincosf(cam.bokehRotation + (index * step), &s0, &c0);
+    sincosf(cam.bokehRotation + (index + 1) * step, &s1, &c1);
+    const float u1 = rng.next();
+    const float u2 = rng.next();
+    const float su = sqrtf(u1);
+    // SampleTriangle(c0 = 0, c1, c2), optix.cu:82-88
+    return (su * (1 - u2)) * make_float2(c0, s0) + (su * u2) * make_float2(c1, s1);
+}
+
+__device__ __forceinline__ bool distort(float2& lens, float tanFov2, float distortion)
+{
+    if (lens.x == 0 && lens.y == 0)
+        return true;
+    if (distortion <= 0)
+        return true;
+    const float scale = sqrtf(lens.x * lens.x + lens.y * lens.y);
+    const float d = (tanFov2 * distortion) * .5f;
+    const float distorted = (scale * distortion * atanf(d)) / d;
+    if (distorted >= kPiOver2)
+        return false;
+    lens = lens * (tanf(distorted) / (scale * distortion));
+    return true;
+}
+
+// GenerateCameraRay, optix.cu:142-174
+template <class Rng>
+__device__ __forceinline__ void camera_ray(const Camera& cam, uint32_t resX, uint32_t resY, uint32_t ix, uint32_t iy,
+                                           Rng& rng, bool rtl, float3& O, float3& D, float& T)
+{
+    O = cam.pos;
+    D = cam.forward;
+    T = 1.f;
+    float jx, jy;
+    draw2(rng, rtl, jx, jy);
+    const float rx = float(resX), ry = float(resY);
+    const float aspect = rx / ry;
+    float2 screen = make_float2((((float(ix) + jx) / rx) * 2.0f) - 1.f, (((float(iy) + jy) / ry) * 2.0f) - 1.f);
+    screen.y /= aspect;
+    const float2 ccd = sample_bokeh(cam, rng, rtl) * cam.aperture;
+    float2 lens = make_float2((cam.tanFov2 * screen.x) - (ccd.x / cam.focalDist),
+                              (cam.tanFov2 * screen.y) - (ccd.y / cam.focalDist));
+    if (!distort(lens, cam.tanFov2, cam.distortion))
+        return;
+    D = normalize(cam.forward + (lens.x * cam.side) + (lens.y * cam.up));
+    O = cam.pos + (cam.side * ccd.x) + (cam.up * ccd.y);
+    const float v = fmaxf(0.f, dot(D, cam.forward));
+    const float v2 = v * v;
+    T = v2 * v2;
+}
+
+// ------------------------------------------------------------------ kernels
+template <bool REF>
+__global__ void __launch_bounds__(256) generate_kernel(FrameView f, Camera cam, Settings st)
+{
+    const uint32_t pathIx = blockIdx.x * blockDim.x + threadIdx.x;
+    if (pathIx >= f.pathCount)
+        return;
+    const uint32_t wh = f.resX * f.resY;
+    const uint32_t pixelIx = pathIx % wh;
+    const uint32_t sampleIx = pathIx / wh;
+    const uint32_t sc = *f.sampleCount;
+    float3 O, D;
+    float T;
+    if (REF) {
+        RefRng rng{tea2(st.seed + pathIx, sc << 1)};
+        const bool rtl = (st.flags & TR_FLAG_REFERENCE_DRAW_RTL) != 0;
+        camera_ray(cam, f.resX, f.resY, pixelIx % f.resX, pixelIx / f.resX, rng, rtl, O, D, T);
+    } else {
+        CounterRng rng;
+        rng.init(pixelIx, sc + sampleIx, 0u, st.seed);
+        camera_ray(cam, f.resX, f.resY, pixelIx % f.resX, pixelIx / f.resX, rng, false, O, D, T);
+    }
+    const uint32_t cap = f.capacity;
+    float4* s = f.state[0];
+    s[pathIx] = f4(O, u2f(pack_path(pathIx, 0)));
+    s[pathIx + cap] = f4(D, 0.f);
+    s[pathIx + 2 * cap] = make_float4(T, T, T, 1.f);
+    f.radiance[pathIx] = make_float4(0.f, 0.f, 0.f, 0.f);
+}
+
+__device__ __forceinline__ uint32_t queue_length(const FrameView& f, uint32_t bounce)
+{
+    return bounce == 0 ? f.pathCount : __ldcg(f.counters + bounce);
+}
+
+// Sums per-thread traversal work into a device counter, one atomic per warp.
+__device__ __forceinline__ void add_counts(unsigned long long* dst, const TraversalCounts& c)
+{
+    unsigned long long n = c.nodes, t = c.tris;
+    for (int o = 16; o > 0; o >>= 1) {
+        n += __shfl_down_sync(kFull, n, o);
+        t += __shfl_down_sync(kFull, t, o);
+    }
+    if (lane_id() == 0) {
+        atomicAdd(dst, n);
+        atomicAdd(dst + 1, t);
+    }
+}
+
+// COUNT = true also sums the nodes visited and triangles tested (for the
+// traversal bytes of the roofline); it is launched outside timed regions.
+template <bool COUNT>
+__global__ void __launch_bounds__(128) extend_kernel(SceneView s, FrameView f, Settings st, uint32_t bounce)
+{
+    const uint32_t count = queue_length(f, bounce);
+    const float4* __restrict__ in = f.state[bounce & 1u];
+    const uint32_t cap = f.capacity;
+    uint32_t* work = f.counters + kExtendWorkBase + bounce;
+    const uint32_t lane = lane_id();
+    TraversalCounts cnt{0, 0};
+    while (true) {
+        uint32_t base = 0;
+        if (lane == 0)
+            base = atomicAdd(work, 32u);
+        base = __shfl_sync(kFull, base, 0);
+        if (base >= count)
+            break;
+        const uint32_t i = base + lane;
+        if (i < count) {
+            const float4 O4 = __ldcs(in + i);
+            const float4 D4 = __ldcs(in + i + cap);
+            float tmax = kDstMax;
+            uint32_t slot = 0xffffffffu;
+            float u = 0.f, v = 0.f;
+            const bool ok = traverse<false, COUNT>(s, f3(O4), f3(D4), st.rayEpsilon, tmax, slot, u, v, &cnt);
+            if (!ok)
+                atomicOr(f.errorFlag, 1u);
+            uint4 h;
+            if (slot != 0xffffffffu) {
+                const uint32_t prim = __float_as_uint(__ldg(s.bvhTris + 3u * slot).w);
+                h = make_uint4(encode_bary(u, v), 0u, prim, __float_as_uint(tmax));
+            } else {
+                h = make_uint4(0u, 0xffffffffu, 0xffffffffu, __float_as_uint(kDstMax));
+            }
+            __stcs(f.hits + i, h);
+        }
+    }
+    if (COUNT)
+        add_counts(f.traversal, cnt);
+}
+
+// Light sample, CudaLights.h:38-124.
+template <bool REF, class Rng>
+__device__ __forceinline__ float3 sample_light(const SceneView& s, Rng& rng, bool rtl, const float3& I,
+                                               const float3& N, float& prob, float& pdf, float3& radiance,
+                                               float& dist)
+{
+    const float total = REF ? s.lightEnergy : s.lightEnergyTotal;
+    if (total == 0 || s.lightCount == 0) {
+        prob = 0;
+        pdf = 0;
+        radiance = f3(0.f);
+        dist = 1e20f;
+        return make_float3(0, 1, 0);
+    }
+    int32_t lightIx;
+    float3 P;
+    if (REF) {
+        // binary search over the exclusive energy prefix (SelectLight)
+        const float e = rng.next() * s.lightEnergy;
+        int32_t low = 0, high = s.lightCount - 1;
+        lightIx = -1;
+        for (int it = 0; it < 64 && low <= high; ++it) {
+            const int32_t mid = (low + high) >> 1;
+            const float se = __ldg(&s.lights[mid].sumEnergy);
+            const float en = __ldg(&s.lights[mid].energy);
+            if (e < se) {
+                high = mid;
+            } else if (e > se + en) {
+                low = mid + 1;
+            } else {
+                lightIx = mid;
+                break;
+            }
+        }
+        if (lightIx < 0) {
+            const int c = static_cast<int>(rng.next() * s.lightCount);
+            lightIx = c < 0 ? 0 : (c > s.lightCount - 1 ? s.lightCount - 1 : c);
+        }
+        const LightTri& L = s.lights[lightIx];
+        float b0, b1, b2;
+        if (rtl) {
+            b2 = rng.next();
+            b1 = rng.next();
+            b0 = rng.next();
+        } else {
+            b0 = rng.next();
+            b1 = rng.next();
+            b2 = rng.next();
+        }
+        P = (b0 * L.V0) + (b1 * L.V1) + (b2 * L.V2);
+    } else {
+        const float u = rng.next();
+        const float coin = rng.next();
+        uint32_t k = static_cast<uint32_t>(u * float(s.lightCount));
+        k = k < uint32_t(s.lightCount) ? k : uint32_t(s.lightCount) - 1u;
+        const AliasEntry a = s.alias[k];
+        lightIx = int32_t(coin < a.prob ? k : a.alias);
+        const LightTri& L = s.lights[lightIx];
+        const float r0 = rng.next(), r1 = rng.next();
+        const float su = sqrtf(r0);
+        P = ((1.f - su) * L.V0) + ((su * (1.f - r1)) * L.V1) + ((su * r1) * L.V2);
+    }
+    const LightTri& L = s.lights[lightIx];
+    float3 Ld = I - P;
+    const float sqDist = dot(Ld, Ld);
+    Ld = normalize(Ld);
+    const float LNdotL = dot(L.N, Ld);
+    prob = L.energy / total;
+    const bool facing = REF ? (dot(N, Ld) != 0.f) : (dot(N, Ld) < 0.f);
+    pdf = (LNdotL > 0 && facing) ? sqDist / (L.area * LNdotL) : 0;
+    dist = sqrtf(sqDist);
+    radiance = L.radiance;
+    return -Ld;
+}
+
+__device__ __forceinline__ float3 xform(const float4& tx, const float4& ty, const float4& tz, const float3& v)
+{
+    return make_float3(dot(v, make_float3(tx.x, ty.x, tz.x)), dot(v, make_float3(tx.y, ty.y, tz.y)),
+                       dot(v, make_float3(tx.z, ty.z, tz.z)));
+}
+
+struct Surface {
+    float3 N;   // shading normal
+    float3 Ng;  // geometric normal
+    float3 T;   // tangent
+    float3 B;   // bitangent
+    float area;
+    uint32_t matIx;
+};
+
+// GetIntersectionAttributes + FixNormals, CudaMaterial.h:117-212
+__device__ __forceinline__ Surface surface_at(const SceneView& s, uint32_t instIx, uint32_t primIx, float2 bary,
+                                              const float3& D)
+{
+    Surface sf;
+    const TriShade& tri = s.tris[primIx];
+    sf.matIx = __ldg(s.matIdx + primIx);
+    const float3 v0 = make_float3(tri.v0x, tri.v0y, tri.v0z);
+    const float3 v1 = make_float3(tri.v1x, tri.v1y, tri.v1z);
+    const float3 v2 = make_float3(tri.v2x, tri.v2y, tri.v2z);
+    const float3 e1 = v1 - v0;
+    const float3 e2 = v2 - v0;
+    sf.area = length(cross(e1, e2)) * 0.5f;
+    const float3 N0 = make_float3(h2f(tri.N0x), h2f(tri.N0y), h2f(tri.N0z));
+    const float3 N1 = make_float3(h2f(tri.N1x), h2f(tri.N1y), h2f(tri.N1z));
+    const float3 N2 = make_float3(h2f(tri.N2x), h2f(tri.N2y), h2f(tri.N2z));
+    sf.N = normalize(N0 + ((N1 - N0) * bary.x) + ((N2 - N0) * bary.y));
+    sf.Ng = make_float3(h2f(tri.Nx), h2f(tri.Ny), h2f(tri.Nz));
+
+    // tangents from texcoord derivatives (differences taken in fp16)
+    const __half u0x = __ushort_as_half(tri.uv0x), u0y = __ushort_as_half(tri.uv0y);
+    const float s1 = __half2float(__hsub(__ushort_as_half(tri.uv1x), u0x));
+    const float t1 = __half2float(__hsub(__ushort_as_half(tri.uv1y), u0y));
+    const float s2 = __half2float(__hsub(__ushort_as_half(tri.uv2x), u0x));
+    const float t2 = __half2float(__hsub(__ushort_as_half(tri.uv2y), u0y));
+    const float r = (s1 * t2) - (s2 * t1);
+    if (fabsf(r) < 1e-6f) {
+        sf.B = normalize(cross(sf.N, e1));
+        sf.T = normalize(cross(sf.N, sf.B));
+    } else {
+        const float rr = 1.f / r;
+        const float3 tv = ((s1 * e2) - (s2 * e1)) * rr;
+        sf.B = normalize(tv - sf.N * dot(sf.N, tv));
+        sf.T = normalize(cross(sf.N, sf.B));
+    }
+    const float4 tx = __ldg(s.invTransforms + instIx * 3 + 0);
+    const float4 ty = __ldg(s.invTransforms + instIx * 3 + 1);
+    const float4 tz = __ldg(s.invTransforms + instIx * 3 + 2);
+    sf.N = normalize(xform(tx, ty, tz, sf.N));
+    sf.Ng = normalize(xform(tx, ty, tz, sf.Ng));
+    sf.B = normalize(xform(tx, ty, tz, sf.B));
+    sf.T = normalize(xform(tx, ty, tz, sf.T));
+    if (dot(D, sf.N) > 0) {
+        sf.Ng = -sf.Ng;
+        sf.N = -sf.N;
+        sf.T = -sf.T;
+        sf.B = -sf.B;
+    }
+    return sf;
+}
+
+__device__ __forceinline__ HitMat load_material(const Material* __restrict__ mats, uint32_t ix, uint32_t& closure,
+                                                uint32_t& emissiveFlag)
+{
+    const float4* p = reinterpret_cast<const float4*>(mats + ix);
+    const float4 a = __ldg(p + 0), b = __ldg(p + 1), c = __ldg(p + 2), d = __ldg(p + 3), e = __ldg(p + 4);
+    const uint4 g = __ldg(reinterpret_cast<const uint4*>(p + 5));
+    HitMat m;
+    m.diffuse = make_float3(a.x, a.y, a.z);
+    m.metallic = a.w;
+    m.emissive = make_float3(b.x, b.y, b.z);
+    m.subsurface = b.w;
+    m.tint = make_float3(c.x, c.y, c.z);
+    m.specular = c.w;
+    m.roughness = d.x;
+    m.specularTint = d.y;
+    m.anisotropic = d.z;
+    m.sheen = d.w;
+    m.sheenTint = e.x;
+    m.clearcoat = e.y;
+    m.clearcoatGloss = e.z;
+    m.luminance = e.w;
+    closure = g.x;
+    emissiveFlag = g.y;
+    return m;
+}
+
+template <bool REF, class Rng>
+__device__ __forceinline__ void shade_path(const SceneView& s, const FrameView& f, const Settings& st, uint32_t bounce,
+                                           uint32_t sc, const float4& O4, const float4& D4, const float4& T4,
+                                           const uint4& hd, Rng& rng, bool& wantExt, float4 (&ext)[3],
+                                           bool& wantShadow, float4 (&sh)[3])
+{
+    const uint32_t wh = f.resX * f.resY;
+    const float3 O = f3(O4), D = f3(D4), T = f3(T4);
+    const uint32_t data = __float_as_uint(O4.w);
+    const uint32_t pathIx = path_ix(data);
+    uint32_t flags = path_flags(data);
+    const float extendPdf = T4.w;
+    const uint32_t pixelIx = pathIx % wh;
+    const bool aov = (st.flags & TR_FLAG_WRITE_AOVS) && bounce == 0 && pathIx < wh;
+
+    const float2 bary = decode_bary(hd.x);
+    const uint32_t instIx = hd.y, primIx = hd.z;
+    const float tmax = __uint_as_float(hd.w);
+    const float3 I = O + D * tmax;
+
+    if (primIx == 0xffffffffu) {
+        // miss: the sky is disabled, SampleSky returns black (CudaSky.h:108-109)
+        if (aov) {
+            f.albedo[pixelIx] = make_float4(0.f, 0.f, 0.f, 0.f);
+            f.normals[pixelIx] = make_float4(0.f, 0.f, 0.f, 0.f);
+        }
+        return;
+    }
+
+    const Surface sf = surface_at(s, instIx, primIx, bary, D);
+    uint32_t closure, emissiveFlag;
+    const HitMat m = load_material(s.materials, sf.matIx, closure, emissiveFlag);
+    if (aov) {
+        f.albedo[pixelIx] = f4(m.diffuse, 0.f);
+        f.normals[pixelIx] = f4(sf.N, 0.f);
+    }
+
+    if (emissiveFlag) {
+        float3 contrib = f3(0.f);
+        if (bounce == 0 || (flags & kFlagSpecular)) {
+            contrib = m.emissive;
+        } else {
+            const float lightPdf = (tmax * tmax) / (fabsf(dot(D, sf.N)) * sf.area);
+            const float3 en = m.emissive * sf.area;
+            const float total = REF ? s.lightEnergy : s.lightEnergyTotal;
+            const float pick = (en.x + en.y + en.z) / total;
+            const float denom = extendPdf + lightPdf * pick;
+            if (REF) {
+                if (denom > 0)
+                    contrib = T * m.diffuse * (1.0f / denom);
+            } else {
+                if (denom > 0)
+                    contrib = T * m.emissive * (extendPdf / denom);
+            }
+        }
+        float3 add = safe_color(contrib, st.maxColor);
+        if (REF && bounce == 0)
+            add += m.emissive;  // the reference adds the primary emission a second time (PathTracing.h:93-97)
+        float4 r = f.radiance[pathIx];
+        f.radiance[pathIx] = make_float4(r.x + add.x, r.y + add.y, r.z + add.z, r.w);
+        return;
+    }
+
+    float lightProb, lightPdf, lightDist;
+    float3 lightRadiance;
+    const bool rtl = REF && (st.flags & TR_FLAG_REFERENCE_DRAW_RTL) != 0;
+    const float3 L = sample_light<REF>(s, rng, rtl, I, sf.N, lightProb, lightPdf, lightRadiance, lightDist);
+
+    const float3 wow = -D;
+    const float3 wo = normalize(make_float3(dot(wow, sf.T), dot(wow, sf.B), dot(wow, sf.N)));
+    const float3 wi = normalize(make_float3(dot(L, sf.T), dot(L, sf.B), dot(L, sf.N)));
+
+    float r0, r1;
+    draw2(rng, rtl, r0, r1);
+    ClosureResult c;
+    if (closure == TR_CLOSURE_DISNEY)
+        c = disney_closure<REF>(wo, wi, T, m, r0, r1);
+    else if (closure == TR_CLOSURE_DIFFUSE)
+        c = diffuse_closure(wo, wi, T, m, r0, r1);
+    else
+        c = lambert_closure(wo, wi, T, m, r0, r1);
+
+    if ((lightPdf > kEpsilon) && (c.shPdf > kEpsilon) && ((c.extFlags & kFlagSpecular) == 0)) {
+        const float3 shadowT = (c.shT * lightRadiance) / (lightProb * lightPdf + c.shPdf);
+        wantShadow = true;
+        sh[0] = f4(I, __uint_as_float(pathIx));
+        sh[1] = f4(L, lightDist);
+        sh[2] = f4(safe_color(shadowT, st.maxColor), 0.f);
+    }
+
+    if (c.extPdf > kEpsilon) {
+        float3 tp = c.extT / fabsf(c.extPdf);
+        if (bounce >= st.rrStart) {
+            const float rr = fminf(1.0f, fmaxf(tp.x, fmaxf(tp.y, tp.z)));
+            if (rr < rng.next())
+                return;
+            tp *= 1.f / rr;
+        }
+        const float3 nd = normalize((c.extWi.x * sf.T) + (c.extWi.y * sf.B) + (c.extWi.z * sf.N));
+        if (c.extFlags & kFlagSpecular)
+            flags |= kFlagSpecular;
+        else
+            flags &= ~kFlagSpecular;
+        wantExt = true;
+        ext[0] = f4(I, __uint_as_float(pack_path(pathIx, flags)));
+        ext[1] = f4(nd, __uint_as_float(pack_normal(sf.N)));
+        ext[2] = f4(fixnan(tp), c.extPdf);
+    }
+}
+
+template <bool REF>
+__global__ void __launch_bounds__(128) shade_kernel(SceneView s, FrameView f, Settings st, uint32_t bounce)
+{
+    const uint32_t count = queue_length(f, bounce);
+    const float4* __restrict__ in = f.state[bounce & 1u];
+    float4* __restrict__ out = f.state[(bounce + 1u) & 1u];
+    const uint32_t cap = f.capacity;
+    const uint32_t sc = *f.sampleCount;
+    const uint32_t wh = f.resX * f.resY;
+    uint32_t* extCounter = f.counters + bounce + 1u;
+    uint32_t* shCounter = f.counters + kShadowCounterBase + bounce;
+    const uint32_t lane = lane_id();
+    const uint32_t warpGlobal = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+    const uint32_t warpStride = (gridDim.x * blockDim.x) >> 5;
+
+    for (uint32_t base = warpGlobal * 32u; base < count; base += warpStride * 32u) {
+        const uint32_t i = base + lane;
+        bool wantExt = false, wantShadow = false;
+        float4 ext[3], sh[3];
+        if (i < count) {
+            const float4 O4 = __ldcs(in + i);
+            const float4 D4 = __ldcs(in + i + cap);
+            const float4 T4 = __ldcs(in + i + 2 * cap);
+            const uint4 hd = __ldcs(f.hits + i);
+            const uint32_t pathIx = path_ix(__float_as_uint(O4.w));
+            if (REF) {
+                RefRng rng{tea2(st.seed + pathIx, sc + bounce + 1u)};
+                shade_path<REF>(s, f, st, bounce, sc, O4, D4, T4, hd, rng, wantExt, ext, wantShadow, sh);
+            } else {
+                CounterRng rng;
+                rng.init(pathIx % wh, sc + pathIx / wh, bounce + 1u, st.seed);
+                shade_path<REF>(s, f, st, bounce, sc, O4, D4, T4, hd, rng, wantExt, ext, wantShadow, sh);
+            }
+        }
+        const uint32_t shSlot = warp_append(shCounter, wantShadow);
+        if (wantShadow) {
+            __stcs(f.shadow + shSlot, sh[0]);
+            __stcs(f.shadow + shSlot + cap, sh[1]);
+            __stcs(f.shadow + shSlot + 2 * cap, sh[2]);
+        }
+        const uint32_t exSlot = warp_append(extCounter, wantExt);
+        if (wantExt) {
+            __stcs(out + exSlot, ext[0]);
+            __stcs(out + exSlot + cap, ext[1]);
+            __stcs(out + exSlot + 2 * cap, ext[2]);
+        }
+    }
+}
+
+template <bool COUNT>
+__global__ void __launch_bounds__(128) connect_kernel(SceneView s, FrameView f, Settings st, uint32_t bounce)
+{
+    const uint32_t count = __ldcg(f.counters + kShadowCounterBase + bounce);
+    const uint32_t cap = f.capacity;
+    uint32_t* work = f.counters + kConnectWorkBase + bounce;
+    const uint32_t lane = lane_id();
+    TraversalCounts cnt{0, 0};
+    while (true) {
+        uint32_t base = 0;
+        if (lane == 0)
+            base = atomicAdd(work, 32u);
+        base = __shfl_sync(kFull, base, 0);
+        if (base >= count)
+            break;
+        const uint32_t i = base + lane;
+        if (i < count) {
+            const float4 O4 = __ldcs(f.shadow + i);
+            const float4 L4 = __ldcs(f.shadow + i + cap);
+            float tmax = L4.w - (2 * st.rayEpsilon);
+            uint32_t slot = 0xffffffffu;
+            float u, v;
+            const bool ok = traverse<true, COUNT>(s, f3(O4), f3(L4), st.rayEpsilon, tmax, slot, u, v, &cnt);
+            if (!ok)
+                atomicOr(f.errorFlag, 1u);
+            if (slot == 0xffffffffu) {
+                const float4 T4 = __ldcs(f.shadow + i + 2 * cap);
+                const uint32_t pathIx = __float_as_uint(O4.w);
+                float4 r = f.radiance[pathIx];
+                f.radiance[pathIx] = make_float4(r.x + T4.x, r.y + T4.y, r.z + T4.z, r.w);
+            }
+        }
+    }
+    if (COUNT)
+        add_counts(f.traversal + 2, cnt);
+}
+
+// Sums each pixel's samples in sample order into the accumulator and writes
+// colors = accumulator / sampleCount (FinalizeFrame; the film initialisation
+// of optix.cu:181-188 happens here: a frame with sampleCount == 0 overwrites).
+__global__ void __launch_bounds__(256) finalize_kernel(FrameView f, Settings st)
+{
+    const uint32_t p = blockIdx.x * blockDim.x + threadIdx.x;
+    const uint32_t wh = f.resX * f.resY;
+    if (p >= wh)
+        return;
+    const uint32_t sc = *f.sampleCount;
+    float3 sum = f3(0.f);
+    for (uint32_t k = 0; k < st.multiSample; ++k) {
+        const float4 r = f.radiance[p + k * wh];
+        sum = sum + f3(r);
+    }
+    float4 acc = sc == 0 ? make_float4(0.f, 0.f, 0.f, 0.f) : f.accumulator[p];
+    acc = make_float4(acc.x + sum.x, acc.y + sum.y, acc.z + sum.z, acc.w + float(st.multiSample));
+    f.accumulator[p] = acc;
+    const float n = float(sc + st.multiSample);
+    f.colors[p] = make_float4(acc.x / n, acc.y / n, acc.z / n, acc.w / n);
+}
+
+__global__ void advance_kernel(FrameView f, Settings st)
+{
+    if (threadIdx.x == 0 && blockIdx.x == 0)
+        *f.sampleCount += st.multiSample;
+}
+
+} // namespace
+
+// ------------------------------------------------------------------ launchers
+cudaError_t launch_generate(const FrameView& f, const Camera& cam, const Settings& st, cudaStream_t stream)
+{
+    if (f.pathCount == 0)
+        return cudaSuccess;
+    const uint32_t blocks = (f.pathCount + 255u) / 256u;
+    if (st.flags & TR_FLAG_REFERENCE_SAMPLING)
+        generate_kernel<true><<<blocks, 256, 0, stream>>>(f, cam, st);
+    else
+        generate_kernel<false><<<blocks, 256, 0, stream>>>(f, cam, st);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_extend(const SceneView& s, const FrameView& f, const Settings& st, uint32_t bounce,
+                          const LaunchShape& shape, cudaStream_t stream)
+{
+    if (st.flags & TR_FLAG_COUNT_TRAVERSAL)
+        extend_kernel<true><<<shape.extendBlocks, 128, 0, stream>>>(s, f, st, bounce);
+    else
+        extend_kernel<false><<<shape.extendBlocks, 128, 0, stream>>>(s, f, st, bounce);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_shade(const SceneView& s, const FrameView& f, const Settings& st, uint32_t bounce,
+                         const LaunchShape& shape, cudaStream_t stream)
+{
+    if (st.flags & TR_FLAG_REFERENCE_SAMPLING)
+        shade_kernel<true><<<shape.shadeBlocks, 128, 0, stream>>>(s, f, st, bounce);
+    else
+        shade_kernel<false><<<shape.shadeBlocks, 128, 0, stream>>>(s, f, st, bounce);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_connect(const SceneView& s, const FrameView& f, const Settings& st, uint32_t bounce,
+                           const LaunchShape& shape, cudaStream_t stream)
+{
+    if (st.flags & TR_FLAG_COUNT_TRAVERSAL)
+        connect_kernel<true><<<shape.connectBlocks, 128, 0, stream>>>(s, f, st, bounce);
+    else
+        connect_kernel<false><<<shape.connectBlocks, 128, 0, stream>>>(s, f, st, bounce);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_finalize(const FrameView& f, const Settings& st, cudaStream_t stream)
+{
+    const uint32_t wh = f.resX * f.resY;
+    if (wh == 0)
+        return cudaSuccess;
+    finalize_kernel<<<(wh + 255u) / 256u, 256, 0, stream>>>(f, st);
+    advance_kernel<<<1, 32, 0, stream>>>(f, st);
+    return cudaGetLastError();
+}
+
+LaunchShape default_launch_shape(int device, uint32_t capacity)
+{
+    LaunchShape shape;
+    int sms = 0;
+    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, device);
+    if (sms <= 0)
+        sms = 1;
+    int perSm = 0;
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&perSm, extend_kernel<false>, 128, 0);
+    shape.extendBlocks = uint32_t(sms) * uint32_t(perSm > 0 ? perSm : 4);
+    perSm = 0;
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&perSm, connect_kernel<false>, 128, 0);
+    shape.connectBlocks = uint32_t(sms) * uint32_t(perSm > 0 ? perSm : 4);
+    perSm = 0;
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&perSm, shade_kernel<false>, 128, 0);
+    const uint32_t maxShade = uint32_t(sms) * uint32_t(perSm > 0 ? perSm : 4) * 4u;
+    const uint32_t need = (capacity + 127u) / 128u;
+    shape.shadeBlocks = need < maxShade ? (need > 0 ? need : 1u) : maxShade;
+    shape.sms = uint32_t(sms);
+    return shape;
+}
+
+} // namespace tr

@@ -1,0 +1,31 @@
+// Host-side launchers of the wavefront kernels.
+#pragma once
+
+#include <cuda_runtime.h>
+
+#include "tr_device.h"
+
+namespace tr {
+
+// Grid sizes: extend/connect are persistent (resident blocks per SM x SMs,
+// warps fetch 32 rays at a time from a device cursor); shade is a
+// warp-strided grid capped at a few waves.
+struct LaunchShape {
+    uint32_t extendBlocks = 0;
+    uint32_t connectBlocks = 0;
+    uint32_t shadeBlocks = 0;
+    uint32_t sms = 0;
+};
+
+LaunchShape default_launch_shape(int device, uint32_t capacity);
+
+cudaError_t launch_generate(const FrameView& f, const Camera& cam, const Settings& st, cudaStream_t stream);
+cudaError_t launch_extend(const SceneView& s, const FrameView& f, const Settings& st, uint32_t bounce,
+                          const LaunchShape& shape, cudaStream_t stream);
+cudaError_t launch_shade(const SceneView& s, const FrameView& f, const Settings& st, uint32_t bounce,
+                         const LaunchShape& shape, cudaStream_t stream);
+cudaError_t launch_connect(const SceneView& s, const FrameView& f, const Settings& st, uint32_t bounce,
+                           const LaunchShape& shape, cudaStream_t stream);
+cudaError_t launch_finalize(const FrameView& f, const Settings& st, cudaStream_t stream);
+
+} // namespace tr

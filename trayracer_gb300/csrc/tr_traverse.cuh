@@ -1,0 +1,298 @@
+// Closest-hit and any-hit traversal of the 8-wide compressed BVH (CWBVH).
+//
+// Replaces optixTrace (Tracer/Optix/GPU/optix.cu:264,308,333) with a software
+// traversal following Ylitie, Karras and Laine (HPG 2017): node groups on a
+// short stack, octant-ordered child slots, 8-bit quantized child boxes decoded
+// against the ray with one FMA per slab, leaf triangles visited as a bit mask.
+// Node words are fetched as 128-bit read-only loads.
+//
+// OptiX semantics kept: no face culling (Tracer/Resources/Model.cpp:270),
+// closest hit over [tmin, tmax], any-hit termination for shadow rays
+// (OPTIX_RAY_FLAG_TERMINATE_ON_FIRST_HIT, optix.cu:333-335).
+//
+// The triangle test is Moller-Trumbore on (v0, e1 = v1 - v0, e2 = v2 - v0)
+// written with explicit round-to-nearest operations (no contraction choice
+// left to the compiler), so the oracle's host copy of the same sequence gives
+// bit-identical t, u, v.
+#pragma once
+
+#include <cmath>
+
+#include "tr_device.h"
+
+namespace tr {
+
+// Round-to-nearest arithmetic and bit operations with one meaning on the
+// device and on the host (the host copy is built with -ffp-contract=off).
+TR_HD float fma_rn(float a, float b, float c)
+{
+#if defined(__CUDA_ARCH__)
+    return __fmaf_rn(a, b, c);
+#else
+    return std::fma(a, b, c);
+#endif
+}
+TR_HD float mul_rn(float a, float b)
+{
+#if defined(__CUDA_ARCH__)
+    return __fmul_rn(a, b);
+#else
+    return a * b;
+#endif
+}
+TR_HD float add_rn(float a, float b)
+{
+#if defined(__CUDA_ARCH__)
+    return __fadd_rn(a, b);
+#else
+    return a + b;
+#endif
+}
+TR_HD float sub_rn(float a, float b)
+{
+#if defined(__CUDA_ARCH__)
+    return __fsub_rn(a, b);
+#else
+    return a - b;
+#endif
+}
+TR_HD float rcp_rn(float a)
+{
+#if defined(__CUDA_ARCH__)
+    return __frcp_rn(a);
+#else
+    return 1.0f / a;
+#endif
+}
+TR_HD uint32_t clz32(uint32_t x)
+{
+#if defined(__CUDA_ARCH__)
+    return uint32_t(__clz(x));
+#else
+    return x ? uint32_t(__builtin_clz(x)) : 32u;
+#endif
+}
+TR_HD uint32_t popc32(uint32_t x)
+{
+#if defined(__CUDA_ARCH__)
+    return uint32_t(__popc(x));
+#else
+    return uint32_t(__builtin_popcount(x));
+#endif
+}
+TR_HD uint32_t ffs32(uint32_t x)
+{
+#if defined(__CUDA_ARCH__)
+    return uint32_t(__ffs(x));
+#else
+    return uint32_t(__builtin_ffs(int(x)));
+#endif
+}
+template <class T> TR_HD T ldg(const T* p)
+{
+#if defined(__CUDA_ARCH__)
+    return __ldg(p);
+#else
+    return *p;
+#endif
+}
+
+// Traversal work of one ray (counting variant only).
+struct TraversalCounts {
+    uint32_t nodes;
+    uint32_t tris;
+};
+
+constexpr int kTraversalStack = 32;
+constexpr uint32_t kMaxTraversalSteps = 1u << 22;  // bound on node + leaf visits of one ray
+
+struct TriHit {
+    float t;
+    float u;
+    float v;
+    uint32_t slot;
+};
+
+TR_HD bool intersect_triangle(const float3& O, const float3& D, const float4& a, const float4& b,
+                                                   const float4& c, float tmin, float tmax, float& t, float& u, float& v)
+{
+    // pvec = D x e2
+    const float px = fma_rn(D.y, c.z, -mul_rn(D.z, c.y));
+    const float py = fma_rn(D.z, c.x, -mul_rn(D.x, c.z));
+    const float pz = fma_rn(D.x, c.y, -mul_rn(D.y, c.x));
+    const float det = fma_rn(b.x, px, fma_rn(b.y, py, mul_rn(b.z, pz)));
+    if (det == 0.0f)
+        return false;
+    const float inv = rcp_rn(det);
+    const float tx = sub_rn(O.x, a.x);
+    const float ty = sub_rn(O.y, a.y);
+    const float tz = sub_rn(O.z, a.z);
+    const float uu = mul_rn(fma_rn(tx, px, fma_rn(ty, py, mul_rn(tz, pz))), inv);
+    if (!(uu >= 0.0f && uu <= 1.0f))
+        return false;
+    // qvec = tvec x e1
+    const float qx = fma_rn(ty, b.z, -mul_rn(tz, b.y));
+    const float qy = fma_rn(tz, b.x, -mul_rn(tx, b.z));
+    const float qz = fma_rn(tx, b.y, -mul_rn(ty, b.x));
+    const float vv = mul_rn(fma_rn(D.x, qx, fma_rn(D.y, qy, mul_rn(D.z, qz))), inv);
+    if (!(vv >= 0.0f && add_rn(uu, vv) <= 1.0f))
+        return false;
+    const float tt = mul_rn(fma_rn(c.x, qx, fma_rn(c.y, qy, mul_rn(c.z, qz))), inv);
+    if (!(tt >= tmin && tt <= tmax))
+        return false;
+    t = tt;
+    u = uu;
+    v = vv;
+    return true;
+}
+
+TR_HD float byte_to_float(uint32_t w, int i) { return float((w >> (8 * i)) & 0xffu); }
+
+// Intersects the 8 children of a node; returns the hit mask: bits 24..31 for
+// internal children (position 24 + (slot ^ (7 - octant))), bits 0..23 for
+// leaf triangles (offset from the node's triangle base).
+TR_HD uint32_t intersect_node(const CwbvhNode* __restrict__ nodes, uint32_t nodeIx,
+                                                   const float3& O, const float3& invD, uint32_t octInv, float tmin,
+                                                   float tmax, uint32_t& childBase, uint32_t& triBase,
+                                                   uint32_t& imask)
+{
+    const uint4* nw = reinterpret_cast<const uint4*>(nodes + nodeIx);
+    const uint4 w0 = ldg(nw + 0);
+    const uint4 w1 = ldg(nw + 1);
+    const uint4 w2 = ldg(nw + 2);
+    const uint4 w3 = ldg(nw + 3);
+    const uint4 w4 = ldg(nw + 4);
+
+    const float px = u2f(w0.x), py = u2f(w0.y), pz = u2f(w0.z);
+    const float sx = u2f((w0.w & 0xffu) << 23);
+    const float sy = u2f(((w0.w >> 8) & 0xffu) << 23);
+    const float sz = u2f(((w0.w >> 16) & 0xffu) << 23);
+    imask = w0.w >> 24;
+    childBase = w1.x;
+    triBase = w1.y;
+
+    const float ax = sx * invD.x, ay = sy * invD.y, az = sz * invD.z;
+    const float bx = (px - O.x) * invD.x, by = (py - O.y) * invD.y, bz = (pz - O.z) * invD.z;
+
+    // octant swizzle: the near plane is qhi on axes the ray walks backwards
+    const bool nx = invD.x < 0.f, ny = invD.y < 0.f, nz = invD.z < 0.f;
+    const uint32_t loX0 = nx ? w3.z : w2.x, loX1 = nx ? w3.w : w2.y;
+    const uint32_t hiX0 = nx ? w2.x : w3.z, hiX1 = nx ? w2.y : w3.w;
+    const uint32_t loY0 = ny ? w4.x : w2.z, loY1 = ny ? w4.y : w2.w;
+    const uint32_t hiY0 = ny ? w2.z : w4.x, hiY1 = ny ? w2.w : w4.y;
+    const uint32_t loZ0 = nz ? w4.z : w3.x, loZ1 = nz ? w4.w : w3.y;
+    const uint32_t hiZ0 = nz ? w3.x : w4.z, hiZ1 = nz ? w3.y : w4.w;
+
+    uint32_t hitmask = 0;
+#pragma unroll
+    for (int half = 0; half < 2; ++half) {
+        const uint32_t meta4 = half == 0 ? w1.z : w1.w;
+        const uint32_t lx = half == 0 ? loX0 : loX1, hx = half == 0 ? hiX0 : hiX1;
+        const uint32_t ly = half == 0 ? loY0 : loY1, hy = half == 0 ? hiY0 : hiY1;
+        const uint32_t lz = half == 0 ? loZ0 : loZ1, hz = half == 0 ? hiZ0 : hiZ1;
+#pragma unroll
+        for (int j = 0; j < 4; ++j) {
+            const uint32_t meta = (meta4 >> (8 * j)) & 0xffu;
+            if (meta == 0)
+                continue;
+            const float t0x = fma_rn(byte_to_float(lx, j), ax, bx);
+            const float t1x = fma_rn(byte_to_float(hx, j), ax, bx);
+            const float t0y = fma_rn(byte_to_float(ly, j), ay, by);
+            const float t1y = fma_rn(byte_to_float(hy, j), ay, by);
+            const float t0z = fma_rn(byte_to_float(lz, j), az, bz);
+            const float t1z = fma_rn(byte_to_float(hz, j), az, bz);
+            const float tn = fmaxf(fmaxf(t0x, t0y), fmaxf(t0z, tmin));
+            const float tf = fminf(fminf(t1x, t1y), fminf(t1z, tmax));
+            if (tn <= tf * 1.0000004f) {
+                uint32_t bit = meta & 0x1fu;
+                if (bit >= 24u)
+                    bit = 24u + ((bit - 24u) ^ octInv);
+                hitmask |= (meta >> 5) << bit;
+            }
+        }
+    }
+    return hitmask;
+}
+
+// Traverses the CWBVH. ANY = true stops at the first hit inside [tmin, tmax].
+// Returns false when a bound (stack depth, step count) was exceeded; the hit
+// reported so far is kept. COUNT adds the nodes and triangles visited to *cnt.
+template <bool ANY, bool COUNT = false>
+TR_HD bool traverse(const SceneView& s, const float3& O, const float3& D, float tmin, float& tmax, uint32_t& hitSlot,
+                    float& hu, float& hv, TraversalCounts* cnt = nullptr)
+{
+    const float kTiny = 1e-20f;
+    const float3 invD = make_float3(1.0f / (fabsf(D.x) > kTiny ? D.x : copysignf(kTiny, D.x)),
+                                    1.0f / (fabsf(D.y) > kTiny ? D.y : copysignf(kTiny, D.y)),
+                                    1.0f / (fabsf(D.z) > kTiny ? D.z : copysignf(kTiny, D.z)));
+    const uint32_t octant = (invD.x < 0.f ? 1u : 0u) | (invD.y < 0.f ? 2u : 0u) | (invD.z < 0.f ? 4u : 0u);
+    const uint32_t octInv = 7u - octant;
+
+    uint2 stack[kTraversalStack];
+    int sp = 0;
+    uint2 group = make_uint2(0u, 0x80000000u);  // the root as the only internal child of a virtual parent
+    uint32_t steps = 0;
+    bool ok = true;
+
+    while (true) {
+        uint2 tris = make_uint2(0u, 0u);
+        if (group.y > 0x00ffffffu) {
+            const uint32_t hits = group.y;
+            const uint32_t bit = 31u - clz32(hits);
+            group.y &= ~(1u << bit);
+            const uint32_t slot = (bit - 24u) ^ octInv;
+            const uint32_t rel = popc32(hits & 0xffu & ((1u << slot) - 1u));
+            const uint32_t nodeIx = group.x + rel;
+            if (group.y > 0x00ffffffu) {
+                if (sp < kTraversalStack) {
+                    stack[sp++] = group;
+                } else {
+                    ok = false;
+                }
+            }
+            uint32_t childBase, triBase, imask;
+            const uint32_t hm = intersect_node(s.nodes, nodeIx, O, invD, octInv, tmin, tmax, childBase, triBase, imask);
+            if (COUNT)
+                cnt->nodes++;
+            group = make_uint2(childBase, (hm & 0xff000000u) | imask);
+            tris = make_uint2(triBase, hm & 0x00ffffffu);
+            if (++steps > kMaxTraversalSteps) {
+                ok = false;
+                break;
+            }
+        }
+        while (tris.y != 0u) {
+            const uint32_t t = ffs32(tris.y) - 1u;
+            tris.y &= tris.y - 1u;
+            const uint32_t slot = tris.x + t;
+            const float4* tp = s.bvhTris + 3u * slot;
+            const float4 a = ldg(tp + 0);
+            const float4 b = ldg(tp + 1);
+            const float4 c = ldg(tp + 2);
+            if (COUNT)
+                cnt->tris++;
+            float tt, uu, vv;
+            if (intersect_triangle(O, D, a, b, c, tmin, tmax, tt, uu, vv)) {
+                if (ANY) {
+                    tmax = tt;
+                    hitSlot = slot;
+                    return ok;
+                }
+                if (tt < tmax || hitSlot == 0xffffffffu) {
+                    tmax = tt;
+                    hitSlot = slot;
+                    hu = uu;
+                    hv = vv;
+                }
+            }
+        }
+        if (group.y <= 0x00ffffffu) {
+            if (sp == 0)
+                break;
+            group = stack[--sp];
+        }
+    }
+    return ok;
+}
+
+} // namespace tr

@@ -1,0 +1,274 @@
+"""Host-side mirror of the reference renderer's per-stage interface over the C ABI.
+
+``DeviceRenderer`` follows Tracer::DeviceRenderer (Tracer/Renderer/DeviceRenderer.h:21-67):
+RenderFrame(kernelSettings, renderMode, renderFlags), Reset, SetCamera, Resize,
+Statistics, SampleCount, Resolution, Accumulator/ColorBuffer; ``UpdateScene``
+follows Renderer::UpdateScene (Tracer/Renderer/Renderer.h:49). Where the
+reference calls FatalError -> exit (Tracer/CUDA/CudaError.cpp:13-25) these
+methods raise ``TracerError`` with the C status.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import enum
+from dataclasses import dataclass
+
+import numpy as np
+
+from . import _abi
+from ._abi import TR_FLAG_REFERENCE_SAMPLING, TR_FLAG_WRITE_AOVS  # noqa: F401
+from .scenes import MATERIAL_DTYPE, CameraSpec, Scene
+
+
+class TracerError(RuntimeError):
+    def __init__(self, status: int, where: str, detail: str = ""):
+        self.status = status
+        super().__init__(f"{where}: {_abi.STATUS.get(status, status)}{': ' + detail if detail else ''}")
+
+
+class RenderModes(enum.IntEnum):
+    """Tracer/Common/CommonStructs.h:110-125; only PathTracing is the hot path."""
+
+    AmbientOcclusion = 0
+    AmbientOcclusionShading = 1
+    Bitangent = 2
+    GeometricNormal = 3
+    MaterialID = 4
+    MaterialProperty = 5
+    ObjectID = 6
+    PathTracing = 7
+    ShadingNormal = 8
+    Tangent = 9
+    TextureCoordinate = 10
+    Wireframe = 11
+    ZDepth = 12
+
+
+@dataclass
+class KernelSettings:
+    """KernelSettings (Tracer/Common/CommonStructs.h:145-153) plus the knobs the reference hard-wires.
+
+    Defaults follow Renderer::DefaultSettings (Tracer/Renderer/Renderer.cpp:255-266)."""
+
+    multiSample: int = 1
+    maxDepth: int = 16
+    seed: int = 0
+    aoDist: float = 1.0
+    zDepthMax: float = 1.0
+    rayEpsilon: float = 1e-3
+    rrStart: int = 1           # PathTracing.h:149 (pathLength > 0)
+    flags: int = 0
+    maxColor: float = 10.0     # gMaxColorIntensity, CudaUtility.h:91
+
+    def to_c(self) -> _abi.KernelSettings:
+        return _abi.KernelSettings(self.multiSample, self.maxDepth, self.seed & 0xFFFFFFFF, self.rayEpsilon,
+                                   min(self.rrStart, 0xFFFFFFFF), self.flags, self.maxColor, 0)
+
+
+def camera_to_c(cam: CameraSpec) -> _abi.Camera:
+    side, up, fwd = cam.basis()
+    c = _abi.Camera()
+    c.position[:] = [float(x) for x in np.asarray(cam.position, np.float32)]
+    c.side[:] = [float(x) for x in side]
+    c.up[:] = [float(x) for x in up]
+    c.forward[:] = [float(x) for x in fwd]
+    c.aperture = cam.aperture
+    c.distortion = cam.distortion
+    c.focal_dist = cam.focal_dist
+    c.fov = cam.fov
+    c.bokeh_side_count = cam.bokeh_side_count
+    c.bokeh_rotation = cam.bokeh_rotation
+    return c
+
+
+class SceneDescHolder:
+    """Keeps the numpy arrays of a Scene alive while the C structs point at them."""
+
+    def __init__(self, scene: Scene, leaf_size: int = 0, build_threads: int = 0):
+        self.scene = scene
+        self.pos = np.ascontiguousarray(scene.positions, np.float32)
+        self.nrm = None if scene.normals is None else np.ascontiguousarray(scene.normals, np.float32)
+        self.uv = None if scene.texcoords is None else np.ascontiguousarray(scene.texcoords, np.float32)
+        self.idx = np.ascontiguousarray(scene.indices, np.uint32)
+        self.mat = np.ascontiguousarray(scene.material_indices, np.uint32)
+        self.mats = np.ascontiguousarray(scene.materials, MATERIAL_DTYPE)
+        self.mesh = _abi.MeshDesc(
+            self.pos.ctypes.data,
+            None if self.nrm is None else self.nrm.ctypes.data,
+            None if self.uv is None else self.uv.ctypes.data,
+            self.pos.shape[0],
+            self.idx.shape[0],
+            self.idx.ctypes.data,
+            self.mat.ctypes.data,
+        )
+        self.desc = _abi.SceneDesc(C.pointer(self.mesh), C.cast(self.mats.ctypes.data, C.POINTER(_abi.MaterialDesc)),
+                                   self.mats.shape[0], leaf_size, build_threads, 0)
+
+    def ptr(self):
+        return C.byref(self.desc)
+
+
+class DeviceRenderer:
+    def __init__(self, device: int = 0):
+        self._lib = _abi.load_library()
+        self._ctx = C.c_void_p()
+        cfg = _abi.Config(device, _abi.TR_ABI_VERSION)
+        st = self._lib.tr_create(C.byref(cfg), C.byref(self._ctx))
+        if st != 0:
+            raise TracerError(st, "tr_create")
+        self._scene_holder = None
+        self._settings = KernelSettings()
+        self._resolution = (0, 0)
+
+    # ------------------------------------------------------------------ plumbing
+    def _check(self, st: int, where: str):
+        if st != 0:
+            detail = self._lib.tr_last_error(self._ctx).decode(errors="replace") if self._ctx else ""
+            raise TracerError(st, where, detail)
+
+    def close(self):
+        if self._ctx:
+            self._lib.tr_destroy(self._ctx)
+            self._ctx = C.c_void_p()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *exc):
+        self.close()
+
+    @property
+    def handle(self):
+        return self._ctx
+
+    # ------------------------------------------------------------------ scene / camera / settings
+    def UpdateScene(self, scene: Scene, leaf_size: int = 0, build_threads: int = 0):
+        holder = SceneDescHolder(scene, leaf_size, build_threads)
+        self._check(self._lib.tr_scene_upload(self._ctx, holder.ptr()), "tr_scene_upload")
+        self._scene_holder = holder
+
+    def SceneInfo(self) -> dict:
+        info = _abi.SceneInfo()
+        self._check(self._lib.tr_get_scene_info(self._ctx, C.byref(info)), "tr_get_scene_info")
+        return {f: (list(getattr(info, f)) if f == "scene_bounds" else getattr(info, f)) for f, _ in info._fields_}
+
+    def SetCamera(self, cam: CameraSpec):
+        self._check(self._lib.tr_set_camera(self._ctx, C.byref(camera_to_c(cam))), "tr_set_camera")
+
+    def SetSettings(self, settings: KernelSettings):
+        self._check(self._lib.tr_set_settings(self._ctx, C.byref(settings.to_c())), "tr_set_settings")
+        self._settings = settings
+
+    def Resize(self, resolution):
+        w, h = resolution
+        self._check(self._lib.tr_resize(self._ctx, int(w), int(h)), "tr_resize")
+        self._resolution = (int(w), int(h))
+
+    def Reset(self):
+        self._check(self._lib.tr_reset(self._ctx), "tr_reset")
+
+    # ------------------------------------------------------------------ rendering
+    def RenderFrame(self, kernelSettings: KernelSettings | None = None,
+                    renderMode: RenderModes = RenderModes.PathTracing, renderFlags: int = 0, stream: int = 0,
+                    use_graph: bool = False):
+        if renderMode != RenderModes.PathTracing:
+            raise TracerError(1, "RenderFrame", f"render mode {renderMode.name} is not part of this hot path")
+        if kernelSettings is not None:
+            self.SetSettings(kernelSettings)
+        self._check(self._lib.tr_render_frame(self._ctx, C.c_void_p(stream or None), int(use_graph)),
+                    "tr_render_frame")
+
+    def BeginFrame(self, stream: int = 0):
+        self._check(self._lib.tr_begin_frame(self._ctx, C.c_void_p(stream or None)), "tr_begin_frame")
+
+    def Generate(self, stream: int = 0):
+        self._check(self._lib.tr_generate(self._ctx, C.c_void_p(stream or None)), "tr_generate")
+
+    def Extend(self, bounce: int, stream: int = 0):
+        self._check(self._lib.tr_extend(self._ctx, C.c_void_p(stream or None), bounce), "tr_extend")
+
+    def Shade(self, bounce: int, stream: int = 0):
+        self._check(self._lib.tr_shade(self._ctx, C.c_void_p(stream or None), bounce), "tr_shade")
+
+    def Connect(self, bounce: int, stream: int = 0):
+        self._check(self._lib.tr_connect(self._ctx, C.c_void_p(stream or None), bounce), "tr_connect")
+
+    def Finalize(self, stream: int = 0):
+        self._check(self._lib.tr_finalize(self._ctx, C.c_void_p(stream or None)), "tr_finalize")
+
+    def Synchronize(self, stream: int = 0):
+        self._check(self._lib.tr_synchronize(self._ctx, C.c_void_p(stream or None)), "tr_synchronize")
+
+    # ------------------------------------------------------------------ results
+    def Statistics(self) -> dict:
+        s = _abi.Statistics()
+        self._check(self._lib.tr_get_statistics(self._ctx, C.byref(s)), "tr_get_statistics")
+        out = {}
+        for f, _ in s._fields_:
+            v = getattr(s, f)
+            out[f] = list(v) if f in ("extend_rays", "shadow_rays") else v
+        return out
+
+    def SampleCount(self) -> int:
+        return int(self.Statistics()["sample_count"])
+
+    def Resolution(self):
+        return self._resolution
+
+    def Buffers(self) -> dict:
+        b = _abi.Buffers()
+        self._check(self._lib.tr_get_buffers(self._ctx, C.byref(b)), "tr_get_buffers")
+        return {
+            "path_state": [b.path_state[0], b.path_state[1]],
+            "hits": b.hits,
+            "shadow": b.shadow,
+            "radiance": b.radiance,
+            "accumulator": b.accumulator,
+            "albedo": b.albedo,
+            "normals": b.normals,
+            "colors": b.colors,
+            "counters": b.counters,
+            "capacity": b.capacity,
+            "width": b.width,
+            "height": b.height,
+        }
+
+    def ColorBuffer(self, out: np.ndarray | None = None, stream: int = 0) -> np.ndarray:
+        w, h = self._resolution
+        if out is None:
+            out = np.empty((h, w, 4), np.float32)
+        self._check(self._lib.tr_download_image(self._ctx, C.c_void_p(stream or None), out.ctypes.data, out.nbytes),
+                    "tr_download_image")
+        return out
+
+    def Accumulator(self) -> np.ndarray:
+        w, h = self._resolution
+        out = np.empty((h, w, 4), np.float32)
+        self._check(self._lib.tr_download_accumulator(self._ctx, None, out.ctypes.data, out.nbytes),
+                    "tr_download_accumulator")
+        return out
+
+    def read_device(self, ptr: int, dtype, count: int) -> np.ndarray:
+        out = np.empty(count, dtype)
+        self._check(self._lib.tr_copy_from_device(self._ctx, out.ctypes.data, C.c_void_p(ptr), out.nbytes),
+                    "tr_copy_from_device")
+        return out
+
+    def write_device(self, ptr: int, arr: np.ndarray):
+        a = np.ascontiguousarray(arr)
+        self._check(self._lib.tr_copy_to_device(self._ctx, C.c_void_p(ptr), a.ctypes.data, a.nbytes),
+                    "tr_copy_to_device")
+
+
+def settings_for(scene: Scene, multi_sample: int = 1, reference: bool = False, seed: int | None = None,
+                 aovs: bool = False) -> KernelSettings:
+    flags = (TR_FLAG_REFERENCE_SAMPLING if reference else 0) | (TR_FLAG_WRITE_AOVS if aovs else 0)
+    return KernelSettings(multiSample=multi_sample, maxDepth=scene.max_depth,
+                          seed=scene.seed if seed is None else seed, rrStart=1 if reference else scene.rr_start,
+                          flags=flags)

@@ -1,0 +1,314 @@
+"""Seeded procedural scenes for the benchmark configurations.
+
+The reference's own scenes (Resources/scenes/*.json) point at model files of a
+submodule that is not part of the reference tree, so these synthetic scenes
+stand in for them. Only +, -, *, / and sqrt are used so the arrays are
+bit-identical on every platform numpy runs on.
+"""
+from __future__ import annotations
+
+import hashlib
+from dataclasses import dataclass, field
+
+import numpy as np
+
+from ._abi import TR_CLOSURE_DIFFUSE, TR_CLOSURE_DISNEY, TR_CLOSURE_LAMBERT
+
+MATERIAL_DTYPE = np.dtype(
+    [
+        ("diffuse", "<f4", (3,)),
+        ("emissive", "<f4", (3,)),
+        ("metallic", "<f4"),
+        ("subsurface", "<f4"),
+        ("specular", "<f4"),
+        ("roughness", "<f4"),
+        ("specular_tint", "<f4"),
+        ("anisotropic", "<f4"),
+        ("sheen", "<f4"),
+        ("sheen_tint", "<f4"),
+        ("clearcoat", "<f4"),
+        ("clearcoat_gloss", "<f4"),
+        ("closure", "<u4"),
+    ]
+)
+assert MATERIAL_DTYPE.itemsize == 68
+
+
+def material(diffuse=(1.0, 1.0, 1.0), emissive=(0.0, 0.0, 0.0), closure=TR_CLOSURE_DIFFUSE, metallic=0.0,
+             subsurface=0.0, specular=0.0, roughness=1.0, specular_tint=0.0, anisotropic=0.0, sheen=0.0,
+             sheen_tint=0.0, clearcoat=0.0, clearcoat_gloss=0.0):
+    """One material record; defaults follow Material::Material (Tracer/Resources/Material.cpp:102-114)."""
+    m = np.zeros((), MATERIAL_DTYPE)
+    m["diffuse"] = diffuse
+    m["emissive"] = emissive
+    m["metallic"] = metallic
+    m["subsurface"] = subsurface
+    m["specular"] = specular
+    m["roughness"] = roughness
+    m["specular_tint"] = specular_tint
+    m["anisotropic"] = anisotropic
+    m["sheen"] = sheen
+    m["sheen_tint"] = sheen_tint
+    m["clearcoat"] = clearcoat
+    m["clearcoat_gloss"] = clearcoat_gloss
+    m["closure"] = closure
+    return m
+
+
+@dataclass
+class CameraSpec:
+    """CameraNode (Tracer/Resources/CameraNode.h): position, target, up, fov in radians."""
+
+    position: tuple = (0.0, 0.0, -1.0)
+    target: tuple = (0.0, 0.0, 0.0)
+    up: tuple = (0.0, 1.0, 0.0)
+    fov: float = float(np.float32(90.0 * np.pi / 180.0))
+    aperture: float = 0.0
+    distortion: float = 0.0
+    focal_dist: float = 1e5
+    bokeh_side_count: int = 0
+    bokeh_rotation: float = 0.0
+
+    def basis(self):
+        """CameraNode::Transform (Tracer/Resources/CameraNode.cpp:49-63): side, up, forward."""
+        f32 = np.float32
+
+        def nrm(v):
+            return (v * (f32(1.0) / np.sqrt((v[0] * v[0] + v[1] * v[1]) + v[2] * v[2]))).astype(np.float32)
+
+        pos = np.asarray(self.position, np.float32)
+        tgt = np.asarray(self.target, np.float32)
+        up = np.asarray(self.up, np.float32)
+        fwd = nrm(tgt - pos)
+        side = nrm(np.cross(fwd, up).astype(np.float32))
+        up2 = nrm(np.cross(side, fwd).astype(np.float32))
+        return side, up2, fwd
+
+
+@dataclass
+class Scene:
+    name: str
+    positions: np.ndarray            # (V, 3) float32
+    normals: np.ndarray | None       # (V, 3) float32
+    texcoords: np.ndarray | None     # (V, 2) float32
+    indices: np.ndarray              # (T, 3) uint32
+    material_indices: np.ndarray     # (T,) uint32
+    materials: np.ndarray            # (M,) MATERIAL_DTYPE
+    camera: CameraSpec = field(default_factory=CameraSpec)
+    width: int = 256
+    height: int = 256
+    spp: int = 16
+    max_depth: int = 5
+    rr_start: int = 1 << 30
+    seed: int = 1
+
+    @property
+    def triangle_count(self) -> int:
+        return int(self.indices.shape[0])
+
+    def digest(self) -> str:
+        h = hashlib.sha256()
+        for a in (self.positions, self.normals, self.texcoords, self.indices, self.material_indices, self.materials):
+            if a is not None:
+                h.update(np.ascontiguousarray(a).tobytes())
+        return h.hexdigest()[:16]
+
+
+class _Builder:
+    def __init__(self):
+        self.pos, self.nrm, self.uv, self.idx, self.mat = [], [], [], [], []
+        self.count = 0
+
+    def quad(self, corners, normal, mat):
+        c = np.asarray(corners, np.float32)
+        base = self.count
+        self.pos.append(c)
+        self.nrm.append(np.tile(np.asarray(normal, np.float32), (4, 1)))
+        self.uv.append(np.array([[0, 0], [1, 0], [1, 1], [0, 1]], np.float32))
+        self.idx.append(np.array([[base, base + 1, base + 2], [base, base + 2, base + 3]], np.uint32))
+        self.mat.append(np.array([mat, mat], np.uint32))
+        self.count += 4
+
+    def box(self, center, size, angle_cos, angle_sin, mat):
+        """Axis box rotated about y (cos, sin given exactly)."""
+        cx, cy, cz = center
+        hx, hy, hz = (s * 0.5 for s in size)
+        c, s = np.float32(angle_cos), np.float32(angle_sin)
+
+        def p(x, y, z):
+            return (cx + c * x + s * z, cy + y, cz - s * x + c * z)
+
+        def n(x, y, z):
+            return (c * x + s * z, y, -s * x + c * z)
+
+        faces = [
+            ([p(-hx, -hy, -hz), p(hx, -hy, -hz), p(hx, hy, -hz), p(-hx, hy, -hz)], n(0, 0, -1)),
+            ([p(hx, -hy, hz), p(-hx, -hy, hz), p(-hx, hy, hz), p(hx, hy, hz)], n(0, 0, 1)),
+            ([p(-hx, -hy, hz), p(-hx, -hy, -hz), p(-hx, hy, -hz), p(-hx, hy, hz)], n(-1, 0, 0)),
+            ([p(hx, -hy, -hz), p(hx, -hy, hz), p(hx, hy, hz), p(hx, hy, -hz)], n(1, 0, 0)),
+            ([p(-hx, hy, -hz), p(hx, hy, -hz), p(hx, hy, hz), p(-hx, hy, hz)], n(0, 1, 0)),
+            ([p(-hx, -hy, hz), p(hx, -hy, hz), p(hx, -hy, -hz), p(-hx, -hy, -hz)], n(0, -1, 0)),
+        ]
+        for corners, normal in faces:
+            self.quad(corners, normal, mat)
+
+    def arrays(self):
+        return (np.concatenate(self.pos).astype(np.float32), np.concatenate(self.nrm).astype(np.float32),
+                np.concatenate(self.uv).astype(np.float32), np.concatenate(self.idx).astype(np.uint32),
+                np.concatenate(self.mat).astype(np.uint32))
+
+
+def cornell_box(seed: int = 1, width: int = 256, height: int = 256, spp: int = 16, max_depth: int = 5,
+                wall_closure: int = TR_CLOSURE_DIFFUSE) -> Scene:
+    """Closed box: 5 axis-aligned quad walls (10 tris), 2 rotated boxes (24 tris), 1 quad light (2 tris,
+    radiance 15). Walls Lambertian with albedo U[0.2, 0.8]^3, the tall box a GGX conductor (Disney,
+    metallic 1, roughness 0.3), the short box Lambertian. Camera: the reference's default camera
+    (Apps/Demo/App.cpp:27), at (0, 0, -1) looking at the origin, fov 90 degrees. With
+    wall_closure = TR_CLOSURE_LAMBERT every material uses the reference's live Lambert closure."""
+    rng = np.random.default_rng(seed)
+    b = _Builder()
+    mats = []
+    walls = [
+        ([(-1, -1, -1), (1, -1, -1), (1, -1, 1), (-1, -1, 1)], (0, 1, 0)),   # floor
+        ([(-1, 1, 1), (1, 1, 1), (1, 1, -1), (-1, 1, -1)], (0, -1, 0)),     # ceiling
+        ([(-1, -1, 1), (1, -1, 1), (1, 1, 1), (-1, 1, 1)], (0, 0, -1)),     # back
+        ([(-1, -1, -1), (-1, -1, 1), (-1, 1, 1), (-1, 1, -1)], (1, 0, 0)),  # left
+        ([(1, -1, 1), (1, -1, -1), (1, 1, -1), (1, 1, 1)], (-1, 0, 0)),     # right
+    ]
+    for corners, normal in walls:
+        albedo = rng.uniform(0.2, 0.8, 3).astype(np.float32)
+        mats.append(material(diffuse=albedo, closure=wall_closure))
+        b.quad(corners, normal, len(mats) - 1)
+    # short Lambertian box, rotated by -0.3 rad about y (cos, sin rounded to float32)
+    mats.append(material(diffuse=rng.uniform(0.2, 0.8, 3).astype(np.float32), closure=wall_closure))
+    b.box((0.35, -0.7, -0.1), (0.6, 0.6, 0.6), 0.9553365, -0.29552022, len(mats) - 1)
+    # tall GGX conductor box, rotated by +0.3 rad
+    mats.append(material(diffuse=(0.95, 0.64, 0.54), closure=TR_CLOSURE_DISNEY, metallic=1.0, roughness=0.3,
+                         specular=0.5))
+    b.box((-0.35, -0.4, 0.35), (0.6, 1.2, 0.6), 0.9553365, 0.29552022, len(mats) - 1)
+    # quad area light just below the ceiling, facing down
+    mats.append(material(diffuse=(1, 1, 1), emissive=(15, 15, 15), closure=TR_CLOSURE_DIFFUSE))
+    b.quad([(-0.25, 0.99, -0.25), (0.25, 0.99, -0.25), (0.25, 0.99, 0.25), (-0.25, 0.99, 0.25)], (0, -1, 0),
+           len(mats) - 1)
+    pos, nrm, uv, idx, mat = b.arrays()
+    mats = np.array(mats, MATERIAL_DTYPE)
+    if wall_closure == TR_CLOSURE_LAMBERT:
+        # the reference shades every material with its Lambert closure (PathTracing.h:129)
+        mats["closure"] = TR_CLOSURE_LAMBERT
+    return Scene("cornell_box", pos, nrm, uv, idx, mat, mats, CameraSpec(), width, height, spp, max_depth, 1 << 30,
+                 seed)
+
+
+def _value_noise(n: int, rng: np.random.Generator, octaves: int = 6, base: int = 4) -> np.ndarray:
+    """Sum of octaves of smoothstep-interpolated random lattices, values in about [0, 1]."""
+    h = np.zeros((n, n), np.float32)
+    amp = np.float32(0.5)
+    total = np.float32(0.0)
+    for o in range(octaves):
+        cells = base << o
+        lat = rng.random((cells + 1, cells + 1)).astype(np.float32)
+        u = (np.arange(n, dtype=np.float32) * np.float32(cells)) / np.float32(n - 1)
+        i0 = np.minimum(u.astype(np.int64), cells - 1)
+        f = u - i0.astype(np.float32)
+        f = f * f * (np.float32(3.0) - np.float32(2.0) * f)
+        a = lat[i0][:, i0]
+        b = lat[i0][:, i0 + 1]
+        c = lat[i0 + 1][:, i0]
+        d = lat[i0 + 1][:, i0 + 1]
+        fx = f[None, :]
+        fy = f[:, None]
+        top = a + (b - a) * fx
+        bot = c + (d - c) * fx
+        h += amp * (top + (bot - top) * fy)
+        total += amp
+        amp = amp * np.float32(0.5)
+    return (h / total).astype(np.float32)
+
+
+def heightfield(n: int = 1024, seed: int = 1, width: int = 1920, height: int = 1080, spp: int = 64,
+                max_depth: int = 8, rr_start: int = 3, n_lights: int = 64, tiles: int = 16,
+                extent: float = 10.0, relief: float = 2.5) -> Scene:
+    """Value-noise heightfield of (n-1)^2 * 2 triangles over [-extent, extent]^2, 256 Disney materials
+    (baseColor/roughness/metallic/specular U[0,1]) assigned per (n/16)^2 tile, and n_lights emissive
+    triangles above it with log-uniform intensity in [1, 1000]."""
+    rng = np.random.default_rng(seed)
+    f32 = np.float32
+    h = _value_noise(n, rng) * f32(relief)
+    coord = (np.arange(n, dtype=np.float32) * f32(2.0 * extent)) / f32(n - 1) - f32(extent)
+    X, Z = np.meshgrid(coord, coord)
+    pos = np.stack([X, h, Z], axis=-1).reshape(-1, 3).astype(np.float32)
+    # normals from central differences
+    step = f32(2.0 * extent) / f32(n - 1)
+    hp = np.pad(h, 1, mode="edge")
+    dx = (hp[1:-1, 2:] - hp[1:-1, :-2]) / (f32(2.0) * step)
+    dz = (hp[2:, 1:-1] - hp[:-2, 1:-1]) / (f32(2.0) * step)
+    nx, ny, nz = -dx, np.ones_like(dx), -dz
+    inv = f32(1.0) / np.sqrt((nx * nx + ny * ny) + nz * nz)
+    nrm = np.stack([nx * inv, ny * inv, nz * inv], axis=-1).reshape(-1, 3).astype(np.float32)
+    uvc = np.arange(n, dtype=np.float32) / f32(n - 1)
+    U, V = np.meshgrid(uvc, uvc)
+    uv = np.stack([U, V], axis=-1).reshape(-1, 2).astype(np.float32)
+    # two triangles per cell
+    j, i = np.meshgrid(np.arange(n - 1, dtype=np.uint32), np.arange(n - 1, dtype=np.uint32))
+    v00 = (i * n + j).ravel()
+    v01 = v00 + 1
+    v10 = v00 + n
+    v11 = v10 + 1
+    idx = np.empty((2 * v00.size, 3), np.uint32)
+    idx[0::2] = np.stack([v00, v10, v11], axis=-1)
+    idx[1::2] = np.stack([v00, v11, v01], axis=-1)
+    tile = (n - 1 + tiles - 1) // tiles
+    ti = (i.ravel() // tile).astype(np.uint32)
+    tj = (j.ravel() // tile).astype(np.uint32)
+    cell_mat = ti * tiles + tj
+    mat = np.repeat(cell_mat, 2).astype(np.uint32)
+    mats = []
+    for _ in range(tiles * tiles):
+        p = rng.random(4).astype(np.float32)
+        base_color = rng.random(3).astype(np.float32)
+        mats.append(material(diffuse=base_color, closure=TR_CLOSURE_DISNEY, roughness=p[0], metallic=p[1],
+                             specular=p[2]))
+    # emissive triangles, facing down, above the terrain
+    top = float(h.max())
+    lp, ln, luv, li, lm = [], [], [], [], []
+    base = pos.shape[0]
+    for k in range(n_lights):
+        cx, cz = (rng.random(2).astype(np.float32) * f32(2.0 * extent * 0.9) - f32(extent * 0.9))
+        cy = f32(top) + f32(1.0) + rng.random(dtype=np.float32) * f32(2.0)
+        s = f32(0.3)
+        tri = np.array([[cx - s, cy, cz - s], [cx + s, cy, cz - s], [cx, cy, cz + s]], np.float32)
+        intensity = np.float32(10.0 ** (3.0 * rng.random()))
+        mats.append(material(diffuse=(1, 1, 1), emissive=(intensity, intensity, intensity),
+                             closure=TR_CLOSURE_DIFFUSE))
+        lp.append(tri)
+        ln.append(np.tile(np.array([0, -1, 0], np.float32), (3, 1)))
+        luv.append(np.zeros((3, 2), np.float32))
+        li.append(np.array([[base + 3 * k, base + 3 * k + 1, base + 3 * k + 2]], np.uint32))
+        lm.append(np.array([len(mats) - 1], np.uint32))
+    pos = np.concatenate([pos] + lp).astype(np.float32)
+    nrm = np.concatenate([nrm] + ln).astype(np.float32)
+    uv = np.concatenate([uv] + luv).astype(np.float32)
+    idx = np.concatenate([idx] + li).astype(np.uint32)
+    mat = np.concatenate([mat] + lm).astype(np.uint32)
+    cam = CameraSpec(position=(0.0, 9.0, -17.0), target=(0.0, 0.0, -1.0), up=(0.0, 1.0, 0.0),
+                     fov=float(np.float32(60.0 * np.pi / 180.0)))
+    return Scene(f"heightfield_{n}", pos, nrm, uv, idx, mat, np.array(mats, MATERIAL_DTYPE), cam, width, height,
+                 spp, max_depth, rr_start, seed)
+
+
+def random_soup(n_tris: int = 2000, seed: int = 7, extent: float = 1.0) -> Scene:
+    """Random triangles in a cube, for traversal tests."""
+    rng = np.random.default_rng(seed)
+    centers = rng.uniform(-extent, extent, (n_tris, 1, 3)).astype(np.float32)
+    offs = rng.normal(0, 0.08 * extent, (n_tris, 3, 3)).astype(np.float32)
+    pos = (centers + offs).reshape(-1, 3).astype(np.float32)
+    idx = np.arange(3 * n_tris, dtype=np.uint32).reshape(-1, 3)
+    mats = np.array([material(diffuse=(0.5, 0.5, 0.5))], MATERIAL_DTYPE)
+    return Scene("soup", pos, None, None, idx, np.zeros(n_tris, np.uint32), mats,
+                 CameraSpec(position=(0.0, 0.0, -3.0)), 64, 64, 1, 1)
+
+
+CONFIGS = {
+    "cornell_box": cornell_box,
+    "heightfield": heightfield,
+}
