@@ -1,0 +1,180 @@
+"""C ABI behaviour on the GPU: status codes instead of exits, graph replay
+equal to per-stage launches, deterministic frames, accumulation and reset."""
+import ctypes as C
+
+import numpy as np
+import pytest
+
+import trayracer_gb300 as tr
+from trayracer_gb300 import _abi
+from trayracer_gb300.renderer import KernelSettings, TracerError
+
+pytestmark = pytest.mark.gpu
+
+
+def renderer(scene, st):
+    r = tr.DeviceRenderer(0)
+    r.UpdateScene(scene)
+    r.SetCamera(scene.camera)
+    r.Resize((scene.width, scene.height))
+    r.SetSettings(st)
+    return r
+
+
+def test_errors_are_statuses():
+    r = tr.DeviceRenderer(0)
+    with pytest.raises(TracerError) as e:
+        r.RenderFrame(KernelSettings(maxDepth=4))
+    assert e.value.status == 4  # TR_ERR_NO_SCENE
+    with pytest.raises(TracerError) as e:
+        r.SetSettings(KernelSettings(maxDepth=17))
+    assert e.value.status == 1
+    with pytest.raises(TracerError) as e:
+        r.SetSettings(KernelSettings(multiSample=0))
+    assert e.value.status == 1
+    with pytest.raises(TracerError) as e:
+        r.Resize((0, 10))
+    assert e.value.status == 1
+    scene = tr.cornell_box(width=8, height=8)
+    bad = tr.Scene("bad", scene.positions, scene.normals, scene.texcoords, scene.indices,
+                   scene.material_indices.copy(), scene.materials)
+    bad.material_indices[3] = 99
+    with pytest.raises(TracerError) as e:
+        r.UpdateScene(bad)
+    assert e.value.status == 1
+    r.UpdateScene(scene)
+    with pytest.raises(TracerError) as e:
+        r.RenderFrame()
+    assert e.value.status == 5  # camera not set
+    r.SetCamera(scene.camera)
+    with pytest.raises(TracerError) as e:
+        r.RenderFrame()
+    assert e.value.status == 5  # resolution not set
+    r.Resize((8, 8))
+    with pytest.raises(TracerError) as e:
+        r.Resize((1 << 15, 1 << 14))
+    assert e.value.status == 1
+    r.RenderFrame(KernelSettings(maxDepth=3))
+    assert r.Statistics()["device_error"] == 0
+    lib = _abi.load_library()
+    assert lib.tr_extend(r.handle, None, 16) == 1
+    r.close()
+
+
+@pytest.mark.parametrize("reference", [False, True])
+def test_graph_equals_eager_and_is_deterministic(reference):
+    scene = tr.heightfield(n=96, width=96, height=54, rr_start=2)
+    st = tr.settings_for(scene, multi_sample=4, reference=reference)
+    r = renderer(scene, st)
+    r.RenderFrame(use_graph=False)
+    a = r.Accumulator()
+    sa = r.Statistics()
+    r.Reset()
+    r.RenderFrame(use_graph=True)
+    b = r.Accumulator()
+    sb = r.Statistics()
+    r.Reset()
+    r.RenderFrame(use_graph=True)
+    c = r.Accumulator()
+    r.close()
+    np.testing.assert_array_equal(a, b)
+    np.testing.assert_array_equal(b, c)
+    assert sa["extend_rays"] == sb["extend_rays"] and sa["shadow_rays"] == sb["shadow_rays"]
+
+
+def test_stages_equal_render_frame():
+    scene = tr.cornell_box(width=40, height=40)
+    st = tr.settings_for(scene, multi_sample=2)
+    r = renderer(scene, st)
+    r.RenderFrame()
+    want = r.Accumulator()
+    r.Reset()
+    r.BeginFrame()
+    r.Generate()
+    for b in range(st.maxDepth):
+        r.Extend(b)
+        r.Shade(b)
+        r.Connect(b)
+    r.Finalize()
+    got = r.Accumulator()
+    r.close()
+    np.testing.assert_array_equal(got, want)
+
+
+def test_accumulation_and_reset():
+    scene = tr.cornell_box(width=32, height=32)
+    st = tr.settings_for(scene, multi_sample=2)
+    r = renderer(scene, st)
+    r.RenderFrame()
+    r.RenderFrame()
+    acc = r.Accumulator()
+    img = r.ColorBuffer()
+    assert r.SampleCount() == 4
+    np.testing.assert_array_equal(acc[..., 3], 4.0)
+    np.testing.assert_allclose(img[..., :3], acc[..., :3] / 4.0, rtol=1e-6)
+    # frames are not repeats: the second frame uses other sample indices
+    r.Reset()
+    r.RenderFrame()
+    first = r.Accumulator()
+    assert not np.array_equal(first[..., :3] * 2, acc[..., :3])
+    r.SetCamera(tr.CameraSpec(position=(0.0, 0.1, -1.0)))
+    assert r.SampleCount() == 0
+    r.close()
+
+
+def test_counts_and_aovs():
+    scene = tr.cornell_box(width=32, height=32)
+    st = tr.settings_for(scene, multi_sample=1, aovs=True)
+    st.flags |= _abi.TR_FLAG_COUNT_TRAVERSAL
+    r = renderer(scene, st)
+    r.RenderFrame(use_graph=False)
+    s = r.Statistics()
+    buf = r.Buffers()
+    albedo = r.read_device(buf["albedo"], np.float32, 32 * 32 * 4).reshape(32, 32, 4)
+    r.close()
+    ext = s["extend_rays"]
+    assert ext[0] == 32 * 32
+    assert all(ext[i + 1] <= ext[i] for i in range(st.maxDepth - 1))
+    assert all(s["shadow_rays"][i] <= ext[i] for i in range(st.maxDepth))
+    assert s["path_count"] == sum(ext) + sum(s["shadow_rays"])
+    assert s["traversal_extend_nodes"] >= sum(ext)
+    assert (albedo[..., :3] > 0).any()
+    assert s["render_time_ms"] > 0 and s["extend_time_ms"] > 0
+
+
+def test_empty_scene_and_no_lights():
+    mats = np.array([tr.scenes.material()], tr.scenes.MATERIAL_DTYPE)
+    pos = np.array([[-1, -1, 1], [1, -1, 1], [0, 1, 1]], np.float32)
+    scene = tr.Scene("tri", pos, None, None, np.array([[0, 1, 2]], np.uint32), np.zeros(1, np.uint32), mats,
+                     width=16, height=16)
+    r = renderer(scene, tr.settings_for(scene, multi_sample=1))
+    r.RenderFrame()
+    img = r.ColorBuffer()
+    s = r.Statistics()
+    assert np.all(img[..., :3] == 0) and s["shadow_ray_count"] == 0 and s["device_error"] == 0
+    empty = tr.Scene("empty", np.zeros((0, 3), np.float32), None, None, np.zeros((0, 3), np.uint32),
+                     np.zeros(0, np.uint32), mats, width=16, height=16)
+    r.UpdateScene(empty)
+    r.RenderFrame()
+    assert np.all(r.ColorBuffer()[..., :3] == 0)
+    r.close()
+
+
+def test_full_size_heightfield_properties():
+    """The benchmark scene at full size: determinism, sane counts, finite image."""
+    scene = tr.heightfield()
+    st = tr.settings_for(scene, multi_sample=4)
+    r = renderer(scene, st)
+    info = r.SceneInfo()
+    assert info["triangle_count"] == 1023 * 1023 * 2 + 64 and info["light_count"] == 64
+    r.RenderFrame(use_graph=True)
+    a = r.Accumulator()
+    s = r.Statistics()
+    r.Reset()
+    r.RenderFrame(use_graph=False)
+    b = r.Accumulator()
+    r.close()
+    np.testing.assert_array_equal(a, b)
+    assert np.isfinite(a).all() and a[..., :3].mean() > 0
+    assert s["device_error"] == 0
+    assert s["extend_rays"][0] == 1920 * 1080 * 4

@@ -462,6 +462,8 @@ tr_status tr_set_camera(void* ctx, const tr_camera* cam)
     k.tanFov2 = tanf(cam->fov / 2.0f);
     if (!(cam->fov > 0.f && cam->fov < 3.14159f) || !(cam->focal_dist > 0.f))
         return fail(c, TR_ERR_INVALID_ARGUMENT, "camera fov must be in (0, pi) and focal_dist > 0");
+    if (c->hasCamera && std::memcmp(&k, &c->camera, sizeof(Camera)) == 0)
+        return TR_OK;  // unchanged camera: keep the accumulation and the captured frame graph
     c->camera = k;
     c->hasCamera = true;
     invalidate_graph(c);
