@@ -255,6 +255,13 @@ const char* tr_last_error(void* ctx);
 /* ---- scene / camera / settings ---- */
 tr_status tr_scene_upload(void* ctx, const tr_scene_desc* scene);
 tr_status tr_get_scene_info(void* ctx, tr_scene_info* info);
+/* Replaces the material table of the uploaded scene (same count) without
+ * rebuilding the BVH; emissive materials may change radiance but the set of
+ * emissive triangles must stay the same (light records and the alias table
+ * are rebuilt). Resets the accumulation. No reference counterpart: the
+ * reference re-uploads changed materials through Renderer::UpdateScene
+ * (Renderer.cpp:79-143). */
+tr_status tr_update_materials(void* ctx, const tr_material_desc* materials, uint32_t count);
 tr_status tr_set_camera(void* ctx, const tr_camera* camera);
 tr_status tr_set_settings(void* ctx, const tr_kernel_settings* settings);
 tr_status tr_resize(void* ctx, uint32_t width, uint32_t height);
@@ -273,6 +280,18 @@ tr_status tr_finalize(void* ctx, void* stream);
  * round trips; with use_graph != 0 it is captured once per configuration into
  * a CUDA graph and replayed. */
 tr_status tr_render_frame(void* ctx, void* stream, int32_t use_graph);
+
+/* Path-replay adjoint (Vicini, Speierer, Jakob, SIGGRAPH 2021) of the last
+ * rendered frame: adds to param_grad (device, material_count x 9 floats:
+ * d/d base colour r, g, b, roughness, metallic, specular, emission r, g, b)
+ * the gradient of a loss whose derivative with respect to each path's
+ * radiance is scale * pixel_grad[pixel] (device, float4 per pixel; for an
+ * image averaged over S samples per pixel pass scale = 1/S). Paths are
+ * replayed from their random keys (rays re-traced, nothing stored per
+ * vertex); sampled directions, pdfs and MIS weights are held fixed.
+ * Default sampling mode only. No reference counterpart (the reference does
+ * not differentiate). */
+tr_status tr_adjoint_frame(void* ctx, void* stream, const float* pixel_grad, float scale, float* param_grad);
 
 /* ---- results ---- */
 tr_status tr_synchronize(void* ctx, void* stream);

@@ -65,6 +65,9 @@ class Oracle:
             lib.orc_reference_rng.argtypes = [_U, _U, _U, _P]
             lib.orc_set_reference_draw_order.argtypes = [C.c_int]
             lib.orc_closure.argtypes = [C.c_int, C.c_int, C.c_int, _P, _P]
+            lib.orc_closure_value_grad.argtypes = [_P, _U, _P, _P, _P]
+            lib.orc_adjoint.restype = C.c_int
+            lib.orc_adjoint.argtypes = [_P, _P, _P, _U, _U, _U, _P, C.c_float, C.c_int, C.c_int, _P]
             cls._lib = lib
         return cls._lib
 
@@ -148,6 +151,27 @@ class Oracle:
         self._lib.orc_render(self._s, C.addressof(cc), C.addressof(st), width, height, frames, first_pixel,
                              pixel_count, int(use_double), threads, _ptr(acc), _ptr(paths), _ptr(counts))
         return acc, paths, (int(counts[0]), int(counts[1]))
+
+    def adjoint(self, cam: CameraSpec, settings, width, height, sample_count, pixel_grad, scale=1.0,
+                use_double=True, threads=0):
+        """Path-replay gradient (material_count, 9) of the frame with sample_count."""
+        pg = np.ascontiguousarray(pixel_grad, np.float32).reshape(-1, 4)
+        grads = np.zeros((self.scene.materials.shape[0], 9), np.float64)
+        cc = camera_to_c(cam)
+        st = settings.to_c()
+        rc = self._lib.orc_adjoint(self._s, C.addressof(cc), C.addressof(st), width, height, sample_count,
+                                   _ptr(pg), scale, int(use_double), threads, _ptr(grads))
+        if rc != 0:
+            raise RuntimeError("the adjoint differentiates the default sampling mode only")
+        return grads
+
+    def closure_value_grad(self, material: int, wo, wi) -> np.ndarray:
+        """(3, 7): per channel the closure value and its 6 parameter derivatives."""
+        o = np.ascontiguousarray(wo, np.float32)
+        i = np.ascontiguousarray(wi, np.float32)
+        out = np.zeros((3, 7), np.float64)
+        self._lib.orc_closure_value_grad(self._s, material, _ptr(o), _ptr(i), _ptr(out))
+        return out
 
     @classmethod
     def closure(cls, ctype: int, inputs: np.ndarray, reference: bool = True, use_double: bool = False):

@@ -18,6 +18,59 @@
 
 namespace {
 
+// ------------------------------------------------------------------ scalars
+// Math entry points for float, double and the dual numbers of the adjoint.
+template <class T> inline T msqrt(T x) { using std::sqrt; return sqrt(x); }
+template <class T> inline T mfabs(T x) { using std::fabs; return fabs(x); }
+template <class T> inline T mlog(T x) { using std::log; return log(x); }
+
+// Forward-mode dual number over B (double for the FP64 gradient): value and
+// derivatives with respect to base colour r, g, b, roughness, metallic, specular.
+constexpr int kDP = 6;
+template <class B>
+struct DualT {
+    B v;
+    B d[kDP];
+    DualT() : v(0) { for (int i = 0; i < kDP; ++i) d[i] = 0; }
+    DualT(double x) : v(B(x)) { for (int i = 0; i < kDP; ++i) d[i] = 0; }
+    static DualT var(B x, int k) { DualT r(0.0); r.v = x; r.d[k] = 1; return r; }
+};
+template <class B> inline DualT<B> operator+(const DualT<B>& a, const DualT<B>& b)
+{ DualT<B> r; r.v = a.v + b.v; for (int i = 0; i < kDP; ++i) r.d[i] = a.d[i] + b.d[i]; return r; }
+template <class B> inline DualT<B> operator-(const DualT<B>& a, const DualT<B>& b)
+{ DualT<B> r; r.v = a.v - b.v; for (int i = 0; i < kDP; ++i) r.d[i] = a.d[i] - b.d[i]; return r; }
+template <class B> inline DualT<B> operator-(const DualT<B>& a)
+{ DualT<B> r; r.v = -a.v; for (int i = 0; i < kDP; ++i) r.d[i] = -a.d[i]; return r; }
+template <class B> inline DualT<B> operator*(const DualT<B>& a, const DualT<B>& b)
+{ DualT<B> r; r.v = a.v * b.v; for (int i = 0; i < kDP; ++i) r.d[i] = a.d[i] * b.v + a.v * b.d[i]; return r; }
+template <class B> inline DualT<B> operator/(const DualT<B>& a, const DualT<B>& b)
+{ DualT<B> r; r.v = a.v / b.v; for (int i = 0; i < kDP; ++i) r.d[i] = (a.d[i] - r.v * b.d[i]) / b.v; return r; }
+template <class B> inline DualT<B> sqrt(const DualT<B>& a)
+{ DualT<B> r; r.v = std::sqrt(a.v); const B k = r.v > 0 ? B(0.5) / r.v : B(0); for (int i = 0; i < kDP; ++i) r.d[i] = a.d[i] * k; return r; }
+template <class B> inline DualT<B> fabs(const DualT<B>& a) { return a.v < 0 ? -a : a; }
+template <class B> inline DualT<B> log(const DualT<B>& a)
+{ DualT<B> r; r.v = std::log(a.v); for (int i = 0; i < kDP; ++i) r.d[i] = a.d[i] / a.v; return r; }
+template <class B> inline bool operator<(const DualT<B>& a, const DualT<B>& b) { return a.v < b.v; }
+template <class B> inline bool operator>(const DualT<B>& a, const DualT<B>& b) { return a.v > b.v; }
+template <class B> inline bool operator<=(const DualT<B>& a, const DualT<B>& b) { return a.v <= b.v; }
+template <class B> inline bool operator==(const DualT<B>& a, const DualT<B>& b) { return a.v == b.v; }
+template <class B> inline bool operator!=(const DualT<B>& a, const DualT<B>& b) { return a.v != b.v; }
+template <class B> inline bool operator<(const DualT<B>& a, double b) { return a.v < b; }
+template <class B> inline bool operator>(const DualT<B>& a, double b) { return a.v > b; }
+template <class B> inline bool operator==(const DualT<B>& a, double b) { return a.v == b; }
+template <class B> inline bool operator!=(const DualT<B>& a, double b) { return a.v != b; }
+template <class B> inline bool operator<(const DualT<B>& a, int b) { return a.v < b; }
+template <class B> inline bool operator>(const DualT<B>& a, int b) { return a.v > b; }
+template <class B> inline bool operator<=(const DualT<B>& a, int b) { return a.v <= b; }
+template <class B> inline DualT<B> operator+(const DualT<B>& a, double b) { return a + DualT<B>(b); }
+template <class B> inline DualT<B> operator+(double b, const DualT<B>& a) { return DualT<B>(b) + a; }
+template <class B> inline DualT<B> operator-(const DualT<B>& a, double b) { return a - DualT<B>(b); }
+template <class B> inline DualT<B> operator-(double b, const DualT<B>& a) { return DualT<B>(b) - a; }
+template <class B> inline DualT<B> operator*(const DualT<B>& a, double b) { return a * DualT<B>(b); }
+template <class B> inline DualT<B> operator*(double b, const DualT<B>& a) { return DualT<B>(b) * a; }
+template <class B> inline DualT<B> operator/(const DualT<B>& a, double b) { return a / DualT<B>(b); }
+template <class B> inline DualT<B> operator/(double b, const DualT<B>& a) { return DualT<B>(b) / a; }
+
 // ------------------------------------------------------------------ vectors
 template <class T>
 struct V3 {
@@ -40,9 +93,9 @@ template <class T> inline V3<T> cross(V3<T> a, V3<T> b)
 {
     return {a.y * b.z - a.z * b.y, a.z * b.x - a.x * b.z, a.x * b.y - a.y * b.x};
 }
-template <class T> inline T length(V3<T> v) { return std::sqrt(dot(v, v)); }
+template <class T> inline T length(V3<T> v) { return msqrt(dot(v, v)); }
 // helper_math normalize: v * rsqrtf(dot(v, v)); host rsqrtf = 1 / sqrtf
-template <class T> inline V3<T> normalize(V3<T> v) { return v * (T(1) / std::sqrt(dot(v, v))); }
+template <class T> inline V3<T> normalize(V3<T> v) { return v * (T(1) / msqrt(dot(v, v))); }
 template <class T> inline T sq(T x) { return x * x; }
 template <class T> inline T mix(T a, T b, T t) { return (a * (T(1) - t)) + (b * t); }
 template <class T> inline T lerp(T a, T b, T t) { return a + t * (b - a); }
@@ -68,6 +121,14 @@ template <> struct K<float> {
     static constexpr float RcpTwoPi = 0.1591549430918953f;
     static constexpr float PiOver2 = 1.57079632679f;
     static constexpr float PiOver4 = 0.78539816339f;
+};
+template <class B> struct K<DualT<B>> {
+    static inline const DualT<B> Pi = DualT<B>(3.1415926535897932);
+    static inline const DualT<B> TwoPi = DualT<B>(6.2831853071795865);
+    static inline const DualT<B> RcpPi = DualT<B>(0.3183098861837907);
+    static inline const DualT<B> RcpTwoPi = DualT<B>(0.1591549430918953);
+    static inline const DualT<B> PiOver2 = DualT<B>(1.57079632679);
+    static inline const DualT<B> PiOver4 = DualT<B>(0.78539816339);
 };
 constexpr float kEps = 1e-3f;   // CudaGlobals.h:10
 constexpr float kDstMax = 1e30f; // optix.cu:16
@@ -160,6 +221,7 @@ struct MatRaw {            // fp16-rounded properties (Material::Property::Build
 struct Light {
     float V0[3], V1[3], V2[3], N[3];
     float area, energy, radiance[3], sumEnergy;
+    uint32_t triIx;
 };
 struct Alias {
     float prob;
@@ -365,7 +427,7 @@ inline bool box_hit(const Node& n, const double O[3], const double inv[3], doubl
     }
     tnear = t0;
     // slack so that round-off never culls a triangle lying on the box face
-    return t0 <= t1 + 1e-9 * std::max(1.0, std::fabs(t1));
+    return t0 <= t1 + 1e-9 * std::max(1.0, mfabs(t1));
 }
 
 // Closest hit (any = false) or first hit (any = true) of one ray; T selects the triangle test precision.
@@ -508,17 +570,17 @@ template <class T> V3<T> cos_hemi(T r0, T r1)
 {
     T s, c;
     sincosT(K<T>::TwoPi * r0, s, c);
-    const T b = std::sqrt(T(1) - r1);
-    return v3(c * b, s * b, std::sqrt(r1));
+    const T b = msqrt(T(1) - r1);
+    return v3(c * b, s * b, msqrt(r1));
 }
 
 // FinalizeClosure, Closure.h:57-74
 template <class T> Clos<T> finalize(V3<T> Tp, const Lobe<T>& e, const Lobe<T>& s)
 {
     Clos<T> c;
-    c.shT = e.Tv * std::fabs(e.wi.z) * Tp;
+    c.shT = e.Tv * mfabs(e.wi.z) * Tp;
     c.shPdf = e.pdf;
-    c.extT = s.Tv * std::fabs(s.wi.z) * Tp;
+    c.extT = s.Tv * mfabs(s.wi.z) * Tp;
     c.extPdf = s.pdf;
     c.extWi = s.wi;
     c.extFlags = s.flags;
@@ -564,7 +626,7 @@ template <class T> Clos<T> diffuse(V3<T> wo, V3<T> wi, V3<T> Tp, const HitMat<T>
 template <class T> void alpha_xy(T rough, T aniso, T& ax, T& ay)
 {
     const T r2 = sq(rough);
-    const T aspect = std::sqrt(T(1) + aniso * (aniso < 0 ? T(0.9f) : T(-0.9f)));
+    const T aspect = msqrt(T(1) + aniso * (aniso < 0 ? T(0.9f) : T(-0.9f)));
     ax = fmx(T(0.001f), r2 / aspect);
     ay = fmx(T(0.001f), r2 * aspect);
 }
@@ -578,7 +640,7 @@ template <class T> T projected(V3<T> m, T s, T ax, T ay)
 {
     if (ax == ay || s == T(0))
         return ax;
-    return std::sqrt(sq((m.x * ax) / s) + sq((m.y * ay) / s));
+    return msqrt(sq((m.x * ax) / s) + sq((m.y * ay) / s));
 }
 template <class T> T ggx_lambda(V3<T> v, T ax, T ay)
 {
@@ -586,10 +648,10 @@ template <class T> T ggx_lambda(V3<T> v, T ax, T ay)
     if (c == T(0))
         return 0;
     const T c2 = sq(c);
-    const T s = std::sqrt(fmx(T(0), T(1) - c2));
+    const T s = msqrt(fmx(T(0), T(1) - c2));
     const T a = projected(v, s, ax, ay);
     const T t2 = sq(s) / c2;
-    return (T(-1) + std::sqrt(T(1) + sq(a) * t2)) * T(0.5f);
+    return (T(-1) + msqrt(T(1) + sq(a) * t2)) * T(0.5f);
 }
 template <class T> T ggx_D(V3<T> m, T ax, T ay)
 {
@@ -597,7 +659,7 @@ template <class T> T ggx_D(V3<T> m, T ax, T ay)
     if (c == T(0))
         return sq(ax) * K<T>::RcpPi;
     const T c2 = sq(c);
-    const T s = std::sqrt(fmx(T(0), T(1) - c2));
+    const T s = msqrt(fmx(T(0), T(1) - c2));
     const T c4 = sq(c2);
     const T t2 = (T(1) - c2) / c2;
     const T A = stretched(m, s, ax, ay);
@@ -613,7 +675,7 @@ template <class T> T ggx_pdf(V3<T> v, V3<T> m, T ax, T ay)
     if (v.z == T(0))
         return 0;
     const T G1 = T(1) / (T(1) + ggx_lambda(v, ax, ay));
-    return G1 * std::fabs(dot(v, m)) * ggx_D(m, ax, ay) / std::fabs(v.z);
+    return G1 * mfabs(dot(v, m)) * ggx_D(m, ax, ay) / mfabs(v.z);
 }
 template <class T> V3<T> ggx_sample_m(V3<T> v, T r0, T r1, T ax, T ay)
 {
@@ -622,13 +684,13 @@ template <class T> V3<T> ggx_sample_m(V3<T> v, T r0, T r1, T ax, T ay)
     const V3<T> t1 = v.y < T(0.9999f) ? normalize(cross(st, v3(T(0), T(0), T(1)))) : v3(T(1), T(0), T(0));
     const V3<T> t2 = cross(t1, st);
     const T a = T(1) / (T(1) + st.z);
-    const T r = std::sqrt(r0);
+    const T r = msqrt(r0);
     const T phi = r1 < a ? r1 / a * K<T>::Pi : K<T>::Pi + (r1 - a) / (T(1) - a) * K<T>::Pi;
     T sp, cp;
     sincosT(phi, sp, cp);
     const T p1 = r * cp;
     const T p2 = r * sp * (r1 < a ? T(1) : st.z);
-    const V3<T> h = p1 * t1 + p2 * t2 + std::sqrt(fmx(T(0), T(1) - p1 * p1 - p2 * p2)) * st;
+    const V3<T> h = p1 * t1 + p2 * t2 + msqrt(fmx(T(0), T(1) - p1 * p1 - p2 * p2)) * st;
     return normalize(v3(h.x * ax, h.y * ay, fmx(T(0), h.z)));
 }
 template <class T> T gtr1_lambda(V3<T> v, T ax)
@@ -637,38 +699,38 @@ template <class T> T gtr1_lambda(V3<T> v, T ax)
     if (c == T(0))
         return 0;
     const T c2 = sq(c);
-    const T s = std::sqrt(fmx(T(0), T(1) - c2));
+    const T s = msqrt(fmx(T(0), T(1) - c2));
     if (s == T(0))
         return 0;
     const T cot2 = c2 / sq(s);
-    const T cot = std::sqrt(cot2);
+    const T cot = msqrt(cot2);
     const T alpha = clampT(ax, T(0.001f), T(0.999f));
     const T a2 = sq(alpha);
-    const T a = std::sqrt(cot2 + a2);
-    const T b = std::sqrt(cot2 + T(1));
-    const T lc = std::log(cot + b);
-    const T ld = std::log(cot + a);
-    return (a - b + cot * (lc - ld)) / (cot * std::log(a2));
+    const T a = msqrt(cot2 + a2);
+    const T b = msqrt(cot2 + T(1));
+    const T lc = mlog(cot + b);
+    const T ld = mlog(cot + a);
+    return (a - b + cot * (lc - ld)) / (cot * mlog(a2));
 }
 template <class T> T gtr1_D(V3<T> m, T ax)
 {
     const T alpha = clampT(ax, T(0.001f), T(0.999f));
     const T a2 = sq(alpha);
     const T c2 = sq(m.z);
-    const T a = (a2 - T(1)) / (K<T>::Pi * std::log(a2));
+    const T a = (a2 - T(1)) / (K<T>::Pi * mlog(a2));
     const T b = T(1) / (T(1) + (a2 - T(1)) * c2);
     return a * b;
 }
 template <class T> T gtr1_G(V3<T> wi, V3<T> wo, T ax) { return T(1) / (T(1) + gtr1_lambda(wo, ax) + gtr1_lambda(wi, ax)); }
-template <class T> T gtr1_pdf(V3<T> m, T ax) { return gtr1_D(m, ax) * std::fabs(m.y); }
+template <class T> T gtr1_pdf(V3<T> m, T ax) { return gtr1_D(m, ax) * mfabs(m.y); }
 template <class T> V3<T> gtr1_sample_m(T r0, T r1, T ax)
 {
     const T alpha = clampT(ax, T(0.001f), T(0.999f));
     const T a2 = sq(alpha);
     const T a = T(1) - std::pow(a2, T(1) - r0);
     const T c2 = a / (T(1) - a2);
-    const T c = std::sqrt(c2);
-    const T s = std::sqrt(fmx(T(0), T(1) - c2));
+    const T c = msqrt(c2);
+    const T s = msqrt(fmx(T(0), T(1) - c2));
     T sp, cp;
     sincosT(K<T>::TwoPi * r1, sp, cp);
     return v3(cp * s, sp * s, c);
@@ -686,12 +748,12 @@ template <class T> V3<T> spec_fresnel(const HitMat<T>& mat, V3<T> o, V3<T> h)
     V3<T> v = (T(1) - mat.specularTint) + (mat.specularTint * mat.tint);
     v = v * (mat.specular * T(0.08f));
     v = ((T(1) - mat.metallic) * v) + (mat.metallic * mat.diffuse);
-    const T f = schlick(std::fabs(dot(o, h)));
+    const T f = schlick(mfabs(dot(o, h)));
     return ((T(1) - f) * v) + f;
 }
 template <class T> V3<T> cc_fresnel(const HitMat<T>& mat, V3<T> o, V3<T> h)
 {
-    const T f = schlick(std::fabs(dot(o, h)));
+    const T f = schlick(mfabs(dot(o, h)));
     return v3s(mix(T(0.04f), T(1), f) * T(0.25f) * mat.clearcoat);
 }
 template <class T> bool force_above(V3<T>& d)
@@ -715,11 +777,11 @@ template <class T> T d_diffuse(const HitMat<T>& mat, V3<T> wo, V3<T> wi, V3<T>& 
     if (mat.subsurface > T(0)) {
         const T fss90 = sq(cih) * mat.roughness;
         const T fss = mix(T(1), fss90, fl) * mix(T(1), fss90, fv);
-        const T ss = T(1.25f) * (fss * (T(1) / (std::fabs(con) + std::fabs(cin)) - T(0.5f)) + T(0.5f));
+        const T ss = T(1.25f) * (fss * (T(1) / (mfabs(con) + mfabs(cin)) - T(0.5f)) + T(0.5f));
         fd = mix(fd, ss, mat.subsurface);
     }
     value = mat.diffuse * (fd * K<T>::RcpPi * (T(1) - mat.metallic));
-    return std::fabs(cin) * K<T>::RcpPi;
+    return mfabs(cin) * K<T>::RcpPi;
 }
 template <class T> T d_sheen(const HitMat<T>& mat, V3<T> wo, V3<T> wi, V3<T>& value)
 {
@@ -740,8 +802,8 @@ template <class T> T d_ggx_eval(T ax, T ay, const HitMat<T>& mat, V3<T> wo, V3<T
     const T D = ggx_D(m, ax, ay);
     const T G = ggx_G(wi, wo, ax, ay);
     value = spec_fresnel(mat, wo, m);
-    value = value * (D * G / std::fabs(T(4) * wo.z * wi.z));
-    return ggx_pdf(wo, m, ax, ay) / std::fabs(T(4) * coh);
+    value = value * (D * G / mfabs(T(4) * wo.z * wi.z));
+    return ggx_pdf(wo, m, ax, ay) / mfabs(T(4) * coh);
 }
 template <class T>
 void d_ggx_sample(T ax, T ay, const HitMat<T>& mat, T r0, T r1, V3<T> wo, V3<T>& wi, T& pdf, V3<T>& value)
@@ -755,13 +817,13 @@ void d_ggx_sample(T ax, T ay, const HitMat<T>& mat, T r0, T r1, V3<T> wo, V3<T>&
     if (wi.z == T(0))
         return;
     const T coh = dot(wo, m);
-    pdf = ggx_pdf(wo, m, ax, ay) / std::fabs(T(4) * coh);
+    pdf = ggx_pdf(wo, m, ax, ay) / mfabs(T(4) * coh);
     if (pdf < T(1e-6f))
         return;
     const T D = ggx_D(m, ax, ay);
     const T G = ggx_G(wi, wo, ax, ay);
     value = spec_fresnel(mat, wo, m);
-    value = value * (D * G / std::fabs(T(4) * wo.z * wi.z));
+    value = value * (D * G / mfabs(T(4) * wo.z * wi.z));
 }
 template <class T> T d_gtr1_eval(T a, const HitMat<T>& mat, V3<T> wo, V3<T> wi, V3<T>& value)
 {
@@ -774,8 +836,8 @@ template <class T> T d_gtr1_eval(T a, const HitMat<T>& mat, V3<T> wo, V3<T> wi, 
     const T D = gtr1_D(m, a);
     const T G = gtr1_G(wi, wo, a);
     value = cc_fresnel(mat, wo, m);
-    value = value * (D * G / std::fabs(T(4) * wo.z * wi.z));
-    return gtr1_pdf(m, a) / std::fabs(T(4) * coh);
+    value = value * (D * G / mfabs(T(4) * wo.z * wi.z));
+    return gtr1_pdf(m, a) / mfabs(T(4) * coh);
 }
 template <class T>
 void d_gtr1_sample(T a, const HitMat<T>& mat, T r0, T r1, V3<T> wo, V3<T>& wi, T& pdf, V3<T>& value)
@@ -789,13 +851,13 @@ void d_gtr1_sample(T a, const HitMat<T>& mat, T r0, T r1, V3<T> wo, V3<T>& wi, T
     if (wi.z == T(0))
         return;
     const T coh = dot(wo, m);
-    pdf = gtr1_pdf(m, a) / std::fabs(T(4) * coh);
+    pdf = gtr1_pdf(m, a) / mfabs(T(4) * coh);
     if (pdf < T(1e-6f))
         return;
     const T D = gtr1_D(m, a);
     const T G = gtr1_G(wi, wo, a);
     value = spec_fresnel(mat, wo, m);
-    value = value * (D * G / std::fabs(T(4) * wo.z * wi.z));
+    value = value * (D * G / mfabs(T(4) * wo.z * wi.z));
 }
 template <class T> bool d_weights(const HitMat<T>& m, T& wd, T& ws, T& wsp, T& wc)
 {
@@ -871,7 +933,7 @@ template <class T, bool REF> Lobe<T> d_sample(V3<T> wo, const HitMat<T>& m, T r0
         cpdf = d_sheen(m, wo, wi, value);
         prob = ws * cpdf;
         ws = 0;
-        flags |= kSpec;
+        flags |= REF ? kSpec : 0u;
     } else if (r0 < csp) {
         const T u = REF ? r0 : fmn((r0 - cs) / wsp, T(0.99999994f));
         T ax, ay;
@@ -879,13 +941,13 @@ template <class T, bool REF> Lobe<T> d_sample(V3<T> wo, const HitMat<T>& m, T r0
         d_ggx_sample(ax, ay, m, u, r1, wo, wi, cpdf, value);
         prob = wsp * cpdf;
         wsp = 0;
-        flags |= kSpec;
+        flags |= REF ? kSpec : 0u;
     } else {
         const T u = REF ? r0 : fmn((r0 - csp) / wc, T(0.99999994f));
         d_gtr1_sample(cc_alpha(m), m, u, r1, wo, wi, cpdf, value);
         prob = wc * cpdf;
         wc = 0;
-        flags |= kSpec;
+        flags |= REF ? kSpec : 0u;
     }
     if (wd > 0) {
         V3<T> v;
@@ -931,7 +993,7 @@ template <class T, class Rng> void sample_disk(Rng& rng, T& x, T& y)
         return;
     }
     T theta, r;
-    if (std::fabs(lx) > std::fabs(ly)) {
+    if (mfabs(lx) > mfabs(ly)) {
         r = lx;
         theta = K<T>::PiOver4 * (ly / lx);
     } else {
@@ -974,7 +1036,7 @@ void camera_ray(const tr_camera& cam, T tanFov2, uint32_t W, uint32_t H, uint32_
         sincosT(T(cam.bokeh_rotation) + (T(index) * step), s0, c0);
         sincosT(T(cam.bokeh_rotation) + T(index + 1) * step, s1, c1);
         const T u1 = T(rng.next()), u2 = T(rng.next());
-        const T su = std::sqrt(u1);
+        const T su = msqrt(u1);
         bx = (su * (T(1) - u2)) * c0 + (su * u2) * c1;
         by = (su * (T(1) - u2)) * s0 + (su * u2) * s1;
     }
@@ -983,7 +1045,7 @@ void camera_ray(const tr_camera& cam, T tanFov2, uint32_t W, uint32_t H, uint32_
     T ly = (tanFov2 * sy) - (ccy / T(cam.focal_dist));
     const T dist = T(cam.distortion);
     if (!(lx == 0 && ly == 0) && dist > 0) {
-        const T scale = std::sqrt(lx * lx + ly * ly);
+        const T scale = msqrt(lx * lx + ly * ly);
         const T d = (tanFov2 * dist) * T(0.5f);
         const T distorted = (scale * dist * std::atan(d)) / d;
         if (distorted >= K<T>::PiOver2)
@@ -1029,7 +1091,7 @@ template <class T> Surface<T> surface_at(const orc_scene& S, uint32_t prim, T bu
     const T s2 = T(hround(hval(t.uv[2][0]) - hval(t.uv[0][0])));
     const T t2 = T(hround(hval(t.uv[2][1]) - hval(t.uv[0][1])));
     const T r = (s1 * t2) - (s2 * t1);
-    if (std::fabs(r) < T(1e-6f)) {
+    if (mfabs(r) < T(1e-6f)) {
         sf.B = normalize(cross(sf.N, e1));
         sf.Tn = normalize(cross(sf.N, sf.B));
     } else {
@@ -1105,11 +1167,17 @@ template <class T> struct ShadeOut {
     V3<T> shO, shL, shT;
     T shDist = 0;
     V3<T> add = v3s(T(0));
+    // vertex data for the adjoint
+    bool hit = false, emissive = false;
+    uint32_t matIx = 0;
+    int lightIx = -1;
+    V3<T> wo, wiLight, wiExt;
 };
 
 // SampleLight / SelectLight, CudaLights.h:38-124
 template <class T, bool REF, class Rng>
-V3<T> sample_light(const orc_scene& S, Rng& rng, V3<T> I, V3<T> N, T& prob, T& pdf, V3<T>& rad, T& dist)
+V3<T> sample_light(const orc_scene& S, Rng& rng, V3<T> I, V3<T> N, T& prob, T& pdf, V3<T>& rad, T& dist,
+                   int* lightOut = nullptr)
 {
     const float total = REF ? S.lightEnergy : S.lightEnergyTotal;
     const int32_t count = int32_t(S.lights.size());
@@ -1155,11 +1223,13 @@ V3<T> sample_light(const orc_scene& S, Rng& rng, V3<T> I, V3<T> N, T& prob, T& p
         ix = int32_t(coin < S.alias[k].prob ? k : S.alias[k].alias);
         const Light& L = S.lights[ix];
         const T r0 = T(rng.next()), r1 = T(rng.next());
-        const T su = std::sqrt(r0);
+        const T su = msqrt(r0);
         P = ((T(1) - su) * v3(T(L.V0[0]), T(L.V0[1]), T(L.V0[2]))) +
             ((su * (T(1) - r1)) * v3(T(L.V1[0]), T(L.V1[1]), T(L.V1[2]))) +
             ((su * r1) * v3(T(L.V2[0]), T(L.V2[1]), T(L.V2[2])));
     }
+    if (lightOut)
+        *lightOut = ix;
     const Light& L = S.lights[ix];
     V3<T> Ld = I - P;
     const T sqDist = dot(Ld, Ld);
@@ -1169,7 +1239,7 @@ V3<T> sample_light(const orc_scene& S, Rng& rng, V3<T> I, V3<T> N, T& prob, T& p
     prob = T(L.energy) / T(total);
     const bool facing = REF ? (dot(N, Ld) != T(0)) : (dot(N, Ld) < T(0));
     pdf = (LNdotL > 0 && facing) ? sqDist / (T(L.area) * LNdotL) : T(0);
-    dist = std::sqrt(sqDist);
+    dist = msqrt(sqDist);
     rad = v3(T(L.radiance[0]), T(L.radiance[1]), T(L.radiance[2]));
     return -Ld;
 }
@@ -1187,12 +1257,15 @@ ShadeOut<T> shade_one(const orc_scene& S, const tr_kernel_settings& st, uint32_t
         return out;  // sky disabled: black
     const Surface<T> sf = surface_at<T>(S, primIx, bu, bv, D);
     const HitMat<T> m = hit_material<T>(S.mats[sf.matIx]);
+    out.hit = true;
+    out.matIx = sf.matIx;
     if (m.emissive.x + m.emissive.y + m.emissive.z > T(kEps)) {
+        out.emissive = true;
         V3<T> contrib = v3s(T(0));
         if (bounce == 0 || (flags & kSpec)) {
             contrib = m.emissive;
         } else {
-            const T lightPdf = (tmax * tmax) / (std::fabs(dot(D, sf.N)) * sf.area);
+            const T lightPdf = (tmax * tmax) / (mfabs(dot(D, sf.N)) * sf.area);
             const V3<T> en = m.emissive * sf.area;
             const T total = T(REF ? S.lightEnergy : S.lightEnergyTotal);
             const T pick = (en.x + en.y + en.z) / total;
@@ -1213,7 +1286,7 @@ ShadeOut<T> shade_one(const orc_scene& S, const tr_kernel_settings& st, uint32_t
 
     T lightProb, lightPdf, lightDist;
     V3<T> lightRad;
-    const V3<T> L = sample_light<T, REF>(S, rng, I, sf.N, lightProb, lightPdf, lightRad, lightDist);
+    const V3<T> L = sample_light<T, REF>(S, rng, I, sf.N, lightProb, lightPdf, lightRad, lightDist, &out.lightIx);
     const V3<T> wow = -D;
     const V3<T> wo = normalize(v3(dot(wow, sf.Tn), dot(wow, sf.B), dot(wow, sf.N)));
     const V3<T> wi = normalize(v3(dot(L, sf.Tn), dot(L, sf.B), dot(L, sf.N)));
@@ -1237,8 +1310,11 @@ ShadeOut<T> shade_one(const orc_scene& S, const tr_kernel_settings& st, uint32_t
         out.shDist = lightDist;
         out.shT = safe_color(shadowT, maxColor);
     }
+    out.wo = wo;
+    out.wiLight = wi;
+    out.wiExt = c.extWi;
     if (c.extPdf > T(kEps)) {
-        V3<T> tp = c.extT / std::fabs(c.extPdf);
+        V3<T> tp = c.extT / mfabs(c.extPdf);
         if (bounce >= st.rr_start) {
             const T rr = fmn(T(1), fmx(tp.x, fmx(tp.y, tp.z)));
             if (rr < T(rng.next()))
@@ -1342,6 +1418,162 @@ V3<T> render_path(const orc_scene& S, const tr_camera& cam, T tanFov2, const tr_
     return radiance;
 }
 
+
+// ---------------------------------------------------------------- adjoint
+// Path-replay gradient of one path (default sampling mode): the path is
+// traced once recording each vertex's contributions, then the closure value
+// at every vertex is differentiated (dual numbers) and weighted by the
+// radiance that went through it: its own NEE contribution for the light
+// direction, the sum of all later contributions for the extend direction.
+// Sampled directions, pdfs and MIS weights are held fixed.
+template <class T>
+struct VertexRec {
+    ShadeOut<T> so;
+    bool visible = false;
+    V3<T> cNee = v3s(T(0));
+};
+
+template <class T>
+V3<DualT<double>> dual_value(const orc_scene& S, uint32_t matIx, V3<T> wo, V3<T> wi)
+{
+    using D = DualT<double>;
+    const MatRaw& r = S.mats[matIx];
+    // seed the six parameters, then resolve tint/luminance with duals (CudaMaterial.h:155-183)
+    MatRaw rr = r;
+    HitMat<D> m = hit_material<D>(rr);
+    m.diffuse = v3(D::var(r.diffuse[0], 0), D::var(r.diffuse[1], 1), D::var(r.diffuse[2], 2));
+    {
+        const V3<D> d = m.diffuse;
+        const V3<D> xyz = v3(fmx(D(0.0), D(0.412453f) * d.x + D(0.357580f) * d.y + D(0.180423f) * d.z),
+                             fmx(D(0.0), D(0.212671f) * d.x + D(0.715160f) * d.y + D(0.072169f) * d.z),
+                             fmx(D(0.0), D(0.019334f) * d.x + D(0.119193f) * d.y + D(0.950227f) * d.z));
+        if (xyz.y > 0) {
+            const V3<D> x = xyz * (D(1.0) / xyz.y);
+            m.tint = v3(fmx(D(0.0), D(3.240479f) * x.x - D(1.537150f) * x.y - D(0.498535f) * x.z),
+                        fmx(D(0.0), D(-0.969256f) * x.x + D(1.875992f) * x.y + D(0.041556f) * x.z),
+                        fmx(D(0.0), D(0.055648f) * x.x - D(0.204043f) * x.y + D(1.057311f) * x.z));
+        } else {
+            m.tint = v3s(D(1.0));
+        }
+        m.luminance = xyz.y;
+    }
+    m.roughness = D::var(r.roughness, 3);
+    m.metallic = D::var(r.metallic, 4);
+    m.specular = D::var(r.specular, 5);
+    const V3<D> o = v3(D(double(wo.x)), D(double(wo.y)), D(double(wo.z)));
+    const V3<D> i = v3(D(double(wi.x)), D(double(wi.y)), D(double(wi.z)));
+    if (r.closure == TR_CLOSURE_DIFFUSE)
+        return m.diffuse * K<D>::RcpPi;
+    if (r.closure != TR_CLOSURE_DISNEY)
+        return v3s(D(0.0));
+    return d_evaluate<D, false>(o, i, m).Tv;
+}
+
+template <class T>
+void adjoint_path(const orc_scene& S, const tr_camera& cam, T tanFov2, const tr_kernel_settings& st, uint32_t W,
+                  uint32_t H, uint32_t sampleCount, uint32_t pathIx, const double delta[3], double* grads)
+{
+    const uint32_t wh = W * H;
+    const uint32_t pixel = pathIx % wh;
+    V3<T> O, D;
+    T Tv;
+    {
+        CounterRng rng{pixel, sampleCount + pathIx / wh, 0u, st.seed};
+        camera_ray<T>(cam, tanFov2, W, H, pixel % W, pixel / W, rng, O, D, Tv);
+    }
+    V3<T> Tp = v3s(Tv);
+    T extendPdf = 1;
+    uint32_t flags = 0;
+    const T eps = T(st.ray_epsilon);
+    std::vector<VertexRec<T>> verts;
+    for (uint32_t b = 0; b < st.max_depth; ++b) {
+        T tmax = T(kDstMax);
+        uint32_t prim = 0xffffffffu;
+        T bu = 0, bv = 0;
+        const T Oa[3] = {O.x, O.y, O.z}, Da[3] = {D.x, D.y, D.z};
+        if (!trace<T>(S, Oa, Da, eps, tmax, false, prim, bu, bv)) {
+            prim = 0xffffffffu;
+            tmax = T(kDstMax);
+        }
+        T u16 = 0, v16 = 0;
+        if (prim != 0xffffffffu) {
+            const uint32_t eb = encode_bary(float(bu), float(bv));
+            u16 = decode16<T>(eb >> 16);
+            v16 = decode16<T>(eb & 0xFFFFu);
+        }
+        CounterRng rng{pixel, sampleCount + pathIx / wh, b + 1u, st.seed};
+        VertexRec<T> vr;
+        vr.so = shade_one<T, false>(S, st, b, O, D, Tp, extendPdf, pathIx, flags, prim, u16, v16, tmax, rng);
+        if (vr.so.sh) {
+            T smax = vr.so.shDist - T(2) * eps;
+            uint32_t p2 = 0;
+            T a, c;
+            const T So[3] = {vr.so.shO.x, vr.so.shO.y, vr.so.shO.z}, Sd[3] = {vr.so.shL.x, vr.so.shL.y, vr.so.shL.z};
+            vr.visible = !trace<T>(S, So, Sd, eps, smax, true, p2, a, c);
+            if (vr.visible)
+                vr.cNee = vr.so.shT;
+        }
+        verts.push_back(vr);
+        if (!vr.so.ext)
+            break;
+        O = vr.so.extO;
+        D = vr.so.extD;
+        Tp = vr.so.extT;
+        extendPdf = vr.so.extPdf;
+        flags = vr.so.extPacked & 15u;
+    }
+    // suffix sums of the contributions after each vertex
+    const size_t n = verts.size();
+    std::vector<V3<double>> after(n + 1, v3(0.0, 0.0, 0.0));
+    for (size_t k = n; k-- > 0;) {
+        const V3<T>& a = verts[k].so.add;
+        after[k] = after[k + 1] + v3(double(a.x) + double(verts[k].cNee.x), double(a.y) + double(verts[k].cNee.y),
+                                     double(a.z) + double(verts[k].cNee.z));
+    }
+    for (size_t k = 0; k < n; ++k) {
+        const VertexRec<T>& vr = verts[k];
+        if (!vr.so.hit)
+            break;
+        double* g = grads + size_t(vr.so.matIx) * 9;
+        if (vr.so.emissive) {
+            // emission = Emissive * diffuse (CudaMaterial.h:158): linear in both
+            const MatRaw& mr = S.mats[vr.so.matIx];
+            const double C[3] = {double(vr.so.add.x), double(vr.so.add.y), double(vr.so.add.z)};
+            for (int c = 0; c < 3; ++c) {
+                if (mr.emissive[c] > 0)
+                    g[6 + c] += delta[c] * C[c] / double(mr.emissive[c]);
+                if (mr.diffuse[c] > 0)
+                    g[c] += delta[c] * C[c] / double(mr.diffuse[c]);
+            }
+            break;
+        }
+        auto accumulate = [&](const V3<T>& wi, const double w[3]) {
+            const V3<DualT<double>> f = dual_value<T>(S, vr.so.matIx, vr.so.wo, wi);
+            const DualT<double>* fc[3] = {&f.x, &f.y, &f.z};
+            for (int c = 0; c < 3; ++c)
+                if (w[c] != 0.0 && fc[c]->v != 0.0)
+                    for (int p = 0; p < kDP; ++p)
+                        g[p] += w[c] * fc[c]->d[p] / fc[c]->v;
+        };
+        if (vr.visible) {
+            const double w[3] = {delta[0] * double(vr.cNee.x), delta[1] * double(vr.cNee.y),
+                                 delta[2] * double(vr.cNee.z)};
+            accumulate(vr.so.wiLight, w);
+            if (vr.so.lightIx >= 0) {
+                const Light& L = S.lights[size_t(vr.so.lightIx)];
+                double* ge = grads + size_t(S.matIdx[size_t(L.triIx)]) * 9;
+                for (int c = 0; c < 3; ++c)
+                    if (L.radiance[c] > 0)
+                        ge[6 + c] += w[c] / double(L.radiance[c]);
+            }
+        }
+        if (vr.so.ext) {
+            const double w[3] = {delta[0] * after[k + 1].x, delta[1] * after[k + 1].y, delta[2] * after[k + 1].z};
+            accumulate(vr.so.wiExt, w);
+        }
+    }
+}
+
 } // namespace
 
 extern "C" {
@@ -1420,6 +1652,7 @@ orc_scene* orc_scene_create(const tr_scene_desc* desc)
         const V3<float> em = v3(md.emissive[0], md.emissive[1], md.emissive[2]);
         if (em.x + em.y + em.z > kEps) {
             Light L{};
+            L.triIx = t;
             for (int a = 0; a < 3; ++a) {
                 L.V0[a] = tr.v[0][a];
                 L.V1[a] = tr.v[1][a];
@@ -1431,7 +1664,7 @@ orc_scene* orc_scene_create(const tr_scene_desc* desc)
             L.N[2] = ln.z;
             const float a = length(p[1] - p[0]), b = length(p[2] - p[1]), c = length(p[0] - p[2]);
             const float s = (a + b + c) * .5f;
-            L.area = std::sqrt(s * (s - a) * (s - b) * (s - c));
+            L.area = msqrt(s * (s - a) * (s - b) * (s - c));
             L.radiance[0] = em.x;
             L.radiance[1] = em.y;
             L.radiance[2] = em.z;
@@ -1525,7 +1758,7 @@ uint32_t orc_ties(const orc_scene* s, const float* O, const float* D, float tmin
     for (uint32_t p = 0; p < s->tris.size(); ++p) {
         float tt, u, v;
         if (tri_test_f(&s->geo[9 * size_t(p)], O, D, tmin, kDstMax, tt, u, v) &&
-            std::fabs(tt - t) <= rel * std::fabs(t)) {
+            mfabs(tt - t) <= rel * mfabs(t)) {
             if (count < max_out)
                 prims[count] = p;
             ++count;
@@ -1706,6 +1939,68 @@ void orc_closure(int type, int reference, int use_double, const float* in, float
         run(0.0);
     else
         run(0.0f);
+}
+
+int orc_adjoint(const orc_scene* s, const tr_camera* cam, const tr_kernel_settings* st, uint32_t width,
+                uint32_t height, uint32_t sample_count, const float* pixel_grad, float scale, int use_double,
+                int threads, double* grads)
+{
+    if (st->flags & TR_FLAG_REFERENCE_SAMPLING)
+        return 1;
+    const uint32_t wh = width * height;
+    const uint32_t n = wh * st->multi_sample;
+    const size_t m = s->mats.size() * 9;
+    const unsigned hw = std::max(1u, std::thread::hardware_concurrency());
+    const unsigned nt = threads > 0 ? unsigned(threads) : hw;
+    std::vector<std::vector<double>> partial(nt, std::vector<double>(m, 0.0));
+    std::atomic<uint32_t> next{0};
+    const float tanFov2f = std::tan(cam->fov / 2.0f);
+    auto worker = [&](unsigned t) {
+        while (true) {
+            const uint32_t chunk = next.fetch_add(256);
+            if (chunk >= n)
+                break;
+            for (uint32_t p = chunk; p < std::min(n, chunk + 256); ++p) {
+                const uint32_t px = p % wh;
+                const double delta[3] = {double(pixel_grad[4 * px]) * scale, double(pixel_grad[4 * px + 1]) * scale,
+                                         double(pixel_grad[4 * px + 2]) * scale};
+                if (delta[0] == 0 && delta[1] == 0 && delta[2] == 0)
+                    continue;
+                if (use_double)
+                    adjoint_path<double>(*s, *cam, double(tanFov2f), *st, width, height, sample_count, p, delta,
+                                         partial[t].data());
+                else
+                    adjoint_path<float>(*s, *cam, tanFov2f, *st, width, height, sample_count, p, delta,
+                                        partial[t].data());
+            }
+        }
+    };
+    std::vector<std::thread> pool;
+    for (unsigned t = 1; t < nt; ++t)
+        pool.emplace_back(worker, t);
+    worker(0);
+    for (auto& th : pool)
+        th.join();
+    for (size_t k = 0; k < m; ++k) {
+        double acc = 0.0;
+        for (unsigned t = 0; t < nt; ++t)
+            acc += partial[t][k];
+        grads[k] += acc;
+    }
+    return 0;
+}
+
+void orc_closure_value_grad(const orc_scene* s, uint32_t material, const float* wo, const float* wi, double* out)
+{
+    const V3<double> o = v3(double(wo[0]), double(wo[1]), double(wo[2]));
+    const V3<double> i = v3(double(wi[0]), double(wi[1]), double(wi[2]));
+    const V3<DualT<double>> f = dual_value<double>(*s, material, o, i);
+    const DualT<double>* fc[3] = {&f.x, &f.y, &f.z};
+    for (int c = 0; c < 3; ++c) {
+        out[7 * c] = fc[c]->v;
+        for (int p = 0; p < kDP; ++p)
+            out[7 * c + 1 + p] = fc[c]->d[p];
+    }
 }
 
 void orc_set_reference_draw_order(int right_to_left) { g_refRightToLeft = right_to_left != 0; }

@@ -93,6 +93,21 @@ int orc_render(const orc_scene* s, const tr_camera* cam, const tr_kernel_setting
  * shadow T[3], pdf, 0, 0. */
 void orc_closure(int type, int reference, int use_double, const float* in, float* out);
 
+/* Path-replay gradient (default sampling mode) of the frame with the given
+ * sample_count: adds to grads (material_count x 9 doubles: base colour rgb,
+ * roughness, metallic, specular, emission rgb) the gradient of a loss whose
+ * derivative with respect to each path's radiance is scale * pixel_grad[pixel]
+ * (float4 per pixel). use_double selects the FP64 instantiation. Returns 0,
+ * or 1 for the reference sampling mode (not differentiated). */
+int orc_adjoint(const orc_scene* s, const tr_camera* cam, const tr_kernel_settings* st, uint32_t width,
+                uint32_t height, uint32_t sample_count, const float* pixel_grad, float scale, int use_double,
+                int threads, double* grads);
+
+/* Closure value of a scene material at tangent-space (wo, wi) in the default
+ * mode with its derivatives: out[7c] = f_c, out[7c+1+p] = d f_c / d param p
+ * (base colour rgb, roughness, metallic, specular), c = 0..2. */
+void orc_closure_value_grad(const orc_scene* s, uint32_t material, const float* wo, const float* wi, double* out);
+
 /* Random numbers of the counter-based stream (testing): the first n draws
  * of (pixel, sample, bounce, seed). */
 void orc_counter_rng(uint32_t pixel, uint32_t sample, uint32_t bounce, uint32_t seed, uint32_t n, float* out);

@@ -184,6 +184,8 @@ FUNCTIONS = {
     "tr_copy_from_device": (C.c_int, [_V, _V, _V, C.c_uint64]),
     "tr_copy_to_device": (C.c_int, [_V, _V, _V, C.c_uint64]),
     "tr_trace_host": (C.c_int, [C.POINTER(SceneDesc), _V, _V, _U, C.c_float, C.c_int32, _V, _V]),
+    "tr_update_materials": (C.c_int, [_V, C.POINTER(MaterialDesc), _U]),
+    "tr_adjoint_frame": (C.c_int, [_V, _V, _V, C.c_float, _V]),
 }
 
 LIB_PATH = Path(__file__).resolve().parent / "libtrayracer.so"

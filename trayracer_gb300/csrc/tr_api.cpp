@@ -51,6 +51,10 @@ struct Context {
     DeviceArena sceneArena;
     SceneView scene{};
     tr_scene_info info{};
+    // host copies kept for material updates without a BVH rebuild
+    std::vector<LightTri> hostLights;
+    std::vector<uint32_t> hostMatIdx;
+    uint32_t materialCount = 0;
 
     // settings / camera
     Settings settings{};
@@ -425,10 +429,93 @@ tr_status tr_scene_upload(void* ctx, const tr_scene_desc* desc)
     in.upload_time_ms = std::chrono::duration<float, std::milli>(t2 - t1).count();
     for (int i = 0; i < 6; ++i)
         in.scene_bounds[i] = fs.bounds[i];
+    c->hostLights = fs.lights;
+    c->hostMatIdx = fs.matIdx;
+    c->materialCount = desc->material_count;
     c->hasScene = true;
     c->sampleCount = 0;
     if (c->frame.sampleCount)
         cudaMemset(c->frame.sampleCount, 0, sizeof(uint32_t));
+    return TR_OK;
+}
+
+tr_status tr_update_materials(void* ctx, const tr_material_desc* materials, uint32_t count)
+{
+    if (!ctx)
+        return TR_ERR_INVALID_ARGUMENT;
+    Context* c = static_cast<Context*>(ctx);
+    if (!c->hasScene)
+        return fail(c, TR_ERR_NO_SCENE, "no scene uploaded");
+    if (!materials || count != c->materialCount)
+        return fail(c, TR_ERR_INVALID_ARGUMENT, "material count differs from the uploaded scene");
+    for (uint32_t i = 0; i < count; ++i)
+        if (materials[i].closure > TR_CLOSURE_DISNEY)
+            return fail(c, TR_ERR_INVALID_ARGUMENT, "unknown closure");
+    // the emissive triangles must stay the same set: only their radiance may change
+    size_t emissiveTris = 0;
+    for (uint32_t m : c->hostMatIdx) {
+        const tr_material_desc& d = materials[m];
+        if (d.emissive[0] + d.emissive[1] + d.emissive[2] > kEpsilon)
+            ++emissiveTris;
+    }
+    if (emissiveTris != c->hostLights.size())
+        return fail(c, TR_ERR_INVALID_ARGUMENT, "the set of emissive triangles changed: upload the scene again");
+    std::vector<Material> mats(count);
+    for (uint32_t i = 0; i < count; ++i)
+        mats[i] = resolve_material(materials[i]);
+    std::vector<LightTri> lights = c->hostLights;
+    std::vector<double> energies(lights.size());
+    float sumEnergy = 0.f;
+    for (size_t i = 0; i < lights.size(); ++i) {
+        LightTri& lt = lights[i];
+        const tr_material_desc& d = materials[c->hostMatIdx[size_t(lt.triIx)]];
+        if (!(d.emissive[0] + d.emissive[1] + d.emissive[2] > kEpsilon))
+            return fail(c, TR_ERR_INVALID_ARGUMENT, "the set of emissive triangles changed: upload the scene again");
+        lt.radiance = make_float3(d.emissive[0], d.emissive[1], d.emissive[2]);
+        const float3 e = lt.radiance * lt.area;
+        lt.energy = e.x + e.y + e.z;
+        lt.sumEnergy = sumEnergy;
+        sumEnergy += lt.energy;
+        energies[i] = double(lt.energy);
+    }
+    const std::vector<AliasEntry> alias = build_alias_table(energies);
+    cudaSetDevice(c->device);
+    if (c->stream)
+        TR_CUDA(c, cudaStreamSynchronize(c->stream));
+    TR_CUDA(c, cudaMemcpy(const_cast<Material*>(c->scene.materials), mats.data(), mats.size() * sizeof(Material),
+                          cudaMemcpyHostToDevice));
+    if (!lights.empty()) {
+        TR_CUDA(c, cudaMemcpy(const_cast<LightTri*>(c->scene.lights), lights.data(), lights.size() * sizeof(LightTri),
+                              cudaMemcpyHostToDevice));
+        TR_CUDA(c, cudaMemcpy(const_cast<AliasEntry*>(c->scene.alias), alias.data(), alias.size() * sizeof(AliasEntry),
+                              cudaMemcpyHostToDevice));
+    }
+    c->hostLights = lights;
+    c->scene.lightEnergy = lights.empty() ? 0.f : lights.back().sumEnergy;
+    c->scene.lightEnergyTotal = sumEnergy;
+    c->info.light_energy = sumEnergy;
+    invalidate_graph(c);  // light energies are kernel parameters
+    return tr_reset(ctx);
+}
+
+tr_status tr_adjoint_frame(void* ctx, void* stream, const float* pixel_grad, float scale, float* param_grad)
+{
+    if (!ctx)
+        return TR_ERR_INVALID_ARGUMENT;
+    Context* c = static_cast<Context*>(ctx);
+    if (!pixel_grad || !param_grad)
+        return fail(c, TR_ERR_INVALID_ARGUMENT, "null gradient buffer");
+    if (c->settings.flags & TR_FLAG_REFERENCE_SAMPLING)
+        return fail(c, TR_ERR_INVALID_ARGUMENT, "the adjoint differentiates the default sampling mode only");
+    tr_status st = check_ready(c);
+    if (st != TR_OK)
+        return st;
+    if (c->sampleCount < c->settings.multiSample)
+        return fail(c, TR_ERR_NOT_READY, "render a frame before its adjoint");
+    cudaSetDevice(c->device);
+    const uint32_t sc = c->sampleCount - c->settings.multiSample;
+    TR_CUDA(c, launch_adjoint(c->scene, c->frame, c->camera, c->settings, reinterpret_cast<const float4*>(pixel_grad),
+                              scale, param_grad, sc, c->shape, pick_stream(c, stream)));
     return TR_OK;
 }
 

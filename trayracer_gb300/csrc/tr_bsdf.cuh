@@ -13,10 +13,14 @@
 //     output, so a sheen lobe replaces the diffuse value (Disney.h:416-422);
 //   * Disney::Sample feeds the lobe-selection number r0 unchanged to the
 //     chosen lobe (Disney.h:491-521) and leaves clearcoat out of the pdf
-//     (Disney.h:549-556).
+//     (Disney.h:549-556);
+//   * a sample of the sheen, GGX or clearcoat lobe is flagged specular
+//     (Disney.h:502,512,520), which skips NEE at this vertex and MIS at the
+//     next emissive hit.
 // REF = false sums all lobe values, rescales r0 into the chosen lobe's
-// interval and includes the clearcoat pdf. Values the reference leaves unset
-// on early returns are zero here in both modes.
+// interval, includes the clearcoat pdf and flags no Disney lobe as specular
+// (none is a delta lobe), so NEE and BSDF sampling always combine by MIS.
+// Values the reference leaves unset on early returns are zero in both modes.
 #pragma once
 
 #include "tr_device.h"
@@ -494,7 +498,7 @@ __device__ __forceinline__ Lobe sample(const float3& wo, const HitMat& mat, floa
         cpdf = sheen_eval(mat, wo, wi, value);
         prob = ws * cpdf;
         ws = 0;
-        flags |= kFlagSpecular;
+        flags |= REF ? kFlagSpecular : 0u;
     } else if (r0 < csp) {
         const float u = REF ? r0 : fminf_((r0 - cs) / wsp, 0.99999994f);
         float ax, ay;
@@ -502,13 +506,13 @@ __device__ __forceinline__ Lobe sample(const float3& wo, const HitMat& mat, floa
         ggx_sample(ax, ay, mat, u, r1, wo, wi, cpdf, value);
         prob = wsp * cpdf;
         wsp = 0;
-        flags |= kFlagSpecular;
+        flags |= REF ? kFlagSpecular : 0u;
     } else {
         const float u = REF ? r0 : fminf_((r0 - csp) / wc, 0.99999994f);
         gtr1_sample(clearcoat_alpha(mat), mat, u, r1, wo, wi, cpdf, value);
         prob = wc * cpdf;
         wc = 0;
-        flags |= kFlagSpecular;
+        flags |= REF ? kFlagSpecular : 0u;
     }
     if (wd > 0) {
         float3 v;

@@ -18,6 +18,7 @@
 #include "tr_kernels.h"
 
 #include "tr_bsdf.cuh"
+#include "tr_bsdf_dual.cuh"
 #include "tr_rng.h"
 #include "tr_traverse.cuh"
 
@@ -269,8 +270,9 @@ __global__ void __launch_bounds__(128) extend_kernel(SceneView s, FrameView f, S
 template <bool REF, class Rng>
 __device__ __forceinline__ float3 sample_light(const SceneView& s, Rng& rng, bool rtl, const float3& I,
                                                const float3& N, float& prob, float& pdf, float3& radiance,
-                                               float& dist)
+                                               float& dist, int32_t& lightOut)
 {
+    lightOut = -1;
     const float total = REF ? s.lightEnergy : s.lightEnergyTotal;
     if (total == 0 || s.lightCount == 0) {
         prob = 0;
@@ -327,6 +329,7 @@ __device__ __forceinline__ float3 sample_light(const SceneView& s, Rng& rng, boo
         const float su = sqrtf(r0);
         P = ((1.f - su) * L.V0) + ((su * (1.f - r1)) * L.V1) + ((su * r1) * L.V2);
     }
+    lightOut = lightIx;
     const LightTri& L = s.lights[lightIx];
     float3 Ld = I - P;
     const float sqDist = dot(Ld, Ld);
@@ -432,11 +435,28 @@ __device__ __forceinline__ HitMat load_material(const Material* __restrict__ mat
     return m;
 }
 
+// What the path-replay adjoint needs to know about one shaded vertex.
+struct VertexInfo {
+    bool hit;
+    bool emissive;
+    float3 emitted;       // radiance added at an emissive hit (after SafeColor)
+    uint32_t matIx;
+    uint32_t closure;
+    HitMat mat;
+    float3 wo;            // tangent space
+    float3 wiLight;
+    float3 wiExt;
+    int32_t lightIx;
+};
+
+// One PathTracingKernel step (PathTracing.h:15-174) for one queue entry. With
+// vi == nullptr (the shade kernel) it adds emitted radiance and writes the
+// guide buffers; the adjoint replay passes vi and gets the vertex instead.
 template <bool REF, class Rng>
 __device__ __forceinline__ void shade_path(const SceneView& s, const FrameView& f, const Settings& st, uint32_t bounce,
                                            uint32_t sc, const float4& O4, const float4& D4, const float4& T4,
                                            const uint4& hd, Rng& rng, bool& wantExt, float4 (&ext)[3],
-                                           bool& wantShadow, float4 (&sh)[3])
+                                           bool& wantShadow, float4 (&sh)[3], VertexInfo* vi = nullptr)
 {
     const uint32_t wh = f.resX * f.resY;
     const float3 O = f3(O4), D = f3(D4), T = f3(T4);
@@ -445,7 +465,12 @@ __device__ __forceinline__ void shade_path(const SceneView& s, const FrameView& 
     uint32_t flags = path_flags(data);
     const float extendPdf = T4.w;
     const uint32_t pixelIx = pathIx % wh;
-    const bool aov = (st.flags & TR_FLAG_WRITE_AOVS) && bounce == 0 && pathIx < wh;
+    const bool aov = vi == nullptr && (st.flags & TR_FLAG_WRITE_AOVS) && bounce == 0 && pathIx < wh;
+    if (vi) {
+        vi->hit = false;
+        vi->emissive = false;
+        vi->lightIx = -1;
+    }
 
     const float2 bary = decode_bary(hd.x);
     const uint32_t instIx = hd.y, primIx = hd.z;
@@ -464,6 +489,12 @@ __device__ __forceinline__ void shade_path(const SceneView& s, const FrameView& 
     const Surface sf = surface_at(s, instIx, primIx, bary, D);
     uint32_t closure, emissiveFlag;
     const HitMat m = load_material(s.materials, sf.matIx, closure, emissiveFlag);
+    if (vi) {
+        vi->hit = true;
+        vi->matIx = sf.matIx;
+        vi->closure = closure;
+        vi->mat = m;
+    }
     if (aov) {
         f.albedo[pixelIx] = f4(m.diffuse, 0.f);
         f.normals[pixelIx] = f4(sf.N, 0.f);
@@ -490,6 +521,11 @@ __device__ __forceinline__ void shade_path(const SceneView& s, const FrameView& 
         float3 add = safe_color(contrib, st.maxColor);
         if (REF && bounce == 0)
             add += m.emissive;  // the reference adds the primary emission a second time (PathTracing.h:93-97)
+        if (vi) {
+            vi->emissive = true;
+            vi->emitted = add;
+            return;
+        }
         float4 r = f.radiance[pathIx];
         f.radiance[pathIx] = make_float4(r.x + add.x, r.y + add.y, r.z + add.z, r.w);
         return;
@@ -498,11 +534,18 @@ __device__ __forceinline__ void shade_path(const SceneView& s, const FrameView& 
     float lightProb, lightPdf, lightDist;
     float3 lightRadiance;
     const bool rtl = REF && (st.flags & TR_FLAG_REFERENCE_DRAW_RTL) != 0;
-    const float3 L = sample_light<REF>(s, rng, rtl, I, sf.N, lightProb, lightPdf, lightRadiance, lightDist);
+    int32_t lightIx;
+    const float3 L =
+        sample_light<REF>(s, rng, rtl, I, sf.N, lightProb, lightPdf, lightRadiance, lightDist, lightIx);
 
     const float3 wow = -D;
     const float3 wo = normalize(make_float3(dot(wow, sf.T), dot(wow, sf.B), dot(wow, sf.N)));
     const float3 wi = normalize(make_float3(dot(L, sf.T), dot(L, sf.B), dot(L, sf.N)));
+    if (vi) {
+        vi->wo = wo;
+        vi->wiLight = wi;
+        vi->lightIx = lightIx;
+    }
 
     float r0, r1;
     draw2(rng, rtl, r0, r1);
@@ -522,6 +565,8 @@ __device__ __forceinline__ void shade_path(const SceneView& s, const FrameView& 
         sh[2] = f4(safe_color(shadowT, st.maxColor), 0.f);
     }
 
+    if (vi)
+        vi->wiExt = c.extWi;
     if (c.extPdf > kEpsilon) {
         float3 tp = c.extT / fabsf(c.extPdf);
         if (bounce >= st.rrStart) {
@@ -650,6 +695,180 @@ __global__ void __launch_bounds__(256) finalize_kernel(FrameView f, Settings st)
     f.colors[p] = make_float4(acc.x / n, acc.y / n, acc.z / n, acc.w / n);
 }
 
+// Gradient atomics: lanes with the same key (material) sum their values
+// first; one lane per key adds the sums. key == ~0: nothing to add.
+__device__ __forceinline__ void warp_add_grads(float* __restrict__ grads, uint32_t key, const float (&g)[kGradSlots],
+                                               int first, int last)
+{
+    const uint32_t peers = __match_any_sync(kFull, key);
+    const uint32_t lane = lane_id();
+    float sum[kGradSlots];
+    if (peers == kFull) {
+#pragma unroll
+        for (int k = 0; k < kGradSlots; ++k) {
+            float v = (k >= first && k < last) ? g[k] : 0.f;
+#pragma unroll
+            for (int o = 16; o > 0; o >>= 1)
+                v += __shfl_xor_sync(kFull, v, o);
+            sum[k] = v;
+        }
+    } else {
+#pragma unroll
+        for (int k = 0; k < kGradSlots; ++k)
+            sum[k] = 0.f;
+        for (int i = 0; i < 32; ++i) {
+            const uint32_t ki = __shfl_sync(kFull, key, i);
+#pragma unroll
+            for (int k = 0; k < kGradSlots; ++k) {
+                const float o = __shfl_sync(kFull, (k >= first && k < last) ? g[k] : 0.f, i);
+                if (ki == key)
+                    sum[k] += o;
+            }
+        }
+    }
+    if (key != 0xffffffffu && lane == __ffs(peers) - 1u) {
+        for (int k = first; k < last; ++k)
+            if (sum[k] != 0.f)
+                atomicAdd(grads + size_t(key) * kGradSlots + k, sum[k]);
+    }
+}
+
+// Path-replay adjoint of one frame (default sampling mode): every path is
+// replayed from its random keys, re-tracing its extend and shadow rays; at
+// each vertex the derivative of the closure value (dual numbers) is weighted
+// by the radiance that reached the camera through that value: the vertex's
+// own NEE contribution for the light direction, and the radiance still to
+// come (the path's total minus what was already accounted for) for the
+// extend direction. Emission gradients come from emissive hits and NEE.
+__global__ void __launch_bounds__(128) adjoint_kernel(SceneView s, FrameView f, Camera cam, Settings st,
+                                                      const float4* __restrict__ pixelGrad, float scale,
+                                                      float* __restrict__ grads, uint32_t sc)
+{
+    const uint32_t wh = f.resX * f.resY;
+    const uint32_t lane = lane_id();
+    const uint32_t warpGlobal = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+    const uint32_t warpStride = (gridDim.x * blockDim.x) >> 5;
+    for (uint32_t base = warpGlobal * 32u; base < f.pathCount; base += warpStride * 32u) {
+        const uint32_t pathIx = base + lane;
+        bool alive = false;
+        float3 delta = f3(0.f), lrem = f3(0.f);
+        float4 O4 = make_float4(0.f, 0.f, 0.f, 0.f), D4 = O4, T4 = O4;
+        uint32_t pixel = 0, sampleIx = 0;
+        if (pathIx < f.pathCount) {
+            pixel = pathIx % wh;
+            sampleIx = pathIx / wh;
+            const float4 pg = pixelGrad[pixel];
+            delta = make_float3(pg.x * scale, pg.y * scale, pg.z * scale);
+            const float4 rad = f.radiance[pathIx];
+            lrem = f3(rad);
+            alive = (delta.x != 0.f || delta.y != 0.f || delta.z != 0.f) &&
+                    (lrem.x != 0.f || lrem.y != 0.f || lrem.z != 0.f);
+            if (alive) {
+                CounterRng rng;
+                rng.init(pixel, sc + sampleIx, 0u, st.seed);
+                float3 O, D;
+                float T;
+                camera_ray(cam, f.resX, f.resY, pixel % f.resX, pixel / f.resX, rng, false, O, D, T);
+                O4 = f4(O, __uint_as_float(pack_path(pathIx, 0)));
+                D4 = f4(D, 0.f);
+                T4 = make_float4(T, T, T, 1.f);
+            }
+        }
+        for (uint32_t b = 0; b < st.maxDepth; ++b) {
+            float g[kGradSlots], ge[kGradSlots];
+#pragma unroll
+            for (int k = 0; k < kGradSlots; ++k)
+                g[k] = ge[k] = 0.f;
+            uint32_t key = 0xffffffffu, keyE = 0xffffffffu;
+            if (alive) {
+                float tmax = kDstMax;
+                uint32_t slot = 0xffffffffu;
+                float u = 0.f, v = 0.f;
+                if (!traverse<false>(s, f3(O4), f3(D4), st.rayEpsilon, tmax, slot, u, v))
+                    atomicOr(f.errorFlag, 1u);
+                uint4 hd;
+                if (slot != 0xffffffffu)
+                    hd = make_uint4(encode_bary(u, v), 0u, __float_as_uint(__ldg(s.bvhTris + 3u * slot).w),
+                                    __float_as_uint(tmax));
+                else
+                    hd = make_uint4(0u, 0xffffffffu, 0xffffffffu, __float_as_uint(kDstMax));
+                CounterRng rng;
+                rng.init(pixel, sc + sampleIx, b + 1u, st.seed);
+                VertexInfo vi;
+                bool wantExt = false, wantShadow = false;
+                float4 ext[3], sh[3];
+                shade_path<false>(s, f, st, b, sc, O4, D4, T4, hd, rng, wantExt, ext, wantShadow, sh, &vi);
+                if (!vi.hit) {
+                    alive = false;
+                } else if (vi.emissive) {
+                    const float C[3] = {vi.emitted.x, vi.emitted.y, vi.emitted.z};
+                    const float E[3] = {vi.mat.emissive.x, vi.mat.emissive.y, vi.mat.emissive.z};
+                    const float dl[3] = {delta.x, delta.y, delta.z};
+                    const float Dc[3] = {vi.mat.diffuse.x, vi.mat.diffuse.y, vi.mat.diffuse.z};
+                    // emission = Emissive * diffuse (CudaMaterial.h:158): linear in both
+                    for (int c = 0; c < 3; ++c) {
+                        if (E[c] > 0.f)
+                            ge[kGEmR + c] = dl[c] * C[c] / E[c] * Dc[c];
+                        if (Dc[c] > 0.f)
+                            g[kGBaseR + c] = dl[c] * C[c] / Dc[c];
+                    }
+                    keyE = vi.matIx;
+                    key = vi.matIx;
+                    lrem = lrem - vi.emitted;
+                    alive = false;
+                } else {
+                    if (wantShadow) {
+                        float smax = sh[1].w - (2 * st.rayEpsilon);
+                        uint32_t occ = 0xffffffffu;
+                        float su, sv;
+                        if (!traverse<true>(s, f3(sh[0]), f3(sh[1]), st.rayEpsilon, smax, occ, su, sv))
+                            atomicOr(f.errorFlag, 1u);
+                        if (occ == 0xffffffffu) {
+                            const float3 C = f3(sh[2]);
+                            lrem = lrem - C;
+                            const Vec3<Dual> fv = dual::closure_value(vi.closure, vi.mat, vi.wo, vi.wiLight);
+                            const Dual* fc[3] = {&fv.x, &fv.y, &fv.z};
+                            const float w[3] = {delta.x * C.x, delta.y * C.y, delta.z * C.z};
+                            for (int c = 0; c < 3; ++c)
+                                if (w[c] != 0.f && fc[c]->v != 0.f)
+                                    for (int k = 0; k < kGradParams; ++k)
+                                        g[k] += w[c] * fc[c]->d[k] / fc[c]->v;
+                            key = vi.matIx;
+                            if (vi.lightIx >= 0) {
+                                const LightTri& Lt = s.lights[vi.lightIx];
+                                const float E[3] = {Lt.radiance.x, Lt.radiance.y, Lt.radiance.z};
+                                for (int c = 0; c < 3; ++c)
+                                    if (E[c] > 0.f)
+                                        ge[kGEmR + c] = w[c] / E[c];
+                                keyE = __ldg(s.matIdx + Lt.triIx);
+                            }
+                        }
+                    }
+                    if (wantExt) {
+                        const Vec3<Dual> fv = dual::closure_value(vi.closure, vi.mat, vi.wo, vi.wiExt);
+                        const Dual* fc[3] = {&fv.x, &fv.y, &fv.z};
+                        const float w[3] = {delta.x * lrem.x, delta.y * lrem.y, delta.z * lrem.z};
+                        for (int c = 0; c < 3; ++c)
+                            if (w[c] != 0.f && fc[c]->v != 0.f)
+                                for (int k = 0; k < kGradParams; ++k)
+                                    g[k] += w[c] * fc[c]->d[k] / fc[c]->v;
+                        key = vi.matIx;
+                        O4 = ext[0];
+                        D4 = ext[1];
+                        T4 = ext[2];
+                    } else {
+                        alive = false;
+                    }
+                }
+            }
+            warp_add_grads(grads, key, g, 0, kGradParams);
+            warp_add_grads(grads, keyE, ge, kGEmR, kGradSlots);
+            if (!__any_sync(kFull, alive))
+                break;
+        }
+    }
+}
+
 __global__ void advance_kernel(FrameView f, Settings st)
 {
     if (threadIdx.x == 0 && blockIdx.x == 0)
@@ -708,6 +927,14 @@ cudaError_t launch_finalize(const FrameView& f, const Settings& st, cudaStream_t
         return cudaSuccess;
     finalize_kernel<<<(wh + 255u) / 256u, 256, 0, stream>>>(f, st);
     advance_kernel<<<1, 32, 0, stream>>>(f, st);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_adjoint(const SceneView& s, const FrameView& f, const Camera& cam, const Settings& st,
+                           const float4* pixelGrad, float scale, float* grads, uint32_t sampleCount,
+                           const LaunchShape& shape, cudaStream_t stream)
+{
+    adjoint_kernel<<<shape.shadeBlocks, 128, 0, stream>>>(s, f, cam, st, pixelGrad, scale, grads, sampleCount);
     return cudaGetLastError();
 }
 

@@ -27,5 +27,8 @@ cudaError_t launch_shade(const SceneView& s, const FrameView& f, const Settings&
 cudaError_t launch_connect(const SceneView& s, const FrameView& f, const Settings& st, uint32_t bounce,
                            const LaunchShape& shape, cudaStream_t stream);
 cudaError_t launch_finalize(const FrameView& f, const Settings& st, cudaStream_t stream);
+cudaError_t launch_adjoint(const SceneView& s, const FrameView& f, const Camera& cam, const Settings& st,
+                           const float4* pixelGrad, float scale, float* grads, uint32_t sampleCount,
+                           const LaunchShape& shape, cudaStream_t stream);
 
 } // namespace tr
