@@ -409,6 +409,8 @@ def main():
                 "compulsory_frac": round(compulsory / peak, 4),
                 "nodes_per_ray": round(cs["traversal_extend_nodes"] / max(1, ext_rays), 3),
                 "tris_per_ray": round(cs["traversal_extend_tris"] / max(1, ext_rays), 3),
+                "connect_nodes_per_ray": round(cs["traversal_connect_nodes"] / max(1, sh_rays), 3),
+                "connect_tris_per_ray": round(cs["traversal_connect_tris"] / max(1, sh_rays), 3),
             },
             "cpu_baseline": cpu,
             "clocks": clocks.summary(),

@@ -202,6 +202,17 @@ class DeviceRenderer:
     def Finalize(self, stream: int = 0):
         self._check(self._lib.tr_finalize(self._ctx, C.c_void_p(stream or None)), "tr_finalize")
 
+    def UpdateMaterials(self, materials: np.ndarray):
+        """tr_update_materials: new material table for the uploaded scene (no BVH rebuild)."""
+        mats = np.ascontiguousarray(materials, MATERIAL_DTYPE)
+        self._check(self._lib.tr_update_materials(self._ctx, C.cast(mats.ctypes.data, C.POINTER(_abi.MaterialDesc)),
+                                                  mats.shape[0]), "tr_update_materials")
+
+    def AdjointFrame(self, pixel_grad_ptr: int, scale: float, param_grad_ptr: int, stream: int = 0):
+        """tr_adjoint_frame on device buffers: pixel gradient (float4 per pixel) -> (materials, 9) gradient."""
+        self._check(self._lib.tr_adjoint_frame(self._ctx, C.c_void_p(stream or None), C.c_void_p(pixel_grad_ptr),
+                                               scale, C.c_void_p(param_grad_ptr)), "tr_adjoint_frame")
+
     def Synchronize(self, stream: int = 0):
         self._check(self._lib.tr_synchronize(self._ctx, C.c_void_p(stream or None)), "tr_synchronize")
 
