@@ -59,6 +59,7 @@ class Oracle:
             lib.orc_ties.argtypes = [_P, _P, _P, C.c_float, C.c_float, C.c_float, _P, _U]
             lib.orc_trace_any.argtypes = [_P, _P, _P, _U, C.c_float, _P]
             lib.orc_shade.argtypes = [_P, _P, _U, _U, _U, _U, _U, _P, _P, _P, _P, _P, _P, _P, _P, _P]
+            lib.orc_shade_fp64.argtypes = [_P, _P, _U, _U, _U, _U, _U, _P, _P, _P, _P, _P, _P, _P, _P, _P]
             lib.orc_render.restype = C.c_int
             lib.orc_render.argtypes = [_P, _P, _P, _U, _U, _U, _U, _U, C.c_int, C.c_int, _P, _P, _P]
             lib.orc_counter_rng.argtypes = [_U, _U, _U, _U, _U, _P]
@@ -122,7 +123,7 @@ class Oracle:
         self._lib.orc_trace_any(self._s, _ptr(O), _ptr(L), O.shape[0], eps, _ptr(occ))
         return occ
 
-    def shade(self, settings, bounce, sample_count, width, height, O, D, T, hits):
+    def shade(self, settings, bounce, sample_count, width, height, O, D, T, hits, fp64=False):
         n = O.shape[0]
         O = np.ascontiguousarray(O, np.float32)
         D = np.ascontiguousarray(D, np.float32)
@@ -134,8 +135,9 @@ class Oracle:
         sv = np.zeros(n, np.uint8)
         rad = np.zeros((n, 4), np.float32)
         st = settings.to_c()
-        self._lib.orc_shade(self._s, C.addressof(st), bounce, sample_count, width, height, n, _ptr(O), _ptr(D),
-                            _ptr(T), _ptr(hits), _ptr(ext), _ptr(ev), _ptr(sh), _ptr(sv), _ptr(rad))
+        fn = self._lib.orc_shade_fp64 if fp64 else self._lib.orc_shade
+        fn(self._s, C.addressof(st), bounce, sample_count, width, height, n, _ptr(O), _ptr(D), _ptr(T), _ptr(hits),
+           _ptr(ext), _ptr(ev), _ptr(sh), _ptr(sv), _ptr(rad))
         return ext, ev.astype(bool), sh, sv.astype(bool), rad
 
     def render(self, cam: CameraSpec, settings, width, height, frames=1, first_pixel=0, pixel_count=None,

@@ -1574,6 +1574,50 @@ void adjoint_path(const orc_scene& S, const tr_camera& cam, T tanFov2, const tr_
     }
 }
 
+template <class T>
+void shade_entries(const orc_scene* s, const tr_kernel_settings* st, uint32_t bounce, uint32_t sc, uint32_t W,
+                   uint32_t H, uint32_t n, const float* O4, const float* D4, const float* T4, const uint32_t* hits,
+                   float* ext, uint8_t* ext_valid, float* sh, uint8_t* sh_valid, float* radiance_add)
+{
+    const uint32_t wh = W * H;
+    const bool ref = st->flags & TR_FLAG_REFERENCE_SAMPLING;
+    for (uint32_t i = 0; i < n; ++i) {
+        const V3<T> O = v3(T(O4[4 * i]), T(O4[4 * i + 1]), T(O4[4 * i + 2]));
+        const V3<T> D = v3(T(D4[4 * i]), T(D4[4 * i + 1]), T(D4[4 * i + 2]));
+        const V3<T> Tp = v3(T(T4[4 * i]), T(T4[4 * i + 1]), T(T4[4 * i + 2]));
+        const T extendPdf = T(T4[4 * i + 3]);
+        const uint32_t data = f2u(O4[4 * i + 3]);
+        const uint32_t pathIx = data >> 4, flags = data & 15u;
+        const uint32_t* h = hits + 4 * size_t(i);
+        const T bu = decode16<T>(h[0] >> 16), bv = decode16<T>(h[0] & 0xFFFFu);
+        const T tmax = T(u2f(h[3]));
+        ShadeOut<T> so;
+        if (ref) {
+            RefRng rng{tea2(st->seed + pathIx, sc + bounce + 1u)};
+            so = shade_one<T, true>(*s, *st, bounce, O, D, Tp, extendPdf, pathIx, flags, h[2], bu, bv, tmax, rng);
+        } else {
+            CounterRng rng{pathIx % wh, sc + pathIx / wh, bounce + 1u, st->seed};
+            so = shade_one<T, false>(*s, *st, bounce, O, D, Tp, extendPdf, pathIx, flags, h[2], bu, bv, tmax, rng);
+        }
+        ext_valid[i] = so.ext;
+        sh_valid[i] = so.sh;
+        float* e = ext + 12 * size_t(i);
+        const float ev[12] = {float(so.extO.x), float(so.extO.y), float(so.extO.z), u2f(so.extPacked),
+                              float(so.extD.x), float(so.extD.y), float(so.extD.z), u2f(so.extNormal),
+                              float(so.extT.x), float(so.extT.y), float(so.extT.z), float(so.extPdf)};
+        std::memcpy(e, ev, sizeof(ev));
+        float* q = sh + 12 * size_t(i);
+        const float sv[12] = {float(so.shO.x), float(so.shO.y), float(so.shO.z), u2f(pathIx),
+                              float(so.shL.x), float(so.shL.y), float(so.shL.z), float(so.shDist),
+                              float(so.shT.x), float(so.shT.y), float(so.shT.z), 0.f};
+        std::memcpy(q, sv, sizeof(sv));
+        radiance_add[4 * i] = float(so.add.x);
+        radiance_add[4 * i + 1] = float(so.add.y);
+        radiance_add[4 * i + 2] = float(so.add.z);
+        radiance_add[4 * i + 3] = 0.f;
+    }
+}
+
 } // namespace
 
 extern "C" {
@@ -1783,41 +1827,14 @@ void orc_shade(const orc_scene* s, const tr_kernel_settings* st, uint32_t bounce
                uint32_t n, const float* O4, const float* D4, const float* T4, const uint32_t* hits, float* ext,
                uint8_t* ext_valid, float* sh, uint8_t* sh_valid, float* radiance_add)
 {
-    const uint32_t wh = W * H;
-    const bool ref = st->flags & TR_FLAG_REFERENCE_SAMPLING;
-    for (uint32_t i = 0; i < n; ++i) {
-        const V3<float> O = v3(O4[4 * i], O4[4 * i + 1], O4[4 * i + 2]);
-        const V3<float> D = v3(D4[4 * i], D4[4 * i + 1], D4[4 * i + 2]);
-        const V3<float> Tp = v3(T4[4 * i], T4[4 * i + 1], T4[4 * i + 2]);
-        const float extendPdf = T4[4 * i + 3];
-        const uint32_t data = f2u(O4[4 * i + 3]);
-        const uint32_t pathIx = data >> 4, flags = data & 15u;
-        const uint32_t* h = hits + 4 * size_t(i);
-        const float bu = decode16<float>(h[0] >> 16), bv = decode16<float>(h[0] & 0xFFFFu);
-        const float tmax = u2f(h[3]);
-        ShadeOut<float> so;
-        if (ref) {
-            RefRng rng{tea2(st->seed + pathIx, sc + bounce + 1u)};
-            so = shade_one<float, true>(*s, *st, bounce, O, D, Tp, extendPdf, pathIx, flags, h[2], bu, bv, tmax, rng);
-        } else {
-            CounterRng rng{pathIx % wh, sc + pathIx / wh, bounce + 1u, st->seed};
-            so = shade_one<float, false>(*s, *st, bounce, O, D, Tp, extendPdf, pathIx, flags, h[2], bu, bv, tmax, rng);
-        }
-        ext_valid[i] = so.ext;
-        sh_valid[i] = so.sh;
-        float* e = ext + 12 * size_t(i);
-        const float ev[12] = {so.extO.x, so.extO.y, so.extO.z, u2f(so.extPacked), so.extD.x, so.extD.y,
-                              so.extD.z, u2f(so.extNormal), so.extT.x, so.extT.y, so.extT.z, so.extPdf};
-        std::memcpy(e, ev, sizeof(ev));
-        float* q = sh + 12 * size_t(i);
-        const float sv[12] = {so.shO.x, so.shO.y, so.shO.z, u2f(pathIx), so.shL.x, so.shL.y,
-                              so.shL.z, so.shDist,  so.shT.x, so.shT.y, so.shT.z, 0.f};
-        std::memcpy(q, sv, sizeof(sv));
-        radiance_add[4 * i] = so.add.x;
-        radiance_add[4 * i + 1] = so.add.y;
-        radiance_add[4 * i + 2] = so.add.z;
-        radiance_add[4 * i + 3] = 0.f;
-    }
+    shade_entries<float>(s, st, bounce, sc, W, H, n, O4, D4, T4, hits, ext, ext_valid, sh, sh_valid, radiance_add);
+}
+
+void orc_shade_fp64(const orc_scene* s, const tr_kernel_settings* st, uint32_t bounce, uint32_t sc, uint32_t W,
+                    uint32_t H, uint32_t n, const float* O4, const float* D4, const float* T4, const uint32_t* hits,
+                    float* ext, uint8_t* ext_valid, float* sh, uint8_t* sh_valid, float* radiance_add)
+{
+    shade_entries<double>(s, st, bounce, sc, W, H, n, O4, D4, T4, hits, ext, ext_valid, sh, sh_valid, radiance_add);
 }
 
 int orc_render(const orc_scene* s, const tr_camera* cam, const tr_kernel_settings* st, uint32_t W, uint32_t H,

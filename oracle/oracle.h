@@ -73,6 +73,13 @@ void orc_shade(const orc_scene* s, const tr_kernel_settings* st, uint32_t bounce
                const uint32_t* hits, float* ext, uint8_t* ext_valid, float* sh, uint8_t* sh_valid,
                float* radiance_add);
 
+/* orc_shade computed in double (outputs rounded to float): the conditioning
+ * reference for comparisons of fp32 shading. */
+void orc_shade_fp64(const orc_scene* s, const tr_kernel_settings* st, uint32_t bounce, uint32_t sample_count,
+                    uint32_t width, uint32_t height, uint32_t n, const float* O4, const float* D4, const float* T4,
+                    const uint32_t* hits, float* ext, uint8_t* ext_valid, float* sh, uint8_t* sh_valid,
+                    float* radiance_add);
+
 /* Renders `frames` frames of multi_sample samples for pixels
  * [first_pixel, first_pixel + pixel_count), each path traced depth first with
  * the same per-path random streams as the wavefront. Writes per path the

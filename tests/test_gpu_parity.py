@@ -42,14 +42,9 @@ def read_state(r, buf, k, n):
     return a[:, :n].copy()
 
 
-def sharp_path(scene, hits):
-    """Paths whose hit material has a Disney GGX lobe with alpha < 0.04 (roughness < 0.2)."""
-    prim = hits[:, 2]
-    out = np.zeros(prim.shape[0], bool)
-    valid = prim != 0xFFFFFFFF
-    mats = scene.materials[scene.material_indices[prim[valid]]]
-    out[valid] = (mats["closure"] == tr.TR_CLOSURE_DISNEY) & (mats["roughness"] < 0.2)
-    return out
+def within_conditioning(gpu, o32, o64):
+    """|gpu - fp64| <= 1e-4 max(1, |fp64|) + 4 |fp32 oracle - fp64|, element-wise."""
+    return np.abs(gpu - o64) <= RTOL * np.maximum(1.0, np.abs(o64)) + 4.0 * np.abs(o32 - o64) + 1e-6
 
 
 def check_hits(o, O, D, got, eps):
@@ -111,6 +106,7 @@ def test_stagewise_parity(name):
         sh_gpu = r.read_device(buf["shadow"], np.float32, 3 * n * 4).reshape(3, n, 4)[:, :n_sh]
         rad_gpu = r.read_device(buf["radiance"], np.float32, n * 4).reshape(n, 4)
         ext, ev, sh, sv, add = o.shade(st, b, 0, W, H, state[0], state[1], state[2], hits)
+        ext64, _, sh64, _, _ = o.shade(st, b, 0, W, H, state[0], state[1], state[2], hits, fp64=True)
         path = state[0][:, 3].view(np.uint32) >> 4
 
         # extend rays, matched by path index
@@ -126,12 +122,11 @@ def test_stagewise_parity(name):
         np.testing.assert_array_equal(ext_gpu[0][gi, 3].view(np.uint32), oe[oi, 0, 3].view(np.uint32))
         ok = close(ext_gpu[0][gi, :3], oe[oi, 0, :3]).all(1) & close(ext_gpu[1][gi, :3], oe[oi, 1, :3]).all(1)
         assert ok.mean() >= 0.998, f"bounce {b}: extend ray origins/directions agree for {ok.mean():.4f}"
-        # throughput and pdf: a GGX lobe with alpha = roughness^2 < 0.04 is ill-conditioned in fp32
-        # (fp32 vs fp64 of the same formulas differ by > 1e-4 for most samples), so those paths
-        # get a conditioning-sized tolerance
-        sharp = sharp_path(scene, hits[np.argsort(path)[np.searchsorted(np.sort(path), common)]])
-        okt = np.where(sharp, close(ext_gpu[2][gi], oe[oi, 2], rtol=5e-2).all(1),
-                       close(ext_gpu[2][gi], oe[oi, 2]).all(1))
+        # throughput and pdf: near-specular GGX lobes are ill-conditioned in fp32, so the GPU is
+        # held to the FP64 shading of the same inputs within 1e-4 plus a few times the fp32
+        # oracle's own distance from it
+        oe64 = ext64[ev]
+        okt = within_conditioning(ext_gpu[2][gi], oe[oi, 2], oe64[oi, 2]).all(1)
         assert okt.mean() >= 0.998, f"bounce {b}: extend throughputs agree for {okt.mean():.4f}"
 
         # shadow rays, matched by path index
@@ -144,9 +139,8 @@ def test_stagewise_parity(name):
         gi = np.argsort(gpu_sh_paths)[np.searchsorted(np.sort(gpu_sh_paths), common)]
         osh = sh[sv]
         oi = np.argsort(orc_sh_paths)[np.searchsorted(np.sort(orc_sh_paths), common)]
-        sharp = sharp_path(scene, hits[np.argsort(path)[np.searchsorted(np.sort(path), common)]])
         ok = close(sh_gpu[0][gi, :3], osh[oi, 0, :3]).all(1) & close(sh_gpu[1][gi], osh[oi, 1]).all(1) \
-            & close(sh_gpu[2][gi, :3], osh[oi, 2, :3], rtol=np.where(sharp, 5e-2, 1e-3)[:, None]).all(1)
+            & within_conditioning(sh_gpu[2][gi, :3], osh[oi, 2, :3], sh64[sv][oi, 2, :3]).all(1)
         assert ok.mean() >= 0.998, f"bounce {b}: shadow rays agree for {ok.mean():.4f}"
 
         # radiance added by shade
