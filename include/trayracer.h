@@ -293,6 +293,25 @@ tr_status tr_render_frame(void* ctx, void* stream, int32_t use_graph);
  * not differentiate). */
 tr_status tr_adjoint_frame(void* ctx, void* stream, const float* pixel_grad, float scale, float* param_grad);
 
+/* One frame (as tr_render_frame without a graph) into caller-owned device
+ * buffers, allocating no device memory: for callers that cannot allocate
+ * where they render (a render loop that must not stall the device on
+ * cudaMalloc/cudaFree, a host that owns all device memory through its own
+ * pool). No counterpart in the reference. The frame's scratch (path queues,
+ * hits, per-path radiance, counters) lives in one file-scope device array of
+ * the library (about 22 MiB, held by every GPU that loads the library until
+ * exit), so width * height * multi_sample must not exceed 131072 paths
+ * (TR_ERR_LIMIT otherwise). accumulator (float4 per pixel) is read unless
+ * sample_count is 0 and written; colors (float4 per pixel) = accumulator /
+ * (sample_count + multi_sample). The scene, camera, settings and resolution
+ * come from the context (set up beforehand; tr_scene_upload allocates). The
+ * first call on a device looks up the array's device address (which loads the
+ * library's device image there); make that first call before any stream
+ * capture. Every call shares the array and rewrites what it must start from:
+ * calls that overlap on the GPU (other streams, other threads, other
+ * contexts) race. Guide buffers (TR_FLAG_WRITE_AOVS) are not written. */
+tr_status tr_render_frame_noalloc(void* ctx, void* stream, float* accumulator, float* colors, uint32_t sample_count);
+
 /* ---- results ---- */
 tr_status tr_synchronize(void* ctx, void* stream);
 tr_status tr_get_statistics(void* ctx, tr_statistics* stats);

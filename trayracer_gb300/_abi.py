@@ -186,6 +186,7 @@ FUNCTIONS = {
     "tr_trace_host": (C.c_int, [C.POINTER(SceneDesc), _V, _V, _U, C.c_float, C.c_int32, _V, _V]),
     "tr_update_materials": (C.c_int, [_V, C.POINTER(MaterialDesc), _U]),
     "tr_adjoint_frame": (C.c_int, [_V, _V, _V, C.c_float, _V]),
+    "tr_render_frame_noalloc": (C.c_int, [_V, _V, _V, _V, _U]),
 }
 
 LIB_PATH = Path(__file__).resolve().parent / "libtrayracer.so"

@@ -19,6 +19,7 @@
 #include <vector>
 
 #include "../../include/trayracer.h"
+#include "tr_api_internal.h"
 #include "tr_bvh.h"
 #include "tr_kernels.h"
 #include "tr_scene.h"
@@ -234,6 +235,36 @@ tr_status enqueue_frame(Context* c, cudaStream_t s, bool timed)
 }
 
 } // namespace
+
+namespace tr {
+
+tr_status context_views(void* ctx, ContextViews* out)
+{
+    if (!ctx || !out)
+        return TR_ERR_INVALID_ARGUMENT;
+    Context* c = static_cast<Context*>(ctx);
+    if (!c->hasScene)
+        return fail(c, TR_ERR_NO_SCENE, "no scene uploaded");
+    if (!c->hasCamera)
+        return fail(c, TR_ERR_NOT_READY, "camera not set");
+    if (c->width == 0 || c->height == 0)
+        return fail(c, TR_ERR_NOT_READY, "resolution not set (tr_resize)");
+    out->device = c->device;
+    out->stream = c->stream;
+    out->scene = c->scene;
+    out->camera = c->camera;
+    out->settings = c->settings;
+    out->width = c->width;
+    out->height = c->height;
+    return TR_OK;
+}
+
+tr_status context_fail(void* ctx, tr_status st, const std::string& msg)
+{
+    return fail(static_cast<Context*>(ctx), st, msg);
+}
+
+} // namespace tr
 
 extern "C" {
 
