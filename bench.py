@@ -34,7 +34,8 @@ import numpy as np
 ROOT = Path(__file__).resolve().parent
 sys.path.insert(0, str(ROOT))
 
-EXTEND_BYTES_PER_RAY = 48      # O, D in (32 B) + hit out (16 B)
+EXTEND_BYTES_PER_RAY = 48      # path state in (O, D, T: 48 B)
+EXTEND_BYTES_PER_HIT = 64      # path state (48 B) + hit record (16 B) appended to the hit queue
 NODE_BYTES = 80                # one CWBVH node
 TRI_BYTES = 48                 # one traversal triangle (v0, e1, e2)
 SHADE_BYTES_FIXED = 140        # state 48 + hit 16 + triangle record 72 + material index 4
@@ -54,6 +55,8 @@ def parse():
     p.add_argument("--ms", type=int, default=16, help="samples per pixel per wavefront frame")
     p.add_argument("--cpu-seconds", type=float, default=12.0, help="target CPU work of the CPU baseline sample")
     p.add_argument("--no-cpu-baseline", action="store_true")
+    p.add_argument("--profile", action="store_true",
+                   help="render one eager frame of the workload and exit (the case the ncu captures use)")
     return p.parse_args()
 
 
@@ -249,6 +252,14 @@ def main():
     r.SetSettings(st)
     stream = torch.cuda.current_stream()
     sptr = stream.cuda_stream
+    if args.profile:
+        r.RenderFrame(stream=sptr, use_graph=False)
+        s = r.Statistics()
+        print(json.dumps({k: s[k] for k in ("path_count", "extend_rays", "hit_rays", "shadow_rays",
+                                             "extend_time_ms", "shade_time_ms", "connect_time_ms",
+                                             "device_error")}))
+        r.close()
+        return
     flush = torch.empty(256 * 1024 * 1024 // 4, dtype=torch.float32, device=f"cuda:{local}")
 
     def step(use_graph=True):
@@ -259,6 +270,7 @@ def main():
     # --- counting pass (rays per step, traversal work), outside the timed region
     stage_ms = {"generate": 0.0, "extend": 0.0, "shade": 0.0, "connect": 0.0, "finalize": 0.0}
     ext_rays = sh_rays = 0
+    hit_rays = 0
     ext_per_bounce = np.zeros(16, np.int64)
     r.Reset()
     for _ in range(frames_per_step):
@@ -266,6 +278,7 @@ def main():
         s = r.Statistics()
         ext_rays += sum(s["extend_rays"])
         sh_rays += sum(s["shadow_rays"])
+        hit_rays += sum(s["hit_rays"])
         ext_per_bounce += np.array(s["extend_rays"], np.int64)
     rays_per_step = ext_rays + sh_rays
     cnt_settings = tr.settings_for(scene, multi_sample=args.ms)
@@ -338,12 +351,13 @@ def main():
 
     # --- roofline of the dominant kernel (extend): algorithmic bytes / time
     peak, peak_kind = measured_peak()
-    ext_bytes = (ext_rays * EXTEND_BYTES_PER_RAY + cs["traversal_extend_nodes"] * NODE_BYTES
+    ext_bytes = (ext_rays * EXTEND_BYTES_PER_RAY + hit_rays * EXTEND_BYTES_PER_HIT
+                 + cs["traversal_extend_nodes"] * NODE_BYTES
                  + cs["traversal_extend_tris"] * TRI_BYTES)
     ext_s = stage_ms["extend"] / 1e3
     launches = frames_per_step * st.maxDepth
     achieved = ext_bytes / ext_s / 1e9
-    compulsory = ext_rays * EXTEND_BYTES_PER_RAY / ext_s / 1e9
+    compulsory = (ext_rays * EXTEND_BYTES_PER_RAY + hit_rays * EXTEND_BYTES_PER_HIT) / ext_s / 1e9
     traffic = None
     prof = ROOT / "profiles" / "extend_traffic.json"
     if prof.exists():
@@ -393,6 +407,7 @@ def main():
             "rays_per_step": int(rays_per_step),
             "extend_rays_per_step": int(ext_rays),
             "shadow_rays_per_step": int(sh_rays),
+            "hit_rays_per_step": int(hit_rays),
             "stage_ms_per_step": {k: round(v, 3) for k, v in stage_ms.items()},
             "rmse_vs_fp64_band": rmse,
             "roofline": {

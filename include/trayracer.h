@@ -203,6 +203,7 @@ typedef struct tr_statistics {
     uint64_t traversal_extend_tris;
     uint64_t traversal_connect_nodes;
     uint64_t traversal_connect_tris;
+    uint32_t hit_rays[TR_MAX_DEPTH];    /* extend rays per bounce that hit something */
 } tr_statistics;
 
 /* Scene numbers: triangle/light/BVH sizes and the host build time. */
@@ -221,16 +222,21 @@ typedef struct tr_scene_info {
 /* Device pointers of the wavefront buffers (plane-major SoA), for parity
  * dumps and external consumers. `capacity` is the plane stride in elements.
  *   path_state[k]: 3 planes of float4: (O.xyz, bits(pathIx<<4|flags)),
- *                  (D.xyz, bits(packed normal)), (T.xyz, extend pdf);
- *                  k = bounce & 1 holds the queue of that bounce.
- *   hits:          uint4 per queue slot: (bary 16:16, instIx, primIx, bits(t)).
+ *                  (D.xyz, bits(packed normal)), (T.xyz, extend pdf).
+ *                  k = 0: the extend queue (written by tr_generate and
+ *                  tr_shade, read by tr_extend); k = 1: the hit queue (the
+ *                  extend queue's rays that hit something, in no particular
+ *                  order, written by tr_extend, read by tr_shade).
+ *   hits:          uint4 per hit-queue slot: (bary 16:16, instIx, primIx, bits(t)).
  *   shadow:        3 planes of float4: (O.xyz, bits(pathIx)), (L.xyz, dist),
  *                  (T.xyz, 0).
  *   radiance:      float4 per path index (sum of this frame's contributions).
  *   accumulator:   float4 per pixel (sum over frames, .w = sample count).
- *   counters:      uint32[4*(TR_MAX_DEPTH+1)]: extend queue length per bounce,
- *                  shadow queue length per bounce, then the work cursors of
- *                  the extend and connect launches. */
+ *   counters:      uint32[5*(TR_MAX_DEPTH+1)+1], 17 words per group: extend
+ *                  queue length per bounce, shadow queue length per bounce,
+ *                  the work cursors of the extend and connect launches, the
+ *                  hit queue length per bounce; then the path cursor of
+ *                  tr_adjoint_frame. */
 typedef struct tr_buffers {
     void* path_state[2];
     void* hits;

@@ -117,24 +117,33 @@ def test_gpu_adjoint_matches_finite_differences():
 
 
 def test_gpu_adjoint_roughness_statistically_consistent_with_fd():
-    """Roughness moves the sampled GGX directions, so per sample the finite difference and the
-    detached-sampling adjoint differ; both estimate the same derivative, and on 256x256x16 paths
-    they agree to within the Monte Carlo error."""
-    scene = diff_scene(256, 256)
-    st = settings(16)
+    """Roughness moves the sampled GGX directions (and rays across geometric edges), so the
+    fixed-seed finite difference is a noisy estimator of the derivative while the
+    detached-sampling adjoint is not. Over independent seeds (batch means) the two must agree
+    within three standard errors of their difference."""
+    scene = diff_scene(128, 128)
     rng = np.random.default_rng(4)
-    w = rng.uniform(0.0, 1.0, (256 * 256, 4)).astype(np.float32)
+    w = rng.uniform(0.0, 1.0, (128 * 128, 4)).astype(np.float32)
     w[:, 3] = 0
-    g = gpu_adjoint(scene, st, w)
-    r = _fd_renderer(scene, st)
+    h = 2.0 ** -8
     rows = []
     for mi in (0, 2, 6):
-        fd = _fd(r, scene, w, mi, "roughness", None, 2.0 ** -6)
-        rows.append((mi, fd, float(g[mi, 3])))
-    r.close()
-    print("roughness gradient (material, fd, adjoint):", rows)
-    for mi, fd, adj in rows:
-        assert abs(fd - adj) <= 0.1 * abs(fd) + 1e-3, rows
+        diffs = []
+        for seed in range(12):
+            st = settings(16)
+            st.seed = 1000 + seed
+            g = gpu_adjoint(scene, st, w)
+            r = _fd_renderer(scene, st)
+            fd = _fd(r, scene, w, mi, "roughness", None, h)
+            r.close()
+            diffs.append((fd, float(g[mi, 3])))
+        d = np.array(diffs)
+        delta = d[:, 0] - d[:, 1]
+        se = delta.std(ddof=1) / np.sqrt(len(delta))
+        rows.append((mi, d[:, 0].mean(), d[:, 1].mean(), delta.mean(), se))
+    print("roughness gradient (material, fd mean, adjoint mean, mean difference, standard error):", rows)
+    for mi, fdm, adm, dm, se in rows:
+        assert abs(dm) <= 3.0 * se + 1e-3 * abs(adm), rows
 
 
 def test_torch_autograd_function():
@@ -182,5 +191,5 @@ def test_adjoint_cost_relative_to_forward():
     fwd, adj = a.elapsed_time(b), b.elapsed_time(c)
     print(f"forward {fwd:.3f} ms, adjoint {adj:.3f} ms, ratio {adj / fwd:.2f}")
     r.close()
-    assert adj / fwd < 6.0, f"adjoint {adj:.3f} ms vs forward {fwd:.3f} ms"
+    assert adj / fwd < 3.0, f"adjoint {adj:.3f} ms vs forward {fwd:.3f} ms"
 

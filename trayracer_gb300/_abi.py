@@ -121,6 +121,7 @@ class Statistics(C.Structure):
         ("traversal_extend_tris", C.c_uint64),
         ("traversal_connect_nodes", C.c_uint64),
         ("traversal_connect_tris", C.c_uint64),
+        ("hit_rays", C.c_uint32 * TR_MAX_DEPTH),
     ]
 
 

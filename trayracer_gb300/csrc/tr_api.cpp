@@ -546,7 +546,7 @@ tr_status tr_adjoint_frame(void* ctx, void* stream, const float* pixel_grad, flo
     cudaSetDevice(c->device);
     const uint32_t sc = c->sampleCount - c->settings.multiSample;
     TR_CUDA(c, launch_adjoint(c->scene, c->frame, c->camera, c->settings, reinterpret_cast<const float4*>(pixel_grad),
-                              scale, param_grad, sc, c->shape, pick_stream(c, stream)));
+                              scale, param_grad, sc, c->materialCount, c->shape, pick_stream(c, stream)));
     return TR_OK;
 }
 
@@ -794,6 +794,7 @@ tr_status tr_get_statistics(void* ctx, tr_statistics* out)
     for (uint32_t b = 0; b < depth; ++b) {
         s.extend_rays[b] = b == 0 ? c->frame.pathCount : c->hostCounters[b];
         s.shadow_rays[b] = c->hostCounters[kShadowCounterBase + b];
+        s.hit_rays[b] = c->hostCounters[kHitCounterBase + b];
         s.path_count += s.extend_rays[b] + s.shadow_rays[b];
         s.shadow_ray_count += s.shadow_rays[b];
         if (b == 0)

@@ -105,8 +105,8 @@ struct SceneView {
 // Per-frame constants of the wavefront (constant between resizes / setting
 // changes). Passed by value as a kernel parameter.
 struct FrameView {
-    float4* state[2];      // 3 planes each, plane stride = capacity
-    uint4* hits;           // by queue slot
+    float4* state[2];      // 3 planes each, plane stride = capacity: [0] extend queue, [1] hit queue
+    uint4* hits;           // by hit-queue slot
     float4* shadow;        // 3 planes, plane stride = capacity
     float4* radiance;      // by path index
     float4* accumulator;   // by pixel
@@ -148,12 +148,16 @@ struct Settings {
     uint32_t pad;
 };
 
-// Device counter words: queue lengths per bounce, then the work-fetch cursors
-// of the persistent extend and connect launches.
+// Device counter words: per bounce the extend queue length, the shadow queue
+// length, the work-fetch cursors of the persistent extend and connect launches,
+// and the hit queue length (rays of the extend queue that hit something); then
+// the path cursor of the persistent adjoint launch.
 constexpr uint32_t kShadowCounterBase = TR_MAX_DEPTH + 1;
 constexpr uint32_t kExtendWorkBase = 2 * (TR_MAX_DEPTH + 1);
 constexpr uint32_t kConnectWorkBase = 3 * (TR_MAX_DEPTH + 1);
-constexpr uint32_t kCounterWords = 4 * (TR_MAX_DEPTH + 1);
+constexpr uint32_t kHitCounterBase = 4 * (TR_MAX_DEPTH + 1);
+constexpr uint32_t kAdjointCursor = 5 * (TR_MAX_DEPTH + 1);
+constexpr uint32_t kCounterWords = kAdjointCursor + 1;
 
 // Path index / flag packing, Tracer/Common/CommonStructs.h:46-71.
 constexpr uint32_t kPathIxShift = 4;

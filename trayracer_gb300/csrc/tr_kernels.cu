@@ -2,11 +2,15 @@
 // connect, finalize.
 //
 // Data layout (all in HBM):
-//   path state  3 float4 planes per queue (coalesced 16-byte accesses), two
-//               queues ping-ponged by bounce parity so a launch never reads
-//               and writes the same queue (the reference compacts in place,
-//               PathTracing.h:16-18 vs :171-173);
-//   hits        one uint4 per queue slot, written and read in queue order;
+//   path state  3 float4 planes per queue (coalesced 16-byte accesses): the
+//               extend queue (rays of the bounce) and the hit queue (the rays
+//               that hit something, state copied by the extend launch next to
+//               their hit record); extend reads the first and fills the
+//               second, shade reads the second and refills the first, so no
+//               launch reads and writes the same queue (the reference
+//               compacts in place, PathTracing.h:16-18 vs :171-173) and
+//               missed rays (black sky) never reach the shade launch;
+//   hits        one uint4 per hit-queue slot;
 //   shadow      3 float4 planes, compacted;
 //   radiance    one float4 per path index; every contribution of a path is
 //               added here by the only thread that owns the path in that
@@ -224,43 +228,84 @@ __device__ __forceinline__ void add_counts(unsigned long long* dst, const Traver
     }
 }
 
-// COUNT = true also sums the nodes visited and triangles tested (for the
-// traversal bytes of the roofline); it is launched outside timed regions.
+// Persistent warps refill a lane with the next ray of the queue when fewer
+// than this many of its 32 rays are still traversing (incoherent secondary
+// rays end at very different times).
+constexpr uint32_t kRefillBelow = 24;
+
+// Closest hit of the bounce's extend queue. Rays that hit are appended (one
+// warp ballot and one atomic per step) to the hit queue with their full path
+// state and hit record; missed rays end here. COUNT = true also sums the nodes
+// visited and triangles tested (for the traversal bytes of the roofline); it
+// is launched outside timed regions.
 template <bool COUNT>
 __global__ void __launch_bounds__(128) extend_kernel(SceneView s, FrameView f, Settings st, uint32_t bounce)
 {
     const uint32_t count = queue_length(f, bounce);
-    const float4* __restrict__ in = f.state[bounce & 1u];
+    const float4* __restrict__ in = f.state[0];
+    float4* __restrict__ hq = f.state[1];
     const uint32_t cap = f.capacity;
     uint32_t* work = f.counters + kExtendWorkBase + bounce;
+    uint32_t* hitCounter = f.counters + kHitCounterBase + bounce;
     const uint32_t lane = lane_id();
+    const bool aov = (st.flags & TR_FLAG_WRITE_AOVS) && bounce == 0;
+    const uint32_t wh = f.resX * f.resY;
     TraversalCounts cnt{0, 0};
+    Traversal t;
+    uint2 stack[kTraversalStack];
+    float4 O4 = make_float4(0.f, 0.f, 0.f, 0.f), D4 = O4, T4 = O4;
+    bool alive = false, more = true;
     while (true) {
-        uint32_t base = 0;
-        if (lane == 0)
-            base = atomicAdd(work, 32u);
-        base = __shfl_sync(kFull, base, 0);
-        if (base >= count)
-            break;
-        const uint32_t i = base + lane;
-        if (i < count) {
-            const float4 O4 = __ldcs(in + i);
-            const float4 D4 = __ldcs(in + i + cap);
-            float tmax = kDstMax;
-            uint32_t slot = 0xffffffffu;
-            float u = 0.f, v = 0.f;
-            const bool ok = traverse<false, COUNT>(s, f3(O4), f3(D4), st.rayEpsilon, tmax, slot, u, v, &cnt);
-            if (!ok)
-                atomicOr(f.errorFlag, 1u);
-            uint4 h;
-            if (slot != 0xffffffffu) {
-                const uint32_t prim = __float_as_uint(__ldg(s.bvhTris + 3u * slot).w);
-                h = make_uint4(encode_bary(u, v), 0u, prim, __float_as_uint(tmax));
-            } else {
-                h = make_uint4(0u, 0xffffffffu, 0xffffffffu, __float_as_uint(kDstMax));
+        const uint32_t idle = __ballot_sync(kFull, !alive && more);
+        if (idle) {
+            const uint32_t leader = __ffs(idle) - 1u;
+            uint32_t base = 0;
+            if (lane == leader)
+                base = atomicAdd(work, __popc(idle));
+            base = __shfl_sync(kFull, base, leader);
+            if (!alive && more) {
+                const uint32_t i = base + __popc(idle & ((1u << lane) - 1u));
+                if (i < count) {
+                    O4 = __ldcs(in + i);
+                    D4 = __ldcs(in + i + cap);
+                    T4 = __ldcs(in + i + 2 * cap);
+                    traversal_begin(t, f3(O4), f3(D4), st.rayEpsilon, kDstMax);
+                    alive = true;
+                } else {
+                    more = false;
+                }
             }
-            __stcs(f.hits + i, h);
         }
+        if (!__any_sync(kFull, alive))
+            break;
+        uint32_t active;
+        do {
+            bool done = false;
+            if (alive)
+                done = traversal_step<false, COUNT>(t, stack, s, &cnt);
+            const bool hit = done && t.hitSlot != 0xffffffffu;
+            const uint32_t slot = warp_append(hitCounter, hit);
+            if (done) {
+                if (!t.ok)
+                    atomicOr(f.errorFlag, 1u);
+                if (hit) {
+                    const uint32_t prim = __float_as_uint(__ldg(s.bvhTris + 3u * t.hitSlot).w);
+                    __stcs(hq + slot, O4);
+                    __stcs(hq + slot + cap, D4);
+                    __stcs(hq + slot + 2 * cap, T4);
+                    __stcs(f.hits + slot, make_uint4(encode_bary(t.u, t.v), 0u, prim, __float_as_uint(t.tmax)));
+                } else if (aov) {
+                    // a primary miss sees the (disabled) sky: black guide values (PathTracing.h:48-52)
+                    const uint32_t pathIx = path_ix(__float_as_uint(O4.w));
+                    if (pathIx < wh) {
+                        f.albedo[pathIx] = make_float4(0.f, 0.f, 0.f, 0.f);
+                        f.normals[pathIx] = make_float4(0.f, 0.f, 0.f, 0.f);
+                    }
+                }
+                alive = false;
+            }
+            active = __ballot_sync(kFull, alive);
+        } while (uint32_t(__popc(active)) >= kRefillBelow);
     }
     if (COUNT)
         add_counts(f.traversal, cnt);
@@ -590,9 +635,9 @@ __device__ __forceinline__ void shade_path(const SceneView& s, const FrameView& 
 template <bool REF>
 __global__ void __launch_bounds__(128) shade_kernel(SceneView s, FrameView f, Settings st, uint32_t bounce)
 {
-    const uint32_t count = queue_length(f, bounce);
-    const float4* __restrict__ in = f.state[bounce & 1u];
-    float4* __restrict__ out = f.state[(bounce + 1u) & 1u];
+    const uint32_t count = __ldcg(f.counters + kHitCounterBase + bounce);
+    const float4* __restrict__ in = f.state[1];
+    float4* __restrict__ out = f.state[0];
     const uint32_t cap = f.capacity;
     const uint32_t sc = *f.sampleCount;
     const uint32_t wh = f.resX * f.resY;
@@ -636,6 +681,8 @@ __global__ void __launch_bounds__(128) shade_kernel(SceneView s, FrameView f, Se
     }
 }
 
+// Any hit of the bounce's shadow queue over [eps, dist - 2 eps]; an unoccluded
+// ray adds its radiance to its path. Same lane refill as extend_kernel.
 template <bool COUNT>
 __global__ void __launch_bounds__(128) connect_kernel(SceneView s, FrameView f, Settings st, uint32_t bounce)
 {
@@ -644,30 +691,48 @@ __global__ void __launch_bounds__(128) connect_kernel(SceneView s, FrameView f, 
     uint32_t* work = f.counters + kConnectWorkBase + bounce;
     const uint32_t lane = lane_id();
     TraversalCounts cnt{0, 0};
+    Traversal t;
+    uint2 stack[kTraversalStack];
+    uint32_t ray = 0, pathIx = 0;
+    bool alive = false, more = true;
     while (true) {
-        uint32_t base = 0;
-        if (lane == 0)
-            base = atomicAdd(work, 32u);
-        base = __shfl_sync(kFull, base, 0);
-        if (base >= count)
-            break;
-        const uint32_t i = base + lane;
-        if (i < count) {
-            const float4 O4 = __ldcs(f.shadow + i);
-            const float4 L4 = __ldcs(f.shadow + i + cap);
-            float tmax = L4.w - (2 * st.rayEpsilon);
-            uint32_t slot = 0xffffffffu;
-            float u, v;
-            const bool ok = traverse<true, COUNT>(s, f3(O4), f3(L4), st.rayEpsilon, tmax, slot, u, v, &cnt);
-            if (!ok)
-                atomicOr(f.errorFlag, 1u);
-            if (slot == 0xffffffffu) {
-                const float4 T4 = __ldcs(f.shadow + i + 2 * cap);
-                const uint32_t pathIx = __float_as_uint(O4.w);
-                float4 r = f.radiance[pathIx];
-                f.radiance[pathIx] = make_float4(r.x + T4.x, r.y + T4.y, r.z + T4.z, r.w);
+        const uint32_t idle = __ballot_sync(kFull, !alive && more);
+        if (idle) {
+            const uint32_t leader = __ffs(idle) - 1u;
+            uint32_t base = 0;
+            if (lane == leader)
+                base = atomicAdd(work, __popc(idle));
+            base = __shfl_sync(kFull, base, leader);
+            if (!alive && more) {
+                const uint32_t i = base + __popc(idle & ((1u << lane) - 1u));
+                if (i < count) {
+                    const float4 O4 = __ldcs(f.shadow + i);
+                    const float4 L4 = __ldcs(f.shadow + i + cap);
+                    ray = i;
+                    pathIx = __float_as_uint(O4.w);
+                    traversal_begin(t, f3(O4), f3(L4), st.rayEpsilon, L4.w - (2 * st.rayEpsilon));
+                    alive = true;
+                } else {
+                    more = false;
+                }
             }
         }
+        if (!__any_sync(kFull, alive))
+            break;
+        uint32_t active;
+        do {
+            if (alive && traversal_step<true, COUNT>(t, stack, s, &cnt)) {
+                if (!t.ok)
+                    atomicOr(f.errorFlag, 1u);
+                if (t.hitSlot == 0xffffffffu) {
+                    const float4 T4 = __ldcs(f.shadow + ray + 2 * cap);
+                    float4 r = f.radiance[pathIx];
+                    f.radiance[pathIx] = make_float4(r.x + T4.x, r.y + T4.y, r.z + T4.z, r.w);
+                }
+                alive = false;
+            }
+            active = __ballot_sync(kFull, alive);
+        } while (uint32_t(__popc(active)) >= kRefillBelow);
     }
     if (COUNT)
         add_counts(f.traversal + 2, cnt);
@@ -695,43 +760,48 @@ __global__ void __launch_bounds__(256) finalize_kernel(FrameView f, Settings st)
     f.colors[p] = make_float4(acc.x / n, acc.y / n, acc.z / n, acc.w / n);
 }
 
-// Gradient atomics: lanes with the same key (material) sum their values
-// first; one lane per key adds the sums. key == ~0: nothing to add.
-__device__ __forceinline__ void warp_add_grads(float* __restrict__ grads, uint32_t key, const float (&g)[kGradSlots],
+// Adds each lane's gradient slots [first, last) to the row of its key
+// (material); key == ~0: nothing to add. Lanes that share a key are summed by
+// a butterfly over the warp, one distinct key at a time, and the first lane of
+// the key adds the sums: with SMEM to the warp's private copy in shared memory
+// (plain read-modify-write: only that lane writes there), else with global
+// atomics.
+template <bool SMEM>
+__device__ __forceinline__ void warp_add_grads(float* __restrict__ dst, uint32_t key, const float (&g)[kGradSlots],
                                                int first, int last)
 {
-    const uint32_t peers = __match_any_sync(kFull, key);
     const uint32_t lane = lane_id();
-    float sum[kGradSlots];
-    if (peers == kFull) {
+    uint32_t pending = __ballot_sync(kFull, key != 0xffffffffu);
+    while (pending) {
+        const uint32_t leader = __ffs(pending) - 1u;
+        const uint32_t cur = __shfl_sync(kFull, key, leader);
+        const bool mine = key == cur;
+        pending &= ~__ballot_sync(kFull, mine);
 #pragma unroll
         for (int k = 0; k < kGradSlots; ++k) {
-            float v = (k >= first && k < last) ? g[k] : 0.f;
+            if (k < first || k >= last)
+                continue;
+            float v = mine ? g[k] : 0.f;
 #pragma unroll
             for (int o = 16; o > 0; o >>= 1)
                 v += __shfl_xor_sync(kFull, v, o);
-            sum[k] = v;
-        }
-    } else {
-#pragma unroll
-        for (int k = 0; k < kGradSlots; ++k)
-            sum[k] = 0.f;
-        for (int i = 0; i < 32; ++i) {
-            const uint32_t ki = __shfl_sync(kFull, key, i);
-#pragma unroll
-            for (int k = 0; k < kGradSlots; ++k) {
-                const float o = __shfl_sync(kFull, (k >= first && k < last) ? g[k] : 0.f, i);
-                if (ki == key)
-                    sum[k] += o;
+            if (lane == leader && v != 0.f) {
+                float* a = dst + size_t(cur) * kGradSlots + k;
+                if (SMEM)
+                    *a += v;
+                else
+                    atomicAdd(a, v);
             }
         }
     }
-    if (key != 0xffffffffu && lane == __ffs(peers) - 1u) {
-        for (int k = first; k < last; ++k)
-            if (sum[k] != 0.f)
-                atomicAdd(grads + size_t(key) * kGradSlots + k, sum[k]);
-    }
 }
+
+// Shared memory of one adjoint block: one copy of the gradient table per warp.
+constexpr uint32_t kAdjointThreads = 128;
+constexpr uint32_t kAdjointWarps = kAdjointThreads / 32;
+// Largest dynamic shared memory without the opt-in attribute: 4 copies of
+// 9 floats per material, up to 341 materials; more use global atomics.
+constexpr size_t kAdjointSmemMax = 48 * 1024;
 
 // Path-replay adjoint of one frame (default sampling mode): every path is
 // replayed from its random keys, re-tracing its extend and shadow rays; at
@@ -740,131 +810,170 @@ __device__ __forceinline__ void warp_add_grads(float* __restrict__ grads, uint32
 // own NEE contribution for the light direction, and the radiance still to
 // come (the path's total minus what was already accounted for) for the
 // extend direction. Emission gradients come from emissive hits and NEE.
-__global__ void __launch_bounds__(128) adjoint_kernel(SceneView s, FrameView f, Camera cam, Settings st,
-                                                      const float4* __restrict__ pixelGrad, float scale,
-                                                      float* __restrict__ grads, uint32_t sc)
+//
+// Persistent warps: a lane whose path ended takes the next path index from
+// a device cursor, so lanes of one warp may be at different bounces and no
+// warp idles behind its longest path. With SMEM the gradients are summed per
+// block in shared memory and added to the global table once per block.
+template <bool SMEM>
+__global__ void __launch_bounds__(kAdjointThreads) adjoint_kernel(SceneView s, FrameView f, Camera cam, Settings st,
+                                                                  const float4* __restrict__ pixelGrad, float scale,
+                                                                  float* __restrict__ grads, uint32_t sc,
+                                                                  uint32_t materialCount)
 {
+    extern __shared__ float sgrad[];
+    const uint32_t rows = materialCount * kGradSlots;
+    float* dst = grads;
+    if (SMEM) {
+        for (uint32_t i = threadIdx.x; i < kAdjointWarps * rows; i += blockDim.x)
+            sgrad[i] = 0.f;
+        __syncthreads();
+        dst = sgrad + (threadIdx.x >> 5) * rows;
+    }
     const uint32_t wh = f.resX * f.resY;
     const uint32_t lane = lane_id();
-    const uint32_t warpGlobal = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
-    const uint32_t warpStride = (gridDim.x * blockDim.x) >> 5;
-    for (uint32_t base = warpGlobal * 32u; base < f.pathCount; base += warpStride * 32u) {
-        const uint32_t pathIx = base + lane;
-        bool alive = false;
-        float3 delta = f3(0.f), lrem = f3(0.f);
-        float4 O4 = make_float4(0.f, 0.f, 0.f, 0.f), D4 = O4, T4 = O4;
-        uint32_t pixel = 0, sampleIx = 0;
-        if (pathIx < f.pathCount) {
-            pixel = pathIx % wh;
-            sampleIx = pathIx / wh;
-            const float4 pg = pixelGrad[pixel];
-            delta = make_float3(pg.x * scale, pg.y * scale, pg.z * scale);
-            const float4 rad = f.radiance[pathIx];
-            lrem = f3(rad);
-            alive = (delta.x != 0.f || delta.y != 0.f || delta.z != 0.f) &&
-                    (lrem.x != 0.f || lrem.y != 0.f || lrem.z != 0.f);
-            if (alive) {
-                CounterRng rng;
-                rng.init(pixel, sc + sampleIx, 0u, st.seed);
-                float3 O, D;
-                float T;
-                camera_ray(cam, f.resX, f.resY, pixel % f.resX, pixel / f.resX, rng, false, O, D, T);
-                O4 = f4(O, __uint_as_float(pack_path(pathIx, 0)));
-                D4 = f4(D, 0.f);
-                T4 = make_float4(T, T, T, 1.f);
+    uint32_t* cursor = f.counters + kAdjointCursor;
+    bool alive = false, more = true;
+    uint32_t b = 0, pixel = 0, sampleIx = 0;
+    float3 delta = f3(0.f), lrem = f3(0.f);
+    float4 O4 = make_float4(0.f, 0.f, 0.f, 0.f), D4 = O4, T4 = O4;
+    while (true) {
+        uint32_t idle;
+        while ((idle = __ballot_sync(kFull, !alive && more)) != 0u) {
+            const uint32_t leader = __ffs(idle) - 1u;
+            uint32_t base = 0;
+            if (lane == leader)
+                base = atomicAdd(cursor, __popc(idle));
+            base = __shfl_sync(kFull, base, leader);
+            if (!alive && more) {
+                const uint32_t pathIx = base + __popc(idle & ((1u << lane) - 1u));
+                if (pathIx < f.pathCount) {
+                    pixel = pathIx % wh;
+                    sampleIx = pathIx / wh;
+                    const float4 pg = pixelGrad[pixel];
+                    delta = make_float3(pg.x * scale, pg.y * scale, pg.z * scale);
+                    lrem = f3(f.radiance[pathIx]);
+                    alive = (delta.x != 0.f || delta.y != 0.f || delta.z != 0.f) &&
+                            (lrem.x != 0.f || lrem.y != 0.f || lrem.z != 0.f);
+                    if (alive) {
+                        CounterRng rng;
+                        rng.init(pixel, sc + sampleIx, 0u, st.seed);
+                        float3 O, D;
+                        float T;
+                        camera_ray(cam, f.resX, f.resY, pixel % f.resX, pixel / f.resX, rng, false, O, D, T);
+                        O4 = f4(O, __uint_as_float(pack_path(pathIx, 0)));
+                        D4 = f4(D, 0.f);
+                        T4 = make_float4(T, T, T, 1.f);
+                        b = 0;
+                    }
+                } else {
+                    more = false;
+                }
             }
         }
-        for (uint32_t b = 0; b < st.maxDepth; ++b) {
-            float g[kGradSlots], ge[kGradSlots];
+        if (!__any_sync(kFull, alive))
+            break;
+
+        float g[kGradSlots], ge[kGradSlots];
 #pragma unroll
-            for (int k = 0; k < kGradSlots; ++k)
-                g[k] = ge[k] = 0.f;
-            uint32_t key = 0xffffffffu, keyE = 0xffffffffu;
-            if (alive) {
-                float tmax = kDstMax;
-                uint32_t slot = 0xffffffffu;
-                float u = 0.f, v = 0.f;
-                if (!traverse<false>(s, f3(O4), f3(D4), st.rayEpsilon, tmax, slot, u, v))
-                    atomicOr(f.errorFlag, 1u);
-                uint4 hd;
-                if (slot != 0xffffffffu)
-                    hd = make_uint4(encode_bary(u, v), 0u, __float_as_uint(__ldg(s.bvhTris + 3u * slot).w),
-                                    __float_as_uint(tmax));
-                else
-                    hd = make_uint4(0u, 0xffffffffu, 0xffffffffu, __float_as_uint(kDstMax));
-                CounterRng rng;
-                rng.init(pixel, sc + sampleIx, b + 1u, st.seed);
-                VertexInfo vi;
-                bool wantExt = false, wantShadow = false;
-                float4 ext[3], sh[3];
-                shade_path<false>(s, f, st, b, sc, O4, D4, T4, hd, rng, wantExt, ext, wantShadow, sh, &vi);
-                if (!vi.hit) {
-                    alive = false;
-                } else if (vi.emissive) {
-                    const float C[3] = {vi.emitted.x, vi.emitted.y, vi.emitted.z};
-                    const float E[3] = {vi.mat.emissive.x, vi.mat.emissive.y, vi.mat.emissive.z};
-                    const float dl[3] = {delta.x, delta.y, delta.z};
-                    const float Dc[3] = {vi.mat.diffuse.x, vi.mat.diffuse.y, vi.mat.diffuse.z};
-                    // emission = Emissive * diffuse (CudaMaterial.h:158): linear in both
-                    for (int c = 0; c < 3; ++c) {
-                        if (E[c] > 0.f)
-                            ge[kGEmR + c] = dl[c] * C[c] / E[c] * Dc[c];
-                        if (Dc[c] > 0.f)
-                            g[kGBaseR + c] = dl[c] * C[c] / Dc[c];
-                    }
-                    keyE = vi.matIx;
-                    key = vi.matIx;
-                    lrem = lrem - vi.emitted;
-                    alive = false;
-                } else {
-                    if (wantShadow) {
-                        float smax = sh[1].w - (2 * st.rayEpsilon);
-                        uint32_t occ = 0xffffffffu;
-                        float su, sv;
-                        if (!traverse<true>(s, f3(sh[0]), f3(sh[1]), st.rayEpsilon, smax, occ, su, sv))
-                            atomicOr(f.errorFlag, 1u);
-                        if (occ == 0xffffffffu) {
-                            const float3 C = f3(sh[2]);
-                            lrem = lrem - C;
-                            const Vec3<Dual> fv = dual::closure_value(vi.closure, vi.mat, vi.wo, vi.wiLight);
-                            const Dual* fc[3] = {&fv.x, &fv.y, &fv.z};
-                            const float w[3] = {delta.x * C.x, delta.y * C.y, delta.z * C.z};
-                            for (int c = 0; c < 3; ++c)
-                                if (w[c] != 0.f && fc[c]->v != 0.f)
-                                    for (int k = 0; k < kGradParams; ++k)
-                                        g[k] += w[c] * fc[c]->d[k] / fc[c]->v;
-                            key = vi.matIx;
-                            if (vi.lightIx >= 0) {
-                                const LightTri& Lt = s.lights[vi.lightIx];
-                                const float E[3] = {Lt.radiance.x, Lt.radiance.y, Lt.radiance.z};
-                                for (int c = 0; c < 3; ++c)
-                                    if (E[c] > 0.f)
-                                        ge[kGEmR + c] = w[c] / E[c];
-                                keyE = __ldg(s.matIdx + Lt.triIx);
-                            }
-                        }
-                    }
-                    if (wantExt) {
-                        const Vec3<Dual> fv = dual::closure_value(vi.closure, vi.mat, vi.wo, vi.wiExt);
+        for (int k = 0; k < kGradSlots; ++k)
+            g[k] = ge[k] = 0.f;
+        uint32_t key = 0xffffffffu, keyE = 0xffffffffu;
+        if (alive) {
+            float tmax = kDstMax;
+            uint32_t slot = 0xffffffffu;
+            float u = 0.f, v = 0.f;
+            if (!traverse<false>(s, f3(O4), f3(D4), st.rayEpsilon, tmax, slot, u, v))
+                atomicOr(f.errorFlag, 1u);
+            uint4 hd;
+            if (slot != 0xffffffffu)
+                hd = make_uint4(encode_bary(u, v), 0u, __float_as_uint(__ldg(s.bvhTris + 3u * slot).w),
+                                __float_as_uint(tmax));
+            else
+                hd = make_uint4(0u, 0xffffffffu, 0xffffffffu, __float_as_uint(kDstMax));
+            CounterRng rng;
+            rng.init(pixel, sc + sampleIx, b + 1u, st.seed);
+            VertexInfo vi;
+            bool wantExt = false, wantShadow = false;
+            float4 ext[3], sh[3];
+            shade_path<false>(s, f, st, b, sc, O4, D4, T4, hd, rng, wantExt, ext, wantShadow, sh, &vi);
+            if (!vi.hit) {
+                alive = false;
+            } else if (vi.emissive) {
+                const float C[3] = {vi.emitted.x, vi.emitted.y, vi.emitted.z};
+                const float E[3] = {vi.mat.emissive.x, vi.mat.emissive.y, vi.mat.emissive.z};
+                const float dl[3] = {delta.x, delta.y, delta.z};
+                const float Dc[3] = {vi.mat.diffuse.x, vi.mat.diffuse.y, vi.mat.diffuse.z};
+                // emission = Emissive * diffuse (CudaMaterial.h:158): linear in both
+                for (int c = 0; c < 3; ++c) {
+                    if (E[c] > 0.f)
+                        ge[kGEmR + c] = dl[c] * C[c] / E[c] * Dc[c];
+                    if (Dc[c] > 0.f)
+                        g[kGBaseR + c] = dl[c] * C[c] / Dc[c];
+                }
+                keyE = vi.matIx;
+                key = vi.matIx;
+                lrem = lrem - vi.emitted;
+                alive = false;
+            } else {
+                if (wantShadow) {
+                    float smax = sh[1].w - (2 * st.rayEpsilon);
+                    uint32_t occ = 0xffffffffu;
+                    float su, sv;
+                    if (!traverse<true>(s, f3(sh[0]), f3(sh[1]), st.rayEpsilon, smax, occ, su, sv))
+                        atomicOr(f.errorFlag, 1u);
+                    if (occ == 0xffffffffu) {
+                        const float3 C = f3(sh[2]);
+                        lrem = lrem - C;
+                        const Vec3<Dual> fv = dual::closure_value(vi.closure, vi.mat, vi.wo, vi.wiLight);
                         const Dual* fc[3] = {&fv.x, &fv.y, &fv.z};
-                        const float w[3] = {delta.x * lrem.x, delta.y * lrem.y, delta.z * lrem.z};
+                        const float w[3] = {delta.x * C.x, delta.y * C.y, delta.z * C.z};
                         for (int c = 0; c < 3; ++c)
                             if (w[c] != 0.f && fc[c]->v != 0.f)
                                 for (int k = 0; k < kGradParams; ++k)
                                     g[k] += w[c] * fc[c]->d[k] / fc[c]->v;
                         key = vi.matIx;
-                        O4 = ext[0];
-                        D4 = ext[1];
-                        T4 = ext[2];
-                    } else {
-                        alive = false;
+                        if (vi.lightIx >= 0) {
+                            const LightTri& Lt = s.lights[vi.lightIx];
+                            const float E[3] = {Lt.radiance.x, Lt.radiance.y, Lt.radiance.z};
+                            for (int c = 0; c < 3; ++c)
+                                if (E[c] > 0.f)
+                                    ge[kGEmR + c] = w[c] / E[c];
+                            keyE = __ldg(s.matIdx + Lt.triIx);
+                        }
                     }
                 }
+                if (wantExt) {
+                    const Vec3<Dual> fv = dual::closure_value(vi.closure, vi.mat, vi.wo, vi.wiExt);
+                    const Dual* fc[3] = {&fv.x, &fv.y, &fv.z};
+                    const float w[3] = {delta.x * lrem.x, delta.y * lrem.y, delta.z * lrem.z};
+                    for (int c = 0; c < 3; ++c)
+                        if (w[c] != 0.f && fc[c]->v != 0.f)
+                            for (int k = 0; k < kGradParams; ++k)
+                                g[k] += w[c] * fc[c]->d[k] / fc[c]->v;
+                    key = vi.matIx;
+                    O4 = ext[0];
+                    D4 = ext[1];
+                    T4 = ext[2];
+                    if (++b >= st.maxDepth)
+                        alive = false;
+                } else {
+                    alive = false;
+                }
             }
-            warp_add_grads(grads, key, g, 0, kGradParams);
-            warp_add_grads(grads, keyE, ge, kGEmR, kGradSlots);
-            if (!__any_sync(kFull, alive))
-                break;
+        }
+        warp_add_grads<SMEM>(dst, key, g, 0, kGradParams);
+        warp_add_grads<SMEM>(dst, keyE, ge, kGEmR, kGradSlots);
+    }
+    if (SMEM) {
+        __syncthreads();
+        for (uint32_t i = threadIdx.x; i < rows; i += blockDim.x) {
+            float v = 0.f;
+#pragma unroll
+            for (uint32_t w = 0; w < kAdjointWarps; ++w)
+                v += sgrad[w * rows + i];
+            if (v != 0.f)
+                atomicAdd(grads + i, v);
         }
     }
 }
@@ -932,9 +1041,30 @@ cudaError_t launch_finalize(const FrameView& f, const Settings& st, cudaStream_t
 
 cudaError_t launch_adjoint(const SceneView& s, const FrameView& f, const Camera& cam, const Settings& st,
                            const float4* pixelGrad, float scale, float* grads, uint32_t sampleCount,
-                           const LaunchShape& shape, cudaStream_t stream)
+                           uint32_t materialCount, const LaunchShape& shape, cudaStream_t stream)
 {
-    adjoint_kernel<<<shape.shadeBlocks, 128, 0, stream>>>(s, f, cam, st, pixelGrad, scale, grads, sampleCount);
+    if (f.pathCount == 0)
+        return cudaSuccess;
+    cudaError_t e = cudaMemsetAsync(f.counters + kAdjointCursor, 0, sizeof(uint32_t), stream);
+    if (e != cudaSuccess)
+        return e;
+    const size_t smem = size_t(kAdjointWarps) * materialCount * kGradSlots * sizeof(float);
+    int perSm = 0;
+    if (smem <= kAdjointSmemMax) {
+        e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&perSm, adjoint_kernel<true>, kAdjointThreads, smem);
+        if (e != cudaSuccess)
+            return e;
+        const uint32_t blocks = shape.sms * uint32_t(perSm > 0 ? perSm : 1);
+        adjoint_kernel<true><<<blocks, kAdjointThreads, smem, stream>>>(s, f, cam, st, pixelGrad, scale, grads,
+                                                                        sampleCount, materialCount);
+    } else {
+        e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&perSm, adjoint_kernel<false>, kAdjointThreads, 0);
+        if (e != cudaSuccess)
+            return e;
+        const uint32_t blocks = shape.sms * uint32_t(perSm > 0 ? perSm : 1);
+        adjoint_kernel<false><<<blocks, kAdjointThreads, 0, stream>>>(s, f, cam, st, pixelGrad, scale, grads,
+                                                                      sampleCount, materialCount);
+    }
     return cudaGetLastError();
 }
 

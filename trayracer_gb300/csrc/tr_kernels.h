@@ -29,6 +29,6 @@ cudaError_t launch_connect(const SceneView& s, const FrameView& f, const Setting
 cudaError_t launch_finalize(const FrameView& f, const Settings& st, cudaStream_t stream);
 cudaError_t launch_adjoint(const SceneView& s, const FrameView& f, const Camera& cam, const Settings& st,
                            const float4* pixelGrad, float scale, float* grads, uint32_t sampleCount,
-                           const LaunchShape& shape, cudaStream_t stream);
+                           uint32_t materialCount, const LaunchShape& shape, cudaStream_t stream);
 
 } // namespace tr

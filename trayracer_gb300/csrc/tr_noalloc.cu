@@ -28,7 +28,7 @@ constexpr uint32_t kNoAllocMaxPaths = 1u << 17;
 constexpr size_t kNoAllocPathBytes = 2 * 3 * 16 + 16 + 3 * 16 + 16;
 constexpr size_t kNoAllocTailBytes = 1024;  // counters, sample count, error word, traversal counters
 constexpr size_t kNoAllocScratchBytes = size_t(kNoAllocMaxPaths) * kNoAllocPathBytes + kNoAllocTailBytes;
-static_assert(kCounterWords * 4 + 4 + 4 + 32 <= kNoAllocTailBytes, "scratch tail too small");
+static_assert(kCounterWords * 4 + 4 + 4 <= 512 && 512 + 32 <= kNoAllocTailBytes, "scratch tail too small");
 
 __device__ __align__(256) unsigned char g_noallocScratch[kNoAllocScratchBytes];
 

@@ -146,7 +146,17 @@ TR_HD bool intersect_triangle(const float3& O, const float3& D, const float4& a,
     return true;
 }
 
-TR_HD float byte_to_float(uint32_t w, int i) { return float((w >> (8 * i)) & 0xffu); }
+// float(byte i of w), exact. On the device the byte is placed in the low
+// mantissa bits of 2^23 (one byte permute) and 2^23 subtracted (one add), which
+// avoids the quarter-rate integer-to-float conversion.
+TR_HD float byte_to_float(uint32_t w, int i)
+{
+#ifdef __CUDA_ARCH__
+    return __uint_as_float(__byte_perm(w, 0x4B00u, 0x5440u | uint32_t(i))) - 8388608.0f;
+#else
+    return float((w >> (8 * i)) & 0xffu);
+#endif
+}
 
 // Intersects the 8 children of a node; returns the hit mask: bits 24..31 for
 // internal children (position 24 + (slot ^ (7 - octant))), bits 0..23 for
@@ -183,18 +193,23 @@ TR_HD uint32_t intersect_node(const CwbvhNode* __restrict__ nodes, uint32_t node
     const uint32_t loZ0 = nz ? w4.z : w3.x, loZ1 = nz ? w4.w : w3.y;
     const uint32_t hiZ0 = nz ? w3.x : w4.z, hiZ1 = nz ? w3.y : w4.w;
 
+    // Per byte of meta: the hit-mask bit position (internal children, whose
+    // low five bits are >= 24, are re-ordered by the ray octant) and the bits
+    // to set there (the unary triangle count, or one bit for an internal
+    // child; zero for an empty slot, so empty slots need no branch).
+    const uint32_t octInv4 = octInv * 0x01010101u;
     uint32_t hitmask = 0;
 #pragma unroll
     for (int half = 0; half < 2; ++half) {
         const uint32_t meta4 = half == 0 ? w1.z : w1.w;
+        const uint32_t inner4 = ((meta4 & (meta4 << 1)) & 0x10101010u) >> 4;  // 1 per internal child
+        const uint32_t bitIndex4 = (meta4 ^ (octInv4 & (inner4 * 0xffu))) & 0x1f1f1f1fu;
+        const uint32_t childBits4 = (meta4 >> 5) & 0x07070707u;
         const uint32_t lx = half == 0 ? loX0 : loX1, hx = half == 0 ? hiX0 : hiX1;
         const uint32_t ly = half == 0 ? loY0 : loY1, hy = half == 0 ? hiY0 : hiY1;
         const uint32_t lz = half == 0 ? loZ0 : loZ1, hz = half == 0 ? hiZ0 : hiZ1;
 #pragma unroll
         for (int j = 0; j < 4; ++j) {
-            const uint32_t meta = (meta4 >> (8 * j)) & 0xffu;
-            if (meta == 0)
-                continue;
             const float t0x = fma_rn(byte_to_float(lx, j), ax, bx);
             const float t1x = fma_rn(byte_to_float(hx, j), ax, bx);
             const float t0y = fma_rn(byte_to_float(ly, j), ay, by);
@@ -203,96 +218,136 @@ TR_HD uint32_t intersect_node(const CwbvhNode* __restrict__ nodes, uint32_t node
             const float t1z = fma_rn(byte_to_float(hz, j), az, bz);
             const float tn = fmaxf(fmaxf(t0x, t0y), fmaxf(t0z, tmin));
             const float tf = fminf(fminf(t1x, t1y), fminf(t1z, tmax));
-            if (tn <= tf * 1.0000004f) {
-                uint32_t bit = meta & 0x1fu;
-                if (bit >= 24u)
-                    bit = 24u + ((bit - 24u) ^ octInv);
-                hitmask |= (meta >> 5) << bit;
-            }
+            if (tn <= tf * 1.0000004f)
+                hitmask |= ((childBits4 >> (8 * j)) & 7u) << ((bitIndex4 >> (8 * j)) & 31u);
         }
     }
     return hitmask;
 }
 
-// Traverses the CWBVH. ANY = true stops at the first hit inside [tmin, tmax].
-// Returns false when a bound (stack depth, step count) was exceeded; the hit
-// reported so far is kept. COUNT adds the nodes and triangles visited to *cnt.
+// Resumable traversal state of one ray: the persistent extend/connect kernels
+// keep one per lane and refill a lane with a new ray as soon as its ray ends.
+struct Traversal {
+    float3 O;
+    float3 D;
+    float3 invD;
+    float tmin;
+    float tmax;
+    float u;
+    float v;
+    uint32_t octInv;
+    uint32_t hitSlot;
+    uint32_t steps;
+    uint2 group;
+    int sp;
+    bool ok;
+};
+
+TR_HD void traversal_begin(Traversal& t, const float3& O, const float3& D, float tmin, float tmax)
+{
+    const float kTiny = 1e-20f;
+    t.O = O;
+    t.D = D;
+    t.invD = make_float3(1.0f / (fabsf(D.x) > kTiny ? D.x : copysignf(kTiny, D.x)),
+                         1.0f / (fabsf(D.y) > kTiny ? D.y : copysignf(kTiny, D.y)),
+                         1.0f / (fabsf(D.z) > kTiny ? D.z : copysignf(kTiny, D.z)));
+    const uint32_t octant = (t.invD.x < 0.f ? 1u : 0u) | (t.invD.y < 0.f ? 2u : 0u) | (t.invD.z < 0.f ? 4u : 0u);
+    t.octInv = 7u - octant;
+    t.tmin = tmin;
+    t.tmax = tmax;
+    t.u = 0.f;
+    t.v = 0.f;
+    t.hitSlot = 0xffffffffu;
+    t.steps = 0;
+    t.group = make_uint2(0u, 0x80000000u);  // the root as the only internal child of a virtual parent
+    t.sp = 0;
+    t.ok = true;
+}
+
+// One step: the next hit child node of the current group with the leaf
+// triangles it reports, then a stack pop if the group is exhausted. Returns
+// true when the ray is finished (t.hitSlot, t.tmax, t.u, t.v hold the result;
+// t.ok is false if a bound was exceeded).
+template <bool ANY, bool COUNT>
+TR_HD bool traversal_step(Traversal& t, uint2* stack, const SceneView& s, TraversalCounts* cnt)
+{
+    uint2 tris = make_uint2(0u, 0u);
+    if (t.group.y > 0x00ffffffu) {
+        const uint32_t hits = t.group.y;
+        const uint32_t bit = 31u - clz32(hits);
+        t.group.y &= ~(1u << bit);
+        const uint32_t slot = (bit - 24u) ^ t.octInv;
+        const uint32_t rel = popc32(hits & 0xffu & ((1u << slot) - 1u));
+        const uint32_t nodeIx = t.group.x + rel;
+        if (t.group.y > 0x00ffffffu) {
+            if (t.sp < kTraversalStack)
+                stack[t.sp++] = t.group;
+            else
+                t.ok = false;
+        }
+        uint32_t childBase, triBase, imask;
+        const uint32_t hm =
+            intersect_node(s.nodes, nodeIx, t.O, t.invD, t.octInv, t.tmin, t.tmax, childBase, triBase, imask);
+        if (COUNT)
+            cnt->nodes++;
+        t.group = make_uint2(childBase, (hm & 0xff000000u) | imask);
+        tris = make_uint2(triBase, hm & 0x00ffffffu);
+        if (++t.steps > kMaxTraversalSteps) {
+            t.ok = false;
+            return true;
+        }
+    }
+    while (tris.y != 0u) {
+        const uint32_t k = ffs32(tris.y) - 1u;
+        tris.y &= tris.y - 1u;
+        const uint32_t slot = tris.x + k;
+        const float4* tp = s.bvhTris + 3u * slot;
+        const float4 a = ldg(tp + 0);
+        const float4 b = ldg(tp + 1);
+        const float4 c = ldg(tp + 2);
+        if (COUNT)
+            cnt->tris++;
+        float tt, uu, vv;
+        if (intersect_triangle(t.O, t.D, a, b, c, t.tmin, t.tmax, tt, uu, vv)) {
+            if (ANY) {
+                t.tmax = tt;
+                t.hitSlot = slot;
+                return true;
+            }
+            if (tt < t.tmax || t.hitSlot == 0xffffffffu) {
+                t.tmax = tt;
+                t.hitSlot = slot;
+                t.u = uu;
+                t.v = vv;
+            }
+        }
+    }
+    if (t.group.y <= 0x00ffffffu) {
+        if (t.sp == 0)
+            return true;
+        t.group = stack[--t.sp];
+    }
+    return false;
+}
+
+// Traverses the CWBVH to the end. ANY = true stops at the first hit inside
+// [tmin, tmax]. Returns false when a bound (stack depth, step count) was
+// exceeded; the hit reported so far is kept. COUNT adds the nodes and
+// triangles visited to *cnt.
 template <bool ANY, bool COUNT = false>
 TR_HD bool traverse(const SceneView& s, const float3& O, const float3& D, float tmin, float& tmax, uint32_t& hitSlot,
                     float& hu, float& hv, TraversalCounts* cnt = nullptr)
 {
-    const float kTiny = 1e-20f;
-    const float3 invD = make_float3(1.0f / (fabsf(D.x) > kTiny ? D.x : copysignf(kTiny, D.x)),
-                                    1.0f / (fabsf(D.y) > kTiny ? D.y : copysignf(kTiny, D.y)),
-                                    1.0f / (fabsf(D.z) > kTiny ? D.z : copysignf(kTiny, D.z)));
-    const uint32_t octant = (invD.x < 0.f ? 1u : 0u) | (invD.y < 0.f ? 2u : 0u) | (invD.z < 0.f ? 4u : 0u);
-    const uint32_t octInv = 7u - octant;
-
+    Traversal t;
+    traversal_begin(t, O, D, tmin, tmax);
     uint2 stack[kTraversalStack];
-    int sp = 0;
-    uint2 group = make_uint2(0u, 0x80000000u);  // the root as the only internal child of a virtual parent
-    uint32_t steps = 0;
-    bool ok = true;
-
-    while (true) {
-        uint2 tris = make_uint2(0u, 0u);
-        if (group.y > 0x00ffffffu) {
-            const uint32_t hits = group.y;
-            const uint32_t bit = 31u - clz32(hits);
-            group.y &= ~(1u << bit);
-            const uint32_t slot = (bit - 24u) ^ octInv;
-            const uint32_t rel = popc32(hits & 0xffu & ((1u << slot) - 1u));
-            const uint32_t nodeIx = group.x + rel;
-            if (group.y > 0x00ffffffu) {
-                if (sp < kTraversalStack) {
-                    stack[sp++] = group;
-                } else {
-                    ok = false;
-                }
-            }
-            uint32_t childBase, triBase, imask;
-            const uint32_t hm = intersect_node(s.nodes, nodeIx, O, invD, octInv, tmin, tmax, childBase, triBase, imask);
-            if (COUNT)
-                cnt->nodes++;
-            group = make_uint2(childBase, (hm & 0xff000000u) | imask);
-            tris = make_uint2(triBase, hm & 0x00ffffffu);
-            if (++steps > kMaxTraversalSteps) {
-                ok = false;
-                break;
-            }
-        }
-        while (tris.y != 0u) {
-            const uint32_t t = ffs32(tris.y) - 1u;
-            tris.y &= tris.y - 1u;
-            const uint32_t slot = tris.x + t;
-            const float4* tp = s.bvhTris + 3u * slot;
-            const float4 a = ldg(tp + 0);
-            const float4 b = ldg(tp + 1);
-            const float4 c = ldg(tp + 2);
-            if (COUNT)
-                cnt->tris++;
-            float tt, uu, vv;
-            if (intersect_triangle(O, D, a, b, c, tmin, tmax, tt, uu, vv)) {
-                if (ANY) {
-                    tmax = tt;
-                    hitSlot = slot;
-                    return ok;
-                }
-                if (tt < tmax || hitSlot == 0xffffffffu) {
-                    tmax = tt;
-                    hitSlot = slot;
-                    hu = uu;
-                    hv = vv;
-                }
-            }
-        }
-        if (group.y <= 0x00ffffffu) {
-            if (sp == 0)
-                break;
-            group = stack[--sp];
-        }
+    while (!traversal_step<ANY, COUNT>(t, stack, s, cnt)) {
     }
-    return ok;
+    tmax = t.tmax;
+    hitSlot = t.hitSlot;
+    hu = t.u;
+    hv = t.v;
+    return t.ok;
 }
 
 } // namespace tr

@@ -223,7 +223,7 @@ class DeviceRenderer:
         out = {}
         for f, _ in s._fields_:
             v = getattr(s, f)
-            out[f] = list(v) if f in ("extend_rays", "shadow_rays") else v
+            out[f] = list(v) if f in ("extend_rays", "shadow_rays", "hit_rays") else v
         return out
 
     def SampleCount(self) -> int:
