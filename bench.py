@@ -57,6 +57,11 @@ def parse():
     p.add_argument("--no-cpu-baseline", action="store_true")
     p.add_argument("--profile", action="store_true",
                    help="render one eager frame of the workload and exit (the case the ncu captures use)")
+    p.add_argument("--workload", default="plain", choices=["plain", "batch", "adjoint"],
+                   help="plain: the heightfield (default); batch: the 64-scene mix in one wavefront against "
+                        "per-scene renders; adjoint: forward frame and path-replay adjoint of the "
+                        "differentiation scene")
+    p.add_argument("--batch-count", type=int, default=64)
     return p.parse_args()
 
 
@@ -222,11 +227,208 @@ def config_dict(args, scene):
     }
 
 
+def run_batch(args):
+    """The batching mix: 64 seeded sphere scenes (1k-500k triangles, 128^2-1024^2, 4/16/64 spp,
+    1-16 lights, 6 bounces, RR from bounce 3) rendered by one wavefront (all waves in one CUDA
+    graph) against the same scenes rendered one after the other through tr_render_frame
+    (graph per frame, multi_sample = min(spp, 16), the reference's largest multi-sample)."""
+    import torch
+
+    import trayracer_gb300 as tr
+    from trayracer_gb300.renderer import KernelSettings
+
+    torch.cuda.set_device(0)
+    stream = torch.cuda.current_stream()
+    sptr = stream.cuda_stream
+    flush = torch.empty(256 * 1024 * 1024 // 4, dtype=torch.float32, device="cuda")
+    t = time.perf_counter()
+    scenes = tr.sphere_batch(args.batch_count)
+    gen_s = time.perf_counter() - t
+    st = KernelSettings(multiSample=1, maxDepth=6, seed=1, rrStart=3)
+    samples = sum(s.width * s.height * s.spp for s in scenes)
+
+    # batched: one wavefront, all waves replayed from one graph
+    t = time.perf_counter()
+    b = tr.BatchRenderer(scenes)
+    build_s = time.perf_counter() - t
+    info = b.Info()
+    if args.profile:
+        b.Render(st, stream=sptr, use_graph=False)
+        print(json.dumps({"batch": b.Statistics(), "info": b.Info()}))
+        b.close()
+        return
+    for _ in range(args.warmup):
+        b.Render(st, stream=sptr)
+    torch.cuda.synchronize()
+    times = []
+    with ClockSampler(0) as clocks:
+        for _ in range(args.steps):
+            flush.fill_(1.0)
+            e0 = torch.cuda.Event(enable_timing=True)
+            e1 = torch.cuda.Event(enable_timing=True)
+            e0.record(stream)
+            b.Render(st, stream=sptr)
+            e1.record(stream)
+            e1.synchronize()
+            times.append(e0.elapsed_time(e1))
+    bstats = b.Statistics()
+    info = b.Info()
+    assert bstats["device_error"] == 0
+    batch_ms = float(statistics.median(times))
+    rays = bstats["extend_rays"] + bstats["shadow_rays"]
+    b.close()
+
+    # per scene: one context, each scene uploaded (untimed) and rendered as spp / ms graph frames
+    r = tr.DeviceRenderer(0)
+    plain_ms = 0.0
+    plain_rays = 0
+    launches = 0
+    for s in scenes:
+        ms = min(s.spp, 16)
+        frames = s.spp // ms
+        r.UpdateScene(s)
+        r.SetCamera(s.camera)
+        r.Resize((s.width, s.height))
+        r.SetSettings(KernelSettings(**{**st.__dict__, "multiSample": ms}))
+        best = None
+        for rep in range(2):  # the first pass allocates and captures the graph
+            r.Reset()
+            flush.fill_(1.0)
+            e0 = torch.cuda.Event(enable_timing=True)
+            e1 = torch.cuda.Event(enable_timing=True)
+            e0.record(stream)
+            for _ in range(frames):
+                r.RenderFrame(stream=sptr, use_graph=True)
+            e1.record(stream)
+            e1.synchronize()
+            best = e0.elapsed_time(e1)
+        plain_ms += best
+        frame_rays = 0
+        r.Reset()
+        for _ in range(frames):
+            r.RenderFrame(stream=sptr, use_graph=False)
+            frame_rays += r.Statistics()["path_count"]
+        plain_rays += frame_rays
+        launches += frames * (3 * st.maxDepth + 3)
+    r.close()
+    line = {
+        "metric": "samples/s",
+        "value": round(samples / (batch_ms / 1e3), 1),
+        "unit": "samples/s",
+        "n_gpus": 1,
+        "steps": args.steps,
+        "warmup": args.warmup,
+        "ms_per_step": round(batch_ms, 3),
+        "higher_is_better": True,
+        "scaling": "weak",
+        "vs_baseline": None,
+        "dtype": "f32",
+        "data": "synthetic",
+        "config": {"workload": f"{len(scenes)} sphere scenes, {info['triangle_count']} tris, "
+                               f"{info['pixel_count']} pixels, {samples} samples, 6 bounces, RR from 3",
+                   "waves": info["wave_count"], "wave_paths": info["wave_paths"],
+                   "l2": "flushed before each timed render (256 MiB write)"},
+        "mrays_per_s": round(rays / (batch_ms / 1e3) / 1e6, 1),
+        "gpu_launches": info["launches"],
+        "per_scene": {"ms": round(plain_ms, 3), "samples_per_s": round(samples / (plain_ms / 1e3), 1),
+                      "mrays_per_s": round(plain_rays / (plain_ms / 1e3) / 1e6, 1), "gpu_launches": launches},
+        "speedup_vs_per_scene": round(plain_ms / batch_ms, 3),
+        "rays_batch": int(rays),
+        "rays_per_scene": int(plain_rays),
+        "scene_generation_s": round(gen_s, 2),
+        "batch_build_s": round(build_s, 2),
+        "clocks": clocks.summary(),
+    }
+    print(json.dumps(line), flush=True)
+
+
+def run_adjoint(args):
+    """Differentiation scene (the Cornell box with Disney walls, 512^2, 32 spp, 6 bounces, no RR):
+    one forward frame (graph) and its path-replay adjoint for the L2 loss against a black target
+    (so every path that carried radiance is replayed); reports both times and their ratio."""
+    import torch
+
+    import trayracer_gb300 as tr
+    from trayracer_gb300.renderer import KernelSettings
+
+    torch.cuda.set_device(0)
+    stream = torch.cuda.current_stream()
+    sptr = stream.cuda_stream
+    flush = torch.empty(256 * 1024 * 1024 // 4, dtype=torch.float32, device="cuda")
+    W = H = 512
+    scene = tr.cornell_box(width=W, height=H, wall_closure=tr.TR_CLOSURE_DISNEY, max_depth=6)
+    st = KernelSettings(multiSample=32, maxDepth=6, seed=1, rrStart=1 << 30)
+    r = tr.DeviceRenderer(0)
+    r.UpdateScene(scene)
+    r.SetCamera(scene.camera)
+    r.Resize((W, H))
+    r.SetSettings(st)
+    target = torch.zeros((H, W, 4), dtype=torch.float32, device="cuda")
+    grad = torch.zeros((scene.materials.shape[0], 9), dtype=torch.float32, device="cuda")
+    if args.profile:
+        r.RenderFrame(stream=sptr, use_graph=False)
+        r.AdjointFrame(target.data_ptr(), 1.0 / 32, grad.data_ptr(), stream=sptr)
+        torch.cuda.synchronize()
+        print(json.dumps({"grad_norm": float(grad.norm())}))
+        r.close()
+        return
+    fwd, adj = [], []
+    for i in range(args.warmup + args.steps):
+        flush.fill_(1.0)
+        e0, e1, e2 = (torch.cuda.Event(enable_timing=True) for _ in range(3))
+        r.Reset()
+        e0.record(stream)
+        r.RenderFrame(stream=sptr, use_graph=True)
+        e1.record(stream)
+        # dL/dcolor of 0.5 * |img - target|^2 over the image, then the adjoint of that frame
+        img = torch.from_numpy(r.ColorBuffer()).cuda() if i == 0 else img
+        pg = img - target
+        flush.fill_(1.0)
+        e1b = torch.cuda.Event(enable_timing=True)
+        e1b.record(stream)
+        r.AdjointFrame(pg.data_ptr(), 1.0 / 32, grad.data_ptr(), stream=sptr)
+        e2.record(stream)
+        e2.synchronize()
+        if i >= args.warmup:
+            fwd.append(e0.elapsed_time(e1))
+            adj.append(e1b.elapsed_time(e2))
+    stats = r.Statistics()
+    r.close()
+    f_ms, a_ms = float(statistics.median(fwd)), float(statistics.median(adj))
+    line = {
+        "metric": "adjoint/forward time",
+        "value": round(a_ms / f_ms, 3),
+        "unit": "ratio",
+        "n_gpus": 1,
+        "steps": args.steps,
+        "warmup": args.warmup,
+        "ms_per_step": round(f_ms + a_ms, 3),
+        "higher_is_better": False,
+        "scaling": "weak",
+        "vs_baseline": None,
+        "dtype": "f32",
+        "data": "synthetic",
+        "config": {"workload": "Cornell box with Disney walls, 512x512, 32 spp, 6 bounces, no RR; "
+                               "gradients of 9 parameters for each of the 8 materials",
+                   "l2": "flushed before the forward frame and before the adjoint (256 MiB write)"},
+        "forward_ms": round(f_ms, 3),
+        "adjoint_ms": round(a_ms, 3),
+        "forward_mrays_per_s": round(stats["path_count"] / (f_ms / 1e3) / 1e6, 1),
+    }
+    print(json.dumps(line), flush=True)
+
+
 def main():
     args = parse()
     ws, rank, local = dist_env()
     if args.impl == "reference":
         run_reference(args)
+        return
+    if args.workload == "batch":
+        run_batch(args)
+        return
+    if args.workload == "adjoint":
+        run_adjoint(args)
         return
 
     import torch

@@ -318,6 +318,71 @@ tr_status tr_adjoint_frame(void* ctx, void* stream, const float* pixel_grad, flo
  * contexts) race. Guide buffers (TR_FLAG_WRITE_AOVS) are not written. */
 tr_status tr_render_frame_noalloc(void* ctx, void* stream, float* accumulator, float* colors, uint32_t sample_count);
 
+/* ---- batched rendering ----
+ * Many independent scenes of uneven triangle count, resolution and sample
+ * count rendered by one wavefront. No counterpart in the reference (one
+ * DeviceRenderer renders one scene, Tracer/Renderer/DeviceRenderer.cpp:97-133);
+ * the per-stage kernels are the ones behind tr_extend / tr_shade /
+ * tr_connect. Each item's scene gets its own BVH; the buffers are
+ * concatenated on the device and all items' paths run through the same
+ * launches in waves of at most wave_paths paths (0: 2^24), made of
+ * consecutive (item, sample) units. A path's random numbers are keyed as in
+ * tr_render_frame (pixel, sample, bounce, seed), so an item whose samples fit
+ * in one wave renders the image tr_render_frame gives for that scene with
+ * multi_sample = spp from a reset accumulator, bit for bit. */
+typedef struct tr_batch_item {
+    const tr_scene_desc* scene;     /* read during tr_batch_create only */
+    tr_camera camera;
+    uint32_t width;
+    uint32_t height;
+    uint32_t spp;                   /* samples per pixel of one tr_batch_render */
+    uint32_t reserved;
+} tr_batch_item;
+
+typedef struct tr_batch_info {
+    uint32_t item_count;
+    uint32_t wave_count;
+    uint64_t path_count;            /* sum of width * height * spp */
+    uint64_t pixel_count;           /* sum of width * height */
+    uint64_t triangle_count;
+    uint64_t device_bytes;
+    uint32_t wave_paths;            /* largest wave */
+    uint32_t launches;              /* kernels launched by one tr_batch_render (last settings) */
+    float build_time_ms;            /* host flattening + BVH builds */
+    float upload_time_ms;
+} tr_batch_info;
+
+typedef struct tr_batch_statistics {
+    uint64_t extend_rays;           /* over all waves and bounces of the last render */
+    uint64_t shadow_rays;
+    uint64_t hit_rays;
+    float render_time_ms;           /* CUDA events around the last render */
+    uint32_t device_error;
+    uint64_t traversal_extend_nodes; /* with TR_FLAG_COUNT_TRAVERSAL */
+    uint64_t traversal_extend_tris;
+    uint64_t traversal_connect_nodes;
+    uint64_t traversal_connect_tris;
+} tr_batch_statistics;
+
+/* Builds and uploads all items (host threads build the BVHs). TR_ERR_LIMIT
+ * when an item's width * height exceeds wave_paths. */
+tr_status tr_batch_create(const tr_config* config, const tr_batch_item* items, uint32_t count, uint64_t wave_paths,
+                          void** out_batch);
+tr_status tr_batch_destroy(void* batch);
+const char* tr_batch_last_error(void* batch);
+tr_status tr_batch_get_info(void* batch, tr_batch_info* info);
+/* Renders every item's spp samples from a zeroed accumulator. settings:
+ * max_depth, seed, ray_epsilon, rr_start, max_color as for tr_set_settings;
+ * multi_sample is ignored; TR_FLAG_REFERENCE_SAMPLING, TR_FLAG_WRITE_AOVS and
+ * TR_FLAG_REFERENCE_DRAW_RTL are rejected. use_graph: all waves replay from
+ * one CUDA graph, captured again when the settings change. */
+tr_status tr_batch_render(void* batch, void* stream, const tr_kernel_settings* settings, int32_t use_graph);
+tr_status tr_batch_get_statistics(void* batch, tr_batch_statistics* stats);
+/* Device pointer to an item's colors (float4 per pixel, row-major). */
+tr_status tr_batch_get_colors(void* batch, uint32_t item, void** device_rgba);
+/* Copies an item's colors to host memory (bytes >= width * height * 16). */
+tr_status tr_batch_download(void* batch, void* stream, uint32_t item, float* host_rgba, uint64_t bytes);
+
 /* ---- results ---- */
 tr_status tr_synchronize(void* ctx, void* stream);
 tr_status tr_get_statistics(void* ctx, tr_statistics* stats);

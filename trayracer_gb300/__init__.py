@@ -10,5 +10,5 @@ from ._abi import (  # noqa: F401
     TR_MAX_DEPTH,
     load_library,
 )
-from .renderer import DeviceRenderer, KernelSettings, RenderModes, TracerError, camera_to_c, settings_for  # noqa: F401
-from .scenes import CameraSpec, Scene, cornell_box, heightfield  # noqa: F401
+from .renderer import BatchRenderer, DeviceRenderer, KernelSettings, RenderModes, TracerError, camera_to_c, settings_for  # noqa: F401
+from .scenes import CameraSpec, Scene, cornell_box, heightfield, sphere_batch, sphere_scene  # noqa: F401

@@ -156,6 +156,46 @@ class Buffers(C.Structure):
     ]
 
 
+class BatchItem(C.Structure):
+    _fields_ = [
+        ("scene", C.POINTER(SceneDesc)),
+        ("camera", Camera),
+        ("width", C.c_uint32),
+        ("height", C.c_uint32),
+        ("spp", C.c_uint32),
+        ("reserved", C.c_uint32),
+    ]
+
+
+class BatchInfo(C.Structure):
+    _fields_ = [
+        ("item_count", C.c_uint32),
+        ("wave_count", C.c_uint32),
+        ("path_count", C.c_uint64),
+        ("pixel_count", C.c_uint64),
+        ("triangle_count", C.c_uint64),
+        ("device_bytes", C.c_uint64),
+        ("wave_paths", C.c_uint32),
+        ("launches", C.c_uint32),
+        ("build_time_ms", C.c_float),
+        ("upload_time_ms", C.c_float),
+    ]
+
+
+class BatchStatistics(C.Structure):
+    _fields_ = [
+        ("extend_rays", C.c_uint64),
+        ("shadow_rays", C.c_uint64),
+        ("hit_rays", C.c_uint64),
+        ("render_time_ms", C.c_float),
+        ("device_error", C.c_uint32),
+        ("traversal_extend_nodes", C.c_uint64),
+        ("traversal_extend_tris", C.c_uint64),
+        ("traversal_connect_nodes", C.c_uint64),
+        ("traversal_connect_tris", C.c_uint64),
+    ]
+
+
 # name -> (restype, argtypes) for every function include/trayracer.h declares
 _V = C.c_void_p
 _U = C.c_uint32
@@ -188,6 +228,14 @@ FUNCTIONS = {
     "tr_update_materials": (C.c_int, [_V, C.POINTER(MaterialDesc), _U]),
     "tr_adjoint_frame": (C.c_int, [_V, _V, _V, C.c_float, _V]),
     "tr_render_frame_noalloc": (C.c_int, [_V, _V, _V, _V, _U]),
+    "tr_batch_create": (C.c_int, [C.POINTER(Config), C.POINTER(BatchItem), _U, C.c_uint64, C.POINTER(_V)]),
+    "tr_batch_destroy": (C.c_int, [_V]),
+    "tr_batch_last_error": (C.c_char_p, [_V]),
+    "tr_batch_get_info": (C.c_int, [_V, C.POINTER(BatchInfo)]),
+    "tr_batch_render": (C.c_int, [_V, _V, C.POINTER(KernelSettings), C.c_int32]),
+    "tr_batch_get_statistics": (C.c_int, [_V, C.POINTER(BatchStatistics)]),
+    "tr_batch_get_colors": (C.c_int, [_V, _U, C.POINTER(_V)]),
+    "tr_batch_download": (C.c_int, [_V, _V, _U, _V, C.c_uint64]),
 }
 
 LIB_PATH = Path(__file__).resolve().parent / "libtrayracer.so"

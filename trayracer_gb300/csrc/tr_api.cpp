@@ -264,6 +264,50 @@ tr_status context_fail(void* ctx, tr_status st, const std::string& msg)
     return fail(static_cast<Context*>(ctx), st, msg);
 }
 
+bool convert_camera(const tr_camera& cam, Camera* out, std::string* err)
+{
+    Camera k{};
+    k.pos = make_float3(cam.position[0], cam.position[1], cam.position[2]);
+    k.side = make_float3(cam.side[0], cam.side[1], cam.side[2]);
+    k.up = make_float3(cam.up[0], cam.up[1], cam.up[2]);
+    k.forward = make_float3(cam.forward[0], cam.forward[1], cam.forward[2]);
+    k.aperture = cam.aperture;
+    k.distortion = cam.distortion;
+    k.focalDist = cam.focal_dist;
+    k.fov = cam.fov;
+    k.bokehSideCount = cam.bokeh_side_count;
+    k.bokehRotation = cam.bokeh_rotation;
+    k.tanFov2 = tanf(cam.fov / 2.0f);
+    if (!(cam.fov > 0.f && cam.fov < 3.14159f) || !(cam.focal_dist > 0.f)) {
+        *err = "camera fov must be in (0, pi) and focal_dist > 0";
+        return false;
+    }
+    *out = k;
+    return true;
+}
+
+bool convert_settings(const tr_kernel_settings& s, Settings* out, std::string* err)
+{
+    if (s.max_depth == 0 || s.max_depth > TR_MAX_DEPTH) {
+        *err = "multi_sample must be >= 1 and max_depth in [1, 16]";
+        return false;
+    }
+    if (!(s.ray_epsilon >= 0.f)) {
+        *err = "ray_epsilon must be >= 0";
+        return false;
+    }
+    Settings k{};
+    k.multiSample = s.multi_sample;
+    k.maxDepth = s.max_depth;
+    k.seed = s.seed;
+    k.rayEpsilon = s.ray_epsilon;
+    k.rrStart = s.rr_start;
+    k.flags = s.flags;
+    k.maxColor = s.max_color > 0.f ? s.max_color : 10.f;
+    *out = k;
+    return true;
+}
+
 } // namespace tr
 
 extern "C" {
@@ -567,19 +611,9 @@ tr_status tr_set_camera(void* ctx, const tr_camera* cam)
         return TR_ERR_INVALID_ARGUMENT;
     Context* c = static_cast<Context*>(ctx);
     Camera k{};
-    k.pos = make_float3(cam->position[0], cam->position[1], cam->position[2]);
-    k.side = make_float3(cam->side[0], cam->side[1], cam->side[2]);
-    k.up = make_float3(cam->up[0], cam->up[1], cam->up[2]);
-    k.forward = make_float3(cam->forward[0], cam->forward[1], cam->forward[2]);
-    k.aperture = cam->aperture;
-    k.distortion = cam->distortion;
-    k.focalDist = cam->focal_dist;
-    k.fov = cam->fov;
-    k.bokehSideCount = cam->bokeh_side_count;
-    k.bokehRotation = cam->bokeh_rotation;
-    k.tanFov2 = tanf(cam->fov / 2.0f);
-    if (!(cam->fov > 0.f && cam->fov < 3.14159f) || !(cam->focal_dist > 0.f))
-        return fail(c, TR_ERR_INVALID_ARGUMENT, "camera fov must be in (0, pi) and focal_dist > 0");
+    std::string err;
+    if (!convert_camera(*cam, &k, &err))
+        return fail(c, TR_ERR_INVALID_ARGUMENT, err);
     if (c->hasCamera && std::memcmp(&k, &c->camera, sizeof(Camera)) == 0)
         return TR_OK;  // unchanged camera: keep the accumulation and the captured frame graph
     c->camera = k;
@@ -593,18 +627,12 @@ tr_status tr_set_settings(void* ctx, const tr_kernel_settings* s)
     if (!ctx || !s)
         return TR_ERR_INVALID_ARGUMENT;
     Context* c = static_cast<Context*>(ctx);
-    if (s->multi_sample == 0 || s->max_depth == 0 || s->max_depth > TR_MAX_DEPTH)
+    if (s->multi_sample == 0)
         return fail(c, TR_ERR_INVALID_ARGUMENT, "multi_sample must be >= 1 and max_depth in [1, 16]");
-    if (!(s->ray_epsilon >= 0.f))
-        return fail(c, TR_ERR_INVALID_ARGUMENT, "ray_epsilon must be >= 0");
     Settings k{};
-    k.multiSample = s->multi_sample;
-    k.maxDepth = s->max_depth;
-    k.seed = s->seed;
-    k.rayEpsilon = s->ray_epsilon;
-    k.rrStart = s->rr_start;
-    k.flags = s->flags;
-    k.maxColor = s->max_color > 0.f ? s->max_color : 10.f;
+    std::string err;
+    if (!convert_settings(*s, &k, &err))
+        return fail(c, TR_ERR_INVALID_ARGUMENT, err);
     const bool changed = std::memcmp(&k, &c->settings, sizeof(Settings)) != 0;
     c->settings = k;
     if (changed) {

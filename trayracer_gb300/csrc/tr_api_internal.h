@@ -1,5 +1,6 @@
 // Read access to a context's scene, camera and settings for entry points that
-// live outside tr_api.cpp. Neither function allocates.
+// live outside tr_api.cpp, and the ABI conversions they share. None of these
+// functions allocates device memory.
 #pragma once
 
 #include <cuda_runtime.h>
@@ -24,5 +25,9 @@ struct ContextViews {
 tr_status context_views(void* ctx, ContextViews* out);
 // Records msg as the context's last error and returns st.
 tr_status context_fail(void* ctx, tr_status st, const std::string& msg);
+
+// Checked conversions of the ABI camera and settings (false + *err when invalid).
+bool convert_camera(const tr_camera& cam, Camera* out, std::string* err);
+bool convert_settings(const tr_kernel_settings& s, Settings* out, std::string* err);
 
 } // namespace tr

@@ -102,6 +102,22 @@ struct SceneView {
     uint32_t pad;
 };
 
+struct BatchItem;
+
+// Batched rendering: one wavefront over the paths of many scenes whose
+// buffers are concatenated (node, triangle, material and light indices
+// rebased). A wave holds consecutive (item, sample) units of width * height
+// paths; a segment is the run of one item's samples inside one wave.
+struct BatchSegment {
+    uint32_t pathBase;    // first path index of the segment in the wave
+    uint32_t pixelBase;   // first pixel of the segment among the wave's segments
+    uint32_t item;
+    uint32_t sampleBase;  // sample index of the segment's first unit
+    uint32_t pixels;      // width * height of the item
+    uint32_t samples;     // units (samples per pixel) of the item in the segment
+    uint32_t pad0, pad1;
+};
+
 // Per-frame constants of the wavefront (constant between resizes / setting
 // changes). Passed by value as a kernel parameter.
 struct FrameView {
@@ -119,7 +135,12 @@ struct FrameView {
     unsigned long long* traversal;  // extend nodes, extend tris, connect nodes, connect tris (counting launches)
     uint32_t capacity;
     uint32_t resX, resY;
-    uint32_t pathCount;    // resX * resY * multiSample
+    uint32_t pathCount;    // resX * resY * multiSample (batched: the paths of the wave)
+    // batched rendering only (null / 0 for one scene)
+    const BatchSegment* segments;
+    const BatchItem* items;
+    uint32_t segmentCount;
+    uint32_t pad;
 };
 
 struct Camera {
@@ -135,6 +156,21 @@ struct Camera {
     float bokehRotation;
     float tanFov2;
     float pad;
+};
+
+// One scene of a batch: its camera and film, BVH root, light range and
+// pixel range in the batch accumulator.
+struct BatchItem {
+    Camera camera;
+    uint32_t width, height;
+    uint32_t root;          // BVH root node in the concatenated node array
+    uint32_t lightBase;     // first light and alias entry
+    int32_t lightCount;
+    float lightEnergy;      // last exclusive prefix of the item's lights
+    float lightEnergyTotal;
+    uint32_t pixelBase;     // first pixel in the batch accumulator
+    uint32_t spp;
+    uint32_t pad0, pad1, pad2;
 };
 
 struct Settings {

@@ -179,8 +179,44 @@ __device__ __forceinline__ void camera_ray(const Camera& cam, uint32_t resX, uin
     T = v2 * v2;
 }
 
+// Batched rendering: the segment of a wave path (segments sorted by pathBase).
+__device__ __forceinline__ uint32_t batch_segment(const FrameView& f, uint32_t pathIx)
+{
+    uint32_t lo = 0, hi = f.segmentCount;
+    while (hi - lo > 1u) {
+        const uint32_t mid = (lo + hi) >> 1;
+        if (__ldg(&f.segments[mid].pathBase) <= pathIx)
+            lo = mid;
+        else
+            hi = mid;
+    }
+    return lo;
+}
+
+// BVH root of the scene a path belongs to (node 0 for one scene).
+template <bool BATCH>
+__device__ __forceinline__ uint32_t path_root(const FrameView& f, uint32_t pathIx)
+{
+    if (!BATCH)
+        return 0u;
+    return __ldg(&f.items[__ldg(&f.segments[batch_segment(f, pathIx)].item)].root);
+}
+
+// The scene view of a batch item: the concatenated buffers with the item's
+// light range.
+__device__ __forceinline__ SceneView item_scene(const SceneView& s, const BatchItem& it)
+{
+    SceneView si = s;
+    si.lights = s.lights + it.lightBase;
+    si.alias = s.alias + it.lightBase;
+    si.lightCount = it.lightCount;
+    si.lightEnergy = it.lightEnergy;
+    si.lightEnergyTotal = it.lightEnergyTotal;
+    return si;
+}
+
 // ------------------------------------------------------------------ kernels
-template <bool REF>
+template <bool REF, bool BATCH>
 __global__ void __launch_bounds__(256) generate_kernel(FrameView f, Camera cam, Settings st)
 {
     const uint32_t pathIx = blockIdx.x * blockDim.x + threadIdx.x;
@@ -192,7 +228,16 @@ __global__ void __launch_bounds__(256) generate_kernel(FrameView f, Camera cam, 
     const uint32_t sc = *f.sampleCount;
     float3 O, D;
     float T;
-    if (REF) {
+    if (BATCH) {
+        // the item's camera and film; the counter RNG keyed as for one scene
+        const BatchSegment sg = f.segments[batch_segment(f, pathIx)];
+        const uint32_t rel = pathIx - sg.pathBase;
+        const uint32_t pixel = rel % sg.pixels;
+        const BatchItem& it = f.items[sg.item];
+        CounterRng rng;
+        rng.init(pixel, sg.sampleBase + rel / sg.pixels, 0u, st.seed);
+        camera_ray(it.camera, it.width, it.height, pixel % it.width, pixel / it.width, rng, false, O, D, T);
+    } else if (REF) {
         RefRng rng{tea2(st.seed + pathIx, sc << 1)};
         const bool rtl = (st.flags & TR_FLAG_REFERENCE_DRAW_RTL) != 0;
         camera_ray(cam, f.resX, f.resY, pixelIx % f.resX, pixelIx / f.resX, rng, rtl, O, D, T);
@@ -238,7 +283,7 @@ constexpr uint32_t kRefillBelow = 24;
 // state and hit record; missed rays end here. COUNT = true also sums the nodes
 // visited and triangles tested (for the traversal bytes of the roofline); it
 // is launched outside timed regions.
-template <bool COUNT>
+template <bool COUNT, bool BATCH>
 __global__ void __launch_bounds__(128) extend_kernel(SceneView s, FrameView f, Settings st, uint32_t bounce)
 {
     const uint32_t count = queue_length(f, bounce);
@@ -269,7 +314,8 @@ __global__ void __launch_bounds__(128) extend_kernel(SceneView s, FrameView f, S
                     O4 = __ldcs(in + i);
                     D4 = __ldcs(in + i + cap);
                     T4 = __ldcs(in + i + 2 * cap);
-                    traversal_begin(t, f3(O4), f3(D4), st.rayEpsilon, kDstMax);
+                    traversal_begin(t, f3(O4), f3(D4), st.rayEpsilon, kDstMax,
+                                    path_root<BATCH>(f, path_ix(__float_as_uint(O4.w))));
                     alive = true;
                 } else {
                     more = false;
@@ -632,7 +678,7 @@ __device__ __forceinline__ void shade_path(const SceneView& s, const FrameView& 
     }
 }
 
-template <bool REF>
+template <bool REF, bool BATCH>
 __global__ void __launch_bounds__(128) shade_kernel(SceneView s, FrameView f, Settings st, uint32_t bounce)
 {
     const uint32_t count = __ldcg(f.counters + kHitCounterBase + bounce);
@@ -657,7 +703,14 @@ __global__ void __launch_bounds__(128) shade_kernel(SceneView s, FrameView f, Se
             const float4 T4 = __ldcs(in + i + 2 * cap);
             const uint4 hd = __ldcs(f.hits + i);
             const uint32_t pathIx = path_ix(__float_as_uint(O4.w));
-            if (REF) {
+            if (BATCH) {
+                const BatchSegment sg = f.segments[batch_segment(f, pathIx)];
+                const uint32_t rel = pathIx - sg.pathBase;
+                const SceneView si = item_scene(s, f.items[sg.item]);
+                CounterRng rng;
+                rng.init(rel % sg.pixels, sg.sampleBase + rel / sg.pixels, bounce + 1u, st.seed);
+                shade_path<false>(si, f, st, bounce, sc, O4, D4, T4, hd, rng, wantExt, ext, wantShadow, sh);
+            } else if (REF) {
                 RefRng rng{tea2(st.seed + pathIx, sc + bounce + 1u)};
                 shade_path<REF>(s, f, st, bounce, sc, O4, D4, T4, hd, rng, wantExt, ext, wantShadow, sh);
             } else {
@@ -683,7 +736,7 @@ __global__ void __launch_bounds__(128) shade_kernel(SceneView s, FrameView f, Se
 
 // Any hit of the bounce's shadow queue over [eps, dist - 2 eps]; an unoccluded
 // ray adds its radiance to its path. Same lane refill as extend_kernel.
-template <bool COUNT>
+template <bool COUNT, bool BATCH>
 __global__ void __launch_bounds__(128) connect_kernel(SceneView s, FrameView f, Settings st, uint32_t bounce)
 {
     const uint32_t count = __ldcg(f.counters + kShadowCounterBase + bounce);
@@ -710,7 +763,8 @@ __global__ void __launch_bounds__(128) connect_kernel(SceneView s, FrameView f, 
                     const float4 L4 = __ldcs(f.shadow + i + cap);
                     ray = i;
                     pathIx = __float_as_uint(O4.w);
-                    traversal_begin(t, f3(O4), f3(L4), st.rayEpsilon, L4.w - (2 * st.rayEpsilon));
+                    traversal_begin(t, f3(O4), f3(L4), st.rayEpsilon, L4.w - (2 * st.rayEpsilon),
+                                    path_root<BATCH>(f, pathIx));
                     alive = true;
                 } else {
                     more = false;
@@ -758,6 +812,47 @@ __global__ void __launch_bounds__(256) finalize_kernel(FrameView f, Settings st)
     f.accumulator[p] = acc;
     const float n = float(sc + st.multiSample);
     f.colors[p] = make_float4(acc.x / n, acc.y / n, acc.z / n, acc.w / n);
+}
+
+// Batched rendering: sums each pixel's samples of the wave in sample order
+// and adds them to the item's pixel of the batch accumulator (zeroed before
+// the first wave; waves run in order, and an item has at most one segment per
+// wave, so no two threads add to one pixel).
+__global__ void __launch_bounds__(256) batch_finalize_kernel(FrameView f, uint32_t wavePixels)
+{
+    const uint32_t q = blockIdx.x * blockDim.x + threadIdx.x;
+    if (q >= wavePixels)
+        return;
+    uint32_t lo = 0, hi = f.segmentCount;
+    while (hi - lo > 1u) {
+        const uint32_t mid = (lo + hi) >> 1;
+        if (__ldg(&f.segments[mid].pixelBase) <= q)
+            lo = mid;
+        else
+            hi = mid;
+    }
+    const BatchSegment sg = f.segments[lo];
+    const uint32_t p = q - sg.pixelBase;
+    float3 sum = f3(0.f);
+    for (uint32_t k = 0; k < sg.samples; ++k) {
+        const float4 r = f.radiance[sg.pathBase + k * sg.pixels + p];
+        sum = sum + f3(r);
+    }
+    float4* a = f.accumulator + f.items[sg.item].pixelBase + p;
+    const float4 acc = *a;
+    *a = make_float4(acc.x + sum.x, acc.y + sum.y, acc.z + sum.z, acc.w + float(sg.samples));
+}
+
+// colors = accumulator / samples, over all pixels of a batch.
+__global__ void __launch_bounds__(256) batch_resolve_kernel(const float4* __restrict__ acc, float4* __restrict__ colors,
+                                                            uint32_t pixels)
+{
+    const uint32_t p = blockIdx.x * blockDim.x + threadIdx.x;
+    if (p >= pixels)
+        return;
+    const float4 a = acc[p];
+    const float n = a.w;
+    colors[p] = n > 0.f ? make_float4(a.x / n, a.y / n, a.z / n, a.w / n) : make_float4(0.f, 0.f, 0.f, 0.f);
 }
 
 // Adds each lane's gradient slots [first, last) to the row of its key
@@ -992,40 +1087,60 @@ cudaError_t launch_generate(const FrameView& f, const Camera& cam, const Setting
     if (f.pathCount == 0)
         return cudaSuccess;
     const uint32_t blocks = (f.pathCount + 255u) / 256u;
-    if (st.flags & TR_FLAG_REFERENCE_SAMPLING)
-        generate_kernel<true><<<blocks, 256, 0, stream>>>(f, cam, st);
+    if (f.segments)
+        generate_kernel<false, true><<<blocks, 256, 0, stream>>>(f, cam, st);
+    else if (st.flags & TR_FLAG_REFERENCE_SAMPLING)
+        generate_kernel<true, false><<<blocks, 256, 0, stream>>>(f, cam, st);
     else
-        generate_kernel<false><<<blocks, 256, 0, stream>>>(f, cam, st);
+        generate_kernel<false, false><<<blocks, 256, 0, stream>>>(f, cam, st);
     return cudaGetLastError();
 }
 
 cudaError_t launch_extend(const SceneView& s, const FrameView& f, const Settings& st, uint32_t bounce,
                           const LaunchShape& shape, cudaStream_t stream)
 {
-    if (st.flags & TR_FLAG_COUNT_TRAVERSAL)
-        extend_kernel<true><<<shape.extendBlocks, 128, 0, stream>>>(s, f, st, bounce);
-    else
-        extend_kernel<false><<<shape.extendBlocks, 128, 0, stream>>>(s, f, st, bounce);
+    const bool count = (st.flags & TR_FLAG_COUNT_TRAVERSAL) != 0;
+    if (f.segments) {
+        if (count)
+            extend_kernel<true, true><<<shape.extendBlocks, 128, 0, stream>>>(s, f, st, bounce);
+        else
+            extend_kernel<false, true><<<shape.extendBlocks, 128, 0, stream>>>(s, f, st, bounce);
+    } else {
+        if (count)
+            extend_kernel<true, false><<<shape.extendBlocks, 128, 0, stream>>>(s, f, st, bounce);
+        else
+            extend_kernel<false, false><<<shape.extendBlocks, 128, 0, stream>>>(s, f, st, bounce);
+    }
     return cudaGetLastError();
 }
 
 cudaError_t launch_shade(const SceneView& s, const FrameView& f, const Settings& st, uint32_t bounce,
                          const LaunchShape& shape, cudaStream_t stream)
 {
-    if (st.flags & TR_FLAG_REFERENCE_SAMPLING)
-        shade_kernel<true><<<shape.shadeBlocks, 128, 0, stream>>>(s, f, st, bounce);
+    if (f.segments)
+        shade_kernel<false, true><<<shape.shadeBlocks, 128, 0, stream>>>(s, f, st, bounce);
+    else if (st.flags & TR_FLAG_REFERENCE_SAMPLING)
+        shade_kernel<true, false><<<shape.shadeBlocks, 128, 0, stream>>>(s, f, st, bounce);
     else
-        shade_kernel<false><<<shape.shadeBlocks, 128, 0, stream>>>(s, f, st, bounce);
+        shade_kernel<false, false><<<shape.shadeBlocks, 128, 0, stream>>>(s, f, st, bounce);
     return cudaGetLastError();
 }
 
 cudaError_t launch_connect(const SceneView& s, const FrameView& f, const Settings& st, uint32_t bounce,
                            const LaunchShape& shape, cudaStream_t stream)
 {
-    if (st.flags & TR_FLAG_COUNT_TRAVERSAL)
-        connect_kernel<true><<<shape.connectBlocks, 128, 0, stream>>>(s, f, st, bounce);
-    else
-        connect_kernel<false><<<shape.connectBlocks, 128, 0, stream>>>(s, f, st, bounce);
+    const bool count = (st.flags & TR_FLAG_COUNT_TRAVERSAL) != 0;
+    if (f.segments) {
+        if (count)
+            connect_kernel<true, true><<<shape.connectBlocks, 128, 0, stream>>>(s, f, st, bounce);
+        else
+            connect_kernel<false, true><<<shape.connectBlocks, 128, 0, stream>>>(s, f, st, bounce);
+    } else {
+        if (count)
+            connect_kernel<true, false><<<shape.connectBlocks, 128, 0, stream>>>(s, f, st, bounce);
+        else
+            connect_kernel<false, false><<<shape.connectBlocks, 128, 0, stream>>>(s, f, st, bounce);
+    }
     return cudaGetLastError();
 }
 
@@ -1068,6 +1183,22 @@ cudaError_t launch_adjoint(const SceneView& s, const FrameView& f, const Camera&
     return cudaGetLastError();
 }
 
+cudaError_t launch_batch_finalize(const FrameView& f, uint32_t wavePixels, cudaStream_t stream)
+{
+    if (wavePixels == 0)
+        return cudaSuccess;
+    batch_finalize_kernel<<<(wavePixels + 255u) / 256u, 256, 0, stream>>>(f, wavePixels);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_batch_resolve(const float4* accumulator, float4* colors, uint32_t pixels, cudaStream_t stream)
+{
+    if (pixels == 0)
+        return cudaSuccess;
+    batch_resolve_kernel<<<(pixels + 255u) / 256u, 256, 0, stream>>>(accumulator, colors, pixels);
+    return cudaGetLastError();
+}
+
 LaunchShape default_launch_shape(int device, uint32_t capacity)
 {
     LaunchShape shape;
@@ -1076,13 +1207,13 @@ LaunchShape default_launch_shape(int device, uint32_t capacity)
     if (sms <= 0)
         sms = 1;
     int perSm = 0;
-    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&perSm, extend_kernel<false>, 128, 0);
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&perSm, extend_kernel<false, false>, 128, 0);
     shape.extendBlocks = uint32_t(sms) * uint32_t(perSm > 0 ? perSm : 4);
     perSm = 0;
-    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&perSm, connect_kernel<false>, 128, 0);
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&perSm, connect_kernel<false, false>, 128, 0);
     shape.connectBlocks = uint32_t(sms) * uint32_t(perSm > 0 ? perSm : 4);
     perSm = 0;
-    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&perSm, shade_kernel<false>, 128, 0);
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&perSm, shade_kernel<false, false>, 128, 0);
     const uint32_t maxShade = uint32_t(sms) * uint32_t(perSm > 0 ? perSm : 4) * 4u;
     const uint32_t need = (capacity + 127u) / 128u;
     shape.shadeBlocks = need < maxShade ? (need > 0 ? need : 1u) : maxShade;

@@ -27,6 +27,10 @@ cudaError_t launch_shade(const SceneView& s, const FrameView& f, const Settings&
 cudaError_t launch_connect(const SceneView& s, const FrameView& f, const Settings& st, uint32_t bounce,
                            const LaunchShape& shape, cudaStream_t stream);
 cudaError_t launch_finalize(const FrameView& f, const Settings& st, cudaStream_t stream);
+// Batched rendering: adds a wave's samples to the batch accumulator; then
+// colors = accumulator / samples over all batch pixels.
+cudaError_t launch_batch_finalize(const FrameView& f, uint32_t wavePixels, cudaStream_t stream);
+cudaError_t launch_batch_resolve(const float4* accumulator, float4* colors, uint32_t pixels, cudaStream_t stream);
 cudaError_t launch_adjoint(const SceneView& s, const FrameView& f, const Camera& cam, const Settings& st,
                            const float4* pixelGrad, float scale, float* grads, uint32_t sampleCount,
                            uint32_t materialCount, const LaunchShape& shape, cudaStream_t stream);

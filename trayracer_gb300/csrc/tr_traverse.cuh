@@ -243,7 +243,7 @@ struct Traversal {
     bool ok;
 };
 
-TR_HD void traversal_begin(Traversal& t, const float3& O, const float3& D, float tmin, float tmax)
+TR_HD void traversal_begin(Traversal& t, const float3& O, const float3& D, float tmin, float tmax, uint32_t root = 0)
 {
     const float kTiny = 1e-20f;
     t.O = O;
@@ -259,7 +259,7 @@ TR_HD void traversal_begin(Traversal& t, const float3& O, const float3& D, float
     t.v = 0.f;
     t.hitSlot = 0xffffffffu;
     t.steps = 0;
-    t.group = make_uint2(0u, 0x80000000u);  // the root as the only internal child of a virtual parent
+    t.group = make_uint2(root, 0x80000000u);  // the root as the only internal child of a virtual parent
     t.sp = 0;
     t.ok = true;
 }

@@ -283,3 +283,70 @@ def settings_for(scene: Scene, multi_sample: int = 1, reference: bool = False, s
     return KernelSettings(multiSample=multi_sample, maxDepth=scene.max_depth,
                           seed=scene.seed if seed is None else seed, rrStart=1 if reference else scene.rr_start,
                           flags=flags)
+
+
+class BatchRenderer:
+    """Many independent scenes rendered by one wavefront (tr_batch_*): each item is
+    (scene, spp) with the scene's own camera and resolution."""
+
+    def __init__(self, scenes, spp=None, wave_paths: int = 0, device: int = 0):
+        self._lib = _abi.load_library()
+        self._b = C.c_void_p()
+        self.scenes = list(scenes)
+        self.spp = [s.spp for s in self.scenes] if spp is None else [int(x) for x in spp]
+        holders = [SceneDescHolder(s) for s in self.scenes]
+        items = (_abi.BatchItem * len(self.scenes))()
+        for i, (s, h) in enumerate(zip(self.scenes, holders)):
+            items[i].scene = C.pointer(h.desc)
+            items[i].camera = camera_to_c(s.camera)
+            items[i].width = s.width
+            items[i].height = s.height
+            items[i].spp = self.spp[i]
+        cfg = _abi.Config(device, _abi.TR_ABI_VERSION)
+        st = self._lib.tr_batch_create(C.byref(cfg), items, len(self.scenes), int(wave_paths), C.byref(self._b))
+        if st != 0:
+            raise TracerError(st, "tr_batch_create")
+
+    def _check(self, st: int, where: str):
+        if st != 0:
+            raise TracerError(st, where, self._lib.tr_batch_last_error(self._b).decode(errors="replace"))
+
+    def close(self):
+        if self._b:
+            self._lib.tr_batch_destroy(self._b)
+            self._b = C.c_void_p()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *exc):
+        self.close()
+
+    def Render(self, settings: KernelSettings, stream: int = 0, use_graph: bool = True):
+        c = settings.to_c()
+        self._check(self._lib.tr_batch_render(self._b, C.c_void_p(stream or None), C.byref(c), int(use_graph)),
+                    "tr_batch_render")
+
+    def Info(self) -> dict:
+        i = _abi.BatchInfo()
+        self._check(self._lib.tr_batch_get_info(self._b, C.byref(i)), "tr_batch_get_info")
+        return {f: getattr(i, f) for f, _ in i._fields_}
+
+    def Statistics(self) -> dict:
+        s = _abi.BatchStatistics()
+        self._check(self._lib.tr_batch_get_statistics(self._b, C.byref(s)), "tr_batch_get_statistics")
+        return {f: getattr(s, f) for f, _ in s._fields_}
+
+    def Image(self, item: int, out: np.ndarray | None = None, stream: int = 0) -> np.ndarray:
+        s = self.scenes[item]
+        if out is None:
+            out = np.empty((s.height, s.width, 4), np.float32)
+        self._check(self._lib.tr_batch_download(self._b, C.c_void_p(stream or None), item, out.ctypes.data,
+                                                out.nbytes), "tr_batch_download")
+        return out

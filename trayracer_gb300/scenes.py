@@ -308,7 +308,121 @@ def random_soup(n_tris: int = 2000, seed: int = 7, extent: float = 1.0) -> Scene
                  CameraSpec(position=(0.0, 0.0, -3.0)), 64, 64, 1, 1)
 
 
+def _octahedron_sphere(subdiv: int):
+    """Unit sphere from an octahedron whose faces are cut into subdiv^2 triangles each (8 subdiv^2
+    triangles); grid points are projected onto the sphere with a square root only."""
+    f32 = np.float32
+    axes = np.array([[1, 0, 0], [-1, 0, 0], [0, 1, 0], [0, -1, 0], [0, 0, 1], [0, 0, -1]], np.float32)
+    faces = []
+    for sx in (0, 1):
+        for sy in (2, 3):
+            for sz in (4, 5):
+                a, b, c = axes[sx], axes[sy], axes[sz]
+                # keep the winding outward
+                if float(np.dot(np.cross(b - a, c - a), a + b + c)) < 0.0:
+                    b, c = c, b
+                faces.append((a, b, c))
+    n = subdiv
+    ii, jj = [], []
+    for i in range(n + 1):
+        for j in range(n + 1 - i):
+            ii.append(i)
+            jj.append(j)
+    ii = np.array(ii, np.int64)
+    jj = np.array(jj, np.int64)
+    lookup = -np.ones((n + 1, n + 1), np.int64)
+    lookup[ii, jj] = np.arange(ii.size)
+    tri = []
+    for i in range(n):
+        for j in range(n - i):
+            tri.append((lookup[i, j], lookup[i + 1, j], lookup[i, j + 1]))
+            if i + j < n - 1:
+                tri.append((lookup[i + 1, j], lookup[i + 1, j + 1], lookup[i, j + 1]))
+    tri = np.array(tri, np.int64)
+    pos, idx = [], []
+    for a, b, c in faces:
+        wa = (f32(n) - ii - jj).astype(np.float32)[:, None]
+        p = (wa * a + ii.astype(np.float32)[:, None] * b + jj.astype(np.float32)[:, None] * c) / f32(n)
+        inv = f32(1.0) / np.sqrt((p[:, 0] * p[:, 0] + p[:, 1] * p[:, 1]) + p[:, 2] * p[:, 2])
+        idx.append(tri + len(pos) * ii.size)
+        pos.append((p * inv[:, None]).astype(np.float32))
+    return np.concatenate(pos).astype(np.float32), np.concatenate(idx).astype(np.uint32)
+
+
+def sphere_scene(seed: int, triangles: int, width: int, height: int, spp: int, n_lights: int,
+                 max_depth: int = 6) -> Scene:
+    """Tessellated spheres (radius U[0.1, 2]) in a 20^3 box over a floor, about `triangles`
+    triangles in total, lit by n_lights downward emissive triangles (log-uniform intensity in
+    [10, 1000]); 4 Disney materials."""
+    rng = np.random.default_rng(seed)
+    f32 = np.float32
+    subdiv = 2
+    while 8 * (2 * subdiv) ** 2 <= triangles // 2 and subdiv < 128:
+        subdiv *= 2
+    per = 8 * subdiv * subdiv
+    count = max(1, int(round(triangles / per)))
+    unit_p, unit_i = _octahedron_sphere(subdiv)
+    mats = []
+    for _ in range(4):
+        p = rng.random(3).astype(np.float32)
+        mats.append(material(diffuse=rng.random(3).astype(np.float32) * f32(0.8) + f32(0.1),
+                             closure=TR_CLOSURE_DISNEY, roughness=f32(0.2) + f32(0.8) * p[0], metallic=p[1],
+                             specular=p[2]))
+    pos, nrm, idx, mat = [], [], [], []
+    base = 0
+    for _ in range(count):
+        c = rng.uniform(-8.0, 8.0, 3).astype(np.float32)
+        r = f32(0.1) + f32(1.9) * rng.random(dtype=np.float32)
+        pos.append((unit_p * r + c).astype(np.float32))
+        nrm.append(unit_p)
+        idx.append(unit_i + np.uint32(base))
+        mat.append(np.full(unit_i.shape[0], rng.integers(0, 4), np.uint32))
+        base += unit_p.shape[0]
+    # floor
+    fl = np.array([[-10, -10, -10], [10, -10, -10], [10, -10, 10], [-10, -10, 10]], np.float32)
+    pos.append(fl)
+    nrm.append(np.tile(np.array([0, 1, 0], np.float32), (4, 1)))
+    idx.append(np.array([[base, base + 2, base + 1], [base, base + 3, base + 2]], np.uint32))
+    mat.append(np.zeros(2, np.uint32))
+    base += 4
+    for k in range(n_lights):
+        cx, cz = rng.uniform(-8.0, 8.0, 2).astype(np.float32)
+        cy = f32(10.0)
+        s = f32(0.8)
+        pos.append(np.array([[cx - s, cy, cz - s], [cx + s, cy, cz - s], [cx, cy, cz + s]], np.float32))
+        nrm.append(np.tile(np.array([0, -1, 0], np.float32), (3, 1)))
+        intensity = np.float32(10.0 * 100.0 ** rng.random())
+        mats.append(material(diffuse=(1, 1, 1), emissive=(intensity, intensity, intensity),
+                             closure=TR_CLOSURE_DIFFUSE))
+        idx.append(np.array([[base, base + 1, base + 2]], np.uint32))
+        mat.append(np.array([len(mats) - 1], np.uint32))
+        base += 3
+    cam = CameraSpec(position=(0.0, 4.0, -28.0), target=(0.0, 0.0, 0.0), up=(0.0, 1.0, 0.0),
+                     fov=float(np.float32(60.0 * np.pi / 180.0)))
+    return Scene(f"spheres_{seed}", np.concatenate(pos).astype(np.float32), np.concatenate(nrm).astype(np.float32),
+                 None, np.concatenate(idx).astype(np.uint32), np.concatenate(mat).astype(np.uint32),
+                 np.array(mats, MATERIAL_DTYPE), cam, width, height, spp, max_depth, 1 << 30, seed)
+
+
+def sphere_batch(count: int = 64, seed: int = 11, min_tris: int = 1000, max_tris: int = 500_000,
+                 resolutions=(128, 256, 512, 1024), spps=(4, 16, 64)) -> list[Scene]:
+    """The batching mix: `count` independent seeded scenes with triangle counts log-uniform in
+    [min_tris, max_tris], square resolutions and spp drawn uniformly from the given sets, 1-16
+    emissive triangles each, 6 bounces."""
+    rng = np.random.default_rng(seed)
+    ratio = max_tris / min_tris
+    out = []
+    for k in range(count):
+        tris = int(round(min_tris * ratio ** float(rng.random())))
+        res = int(resolutions[rng.integers(0, len(resolutions))])
+        spp = int(spps[rng.integers(0, len(spps))])
+        lights = int(rng.integers(1, 17))
+        out.append(sphere_scene(seed * 1000 + k, tris, res, res, spp, lights))
+    return out
+
+
 CONFIGS = {
     "cornell_box": cornell_box,
     "heightfield": heightfield,
+    "sphere_batch": sphere_batch,
 }
