@@ -108,8 +108,10 @@ def test_batch_counting_and_errors():
         bad = KernelSettings(**{**st.__dict__, "flags": tr.TR_FLAG_REFERENCE_SAMPLING})
         with pytest.raises(tr.TracerError):
             b.Render(bad)
-        with pytest.raises(tr.TracerError):
-            b.Image(len(scenes))
+        lib = tr.load_library()
+        buf = np.empty(16, np.float32)
+        assert lib.tr_batch_download(b._b, None, len(scenes), buf.ctypes.data, buf.nbytes) == 1
+        assert lib.tr_batch_download(b._b, None, 0, buf.ctypes.data, buf.nbytes) == 1  # buffer too small
     with pytest.raises(tr.TracerError) as e:
         tr.BatchRenderer(scenes, wave_paths=100)  # an item larger than a wave
     assert e.value.status == 6

@@ -66,6 +66,9 @@ struct Context {
     uint32_t width = 0, height = 0;
     DeviceArena frameArena;
     FrameView frame{};
+    DeviceArena adjointArena;      // path-replay scratch, allocated by the first tr_adjoint_frame of a frame size
+    AdjointView adjoint{};
+    uint32_t* adjointCounters = nullptr;
     size_t frameCapacity = 0;
     uint32_t frameW = 0, frameH = 0, frameMs = 0;
     LaunchShape shape{};
@@ -137,6 +140,7 @@ tr_status ensure_frame(Context* c)
 
     invalidate_graph(c);
     c->frameArena.release();
+    c->adjointArena.release();
     const size_t cap = size_t(paths);
     size_t off = 0;
     auto take = [&](size_t bytes) {
@@ -388,6 +392,7 @@ tr_status tr_destroy(void* ctx)
     invalidate_graph(c);
     c->sceneArena.release();
     c->frameArena.release();
+    c->adjointArena.release();
     if (c->hostCounters)
         cudaFreeHost(c->hostCounters);
     cudaEvent_t* evs[] = {&c->evStart, &c->evGenerate, &c->evFinal};
@@ -588,9 +593,43 @@ tr_status tr_adjoint_frame(void* ctx, void* stream, const float* pixel_grad, flo
     if (c->sampleCount < c->settings.multiSample)
         return fail(c, TR_ERR_NOT_READY, "render a frame before its adjoint");
     cudaSetDevice(c->device);
-    const uint32_t sc = c->sampleCount - c->settings.multiSample;
-    TR_CUDA(c, launch_adjoint(c->scene, c->frame, c->camera, c->settings, reinterpret_cast<const float4*>(pixel_grad),
-                              scale, param_grad, sc, c->materialCount, c->shape, pick_stream(c, stream)));
+    const size_t cap = c->frame.capacity;
+    if (!c->adjointArena.base) {
+        // lrem 16 B + pending 80 B + NEE payload 32 B + visible slot 4 B per path, and the counters
+        size_t off = 0;
+        auto take = [&](size_t bytes) {
+            const size_t o = off;
+            off = align256(off + bytes);
+            return o;
+        };
+        const size_t oL = take(cap * sizeof(float4));
+        const size_t oP = take(5 * cap * sizeof(float4));
+        const size_t oS = take(2 * cap * sizeof(float4));
+        const size_t oV = take(cap * sizeof(uint32_t));
+        const size_t oC = take(kCounterWords * sizeof(uint32_t));
+        void* base = nullptr;
+        const cudaError_t e = cudaMalloc(&base, off);
+        if (e != cudaSuccess)
+            return cuda_fail(c, e, "cudaMalloc(adjoint scratch)");
+        c->adjointArena.base = base;
+        c->adjointArena.bytes = off;
+        char* b = static_cast<char*>(base);
+        c->adjoint.lrem = reinterpret_cast<float4*>(b + oL);
+        c->adjoint.pending = reinterpret_cast<float4*>(b + oP);
+        c->adjoint.shadowAdj = reinterpret_cast<float4*>(b + oS);
+        c->adjoint.visible = reinterpret_cast<uint32_t*>(b + oV);
+        c->adjointCounters = reinterpret_cast<uint32_t*>(b + oC);
+    }
+    AdjointView a = c->adjoint;
+    a.pixelGrad = reinterpret_cast<const float4*>(pixel_grad);
+    a.grads = param_grad;
+    a.scale = scale;
+    a.materialCount = c->materialCount;
+    a.sampleBase = c->sampleCount - c->settings.multiSample;
+    // the replay keeps the forward frame's statistics: its queues are reused, its counters are its own
+    FrameView f = c->frame;
+    f.counters = c->adjointCounters;
+    TR_CUDA(c, launch_adjoint(c->scene, f, c->camera, c->settings, a, c->shape, pick_stream(c, stream)));
     return TR_OK;
 }
 

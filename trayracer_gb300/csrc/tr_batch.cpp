@@ -273,7 +273,8 @@ tr_status tr_batch_create(const tr_config* config, const tr_batch_item* items, u
         delete b;
         return st;
     };
-    if (cudaStreamCreateWithFlags(&b->stream, cudaStreamNonBlocking) != cudaSuccess ||
+    // a blocking stream, like the context's: work on it is ordered with the legacy default stream
+    if (cudaStreamCreate(&b->stream) != cudaSuccess ||
         cudaEventCreate(&b->evStart) != cudaSuccess || cudaEventCreate(&b->evStop) != cudaSuccess)
         return bail(TR_ERR_CUDA);
 

@@ -173,6 +173,21 @@ struct BatchItem {
     uint32_t pad0, pad1, pad2;
 };
 
+// Scratch and parameters of the path-replay adjoint (by path index, plane
+// stride = the frame's capacity).
+struct AdjointView {
+    float4* lrem;          // radiance of the path not yet accounted for
+    float4* pending;       // 5 planes: d log f_c / d theta_k of the last extend direction (18 floats, c-major), key
+    float4* shadowAdj;     // 2 planes by shadow slot: (wo, bits(matIx)), (wiLight, bits(lightIx))
+    uint32_t* visible;     // shadow slots found unoccluded
+    const float4* pixelGrad;
+    float* grads;          // materialCount x kGradSlots
+    float scale;
+    uint32_t materialCount;
+    uint32_t sampleBase;   // sample count before the replayed frame (its paths' sample keys start here)
+    uint32_t pad;
+};
+
 struct Settings {
     uint32_t multiSample;
     uint32_t maxDepth;
@@ -186,14 +201,14 @@ struct Settings {
 
 // Device counter words: per bounce the extend queue length, the shadow queue
 // length, the work-fetch cursors of the persistent extend and connect launches,
-// and the hit queue length (rays of the extend queue that hit something); then
-// the path cursor of the persistent adjoint launch.
+// the hit queue length (rays of the extend queue that hit something), and the
+// number of unoccluded shadow rays (adjoint replay only).
 constexpr uint32_t kShadowCounterBase = TR_MAX_DEPTH + 1;
 constexpr uint32_t kExtendWorkBase = 2 * (TR_MAX_DEPTH + 1);
 constexpr uint32_t kConnectWorkBase = 3 * (TR_MAX_DEPTH + 1);
 constexpr uint32_t kHitCounterBase = 4 * (TR_MAX_DEPTH + 1);
-constexpr uint32_t kAdjointCursor = 5 * (TR_MAX_DEPTH + 1);
-constexpr uint32_t kCounterWords = kAdjointCursor + 1;
+constexpr uint32_t kVisibleCounterBase = 5 * (TR_MAX_DEPTH + 1);
+constexpr uint32_t kCounterWords = 6 * (TR_MAX_DEPTH + 1);
 
 // Path index / flag packing, Tracer/Common/CommonStructs.h:46-71.
 constexpr uint32_t kPathIxShift = 4;

@@ -898,103 +898,156 @@ constexpr uint32_t kAdjointWarps = kAdjointThreads / 32;
 // 9 floats per material, up to 341 materials; more use global atomics.
 constexpr size_t kAdjointSmemMax = 48 * 1024;
 
-// Path-replay adjoint of one frame (default sampling mode): every path is
-// replayed from its random keys, re-tracing its extend and shadow rays; at
-// each vertex the derivative of the closure value (dual numbers) is weighted
-// by the radiance that reached the camera through that value: the vertex's
-// own NEE contribution for the light direction, and the radiance still to
-// come (the path's total minus what was already accounted for) for the
-// extend direction. Emission gradients come from emissive hits and NEE.
-//
-// Persistent warps: a lane whose path ended takes the next path index from
-// a device cursor, so lanes of one warp may be at different bounces and no
-// warp idles behind its longest path. With SMEM the gradients are summed per
-// block in shared memory and added to the global table once per block.
+// Gradient table of an adjoint block: the warp's private copy in shared
+// memory (zeroed here) when SMEM, else the global table.
 template <bool SMEM>
-__global__ void __launch_bounds__(kAdjointThreads) adjoint_kernel(SceneView s, FrameView f, Camera cam, Settings st,
-                                                                  const float4* __restrict__ pixelGrad, float scale,
-                                                                  float* __restrict__ grads, uint32_t sc,
-                                                                  uint32_t materialCount)
+__device__ __forceinline__ float* grad_table_begin(float* sgrad, const AdjointView& a)
+{
+    if (!SMEM)
+        return a.grads;
+    const uint32_t rows = a.materialCount * kGradSlots;
+    for (uint32_t i = threadIdx.x; i < kAdjointWarps * rows; i += blockDim.x)
+        sgrad[i] = 0.f;
+    __syncthreads();
+    return sgrad + (threadIdx.x >> 5) * rows;
+}
+
+// Adds the block's shared-memory copies to the global table, one atomic per
+// non-zero entry.
+template <bool SMEM>
+__device__ __forceinline__ void grad_table_end(const float* sgrad, const AdjointView& a)
+{
+    if (!SMEM)
+        return;
+    __syncthreads();
+    const uint32_t rows = a.materialCount * kGradSlots;
+    for (uint32_t i = threadIdx.x; i < rows; i += blockDim.x) {
+        float v = 0.f;
+#pragma unroll
+        for (uint32_t w = 0; w < kAdjointWarps; ++w)
+            v += sgrad[w * rows + i];
+        if (v != 0.f)
+            atomicAdd(a.grads + i, v);
+    }
+}
+
+__device__ __forceinline__ float3 path_delta(const FrameView& f, const AdjointView& a, uint32_t pathIx)
+{
+    const float4 pg = a.pixelGrad[pathIx % (f.resX * f.resY)];
+    return make_float3(pg.x * a.scale, pg.y * a.scale, pg.z * a.scale);
+}
+
+// g[k] += sum_c w_c * (d f_c / d theta_k) / f_c
+__device__ __forceinline__ void add_log_derivative(float (&g)[kGradSlots], const Vec3<Dual>& fv, const float3& w)
+{
+    const Dual* fc[3] = {&fv.x, &fv.y, &fv.z};
+    const float wc[3] = {w.x, w.y, w.z};
+#pragma unroll
+    for (int c = 0; c < 3; ++c)
+        if (wc[c] != 0.f && fc[c]->v != 0.f) {
+            const float r = wc[c] / fc[c]->v;
+#pragma unroll
+            for (int k = 0; k < kGradParams; ++k)
+                g[k] += r * fc[c]->d[k];
+        }
+}
+
+// Path-replay adjoint (Vicini, Speierer, Jakob, "Path Replay Backpropagation",
+// SIGGRAPH 2021) as a wavefront over the same queues as the forward frame:
+// paths are regenerated from their random keys and re-traced by the forward
+// extend kernel; the kernels below replace shade and connect. The gradient
+// of the radiance that reached the camera through a closure value f is that
+// radiance times d log f: for the light direction the vertex's NEE
+// contribution, for the extend direction everything the path collected after
+// the vertex. The latter is the path's total (the forward frame's per-path
+// radiance) minus what was accounted for up to the vertex, so it is known
+// when the path reaches its next vertex: the extend direction's d log f is
+// kept per path (pending) and applied by the next adjoint shade.
+__global__ void __launch_bounds__(256) adjoint_generate_kernel(FrameView f, Camera cam, Settings st, AdjointView a)
+{
+    const uint32_t pathIx = blockIdx.x * blockDim.x + threadIdx.x;
+    if (pathIx >= f.pathCount)
+        return;
+    const uint32_t wh = f.resX * f.resY;
+    const uint32_t pixelIx = pathIx % wh;
+    const uint32_t sc = a.sampleBase;
+    CounterRng rng;
+    rng.init(pixelIx, sc + pathIx / wh, 0u, st.seed);
+    float3 O, D;
+    float T;
+    camera_ray(cam, f.resX, f.resY, pixelIx % f.resX, pixelIx / f.resX, rng, false, O, D, T);
+    const uint32_t cap = f.capacity;
+    float4* s = f.state[0];
+    s[pathIx] = f4(O, u2f(pack_path(pathIx, 0)));
+    s[pathIx + cap] = f4(D, 0.f);
+    s[pathIx + 2 * cap] = make_float4(T, T, T, 1.f);
+    a.lrem[pathIx] = f.radiance[pathIx];
+    a.pending[pathIx + 4 * cap] = make_float4(0.f, 0.f, __uint_as_float(0xffffffffu), 0.f);
+}
+
+// Shade of the replay over the hit queue: applies the pending extend-direction
+// gradient of the previous vertex, the emission gradients of an emissive hit,
+// and queues the NEE ray (with what the NEE gradient needs) and the extend ray
+// (with the new pending d log f) like the forward shade.
+template <bool SMEM>
+__global__ void __launch_bounds__(kAdjointThreads) adjoint_shade_kernel(SceneView s, FrameView f, Settings st,
+                                                                        uint32_t bounce, AdjointView a)
 {
     extern __shared__ float sgrad[];
-    const uint32_t rows = materialCount * kGradSlots;
-    float* dst = grads;
-    if (SMEM) {
-        for (uint32_t i = threadIdx.x; i < kAdjointWarps * rows; i += blockDim.x)
-            sgrad[i] = 0.f;
-        __syncthreads();
-        dst = sgrad + (threadIdx.x >> 5) * rows;
-    }
+    float* table = grad_table_begin<SMEM>(sgrad, a);
+    const uint32_t count = __ldcg(f.counters + kHitCounterBase + bounce);
+    const float4* __restrict__ in = f.state[1];
+    float4* __restrict__ out = f.state[0];
+    const uint32_t cap = f.capacity;
+    const uint32_t sc = a.sampleBase;
     const uint32_t wh = f.resX * f.resY;
-    const uint32_t lane = lane_id();
-    uint32_t* cursor = f.counters + kAdjointCursor;
-    bool alive = false, more = true;
-    uint32_t b = 0, pixel = 0, sampleIx = 0;
-    float3 delta = f3(0.f), lrem = f3(0.f);
-    float4 O4 = make_float4(0.f, 0.f, 0.f, 0.f), D4 = O4, T4 = O4;
-    while (true) {
-        uint32_t idle;
-        while ((idle = __ballot_sync(kFull, !alive && more)) != 0u) {
-            const uint32_t leader = __ffs(idle) - 1u;
-            uint32_t base = 0;
-            if (lane == leader)
-                base = atomicAdd(cursor, __popc(idle));
-            base = __shfl_sync(kFull, base, leader);
-            if (!alive && more) {
-                const uint32_t pathIx = base + __popc(idle & ((1u << lane) - 1u));
-                if (pathIx < f.pathCount) {
-                    pixel = pathIx % wh;
-                    sampleIx = pathIx / wh;
-                    const float4 pg = pixelGrad[pixel];
-                    delta = make_float3(pg.x * scale, pg.y * scale, pg.z * scale);
-                    lrem = f3(f.radiance[pathIx]);
-                    alive = (delta.x != 0.f || delta.y != 0.f || delta.z != 0.f) &&
-                            (lrem.x != 0.f || lrem.y != 0.f || lrem.z != 0.f);
-                    if (alive) {
-                        CounterRng rng;
-                        rng.init(pixel, sc + sampleIx, 0u, st.seed);
-                        float3 O, D;
-                        float T;
-                        camera_ray(cam, f.resX, f.resY, pixel % f.resX, pixel / f.resX, rng, false, O, D, T);
-                        O4 = f4(O, __uint_as_float(pack_path(pathIx, 0)));
-                        D4 = f4(D, 0.f);
-                        T4 = make_float4(T, T, T, 1.f);
-                        b = 0;
-                    }
-                } else {
-                    more = false;
-                }
-            }
-        }
-        if (!__any_sync(kFull, alive))
-            break;
-
-        float g[kGradSlots], ge[kGradSlots];
+    uint32_t* extCounter = f.counters + bounce + 1u;
+    uint32_t* shCounter = f.counters + kShadowCounterBase + bounce;
+    const uint32_t warpGlobal = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+    const uint32_t warpStride = (gridDim.x * blockDim.x) >> 5;
+    for (uint32_t base = warpGlobal * 32u; base < count; base += warpStride * 32u) {
+        const uint32_t i = base + lane_id();
+        bool wantExt = false, wantShadow = false;
+        float4 ext[3], sh[3];
+        float g[kGradSlots], ge[kGradSlots], gp[kGradSlots];
 #pragma unroll
         for (int k = 0; k < kGradSlots; ++k)
-            g[k] = ge[k] = 0.f;
-        uint32_t key = 0xffffffffu, keyE = 0xffffffffu;
-        if (alive) {
-            float tmax = kDstMax;
-            uint32_t slot = 0xffffffffu;
-            float u = 0.f, v = 0.f;
-            if (!traverse<false>(s, f3(O4), f3(D4), st.rayEpsilon, tmax, slot, u, v))
-                atomicOr(f.errorFlag, 1u);
-            uint4 hd;
-            if (slot != 0xffffffffu)
-                hd = make_uint4(encode_bary(u, v), 0u, __float_as_uint(__ldg(s.bvhTris + 3u * slot).w),
-                                __float_as_uint(tmax));
-            else
-                hd = make_uint4(0u, 0xffffffffu, 0xffffffffu, __float_as_uint(kDstMax));
-            CounterRng rng;
-            rng.init(pixel, sc + sampleIx, b + 1u, st.seed);
-            VertexInfo vi;
-            bool wantExt = false, wantShadow = false;
-            float4 ext[3], sh[3];
-            shade_path<false>(s, f, st, b, sc, O4, D4, T4, hd, rng, wantExt, ext, wantShadow, sh, &vi);
-            if (!vi.hit) {
-                alive = false;
-            } else if (vi.emissive) {
+            g[k] = ge[k] = gp[k] = 0.f;
+        uint32_t key = 0xffffffffu, keyE = 0xffffffffu, keyP = 0xffffffffu;
+        uint32_t pathIx = 0;
+        VertexInfo vi;
+        vi.hit = false;
+        if (i < count) {
+            const float4 O4 = __ldcs(in + i);
+            const float4 D4 = __ldcs(in + i + cap);
+            const float4 T4 = __ldcs(in + i + 2 * cap);
+            const uint4 hd = __ldcs(f.hits + i);
+            pathIx = path_ix(__float_as_uint(O4.w));
+            const float3 delta = path_delta(f, a, pathIx);
+            float3 lrem = f3(a.lrem[pathIx]);
+            // the previous vertex's extend direction carried everything still unaccounted for
+            const float4 p4 = a.pending[pathIx + 4 * cap];
+            keyP = __float_as_uint(p4.z);
+            if (keyP != 0xffffffffu) {
+                const float4 p0 = a.pending[pathIx], p1 = a.pending[pathIx + cap];
+                const float4 p2 = a.pending[pathIx + 2 * cap], p3 = a.pending[pathIx + 3 * cap];
+                const float dl[18] = {p0.x, p0.y, p0.z, p0.w, p1.x, p1.y, p1.z, p1.w, p2.x,
+                                      p2.y, p2.z, p2.w, p3.x, p3.y, p3.z, p3.w, p4.x, p4.y};
+                const float w[3] = {delta.x * lrem.x, delta.y * lrem.y, delta.z * lrem.z};
+#pragma unroll
+                for (int c = 0; c < 3; ++c)
+#pragma unroll
+                    for (int k = 0; k < kGradParams; ++k)
+                        gp[k] += w[c] * dl[c * kGradParams + k];
+            }
+            const bool live = (delta.x != 0.f || delta.y != 0.f || delta.z != 0.f) &&
+                              (lrem.x != 0.f || lrem.y != 0.f || lrem.z != 0.f);
+            if (live) {
+                CounterRng rng;
+                rng.init(pathIx % wh, sc + pathIx / wh, bounce + 1u, st.seed);
+                shade_path<false>(s, f, st, bounce, sc, O4, D4, T4, hd, rng, wantExt, ext, wantShadow, sh, &vi);
+            }
+            if (vi.hit && vi.emissive) {
                 const float C[3] = {vi.emitted.x, vi.emitted.y, vi.emitted.z};
                 const float E[3] = {vi.mat.emissive.x, vi.mat.emissive.y, vi.mat.emissive.z};
                 const float dl[3] = {delta.x, delta.y, delta.z};
@@ -1009,68 +1062,157 @@ __global__ void __launch_bounds__(kAdjointThreads) adjoint_kernel(SceneView s, F
                 keyE = vi.matIx;
                 key = vi.matIx;
                 lrem = lrem - vi.emitted;
-                alive = false;
-            } else {
-                if (wantShadow) {
-                    float smax = sh[1].w - (2 * st.rayEpsilon);
-                    uint32_t occ = 0xffffffffu;
-                    float su, sv;
-                    if (!traverse<true>(s, f3(sh[0]), f3(sh[1]), st.rayEpsilon, smax, occ, su, sv))
-                        atomicOr(f.errorFlag, 1u);
-                    if (occ == 0xffffffffu) {
-                        const float3 C = f3(sh[2]);
-                        lrem = lrem - C;
-                        const Vec3<Dual> fv = dual::closure_value(vi.closure, vi.mat, vi.wo, vi.wiLight);
-                        const Dual* fc[3] = {&fv.x, &fv.y, &fv.z};
-                        const float w[3] = {delta.x * C.x, delta.y * C.y, delta.z * C.z};
-                        for (int c = 0; c < 3; ++c)
-                            if (w[c] != 0.f && fc[c]->v != 0.f)
-                                for (int k = 0; k < kGradParams; ++k)
-                                    g[k] += w[c] * fc[c]->d[k] / fc[c]->v;
-                        key = vi.matIx;
-                        if (vi.lightIx >= 0) {
-                            const LightTri& Lt = s.lights[vi.lightIx];
-                            const float E[3] = {Lt.radiance.x, Lt.radiance.y, Lt.radiance.z};
-                            for (int c = 0; c < 3; ++c)
-                                if (E[c] > 0.f)
-                                    ge[kGEmR + c] = w[c] / E[c];
-                            keyE = __ldg(s.matIdx + Lt.triIx);
-                        }
-                    }
+                a.lrem[pathIx] = f4(lrem, 0.f);
+            } else if (vi.hit && wantExt) {
+                // d log f of the extend direction, applied at the path's next vertex
+                const Vec3<Dual> fv = dual::closure_value(vi.closure, vi.mat, vi.wo, vi.wiExt);
+                const Dual* fc[3] = {&fv.x, &fv.y, &fv.z};
+                float dl[18];
+#pragma unroll
+                for (int c = 0; c < 3; ++c) {
+                    const float r = fc[c]->v != 0.f ? 1.0f / fc[c]->v : 0.f;
+#pragma unroll
+                    for (int k = 0; k < kGradParams; ++k)
+                        dl[c * kGradParams + k] = fc[c]->d[k] * r;
                 }
-                if (wantExt) {
-                    const Vec3<Dual> fv = dual::closure_value(vi.closure, vi.mat, vi.wo, vi.wiExt);
-                    const Dual* fc[3] = {&fv.x, &fv.y, &fv.z};
-                    const float w[3] = {delta.x * lrem.x, delta.y * lrem.y, delta.z * lrem.z};
-                    for (int c = 0; c < 3; ++c)
-                        if (w[c] != 0.f && fc[c]->v != 0.f)
-                            for (int k = 0; k < kGradParams; ++k)
-                                g[k] += w[c] * fc[c]->d[k] / fc[c]->v;
-                    key = vi.matIx;
-                    O4 = ext[0];
-                    D4 = ext[1];
-                    T4 = ext[2];
-                    if (++b >= st.maxDepth)
-                        alive = false;
+                a.pending[pathIx] = make_float4(dl[0], dl[1], dl[2], dl[3]);
+                a.pending[pathIx + cap] = make_float4(dl[4], dl[5], dl[6], dl[7]);
+                a.pending[pathIx + 2 * cap] = make_float4(dl[8], dl[9], dl[10], dl[11]);
+                a.pending[pathIx + 3 * cap] = make_float4(dl[12], dl[13], dl[14], dl[15]);
+                a.pending[pathIx + 4 * cap] = make_float4(dl[16], dl[17], __uint_as_float(vi.matIx), 0.f);
+            }
+        }
+        if (vi.emissive)
+            wantExt = wantShadow = false;
+        const uint32_t shSlot = warp_append(shCounter, wantShadow);
+        if (wantShadow) {
+            __stcs(f.shadow + shSlot, sh[0]);
+            __stcs(f.shadow + shSlot + cap, sh[1]);
+            __stcs(f.shadow + shSlot + 2 * cap, sh[2]);
+            a.shadowAdj[shSlot] = f4(vi.wo, __uint_as_float(vi.matIx));
+            a.shadowAdj[shSlot + cap] = f4(vi.wiLight, __int_as_float(vi.lightIx));
+        }
+        const uint32_t exSlot = warp_append(extCounter, wantExt);
+        if (wantExt) {
+            __stcs(out + exSlot, ext[0]);
+            __stcs(out + exSlot + cap, ext[1]);
+            __stcs(out + exSlot + 2 * cap, ext[2]);
+        }
+        warp_add_grads<SMEM>(table, keyP, gp, 0, kGradParams);
+        warp_add_grads<SMEM>(table, key, g, 0, kGradParams);
+        warp_add_grads<SMEM>(table, keyE, ge, kGEmR, kGradSlots);
+    }
+    grad_table_end<SMEM>(sgrad, a);
+}
+
+// Visibility of the replay's NEE rays (as connect_kernel): an unoccluded ray
+// takes its contribution off the path's remaining radiance and is listed for
+// nee_grad_kernel.
+__global__ void __launch_bounds__(128) adjoint_connect_kernel(SceneView s, FrameView f, Settings st, uint32_t bounce,
+                                                              AdjointView a)
+{
+    const uint32_t count = __ldcg(f.counters + kShadowCounterBase + bounce);
+    const uint32_t cap = f.capacity;
+    uint32_t* work = f.counters + kConnectWorkBase + bounce;
+    uint32_t* visCounter = f.counters + kVisibleCounterBase + bounce;
+    const uint32_t lane = lane_id();
+    Traversal t;
+    uint2 stack[kTraversalStack];
+    uint32_t ray = 0, pathIx = 0;
+    bool alive = false, more = true;
+    while (true) {
+        const uint32_t idle = __ballot_sync(kFull, !alive && more);
+        if (idle) {
+            const uint32_t leader = __ffs(idle) - 1u;
+            uint32_t base = 0;
+            if (lane == leader)
+                base = atomicAdd(work, __popc(idle));
+            base = __shfl_sync(kFull, base, leader);
+            if (!alive && more) {
+                const uint32_t i = base + __popc(idle & ((1u << lane) - 1u));
+                if (i < count) {
+                    const float4 O4 = __ldcs(f.shadow + i);
+                    const float4 L4 = __ldcs(f.shadow + i + cap);
+                    ray = i;
+                    pathIx = __float_as_uint(O4.w);
+                    traversal_begin(t, f3(O4), f3(L4), st.rayEpsilon, L4.w - (2 * st.rayEpsilon));
+                    alive = true;
                 } else {
-                    alive = false;
+                    more = false;
                 }
             }
         }
-        warp_add_grads<SMEM>(dst, key, g, 0, kGradParams);
-        warp_add_grads<SMEM>(dst, keyE, ge, kGEmR, kGradSlots);
+        if (!__any_sync(kFull, alive))
+            break;
+        uint32_t active;
+        do {
+            bool visible = false;
+            if (alive && traversal_step<true, false>(t, stack, s, nullptr)) {
+                if (!t.ok)
+                    atomicOr(f.errorFlag, 1u);
+                if (t.hitSlot == 0xffffffffu) {
+                    const float4 T4 = __ldcs(f.shadow + ray + 2 * cap);
+                    const float4 r = a.lrem[pathIx];
+                    a.lrem[pathIx] = make_float4(r.x - T4.x, r.y - T4.y, r.z - T4.z, r.w);
+                    visible = true;
+                }
+                alive = false;
+            }
+            const uint32_t slot = warp_append(visCounter, visible);
+            if (visible)
+                a.visible[slot] = ray;
+            active = __ballot_sync(kFull, alive);
+        } while (uint32_t(__popc(active)) >= kRefillBelow);
     }
-    if (SMEM) {
-        __syncthreads();
-        for (uint32_t i = threadIdx.x; i < rows; i += blockDim.x) {
-            float v = 0.f;
+}
+
+// Gradients of the visible NEE contributions: d log f of the light direction
+// at the vertex, and the light's emission.
+template <bool SMEM>
+__global__ void __launch_bounds__(kAdjointThreads) nee_grad_kernel(SceneView s, FrameView f, uint32_t bounce,
+                                                                   AdjointView a)
+{
+    extern __shared__ float sgrad[];
+    float* table = grad_table_begin<SMEM>(sgrad, a);
+    const uint32_t count = __ldcg(f.counters + kVisibleCounterBase + bounce);
+    const uint32_t cap = f.capacity;
+    const uint32_t warpGlobal = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+    const uint32_t warpStride = (gridDim.x * blockDim.x) >> 5;
+    for (uint32_t base = warpGlobal * 32u; base < count; base += warpStride * 32u) {
+        const uint32_t i = base + lane_id();
+        float g[kGradSlots], ge[kGradSlots];
 #pragma unroll
-            for (uint32_t w = 0; w < kAdjointWarps; ++w)
-                v += sgrad[w * rows + i];
-            if (v != 0.f)
-                atomicAdd(grads + i, v);
+        for (int k = 0; k < kGradSlots; ++k)
+            g[k] = ge[k] = 0.f;
+        uint32_t key = 0xffffffffu, keyE = 0xffffffffu;
+        if (i < count) {
+            const uint32_t ray = a.visible[i];
+            const uint32_t pathIx = __float_as_uint(f.shadow[ray].w);
+            const float3 C = f3(f.shadow[ray + 2 * cap]);
+            const float4 wo4 = a.shadowAdj[ray];
+            const float4 wi4 = a.shadowAdj[ray + cap];
+            const uint32_t matIx = __float_as_uint(wo4.w);
+            const int32_t lightIx = __float_as_int(wi4.w);
+            const float3 delta = path_delta(f, a, pathIx);
+            const float3 w = make_float3(delta.x * C.x, delta.y * C.y, delta.z * C.z);
+            uint32_t closure, emissiveFlag;
+            const HitMat m = load_material(s.materials, matIx, closure, emissiveFlag);
+            add_log_derivative(g, dual::closure_value(closure, m, f3(wo4), f3(wi4)), w);
+            key = matIx;
+            if (lightIx >= 0) {
+                const LightTri& Lt = s.lights[lightIx];
+                const float E[3] = {Lt.radiance.x, Lt.radiance.y, Lt.radiance.z};
+                const float wc[3] = {w.x, w.y, w.z};
+                for (int c = 0; c < 3; ++c)
+                    if (E[c] > 0.f)
+                        ge[kGEmR + c] = wc[c] / E[c];
+                keyE = __ldg(s.matIdx + Lt.triIx);
+            }
         }
+        warp_add_grads<SMEM>(table, key, g, 0, kGradParams);
+        warp_add_grads<SMEM>(table, keyE, ge, kGEmR, kGradSlots);
     }
+    grad_table_end<SMEM>(sgrad, a);
 }
 
 __global__ void advance_kernel(FrameView f, Settings st)
@@ -1155,30 +1297,37 @@ cudaError_t launch_finalize(const FrameView& f, const Settings& st, cudaStream_t
 }
 
 cudaError_t launch_adjoint(const SceneView& s, const FrameView& f, const Camera& cam, const Settings& st,
-                           const float4* pixelGrad, float scale, float* grads, uint32_t sampleCount,
-                           uint32_t materialCount, const LaunchShape& shape, cudaStream_t stream)
+                           const AdjointView& a, const LaunchShape& shape, cudaStream_t stream)
 {
     if (f.pathCount == 0)
         return cudaSuccess;
-    cudaError_t e = cudaMemsetAsync(f.counters + kAdjointCursor, 0, sizeof(uint32_t), stream);
+    cudaError_t e = cudaMemsetAsync(f.counters, 0, kCounterWords * sizeof(uint32_t), stream);
     if (e != cudaSuccess)
         return e;
-    const size_t smem = size_t(kAdjointWarps) * materialCount * kGradSlots * sizeof(float);
+    const size_t smem = size_t(kAdjointWarps) * a.materialCount * kGradSlots * sizeof(float);
+    const bool useSmem = smem <= kAdjointSmemMax;
     int perSm = 0;
-    if (smem <= kAdjointSmemMax) {
-        e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&perSm, adjoint_kernel<true>, kAdjointThreads, smem);
-        if (e != cudaSuccess)
-            return e;
-        const uint32_t blocks = shape.sms * uint32_t(perSm > 0 ? perSm : 1);
-        adjoint_kernel<true><<<blocks, kAdjointThreads, smem, stream>>>(s, f, cam, st, pixelGrad, scale, grads,
-                                                                        sampleCount, materialCount);
-    } else {
-        e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&perSm, adjoint_kernel<false>, kAdjointThreads, 0);
-        if (e != cudaSuccess)
-            return e;
-        const uint32_t blocks = shape.sms * uint32_t(perSm > 0 ? perSm : 1);
-        adjoint_kernel<false><<<blocks, kAdjointThreads, 0, stream>>>(s, f, cam, st, pixelGrad, scale, grads,
-                                                                      sampleCount, materialCount);
+    e = useSmem ? cudaOccupancyMaxActiveBlocksPerMultiprocessor(&perSm, adjoint_shade_kernel<true>, kAdjointThreads,
+                                                                smem)
+                : cudaOccupancyMaxActiveBlocksPerMultiprocessor(&perSm, adjoint_shade_kernel<false>, kAdjointThreads,
+                                                                0);
+    if (e != cudaSuccess)
+        return e;
+    const uint32_t gradBlocks = shape.sms * uint32_t(perSm > 0 ? perSm : 1);
+    Settings fwd = st;
+    fwd.flags &= ~uint32_t(TR_FLAG_COUNT_TRAVERSAL | TR_FLAG_WRITE_AOVS);
+    adjoint_generate_kernel<<<(f.pathCount + 255u) / 256u, 256, 0, stream>>>(f, cam, fwd, a);
+    for (uint32_t bounce = 0; bounce < st.maxDepth; ++bounce) {
+        extend_kernel<false, false><<<shape.extendBlocks, 128, 0, stream>>>(s, f, fwd, bounce);
+        if (useSmem)
+            adjoint_shade_kernel<true><<<gradBlocks, kAdjointThreads, smem, stream>>>(s, f, fwd, bounce, a);
+        else
+            adjoint_shade_kernel<false><<<gradBlocks, kAdjointThreads, 0, stream>>>(s, f, fwd, bounce, a);
+        adjoint_connect_kernel<<<shape.connectBlocks, 128, 0, stream>>>(s, f, fwd, bounce, a);
+        if (useSmem)
+            nee_grad_kernel<true><<<gradBlocks, kAdjointThreads, smem, stream>>>(s, f, bounce, a);
+        else
+            nee_grad_kernel<false><<<gradBlocks, kAdjointThreads, 0, stream>>>(s, f, bounce, a);
     }
     return cudaGetLastError();
 }

@@ -31,8 +31,10 @@ cudaError_t launch_finalize(const FrameView& f, const Settings& st, cudaStream_t
 // colors = accumulator / samples over all batch pixels.
 cudaError_t launch_batch_finalize(const FrameView& f, uint32_t wavePixels, cudaStream_t stream);
 cudaError_t launch_batch_resolve(const float4* accumulator, float4* colors, uint32_t pixels, cudaStream_t stream);
+// Path-replay adjoint of the frame `f` (its per-path radiance and sample
+// count are the forward frame's; its queues are overwritten, its counters
+// are the adjoint's own).
 cudaError_t launch_adjoint(const SceneView& s, const FrameView& f, const Camera& cam, const Settings& st,
-                           const float4* pixelGrad, float scale, float* grads, uint32_t sampleCount,
-                           uint32_t materialCount, const LaunchShape& shape, cudaStream_t stream);
+                           const AdjointView& a, const LaunchShape& shape, cudaStream_t stream);
 
 } // namespace tr
