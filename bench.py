@@ -62,6 +62,7 @@ def parse():
                         "per-scene renders; adjoint: forward frame and path-replay adjoint of the "
                         "differentiation scene")
     p.add_argument("--batch-count", type=int, default=64)
+    p.add_argument("--wave-paths", type=int, default=0, help="batched waves: paths per wave (0: library default)")
     return p.parse_args()
 
 
@@ -249,7 +250,7 @@ def run_batch(args):
 
     # batched: one wavefront, all waves replayed from one graph
     t = time.perf_counter()
-    b = tr.BatchRenderer(scenes)
+    b = tr.BatchRenderer(scenes, wave_paths=args.wave_paths)
     build_s = time.perf_counter() - t
     info = b.Info()
     if args.profile:
@@ -278,38 +279,42 @@ def run_batch(args):
     rays = bstats["extend_rays"] + bstats["shadow_rays"]
     b.close()
 
-    # per scene: one context, each scene uploaded (untimed) and rendered as spp / ms graph frames
+    # per scene: one context, each scene uploaded (untimed) and rendered as spp / ms graph frames,
+    # with ms = min(spp, 16) (the reference's largest multi-sample) and with ms = 1 (its default,
+    # Renderer.cpp:259)
     r = tr.DeviceRenderer(0)
-    plain_ms = 0.0
-    plain_rays = 0
-    launches = 0
-    for s in scenes:
-        ms = min(s.spp, 16)
-        frames = s.spp // ms
-        r.UpdateScene(s)
-        r.SetCamera(s.camera)
-        r.Resize((s.width, s.height))
-        r.SetSettings(KernelSettings(**{**st.__dict__, "multiSample": ms}))
-        best = None
-        for rep in range(2):  # the first pass allocates and captures the graph
+
+    def per_scene(max_ms):
+        total_ms, total_rays, n_launch = 0.0, 0, 0
+        for s in scenes:
+            ms = min(s.spp, max_ms)
+            frames = s.spp // ms
+            r.UpdateScene(s)
+            r.SetCamera(s.camera)
+            r.Resize((s.width, s.height))
+            r.SetSettings(KernelSettings(**{**st.__dict__, "multiSample": ms}))
+            elapsed = None
+            for _ in range(2):  # the first pass allocates and captures the graph
+                r.Reset()
+                flush.fill_(1.0)
+                e0 = torch.cuda.Event(enable_timing=True)
+                e1 = torch.cuda.Event(enable_timing=True)
+                e0.record(stream)
+                for _ in range(frames):
+                    r.RenderFrame(stream=sptr, use_graph=True)
+                e1.record(stream)
+                e1.synchronize()
+                elapsed = e0.elapsed_time(e1)
+            total_ms += elapsed
             r.Reset()
-            flush.fill_(1.0)
-            e0 = torch.cuda.Event(enable_timing=True)
-            e1 = torch.cuda.Event(enable_timing=True)
-            e0.record(stream)
             for _ in range(frames):
-                r.RenderFrame(stream=sptr, use_graph=True)
-            e1.record(stream)
-            e1.synchronize()
-            best = e0.elapsed_time(e1)
-        plain_ms += best
-        frame_rays = 0
-        r.Reset()
-        for _ in range(frames):
-            r.RenderFrame(stream=sptr, use_graph=False)
-            frame_rays += r.Statistics()["path_count"]
-        plain_rays += frame_rays
-        launches += frames * (3 * st.maxDepth + 3)
+                r.RenderFrame(stream=sptr, use_graph=False)
+                total_rays += r.Statistics()["path_count"]
+            n_launch += frames * (3 * st.maxDepth + 3)
+        return total_ms, total_rays, n_launch
+
+    plain_ms, plain_rays, launches = per_scene(16)
+    ms1_ms, ms1_rays, ms1_launches = per_scene(1)
     r.close()
     line = {
         "metric": "samples/s",
@@ -332,7 +337,10 @@ def run_batch(args):
         "gpu_launches": info["launches"],
         "per_scene": {"ms": round(plain_ms, 3), "samples_per_s": round(samples / (plain_ms / 1e3), 1),
                       "mrays_per_s": round(plain_rays / (plain_ms / 1e3) / 1e6, 1), "gpu_launches": launches},
+        "per_scene_ms1": {"ms": round(ms1_ms, 3), "samples_per_s": round(samples / (ms1_ms / 1e3), 1),
+                          "mrays_per_s": round(ms1_rays / (ms1_ms / 1e3) / 1e6, 1), "gpu_launches": ms1_launches},
         "speedup_vs_per_scene": round(plain_ms / batch_ms, 3),
+        "speedup_vs_per_scene_ms1": round(ms1_ms / batch_ms, 3),
         "rays_batch": int(rays),
         "rays_per_scene": int(plain_rays),
         "scene_generation_s": round(gen_s, 2),
