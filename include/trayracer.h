@@ -252,6 +252,24 @@ typedef struct tr_buffers {
     uint32_t height;
 } tr_buffers;
 
+/* Launch and build parameters chosen by tr_autotune (0 = default). */
+typedef struct tr_tuning {
+    uint32_t bvh_leaf_size;         /* triangles per BVH leaf, 1..3 (BVH rebuilt from the kept host copy) */
+    uint32_t refill_below;          /* persistent traversal warps take new rays below this many active lanes, 1..32 */
+    uint32_t extend_blocks_per_sm;  /* persistent extend grid, 1..occupancy */
+    uint32_t connect_blocks_per_sm; /* persistent connect grid, 1..occupancy */
+    uint32_t shade_waves;           /* shade grid cap in waves of resident blocks, 1..64 */
+    uint32_t reserved[3];
+} tr_tuning;
+
+typedef struct tr_tune_report {
+    tr_tuning chosen;
+    float frame_ms_default;         /* one frame with the default tuning */
+    float frame_ms_tuned;           /* one frame with the chosen tuning */
+    uint32_t trials;                /* configurations timed */
+    uint32_t reserved;
+} tr_tune_report;
+
 /* ---- lifetime ---- */
 tr_status tr_create(const tr_config* config, void** out_ctx);
 tr_status tr_destroy(void* ctx);
@@ -318,6 +336,21 @@ tr_status tr_adjoint_frame(void* ctx, void* stream, const float* pixel_grad, flo
  * contexts) race. Guide buffers (TR_FLAG_WRITE_AOVS) are not written. */
 tr_status tr_render_frame_noalloc(void* ctx, void* stream, float* accumulator, float* colors, uint32_t sample_count);
 
+/* ---- tuning ----
+ * No counterpart in the reference (OptiX picks its own launch shapes). */
+#define TR_TUNE_SKIP_BVH (1u << 0)  /* tr_autotune: keep the BVH leaf size */
+/* Current tuning (after the first frame: the launch shapes in use). */
+tr_status tr_get_tuning(void* ctx, tr_tuning* tuning);
+/* Applies a tuning; a new bvh_leaf_size rebuilds the BVH from the host copy of
+ * the mesh kept since tr_scene_upload. Zero fields take the defaults. */
+tr_status tr_set_tuning(void* ctx, const tr_tuning* tuning);
+/* Times graph-replayed frames of the current scene, camera, settings and
+ * resolution (one warm-up + two timed frames per configuration) over the
+ * lane refill threshold, the persistent extend / connect grids, the shade grid
+ * cap and (unless TR_TUNE_SKIP_BVH) the BVH leaf size, one parameter at a time,
+ * keeps the fastest and resets the accumulation. */
+tr_status tr_autotune(void* ctx, void* stream, uint32_t flags, tr_tune_report* report);
+
 /* ---- batched rendering ----
  * Many independent scenes of uneven triangle count, resolution and sample
  * count rendered by one wavefront. No counterpart in the reference (one
@@ -325,7 +358,7 @@ tr_status tr_render_frame_noalloc(void* ctx, void* stream, float* accumulator, f
  * the per-stage kernels are the ones behind tr_extend / tr_shade /
  * tr_connect. Each item's scene gets its own BVH; the buffers are
  * concatenated on the device and all items' paths run through the same
- * launches in waves of at most wave_paths paths (0: 2^24), made of
+ * launches in waves of at most wave_paths paths (0: 2^26), made of
  * consecutive (item, sample) units. A path's random numbers are keyed as in
  * tr_render_frame (pixel, sample, bounce, seed), so an item whose samples fit
  * in one wave renders the image tr_render_frame gives for that scene with

@@ -178,3 +178,31 @@ def test_full_size_heightfield_properties():
     assert np.isfinite(a).all() and a[..., :3].mean() > 0
     assert s["device_error"] == 0
     assert s["extend_rays"][0] == 1920 * 1080 * 4
+
+
+def test_tuning_keeps_images_and_autotune_picks_fastest():
+    scene = tr.heightfield(n=256, width=160, height=90, spp=4, max_depth=6)
+    st = tr.settings_for(scene, multi_sample=4)
+    r = renderer(scene, st)
+    r.RenderFrame()
+    want = r.ColorBuffer().copy()
+    # launch shapes change the order work is picked up, never a path's result
+    r.SetTuning(refill_below=12, extend_blocks_per_sm=2, connect_blocks_per_sm=3, shade_waves=1)
+    r.Reset()
+    r.RenderFrame()
+    np.testing.assert_array_equal(r.ColorBuffer(), want)
+    t = r.Tuning()
+    assert t["refill_below"] == 12 and t["extend_blocks_per_sm"] == 2 and t["shade_waves"] == 1
+    r.SetTuning()  # back to the defaults
+    rep = r.Autotune()
+    assert rep["trials"] >= 10
+    assert rep["frame_ms_tuned"] <= rep["frame_ms_default"]
+    assert rep["chosen"] == r.Tuning()
+    r.RenderFrame()
+    got = r.ColorBuffer()
+    # another leaf size may pick another of two triangles at the same distance (near ties)
+    same = np.isclose(got, want, rtol=1e-4, atol=1e-6).all(-1).mean()
+    assert same >= 0.995, same
+    with pytest.raises(TracerError):
+        r.SetTuning(bvh_leaf_size=4)
+    r.close()

@@ -156,6 +156,30 @@ class Buffers(C.Structure):
     ]
 
 
+class Tuning(C.Structure):
+    _fields_ = [
+        ("bvh_leaf_size", C.c_uint32),
+        ("refill_below", C.c_uint32),
+        ("extend_blocks_per_sm", C.c_uint32),
+        ("connect_blocks_per_sm", C.c_uint32),
+        ("shade_waves", C.c_uint32),
+        ("reserved", C.c_uint32 * 3),
+    ]
+
+
+class TuneReport(C.Structure):
+    _fields_ = [
+        ("chosen", Tuning),
+        ("frame_ms_default", C.c_float),
+        ("frame_ms_tuned", C.c_float),
+        ("trials", C.c_uint32),
+        ("reserved", C.c_uint32),
+    ]
+
+
+TR_TUNE_SKIP_BVH = 1 << 0
+
+
 class BatchItem(C.Structure):
     _fields_ = [
         ("scene", C.POINTER(SceneDesc)),
@@ -228,6 +252,9 @@ FUNCTIONS = {
     "tr_update_materials": (C.c_int, [_V, C.POINTER(MaterialDesc), _U]),
     "tr_adjoint_frame": (C.c_int, [_V, _V, _V, C.c_float, _V]),
     "tr_render_frame_noalloc": (C.c_int, [_V, _V, _V, _V, _U]),
+    "tr_get_tuning": (C.c_int, [_V, C.POINTER(Tuning)]),
+    "tr_set_tuning": (C.c_int, [_V, C.POINTER(Tuning)]),
+    "tr_autotune": (C.c_int, [_V, _V, _U, C.POINTER(TuneReport)]),
     "tr_batch_create": (C.c_int, [C.POINTER(Config), C.POINTER(BatchItem), _U, C.c_uint64, C.POINTER(_V)]),
     "tr_batch_destroy": (C.c_int, [_V]),
     "tr_batch_last_error": (C.c_char_p, [_V]),

@@ -50,6 +50,11 @@ struct Context {
     // scene
     bool hasScene = false;
     DeviceArena sceneArena;
+    DeviceArena bvhArena;          // nodes + traversal triangles (rebuilt when the leaf size is tuned)
+    std::vector<float> hostPositions;
+    std::vector<uint32_t> hostIndices;
+    uint32_t leafSize = 3;
+    tr_tuning tuning{};
     SceneView scene{};
     tr_scene_info info{};
     // host copies kept for material updates without a BVH rebuild
@@ -127,6 +132,53 @@ void invalidate_graph(Context* c)
     c->graphValid = false;
 }
 
+// Uploads a CWBVH into its own arena and points the scene view at it.
+tr_status upload_bvh(Context* c, const Cwbvh& wide)
+{
+    const size_t nb = align256(std::max<size_t>(wide.nodes.size() * sizeof(CwbvhNode), 16));
+    const size_t tb = std::max<size_t>(wide.tris.size() * sizeof(float4), 16);
+    void* base = nullptr;
+    cudaError_t e = cudaMalloc(&base, nb + tb);
+    if (e != cudaSuccess)
+        return cuda_fail(c, e, "cudaMalloc(bvh)");
+    char* b = static_cast<char*>(base);
+    e = cudaMemcpy(b, wide.nodes.data(), wide.nodes.size() * sizeof(CwbvhNode), cudaMemcpyHostToDevice);
+    if (e == cudaSuccess && !wide.tris.empty())
+        e = cudaMemcpy(b + nb, wide.tris.data(), wide.tris.size() * sizeof(float4), cudaMemcpyHostToDevice);
+    if (e != cudaSuccess) {
+        cudaFree(base);
+        return cuda_fail(c, e, "cudaMemcpy(bvh)");
+    }
+    c->bvhArena.release();
+    c->bvhArena.base = base;
+    c->bvhArena.bytes = nb + tb;
+    c->scene.nodes = reinterpret_cast<const CwbvhNode*>(b);
+    c->scene.bvhTris = reinterpret_cast<const float4*>(b + nb);
+    c->scene.nodeCount = uint32_t(wide.nodes.size());
+    c->info.bvh_node_count = uint32_t(wide.nodes.size());
+    return TR_OK;
+}
+
+// Rebuilds the BVH from the host copy of the mesh with another leaf size.
+tr_status rebuild_bvh(Context* c, uint32_t leafSize)
+{
+    if (leafSize == c->leafSize)
+        return TR_OK;
+    BvhBuildOptions opt;
+    opt.maxLeafSize = leafSize;
+    const uint32_t n = uint32_t(c->hostIndices.size() / 3);
+    const BinaryBvh bin = build_binary_bvh(c->hostPositions.data(), c->hostIndices.data(), n, opt);
+    const Cwbvh wide = collapse_to_cwbvh(bin, c->hostPositions.data(), c->hostIndices.data());
+    if (c->stream)
+        cudaStreamSynchronize(c->stream);
+    cudaDeviceSynchronize();
+    invalidate_graph(c);
+    const tr_status st = upload_bvh(c, wide);
+    if (st == TR_OK)
+        c->leafSize = leafSize;
+    return st;
+}
+
 tr_status ensure_frame(Context* c)
 {
     if (c->width == 0 || c->height == 0)
@@ -192,7 +244,7 @@ tr_status ensure_frame(Context* c)
     c->frameH = c->height;
     c->frameMs = c->settings.multiSample;
     c->sampleCount = 0;
-    c->shape = default_launch_shape(c->device, uint32_t(cap));
+    c->shape = tuned_launch_shape(c->device, uint32_t(cap), c->tuning);
     return TR_OK;
 }
 
@@ -218,11 +270,14 @@ tr_status enqueue_frame(Context* c, cudaStream_t s, bool timed)
         return st;
     if (timed)
         TR_CUDA(c, cudaEventRecord(c->evStart, s));
-    TR_CUDA(c, launch_generate(c->frame, c->camera, c->settings, s));
+    // default sampling mode: the camera rays are made inside the first extend launch
+    const bool fused = (c->settings.flags & TR_FLAG_REFERENCE_SAMPLING) == 0;
+    if (!fused)
+        TR_CUDA(c, launch_generate(c->frame, c->camera, c->settings, s));
     if (timed)
         TR_CUDA(c, cudaEventRecord(c->evGenerate, s));
     for (uint32_t b = 0; b < c->settings.maxDepth; ++b) {
-        TR_CUDA(c, launch_extend(c->scene, c->frame, c->settings, b, c->shape, s));
+        TR_CUDA(c, launch_extend(c->scene, c->frame, c->settings, b, c->shape, s, fused ? &c->camera : nullptr));
         if (timed)
             TR_CUDA(c, cudaEventRecord(c->evExtend[b], s));
         TR_CUDA(c, launch_shade(c->scene, c->frame, c->settings, b, c->shape, s));
@@ -391,6 +446,7 @@ tr_status tr_destroy(void* ctx)
         cudaStreamSynchronize(c->stream);
     invalidate_graph(c);
     c->sceneArena.release();
+    c->bvhArena.release();
     c->frameArena.release();
     c->adjointArena.release();
     if (c->hostCounters)
@@ -432,15 +488,13 @@ tr_status tr_scene_upload(void* ctx, const tr_scene_desc* desc)
     const Cwbvh wide = collapse_to_cwbvh(bin, m.positions, m.indices);
     const auto t1 = std::chrono::steady_clock::now();
 
-    // one arena for all scene buffers
+    // one arena for the shading buffers, one for the BVH
     size_t off = 0;
     auto take = [&](size_t bytes) {
         const size_t o = off;
         off = align256(off + std::max<size_t>(bytes, 16));
         return o;
     };
-    const size_t oNodes = take(wide.nodes.size() * sizeof(CwbvhNode));
-    const size_t oBTris = take(wide.tris.size() * sizeof(float4));
     const size_t oTris = take(fs.tris.size() * sizeof(TriShade));
     const size_t oMat = take(fs.matIdx.size() * sizeof(uint32_t));
     const size_t oMats = take(fs.materials.size() * sizeof(Material));
@@ -452,6 +506,7 @@ tr_status tr_scene_upload(void* ctx, const tr_scene_desc* desc)
         cudaStreamSynchronize(c->stream);
     invalidate_graph(c);
     c->sceneArena.release();
+    c->bvhArena.release();
     c->hasScene = false;
     void* base = nullptr;
     cudaError_t e = cudaMalloc(&base, off);
@@ -466,8 +521,6 @@ tr_status tr_scene_upload(void* ctx, const tr_scene_desc* desc)
         return cudaMemcpy(b + o, src, bytes, cudaMemcpyHostToDevice);
     };
     const cudaError_t es[] = {
-        up(oNodes, wide.nodes.data(), wide.nodes.size() * sizeof(CwbvhNode)),
-        up(oBTris, wide.tris.data(), wide.tris.size() * sizeof(float4)),
         up(oTris, fs.tris.data(), fs.tris.size() * sizeof(TriShade)),
         up(oMat, fs.matIdx.data(), fs.matIdx.size() * sizeof(uint32_t)),
         up(oMats, fs.materials.data(), fs.materials.size() * sizeof(Material)),
@@ -480,11 +533,14 @@ tr_status tr_scene_upload(void* ctx, const tr_scene_desc* desc)
             c->sceneArena.release();
             return cuda_fail(c, x, "cudaMemcpy(scene)");
         }
+    const tr_status bst = upload_bvh(c, wide);
+    if (bst != TR_OK) {
+        c->sceneArena.release();
+        return bst;
+    }
     const auto t2 = std::chrono::steady_clock::now();
 
     SceneView& s = c->scene;
-    s.nodes = reinterpret_cast<const CwbvhNode*>(b + oNodes);
-    s.bvhTris = reinterpret_cast<const float4*>(b + oBTris);
     s.tris = reinterpret_cast<const TriShade*>(b + oTris);
     s.matIdx = reinterpret_cast<const uint32_t*>(b + oMat);
     s.materials = reinterpret_cast<const Material*>(b + oMats);
@@ -494,7 +550,6 @@ tr_status tr_scene_upload(void* ctx, const tr_scene_desc* desc)
     s.lightCount = int32_t(fs.lights.size());
     s.lightEnergy = fs.lightEnergy;
     s.lightEnergyTotal = fs.lightEnergyTotal;
-    s.nodeCount = uint32_t(wide.nodes.size());
     s.triCount = m.triangle_count;
 
     tr_scene_info& in = c->info;
@@ -503,7 +558,7 @@ tr_status tr_scene_upload(void* ctx, const tr_scene_desc* desc)
     in.light_count = uint32_t(fs.lights.size());
     in.material_count = desc->material_count;
     in.bvh_node_count = uint32_t(wide.nodes.size());
-    in.device_bytes = off;
+    in.device_bytes = off + c->bvhArena.bytes;
     in.light_energy = fs.lightEnergyTotal;
     in.build_time_ms = std::chrono::duration<float, std::milli>(t1 - t0).count();
     in.upload_time_ms = std::chrono::duration<float, std::milli>(t2 - t1).count();
@@ -511,6 +566,10 @@ tr_status tr_scene_upload(void* ctx, const tr_scene_desc* desc)
         in.scene_bounds[i] = fs.bounds[i];
     c->hostLights = fs.lights;
     c->hostMatIdx = fs.matIdx;
+    c->hostPositions.assign(m.positions, m.positions + size_t(m.vertex_count) * 3);
+    c->hostIndices.assign(m.indices, m.indices + size_t(m.triangle_count) * 3);
+    c->leafSize = opt.maxLeafSize;
+    c->tuning.bvh_leaf_size = opt.maxLeafSize;
     c->materialCount = desc->material_count;
     c->hasScene = true;
     c->sampleCount = 0;
@@ -630,6 +689,148 @@ tr_status tr_adjoint_frame(void* ctx, void* stream, const float* pixel_grad, flo
     FrameView f = c->frame;
     f.counters = c->adjointCounters;
     TR_CUDA(c, launch_adjoint(c->scene, f, c->camera, c->settings, a, c->shape, pick_stream(c, stream)));
+    return TR_OK;
+}
+
+tr_status tr_get_tuning(void* ctx, tr_tuning* out)
+{
+    if (!ctx || !out)
+        return TR_ERR_INVALID_ARGUMENT;
+    Context* c = static_cast<Context*>(ctx);
+    tr_tuning t = c->tuning;
+    t.bvh_leaf_size = c->leafSize;
+    if (c->shape.sms) {
+        t.refill_below = c->shape.refillBelow;
+        t.extend_blocks_per_sm = c->shape.extendBlocks / c->shape.sms;
+        t.connect_blocks_per_sm = c->shape.connectBlocks / c->shape.sms;
+        t.shade_waves = c->shape.shadeWaves;
+    }
+    *out = t;
+    return TR_OK;
+}
+
+tr_status tr_set_tuning(void* ctx, const tr_tuning* t)
+{
+    if (!ctx || !t)
+        return TR_ERR_INVALID_ARGUMENT;
+    Context* c = static_cast<Context*>(ctx);
+    if (t->bvh_leaf_size > 3 || t->refill_below > 32 || t->shade_waves > 64)
+        return fail(c, TR_ERR_INVALID_ARGUMENT, "tuning out of range (leaf size <= 3, refill <= 32, shade waves <= 64)");
+    cudaSetDevice(c->device);
+    if (t->bvh_leaf_size && c->hasScene) {
+        const tr_status st = rebuild_bvh(c, t->bvh_leaf_size);
+        if (st != TR_OK)
+            return st;
+    }
+    c->tuning = *t;
+    c->tuning.bvh_leaf_size = c->leafSize;
+    invalidate_graph(c);
+    if (c->frameArena.base)
+        c->shape = tuned_launch_shape(c->device, uint32_t(c->frame.capacity), c->tuning);
+    return TR_OK;
+}
+
+// Coordinate search over the tunables, each configuration timed over two
+// graph-replayed frames after one warm-up frame.
+tr_status tr_autotune(void* ctx, void* stream, uint32_t flags, tr_tune_report* report)
+{
+    if (!ctx)
+        return TR_ERR_INVALID_ARGUMENT;
+    Context* c = static_cast<Context*>(ctx);
+    tr_status st = check_ready(c);
+    if (st != TR_OK)
+        return st;
+    cudaSetDevice(c->device);
+    st = ensure_frame(c);
+    if (st != TR_OK)
+        return st;
+    cudaStream_t s = pick_stream(c, stream);
+    cudaEvent_t e0 = nullptr, e1 = nullptr;
+    TR_CUDA(c, cudaEventCreate(&e0));
+    TR_CUDA(c, cudaEventCreate(&e1));
+    uint32_t trials = 0;
+    auto timeFrames = [&](float* ms) -> tr_status {
+        tr_status r = tr_render_frame(ctx, stream, 1);
+        if (r != TR_OK)
+            return r;
+        TR_CUDA(c, cudaEventRecord(e0, s));
+        for (int i = 0; i < 2 && r == TR_OK; ++i)
+            r = tr_render_frame(ctx, stream, 1);
+        if (r != TR_OK)
+            return r;
+        TR_CUDA(c, cudaEventRecord(e1, s));
+        TR_CUDA(c, cudaEventSynchronize(e1));
+        TR_CUDA(c, cudaEventElapsedTime(ms, e0, e1));
+        *ms *= 0.5f;
+        ++trials;
+        return TR_OK;
+    };
+    tr_tuning best{};
+    tr_get_tuning(ctx, &best);
+    const LaunchShape def = default_launch_shape(c->device, uint32_t(c->frame.capacity));
+    float bestMs = 0.f, defaultMs = 0.f;
+    st = timeFrames(&bestMs);
+    defaultMs = bestMs;
+    auto tryTuning = [&](const tr_tuning& t) -> tr_status {
+        tr_status r = tr_set_tuning(ctx, &t);
+        if (r != TR_OK)
+            return r;
+        float ms = 0.f;
+        r = timeFrames(&ms);
+        if (r != TR_OK)
+            return r;
+        if (ms < bestMs) {
+            bestMs = ms;
+            best = t;
+        }
+        return TR_OK;
+    };
+    const uint32_t refills[] = {12, 16, 20, 24, 28, 32};
+    for (uint32_t v : refills) {
+        tr_tuning t = best;
+        t.refill_below = v;
+        if (st == TR_OK && v != best.refill_below)
+            st = tryTuning(t);
+    }
+    for (uint32_t d : {def.extendPerSm / 2, def.extendPerSm * 3 / 4}) {
+        tr_tuning t = best;
+        t.extend_blocks_per_sm = d;
+        if (st == TR_OK && d >= 1 && d != best.extend_blocks_per_sm)
+            st = tryTuning(t);
+    }
+    for (uint32_t d : {def.connectPerSm / 2, def.connectPerSm * 3 / 4}) {
+        tr_tuning t = best;
+        t.connect_blocks_per_sm = d;
+        if (st == TR_OK && d >= 1 && d != best.connect_blocks_per_sm)
+            st = tryTuning(t);
+    }
+    for (uint32_t w : {1u, 2u, 8u}) {
+        tr_tuning t = best;
+        t.shade_waves = w;
+        if (st == TR_OK && w != best.shade_waves)
+            st = tryTuning(t);
+    }
+    if ((flags & TR_TUNE_SKIP_BVH) == 0)
+        for (uint32_t leaf : {1u, 2u, 3u}) {
+            tr_tuning t = best;
+            t.bvh_leaf_size = leaf;
+            if (st == TR_OK && leaf != best.bvh_leaf_size)
+                st = tryTuning(t);
+        }
+    if (st == TR_OK)
+        st = tr_set_tuning(ctx, &best);
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
+    if (st != TR_OK)
+        return st;
+    tr_reset(ctx);
+    if (report) {
+        *report = tr_tune_report{};
+        tr_get_tuning(ctx, &report->chosen);
+        report->frame_ms_default = defaultMs;
+        report->frame_ms_tuned = bestMs;
+        report->trials = trials;
+    }
     return TR_OK;
 }
 

@@ -33,7 +33,7 @@ namespace {
 
 using namespace tr;
 
-constexpr uint64_t kDefaultWavePaths = 1ull << 24;
+constexpr uint64_t kDefaultWavePaths = 1ull << 26;
 
 struct Wave {
     uint32_t segmentOffset = 0;
@@ -216,9 +216,9 @@ cudaError_t enqueue(Batch* b, const Settings& st, cudaStream_t s)
     const Camera noCamera{};  // each path uses its item's camera
     for (uint32_t w = 0; e == cudaSuccess && w < b->waves.size(); ++w) {
         const FrameView f = wave_view(b, w);
-        e = launch_generate(f, noCamera, st, s);
+        // the camera rays are made inside the first extend launch
         for (uint32_t bounce = 0; e == cudaSuccess && bounce < st.maxDepth; ++bounce) {
-            e = launch_extend(b->scene, f, st, bounce, b->shape, s);
+            e = launch_extend(b->scene, f, st, bounce, b->shape, s, &noCamera);
             if (e == cudaSuccess)
                 e = launch_shade(b->scene, f, st, bounce, b->shape, s);
             if (e == cudaSuccess)
@@ -495,7 +495,7 @@ tr_status tr_batch_get_info(void* batch, tr_batch_info* out)
         return TR_ERR_INVALID_ARGUMENT;
     Batch* b = static_cast<Batch*>(batch);
     *out = b->info;
-    out->launches = uint32_t(b->waves.size()) * (2u + 3u * b->lastSettings.maxDepth) + 1u;
+    out->launches = uint32_t(b->waves.size()) * (1u + 3u * b->lastSettings.maxDepth) + 1u;
     return TR_OK;
 }
 

@@ -196,7 +196,7 @@ struct Settings {
     uint32_t rrStart;
     uint32_t flags;
     float maxColor;
-    uint32_t pad;
+    uint32_t refillBelow;  // persistent traversal warps refill lanes below this many active (set per launch)
 };
 
 // Device counter words: per bounce the extend queue length, the shadow queue

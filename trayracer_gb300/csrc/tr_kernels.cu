@@ -216,18 +216,15 @@ __device__ __forceinline__ SceneView item_scene(const SceneView& s, const BatchI
 }
 
 // ------------------------------------------------------------------ kernels
+// Primary ray of a path (the camera half of the Primary raygen program,
+// optix.cu:235-276): sc = samples accumulated before this frame.
 template <bool REF, bool BATCH>
-__global__ void __launch_bounds__(256) generate_kernel(FrameView f, Camera cam, Settings st)
+__device__ __forceinline__ void primary_ray(const FrameView& f, const Camera& cam, const Settings& st, uint32_t pathIx,
+                                            uint32_t sc, float3& O, float3& D, float& T)
 {
-    const uint32_t pathIx = blockIdx.x * blockDim.x + threadIdx.x;
-    if (pathIx >= f.pathCount)
-        return;
     const uint32_t wh = f.resX * f.resY;
     const uint32_t pixelIx = pathIx % wh;
     const uint32_t sampleIx = pathIx / wh;
-    const uint32_t sc = *f.sampleCount;
-    float3 O, D;
-    float T;
     if (BATCH) {
         // the item's camera and film; the counter RNG keyed as for one scene
         const BatchSegment sg = f.segments[batch_segment(f, pathIx)];
@@ -246,6 +243,17 @@ __global__ void __launch_bounds__(256) generate_kernel(FrameView f, Camera cam, 
         rng.init(pixelIx, sc + sampleIx, 0u, st.seed);
         camera_ray(cam, f.resX, f.resY, pixelIx % f.resX, pixelIx / f.resX, rng, false, O, D, T);
     }
+}
+
+template <bool REF, bool BATCH>
+__global__ void __launch_bounds__(256) generate_kernel(FrameView f, Camera cam, Settings st)
+{
+    const uint32_t pathIx = blockIdx.x * blockDim.x + threadIdx.x;
+    if (pathIx >= f.pathCount)
+        return;
+    float3 O, D;
+    float T;
+    primary_ray<REF, BATCH>(f, cam, st, pathIx, *f.sampleCount, O, D, T);
     const uint32_t cap = f.capacity;
     float4* s = f.state[0];
     s[pathIx] = f4(O, u2f(pack_path(pathIx, 0)));
@@ -274,17 +282,21 @@ __device__ __forceinline__ void add_counts(unsigned long long* dst, const Traver
 }
 
 // Persistent warps refill a lane with the next ray of the queue when fewer
-// than this many of its 32 rays are still traversing (incoherent secondary
-// rays end at very different times).
+// than st.refillBelow of its 32 rays are still traversing (incoherent
+// secondary rays end at very different times); tuned per scene, 24 by default.
 constexpr uint32_t kRefillBelow = 24;
 
 // Closest hit of the bounce's extend queue. Rays that hit are appended (one
 // warp ballot and one atomic per step) to the hit queue with their full path
 // state and hit record; missed rays end here. COUNT = true also sums the nodes
 // visited and triangles tested (for the traversal bytes of the roofline); it
-// is launched outside timed regions.
-template <bool COUNT, bool BATCH>
-__global__ void __launch_bounds__(128) extend_kernel(SceneView s, FrameView f, Settings st, uint32_t bounce)
+// is launched outside timed regions. PRIMARY = true (bounce 0 of a frame
+// rendered as a whole, default sampling mode) computes each path's camera ray
+// in place of reading a generated queue, and clears the path's radiance: the
+// primary rays never go through memory.
+template <bool COUNT, bool BATCH, bool PRIMARY>
+__global__ void __launch_bounds__(128, 8) extend_kernel(SceneView s, FrameView f, Settings st, uint32_t bounce,
+                                                     Camera cam)
 {
     const uint32_t count = queue_length(f, bounce);
     const float4* __restrict__ in = f.state[0];
@@ -299,6 +311,7 @@ __global__ void __launch_bounds__(128) extend_kernel(SceneView s, FrameView f, S
     Traversal t;
     uint2 stack[kTraversalStack];
     float4 O4 = make_float4(0.f, 0.f, 0.f, 0.f), D4 = O4, T4 = O4;
+    const uint32_t sc = PRIMARY ? *f.sampleCount : 0u;
     bool alive = false, more = true;
     while (true) {
         const uint32_t idle = __ballot_sync(kFull, !alive && more);
@@ -311,9 +324,19 @@ __global__ void __launch_bounds__(128) extend_kernel(SceneView s, FrameView f, S
             if (!alive && more) {
                 const uint32_t i = base + __popc(idle & ((1u << lane) - 1u));
                 if (i < count) {
-                    O4 = __ldcs(in + i);
-                    D4 = __ldcs(in + i + cap);
-                    T4 = __ldcs(in + i + 2 * cap);
+                    if (PRIMARY) {
+                        float3 O, D;
+                        float T;
+                        primary_ray<false, BATCH>(f, cam, st, i, sc, O, D, T);
+                        O4 = f4(O, u2f(pack_path(i, 0)));
+                        D4 = f4(D, 0.f);
+                        T4 = make_float4(T, T, T, 1.f);
+                        f.radiance[i] = make_float4(0.f, 0.f, 0.f, 0.f);
+                    } else {
+                        O4 = __ldcs(in + i);
+                        D4 = __ldcs(in + i + cap);
+                        T4 = __ldcs(in + i + 2 * cap);
+                    }
                     traversal_begin(t, f3(O4), f3(D4), st.rayEpsilon, kDstMax,
                                     path_root<BATCH>(f, path_ix(__float_as_uint(O4.w))));
                     alive = true;
@@ -351,7 +374,7 @@ __global__ void __launch_bounds__(128) extend_kernel(SceneView s, FrameView f, S
                 alive = false;
             }
             active = __ballot_sync(kFull, alive);
-        } while (uint32_t(__popc(active)) >= kRefillBelow);
+        } while (uint32_t(__popc(active)) >= st.refillBelow);
     }
     if (COUNT)
         add_counts(f.traversal, cnt);
@@ -786,7 +809,7 @@ __global__ void __launch_bounds__(128) connect_kernel(SceneView s, FrameView f, 
                 alive = false;
             }
             active = __ballot_sync(kFull, alive);
-        } while (uint32_t(__popc(active)) >= kRefillBelow);
+        } while (uint32_t(__popc(active)) >= st.refillBelow);
     }
     if (COUNT)
         add_counts(f.traversal + 2, cnt);
@@ -1162,7 +1185,7 @@ __global__ void __launch_bounds__(128) adjoint_connect_kernel(SceneView s, Frame
             if (visible)
                 a.visible[slot] = ray;
             active = __ballot_sync(kFull, alive);
-        } while (uint32_t(__popc(active)) >= kRefillBelow);
+        } while (uint32_t(__popc(active)) >= st.refillBelow);
     }
 }
 
@@ -1238,21 +1261,33 @@ cudaError_t launch_generate(const FrameView& f, const Camera& cam, const Setting
     return cudaGetLastError();
 }
 
-cudaError_t launch_extend(const SceneView& s, const FrameView& f, const Settings& st, uint32_t bounce,
-                          const LaunchShape& shape, cudaStream_t stream)
+template <bool PRIMARY>
+void launch_extend_variant(const SceneView& s, const FrameView& f, const Settings& st, uint32_t bounce,
+                           const Camera& cam, const LaunchShape& shape, cudaStream_t stream)
 {
     const bool count = (st.flags & TR_FLAG_COUNT_TRAVERSAL) != 0;
     if (f.segments) {
         if (count)
-            extend_kernel<true, true><<<shape.extendBlocks, 128, 0, stream>>>(s, f, st, bounce);
+            extend_kernel<true, true, PRIMARY><<<shape.extendBlocks, 128, 0, stream>>>(s, f, st, bounce, cam);
         else
-            extend_kernel<false, true><<<shape.extendBlocks, 128, 0, stream>>>(s, f, st, bounce);
+            extend_kernel<false, true, PRIMARY><<<shape.extendBlocks, 128, 0, stream>>>(s, f, st, bounce, cam);
     } else {
         if (count)
-            extend_kernel<true, false><<<shape.extendBlocks, 128, 0, stream>>>(s, f, st, bounce);
+            extend_kernel<true, false, PRIMARY><<<shape.extendBlocks, 128, 0, stream>>>(s, f, st, bounce, cam);
         else
-            extend_kernel<false, false><<<shape.extendBlocks, 128, 0, stream>>>(s, f, st, bounce);
+            extend_kernel<false, false, PRIMARY><<<shape.extendBlocks, 128, 0, stream>>>(s, f, st, bounce, cam);
     }
+}
+
+cudaError_t launch_extend(const SceneView& s, const FrameView& f, const Settings& st0, uint32_t bounce,
+                          const LaunchShape& shape, cudaStream_t stream, const Camera* primary)
+{
+    Settings st = st0;
+    st.refillBelow = shape.refillBelow;
+    if (primary && bounce == 0 && (st.flags & TR_FLAG_REFERENCE_SAMPLING) == 0)
+        launch_extend_variant<true>(s, f, st, bounce, *primary, shape, stream);
+    else
+        launch_extend_variant<false>(s, f, st, bounce, Camera{}, shape, stream);
     return cudaGetLastError();
 }
 
@@ -1268,9 +1303,11 @@ cudaError_t launch_shade(const SceneView& s, const FrameView& f, const Settings&
     return cudaGetLastError();
 }
 
-cudaError_t launch_connect(const SceneView& s, const FrameView& f, const Settings& st, uint32_t bounce,
+cudaError_t launch_connect(const SceneView& s, const FrameView& f, const Settings& st0, uint32_t bounce,
                            const LaunchShape& shape, cudaStream_t stream)
 {
+    Settings st = st0;
+    st.refillBelow = shape.refillBelow;
     const bool count = (st.flags & TR_FLAG_COUNT_TRAVERSAL) != 0;
     if (f.segments) {
         if (count)
@@ -1316,9 +1353,10 @@ cudaError_t launch_adjoint(const SceneView& s, const FrameView& f, const Camera&
     const uint32_t gradBlocks = shape.sms * uint32_t(perSm > 0 ? perSm : 1);
     Settings fwd = st;
     fwd.flags &= ~uint32_t(TR_FLAG_COUNT_TRAVERSAL | TR_FLAG_WRITE_AOVS);
+    fwd.refillBelow = shape.refillBelow;
     adjoint_generate_kernel<<<(f.pathCount + 255u) / 256u, 256, 0, stream>>>(f, cam, fwd, a);
     for (uint32_t bounce = 0; bounce < st.maxDepth; ++bounce) {
-        extend_kernel<false, false><<<shape.extendBlocks, 128, 0, stream>>>(s, f, fwd, bounce);
+        extend_kernel<false, false, false><<<shape.extendBlocks, 128, 0, stream>>>(s, f, fwd, bounce, Camera{});
         if (useSmem)
             adjoint_shade_kernel<true><<<gradBlocks, kAdjointThreads, smem, stream>>>(s, f, fwd, bounce, a);
         else
@@ -1356,7 +1394,7 @@ LaunchShape default_launch_shape(int device, uint32_t capacity)
     if (sms <= 0)
         sms = 1;
     int perSm = 0;
-    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&perSm, extend_kernel<false, false>, 128, 0);
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&perSm, extend_kernel<false, false, false>, 128, 0);
     shape.extendBlocks = uint32_t(sms) * uint32_t(perSm > 0 ? perSm : 4);
     perSm = 0;
     cudaOccupancyMaxActiveBlocksPerMultiprocessor(&perSm, connect_kernel<false, false>, 128, 0);
@@ -1367,6 +1405,30 @@ LaunchShape default_launch_shape(int device, uint32_t capacity)
     const uint32_t need = (capacity + 127u) / 128u;
     shape.shadeBlocks = need < maxShade ? (need > 0 ? need : 1u) : maxShade;
     shape.sms = uint32_t(sms);
+    shape.refillBelow = kRefillBelow;
+    shape.extendPerSm = uint32_t(shape.extendBlocks / shape.sms);
+    shape.connectPerSm = uint32_t(shape.connectBlocks / shape.sms);
+    shape.shadeWaves = 4;
+    return shape;
+}
+
+LaunchShape tuned_launch_shape(int device, uint32_t capacity, const tr_tuning& t)
+{
+    LaunchShape shape = default_launch_shape(device, capacity);
+    if (t.refill_below >= 1 && t.refill_below <= 32)
+        shape.refillBelow = t.refill_below;
+    if (t.extend_blocks_per_sm >= 1 && t.extend_blocks_per_sm <= shape.extendPerSm)
+        shape.extendBlocks = shape.sms * t.extend_blocks_per_sm;
+    if (t.connect_blocks_per_sm >= 1 && t.connect_blocks_per_sm <= shape.connectPerSm)
+        shape.connectBlocks = shape.sms * t.connect_blocks_per_sm;
+    if (t.shade_waves >= 1 && t.shade_waves <= 64) {
+        int perSm = 0;
+        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&perSm, shade_kernel<false, false>, 128, 0);
+        const uint32_t maxShade = shape.sms * uint32_t(perSm > 0 ? perSm : 4) * t.shade_waves;
+        const uint32_t need = (capacity + 127u) / 128u;
+        shape.shadeBlocks = need < maxShade ? (need > 0 ? need : 1u) : maxShade;
+        shape.shadeWaves = t.shade_waves;
+    }
     return shape;
 }
 

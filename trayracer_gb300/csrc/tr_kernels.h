@@ -4,6 +4,7 @@
 #include <cuda_runtime.h>
 
 #include "tr_device.h"
+#include "../../include/trayracer.h"
 
 namespace tr {
 
@@ -15,13 +16,21 @@ struct LaunchShape {
     uint32_t connectBlocks = 0;
     uint32_t shadeBlocks = 0;
     uint32_t sms = 0;
+    uint32_t refillBelow = 24;   // lane refill threshold of the persistent traversal warps
+    uint32_t extendPerSm = 0;    // resident extend / connect blocks per SM (occupancy limit by default)
+    uint32_t connectPerSm = 0;
+    uint32_t shadeWaves = 4;     // shade grid cap, in waves of resident blocks
 };
 
 LaunchShape default_launch_shape(int device, uint32_t capacity);
+// The default shape with the tunable fields of t applied (zero fields keep the default).
+LaunchShape tuned_launch_shape(int device, uint32_t capacity, const tr_tuning& t);
 
 cudaError_t launch_generate(const FrameView& f, const Camera& cam, const Settings& st, cudaStream_t stream);
+// primary != nullptr at bounce 0 (default sampling mode): the camera rays are
+// computed inside the extend launch and no generate launch is needed.
 cudaError_t launch_extend(const SceneView& s, const FrameView& f, const Settings& st, uint32_t bounce,
-                          const LaunchShape& shape, cudaStream_t stream);
+                          const LaunchShape& shape, cudaStream_t stream, const Camera* primary = nullptr);
 cudaError_t launch_shade(const SceneView& s, const FrameView& f, const Settings& st, uint32_t bounce,
                          const LaunchShape& shape, cudaStream_t stream);
 cudaError_t launch_connect(const SceneView& s, const FrameView& f, const Settings& st, uint32_t bounce,

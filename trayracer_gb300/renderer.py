@@ -213,6 +213,26 @@ class DeviceRenderer:
         self._check(self._lib.tr_adjoint_frame(self._ctx, C.c_void_p(stream or None), C.c_void_p(pixel_grad_ptr),
                                                scale, C.c_void_p(param_grad_ptr)), "tr_adjoint_frame")
 
+    def Tuning(self) -> dict:
+        t = _abi.Tuning()
+        self._check(self._lib.tr_get_tuning(self._ctx, C.byref(t)), "tr_get_tuning")
+        return {f: getattr(t, f) for f, _ in t._fields_ if f != "reserved"}
+
+    def SetTuning(self, **kw):
+        t = _abi.Tuning()
+        for k, v in kw.items():
+            setattr(t, k, int(v))
+        self._check(self._lib.tr_set_tuning(self._ctx, C.byref(t)), "tr_set_tuning")
+
+    def Autotune(self, stream: int = 0, skip_bvh: bool = False) -> dict:
+        """tr_autotune: times launch shapes (and BVH leaf sizes) on the current frame setup."""
+        rep = _abi.TuneReport()
+        self._check(self._lib.tr_autotune(self._ctx, C.c_void_p(stream or None),
+                                          _abi.TR_TUNE_SKIP_BVH if skip_bvh else 0, C.byref(rep)), "tr_autotune")
+        chosen = {f: getattr(rep.chosen, f) for f, _ in rep.chosen._fields_ if f != "reserved"}
+        return {"chosen": chosen, "frame_ms_default": rep.frame_ms_default, "frame_ms_tuned": rep.frame_ms_tuned,
+                "trials": rep.trials}
+
     def Synchronize(self, stream: int = 0):
         self._check(self._lib.tr_synchronize(self._ctx, C.c_void_p(stream or None)), "tr_synchronize")
 
