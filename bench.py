@@ -61,6 +61,7 @@ def parse():
                    help="plain: the heightfield (default); batch: the 64-scene mix in one wavefront against "
                         "per-scene renders; adjoint: forward frame and path-replay adjoint of the "
                         "differentiation scene")
+    p.add_argument("--no-autotune", action="store_true", help="plain workload: keep the default launch shapes")
     p.add_argument("--batch-count", type=int, default=64)
     p.add_argument("--wave-paths", type=int, default=0, help="batched waves: paths per wave (0: library default)")
     return p.parse_args()
@@ -477,6 +478,12 @@ def main():
         for _ in range(frames_per_step):
             r.RenderFrame(stream=sptr, use_graph=use_graph)
 
+    # --- autotuner (launch shapes, BVH leaf size) on this workload, outside the timed region
+    tune = None
+    if not args.no_autotune:
+        tune = r.Autotune(stream=sptr)
+        torch.cuda.synchronize()
+
     # --- counting pass (rays per step, traversal work), outside the timed region
     stage_ms = {"generate": 0.0, "extend": 0.0, "shade": 0.0, "connect": 0.0, "finalize": 0.0}
     ext_rays = sh_rays = 0
@@ -647,6 +654,7 @@ def main():
             },
             "gpu_launches": args.steps * frames_per_step * (3 * st.maxDepth + 3),
             "scene_upload_s": round(upload_s, 2),
+            "tuning": tune,
         }
         print(json.dumps(line), flush=True)
     r.close()
