@@ -62,6 +62,8 @@ def parse():
                         "per-scene renders; adjoint: forward frame and path-replay adjoint of the "
                         "differentiation scene")
     p.add_argument("--no-autotune", action="store_true", help="plain workload: keep the default launch shapes")
+    p.add_argument("--rmse-spp", type=int, default=1024,
+                   help="plain workload: also compare a render of this many spp against the FP64 oracle")
     p.add_argument("--batch-count", type=int, default=64)
     p.add_argument("--wave-paths", type=int, default=0, help="batched waves: paths per wave (0: library default)")
     return p.parse_args()
@@ -576,13 +578,16 @@ def main():
     achieved = ext_bytes / ext_s / 1e9
     compulsory = (ext_rays * EXTEND_BYTES_PER_RAY + hit_rays * EXTEND_BYTES_PER_HIT) / ext_s / 1e9
     traffic = None
-    prof = ROOT / "profiles" / "extend_traffic.json"
+    # DRAM bytes per extend ray from the ncu capture summarised in profiles/ (a text line
+    # "dram_bytes_per_extend_ray: <value>"), scaled to this run's average launch
+    prof = ROOT / "profiles" / "extend_kernel_heightfield_1920x1080_traffic.md"
     if prof.exists():
-        try:
-            pj = json.loads(prof.read_text())
-            traffic = pj["dram_bytes_per_ray"] * ext_rays / launches
-        except (KeyError, ValueError):
-            traffic = None
+        for line in prof.read_text().splitlines():
+            if line.strip().startswith("dram_bytes_per_extend_ray:"):
+                try:
+                    traffic = float(line.split(":", 1)[1]) * ext_rays / launches
+                except ValueError:
+                    traffic = None
 
     # --- image accuracy on a pixel band against the FP64 oracle
     rmse = None
@@ -591,16 +596,39 @@ def main():
         try:
             from oracle import Oracle
 
-            img = r.ColorBuffer()
+            # Same sample keys on both sides, so the difference is fp32 vs fp64 arithmetic only; it
+            # shows as noise where a path's fp32 and fp64 continuations part (near-specular lobes,
+            # Russian roulette and lobe choices on a last-bit difference) and falls as 1/sqrt(spp).
             band0 = (scene.height // 2) * scene.width
             nb = 2 * scene.width
-            acc64, _, _ = Oracle(scene).render(scene.camera, tr.settings_for(scene, multi_sample=args.ms),
-                                               scene.width, scene.height, frames=frames_per_step,
-                                               first_pixel=band0, pixel_count=nb, use_double=True,
-                                               threads=os.cpu_count() or 1)
-            ref = acc64[:, :3] / acc64[:, 3:4]
-            got = img.reshape(-1, 4)[band0:band0 + nb, :3].astype(np.float64)
-            rmse = float(np.sqrt(np.mean((got - ref) ** 2)) / max(1e-12, np.sqrt(np.mean(ref ** 2))))
+            orc = Oracle(scene)
+
+            def band_rmse(img, frames, use_double=True):
+                acc, _, _ = orc.render(scene.camera, tr.settings_for(scene, multi_sample=args.ms), scene.width,
+                                       scene.height, frames=frames, first_pixel=band0, pixel_count=nb,
+                                       use_double=use_double, threads=os.cpu_count() or 1)
+                ref = acc[:, :3] / acc[:, 3:4]
+                got = img.reshape(-1, 4)[band0:band0 + nb, :3].astype(np.float64)
+                return float(np.sqrt(np.mean((got - ref) ** 2)) / max(1e-12, np.sqrt(np.mean(ref ** 2))))
+
+            img = r.ColorBuffer()
+            rmse = {"spp_%d" % args.spp: band_rmse(img, frames_per_step)}
+            # the fp32 oracle against the FP64 oracle: the same divergence without the GPU
+            acc32, _, _ = orc.render(scene.camera, tr.settings_for(scene, multi_sample=args.ms), scene.width,
+                                     scene.height, frames=frames_per_step, first_pixel=band0, pixel_count=nb,
+                                     use_double=False, threads=os.cpu_count() or 1)
+            acc64, _, _ = orc.render(scene.camera, tr.settings_for(scene, multi_sample=args.ms), scene.width,
+                                     scene.height, frames=frames_per_step, first_pixel=band0, pixel_count=nb,
+                                     use_double=True, threads=os.cpu_count() or 1)
+            r32, r64 = acc32[:, :3] / acc32[:, 3:4], acc64[:, :3] / acc64[:, 3:4]
+            rmse["fp32_oracle_spp_%d" % args.spp] = float(np.sqrt(np.mean((r32 - r64) ** 2)) /
+                                                          max(1e-12, np.sqrt(np.mean(r64 ** 2))))
+            if args.rmse_spp > args.spp:
+                frames = args.rmse_spp // args.ms
+                r.Reset()
+                for _ in range(frames):
+                    r.RenderFrame(stream=sptr, use_graph=True)
+                rmse["spp_%d" % (frames * args.ms)] = band_rmse(r.ColorBuffer(), frames)
             cpu = cpu_baseline(scene, args, args.cpu_seconds)
         except Exception as e:  # the checker is optional; the GPU numbers stand
             cpu = {"value": None, "unavailable": str(e)}
@@ -626,7 +654,7 @@ def main():
             "shadow_rays_per_step": int(sh_rays),
             "hit_rays_per_step": int(hit_rays),
             "stage_ms_per_step": {k: round(v, 3) for k, v in stage_ms.items()},
-            "rmse_vs_fp64_band": rmse,
+            "rmse_vs_fp64_band": rmse,  # relative RMSE on 2 image rows, by samples per pixel
             "roofline": {
                 "kernel": "extend_kernel (CWBVH closest hit)",
                 "bound": "hbm",
