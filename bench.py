@@ -446,6 +446,7 @@ def main():
 
     import trayracer_gb300 as tr
     from trayracer_gb300._abi import TR_FLAG_COUNT_TRAVERSAL
+    from trayracer_gb300.shards import max_over_ranks, shard_settings
 
     torch.cuda.set_device(local)
     if ws > 1:
@@ -454,8 +455,7 @@ def main():
         dist.init_process_group("nccl")
     scene = build_scene(args)
     frames_per_step = max(1, args.spp // args.ms)
-    st = tr.settings_for(scene, multi_sample=args.ms)
-    st.seed = scene.seed + 7919 * rank  # disjoint sample streams per shard
+    st = shard_settings(tr.settings_for(scene, multi_sample=args.ms), rank)  # disjoint sample streams per shard
     r = tr.DeviceRenderer(local)
     t = time.perf_counter()
     r.UpdateScene(scene)
@@ -542,9 +542,7 @@ def main():
     torch.cuda.synchronize()
     total_ms = float(sum(times))
     if ws > 1:
-        t_tensor = torch.tensor([total_ms], device=f"cuda:{local}")
-        torch.distributed.all_reduce(t_tensor, op=torch.distributed.ReduceOp.MAX)
-        total_ms = float(t_tensor.item())
+        total_ms = max_over_ranks(total_ms, device=f"cuda:{local}")
     final = r.Statistics()
     assert final["device_error"] == 0
 
