@@ -57,10 +57,11 @@ def parse():
     p.add_argument("--no-cpu-baseline", action="store_true")
     p.add_argument("--profile", action="store_true",
                    help="render one eager frame of the workload and exit (the case the ncu captures use)")
-    p.add_argument("--workload", default="plain", choices=["plain", "batch", "adjoint"],
+    p.add_argument("--workload", default="plain", choices=["plain", "batch", "adjoint", "large"],
                    help="plain: the heightfield (default); batch: the 64-scene mix in one wavefront against "
                         "per-scene renders; adjoint: forward frame and path-replay adjoint of the "
-                        "differentiation scene")
+                        "differentiation scene; large: the 20.5M-triangle displaced-sphere scene at 3840x2160, "
+                        "16 spp, 12 bounces, forward frame and adjoint over its 4096 materials")
     p.add_argument("--no-autotune", action="store_true", help="plain workload: keep the default launch shapes")
     p.add_argument("--rmse-spp", type=int, default=1024,
                    help="plain workload: also compare a render of this many spp against the FP64 oracle")
@@ -429,6 +430,86 @@ def run_adjoint(args):
     print(json.dumps(line), flush=True)
 
 
+def run_large(args):
+    """The large configuration: 4096 displaced spheres (20.48 M triangles, 100k emissive), 4096
+    materials, 3840x2160, 16 spp in one frame (132.7 M paths in flight), 12 bounces, RR from bounce
+    3; a forward frame (graph) and the path-replay adjoint of the L2 loss against a black target
+    over all materials."""
+    import torch
+
+    import trayracer_gb300 as tr
+
+    torch.cuda.set_device(0)
+    stream = torch.cuda.current_stream()
+    sptr = stream.cuda_stream
+    flush = torch.empty(256 * 1024 * 1024 // 4, dtype=torch.float32, device="cuda")
+    t = time.perf_counter()
+    scene = tr.displaced_spheres()
+    gen_s = time.perf_counter() - t
+    st = tr.settings_for(scene, multi_sample=scene.spp)
+    r = tr.DeviceRenderer(0)
+    t = time.perf_counter()
+    r.UpdateScene(scene)
+    upload_s = time.perf_counter() - t
+    info = r.SceneInfo()
+    r.SetCamera(scene.camera)
+    r.Resize((scene.width, scene.height))
+    r.SetSettings(st)
+    W, H = scene.width, scene.height
+    grad = torch.zeros((scene.materials.shape[0], 9), dtype=torch.float32, device="cuda")
+    fwd, adj, rays = [], [], 0
+    pg = None
+    for i in range(args.warmup + args.steps):
+        flush.fill_(1.0)
+        e0, e1, e2, e3 = (torch.cuda.Event(enable_timing=True) for _ in range(4))
+        r.Reset()
+        e0.record(stream)
+        r.RenderFrame(stream=sptr, use_graph=True)
+        e1.record(stream)
+        if pg is None:
+            pg = torch.from_numpy(r.ColorBuffer()).cuda()  # dL/dcolor of 0.5 |img|^2
+            rays = r.Statistics()["path_count"]
+        flush.fill_(1.0)
+        e2.record(stream)
+        r.AdjointFrame(pg.data_ptr(), 1.0 / scene.spp, grad.data_ptr(), stream=sptr)
+        e3.record(stream)
+        e3.synchronize()
+        if i >= args.warmup:
+            fwd.append(e0.elapsed_time(e1))
+            adj.append(e2.elapsed_time(e3))
+    stats = r.Statistics()
+    assert stats["device_error"] == 0
+    r.close()
+    f_ms, a_ms = float(statistics.median(fwd)), float(statistics.median(adj))
+    line = {
+        "metric": "Mrays/s",
+        "value": round(rays / (f_ms / 1e3) / 1e6, 1),
+        "unit": "Mrays/s",
+        "n_gpus": 1,
+        "steps": args.steps,
+        "warmup": args.warmup,
+        "ms_per_step": round(f_ms + a_ms, 3),
+        "higher_is_better": True,
+        "scaling": "weak",
+        "vs_baseline": None,
+        "dtype": "f32",
+        "data": "synthetic",
+        "config": {"workload": f"{info['triangle_count']} triangles (4096 displaced spheres, 100k emissive), "
+                               f"4096 materials, {W}x{H}, {scene.spp} spp, 12 bounces, RR from 3",
+                   "l2": "flushed before the forward frame and before the adjoint (256 MiB write)"},
+        "samples_per_s": round(W * H * scene.spp / (f_ms / 1e3), 1),
+        "forward_ms": round(f_ms, 3),
+        "adjoint_ms": round(a_ms, 3),
+        "adjoint_over_forward": round(a_ms / f_ms, 3),
+        "rays_per_frame": int(rays),
+        "scene_generation_s": round(gen_s, 2),
+        "scene_upload_s": round(upload_s, 2),
+        "scene_device_bytes": int(info["device_bytes"]),
+        "gradient_norm": float(grad.norm()),
+    }
+    print(json.dumps(line), flush=True)
+
+
 def main():
     args = parse()
     ws, rank, local = dist_env()
@@ -440,6 +521,9 @@ def main():
         return
     if args.workload == "adjoint":
         run_adjoint(args)
+        return
+    if args.workload == "large":
+        run_large(args)
         return
 
     import torch

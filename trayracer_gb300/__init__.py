@@ -11,4 +11,12 @@ from ._abi import (  # noqa: F401
     load_library,
 )
 from .renderer import BatchRenderer, DeviceRenderer, KernelSettings, RenderModes, TracerError, camera_to_c, settings_for  # noqa: F401
-from .scenes import CameraSpec, Scene, cornell_box, heightfield, sphere_batch, sphere_scene  # noqa: F401
+from .scenes import (  # noqa: F401
+    CameraSpec,
+    Scene,
+    cornell_box,
+    displaced_spheres,
+    heightfield,
+    sphere_batch,
+    sphere_scene,
+)

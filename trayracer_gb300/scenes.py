@@ -421,8 +421,47 @@ def sphere_batch(count: int = 64, seed: int = 11, min_tris: int = 1000, max_tris
     return out
 
 
+def displaced_spheres(count: int = 4096, subdiv: int = 25, n_emissive: int = 20, seed: int = 13,
+                      width: int = 3840, height: int = 2160, spp: int = 16, max_depth: int = 12, rr_start: int = 3,
+                      extent: float = 40.0) -> Scene:
+    """The large configuration: `count` spheres of 8 subdiv^2 triangles (25 -> 5000, 4096 spheres ->
+    20.48 M triangles) with every vertex displaced along its normal by N(0, 0.02) of the radius,
+    one Disney material per sphere (baseColor/roughness/metallic/specular U[0,1]), and the
+    triangles of `n_emissive` spheres emissive (20 x 5000 = 100k emissive triangles) with
+    log-uniform intensity in [1, 1000] per sphere."""
+    rng = np.random.default_rng(seed)
+    f32 = np.float32
+    unit_p, unit_i = _octahedron_sphere(subdiv)
+    nv, nt = unit_p.shape[0], unit_i.shape[0]
+    centers = rng.uniform(-extent, extent, (count, 1, 3)).astype(np.float32)
+    radii = (f32(0.5) + f32(1.5) * rng.random((count, 1, 1), dtype=np.float32)).astype(np.float32)
+    disp = (f32(1.0) + f32(0.02) * rng.standard_normal((count, nv, 1)).astype(np.float32)).astype(np.float32)
+    pos = (centers + unit_p[None, :, :] * (radii * disp)).reshape(-1, 3).astype(np.float32)
+    nrm = np.broadcast_to(unit_p[None], (count, nv, 3)).reshape(-1, 3).astype(np.float32)
+    idx = (unit_i[None, :, :].astype(np.uint64) + (np.arange(count, dtype=np.uint64) * nv)[:, None, None])
+    idx = idx.reshape(-1, 3).astype(np.uint32)
+    mat = np.repeat(np.arange(count, dtype=np.uint32), nt)
+    emissive = set(int(x) for x in rng.choice(count, size=n_emissive, replace=False))
+    mats = []
+    for k in range(count):
+        p = rng.random(4).astype(np.float32)
+        base = rng.random(3).astype(np.float32)
+        if k in emissive:
+            intensity = np.float32(10.0 ** (3.0 * p[3]))
+            mats.append(material(diffuse=(1, 1, 1), emissive=(intensity, intensity, intensity),
+                                 closure=TR_CLOSURE_DIFFUSE))
+        else:
+            mats.append(material(diffuse=base, closure=TR_CLOSURE_DISNEY, roughness=p[0], metallic=p[1],
+                                 specular=p[2]))
+    cam = CameraSpec(position=(0.0, 10.0, -extent * 2.2), target=(0.0, 0.0, 0.0), up=(0.0, 1.0, 0.0),
+                     fov=float(np.float32(60.0 * np.pi / 180.0)))
+    return Scene(f"displaced_spheres_{count}", pos, nrm, None, idx, mat, np.array(mats, MATERIAL_DTYPE), cam,
+                 width, height, spp, max_depth, rr_start, seed)
+
+
 CONFIGS = {
     "cornell_box": cornell_box,
     "heightfield": heightfield,
     "sphere_batch": sphere_batch,
+    "displaced_spheres": displaced_spheres,
 }
