@@ -379,7 +379,8 @@ def run_adjoint(args):
     grad = torch.zeros((scene.materials.shape[0], 9), dtype=torch.float32, device="cuda")
     if args.profile:
         r.RenderFrame(stream=sptr, use_graph=False)
-        r.AdjointFrame(target.data_ptr(), 1.0 / 32, grad.data_ptr(), stream=sptr)
+        pg = torch.from_numpy(r.ColorBuffer()).cuda() - target  # dL/dcolor of 0.5 |img - target|^2
+        r.AdjointFrame(pg.data_ptr(), 1.0 / 32, grad.data_ptr(), stream=sptr)
         torch.cuda.synchronize()
         print(json.dumps({"grad_norm": float(grad.norm())}))
         r.close()
