@@ -259,7 +259,8 @@ typedef struct tr_tuning {
     uint32_t extend_blocks_per_sm;  /* persistent extend grid, 1..occupancy */
     uint32_t connect_blocks_per_sm; /* persistent connect grid, 1..occupancy */
     uint32_t shade_waves;           /* shade grid cap in waves of resident blocks, 1..64 */
-    uint32_t reserved[3];
+    uint32_t sort_hits;             /* 1: counting sort of each bounce's hits by material before shade */
+    uint32_t reserved[2];
 } tr_tuning;
 
 typedef struct tr_tune_report {
@@ -347,7 +348,8 @@ tr_status tr_set_tuning(void* ctx, const tr_tuning* tuning);
 /* Times graph-replayed frames of the current scene, camera, settings and
  * resolution (one warm-up + two timed frames per configuration) over the
  * lane refill threshold, the persistent extend / connect grids, the shade grid
- * cap and (unless TR_TUNE_SKIP_BVH) the BVH leaf size, one parameter at a time,
+ * cap, the material sort of the hits and (unless TR_TUNE_SKIP_BVH) the BVH leaf
+ * size, one parameter at a time,
  * keeps the fastest and resets the accumulation. */
 tr_status tr_autotune(void* ctx, void* stream, uint32_t flags, tr_tune_report* report);
 

@@ -187,12 +187,23 @@ def test_tuning_keeps_images_and_autotune_picks_fastest():
     r.RenderFrame()
     want = r.ColorBuffer().copy()
     # launch shapes change the order work is picked up, never a path's result
-    r.SetTuning(refill_below=12, extend_blocks_per_sm=2, connect_blocks_per_sm=3, shade_waves=1)
+    r.SetTuning(refill_below=12, extend_blocks_per_sm=2, connect_blocks_per_sm=3, shade_waves=1, sort_hits=1)
     r.Reset()
     r.RenderFrame()
     np.testing.assert_array_equal(r.ColorBuffer(), want)
     t = r.Tuning()
     assert t["refill_below"] == 12 and t["extend_blocks_per_sm"] == 2 and t["shade_waves"] == 1
+    assert t["sort_hits"] == 1
+    # the per-stage entry points sort too when the sort is on
+    r.Reset()
+    r.BeginFrame()
+    r.Generate()
+    for b in range(st.maxDepth):
+        r.Extend(b)
+        r.Shade(b)
+        r.Connect(b)
+    r.Finalize()
+    np.testing.assert_array_equal(r.ColorBuffer(), want)
     r.SetTuning()  # back to the defaults
     rep = r.Autotune()
     assert rep["trials"] >= 10

@@ -163,7 +163,8 @@ class Tuning(C.Structure):
         ("extend_blocks_per_sm", C.c_uint32),
         ("connect_blocks_per_sm", C.c_uint32),
         ("shade_waves", C.c_uint32),
-        ("reserved", C.c_uint32 * 3),
+        ("sort_hits", C.c_uint32),
+        ("reserved", C.c_uint32 * 2),
     ]
 
 

@@ -71,6 +71,7 @@ struct Context {
     uint32_t width = 0, height = 0;
     DeviceArena frameArena;
     FrameView frame{};
+    SortView sort{};               // material sort of the hit queue (keys/order in the frame arena, bins in the scene arena)
     DeviceArena adjointArena;      // path-replay scratch, allocated by the first tr_adjoint_frame of a frame size
     AdjointView adjoint{};
     uint32_t* adjointCounters = nullptr;
@@ -213,6 +214,8 @@ tr_status ensure_frame(Context* c)
     const size_t oSc = take(sizeof(uint32_t));
     const size_t oErr = take(sizeof(uint32_t));
     const size_t oTrav = take(4 * sizeof(unsigned long long));
+    const size_t oKeys = take(cap * sizeof(uint32_t));
+    const size_t oOrder = take(cap * sizeof(uint32_t));
     void* base = nullptr;
     const cudaError_t e = cudaMalloc(&base, off);
     if (e != cudaSuccess)
@@ -234,6 +237,8 @@ tr_status ensure_frame(Context* c)
     f.sampleCount = reinterpret_cast<uint32_t*>(b + oSc);
     f.errorFlag = reinterpret_cast<uint32_t*>(b + oErr);
     f.traversal = reinterpret_cast<unsigned long long*>(b + oTrav);
+    c->sort.keys = reinterpret_cast<uint32_t*>(b + oKeys);
+    c->sort.order = reinterpret_cast<uint32_t*>(b + oOrder);
     f.capacity = uint32_t(cap);
     f.resX = c->width;
     f.resY = c->height;
@@ -245,6 +250,7 @@ tr_status ensure_frame(Context* c)
     c->frameMs = c->settings.multiSample;
     c->sampleCount = 0;
     c->shape = tuned_launch_shape(c->device, uint32_t(cap), c->tuning);
+    f.hitOrder = c->shape.sortHits ? c->sort.order : nullptr;
     return TR_OK;
 }
 
@@ -278,6 +284,8 @@ tr_status enqueue_frame(Context* c, cudaStream_t s, bool timed)
         TR_CUDA(c, cudaEventRecord(c->evGenerate, s));
     for (uint32_t b = 0; b < c->settings.maxDepth; ++b) {
         TR_CUDA(c, launch_extend(c->scene, c->frame, c->settings, b, c->shape, s, fused ? &c->camera : nullptr));
+        if (c->shape.sortHits)
+            TR_CUDA(c, launch_sort_hits(c->scene, c->frame, c->sort, b, c->shape, s));
         if (timed)
             TR_CUDA(c, cudaEventRecord(c->evExtend[b], s));
         TR_CUDA(c, launch_shade(c->scene, c->frame, c->settings, b, c->shape, s));
@@ -501,6 +509,7 @@ tr_status tr_scene_upload(void* ctx, const tr_scene_desc* desc)
     const size_t oLights = take(fs.lights.size() * sizeof(LightTri));
     const size_t oAlias = take(fs.alias.size() * sizeof(AliasEntry));
     const size_t oXf = take(fs.invTransforms.size() * sizeof(float4));
+    const size_t oBins = take(2 * size_t(desc->material_count) * sizeof(uint32_t));  // sort counts + cursors
 
     if (c->stream)
         cudaStreamSynchronize(c->stream);
@@ -547,6 +556,10 @@ tr_status tr_scene_upload(void* ctx, const tr_scene_desc* desc)
     s.lights = reinterpret_cast<const LightTri*>(b + oLights);
     s.alias = reinterpret_cast<const AliasEntry*>(b + oAlias);
     s.invTransforms = reinterpret_cast<const float4*>(b + oXf);
+    TR_CUDA(c, cudaMemset(b + oBins, 0, 2 * size_t(desc->material_count) * sizeof(uint32_t)));
+    c->sort.counts = reinterpret_cast<uint32_t*>(b + oBins);
+    c->sort.cursor = c->sort.counts + desc->material_count;
+    c->sort.bins = desc->material_count;
     s.lightCount = int32_t(fs.lights.size());
     s.lightEnergy = fs.lightEnergy;
     s.lightEnergyTotal = fs.lightEnergyTotal;
@@ -704,6 +717,7 @@ tr_status tr_get_tuning(void* ctx, tr_tuning* out)
         t.extend_blocks_per_sm = c->shape.extendBlocks / c->shape.sms;
         t.connect_blocks_per_sm = c->shape.connectBlocks / c->shape.sms;
         t.shade_waves = c->shape.shadeWaves;
+        t.sort_hits = c->shape.sortHits;
     }
     *out = t;
     return TR_OK;
@@ -714,7 +728,7 @@ tr_status tr_set_tuning(void* ctx, const tr_tuning* t)
     if (!ctx || !t)
         return TR_ERR_INVALID_ARGUMENT;
     Context* c = static_cast<Context*>(ctx);
-    if (t->bvh_leaf_size > 3 || t->refill_below > 32 || t->shade_waves > 64)
+    if (t->bvh_leaf_size > 3 || t->refill_below > 32 || t->shade_waves > 64 || t->sort_hits > 1)
         return fail(c, TR_ERR_INVALID_ARGUMENT, "tuning out of range (leaf size <= 3, refill <= 32, shade waves <= 64)");
     cudaSetDevice(c->device);
     if (t->bvh_leaf_size && c->hasScene) {
@@ -725,8 +739,10 @@ tr_status tr_set_tuning(void* ctx, const tr_tuning* t)
     c->tuning = *t;
     c->tuning.bvh_leaf_size = c->leafSize;
     invalidate_graph(c);
-    if (c->frameArena.base)
+    if (c->frameArena.base) {
         c->shape = tuned_launch_shape(c->device, uint32_t(c->frame.capacity), c->tuning);
+        c->frame.hitOrder = c->shape.sortHits ? c->sort.order : nullptr;
+    }
     return TR_OK;
 }
 
@@ -808,6 +824,12 @@ tr_status tr_autotune(void* ctx, void* stream, uint32_t flags, tr_tune_report* r
         tr_tuning t = best;
         t.shade_waves = w;
         if (st == TR_OK && w != best.shade_waves)
+            st = tryTuning(t);
+    }
+    {
+        tr_tuning t = best;
+        t.sort_hits = best.sort_hits ? 0u : 1u;
+        if (st == TR_OK)
             st = tryTuning(t);
     }
     if ((flags & TR_TUNE_SKIP_BVH) == 0)
@@ -946,6 +968,8 @@ tr_status tr_extend(void* ctx, void* stream, uint32_t bounce)
     if (st != TR_OK)
         return st;
     TR_CUDA(c, launch_extend(c->scene, c->frame, c->settings, bounce, c->shape, pick_stream(c, stream)));
+    if (c->shape.sortHits)
+        TR_CUDA(c, launch_sort_hits(c->scene, c->frame, c->sort, bounce, c->shape, pick_stream(c, stream)));
     return TR_OK;
 }
 

@@ -136,6 +136,8 @@ struct FrameView {
     uint32_t capacity;
     uint32_t resX, resY;
     uint32_t pathCount;    // resX * resY * multiSample (batched: the paths of the wave)
+    // material order of the hit queue (null: shade in queue order)
+    const uint32_t* hitOrder;
     // batched rendering only (null / 0 for one scene)
     const BatchSegment* segments;
     const BatchItem* items;
@@ -185,6 +187,16 @@ struct AdjointView {
     float scale;
     uint32_t materialCount;
     uint32_t sampleBase;   // sample count before the replayed frame (its paths' sample keys start here)
+    uint32_t pad;
+};
+
+// Buffers of the material sort of the hit queue.
+struct SortView {
+    uint32_t* keys;        // material of each hit-queue slot
+    uint32_t* order;       // hit-queue slots grouped by material
+    uint32_t* counts;      // hits per material (zeroed again by the scan)
+    uint32_t* cursor;      // next free position per material
+    uint32_t bins;         // materials
     uint32_t pad;
 };
 

@@ -717,10 +717,11 @@ __global__ void __launch_bounds__(128) shade_kernel(SceneView s, FrameView f, Se
     const uint32_t warpStride = (gridDim.x * blockDim.x) >> 5;
 
     for (uint32_t base = warpGlobal * 32u; base < count; base += warpStride * 32u) {
-        const uint32_t i = base + lane;
+        const uint32_t k = base + lane;
         bool wantExt = false, wantShadow = false;
         float4 ext[3], sh[3];
-        if (i < count) {
+        if (k < count) {
+            const uint32_t i = f.hitOrder ? __ldcs(f.hitOrder + k) : k;
             const float4 O4 = __ldcs(in + i);
             const float4 D4 = __ldcs(in + i + cap);
             const float4 T4 = __ldcs(in + i + 2 * cap);
@@ -754,6 +755,103 @@ __global__ void __launch_bounds__(128) shade_kernel(SceneView s, FrameView f, Se
             __stcs(out + exSlot + cap, ext[1]);
             __stcs(out + exSlot + 2 * cap, ext[2]);
         }
+    }
+}
+
+// Material sort of the hit queue (optional, chosen by the tuner): a counting
+// sort by material index so that the lanes of a shade warp mostly share one
+// material record and one closure branch. Histogram in shared memory per
+// block, one exclusive scan, then a scatter with one atomic per (warp,
+// material). The order inside a material is arbitrary; each path's result
+// does not depend on it.
+constexpr uint32_t kSortSmemBins = 8192;
+
+__global__ void __launch_bounds__(256) sort_histogram_kernel(SceneView s, FrameView f, SortView sv, uint32_t bounce)
+{
+    __shared__ uint32_t hist[kSortSmemBins];
+    const bool local = sv.bins <= kSortSmemBins;
+    if (local) {
+        for (uint32_t b = threadIdx.x; b < sv.bins; b += blockDim.x)
+            hist[b] = 0u;
+        __syncthreads();
+    }
+    const uint32_t count = __ldcg(f.counters + kHitCounterBase + bounce);
+    for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < count; i += gridDim.x * blockDim.x) {
+        const uint32_t key = __ldg(s.matIdx + f.hits[i].z);
+        sv.keys[i] = key;
+        if (local)
+            atomicAdd(&hist[key], 1u);
+        else
+            atomicAdd(sv.counts + key, 1u);
+    }
+    if (local) {
+        __syncthreads();
+        for (uint32_t b = threadIdx.x; b < sv.bins; b += blockDim.x)
+            if (hist[b])
+                atomicAdd(sv.counts + b, hist[b]);
+    }
+}
+
+// Exclusive scan of the counts into the cursors (one block), counts zeroed for
+// the next bounce.
+__global__ void __launch_bounds__(1024) sort_scan_kernel(SortView sv)
+{
+    __shared__ uint32_t warpSums[32];
+    __shared__ uint32_t carry;
+    if (threadIdx.x == 0)
+        carry = 0u;
+    __syncthreads();
+    const uint32_t lane = lane_id(), warp = threadIdx.x >> 5;
+    for (uint32_t base = 0; base < sv.bins; base += blockDim.x) {
+        const uint32_t b = base + threadIdx.x;
+        const uint32_t v = b < sv.bins ? sv.counts[b] : 0u;
+        uint32_t x = v;
+        for (int o = 1; o < 32; o <<= 1) {
+            const uint32_t y = __shfl_up_sync(kFull, x, o);
+            if (lane >= uint32_t(o))
+                x += y;
+        }
+        if (lane == 31)
+            warpSums[warp] = x;
+        __syncthreads();
+        if (warp == 0) {
+            uint32_t w = warpSums[lane];
+            for (int o = 1; o < 32; o <<= 1) {
+                const uint32_t y = __shfl_up_sync(kFull, w, o);
+                if (lane >= uint32_t(o))
+                    w += y;
+            }
+            warpSums[lane] = w;
+        }
+        __syncthreads();
+        const uint32_t prefix = carry + (warp ? warpSums[warp - 1] : 0u) + x - v;
+        if (b < sv.bins) {
+            sv.cursor[b] = prefix;
+            sv.counts[b] = 0u;
+        }
+        __syncthreads();
+        if (threadIdx.x == blockDim.x - 1)
+            carry = prefix + v;
+        __syncthreads();
+    }
+}
+
+__global__ void __launch_bounds__(256) sort_scatter_kernel(FrameView f, SortView sv, uint32_t bounce)
+{
+    const uint32_t count = __ldcg(f.counters + kHitCounterBase + bounce);
+    const uint32_t lane = lane_id();
+    for (uint32_t base = (blockIdx.x * blockDim.x + threadIdx.x) & ~31u; base < count;
+         base += gridDim.x * blockDim.x) {
+        const uint32_t i = base + lane;
+        const uint32_t key = i < count ? sv.keys[i] : 0xffffffffu;
+        const uint32_t peers = __match_any_sync(kFull, key);
+        const uint32_t leader = __ffs(peers) - 1u;
+        uint32_t pos = 0;
+        if (lane == leader && key != 0xffffffffu)
+            pos = atomicAdd(sv.cursor + key, __popc(peers));
+        pos = __shfl_sync(kFull, pos, leader);
+        if (key != 0xffffffffu)
+            sv.order[pos + __popc(peers & ((1u << lane) - 1u))] = i;
     }
 }
 
@@ -1370,6 +1468,16 @@ cudaError_t launch_adjoint(const SceneView& s, const FrameView& f, const Camera&
     return cudaGetLastError();
 }
 
+cudaError_t launch_sort_hits(const SceneView& s, const FrameView& f, const SortView& sv, uint32_t bounce,
+                             const LaunchShape& shape, cudaStream_t stream)
+{
+    const uint32_t blocks = shape.sms * 4u;
+    sort_histogram_kernel<<<blocks, 256, 0, stream>>>(s, f, sv, bounce);
+    sort_scan_kernel<<<1, 1024, 0, stream>>>(sv);
+    sort_scatter_kernel<<<blocks, 256, 0, stream>>>(f, sv, bounce);
+    return cudaGetLastError();
+}
+
 cudaError_t launch_batch_finalize(const FrameView& f, uint32_t wavePixels, cudaStream_t stream)
 {
     if (wavePixels == 0)
@@ -1421,6 +1529,7 @@ LaunchShape tuned_launch_shape(int device, uint32_t capacity, const tr_tuning& t
         shape.extendBlocks = shape.sms * t.extend_blocks_per_sm;
     if (t.connect_blocks_per_sm >= 1 && t.connect_blocks_per_sm <= shape.connectPerSm)
         shape.connectBlocks = shape.sms * t.connect_blocks_per_sm;
+    shape.sortHits = t.sort_hits ? 1u : 0u;
     if (t.shade_waves >= 1 && t.shade_waves <= 64) {
         int perSm = 0;
         cudaOccupancyMaxActiveBlocksPerMultiprocessor(&perSm, shade_kernel<false, false>, 128, 0);

@@ -20,6 +20,7 @@ struct LaunchShape {
     uint32_t extendPerSm = 0;    // resident extend / connect blocks per SM (occupancy limit by default)
     uint32_t connectPerSm = 0;
     uint32_t shadeWaves = 4;     // shade grid cap, in waves of resident blocks
+    uint32_t sortHits = 0;       // 1: counting sort of each bounce's hit queue by material before shade
 };
 
 LaunchShape default_launch_shape(int device, uint32_t capacity);
@@ -36,6 +37,10 @@ cudaError_t launch_shade(const SceneView& s, const FrameView& f, const Settings&
 cudaError_t launch_connect(const SceneView& s, const FrameView& f, const Settings& st, uint32_t bounce,
                            const LaunchShape& shape, cudaStream_t stream);
 cudaError_t launch_finalize(const FrameView& f, const Settings& st, cudaStream_t stream);
+// Counting sort of the bounce's hit queue by material into sv.order (shade
+// reads the queue through it when FrameView::hitOrder = sv.order).
+cudaError_t launch_sort_hits(const SceneView& s, const FrameView& f, const SortView& sv, uint32_t bounce,
+                             const LaunchShape& shape, cudaStream_t stream);
 // Batched rendering: adds a wave's samples to the batch accumulator; then
 // colors = accumulator / samples over all batch pixels.
 cudaError_t launch_batch_finalize(const FrameView& f, uint32_t wavePixels, cudaStream_t stream);
