@@ -360,7 +360,7 @@ tr_status tr_autotune(void* ctx, void* stream, uint32_t flags, tr_tune_report* r
  * the per-stage kernels are the ones behind tr_extend / tr_shade /
  * tr_connect. Each item's scene gets its own BVH; the buffers are
  * concatenated on the device and all items' paths run through the same
- * launches in waves of at most wave_paths paths (0: 2^26), made of
+ * launches in waves of at most wave_paths paths (0: 2^25), made of
  * consecutive (item, sample) units. A path's random numbers are keyed as in
  * tr_render_frame (pixel, sample, bounce, seed), so an item whose samples fit
  * in one wave renders the image tr_render_frame gives for that scene with

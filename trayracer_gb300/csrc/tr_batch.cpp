@@ -10,8 +10,10 @@
 // most `wave_paths` paths made of consecutive (item, sample) units; each wave
 // runs the same generate / extend / shade / connect launches as one scene,
 // with the item of a path looked up from the wave's segment table, and adds
-// its samples to the batch accumulator. One tr_batch_render replays all waves
-// from one CUDA graph.
+// its samples to the batch accumulator. Two waves are in flight at a time, on
+// two streams with their own buffers, so one wave's short late bounces overlap
+// the other wave's long early ones; only the waves' accumulator updates are
+// ordered. One tr_batch_render replays all waves from one CUDA graph.
 #include <cuda_runtime.h>
 
 #include <algorithm>
@@ -33,7 +35,8 @@ namespace {
 
 using namespace tr;
 
-constexpr uint64_t kDefaultWavePaths = 1ull << 26;
+constexpr uint64_t kDefaultWavePaths = 1ull << 25;
+constexpr uint32_t kWaveSets = 2;  // waves in flight, each with its own buffers and stream
 
 struct Wave {
     uint32_t segmentOffset = 0;
@@ -57,7 +60,10 @@ struct Batch {
     void* sceneArena = nullptr;
     void* frameArena = nullptr;
     SceneView scene{};
-    FrameView frame{};               // shared by the waves; segments, counts and counters set per wave
+    FrameView frame[kWaveSets]{};    // wave buffers of each set; segments, counts and counters set per wave
+    cudaStream_t lanes[kWaveSets] = {};
+    cudaEvent_t evFork = nullptr;
+    std::vector<cudaEvent_t> evFinal; // per wave: its samples are in the accumulator
     std::vector<Wave> waves;
     std::vector<BatchItem> items;
     BatchSegment* segments = nullptr;
@@ -119,6 +125,14 @@ void release(Batch* b)
         cudaFree(b->sceneArena);
     if (b->frameArena)
         cudaFree(b->frameArena);
+    for (cudaEvent_t e : b->evFinal)
+        if (e)
+            cudaEventDestroy(e);
+    if (b->evFork)
+        cudaEventDestroy(b->evFork);
+    for (cudaStream_t l : b->lanes)
+        if (l)
+            cudaStreamDestroy(l);
     if (b->stream)
         cudaStreamDestroy(b->stream);
 }
@@ -199,7 +213,7 @@ void plan_waves(const std::vector<BatchItem>& items, uint64_t cap, std::vector<W
 
 FrameView wave_view(const Batch* b, uint32_t w)
 {
-    FrameView f = b->frame;
+    FrameView f = b->frame[w % kWaveSets];
     const Wave& wv = b->waves[w];
     f.segments = b->segments + wv.segmentOffset;
     f.segmentCount = wv.segmentCount;
@@ -214,19 +228,36 @@ cudaError_t enqueue(Batch* b, const Settings& st, cudaStream_t s)
     if (e == cudaSuccess)
         e = cudaMemsetAsync(b->counters, 0, b->waves.size() * kCounterWords * sizeof(uint32_t), s);
     const Camera noCamera{};  // each path uses its item's camera
+    if (e == cudaSuccess)
+        e = cudaEventRecord(b->evFork, s);
+    for (uint32_t k = 0; e == cudaSuccess && k < kWaveSets; ++k)
+        e = cudaStreamWaitEvent(b->lanes[k], b->evFork, 0);
     for (uint32_t w = 0; e == cudaSuccess && w < b->waves.size(); ++w) {
+        // a set's stream runs its waves in order, so a wave reuses the buffers of the
+        // wave two before it only after that one finished
+        cudaStream_t ls = b->lanes[w % kWaveSets];
         const FrameView f = wave_view(b, w);
         // the camera rays are made inside the first extend launch
         for (uint32_t bounce = 0; e == cudaSuccess && bounce < st.maxDepth; ++bounce) {
-            e = launch_extend(b->scene, f, st, bounce, b->shape, s, &noCamera);
+            e = launch_extend(b->scene, f, st, bounce, b->shape, ls, &noCamera);
             if (e == cudaSuccess)
-                e = launch_shade(b->scene, f, st, bounce, b->shape, s);
+                e = launch_shade(b->scene, f, st, bounce, b->shape, ls);
             if (e == cudaSuccess)
-                e = launch_connect(b->scene, f, st, bounce, b->shape, s);
+                e = launch_connect(b->scene, f, st, bounce, b->shape, ls);
         }
+        // accumulator updates in wave order: an item split over two waves adds to the same pixels
+        if (e == cudaSuccess && w > 0)
+            e = cudaStreamWaitEvent(ls, b->evFinal[w - 1], 0);
         if (e == cudaSuccess)
-            e = launch_batch_finalize(f, b->waves[w].pixels, s);
+            e = launch_batch_finalize(f, b->waves[w].pixels, ls);
+        if (e == cudaSuccess)
+            e = cudaEventRecord(b->evFinal[w], ls);
     }
+    // the last wave's accumulator update follows every earlier one and its own wave
+    if (e == cudaSuccess && !b->waves.empty())
+        e = cudaStreamWaitEvent(s, b->evFinal[b->waves.size() - 1], 0);
+    for (uint32_t k = 1; e == cudaSuccess && k < kWaveSets && k < b->waves.size(); ++k)
+        e = cudaStreamWaitEvent(s, b->evFinal[b->waves.size() - 1 - k], 0);
     if (e == cudaSuccess)
         e = launch_batch_resolve(b->accumulator, b->colors, uint32_t(b->info.pixel_count), s);
     return e;
@@ -275,8 +306,12 @@ tr_status tr_batch_create(const tr_config* config, const tr_batch_item* items, u
     };
     // a blocking stream, like the context's: work on it is ordered with the legacy default stream
     if (cudaStreamCreate(&b->stream) != cudaSuccess ||
-        cudaEventCreate(&b->evStart) != cudaSuccess || cudaEventCreate(&b->evStop) != cudaSuccess)
+        cudaEventCreate(&b->evStart) != cudaSuccess || cudaEventCreate(&b->evStop) != cudaSuccess ||
+        cudaEventCreateWithFlags(&b->evFork, cudaEventDisableTiming) != cudaSuccess)
         return bail(TR_ERR_CUDA);
+    for (uint32_t k = 0; k < kWaveSets; ++k)
+        if (cudaStreamCreateWithFlags(&b->lanes[k], cudaStreamNonBlocking) != cudaSuccess)
+            return bail(TR_ERR_CUDA);
 
     const auto t0 = std::chrono::steady_clock::now();
     std::vector<ItemBuild> built = build_items(items, count, 3u);
@@ -407,11 +442,15 @@ tr_status tr_batch_create(const tr_config* config, const tr_batch_item* items, u
         capPaths = std::max(capPaths, w.paths);
     const size_t capN = capPaths;
     off = 0;
-    const size_t oS0 = take(3 * capN * sizeof(float4));
-    const size_t oS1 = take(3 * capN * sizeof(float4));
-    const size_t oHits = take(capN * sizeof(uint4));
-    const size_t oShadow = take(3 * capN * sizeof(float4));
-    const size_t oRad = take(capN * sizeof(float4));
+    size_t oS0[kWaveSets], oS1[kWaveSets], oHits[kWaveSets], oShadow[kWaveSets], oRad[kWaveSets];
+    const uint32_t sets = uint32_t(std::min<size_t>(kWaveSets, waves.size()));
+    for (uint32_t k = 0; k < sets; ++k) {
+        oS0[k] = take(3 * capN * sizeof(float4));
+        oS1[k] = take(3 * capN * sizeof(float4));
+        oHits[k] = take(capN * sizeof(uint4));
+        oShadow[k] = take(3 * capN * sizeof(float4));
+        oRad[k] = take(capN * sizeof(float4));
+    }
     const size_t oAcc = take(pixels * sizeof(float4));
     const size_t oCol = take(pixels * sizeof(float4));
     const size_t oCnt = take(waves.size() * kCounterWords * sizeof(uint32_t));
@@ -431,13 +470,7 @@ tr_status tr_batch_create(const tr_config* config, const tr_batch_item* items, u
         cudaMemcpy(fb + oItems, b->items.data(), b->items.size() * sizeof(BatchItem), cudaMemcpyHostToDevice) !=
             cudaSuccess)
         return bail(TR_ERR_CUDA);
-    FrameView& f = b->frame;
-    f = FrameView{};
-    f.state[0] = reinterpret_cast<float4*>(fb + oS0);
-    f.state[1] = reinterpret_cast<float4*>(fb + oS1);
-    f.hits = reinterpret_cast<uint4*>(fb + oHits);
-    f.shadow = reinterpret_cast<float4*>(fb + oShadow);
-    f.radiance = reinterpret_cast<float4*>(fb + oRad);
+    FrameView f{};
     f.accumulator = reinterpret_cast<float4*>(fb + oAcc);
     f.colors = reinterpret_cast<float4*>(fb + oCol);
     f.albedo = nullptr;
@@ -449,6 +482,19 @@ tr_status tr_batch_create(const tr_config* config, const tr_batch_item* items, u
     f.resX = 1;
     f.resY = 1;
     f.items = reinterpret_cast<const BatchItem*>(fb + oItems);
+    for (uint32_t k = 0; k < kWaveSets; ++k) {
+        const uint32_t j = k < sets ? k : 0u;
+        b->frame[k] = f;
+        b->frame[k].state[0] = reinterpret_cast<float4*>(fb + oS0[j]);
+        b->frame[k].state[1] = reinterpret_cast<float4*>(fb + oS1[j]);
+        b->frame[k].hits = reinterpret_cast<uint4*>(fb + oHits[j]);
+        b->frame[k].shadow = reinterpret_cast<float4*>(fb + oShadow[j]);
+        b->frame[k].radiance = reinterpret_cast<float4*>(fb + oRad[j]);
+    }
+    b->evFinal.assign(waves.size(), nullptr);
+    for (cudaEvent_t& ev : b->evFinal)
+        if (cudaEventCreateWithFlags(&ev, cudaEventDisableTiming) != cudaSuccess)
+            return bail(TR_ERR_CUDA);
     b->segments = reinterpret_cast<BatchSegment*>(fb + oSeg);
     b->counters = reinterpret_cast<uint32_t*>(fb + oCnt);
     b->accumulator = f.accumulator;
@@ -541,7 +587,7 @@ tr_status tr_batch_render(void* batch, void* stream, const tr_kernel_settings* s
         TR_BCUDA(b, cudaGraphLaunch(b->graphExec, s));
     } else {
         if (st.flags & TR_FLAG_COUNT_TRAVERSAL)
-            TR_BCUDA(b, cudaMemsetAsync(b->frame.traversal, 0, 4 * sizeof(unsigned long long), s));
+            TR_BCUDA(b, cudaMemsetAsync(b->frame[0].traversal, 0, 4 * sizeof(unsigned long long), s));
         TR_BCUDA(b, enqueue(b, st, s));
     }
     TR_BCUDA(b, cudaEventRecord(b->evStop, s));
@@ -563,8 +609,8 @@ tr_status tr_batch_get_statistics(void* batch, tr_batch_statistics* out)
     TR_BCUDA(b, cudaMemcpy(cnt.data(), b->counters, cnt.size() * sizeof(uint32_t), cudaMemcpyDeviceToHost));
     uint32_t err = 0;
     unsigned long long trav[4] = {0, 0, 0, 0};
-    TR_BCUDA(b, cudaMemcpy(&err, b->frame.errorFlag, sizeof(uint32_t), cudaMemcpyDeviceToHost));
-    TR_BCUDA(b, cudaMemcpy(trav, b->frame.traversal, sizeof(trav), cudaMemcpyDeviceToHost));
+    TR_BCUDA(b, cudaMemcpy(&err, b->frame[0].errorFlag, sizeof(uint32_t), cudaMemcpyDeviceToHost));
+    TR_BCUDA(b, cudaMemcpy(trav, b->frame[0].traversal, sizeof(trav), cudaMemcpyDeviceToHost));
     tr_batch_statistics s{};
     for (size_t w = 0; w < b->waves.size(); ++w) {
         const uint32_t* c = cnt.data() + w * kCounterWords;
