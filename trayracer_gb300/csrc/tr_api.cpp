@@ -667,7 +667,7 @@ tr_status tr_adjoint_frame(void* ctx, void* stream, const float* pixel_grad, flo
     cudaSetDevice(c->device);
     const size_t cap = c->frame.capacity;
     if (!c->adjointArena.base) {
-        // lrem 16 B + pending 80 B + NEE payload 32 B + visible slot 4 B per path, and the counters
+        // lrem 16 B + pending 32 B + NEE payload 32 B + visible slot 4 B per path, and the counters
         size_t off = 0;
         auto take = [&](size_t bytes) {
             const size_t o = off;
@@ -675,7 +675,7 @@ tr_status tr_adjoint_frame(void* ctx, void* stream, const float* pixel_grad, flo
             return o;
         };
         const size_t oL = take(cap * sizeof(float4));
-        const size_t oP = take(5 * cap * sizeof(float4));
+        const size_t oP = take(2 * cap * sizeof(float4));
         const size_t oS = take(2 * cap * sizeof(float4));
         const size_t oV = take(cap * sizeof(uint32_t));
         const size_t oC = take(kCounterWords * sizeof(uint32_t));

@@ -179,7 +179,7 @@ struct BatchItem {
 // stride = the frame's capacity).
 struct AdjointView {
     float4* lrem;          // radiance of the path not yet accounted for
-    float4* pending;       // 5 planes: d log f_c / d theta_k of the last extend direction (18 floats, c-major), key
+    float4* pending;       // 2 planes: (wo, bits(matIx) or ~0), (wi) of the path's last extend direction
     float4* shadowAdj;     // 2 planes by shadow slot: (wo, bits(matIx)), (wiLight, bits(lightIx))
     uint32_t* visible;     // shadow slots found unoccluded
     const float4* pixelGrad;

@@ -1082,8 +1082,9 @@ __device__ __forceinline__ void add_log_derivative(float (&g)[kGradSlots], const
 // contribution, for the extend direction everything the path collected after
 // the vertex. The latter is the path's total (the forward frame's per-path
 // radiance) minus what was accounted for up to the vertex, so it is known
-// when the path reaches its next vertex: the extend direction's d log f is
-// kept per path (pending) and applied by the next adjoint shade.
+// when the path reaches its next vertex: the extend direction (wo, wi,
+// material) is kept per path (pending) and its d log f is evaluated and
+// weighted by ext_grad_kernel when the path's next hit is known.
 __global__ void __launch_bounds__(256) adjoint_generate_kernel(FrameView f, Camera cam, Settings st, AdjointView a)
 {
     const uint32_t pathIx = blockIdx.x * blockDim.x + threadIdx.x;
@@ -1103,15 +1104,59 @@ __global__ void __launch_bounds__(256) adjoint_generate_kernel(FrameView f, Came
     s[pathIx + cap] = f4(D, 0.f);
     s[pathIx + 2 * cap] = make_float4(T, T, T, 1.f);
     a.lrem[pathIx] = f.radiance[pathIx];
-    a.pending[pathIx + 4 * cap] = make_float4(0.f, 0.f, __uint_as_float(0xffffffffu), 0.f);
+    a.pending[pathIx] = make_float4(0.f, 0.f, 0.f, __uint_as_float(0xffffffffu));
 }
 
-// Shade of the replay over the hit queue: applies the pending extend-direction
-// gradient of the previous vertex, the emission gradients of an emissive hit,
-// and queues the NEE ray (with what the NEE gradient needs) and the extend ray
-// (with the new pending d log f) like the forward shade.
+// Gradient of the previous vertex's extend direction, for the paths of the
+// bounce's hit queue (launched after extend, before adjoint_shade_kernel
+// takes this vertex's emission off the remaining radiance): the radiance
+// still unaccounted for arrived through that direction.
 template <bool SMEM>
-__global__ void __launch_bounds__(kAdjointThreads) adjoint_shade_kernel(SceneView s, FrameView f, Settings st,
+__global__ void __launch_bounds__(kAdjointThreads) ext_grad_kernel(SceneView s, FrameView f, uint32_t bounce,
+                                                                   AdjointView a)
+{
+    extern __shared__ float sgrad[];
+    float* table = grad_table_begin<SMEM>(sgrad, a);
+    const uint32_t count = __ldcg(f.counters + kHitCounterBase + bounce);
+    const float4* __restrict__ in = f.state[1];
+    const uint32_t cap = f.capacity;
+    const uint32_t warpGlobal = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+    const uint32_t warpStride = (gridDim.x * blockDim.x) >> 5;
+    for (uint32_t base = warpGlobal * 32u; base < count; base += warpStride * 32u) {
+        const uint32_t i = base + lane_id();
+        float g[kGradSlots];
+#pragma unroll
+        for (int k = 0; k < kGradSlots; ++k)
+            g[k] = 0.f;
+        uint32_t key = 0xffffffffu;
+        if (i < count) {
+            const uint32_t pathIx = path_ix(__float_as_uint(__ldg(in + i).w));
+            const float4 wo4 = a.pending[pathIx];
+            const uint32_t matIx = __float_as_uint(wo4.w);
+            if (matIx != 0xffffffffu) {
+                const float3 delta = path_delta(f, a, pathIx);
+                const float3 lrem = f3(a.lrem[pathIx]);
+                const float3 w = make_float3(delta.x * lrem.x, delta.y * lrem.y, delta.z * lrem.z);
+                if (w.x != 0.f || w.y != 0.f || w.z != 0.f) {
+                    const float4 wi4 = a.pending[pathIx + cap];
+                    uint32_t closure, emissiveFlag;
+                    const HitMat m = load_material(s.materials, matIx, closure, emissiveFlag);
+                    add_log_derivative(g, dual::closure_value(closure, m, f3(wo4), f3(wi4)), w);
+                    key = matIx;
+                }
+            }
+        }
+        warp_add_grads<SMEM>(table, key, g, 0, kGradParams);
+    }
+    grad_table_end<SMEM>(sgrad, a);
+}
+
+// Shade of the replay over the hit queue: the emission gradients of an
+// emissive hit; queues the NEE ray (with what the NEE gradient needs) and the
+// extend ray (with its direction kept as the path's pending record) like the
+// forward shade.
+template <bool SMEM>
+__global__ void __launch_bounds__(kAdjointThreads, 4) adjoint_shade_kernel(SceneView s, FrameView f, Settings st,
                                                                         uint32_t bounce, AdjointView a)
 {
     extern __shared__ float sgrad[];
@@ -1130,11 +1175,11 @@ __global__ void __launch_bounds__(kAdjointThreads) adjoint_shade_kernel(SceneVie
         const uint32_t i = base + lane_id();
         bool wantExt = false, wantShadow = false;
         float4 ext[3], sh[3];
-        float g[kGradSlots], ge[kGradSlots], gp[kGradSlots];
+        float g[kGradSlots], ge[kGradSlots];
 #pragma unroll
         for (int k = 0; k < kGradSlots; ++k)
-            g[k] = ge[k] = gp[k] = 0.f;
-        uint32_t key = 0xffffffffu, keyE = 0xffffffffu, keyP = 0xffffffffu;
+            g[k] = ge[k] = 0.f;
+        uint32_t key = 0xffffffffu, keyE = 0xffffffffu;
         uint32_t pathIx = 0;
         VertexInfo vi;
         vi.hit = false;
@@ -1146,21 +1191,6 @@ __global__ void __launch_bounds__(kAdjointThreads) adjoint_shade_kernel(SceneVie
             pathIx = path_ix(__float_as_uint(O4.w));
             const float3 delta = path_delta(f, a, pathIx);
             float3 lrem = f3(a.lrem[pathIx]);
-            // the previous vertex's extend direction carried everything still unaccounted for
-            const float4 p4 = a.pending[pathIx + 4 * cap];
-            keyP = __float_as_uint(p4.z);
-            if (keyP != 0xffffffffu) {
-                const float4 p0 = a.pending[pathIx], p1 = a.pending[pathIx + cap];
-                const float4 p2 = a.pending[pathIx + 2 * cap], p3 = a.pending[pathIx + 3 * cap];
-                const float dl[18] = {p0.x, p0.y, p0.z, p0.w, p1.x, p1.y, p1.z, p1.w, p2.x,
-                                      p2.y, p2.z, p2.w, p3.x, p3.y, p3.z, p3.w, p4.x, p4.y};
-                const float w[3] = {delta.x * lrem.x, delta.y * lrem.y, delta.z * lrem.z};
-#pragma unroll
-                for (int c = 0; c < 3; ++c)
-#pragma unroll
-                    for (int k = 0; k < kGradParams; ++k)
-                        gp[k] += w[c] * dl[c * kGradParams + k];
-            }
             const bool live = (delta.x != 0.f || delta.y != 0.f || delta.z != 0.f) &&
                               (lrem.x != 0.f || lrem.y != 0.f || lrem.z != 0.f);
             if (live) {
@@ -1185,22 +1215,9 @@ __global__ void __launch_bounds__(kAdjointThreads) adjoint_shade_kernel(SceneVie
                 lrem = lrem - vi.emitted;
                 a.lrem[pathIx] = f4(lrem, 0.f);
             } else if (vi.hit && wantExt) {
-                // d log f of the extend direction, applied at the path's next vertex
-                const Vec3<Dual> fv = dual::closure_value(vi.closure, vi.mat, vi.wo, vi.wiExt);
-                const Dual* fc[3] = {&fv.x, &fv.y, &fv.z};
-                float dl[18];
-#pragma unroll
-                for (int c = 0; c < 3; ++c) {
-                    const float r = fc[c]->v != 0.f ? 1.0f / fc[c]->v : 0.f;
-#pragma unroll
-                    for (int k = 0; k < kGradParams; ++k)
-                        dl[c * kGradParams + k] = fc[c]->d[k] * r;
-                }
-                a.pending[pathIx] = make_float4(dl[0], dl[1], dl[2], dl[3]);
-                a.pending[pathIx + cap] = make_float4(dl[4], dl[5], dl[6], dl[7]);
-                a.pending[pathIx + 2 * cap] = make_float4(dl[8], dl[9], dl[10], dl[11]);
-                a.pending[pathIx + 3 * cap] = make_float4(dl[12], dl[13], dl[14], dl[15]);
-                a.pending[pathIx + 4 * cap] = make_float4(dl[16], dl[17], __uint_as_float(vi.matIx), 0.f);
+                // the extend direction, weighted when the path's next vertex is known
+                a.pending[pathIx] = f4(vi.wo, __uint_as_float(vi.matIx));
+                a.pending[pathIx + cap] = f4(vi.wiExt, 0.f);
             }
         }
         if (vi.emissive)
@@ -1219,7 +1236,6 @@ __global__ void __launch_bounds__(kAdjointThreads) adjoint_shade_kernel(SceneVie
             __stcs(out + exSlot + cap, ext[1]);
             __stcs(out + exSlot + 2 * cap, ext[2]);
         }
-        warp_add_grads<SMEM>(table, keyP, gp, 0, kGradParams);
         warp_add_grads<SMEM>(table, key, g, 0, kGradParams);
         warp_add_grads<SMEM>(table, keyE, ge, kGEmR, kGradSlots);
     }
@@ -1455,6 +1471,12 @@ cudaError_t launch_adjoint(const SceneView& s, const FrameView& f, const Camera&
     adjoint_generate_kernel<<<(f.pathCount + 255u) / 256u, 256, 0, stream>>>(f, cam, fwd, a);
     for (uint32_t bounce = 0; bounce < st.maxDepth; ++bounce) {
         extend_kernel<false, false, false><<<shape.extendBlocks, 128, 0, stream>>>(s, f, fwd, bounce, Camera{});
+        if (bounce > 0) {
+            if (useSmem)
+                ext_grad_kernel<true><<<gradBlocks, kAdjointThreads, smem, stream>>>(s, f, bounce, a);
+            else
+                ext_grad_kernel<false><<<gradBlocks, kAdjointThreads, 0, stream>>>(s, f, bounce, a);
+        }
         if (useSmem)
             adjoint_shade_kernel<true><<<gradBlocks, kAdjointThreads, smem, stream>>>(s, f, fwd, bounce, a);
         else
