@@ -158,6 +158,53 @@ TR_HD float byte_to_float(uint32_t w, int i)
 #endif
 }
 
+#ifdef __CUDA_ARCH__
+// Packed fp32 pairs (sm_100 and later): lane 0 in the low word.
+__device__ __forceinline__ unsigned long long pack2(float lo, float hi)
+{
+    unsigned long long d;
+    asm("mov.b64 %0, {%1, %2};" : "=l"(d) : "f"(lo), "f"(hi));
+    return d;
+}
+__device__ __forceinline__ void unpack2(unsigned long long v, float& lo, float& hi)
+{
+    asm("mov.b64 {%0, %1}, %2;" : "=f"(lo), "=f"(hi) : "l"(v));
+}
+__device__ __forceinline__ unsigned long long fma2(unsigned long long a, unsigned long long b, unsigned long long c)
+{
+    unsigned long long d;
+    asm("fma.rn.f32x2 %0, %1, %2, %3;" : "=l"(d) : "l"(a), "l"(b), "l"(c));
+    return d;
+}
+__device__ __forceinline__ unsigned long long add2(unsigned long long a, unsigned long long b)
+{
+    unsigned long long d;
+    asm("add.rn.f32x2 %0, %1, %2;" : "=l"(d) : "l"(a), "l"(b));
+    return d;
+}
+// Byte j of lo and of hi, each placed in the low mantissa bits of 2^23.
+__device__ __forceinline__ unsigned long long byte_pair(uint32_t lo, uint32_t hi, int j)
+{
+    const uint32_t a = __byte_perm(lo, 0x4B00u, 0x5440u | uint32_t(j));
+    const uint32_t b = __byte_perm(hi, 0x4B00u, 0x5440u | uint32_t(j));
+    unsigned long long d;
+    asm("mov.b64 %0, {%1, %2};" : "=l"(d) : "r"(a), "r"(b));
+    return d;
+}
+__device__ __forceinline__ float max3(float a, float b, float c)
+{
+    float d;
+    asm("max.f32 %0, %1, %2, %3;" : "=f"(d) : "f"(a), "f"(b), "f"(c));
+    return d;
+}
+__device__ __forceinline__ float min3(float a, float b, float c)
+{
+    float d;
+    asm("min.f32 %0, %1, %2, %3;" : "=f"(d) : "f"(a), "f"(b), "f"(c));
+    return d;
+}
+#endif
+
 // Intersects the 8 children of a node; returns the hit mask: bits 24..31 for
 // internal children (position 24 + (slot ^ (7 - octant))), bits 0..23 for
 // leaf triangles (offset from the node's triangle base).
@@ -183,6 +230,11 @@ TR_HD uint32_t intersect_node(const CwbvhNode* __restrict__ nodes, uint32_t node
 
     const float ax = sx * invD.x, ay = sy * invD.y, az = sz * invD.z;
     const float bx = (px - O.x) * invD.x, by = (py - O.y) * invD.y, bz = (pz - O.z) * invD.z;
+#ifdef __CUDA_ARCH__
+    const unsigned long long ax2 = pack2(ax, ax), ay2 = pack2(ay, ay), az2 = pack2(az, az);
+    const unsigned long long bx2 = pack2(bx, bx), by2 = pack2(by, by), bz2 = pack2(bz, bz);
+    const unsigned long long kMinus2p23x2 = pack2(-8388608.0f, -8388608.0f);
+#endif
 
     // octant swizzle: the near plane is qhi on axes the ray walks backwards
     const bool nx = invD.x < 0.f, ny = invD.y < 0.f, nz = invD.z < 0.f;
@@ -210,6 +262,16 @@ TR_HD uint32_t intersect_node(const CwbvhNode* __restrict__ nodes, uint32_t node
         const uint32_t lz = half == 0 ? loZ0 : loZ1, hz = half == 0 ? hiZ0 : hiZ1;
 #pragma unroll
         for (int j = 0; j < 4; ++j) {
+#ifdef __CUDA_ARCH__
+            // near and far plane of an axis as one packed pair: two byte permutes, one
+            // packed add, one packed FMA (each lane rounds as the scalar fma_rn does)
+            float t0x, t1x, t0y, t1y, t0z, t1z;
+            unpack2(fma2(add2(byte_pair(lx, hx, j), kMinus2p23x2), ax2, bx2), t0x, t1x);
+            unpack2(fma2(add2(byte_pair(ly, hy, j), kMinus2p23x2), ay2, by2), t0y, t1y);
+            unpack2(fma2(add2(byte_pair(lz, hz, j), kMinus2p23x2), az2, bz2), t0z, t1z);
+            const float tn = max3(t0x, t0y, fmaxf(t0z, tmin));
+            const float tf = min3(t1x, t1y, fminf(t1z, tmax));
+#else
             const float t0x = fma_rn(byte_to_float(lx, j), ax, bx);
             const float t1x = fma_rn(byte_to_float(hx, j), ax, bx);
             const float t0y = fma_rn(byte_to_float(ly, j), ay, by);
@@ -218,6 +280,7 @@ TR_HD uint32_t intersect_node(const CwbvhNode* __restrict__ nodes, uint32_t node
             const float t1z = fma_rn(byte_to_float(hz, j), az, bz);
             const float tn = fmaxf(fmaxf(t0x, t0y), fmaxf(t0z, tmin));
             const float tf = fminf(fminf(t1x, t1y), fminf(t1z, tmax));
+#endif
             if (tn <= tf * 1.0000004f)
                 hitmask |= ((childBits4 >> (8 * j)) & 7u) << ((bitIndex4 >> (8 * j)) & 31u);
         }
