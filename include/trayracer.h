@@ -165,12 +165,27 @@ typedef struct tr_mesh_desc {
     const uint32_t* material_indices; /* triangle_count entries into the scene material list */
 } tr_mesh_desc;
 
+/* One placement of a mesh (≙ Instance: OptixInstance::transform, instanceId;
+ * Tracer/Resources/Instance.cpp:39-49). */
+typedef struct tr_instance_desc {
+    uint32_t mesh;                 /* index into tr_scene_desc.meshes */
+    uint32_t reserved;
+    float transform[12];           /* object -> world, 3 rows (r.x, r.y, r.z, t) as OptixInstance::transform */
+} tr_instance_desc;
+
 typedef struct tr_scene_desc {
-    const tr_mesh_desc* mesh;      /* one mesh, one identity instance */
+    const tr_mesh_desc* mesh;      /* one mesh, one identity instance (when instance_count == 0) */
     const tr_material_desc* materials;
     uint32_t material_count;
     uint32_t bvh_leaf_size;        /* 1..3 triangles per leaf, 0 = default (3) */
     uint32_t build_threads;        /* host threads for the BVH build, 0 = all */
+    uint32_t instance_count;       /* > 0: two-level scene, instances[] place meshes[] */
+    /* two-level scenes (≙ Scene::Instances / Models, Renderer::UploadGeometry,
+     * Renderer.cpp:442-505): one BVH per mesh, one over the instances */
+    const tr_mesh_desc* meshes;
+    const uint32_t* mesh_material_offsets; /* per mesh, added to its material indices (≙ MaterialOffsets); NULL = 0 */
+    const tr_instance_desc* instances;
+    uint32_t mesh_count;
     uint32_t reserved;
 } tr_scene_desc;
 
@@ -399,8 +414,9 @@ typedef struct tr_batch_statistics {
     uint64_t traversal_connect_tris;
 } tr_batch_statistics;
 
-/* Builds and uploads all items (host threads build the BVHs). TR_ERR_LIMIT
- * when an item's width * height exceeds wave_paths. */
+/* Builds and uploads all items (host threads build the BVHs). Items are
+ * one-mesh scenes (instance_count 0). TR_ERR_LIMIT when an item's width *
+ * height exceeds wave_paths. */
 tr_status tr_batch_create(const tr_config* config, const tr_batch_item* items, uint32_t count, uint64_t wave_paths,
                           void** out_batch);
 tr_status tr_batch_destroy(void* batch);

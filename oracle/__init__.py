@@ -54,9 +54,9 @@ class Oracle:
             lib.orc_generate.argtypes = [_P, _P, _P, _U, _U, _U, _U, _U, _P, _P, _P]
             lib.orc_trace_closest.argtypes = [_P, _P, _P, _U, C.c_float, _P]
             lib.orc_trace_ray.restype = C.c_int
-            lib.orc_trace_ray.argtypes = [_P, _P, _P, C.c_float, C.c_float, C.c_int, _P, _P, _P, _P]
+            lib.orc_trace_ray.argtypes = [_P, _P, _P, C.c_float, C.c_float, C.c_int, _P, _P, _P, _P, _P]
             lib.orc_ties.restype = _U
-            lib.orc_ties.argtypes = [_P, _P, _P, C.c_float, C.c_float, C.c_float, _P, _U]
+            lib.orc_ties.argtypes = [_P, _P, _P, C.c_float, C.c_float, C.c_float, _P, _U, _P]
             lib.orc_trace_any.argtypes = [_P, _P, _P, _U, C.c_float, _P]
             lib.orc_shade.argtypes = [_P, _P, _U, _U, _U, _U, _U, _P, _P, _P, _P, _P, _P, _P, _P, _P]
             lib.orc_shade_fp64.argtypes = [_P, _P, _U, _U, _U, _U, _U, _P, _P, _P, _P, _P, _P, _P, _P, _P]
@@ -109,12 +109,17 @@ class Oracle:
         self._lib.orc_trace_closest(self._s, _ptr(O), _ptr(D), O.shape[0], tmin, _ptr(hits))
         return hits
 
-    def ties(self, O, D, tmin: float, t: float, rel: float = 1e-6, max_out: int = 16) -> list[int]:
+    def ties(self, O, D, tmin: float, t: float, rel: float = 1e-6, max_out: int = 16, with_instances=False):
+        """Triangles hit at t within rel (mesh-local indices; with_instances: (instance, triangle) pairs)."""
         o = np.ascontiguousarray(O[:3], np.float32)
         d = np.ascontiguousarray(D[:3], np.float32)
         prims = np.zeros(max_out, np.uint32)
-        n = self._lib.orc_ties(self._s, _ptr(o), _ptr(d), tmin, t, rel, _ptr(prims), max_out)
-        return [int(p) for p in prims[: min(n, max_out)]]
+        insts = np.zeros(max_out, np.uint32)
+        n = self._lib.orc_ties(self._s, _ptr(o), _ptr(d), tmin, t, rel, _ptr(prims), max_out, _ptr(insts))
+        k = min(n, max_out)
+        if with_instances:
+            return [(int(i), int(p)) for i, p in zip(insts[:k], prims[:k])]
+        return [int(p) for p in prims[:k]]
 
     def trace_any(self, O: np.ndarray, L: np.ndarray, eps: float) -> np.ndarray:
         O = np.ascontiguousarray(O, np.float32)

@@ -247,6 +247,13 @@ struct orc_scene {
     float lightEnergyTotal = 0.f;
     std::vector<Node> nodes;
     std::vector<uint32_t> refs;
+    // two-level scenes: meshes placed by instances, one BVH per mesh (refs are
+    // global triangle indices), the inverse transform rows (r | t) per instance
+    bool twoLevel = false;
+    std::vector<uint32_t> meshTriBase, meshTriCount, instMesh;
+    std::vector<float> instInv;
+    std::vector<std::vector<Node>> meshNodes;
+    std::vector<std::vector<uint32_t>> meshRefs;
 };
 
 namespace {
@@ -282,22 +289,23 @@ std::vector<Alias> alias_table(const std::vector<double>& w)
     return t;
 }
 
-void build_bvh(orc_scene& S)
+// Median-split BVH over the triangles [base, base + n) (refs hold global indices).
+void build_bvh_range(const orc_scene& S, uint32_t base, uint32_t n, std::vector<Node>& nodes,
+                     std::vector<uint32_t>& refs)
 {
-    const uint32_t n = uint32_t(S.tris.size());
-    S.refs.resize(n);
+    refs.resize(n);
     for (uint32_t i = 0; i < n; ++i)
-        S.refs[i] = i;
-    S.nodes.clear();
-    S.nodes.reserve(2 * n + 1);
-    std::vector<float> c(3 * size_t(n));
-    for (uint32_t i = 0; i < n; ++i)
+        refs[i] = base + i;
+    nodes.clear();
+    nodes.reserve(2 * size_t(n) + 1);
+    std::vector<float> c(3 * size_t(S.tris.size()));
+    for (uint32_t i = base; i < base + n; ++i)
         for (int a = 0; a < 3; ++a)
-            c[3 * i + a] = (S.tris[i].v[0][a] + S.tris[i].v[1][a] + S.tris[i].v[2][a]) / 3.f;
+            c[3 * size_t(i) + a] = (S.tris[i].v[0][a] + S.tris[i].v[1][a] + S.tris[i].v[2][a]) / 3.f;
     struct Item {
         uint32_t node, begin, end;
     };
-    S.nodes.push_back(Node{});
+    nodes.push_back(Node{});
     std::vector<Item> stack{{0, 0, n}};
     while (!stack.empty()) {
         const Item it = stack.back();
@@ -309,22 +317,22 @@ void build_bvh(orc_scene& S)
         }
         float clo[3] = {INFINITY, INFINITY, INFINITY}, chi[3] = {-INFINITY, -INFINITY, -INFINITY};
         for (uint32_t k = it.begin; k < it.end; ++k) {
-            const Tri& t = S.tris[S.refs[k]];
+            const Tri& t = S.tris[refs[k]];
             for (int v = 0; v < 3; ++v)
                 for (int a = 0; a < 3; ++a) {
                     nd.lo[a] = std::min(nd.lo[a], t.v[v][a]);
                     nd.hi[a] = std::max(nd.hi[a], t.v[v][a]);
                 }
             for (int a = 0; a < 3; ++a) {
-                clo[a] = std::min(clo[a], c[3 * S.refs[k] + a]);
-                chi[a] = std::max(chi[a], c[3 * S.refs[k] + a]);
+                clo[a] = std::min(clo[a], c[3 * refs[k] + a]);
+                chi[a] = std::max(chi[a], c[3 * refs[k] + a]);
             }
         }
         const uint32_t cnt = it.end - it.begin;
         if (cnt <= 4) {
             nd.first = it.begin;
             nd.count = cnt;
-            S.nodes[it.node] = nd;
+            nodes[it.node] = nd;
             continue;
         }
         int axis = 0;
@@ -332,17 +340,29 @@ void build_bvh(orc_scene& S)
             if (chi[a] - clo[a] > chi[axis] - clo[axis])
                 axis = a;
         const uint32_t mid = it.begin + cnt / 2;
-        std::nth_element(S.refs.begin() + it.begin, S.refs.begin() + mid, S.refs.begin() + it.end,
+        std::nth_element(refs.begin() + it.begin, refs.begin() + mid, refs.begin() + it.end,
                          [&](uint32_t x, uint32_t y) { return c[3 * x + axis] < c[3 * y + axis]; });
-        const uint32_t left = uint32_t(S.nodes.size());
-        S.nodes.push_back(Node{});
-        S.nodes.push_back(Node{});
+        const uint32_t left = uint32_t(nodes.size());
+        nodes.push_back(Node{});
+        nodes.push_back(Node{});
         nd.first = left;
         nd.count = 0;
-        S.nodes[it.node] = nd;
+        nodes[it.node] = nd;
         stack.push_back({left, it.begin, mid});
         stack.push_back({left + 1, mid, it.end});
     }
+}
+
+void build_bvh(orc_scene& S)
+{
+    if (!S.twoLevel) {
+        build_bvh_range(S, 0, uint32_t(S.tris.size()), S.nodes, S.refs);
+        return;
+    }
+    S.meshNodes.resize(S.meshTriBase.size());
+    S.meshRefs.resize(S.meshTriBase.size());
+    for (size_t m = 0; m < S.meshTriBase.size(); ++m)
+        build_bvh_range(S, S.meshTriBase[m], S.meshTriCount[m], S.meshNodes[m], S.meshRefs[m]);
 }
 
 // ---------------------------------------------------------------- triangle test
@@ -430,12 +450,13 @@ inline bool box_hit(const Node& n, const double O[3], const double inv[3], doubl
     return t0 <= t1 + 1e-9 * std::max(1.0, mfabs(t1));
 }
 
-// Closest hit (any = false) or first hit (any = true) of one ray; T selects the triangle test precision.
+// Closest hit (any = false) or first hit (any = true) of one ray in one BVH; T
+// selects the triangle test precision.
 template <class T>
-bool trace(const orc_scene& S, const T Oin[3], const T Din[3], T tmin, T& tmax, bool any, uint32_t& prim, T& bu,
-           T& bv)
+bool trace_bvh(const orc_scene& S, const std::vector<Node>& nodes, const std::vector<uint32_t>& refs,
+               const T Oin[3], const T Din[3], T tmin, T& tmax, bool any, uint32_t& prim, T& bu, T& bv)
 {
-    if (S.nodes.empty() || S.tris.empty())
+    if (nodes.empty() || refs.empty())
         return false;
     double O[3], inv[3];
     for (int a = 0; a < 3; ++a) {
@@ -447,14 +468,14 @@ bool trace(const orc_scene& S, const T Oin[3], const T Din[3], T tmin, T& tmax, 
     int sp = 0;
     stack[sp++] = 0;
     while (sp > 0) {
-        const Node& n = S.nodes[stack[--sp]];
+        const Node& n = nodes[stack[--sp]];
         double tn;
         if (!box_hit(n, O, inv, double(tmin), double(tmax), tn))
             continue;
         if (n.count == 0) {
             double tl, tr;
-            const bool hl = box_hit(S.nodes[n.first], O, inv, double(tmin), double(tmax), tl);
-            const bool hr = box_hit(S.nodes[n.first + 1], O, inv, double(tmin), double(tmax), tr);
+            const bool hl = box_hit(nodes[n.first], O, inv, double(tmin), double(tmax), tl);
+            const bool hr = box_hit(nodes[n.first + 1], O, inv, double(tmin), double(tmax), tr);
             if (hl && hr) {
                 if (tl <= tr) {
                     stack[sp++] = n.first + 1;
@@ -473,7 +494,7 @@ bool trace(const orc_scene& S, const T Oin[3], const T Din[3], T tmin, T& tmax, 
             continue;
         }
         for (uint32_t k = n.first; k < n.first + n.count; ++k) {
-            const uint32_t p = S.refs[k];
+            const uint32_t p = refs[k];
             T t, u, v;
             bool h;
             if constexpr (sizeof(T) == 4)
@@ -494,6 +515,55 @@ bool trace(const orc_scene& S, const T Oin[3], const T Din[3], T tmin, T& tmax, 
                 bu = u;
                 bv = v;
             }
+        }
+    }
+    return found;
+}
+
+// World ray -> object ray of an instance: rows (r | t) of its inverse transform,
+// ((r.x p.x + r.y p.y) + r.z p.z) + t, every operation rounded on its own as the
+// GPU traversal does (tr_traverse.cuh xform_point / xform_vector).
+template <class T>
+void to_object(const float* m, const T O[3], const T D[3], T Oo[3], T Do[3])
+{
+    for (int r = 0; r < 3; ++r) {
+        const T a = T(m[4 * r]), b = T(m[4 * r + 1]), c = T(m[4 * r + 2]), t = T(m[4 * r + 3]);
+        Oo[r] = ((a * O[0] + b * O[1]) + c * O[2]) + t;
+        Do[r] = (a * D[0] + b * D[1]) + c * D[2];
+    }
+}
+
+// Closest or first hit of one ray in the scene: one level, or every instance's
+// mesh in object space (the ray parameter t is shared; on equal t the earlier
+// instance keeps the hit). inst = instance of the hit; prim = global triangle.
+template <class T>
+bool trace(const orc_scene& S, const T Oin[3], const T Din[3], T tmin, T& tmax, bool any, uint32_t& prim, T& bu,
+           T& bv, uint32_t* inst = nullptr)
+{
+    if (!S.twoLevel) {
+        if (inst)
+            *inst = 0;
+        return trace_bvh<T>(S, S.nodes, S.refs, Oin, Din, tmin, tmax, any, prim, bu, bv);
+    }
+    bool found = false;
+    for (uint32_t i = 0; i < S.instMesh.size(); ++i) {
+        T Oo[3], Do[3];
+        to_object<T>(&S.instInv[12 * size_t(i)], Oin, Din, Oo, Do);
+        const uint32_t m = S.instMesh[i];
+        T tm = tmax, u = 0, v = 0;
+        uint32_t p = 0;
+        if (!trace_bvh<T>(S, S.meshNodes[m], S.meshRefs[m], Oo, Do, tmin, tm, any, p, u, v))
+            continue;
+        if (any || !found || tm < tmax) {
+            found = true;
+            tmax = tm;
+            prim = p;
+            bu = u;
+            bv = v;
+            if (inst)
+                *inst = i;
+            if (any)
+                return true;
         }
     }
     return found;
@@ -1069,8 +1139,10 @@ struct Surface {
     uint32_t matIx;
 };
 
-// GetIntersectionAttributes + FixNormals, CudaMaterial.h:102-212 (identity instance)
-template <class T> Surface<T> surface_at(const orc_scene& S, uint32_t prim, T bu, T bv, V3<T> D)
+// GetIntersectionAttributes + FixNormals, CudaMaterial.h:102-212. prim is the
+// global triangle index; inst selects the inverse instance transform applied to
+// the frame (two-level scenes; one-level scenes have the identity).
+template <class T> Surface<T> surface_at(const orc_scene& S, uint32_t prim, T bu, T bv, V3<T> D, uint32_t inst = 0)
 {
     const Tri& t = S.tris[prim];
     Surface<T> sf;
@@ -1100,7 +1172,19 @@ template <class T> Surface<T> surface_at(const orc_scene& S, uint32_t prim, T bu
         sf.B = normalize(tv - sf.N * dot(sf.N, tv));
         sf.Tn = normalize(cross(sf.N, sf.B));
     }
-    // identity inverse instance transform: transform() then normalize
+    if (S.twoLevel) {
+        // object -> world: transform(tx, ty, tz, v) with the inverse rows, CudaMaterial.h:204-211
+        const float* m = &S.instInv[12 * size_t(inst)];
+        auto xf = [&](V3<T> v) {
+            return v3(dot(v, v3(T(m[0]), T(m[4]), T(m[8]))), dot(v, v3(T(m[1]), T(m[5]), T(m[9]))),
+                      dot(v, v3(T(m[2]), T(m[6]), T(m[10]))));
+        };
+        sf.N = xf(sf.N);
+        sf.Ng = xf(sf.Ng);
+        sf.B = xf(sf.B);
+        sf.Tn = xf(sf.Tn);
+    }
+    // (one level: the identity inverse instance transform) transform() then normalize
     sf.N = normalize(sf.N);
     sf.Ng = normalize(sf.Ng);
     sf.B = normalize(sf.B);
@@ -1248,14 +1332,14 @@ V3<T> sample_light(const orc_scene& S, Rng& rng, V3<T> I, V3<T> N, T& prob, T& p
 template <class T, bool REF, class Rng>
 ShadeOut<T> shade_one(const orc_scene& S, const tr_kernel_settings& st, uint32_t bounce, V3<T> O, V3<T> D,
                       V3<T> Tp, T extendPdf, uint32_t pathIx, uint32_t flags, uint32_t primIx, T bu, T bv, T tmax,
-                      Rng& rng)
+                      Rng& rng, uint32_t inst = 0)
 {
     ShadeOut<T> out;
     const T maxColor = T(st.max_color > 0.f ? st.max_color : 10.f);
     const V3<T> I = O + D * tmax;
     if (primIx == 0xffffffffu)
         return out;  // sky disabled: black
-    const Surface<T> sf = surface_at<T>(S, primIx, bu, bv, D);
+    const Surface<T> sf = surface_at<T>(S, primIx, bu, bv, D, inst);
     const HitMat<T> m = hit_material<T>(S.mats[sf.matIx]);
     out.hit = true;
     out.matIx = sf.matIx;
@@ -1375,10 +1459,10 @@ V3<T> render_path(const orc_scene& S, const tr_camera& cam, T tanFov2, const tr_
     for (uint32_t b = 0; b < st.max_depth; ++b) {
         ++nExt;
         T tmax = T(kDstMax);
-        uint32_t prim = 0xffffffffu;
+        uint32_t prim = 0xffffffffu, inst = 0;
         T bu = 0, bv = 0;
         const T Oa[3] = {O.x, O.y, O.z}, Da[3] = {D.x, D.y, D.z};
-        if (!trace<T>(S, Oa, Da, eps, tmax, false, prim, bu, bv)) {
+        if (!trace<T>(S, Oa, Da, eps, tmax, false, prim, bu, bv, &inst)) {
             prim = 0xffffffffu;
             tmax = T(kDstMax);
         }
@@ -1392,10 +1476,10 @@ V3<T> render_path(const orc_scene& S, const tr_camera& cam, T tanFov2, const tr_
         ShadeOut<T> so;
         if (REF) {
             RefRng rng{tea2(st.seed + pathIx, sampleCount + b + 1u)};
-            so = shade_one<T, true>(S, st, b, O, D, Tp, extendPdf, pathIx, flags, prim, u16, v16, tmax, rng);
+            so = shade_one<T, true>(S, st, b, O, D, Tp, extendPdf, pathIx, flags, prim, u16, v16, tmax, rng, inst);
         } else {
             CounterRng rng{pixel, sampleCount + pathIx / wh, b + 1u, st.seed};
-            so = shade_one<T, false>(S, st, b, O, D, Tp, extendPdf, pathIx, flags, prim, u16, v16, tmax, rng);
+            so = shade_one<T, false>(S, st, b, O, D, Tp, extendPdf, pathIx, flags, prim, u16, v16, tmax, rng, inst);
         }
         radiance = radiance + so.add;
         if (so.sh) {
@@ -1488,10 +1572,10 @@ void adjoint_path(const orc_scene& S, const tr_camera& cam, T tanFov2, const tr_
     std::vector<VertexRec<T>> verts;
     for (uint32_t b = 0; b < st.max_depth; ++b) {
         T tmax = T(kDstMax);
-        uint32_t prim = 0xffffffffu;
+        uint32_t prim = 0xffffffffu, inst = 0;
         T bu = 0, bv = 0;
         const T Oa[3] = {O.x, O.y, O.z}, Da[3] = {D.x, D.y, D.z};
-        if (!trace<T>(S, Oa, Da, eps, tmax, false, prim, bu, bv)) {
+        if (!trace<T>(S, Oa, Da, eps, tmax, false, prim, bu, bv, &inst)) {
             prim = 0xffffffffu;
             tmax = T(kDstMax);
         }
@@ -1503,7 +1587,7 @@ void adjoint_path(const orc_scene& S, const tr_camera& cam, T tanFov2, const tr_
         }
         CounterRng rng{pixel, sampleCount + pathIx / wh, b + 1u, st.seed};
         VertexRec<T> vr;
-        vr.so = shade_one<T, false>(S, st, b, O, D, Tp, extendPdf, pathIx, flags, prim, u16, v16, tmax, rng);
+        vr.so = shade_one<T, false>(S, st, b, O, D, Tp, extendPdf, pathIx, flags, prim, u16, v16, tmax, rng, inst);
         if (vr.so.sh) {
             T smax = vr.so.shDist - T(2) * eps;
             uint32_t p2 = 0;
@@ -1591,13 +1675,17 @@ void shade_entries(const orc_scene* s, const tr_kernel_settings* st, uint32_t bo
         const uint32_t* h = hits + 4 * size_t(i);
         const T bu = decode16<T>(h[0] >> 16), bv = decode16<T>(h[0] & 0xFFFFu);
         const T tmax = T(u2f(h[3]));
+        // hit record (bary, instIx, primIx within the instance's mesh, t) -> global triangle
+        const uint32_t inst = h[2] == 0xffffffffu ? 0u : h[1];
+        const uint32_t prim = (h[2] == 0xffffffffu || !s->twoLevel) ? h[2] : s->meshTriBase[s->instMesh[inst]] + h[2];
         ShadeOut<T> so;
         if (ref) {
             RefRng rng{tea2(st->seed + pathIx, sc + bounce + 1u)};
-            so = shade_one<T, true>(*s, *st, bounce, O, D, Tp, extendPdf, pathIx, flags, h[2], bu, bv, tmax, rng);
+            so = shade_one<T, true>(*s, *st, bounce, O, D, Tp, extendPdf, pathIx, flags, prim, bu, bv, tmax, rng, inst);
         } else {
             CounterRng rng{pathIx % wh, sc + pathIx / wh, bounce + 1u, st->seed};
-            so = shade_one<T, false>(*s, *st, bounce, O, D, Tp, extendPdf, pathIx, flags, h[2], bu, bv, tmax, rng);
+            so = shade_one<T, false>(*s, *st, bounce, O, D, Tp, extendPdf, pathIx, flags, prim, bu, bv, tmax, rng,
+                                     inst);
         }
         ext_valid[i] = so.ext;
         sh_valid[i] = so.sh;
@@ -1624,15 +1712,22 @@ extern "C" {
 
 orc_scene* orc_scene_create(const tr_scene_desc* desc)
 {
-    if (!desc || !desc->mesh)
+    if (!desc || (desc->instance_count ? !desc->meshes || !desc->instances : !desc->mesh))
         return nullptr;
-    const tr_mesh_desc& m = *desc->mesh;
     orc_scene* S = new orc_scene();
-    const uint32_t n = m.triangle_count;
-    S->tris.resize(n);
-    S->geo.resize(9 * size_t(n));
-    S->geoD.resize(9 * size_t(n));
-    S->matIdx.assign(m.material_indices, m.material_indices + n);
+    S->twoLevel = desc->instance_count > 0;
+    const uint32_t meshCount = S->twoLevel ? desc->mesh_count : 1u;
+    auto meshOf = [&](uint32_t i) -> const tr_mesh_desc& { return S->twoLevel ? desc->meshes[i] : *desc->mesh; };
+    uint32_t total = 0;
+    for (uint32_t mi = 0; mi < meshCount; ++mi) {
+        S->meshTriBase.push_back(total);
+        S->meshTriCount.push_back(meshOf(mi).triangle_count);
+        total += meshOf(mi).triangle_count;
+    }
+    S->tris.resize(total);
+    S->geo.resize(9 * size_t(total));
+    S->geoD.resize(9 * size_t(total));
+    S->matIdx.resize(total);
     S->mats.resize(desc->material_count);
     for (uint32_t i = 0; i < desc->material_count; ++i) {
         const tr_material_desc& d = desc->materials[i];
@@ -1653,62 +1748,117 @@ orc_scene* orc_scene_create(const tr_scene_desc* desc)
         r.clearcoatGloss = hround(d.clearcoat_gloss);
         r.closure = d.closure;
     }
+    // Model::Build (Model.cpp:93-167), object space
+    std::vector<V3<float>> lightN(total);
+    for (uint32_t mi = 0; mi < meshCount; ++mi) {
+        const tr_mesh_desc& m = meshOf(mi);
+        const uint32_t base = S->meshTriBase[mi];
+        const uint32_t offset = S->twoLevel && desc->mesh_material_offsets ? desc->mesh_material_offsets[mi] : 0u;
+        for (uint32_t t = 0; t < m.triangle_count; ++t) {
+            const uint32_t ix[3] = {m.indices[3 * t], m.indices[3 * t + 1], m.indices[3 * t + 2]};
+            V3<float> p[3], nn[3];
+            for (int k = 0; k < 3; ++k)
+                p[k] = v3(m.positions[3 * ix[k]], m.positions[3 * ix[k] + 1], m.positions[3 * ix[k] + 2]);
+            for (int k = 0; k < 3; ++k) {
+                if (m.normals)
+                    nn[k] = v3(m.normals[3 * ix[k]], m.normals[3 * ix[k] + 1], m.normals[3 * ix[k] + 2]);
+                else
+                    nn[k] = normalize(cross(p[1] - p[0], p[2] - p[0]));
+            }
+            Tri& tr = S->tris[base + t];
+            for (int k = 0; k < 3; ++k) {
+                tr.v[k][0] = p[k].x;
+                tr.v[k][1] = p[k].y;
+                tr.v[k][2] = p[k].z;
+                tr.uv[k][0] = hbits(m.texcoords ? m.texcoords[2 * ix[k]] : 0.f);
+                tr.uv[k][1] = hbits(m.texcoords ? m.texcoords[2 * ix[k] + 1] : 0.f);
+                tr.n[k][0] = hbits(nn[k].x);
+                tr.n[k][1] = hbits(nn[k].y);
+                tr.n[k][2] = hbits(nn[k].z);
+            }
+            const V3<float> N = normalize(nn[0] + nn[1] + nn[2]);
+            tr.N[0] = hbits(N.x);
+            tr.N[1] = hbits(N.y);
+            tr.N[2] = hbits(N.z);
+            lightN[base + t] = normalize(normalize(nn[0] + nn[1] + nn[2]));
+            float* g = &S->geo[9 * size_t(base + t)];
+            double* gd = &S->geoD[9 * size_t(base + t)];
+            for (int a = 0; a < 3; ++a) {
+                g[a] = tr.v[0][a];
+                g[3 + a] = tr.v[1][a] - tr.v[0][a];
+                g[6 + a] = tr.v[2][a] - tr.v[0][a];
+                gd[a] = double(tr.v[0][a]);
+                gd[3 + a] = double(tr.v[1][a]) - double(tr.v[0][a]);
+                gd[6 + a] = double(tr.v[2][a]) - double(tr.v[0][a]);
+            }
+            S->matIdx[base + t] = m.material_indices[t] + offset;
+        }
+    }
+    // instances: inverse transforms (LinearMath.h:472-506), lights gathered in
+    // instance then triangle order (Model::BuildLights, Model.cpp:205-230;
+    // Scene::GatherLights, Scene.cpp:275-302): vertices placed with the instance
+    // transform as the geometry is (R p + t), the normal with the inverse
+    // transpose as the shading frame is, area in object space
+    const uint32_t instCount = S->twoLevel ? desc->instance_count : 1u;
     std::vector<double> energies;
     float sumEnergy = 0.f;
-    for (uint32_t t = 0; t < n; ++t) {
-        const uint32_t ix[3] = {m.indices[3 * t], m.indices[3 * t + 1], m.indices[3 * t + 2]};
-        V3<float> p[3], nn[3];
-        for (int k = 0; k < 3; ++k)
-            p[k] = v3(m.positions[3 * ix[k]], m.positions[3 * ix[k] + 1], m.positions[3 * ix[k] + 2]);
-        for (int k = 0; k < 3; ++k) {
-            if (m.normals)
-                nn[k] = v3(m.normals[3 * ix[k]], m.normals[3 * ix[k] + 1], m.normals[3 * ix[k] + 2]);
-            else
-                nn[k] = normalize(cross(p[1] - p[0], p[2] - p[0]));
+    for (uint32_t i = 0; i < instCount; ++i) {
+        const uint32_t mi = S->twoLevel ? desc->instances[i].mesh : 0u;
+        S->instMesh.push_back(mi);
+        float inv[12] = {1, 0, 0, 0, 0, 1, 0, 0, 0, 0, 1, 0};
+        const float* xf = S->twoLevel ? desc->instances[i].transform : nullptr;
+        if (xf) {
+            const float xx = xf[0], xy = xf[1], xz = xf[2], tx = xf[3];
+            const float yx = xf[4], yy = xf[5], yz = xf[6], ty = xf[7];
+            const float zx = xf[8], zy = xf[9], zz = xf[10], tz = xf[11];
+            const float det3 = xx * (yy * zz - yz * zy) - xy * (yx * zz - yz * zx) + xz * (yx * zy - yy * zx);
+            const float id = 1.0f / det3;
+            const float a00 = id * (yy * zz - zy * yz), a01 = id * (xz * zy - zz * xy), a02 = id * (xy * yz - yy * xz);
+            const float a10 = id * (yz * zx - zz * yx), a11 = id * (xx * zz - zx * xz), a12 = id * (xz * yx - yz * xx);
+            const float a20 = id * (yx * zy - zx * yy), a21 = id * (xy * zx - zy * xx), a22 = id * (xx * yy - yx * xy);
+            const float r[12] = {a00, a01, a02, -a00 * tx - a01 * ty - a02 * tz,
+                                 a10, a11, a12, -a10 * tx - a11 * ty - a12 * tz,
+                                 a20, a21, a22, -a20 * tx - a21 * ty - a22 * tz};
+            std::copy(r, r + 12, inv);
         }
-        Tri& tr = S->tris[t];
-        for (int k = 0; k < 3; ++k) {
-            tr.v[k][0] = p[k].x;
-            tr.v[k][1] = p[k].y;
-            tr.v[k][2] = p[k].z;
-            tr.uv[k][0] = hbits(m.texcoords ? m.texcoords[2 * ix[k]] : 0.f);
-            tr.uv[k][1] = hbits(m.texcoords ? m.texcoords[2 * ix[k] + 1] : 0.f);
-            tr.n[k][0] = hbits(nn[k].x);
-            tr.n[k][1] = hbits(nn[k].y);
-            tr.n[k][2] = hbits(nn[k].z);
-        }
-        const V3<float> N = normalize(nn[0] + nn[1] + nn[2]);
-        tr.N[0] = hbits(N.x);
-        tr.N[1] = hbits(N.y);
-        tr.N[2] = hbits(N.z);
-        float* g = &S->geo[9 * size_t(t)];
-        double* gd = &S->geoD[9 * size_t(t)];
-        for (int a = 0; a < 3; ++a) {
-            g[a] = tr.v[0][a];
-            g[3 + a] = tr.v[1][a] - tr.v[0][a];
-            g[6 + a] = tr.v[2][a] - tr.v[0][a];
-            gd[a] = double(tr.v[0][a]);
-            gd[3 + a] = double(tr.v[1][a]) - double(tr.v[0][a]);
-            gd[6 + a] = double(tr.v[2][a]) - double(tr.v[0][a]);
-        }
-        // Model::BuildLights (Model.cpp:205-230) + Scene::GatherLights (Scene.cpp:283-297)
-        const tr_material_desc& md = desc->materials[m.material_indices[t]];
-        const V3<float> em = v3(md.emissive[0], md.emissive[1], md.emissive[2]);
-        if (em.x + em.y + em.z > kEps) {
+        S->instInv.insert(S->instInv.end(), inv, inv + 12);
+        const uint32_t base = S->meshTriBase[mi];
+        for (uint32_t t = 0; t < S->meshTriCount[mi]; ++t) {
+            const Tri& tr = S->tris[base + t];
+            const tr_material_desc& md = desc->materials[S->matIdx[base + t]];
+            const V3<float> em = v3(md.emissive[0], md.emissive[1], md.emissive[2]);
+            if (!(em.x + em.y + em.z > kEps))
+                continue;
             Light L{};
-            L.triIx = t;
-            for (int a = 0; a < 3; ++a) {
-                L.V0[a] = tr.v[0][a];
-                L.V1[a] = tr.v[1][a];
-                L.V2[a] = tr.v[2][a];
+            L.triIx = base + t;
+            V3<float> p[3];
+            for (int k = 0; k < 3; ++k)
+                p[k] = v3(tr.v[k][0], tr.v[k][1], tr.v[k][2]);
+            float* dst[3] = {L.V0, L.V1, L.V2};
+            for (int k = 0; k < 3; ++k) {
+                V3<float> w = p[k];
+                if (xf)
+                    w = v3(((xf[0] * p[k].x + xf[1] * p[k].y) + xf[2] * p[k].z) + xf[3],
+                           ((xf[4] * p[k].x + xf[5] * p[k].y) + xf[6] * p[k].z) + xf[7],
+                           ((xf[8] * p[k].x + xf[9] * p[k].y) + xf[10] * p[k].z) + xf[11]);
+                dst[k][0] = w.x;
+                dst[k][1] = w.y;
+                dst[k][2] = w.z;
             }
-            const V3<float> ln = normalize(normalize(nn[0] + nn[1] + nn[2]));
+            V3<float> ln = lightN[base + t];
+            if (xf) {
+                const V3<float> n0 = ln;
+                ln = normalize(v3((n0.x * inv[0] + n0.y * inv[4]) + n0.z * inv[8],
+                                  (n0.x * inv[1] + n0.y * inv[5]) + n0.z * inv[9],
+                                  (n0.x * inv[2] + n0.y * inv[6]) + n0.z * inv[10]));
+                ln = normalize(ln);
+            }
             L.N[0] = ln.x;
             L.N[1] = ln.y;
             L.N[2] = ln.z;
             const float a = length(p[1] - p[0]), b = length(p[2] - p[1]), c = length(p[0] - p[2]);
-            const float s = (a + b + c) * .5f;
-            L.area = msqrt(s * (s - a) * (s - b) * (s - c));
+            const float sp = (a + b + c) * .5f;
+            L.area = msqrt(sp * (sp - a) * (sp - b) * (sp - c));
             L.radiance[0] = em.x;
             L.radiance[1] = em.y;
             L.radiance[2] = em.z;
@@ -1765,12 +1915,12 @@ void orc_trace_closest(const orc_scene* s, const float* O4, const float* D4, uin
         const float O[3] = {O4[4 * i], O4[4 * i + 1], O4[4 * i + 2]};
         const float D[3] = {D4[4 * i], D4[4 * i + 1], D4[4 * i + 2]};
         float tmax = kDstMax, u = 0, v = 0;
-        uint32_t prim = 0xffffffffu;
+        uint32_t prim = 0xffffffffu, inst = 0;
         uint32_t* h = hits + 4 * size_t(i);
-        if (trace<float>(*s, O, D, tmin, tmax, false, prim, u, v)) {
+        if (trace<float>(*s, O, D, tmin, tmax, false, prim, u, v, &inst)) {
             h[0] = encode_bary(u, v);
-            h[1] = 0;
-            h[2] = prim;
+            h[1] = inst;
+            h[2] = s->twoLevel ? prim - s->meshTriBase[s->instMesh[inst]] : prim;
             h[3] = f2u(tmax);
         } else {
             h[0] = 0;
@@ -1782,13 +1932,15 @@ void orc_trace_closest(const orc_scene* s, const float* O4, const float* D4, uin
 }
 
 int orc_trace_ray(const orc_scene* s, const float* O, const float* D, float tmin, float tmax, int any, uint32_t* prim,
-                  float* t, float* u, float* v)
+                  float* t, float* u, float* v, uint32_t* inst)
 {
     float tm = tmax, uu = 0, vv = 0;
-    uint32_t p = 0xffffffffu;
-    if (!trace<float>(*s, O, D, tmin, tm, any != 0, p, uu, vv))
+    uint32_t p = 0xffffffffu, in = 0;
+    if (!trace<float>(*s, O, D, tmin, tm, any != 0, p, uu, vv, &in))
         return 0;
-    *prim = p;
+    *prim = s->twoLevel ? p - s->meshTriBase[s->instMesh[in]] : p;
+    if (inst)
+        *inst = in;
     *t = tm;
     *u = uu;
     *v = vv;
@@ -1796,16 +1948,29 @@ int orc_trace_ray(const orc_scene* s, const float* O, const float* D, float tmin
 }
 
 uint32_t orc_ties(const orc_scene* s, const float* O, const float* D, float tmin, float t, float rel, uint32_t* prims,
-                  uint32_t max_out)
+                  uint32_t max_out, uint32_t* insts)
 {
     uint32_t count = 0;
-    for (uint32_t p = 0; p < s->tris.size(); ++p) {
-        float tt, u, v;
-        if (tri_test_f(&s->geo[9 * size_t(p)], O, D, tmin, kDstMax, tt, u, v) &&
-            mfabs(tt - t) <= rel * mfabs(t)) {
-            if (count < max_out)
-                prims[count] = p;
-            ++count;
+    const uint32_t instCount = s->twoLevel ? uint32_t(s->instMesh.size()) : 1u;
+    for (uint32_t i = 0; i < instCount; ++i) {
+        float Oo[3] = {O[0], O[1], O[2]}, Do[3] = {D[0], D[1], D[2]};
+        uint32_t base = 0, end = uint32_t(s->tris.size());
+        if (s->twoLevel) {
+            to_object<float>(&s->instInv[12 * size_t(i)], O, D, Oo, Do);
+            base = s->meshTriBase[s->instMesh[i]];
+            end = base + s->meshTriCount[s->instMesh[i]];
+        }
+        for (uint32_t p = base; p < end; ++p) {
+            float tt, u, v;
+            if (tri_test_f(&s->geo[9 * size_t(p)], Oo, Do, tmin, kDstMax, tt, u, v) &&
+                mfabs(tt - t) <= rel * mfabs(t)) {
+                if (count < max_out) {
+                    prims[count] = p - base;
+                    if (insts)
+                        insts[count] = i;
+                }
+                ++count;
+            }
         }
     }
     return count;

@@ -54,12 +54,12 @@ void orc_trace_closest(const orc_scene* s, const float* O4, const float* D4, uin
 /* One ray over [tmin, tmax]: closest hit (any = 0) or first hit (any = 1).
  * Returns 1 on a hit with prim, t and barycentrics (u, v) set. */
 int orc_trace_ray(const orc_scene* s, const float* O, const float* D, float tmin, float tmax, int any, uint32_t* prim,
-                  float* t, float* u, float* v);
+                  float* t, float* u, float* v, uint32_t* inst);
 
 /* All triangles whose hit distance lies within rel_tol of t (near ties of a
  * closest hit). Writes up to max_out primitive indices, returns the count. */
 uint32_t orc_ties(const orc_scene* s, const float* O, const float* D, float tmin, float t, float rel_tol,
-                  uint32_t* prims, uint32_t max_out);
+                  uint32_t* prims, uint32_t max_out, uint32_t* insts);
 
 /* Shadow rays (float4 O, float4 (L, dist)): occluded[i] = any hit in
  * [eps, dist - 2 eps]. */

@@ -16,20 +16,57 @@ namespace {
 
 struct RefCtx {
     orc_scene* orc = nullptr;
-    std::vector<PackedTriangle> tris;
-    std::vector<uint32_t> matIdx;
+    std::vector<std::vector<PackedTriangle>> tris;   // per model
+    std::vector<std::vector<uint32_t>> matIdx;       // per model
     std::vector<CudaMatarial> mats;
     std::vector<LightTriangle> lights;
-    CudaMeshData mesh{};
-    uint32_t materialOffsets[1] = {0};
-    uint32_t modelIndices[1] = {0};
-    float4 invTransforms[3];
+    std::vector<CudaMeshData> meshData;              // per instance (Renderer.cpp:473-486)
+    std::vector<uint32_t> materialOffsets;           // per model
+    std::vector<uint32_t> modelIndices;              // per instance
+    std::vector<float4> invTransforms;               // 3 per instance
     SkyData sky{};
     LaunchParams lp{};
     RayCounters counters{};
 };
 
 RefCtx* g_ctx = nullptr;
+
+// The reference's float3x4 (Tracer/Utility/LinearMath.h:205-210: float3 x; tx; y; ty; z; tz)
+// with its inverse (:472-506) and transform (:274-281), restated here because that
+// header's host intrinsics collide with this shim's.
+struct M34 {
+    float3 x; float tx;
+    float3 y; float ty;
+    float3 z; float tz;
+};
+M34 m34_inverse(const M34& a)
+{
+    const float det3 = a.x.x * (a.y.y * a.z.z - a.y.z * a.z.y) - a.x.y * (a.y.x * a.z.z - a.y.z * a.z.x) +
+                       a.x.z * (a.y.x * a.z.y - a.y.y * a.z.x);
+    const float inv_det3 = 1.0f / det3;
+    const float i00 = inv_det3 * (a.y.y * a.z.z - a.z.y * a.y.z);
+    const float i01 = inv_det3 * (a.x.z * a.z.y - a.z.z * a.x.y);
+    const float i02 = inv_det3 * (a.x.y * a.y.z - a.y.y * a.x.z);
+    const float i10 = inv_det3 * (a.y.z * a.z.x - a.z.z * a.y.x);
+    const float i11 = inv_det3 * (a.x.x * a.z.z - a.z.x * a.x.z);
+    const float i12 = inv_det3 * (a.x.z * a.y.x - a.y.z * a.x.x);
+    const float i20 = inv_det3 * (a.y.x * a.z.y - a.z.x * a.y.y);
+    const float i21 = inv_det3 * (a.x.y * a.z.x - a.z.y * a.x.x);
+    const float i22 = inv_det3 * (a.x.x * a.y.y - a.y.x * a.x.y);
+    M34 r;
+    r.x = make_float3(i00, i01, i02);
+    r.y = make_float3(i10, i11, i12);
+    r.z = make_float3(i20, i21, i22);
+    r.tx = -i00 * a.tx - i01 * a.ty - i02 * a.tz;
+    r.ty = -i10 * a.tx - i11 * a.ty - i12 * a.tz;
+    r.tz = -i20 * a.tx - i21 * a.ty - i22 * a.tz;
+    return r;
+}
+float4 m34_transform(const M34& a, const float4& b)
+{
+    return make_float4(dot(b, make_float4(a.x.x, a.y.x, a.z.x, a.tx)), dot(b, make_float4(a.x.y, a.y.y, a.z.y, a.ty)),
+                       dot(b, make_float4(a.x.z, a.y.z, a.z.z, a.tz)), b.w);
+}
 
 float3 f3n(float x, float y, float z) { return make_float3(x, y, z); }
 float3 nrm(float3 v)
@@ -93,7 +130,8 @@ void ref_host_trace(float3 O, float3 D, float tmin, float tmax, bool anyHit, uin
     const float o[3] = {O.x, O.y, O.z}, d[3] = {D.x, D.y, D.z};
     uint32_t prim = 0;
     float t = 0, u = 0, v = 0;
-    const int hit = orc_trace_ray(g_ctx->orc, o, d, tmin, tmax, anyHit ? 1 : 0, &prim, &t, &u, &v);
+    uint32_t inst = 0;
+    const int hit = orc_trace_ray(g_ctx->orc, o, d, tmin, tmax, anyHit ? 1 : 0, &prim, &t, &u, &v, &inst);
     if (anyHit) {
         if (!hit)
             p0 = 0;
@@ -106,7 +144,7 @@ void ref_host_trace(float3 O, float3 D, float tmin, float tmax, bool anyHit, uin
     const uint32_t bx = static_cast<uint32_t>(u * 65535.f) & 0xFFFF;
     const uint32_t by = static_cast<uint32_t>(v * 65535.f) & 0xFFFF;
     p0 = (bx << 16) | by;
-    p1 = 0;
+    p1 = inst;
     p2 = prim;
     p3 = __float_as_uint(t);
 }
@@ -115,48 +153,85 @@ extern "C" {
 
 void* ref_create(const tr_scene_desc* desc)
 {
-    if (!desc || !desc->mesh)
+    if (!desc || (desc->instance_count ? !desc->meshes || !desc->instances : !desc->mesh))
         return nullptr;
     RefCtx* c = new RefCtx();
     c->orc = orc_scene_create(desc);
-    const tr_mesh_desc& m = *desc->mesh;
-    const uint32_t n = m.triangle_count;
-    c->tris.resize(n);
-    c->matIdx.assign(m.material_indices, m.material_indices + n);
-    float sumEnergy = 0;
-    for (uint32_t t = 0; t < n; ++t) {
-        const uint32_t ix[3] = {m.indices[3 * t], m.indices[3 * t + 1], m.indices[3 * t + 2]};
-        float3 p[3], nn[3];
-        float2 uv[3];
-        for (int k = 0; k < 3; ++k) {
-            p[k] = f3n(m.positions[3 * ix[k]], m.positions[3 * ix[k] + 1], m.positions[3 * ix[k] + 2]);
-            uv[k] = m.texcoords ? make_float2(m.texcoords[2 * ix[k]], m.texcoords[2 * ix[k] + 1]) : make_float2(0, 0);
+    const bool twoLevel = desc->instance_count > 0;
+    const uint32_t models = twoLevel ? desc->mesh_count : 1u;
+    c->tris.resize(models);
+    c->matIdx.resize(models);
+    for (uint32_t mi = 0; mi < models; ++mi) {
+        const tr_mesh_desc& m = twoLevel ? desc->meshes[mi] : *desc->mesh;
+        const uint32_t n = m.triangle_count;
+        c->tris[mi].resize(n);
+        c->matIdx[mi].assign(m.material_indices, m.material_indices + n);
+        c->materialOffsets.push_back(twoLevel && desc->mesh_material_offsets ? desc->mesh_material_offsets[mi] : 0u);
+        for (uint32_t t = 0; t < n; ++t) {
+            const uint32_t ix[3] = {m.indices[3 * t], m.indices[3 * t + 1], m.indices[3 * t + 2]};
+            float3 p[3], nn[3];
+            float2 uv[3];
+            for (int k = 0; k < 3; ++k) {
+                p[k] = f3n(m.positions[3 * ix[k]], m.positions[3 * ix[k] + 1], m.positions[3 * ix[k] + 2]);
+                uv[k] = m.texcoords ? make_float2(m.texcoords[2 * ix[k]], m.texcoords[2 * ix[k] + 1])
+                                    : make_float2(0, 0);
+            }
+            for (int k = 0; k < 3; ++k)
+                nn[k] = m.normals ? f3n(m.normals[3 * ix[k]], m.normals[3 * ix[k] + 1], m.normals[3 * ix[k] + 2])
+                                  : nrm(cross(p[1] - p[0], p[2] - p[0]));
+            // Model::Build, Tracer/Resources/Model.cpp:105-163
+            PackedTriangle& q = c->tris[mi][t];
+            q.v0x = p[0].x; q.v0y = p[0].y; q.v0z = p[0].z;
+            q.v1x = p[1].x; q.v1y = p[1].y; q.v1z = p[1].z;
+            q.v2x = p[2].x; q.v2y = p[2].y; q.v2z = p[2].z;
+            q.uv0x = __float2half(uv[0].x); q.uv0y = __float2half(uv[0].y);
+            q.uv1x = __float2half(uv[1].x); q.uv1y = __float2half(uv[1].y);
+            q.uv2x = __float2half(uv[2].x); q.uv2y = __float2half(uv[2].y);
+            q.N0x = __float2half(nn[0].x); q.N0y = __float2half(nn[0].y); q.N0z = __float2half(nn[0].z);
+            q.N1x = __float2half(nn[1].x); q.N1y = __float2half(nn[1].y); q.N1z = __float2half(nn[1].z);
+            q.N2x = __float2half(nn[2].x); q.N2y = __float2half(nn[2].y); q.N2z = __float2half(nn[2].z);
+            const float3 N = normalize(nn[0] + nn[1] + nn[2]);
+            q.Nx = __float2half(N.x); q.Ny = __float2half(N.y); q.Nz = __float2half(N.z);
         }
-        for (int k = 0; k < 3; ++k)
-            nn[k] = m.normals ? f3n(m.normals[3 * ix[k]], m.normals[3 * ix[k] + 1], m.normals[3 * ix[k] + 2])
-                              : nrm(cross(p[1] - p[0], p[2] - p[0]));
-        // Model::Build, Tracer/Resources/Model.cpp:105-163
-        PackedTriangle& q = c->tris[t];
-        q.v0x = p[0].x; q.v0y = p[0].y; q.v0z = p[0].z;
-        q.v1x = p[1].x; q.v1y = p[1].y; q.v1z = p[1].z;
-        q.v2x = p[2].x; q.v2y = p[2].y; q.v2z = p[2].z;
-        q.uv0x = __float2half(uv[0].x); q.uv0y = __float2half(uv[0].y);
-        q.uv1x = __float2half(uv[1].x); q.uv1y = __float2half(uv[1].y);
-        q.uv2x = __float2half(uv[2].x); q.uv2y = __float2half(uv[2].y);
-        q.N0x = __float2half(nn[0].x); q.N0y = __float2half(nn[0].y); q.N0z = __float2half(nn[0].z);
-        q.N1x = __float2half(nn[1].x); q.N1y = __float2half(nn[1].y); q.N1z = __float2half(nn[1].z);
-        q.N2x = __float2half(nn[2].x); q.N2y = __float2half(nn[2].y); q.N2z = __float2half(nn[2].z);
-        const float3 N = normalize(nn[0] + nn[1] + nn[2]);
-        q.Nx = __float2half(N.x); q.Ny = __float2half(N.y); q.Nz = __float2half(N.z);
-        // Model::BuildLights (Model.cpp:205-230) + Scene::GatherLights (Scene.cpp:283-297)
-        const tr_material_desc& md = desc->materials[m.material_indices[t]];
-        const float3 em = f3n(md.emissive[0], md.emissive[1], md.emissive[2]);
-        if (em.x + em.y + em.z > 1e-3f) {
+    }
+    // instances: mesh data, model index, inverse transform (Renderer.cpp:473-486), then the
+    // lights of each instance (Model::BuildLights, Model.cpp:205-230; Scene::GatherLights,
+    // Scene.cpp:283-297)
+    float sumEnergy = 0;
+    const uint32_t instances = twoLevel ? desc->instance_count : 1u;
+    for (uint32_t i = 0; i < instances; ++i) {
+        const uint32_t mi = twoLevel ? desc->instances[i].mesh : 0u;
+        M34 xf{make_float3(1, 0, 0), 0, make_float3(0, 1, 0), 0, make_float3(0, 0, 1), 0};
+        if (twoLevel)
+            std::memcpy(&xf, desc->instances[i].transform, sizeof(xf));
+        const M34 inv = m34_inverse(xf);
+        float rows[12];
+        std::memcpy(rows, &inv, sizeof(rows));
+        for (int r = 0; r < 3; ++r)
+            c->invTransforms.push_back(make_float4(rows[4 * r], rows[4 * r + 1], rows[4 * r + 2], rows[4 * r + 3]));
+        c->modelIndices.push_back(mi);
+        CudaMeshData md{};
+        md.triangles = c->tris[mi].data();
+        md.materialIndices = c->matIdx[mi].data();
+        c->meshData.push_back(md);
+        const tr_mesh_desc& m = twoLevel ? desc->meshes[mi] : *desc->mesh;
+        for (uint32_t t = 0; t < m.triangle_count; ++t) {
+            const tr_material_desc& md2 = desc->materials[m.material_indices[t] + c->materialOffsets[mi]];
+            const float3 em = f3n(md2.emissive[0], md2.emissive[1], md2.emissive[2]);
+            if (!(em.x + em.y + em.z > 1e-3f))
+                continue;
+            const PackedTriangle& q = c->tris[mi][t];
+            const float3 p0 = f3n(q.v0x, q.v0y, q.v0z), p1 = f3n(q.v1x, q.v1y, q.v1z), p2 = f3n(q.v2x, q.v2y, q.v2z);
+            const uint32_t ix[3] = {m.indices[3 * t], m.indices[3 * t + 1], m.indices[3 * t + 2]};
+            float3 nn[3];
+            for (int k = 0; k < 3; ++k)
+                nn[k] = m.normals ? f3n(m.normals[3 * ix[k]], m.normals[3 * ix[k] + 1], m.normals[3 * ix[k] + 2])
+                                  : nrm(cross(p1 - p0, p2 - p0));
             LightTriangle lt{};
             lt.triIx = int32_t(t);
-            lt.V0 = p[0];
-            lt.V1 = p[1];
-            lt.V2 = p[2];
+            lt.V0 = p0;
+            lt.V1 = p1;
+            lt.V2 = p2;
             lt.N = normalize(normalize(nn[0] + nn[1] + nn[2]));
             const float a = length(lt.V1 - lt.V0), b = length(lt.V2 - lt.V1), cc = length(lt.V0 - lt.V2);
             const float s = (a + b + cc) * .5f;
@@ -164,8 +239,15 @@ void* ref_create(const tr_scene_desc* desc)
             lt.radiance = em;
             const float3 e = em * lt.area;
             lt.energy = e.x + e.y + e.z;
+            if (twoLevel) {
+                // GatherLights: the reference's transform(float3x4, float4) (LinearMath.h:274-281)
+                lt.V0 = make_float3(m34_transform(xf, make_float4(lt.V0, 1)));
+                lt.V1 = make_float3(m34_transform(xf, make_float4(lt.V1, 1)));
+                lt.V2 = make_float3(m34_transform(xf, make_float4(lt.V2, 1)));
+                lt.N = normalize(make_float3(m34_transform(xf, make_float4(lt.N, 0))));
+            }
             lt.sumEnergy = sumEnergy;
-            lt.instIx = 0;
+            lt.instIx = int32_t(i);
             sumEnergy += lt.energy;
             c->lights.push_back(lt);
         }
@@ -189,12 +271,6 @@ void* ref_create(const tr_scene_desc* desc)
         f(MaterialPropertyIds::SpecularTint, d.specular_tint);
         f(MaterialPropertyIds::Subsurface, d.subsurface);
     }
-    c->mesh.triangles = c->tris.data();
-    c->mesh.materialIndices = c->matIdx.data();
-    // inverse of the identity instance transform, as float3x4 rows (Renderer.cpp:482-484)
-    c->invTransforms[0] = make_float4(1, 0, 0, 0);
-    c->invTransforms[1] = make_float4(0, 1, 0, 0);
-    c->invTransforms[2] = make_float4(0, 0, 1, 0);
     c->sky.skyEnabled = 0;
     c->sky.drawSun = 0;
     return c;
@@ -212,11 +288,11 @@ void ref_destroy(void* ctx)
 static void bind_scene(RefCtx* c)
 {
     RefSceneBuffers b;
-    b.meshData = &c->mesh;
+    b.meshData = c->meshData.data();
     b.materials = c->mats.data();
-    b.materialOffsets = c->materialOffsets;
-    b.invTransforms = c->invTransforms;
-    b.modelIndices = c->modelIndices;
+    b.materialOffsets = c->materialOffsets.data();
+    b.invTransforms = c->invTransforms.data();
+    b.modelIndices = c->modelIndices.data();
     b.lightCount = int32_t(c->lights.size());
     // SetCudaLightEnergy(lightData.back().sumEnergy), Renderer.cpp:500
     b.lightEnergy = c->lights.empty() ? 0.f : c->lights.back().sumEnergy;

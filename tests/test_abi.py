@@ -46,6 +46,12 @@ def test_struct_layouts_match_ctypes(tmp_path):
         "tr_statistics": _abi.Statistics,
         "tr_scene_info": _abi.SceneInfo,
         "tr_buffers": _abi.Buffers,
+        "tr_instance_desc": _abi.InstanceDesc,
+        "tr_tuning": _abi.Tuning,
+        "tr_tune_report": _abi.TuneReport,
+        "tr_batch_item": _abi.BatchItem,
+        "tr_batch_info": _abi.BatchInfo,
+        "tr_batch_statistics": _abi.BatchStatistics,
     }
     lines = ['#include <stdio.h>', '#include <stddef.h>', f'#include "{HEADER}"', "int main(void){"]
     for cname, py in structs.items():
@@ -110,7 +116,8 @@ def _check_closest(scene, O, D, hits):
         t_got = float(hits[i, 3].view(np.float32))
         t_want = float(want[i, 3].view(np.float32))
         assert abs(t_got - t_want) <= 1e-6 * abs(t_want), (i, hits[i], want[i])
-        assert int(hits[i, 2]) in o.ties(O[i], D[i], 1e-3, t_want)
+        ties = o.ties(O[i], D[i], 1e-3, t_want, with_instances=True)
+        assert (int(hits[i, 1]), int(hits[i, 2])) in ties, (i, hits[i], ties)
     return same.mean()
 
 
@@ -168,3 +175,40 @@ def test_invalid_scene_rejected_by_host_entry():
     hits = np.zeros((1, 4), np.uint32)
     O = np.zeros((1, 4), np.float32)
     assert lib.tr_trace_host(C.byref(h.desc), O.ctypes.data, O.ctypes.data, 1, 1e-3, 0, hits.ctypes.data, None) == 1
+
+
+def test_host_two_level_matches_oracle():
+    """Instances: the instance BVH, then each mesh's BVH in object space (same ray
+    transform and triangle test as the oracle), closest and any hit."""
+    scene = tr.instanced_cornell()
+    rng = np.random.default_rng(11)
+    n = 12000
+    O = np.zeros((n, 4), np.float32)
+    D = np.zeros((n, 4), np.float32)
+    O[:, :3] = rng.uniform(-0.95, 0.95, (n, 3))
+    d = rng.normal(size=(n, 3))
+    D[:, :3] = d / np.linalg.norm(d, axis=1, keepdims=True)
+    for leaf in (1, 3):
+        hits, counts = _host_trace(scene, O, D, leaf=leaf)
+        # the boxes' bottoms lie on the floor: coplanar ties are the only differences
+        assert _check_closest(scene, O, D, hits) > 0.999
+        assert counts[:, 0].min() >= 1
+    inst = hits[hits[:, 2] != 0xFFFFFFFF, 1]
+    assert set(np.unique(inst)) == set(range(len(scene.instances)))  # every instance is hit
+    D[:, 3] = rng.uniform(0.05, 1.5, n).astype(np.float32)
+    hits, _ = _host_trace(scene, O, D, any_hit=True)
+    L = D.copy()
+    L[:, 3] = D[:, 3] + 2e-3
+    occ = Oracle(scene).trace_any(O, L, 1e-3).astype(bool)
+    assert np.mean((hits[:, 2] != 0xFFFFFFFF) == occ) == 1.0
+
+
+def test_two_level_scene_validation():
+    scene = tr.instanced_cornell()
+    scene.instances[3] = (17, scene.instances[3][1])  # a mesh that does not exist
+    O = np.zeros((1, 4), np.float32)
+    D = np.array([[0, 0, 1, 0]], np.float32)
+    hits = np.zeros((1, 4), np.uint32)
+    lib = _abi.load_library()
+    h = SceneDescHolder(scene)
+    assert lib.tr_trace_host(C.byref(h.desc), O.ctypes.data, D.ctypes.data, 1, 1e-3, 0, hits.ctypes.data, None) == 1

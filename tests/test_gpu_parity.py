@@ -72,14 +72,25 @@ def shade_sensitivity(o, st, b, W, H, state, hits, ext64, sh64):
     return sens_e, sens_s
 
 
-def pdf_tolerance(scene, prims):
+def hit_materials(scene, insts, prims):
+    """Material index of hits (instance, triangle of the instance's mesh)."""
+    if getattr(scene, "instances", None) is None:
+        return scene.material_indices[prims]
+    out = np.empty(len(prims), np.int64)
+    for k, (i, p) in enumerate(zip(insts, prims)):
+        mesh = scene.instances[int(i)][0]
+        out[k] = int(scene.mesh_material_offsets[mesh]) + int(scene.meshes[mesh]["material_indices"][int(p)])
+    return out
+
+
+def pdf_tolerance(scene, insts, prims):
     """Relative tolerance of the extend pdf (T.w) of each shaded hit. The GGX distribution is
     evaluated from tan^2(theta) = (1 - cos^2 theta) / cos^2 theta of the sampled microfacet
     normal (Shade/BSDF/Microfacet.h:143-151); cos theta is within a few fp32 ulps, so near the
     peak of a lobe of width alpha the factor 1 + tan^2(theta) / alpha^2 and hence the pdf are only
     defined to about (ulps * 2^-23) / alpha^2 relative, alpha = max(0.001, roughness^2)
     (Microfacet.h:33-36). Allowed: 1e-4 + 32 * 2^-23 / alpha^2 for Disney materials."""
-    m = scene.materials[scene.material_indices[prims]]
+    m = scene.materials[hit_materials(scene, insts, prims)]
     alpha = np.maximum(0.001, m["roughness"].astype(np.float64) ** 2)
     return np.where(m["closure"] == tr.TR_CLOSURE_DISNEY, RTOL + 32 * 2.0 ** -23 / alpha ** 2, RTOL)
 
@@ -92,7 +103,8 @@ def check_hits(o, O, D, got, eps):
         tg = float(got[i, 3].view(np.float32))
         tw = float(want[i, 3].view(np.float32))
         assert abs(tg - tw) <= 1e-6 * abs(tw), f"ray {i}: gpu {got[i]} oracle {want[i]}"
-        assert int(got[i, 2]) in o.ties(O[i], D[i], eps, tw), f"ray {i}: {got[i]} is no near tie of {want[i]}"
+        ties = o.ties(O[i], D[i], eps, tw, with_instances=True)
+        assert (int(got[i, 1]), int(got[i, 2])) in ties, f"ray {i}: {got[i]} is no near tie of {want[i]}"
         ties += 1
     return ties
 
@@ -102,6 +114,8 @@ SCENES = {
     "cornell_reference": lambda: (tr.cornell_box(width=40, height=32), dict(ms=2, reference=True)),
     "heightfield_counter": lambda: (tr.heightfield(n=128, width=64, height=36, rr_start=2),
                                     dict(ms=2, reference=False)),
+    "instanced_counter": lambda: (tr.instanced_cornell(width=48, height=40), dict(ms=2, reference=False)),
+    "instanced_reference": lambda: (tr.instanced_cornell(width=40, height=32), dict(ms=2, reference=True)),
 }
 
 
@@ -174,7 +188,7 @@ def test_stagewise_parity(name):
         okt = within_conditioning(ext_gpu[2][gi, :3], oe[oi, 2, :3], oe64[oi, 2, :3], sens_e[ev][oi, 2, :3]).all(1)
         assert frac(okt) >= 0.998, f"bounce {b}: extend throughputs agree for {frac(okt):.4f}"
         pdf64 = oe64[oi, 2, 3].astype(np.float64)
-        okp = np.abs(ext_gpu[2][gi, 3] - pdf64) <= pdf_tolerance(scene, hits[ev][oi, 2]) * np.maximum(1.0, pdf64)
+        okp = np.abs(ext_gpu[2][gi, 3] - pdf64) <= pdf_tolerance(scene, hits[ev][oi, 1], hits[ev][oi, 2]) * np.maximum(1.0, pdf64)
         assert frac(okp) >= 0.998, f"bounce {b}: extend pdfs agree for {frac(okp):.4f}"
 
         # shadow rays, matched by path index
@@ -213,9 +227,9 @@ def test_stagewise_parity(name):
     r.close()
 
 
-@pytest.mark.parametrize("reference", [False, True])
-def test_frame_parity_per_path(reference):
-    scene = tr.cornell_box(width=64, height=48)
+@pytest.mark.parametrize("reference,two_level", [(False, False), (True, False), (False, True), (True, True)])
+def test_frame_parity_per_path(reference, two_level):
+    scene = tr.instanced_cornell(width=64, height=48) if two_level else tr.cornell_box(width=64, height=48)
     st = tr.settings_for(scene, multi_sample=4, reference=reference)
     r = make_renderer(scene, st)
     r.RenderFrame()

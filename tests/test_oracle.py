@@ -116,6 +116,25 @@ def test_oracle_matches_reference_kernels_live():
     np.testing.assert_allclose(got[:, :3], acc[:, :3].astype(np.float64), rtol=2e-6, atol=1e-6)
 
 
+@pytest.mark.skipif(not reference_available(), reason="reference host build absent (sources not present)")
+def test_oracle_matches_reference_kernels_two_level():
+    """Two-level scene (meshes placed by instances): the reference's kernels read the mesh of
+    the hit instance, its material offset and its inverse transform (CudaMaterial.h:123-211)."""
+    scene = tr.instanced_cornell(wall_closure=tr.TR_CLOSURE_LAMBERT, width=24, height=16)
+    Oracle.set_reference_draw_order(True)
+    ref = Reference(scene)
+    o = Oracle(scene)
+    for ms, tol in ((1, 0.0), (2, 2e-6)):
+        # one sample per pixel: both sum a path's contributions in the same order; two: the
+        # reference adds the samples into float32 pixels, the oracle in double
+        st = _ref_settings(ms, 91)
+        acc = np.zeros((24 * 16, 4), np.float32)
+        ref.render_frame(scene.camera, st, 24, 16, 0, acc)
+        got, _, _ = o.render(scene.camera, st, 24, 16, frames=1, threads=1)
+        np.testing.assert_allclose(got[:, :3], acc[:, :3].astype(np.float64), rtol=tol, atol=tol)
+        assert acc[:, :3].max() > 0
+
+
 def test_counter_rng_properties():
     u = np.concatenate([Oracle.counter_rng(p, s, b, 1, 8) for p in range(64) for s in range(4) for b in range(3)])
     assert u.min() >= 0.0 and u.max() < 1.0

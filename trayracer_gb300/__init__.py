@@ -17,6 +17,7 @@ from .scenes import (  # noqa: F401
     cornell_box,
     displaced_spheres,
     heightfield,
+    instanced_cornell,
     sphere_batch,
     sphere_scene,
 )

@@ -85,6 +85,14 @@ class MeshDesc(C.Structure):
     ]
 
 
+class InstanceDesc(C.Structure):
+    _fields_ = [
+        ("mesh", C.c_uint32),
+        ("reserved", C.c_uint32),
+        ("transform", C.c_float * 12),
+    ]
+
+
 class SceneDesc(C.Structure):
     _fields_ = [
         ("mesh", C.POINTER(MeshDesc)),
@@ -92,6 +100,11 @@ class SceneDesc(C.Structure):
         ("material_count", C.c_uint32),
         ("bvh_leaf_size", C.c_uint32),
         ("build_threads", C.c_uint32),
+        ("instance_count", C.c_uint32),
+        ("meshes", C.POINTER(MeshDesc)),
+        ("mesh_material_offsets", C.c_void_p),
+        ("instances", C.POINTER(InstanceDesc)),
+        ("mesh_count", C.c_uint32),
         ("reserved", C.c_uint32),
     ]
 

@@ -20,6 +20,7 @@
 
 #include "../../include/trayracer.h"
 #include "tr_api_internal.h"
+#include "tr_accel.h"
 #include "tr_bvh.h"
 #include "tr_kernels.h"
 #include "tr_scene.h"
@@ -42,6 +43,41 @@ struct DeviceArena {
 
 inline size_t align256(size_t x) { return (x + 255) & ~size_t(255); }
 
+// A copy of a scene's meshes and instances that outlives tr_scene_upload's
+// arguments (the BVH is rebuilt from it when the leaf size is tuned).
+struct OwnedGeometry {
+    std::vector<std::vector<float>> positions;
+    std::vector<std::vector<uint32_t>> indices;
+    std::vector<tr_mesh_desc> meshes;
+    std::vector<tr_instance_desc> instances;
+    tr_scene_desc desc{};
+
+    void assign(const tr_scene_desc& d)
+    {
+        const uint32_t n = scene_mesh_count(d);
+        positions.assign(n, {});
+        indices.assign(n, {});
+        meshes.assign(n, tr_mesh_desc{});
+        for (uint32_t i = 0; i < n; ++i) {
+            const tr_mesh_desc& m = scene_mesh(d, i);
+            positions[i].assign(m.positions, m.positions + size_t(m.vertex_count) * 3);
+            indices[i].assign(m.indices, m.indices + size_t(m.triangle_count) * 3);
+            meshes[i] = tr_mesh_desc{positions[i].data(), nullptr, nullptr, m.vertex_count, m.triangle_count,
+                                     indices[i].data(), nullptr};
+        }
+        instances.assign(d.instances, d.instances + d.instance_count);
+        desc = tr_scene_desc{};
+        desc.instance_count = d.instance_count;
+        if (d.instance_count) {
+            desc.meshes = meshes.data();
+            desc.mesh_count = n;
+            desc.instances = instances.data();
+        } else {
+            desc.mesh = meshes.data();
+        }
+    }
+};
+
 struct Context {
     int device = 0;
     cudaStream_t stream = nullptr;
@@ -51,8 +87,8 @@ struct Context {
     bool hasScene = false;
     DeviceArena sceneArena;
     DeviceArena bvhArena;          // nodes + traversal triangles (rebuilt when the leaf size is tuned)
-    std::vector<float> hostPositions;
-    std::vector<uint32_t> hostIndices;
+    OwnedGeometry geom;            // host copy of the meshes and instances, for BVH rebuilds
+    std::vector<uint32_t> meshTriBase;
     uint32_t leafSize = 3;
     tr_tuning tuning{};
     SceneView scene{};
@@ -133,43 +169,63 @@ void invalidate_graph(Context* c)
     c->graphValid = false;
 }
 
-// Uploads a CWBVH into its own arena and points the scene view at it.
-tr_status upload_bvh(Context* c, const Cwbvh& wide)
+// Uploads the acceleration structures into their own arena and points the
+// scene view at them.
+tr_status upload_bvh(Context* c, const SceneAccel& acc)
 {
-    const size_t nb = align256(std::max<size_t>(wide.nodes.size() * sizeof(CwbvhNode), 16));
-    const size_t tb = std::max<size_t>(wide.tris.size() * sizeof(float4), 16);
+    size_t off = 0;
+    auto take = [&](size_t bytes) {
+        const size_t o = off;
+        off = align256(off + std::max<size_t>(bytes, 16));
+        return o;
+    };
+    const size_t oN = take(acc.nodes.size() * sizeof(CwbvhNode));
+    const size_t oT = take(acc.tris.size() * sizeof(float4));
+    const size_t oTl = take(acc.tlasNodes.size() * sizeof(CwbvhNode));
+    const size_t oTi = take(acc.tlasInst.size() * sizeof(uint32_t));
+    const size_t oIi = take(acc.instInfo.size() * sizeof(uint2));
     void* base = nullptr;
-    cudaError_t e = cudaMalloc(&base, nb + tb);
+    cudaError_t e = cudaMalloc(&base, off);
     if (e != cudaSuccess)
         return cuda_fail(c, e, "cudaMalloc(bvh)");
     char* b = static_cast<char*>(base);
-    e = cudaMemcpy(b, wide.nodes.data(), wide.nodes.size() * sizeof(CwbvhNode), cudaMemcpyHostToDevice);
-    if (e == cudaSuccess && !wide.tris.empty())
-        e = cudaMemcpy(b + nb, wide.tris.data(), wide.tris.size() * sizeof(float4), cudaMemcpyHostToDevice);
-    if (e != cudaSuccess) {
-        cudaFree(base);
-        return cuda_fail(c, e, "cudaMemcpy(bvh)");
-    }
+    auto up = [&](size_t o, const void* src, size_t bytes) {
+        return bytes ? cudaMemcpy(b + o, src, bytes, cudaMemcpyHostToDevice) : cudaSuccess;
+    };
+    const cudaError_t es[] = {
+        up(oN, acc.nodes.data(), acc.nodes.size() * sizeof(CwbvhNode)),
+        up(oT, acc.tris.data(), acc.tris.size() * sizeof(float4)),
+        up(oTl, acc.tlasNodes.data(), acc.tlasNodes.size() * sizeof(CwbvhNode)),
+        up(oTi, acc.tlasInst.data(), acc.tlasInst.size() * sizeof(uint32_t)),
+        up(oIi, acc.instInfo.data(), acc.instInfo.size() * sizeof(uint2)),
+    };
+    for (cudaError_t x : es)
+        if (x != cudaSuccess) {
+            cudaFree(base);
+            return cuda_fail(c, x, "cudaMemcpy(bvh)");
+        }
     c->bvhArena.release();
     c->bvhArena.base = base;
-    c->bvhArena.bytes = nb + tb;
-    c->scene.nodes = reinterpret_cast<const CwbvhNode*>(b);
-    c->scene.bvhTris = reinterpret_cast<const float4*>(b + nb);
-    c->scene.nodeCount = uint32_t(wide.nodes.size());
-    c->info.bvh_node_count = uint32_t(wide.nodes.size());
+    c->bvhArena.bytes = off;
+    c->scene.nodes = reinterpret_cast<const CwbvhNode*>(b + oN);
+    c->scene.bvhTris = reinterpret_cast<const float4*>(b + oT);
+    c->scene.nodeCount = uint32_t(acc.nodes.size());
+    const bool twoLevel = !acc.tlasNodes.empty();
+    c->scene.tlasNodes = twoLevel ? reinterpret_cast<const CwbvhNode*>(b + oTl) : nullptr;
+    c->scene.tlasInst = twoLevel ? reinterpret_cast<const uint32_t*>(b + oTi) : nullptr;
+    c->scene.instInfo = twoLevel ? reinterpret_cast<const uint2*>(b + oIi) : nullptr;
+    c->info.bvh_node_count = uint32_t(acc.nodes.size() + acc.tlasNodes.size());
     return TR_OK;
 }
 
-// Rebuilds the BVH from the host copy of the mesh with another leaf size.
+// Rebuilds the BVH from the host copy of the geometry with another leaf size.
 tr_status rebuild_bvh(Context* c, uint32_t leafSize)
 {
     if (leafSize == c->leafSize)
         return TR_OK;
     BvhBuildOptions opt;
     opt.maxLeafSize = leafSize;
-    const uint32_t n = uint32_t(c->hostIndices.size() / 3);
-    const BinaryBvh bin = build_binary_bvh(c->hostPositions.data(), c->hostIndices.data(), n, opt);
-    const Cwbvh wide = collapse_to_cwbvh(bin, c->hostPositions.data(), c->hostIndices.data());
+    const SceneAccel wide = build_accel(c->geom.desc, c->meshTriBase, opt);
     if (c->stream)
         cudaStreamSynchronize(c->stream);
     cudaDeviceSynchronize();
@@ -491,9 +547,8 @@ tr_status tr_scene_upload(void* ctx, const tr_scene_desc* desc)
     BvhBuildOptions opt;
     opt.maxLeafSize = desc->bvh_leaf_size ? desc->bvh_leaf_size : 3u;
     opt.threads = desc->build_threads;
-    const tr_mesh_desc& m = *desc->mesh;
-    const BinaryBvh bin = build_binary_bvh(m.positions, m.indices, m.triangle_count, opt);
-    const Cwbvh wide = collapse_to_cwbvh(bin, m.positions, m.indices);
+    const SceneAccel wide = build_accel(*desc, fs.meshTriBase, opt);
+    const uint32_t triCount = uint32_t(fs.tris.size());
     const auto t1 = std::chrono::steady_clock::now();
 
     // one arena for the shading buffers, one for the BVH
@@ -563,14 +618,14 @@ tr_status tr_scene_upload(void* ctx, const tr_scene_desc* desc)
     s.lightCount = int32_t(fs.lights.size());
     s.lightEnergy = fs.lightEnergy;
     s.lightEnergyTotal = fs.lightEnergyTotal;
-    s.triCount = m.triangle_count;
+    s.triCount = triCount;
 
     tr_scene_info& in = c->info;
     in = tr_scene_info{};
-    in.triangle_count = m.triangle_count;
+    in.triangle_count = triCount;
     in.light_count = uint32_t(fs.lights.size());
     in.material_count = desc->material_count;
-    in.bvh_node_count = uint32_t(wide.nodes.size());
+    in.bvh_node_count = uint32_t(wide.nodes.size() + wide.tlasNodes.size());
     in.device_bytes = off + c->bvhArena.bytes;
     in.light_energy = fs.lightEnergyTotal;
     in.build_time_ms = std::chrono::duration<float, std::milli>(t1 - t0).count();
@@ -579,8 +634,8 @@ tr_status tr_scene_upload(void* ctx, const tr_scene_desc* desc)
         in.scene_bounds[i] = fs.bounds[i];
     c->hostLights = fs.lights;
     c->hostMatIdx = fs.matIdx;
-    c->hostPositions.assign(m.positions, m.positions + size_t(m.vertex_count) * 3);
-    c->hostIndices.assign(m.indices, m.indices + size_t(m.triangle_count) * 3);
+    c->geom.assign(*desc);
+    c->meshTriBase = fs.meshTriBase;
     c->leafSize = opt.maxLeafSize;
     c->tuning.bvh_leaf_size = opt.maxLeafSize;
     c->materialCount = desc->material_count;

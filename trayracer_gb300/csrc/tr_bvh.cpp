@@ -193,22 +193,12 @@ inline void set_byte(uint32_t* words, int i, uint32_t v)
 
 } // namespace
 
-BinaryBvh build_binary_bvh(const float* positions, const uint32_t* indices, uint32_t triCount,
-                           const BvhBuildOptions& options)
+namespace {
+
+BinaryBvh build_from_prims(const std::vector<PrimInfo>& prims, const BvhBuildOptions& options)
 {
     BinaryBvh out;
-    std::vector<PrimInfo> prims(triCount);
-    for (uint32_t t = 0; t < triCount; ++t) {
-        PrimInfo& p = prims[t];
-        for (int a = 0; a < 3; ++a) {
-            const float x0 = positions[3 * indices[3 * t + 0] + a];
-            const float x1 = positions[3 * indices[3 * t + 1] + a];
-            const float x2 = positions[3 * indices[3 * t + 2] + a];
-            p.lo[a] = std::min(x0, std::min(x1, x2));
-            p.hi[a] = std::max(x0, std::max(x1, x2));
-            p.c[a] = 0.5f * (p.lo[a] + p.hi[a]);
-        }
-    }
+    const uint32_t triCount = uint32_t(prims.size());
     out.primRefs.resize(triCount);
     for (uint32_t t = 0; t < triCount; ++t)
         out.primRefs[t] = t;
@@ -228,6 +218,38 @@ BinaryBvh build_binary_bvh(const float* positions, const uint32_t* indices, uint
     b.build(0, 0, triCount);
     out.nodes.resize(b.nodeCount.load());
     return out;
+}
+
+} // namespace
+
+BinaryBvh build_binary_bvh(const float* positions, const uint32_t* indices, uint32_t triCount,
+                           const BvhBuildOptions& options)
+{
+    std::vector<PrimInfo> prims(triCount);
+    for (uint32_t t = 0; t < triCount; ++t) {
+        PrimInfo& p = prims[t];
+        for (int a = 0; a < 3; ++a) {
+            const float x0 = positions[3 * indices[3 * t + 0] + a];
+            const float x1 = positions[3 * indices[3 * t + 1] + a];
+            const float x2 = positions[3 * indices[3 * t + 2] + a];
+            p.lo[a] = std::min(x0, std::min(x1, x2));
+            p.hi[a] = std::max(x0, std::max(x1, x2));
+            p.c[a] = 0.5f * (p.lo[a] + p.hi[a]);
+        }
+    }
+    return build_from_prims(prims, options);
+}
+
+BinaryBvh build_binary_bvh_boxes(const Aabb* boxes, uint32_t count, const BvhBuildOptions& options)
+{
+    std::vector<PrimInfo> prims(count);
+    for (uint32_t i = 0; i < count; ++i)
+        for (int a = 0; a < 3; ++a) {
+            prims[i].lo[a] = boxes[i].lo[a];
+            prims[i].hi[a] = boxes[i].hi[a];
+            prims[i].c[a] = 0.5f * (boxes[i].lo[a] + boxes[i].hi[a]);
+        }
+    return build_from_prims(prims, options);
 }
 
 Cwbvh collapse_to_cwbvh(const BinaryBvh& bvh, const float* positions, const uint32_t* indices)
@@ -376,6 +398,10 @@ Cwbvh collapse_to_cwbvh(const BinaryBvh& bvh, const float* positions, const uint
                 set_byte(meta, s, (unary << 5) | offset);
                 for (uint32_t i = 0; i < kid.count; ++i) {
                     const uint32_t prim = bvh.primRefs[kid.left + i];
+                    if (!positions) {  // a BVH over boxes: the leaf slot only names the primitive
+                        out.triPrim.push_back(prim);
+                        continue;
+                    }
                     const float* p0 = positions + 3 * indices[3 * prim + 0];
                     const float* p1 = positions + 3 * indices[3 * prim + 1];
                     const float* p2 = positions + 3 * indices[3 * prim + 2];

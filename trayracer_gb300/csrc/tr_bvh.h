@@ -45,8 +45,14 @@ struct Cwbvh {
 BinaryBvh build_binary_bvh(const float* positions, const uint32_t* indices, uint32_t triCount,
                            const BvhBuildOptions& options);
 
+// Builds a binary BVH over axis-aligned boxes (the instances of a two-level
+// scene).
+BinaryBvh build_binary_bvh_boxes(const Aabb* boxes, uint32_t count, const BvhBuildOptions& options);
+
 // Collapses a binary BVH into the 8-wide compressed layout and packs the
-// traversal triangles (v0, e1 = v1 - v0, e2 = v2 - v0).
+// traversal triangles (v0, e1 = v1 - v0, e2 = v2 - v0). positions == nullptr
+// (a BVH over boxes): no triangles, triPrim names the primitive of each leaf
+// slot.
 Cwbvh collapse_to_cwbvh(const BinaryBvh& bvh, const float* positions, const uint32_t* indices);
 
 } // namespace tr

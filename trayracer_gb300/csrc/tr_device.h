@@ -94,6 +94,11 @@ struct SceneView {
     const LightTri* lights;
     const AliasEntry* alias;
     const float4* invTransforms; // 3 float4 per instance (inverse instance transform rows)
+    // two-level scenes (null for one mesh): BVH over the instances, the instance
+    // of each of its leaf slots, and per instance (BVH root node, first triangle)
+    const CwbvhNode* tlasNodes;
+    const uint32_t* tlasInst;
+    const uint2* instInfo;
     int32_t lightCount;
     float lightEnergy;          // reference: last exclusive prefix (Renderer.cpp:500)
     float lightEnergyTotal;     // sum of all light energies

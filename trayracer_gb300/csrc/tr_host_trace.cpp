@@ -1,13 +1,15 @@
 // Host-side run of the CWBVH build + traversal code of the extend/connect
 // kernels (tr_trace_host): the same node encoding and the same traversal
-// source, compiled for the CPU, so the BVH can be checked without a GPU and
-// the traversal work per ray (nodes visited, triangles tested) can be counted.
+// source (one or two levels), compiled for the CPU, so the BVH can be checked
+// without a GPU and the traversal work per ray (nodes visited, triangles
+// tested) can be counted.
 #include <cuda_runtime.h>
 
 #include <thread>
 #include <vector>
 
 #include "../../include/trayracer.h"
+#include "tr_accel.h"
 #include "tr_bvh.h"
 #include "tr_scene.h"
 #include "tr_traverse.cuh"
@@ -21,17 +23,22 @@ extern "C" tr_status tr_trace_host(const tr_scene_desc* desc, const float* O4, c
         return TR_ERR_INVALID_ARGUMENT;
     if (!validate_scene(*desc).empty())
         return TR_ERR_INVALID_ARGUMENT;
-    const tr_mesh_desc& m = *desc->mesh;
     BvhBuildOptions opt;
     opt.maxLeafSize = desc->bvh_leaf_size ? desc->bvh_leaf_size : 3u;
     opt.threads = desc->build_threads;
-    const BinaryBvh bin = build_binary_bvh(m.positions, m.indices, m.triangle_count, opt);
-    const Cwbvh wide = collapse_to_cwbvh(bin, m.positions, m.indices);
+    const FlatScene fs = flatten_scene(*desc);
+    const SceneAccel acc = build_accel(*desc, fs.meshTriBase, opt);
     SceneView s{};
-    s.nodes = wide.nodes.data();
-    s.bvhTris = wide.tris.data();
-    s.nodeCount = uint32_t(wide.nodes.size());
-    s.triCount = m.triangle_count;
+    s.nodes = acc.nodes.data();
+    s.bvhTris = acc.tris.data();
+    s.nodeCount = uint32_t(acc.nodes.size());
+    s.triCount = uint32_t(fs.tris.size());
+    s.invTransforms = fs.invTransforms.data();
+    if (!acc.tlasNodes.empty()) {
+        s.tlasNodes = acc.tlasNodes.data();
+        s.tlasInst = acc.tlasInst.data();
+        s.instInfo = acc.instInfo.data();
+    }
 
     const unsigned threads = std::max(1u, std::min(16u, std::thread::hardware_concurrency()));
     auto work = [&](unsigned t) {
@@ -42,17 +49,18 @@ extern "C" tr_status tr_trace_host(const tr_scene_desc* desc, const float* O4, c
             uint32_t slot = 0xffffffffu;
             float u = 0.f, v = 0.f;
             TraversalCounts c{0, 0};
+            uint32_t inst = 0;
             if (any_hit)
-                traverse<true, true>(s, O, D, tmin, tmax, slot, u, v, &c);
+                traverse<true, true>(s, O, D, tmin, tmax, slot, u, v, &c, &inst);
             else
-                traverse<false, true>(s, O, D, tmin, tmax, slot, u, v, &c);
+                traverse<false, true>(s, O, D, tmin, tmax, slot, u, v, &c, &inst);
             uint32_t* h = hits + 4 * size_t(i);
             if (slot != 0xffffffffu) {
                 const uint32_t bx = static_cast<uint32_t>(u * 65535.f) & 0xFFFFu;
                 const uint32_t by = static_cast<uint32_t>(v * 65535.f) & 0xFFFFu;
                 h[0] = (bx << 16) | by;
-                h[1] = 0;
-                h[2] = f2u(wide.tris[3 * size_t(slot)].w);
+                h[1] = inst;
+                h[2] = f2u(acc.tris[3 * size_t(slot)].w);
                 h[3] = f2u(tmax);
             } else {
                 h[0] = 0;

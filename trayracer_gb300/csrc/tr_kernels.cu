@@ -294,7 +294,7 @@ constexpr uint32_t kRefillBelow = 24;
 // rendered as a whole, default sampling mode) computes each path's camera ray
 // in place of reading a generated queue, and clears the path's radiance: the
 // primary rays never go through memory.
-template <bool COUNT, bool BATCH, bool PRIMARY>
+template <bool COUNT, bool BATCH, bool PRIMARY, bool TL>
 __global__ void __launch_bounds__(128, 8) extend_kernel(SceneView s, FrameView f, Settings st, uint32_t bounce,
                                                      Camera cam)
 {
@@ -308,7 +308,7 @@ __global__ void __launch_bounds__(128, 8) extend_kernel(SceneView s, FrameView f
     const bool aov = (st.flags & TR_FLAG_WRITE_AOVS) && bounce == 0;
     const uint32_t wh = f.resX * f.resY;
     TraversalCounts cnt{0, 0};
-    Traversal t;
+    typename TravOf<TL>::type t;
     uint2 stack[kTraversalStack];
     float4 O4 = make_float4(0.f, 0.f, 0.f, 0.f), D4 = O4, T4 = O4;
     const uint32_t sc = PRIMARY ? *f.sampleCount : 0u;
@@ -352,17 +352,18 @@ __global__ void __launch_bounds__(128, 8) extend_kernel(SceneView s, FrameView f
             bool done = false;
             if (alive)
                 done = traversal_step<false, COUNT>(t, stack, s, &cnt);
-            const bool hit = done && t.hitSlot != 0xffffffffu;
+            const bool hit = done && base(t).hitSlot != 0xffffffffu;
             const uint32_t slot = warp_append(hitCounter, hit);
             if (done) {
-                if (!t.ok)
+                if (!base(t).ok)
                     atomicOr(f.errorFlag, 1u);
                 if (hit) {
-                    const uint32_t prim = __float_as_uint(__ldg(s.bvhTris + 3u * t.hitSlot).w);
+                    const uint32_t prim = __float_as_uint(__ldg(s.bvhTris + 3u * base(t).hitSlot).w);
                     __stcs(hq + slot, O4);
                     __stcs(hq + slot + cap, D4);
                     __stcs(hq + slot + 2 * cap, T4);
-                    __stcs(f.hits + slot, make_uint4(encode_bary(t.u, t.v), 0u, prim, __float_as_uint(t.tmax)));
+                    __stcs(f.hits + slot, make_uint4(encode_bary(base(t).u, base(t).v), hit_instance(t), prim,
+                                                     __float_as_uint(base(t).tmax)));
                 } else if (aov) {
                     // a primary miss sees the (disabled) sky: black guide values (PathTracing.h:48-52)
                     const uint32_t pathIx = path_ix(__float_as_uint(O4.w));
@@ -477,8 +478,10 @@ __device__ __forceinline__ Surface surface_at(const SceneView& s, uint32_t instI
                                               const float3& D)
 {
     Surface sf;
-    const TriShade& tri = s.tris[primIx];
-    sf.matIx = __ldg(s.matIdx + primIx);
+    // two-level scenes: primIx counts in the instance's mesh
+    const uint32_t triIx = (s.instInfo ? __ldg(&s.instInfo[instIx].y) : 0u) + primIx;
+    const TriShade& tri = s.tris[triIx];
+    sf.matIx = __ldg(s.matIdx + triIx);
     const float3 v0 = make_float3(tri.v0x, tri.v0y, tri.v0z);
     const float3 v1 = make_float3(tri.v1x, tri.v1y, tri.v1z);
     const float3 v2 = make_float3(tri.v2x, tri.v2y, tri.v2z);
@@ -857,7 +860,7 @@ __global__ void __launch_bounds__(256) sort_scatter_kernel(FrameView f, SortView
 
 // Any hit of the bounce's shadow queue over [eps, dist - 2 eps]; an unoccluded
 // ray adds its radiance to its path. Same lane refill as extend_kernel.
-template <bool COUNT, bool BATCH>
+template <bool COUNT, bool BATCH, bool TL>
 __global__ void __launch_bounds__(128) connect_kernel(SceneView s, FrameView f, Settings st, uint32_t bounce)
 {
     const uint32_t count = __ldcg(f.counters + kShadowCounterBase + bounce);
@@ -865,7 +868,7 @@ __global__ void __launch_bounds__(128) connect_kernel(SceneView s, FrameView f, 
     uint32_t* work = f.counters + kConnectWorkBase + bounce;
     const uint32_t lane = lane_id();
     TraversalCounts cnt{0, 0};
-    Traversal t;
+    typename TravOf<TL>::type t;
     uint2 stack[kTraversalStack];
     uint32_t ray = 0, pathIx = 0;
     bool alive = false, more = true;
@@ -897,9 +900,9 @@ __global__ void __launch_bounds__(128) connect_kernel(SceneView s, FrameView f, 
         uint32_t active;
         do {
             if (alive && traversal_step<true, COUNT>(t, stack, s, &cnt)) {
-                if (!t.ok)
+                if (!base(t).ok)
                     atomicOr(f.errorFlag, 1u);
-                if (t.hitSlot == 0xffffffffu) {
+                if (base(t).hitSlot == 0xffffffffu) {
                     const float4 T4 = __ldcs(f.shadow + ray + 2 * cap);
                     float4 r = f.radiance[pathIx];
                     f.radiance[pathIx] = make_float4(r.x + T4.x, r.y + T4.y, r.z + T4.z, r.w);
@@ -1245,6 +1248,7 @@ __global__ void __launch_bounds__(kAdjointThreads, 4) adjoint_shade_kernel(Scene
 // Visibility of the replay's NEE rays (as connect_kernel): an unoccluded ray
 // takes its contribution off the path's remaining radiance and is listed for
 // nee_grad_kernel.
+template <bool TL>
 __global__ void __launch_bounds__(128) adjoint_connect_kernel(SceneView s, FrameView f, Settings st, uint32_t bounce,
                                                               AdjointView a)
 {
@@ -1253,7 +1257,7 @@ __global__ void __launch_bounds__(128) adjoint_connect_kernel(SceneView s, Frame
     uint32_t* work = f.counters + kConnectWorkBase + bounce;
     uint32_t* visCounter = f.counters + kVisibleCounterBase + bounce;
     const uint32_t lane = lane_id();
-    Traversal t;
+    typename TravOf<TL>::type t;
     uint2 stack[kTraversalStack];
     uint32_t ray = 0, pathIx = 0;
     bool alive = false, more = true;
@@ -1285,9 +1289,9 @@ __global__ void __launch_bounds__(128) adjoint_connect_kernel(SceneView s, Frame
         do {
             bool visible = false;
             if (alive && traversal_step<true, false>(t, stack, s, nullptr)) {
-                if (!t.ok)
+                if (!base(t).ok)
                     atomicOr(f.errorFlag, 1u);
-                if (t.hitSlot == 0xffffffffu) {
+                if (base(t).hitSlot == 0xffffffffu) {
                     const float4 T4 = __ldcs(f.shadow + ray + 2 * cap);
                     const float4 r = a.lrem[pathIx];
                     a.lrem[pathIx] = make_float4(r.x - T4.x, r.y - T4.y, r.z - T4.z, r.w);
@@ -1380,16 +1384,22 @@ void launch_extend_variant(const SceneView& s, const FrameView& f, const Setting
                            const Camera& cam, const LaunchShape& shape, cudaStream_t stream)
 {
     const bool count = (st.flags & TR_FLAG_COUNT_TRAVERSAL) != 0;
+    const uint32_t g = shape.extendBlocks;
     if (f.segments) {
         if (count)
-            extend_kernel<true, true, PRIMARY><<<shape.extendBlocks, 128, 0, stream>>>(s, f, st, bounce, cam);
+            extend_kernel<true, true, PRIMARY, false><<<g, 128, 0, stream>>>(s, f, st, bounce, cam);
         else
-            extend_kernel<false, true, PRIMARY><<<shape.extendBlocks, 128, 0, stream>>>(s, f, st, bounce, cam);
+            extend_kernel<false, true, PRIMARY, false><<<g, 128, 0, stream>>>(s, f, st, bounce, cam);
+    } else if (s.tlasNodes) {
+        if (count)
+            extend_kernel<true, false, PRIMARY, true><<<g, 128, 0, stream>>>(s, f, st, bounce, cam);
+        else
+            extend_kernel<false, false, PRIMARY, true><<<g, 128, 0, stream>>>(s, f, st, bounce, cam);
     } else {
         if (count)
-            extend_kernel<true, false, PRIMARY><<<shape.extendBlocks, 128, 0, stream>>>(s, f, st, bounce, cam);
+            extend_kernel<true, false, PRIMARY, false><<<g, 128, 0, stream>>>(s, f, st, bounce, cam);
         else
-            extend_kernel<false, false, PRIMARY><<<shape.extendBlocks, 128, 0, stream>>>(s, f, st, bounce, cam);
+            extend_kernel<false, false, PRIMARY, false><<<g, 128, 0, stream>>>(s, f, st, bounce, cam);
     }
 }
 
@@ -1423,16 +1433,22 @@ cudaError_t launch_connect(const SceneView& s, const FrameView& f, const Setting
     Settings st = st0;
     st.refillBelow = shape.refillBelow;
     const bool count = (st.flags & TR_FLAG_COUNT_TRAVERSAL) != 0;
+    const uint32_t g = shape.connectBlocks;
     if (f.segments) {
         if (count)
-            connect_kernel<true, true><<<shape.connectBlocks, 128, 0, stream>>>(s, f, st, bounce);
+            connect_kernel<true, true, false><<<g, 128, 0, stream>>>(s, f, st, bounce);
         else
-            connect_kernel<false, true><<<shape.connectBlocks, 128, 0, stream>>>(s, f, st, bounce);
+            connect_kernel<false, true, false><<<g, 128, 0, stream>>>(s, f, st, bounce);
+    } else if (s.tlasNodes) {
+        if (count)
+            connect_kernel<true, false, true><<<g, 128, 0, stream>>>(s, f, st, bounce);
+        else
+            connect_kernel<false, false, true><<<g, 128, 0, stream>>>(s, f, st, bounce);
     } else {
         if (count)
-            connect_kernel<true, false><<<shape.connectBlocks, 128, 0, stream>>>(s, f, st, bounce);
+            connect_kernel<true, false, false><<<g, 128, 0, stream>>>(s, f, st, bounce);
         else
-            connect_kernel<false, false><<<shape.connectBlocks, 128, 0, stream>>>(s, f, st, bounce);
+            connect_kernel<false, false, false><<<g, 128, 0, stream>>>(s, f, st, bounce);
     }
     return cudaGetLastError();
 }
@@ -1470,7 +1486,12 @@ cudaError_t launch_adjoint(const SceneView& s, const FrameView& f, const Camera&
     fwd.refillBelow = shape.refillBelow;
     adjoint_generate_kernel<<<(f.pathCount + 255u) / 256u, 256, 0, stream>>>(f, cam, fwd, a);
     for (uint32_t bounce = 0; bounce < st.maxDepth; ++bounce) {
-        extend_kernel<false, false, false><<<shape.extendBlocks, 128, 0, stream>>>(s, f, fwd, bounce, Camera{});
+        if (s.tlasNodes)
+            extend_kernel<false, false, false, true><<<shape.extendBlocks, 128, 0, stream>>>(s, f, fwd, bounce,
+                                                                                          Camera{});
+        else
+            extend_kernel<false, false, false, false><<<shape.extendBlocks, 128, 0, stream>>>(s, f, fwd, bounce,
+                                                                                           Camera{});
         if (bounce > 0) {
             if (useSmem)
                 ext_grad_kernel<true><<<gradBlocks, kAdjointThreads, smem, stream>>>(s, f, bounce, a);
@@ -1481,7 +1502,10 @@ cudaError_t launch_adjoint(const SceneView& s, const FrameView& f, const Camera&
             adjoint_shade_kernel<true><<<gradBlocks, kAdjointThreads, smem, stream>>>(s, f, fwd, bounce, a);
         else
             adjoint_shade_kernel<false><<<gradBlocks, kAdjointThreads, 0, stream>>>(s, f, fwd, bounce, a);
-        adjoint_connect_kernel<<<shape.connectBlocks, 128, 0, stream>>>(s, f, fwd, bounce, a);
+        if (s.tlasNodes)
+            adjoint_connect_kernel<true><<<shape.connectBlocks, 128, 0, stream>>>(s, f, fwd, bounce, a);
+        else
+            adjoint_connect_kernel<false><<<shape.connectBlocks, 128, 0, stream>>>(s, f, fwd, bounce, a);
         if (useSmem)
             nee_grad_kernel<true><<<gradBlocks, kAdjointThreads, smem, stream>>>(s, f, bounce, a);
         else
@@ -1524,10 +1548,10 @@ LaunchShape default_launch_shape(int device, uint32_t capacity)
     if (sms <= 0)
         sms = 1;
     int perSm = 0;
-    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&perSm, extend_kernel<false, false, false>, 128, 0);
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&perSm, extend_kernel<false, false, false, false>, 128, 0);
     shape.extendBlocks = uint32_t(sms) * uint32_t(perSm > 0 ? perSm : 4);
     perSm = 0;
-    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&perSm, connect_kernel<false, false>, 128, 0);
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&perSm, connect_kernel<false, false, false>, 128, 0);
     shape.connectBlocks = uint32_t(sms) * uint32_t(perSm > 0 ? perSm : 4);
     perSm = 0;
     cudaOccupancyMaxActiveBlocksPerMultiprocessor(&perSm, shade_kernel<false, false>, 128, 0);

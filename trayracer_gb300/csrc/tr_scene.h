@@ -10,8 +10,10 @@
 namespace tr {
 
 struct FlatScene {
-    std::vector<TriShade> tris;        // by triangle index
-    std::vector<uint32_t> matIdx;      // by triangle index
+    std::vector<TriShade> tris;        // by triangle index (two-level: meshes concatenated, object space)
+    std::vector<uint32_t> matIdx;      // by triangle index (two-level: mesh material offset added)
+    std::vector<uint32_t> meshTriBase; // two-level: first triangle of each mesh
+    std::vector<uint32_t> instMesh;    // two-level: mesh of each instance
     std::vector<Material> materials;
     std::vector<LightTri> lights;
     std::vector<AliasEntry> alias;
@@ -30,6 +32,19 @@ std::string validate_scene(const tr_scene_desc& desc);
 // (Tracer/Resources/Material.cpp:56-78) for one mesh with one identity
 // instance, plus the light alias table.
 FlatScene flatten_scene(const tr_scene_desc& desc);
+
+// The mesh of a one-level scene, or mesh i of a two-level one.
+inline const tr_mesh_desc& scene_mesh(const tr_scene_desc& d, uint32_t i)
+{
+    return d.instance_count ? d.meshes[i] : *d.mesh;
+}
+inline uint32_t scene_mesh_count(const tr_scene_desc& d) { return d.instance_count ? d.mesh_count : 1u; }
+
+// Inverse of an affine 3x4 (rows r.x, r.y, r.z, t), the formula of the
+// reference's inverse(float3x4) (Tracer/Utility/LinearMath.h:472-506).
+void inverse_3x4(const float* m, float* out);
+// R p + t for an instance transform's rows (r | t).
+float3 place_point(const float* m, const float3& p);
 
 // Resolves one material as GetIntersectionAttributes does per hit
 // (Tracer/CUDA/GPU/CudaMaterial.h:171-183): fp16-rounded properties,

@@ -331,35 +331,48 @@ TR_HD void traversal_begin(Traversal& t, const float3& O, const float3& D, float
 // triangles it reports, then a stack pop if the group is exhausted. Returns
 // true when the ray is finished (t.hitSlot, t.tmax, t.u, t.v hold the result;
 // t.ok is false if a bound was exceeded).
-template <bool ANY, bool COUNT>
-TR_HD bool traversal_step(Traversal& t, uint2* stack, const SceneView& s, TraversalCounts* cnt)
+// The next hit child node of the current group, intersected: the group
+// becomes its internal children (the rest of the old group waits on the
+// stack); returns its leaf group (base, bits). Returns false when a bound ran
+// out (t.ok cleared).
+template <bool COUNT>
+TR_HD bool node_step(Traversal& t, uint2* stack, const CwbvhNode* __restrict__ nodes, TraversalCounts* cnt,
+                     uint2& leaves)
 {
-    uint2 tris = make_uint2(0u, 0u);
+    leaves = make_uint2(0u, 0u);
+    if (t.group.y <= 0x00ffffffu)
+        return true;
+    const uint32_t hits = t.group.y;
+    const uint32_t bit = 31u - clz32(hits);
+    t.group.y &= ~(1u << bit);
+    const uint32_t slot = (bit - 24u) ^ t.octInv;
+    const uint32_t rel = popc32(hits & 0xffu & ((1u << slot) - 1u));
+    const uint32_t nodeIx = t.group.x + rel;
     if (t.group.y > 0x00ffffffu) {
-        const uint32_t hits = t.group.y;
-        const uint32_t bit = 31u - clz32(hits);
-        t.group.y &= ~(1u << bit);
-        const uint32_t slot = (bit - 24u) ^ t.octInv;
-        const uint32_t rel = popc32(hits & 0xffu & ((1u << slot) - 1u));
-        const uint32_t nodeIx = t.group.x + rel;
-        if (t.group.y > 0x00ffffffu) {
-            if (t.sp < kTraversalStack)
-                stack[t.sp++] = t.group;
-            else
-                t.ok = false;
-        }
-        uint32_t childBase, triBase, imask;
-        const uint32_t hm =
-            intersect_node(s.nodes, nodeIx, t.O, t.invD, t.octInv, t.tmin, t.tmax, childBase, triBase, imask);
-        if (COUNT)
-            cnt->nodes++;
-        t.group = make_uint2(childBase, (hm & 0xff000000u) | imask);
-        tris = make_uint2(triBase, hm & 0x00ffffffu);
-        if (++t.steps > kMaxTraversalSteps) {
+        if (t.sp < kTraversalStack)
+            stack[t.sp++] = t.group;
+        else
             t.ok = false;
-            return true;
-        }
     }
+    uint32_t childBase, triBase, imask;
+    const uint32_t hm = intersect_node(nodes, nodeIx, t.O, t.invD, t.octInv, t.tmin, t.tmax, childBase, triBase, imask);
+    if (COUNT)
+        cnt->nodes++;
+    t.group = make_uint2(childBase, (hm & 0xff000000u) | imask);
+    leaves = make_uint2(triBase, hm & 0x00ffffffu);
+    if (++t.steps > kMaxTraversalSteps) {
+        t.ok = false;
+        return false;
+    }
+    return true;
+}
+
+// Tests the triangles of a leaf group. Returns 2 when an any-hit ray found
+// its hit, 1 when a closer hit was recorded, 0 otherwise.
+template <bool ANY, bool COUNT>
+TR_HD int leaf_triangles(Traversal& t, uint2 tris, const SceneView& s, TraversalCounts* cnt)
+{
+    int found = 0;
     while (tris.y != 0u) {
         const uint32_t k = ffs32(tris.y) - 1u;
         tris.y &= tris.y - 1u;
@@ -375,16 +388,32 @@ TR_HD bool traversal_step(Traversal& t, uint2* stack, const SceneView& s, Traver
             if (ANY) {
                 t.tmax = tt;
                 t.hitSlot = slot;
-                return true;
+                return 2;
             }
             if (tt < t.tmax || t.hitSlot == 0xffffffffu) {
                 t.tmax = tt;
                 t.hitSlot = slot;
                 t.u = uu;
                 t.v = vv;
+                found = 1;
             }
         }
     }
+    return found;
+}
+
+// One step: the next hit child node of the current group with the leaf
+// triangles it reports, then a stack pop if the group is exhausted. Returns
+// true when the ray is finished (t.hitSlot, t.tmax, t.u, t.v hold the result;
+// t.ok is false if a bound was exceeded).
+template <bool ANY, bool COUNT>
+TR_HD bool traversal_step(Traversal& t, uint2* stack, const SceneView& s, TraversalCounts* cnt)
+{
+    uint2 tris;
+    if (!node_step<COUNT>(t, stack, s.nodes, cnt, tris))
+        return true;
+    if (leaf_triangles<ANY, COUNT>(t, tris, s, cnt) == 2)
+        return true;
     if (t.group.y <= 0x00ffffffu) {
         if (t.sp == 0)
             return true;
@@ -393,23 +422,179 @@ TR_HD bool traversal_step(Traversal& t, uint2* stack, const SceneView& s, Traver
     return false;
 }
 
-// Traverses the CWBVH to the end. ANY = true stops at the first hit inside
-// [tmin, tmax]. Returns false when a bound (stack depth, step count) was
-// exceeded; the hit reported so far is kept. COUNT adds the nodes and
-// triangles visited to *cnt.
+// Instance transforms applied to a ray: rows (r | t) of the inverse instance
+// transform, ((r.x p.x + r.y p.y) + r.z p.z) + t with every operation rounded
+// on its own (the oracle applies the same sequence).
+TR_HD float3 xform_point(const float4& r0, const float4& r1, const float4& r2, const float3& p)
+{
+    return make_float3(add_rn(add_rn(add_rn(mul_rn(r0.x, p.x), mul_rn(r0.y, p.y)), mul_rn(r0.z, p.z)), r0.w),
+                       add_rn(add_rn(add_rn(mul_rn(r1.x, p.x), mul_rn(r1.y, p.y)), mul_rn(r1.z, p.z)), r1.w),
+                       add_rn(add_rn(add_rn(mul_rn(r2.x, p.x), mul_rn(r2.y, p.y)), mul_rn(r2.z, p.z)), r2.w));
+}
+TR_HD float3 xform_vector(const float4& r0, const float4& r1, const float4& r2, const float3& v)
+{
+    return make_float3(add_rn(add_rn(mul_rn(r0.x, v.x), mul_rn(r0.y, v.y)), mul_rn(r0.z, v.z)),
+                       add_rn(add_rn(mul_rn(r1.x, v.x), mul_rn(r1.y, v.y)), mul_rn(r1.z, v.z)),
+                       add_rn(add_rn(mul_rn(r2.x, v.x), mul_rn(r2.y, v.y)), mul_rn(r2.z, v.z)));
+}
+
+TR_HD void set_ray(Traversal& t, const float3& O, const float3& D)
+{
+    const float kTiny = 1e-20f;
+    t.O = O;
+    t.D = D;
+    t.invD = make_float3(1.0f / (fabsf(D.x) > kTiny ? D.x : copysignf(kTiny, D.x)),
+                         1.0f / (fabsf(D.y) > kTiny ? D.y : copysignf(kTiny, D.y)),
+                         1.0f / (fabsf(D.z) > kTiny ? D.z : copysignf(kTiny, D.z)));
+    const uint32_t octant = (t.invD.x < 0.f ? 1u : 0u) | (t.invD.y < 0.f ? 2u : 0u) | (t.invD.z < 0.f ? 4u : 0u);
+    t.octInv = 7u - octant;
+}
+
+// Two-level traversal (the instance BVH, then the BVH of each instance's mesh
+// in object space; replaces OptiX's instance acceleration structure). The
+// object-space ray keeps the world ray's parameter t, so t and tmax compare
+// across instances.
+constexpr uint32_t kNoInstance = 0xffffffffu;
+
+struct TraversalTL {
+    Traversal t;          // the current ray (world at the top level, object space inside an instance)
+    float3 wO, wD, wInvD;
+    uint32_t wOctInv;
+    uint32_t inst;        // instance being traversed, kNoInstance at the top level
+    int instSp;           // stack depth when it was entered
+    uint2 leafGroup;      // top level: instances of a reached leaf group still to enter
+    uint32_t hitInst;     // instance of the recorded hit
+};
+
+TR_HD void traversal_begin(TraversalTL& r, const float3& O, const float3& D, float tmin, float tmax, uint32_t = 0)
+{
+    traversal_begin(r.t, O, D, tmin, tmax, 0u);
+    r.wO = O;
+    r.wD = D;
+    r.wInvD = r.t.invD;
+    r.wOctInv = r.t.octInv;
+    r.inst = kNoInstance;
+    r.instSp = -1;
+    r.leafGroup = make_uint2(0u, 0u);
+    r.hitInst = kNoInstance;
+}
+
+template <bool ANY, bool COUNT>
+TR_HD bool traversal_step(TraversalTL& r, uint2* stack, const SceneView& s, TraversalCounts* cnt)
+{
+    Traversal& t = r.t;
+    if (r.inst == kNoInstance && r.leafGroup.y != 0u) {
+        // enter the next instance of a top-level leaf group; the rest of the
+        // group and the node group being walked wait on the stack
+        const uint32_t k = ffs32(r.leafGroup.y) - 1u;
+        const uint32_t rest = r.leafGroup.y & (r.leafGroup.y - 1u);
+        const uint32_t id = ldg(s.tlasInst + r.leafGroup.x + k);
+        const uint32_t need = (t.group.y > 0x00ffffffu ? 1 : 0) + (rest ? 1 : 0);
+        if (t.sp + int(need) > kTraversalStack) {
+            t.ok = false;
+            return true;
+        }
+        if (t.group.y > 0x00ffffffu)
+            stack[t.sp++] = t.group;
+        if (rest)
+            stack[t.sp++] = make_uint2(r.leafGroup.x, rest);
+        r.leafGroup = make_uint2(0u, 0u);
+        const float4 r0 = ldg(s.invTransforms + 3u * id + 0u);
+        const float4 r1 = ldg(s.invTransforms + 3u * id + 1u);
+        const float4 r2 = ldg(s.invTransforms + 3u * id + 2u);
+        set_ray(t, xform_point(r0, r1, r2, r.wO), xform_vector(r0, r1, r2, r.wD));
+        r.inst = id;
+        r.instSp = t.sp;
+        t.group = make_uint2(ldg(&s.instInfo[id].x), 0x80000000u);
+        if (++t.steps > kMaxTraversalSteps) {
+            t.ok = false;
+            return true;
+        }
+        return false;
+    }
+    const bool top = r.inst == kNoInstance;
+    uint2 leaves;
+    if (!node_step<COUNT>(t, stack, top ? s.tlasNodes : s.nodes, cnt, leaves))
+        return true;
+    if (top) {
+        r.leafGroup = leaves;  // entered one by one in the next steps
+    } else {
+        const int found = leaf_triangles<ANY, COUNT>(t, leaves, s, cnt);
+        if (found)
+            r.hitInst = r.inst;
+        if (found == 2)
+            return true;
+    }
+    if (t.group.y <= 0x00ffffffu && r.leafGroup.y == 0u) {
+        if (r.inst != kNoInstance && t.sp == r.instSp) {
+            // the instance is done: back to the world ray at the top level
+            t.O = r.wO;
+            t.D = r.wD;
+            t.invD = r.wInvD;
+            t.octInv = r.wOctInv;
+            r.inst = kNoInstance;
+            r.instSp = -1;
+        }
+        if (t.sp == 0)
+            return true;
+        const uint2 e = stack[--t.sp];
+        if (r.inst == kNoInstance && e.y <= 0x00ffffffu) {
+            r.leafGroup = e;
+            t.group = make_uint2(0u, 0u);
+        } else {
+            t.group = e;
+        }
+    }
+    return false;
+}
+
+template <bool TL>
+struct TravOf {
+    using type = Traversal;
+};
+template <>
+struct TravOf<true> {
+    using type = TraversalTL;
+};
+
+// The result fields of either traversal.
+TR_HD const Traversal& base(const Traversal& t) { return t; }
+TR_HD const Traversal& base(const TraversalTL& r) { return r.t; }
+TR_HD uint32_t hit_instance(const Traversal&) { return 0u; }
+TR_HD uint32_t hit_instance(const TraversalTL& r) { return r.hitInst; }
+
+// Traverses to the end (two levels when the scene has an instance BVH).
+// ANY = true stops at the first hit inside [tmin, tmax]. Returns false when a
+// bound (stack depth, step count) was exceeded; the hit reported so far is
+// kept. COUNT adds the nodes and triangles visited to *cnt.
 template <bool ANY, bool COUNT = false>
 TR_HD bool traverse(const SceneView& s, const float3& O, const float3& D, float tmin, float& tmax, uint32_t& hitSlot,
-                    float& hu, float& hv, TraversalCounts* cnt = nullptr)
+                    float& hu, float& hv, TraversalCounts* cnt = nullptr, uint32_t* hitInst = nullptr)
 {
+    uint2 stack[kTraversalStack];
+    if (s.tlasNodes) {
+        TraversalTL r;
+        traversal_begin(r, O, D, tmin, tmax);
+        while (!traversal_step<ANY, COUNT>(r, stack, s, cnt)) {
+        }
+        tmax = r.t.tmax;
+        hitSlot = r.t.hitSlot;
+        hu = r.t.u;
+        hv = r.t.v;
+        if (hitInst)
+            *hitInst = r.hitInst;
+        return r.t.ok;
+    }
     Traversal t;
     traversal_begin(t, O, D, tmin, tmax);
-    uint2 stack[kTraversalStack];
     while (!traversal_step<ANY, COUNT>(t, stack, s, cnt)) {
     }
     tmax = t.tmax;
     hitSlot = t.hitSlot;
     hu = t.u;
     hv = t.v;
+    if (hitInst)
+        *hitInst = 0u;
     return t.ok;
 }
 

@@ -103,6 +103,31 @@ class SceneDescHolder:
         )
         self.desc = _abi.SceneDesc(C.pointer(self.mesh), C.cast(self.mats.ctypes.data, C.POINTER(_abi.MaterialDesc)),
                                    self.mats.shape[0], leaf_size, build_threads, 0)
+        inst = getattr(scene, "instances", None)
+        if inst is not None:
+            # two-level scene: meshes placed by instances
+            self.meshes = (_abi.MeshDesc * len(scene.meshes))()
+            self.mesh_arrays = []
+            for i, m in enumerate(scene.meshes):
+                arrs = [np.ascontiguousarray(m["positions"], np.float32),
+                        None if m.get("normals") is None else np.ascontiguousarray(m["normals"], np.float32),
+                        None if m.get("texcoords") is None else np.ascontiguousarray(m["texcoords"], np.float32),
+                        np.ascontiguousarray(m["indices"], np.uint32),
+                        np.ascontiguousarray(m["material_indices"], np.uint32)]
+                self.mesh_arrays.append(arrs)
+                self.meshes[i] = _abi.MeshDesc(arrs[0].ctypes.data, None if arrs[1] is None else arrs[1].ctypes.data,
+                                               None if arrs[2] is None else arrs[2].ctypes.data, arrs[0].shape[0],
+                                               arrs[3].shape[0], arrs[3].ctypes.data, arrs[4].ctypes.data)
+            self.offsets = np.ascontiguousarray(scene.mesh_material_offsets, np.uint32)
+            self.inst = (_abi.InstanceDesc * len(inst))()
+            for i, (mesh_ix, xf) in enumerate(inst):
+                self.inst[i].mesh = int(mesh_ix)
+                self.inst[i].transform[:] = [float(x) for x in np.asarray(xf, np.float32).reshape(12)]
+            self.desc.instance_count = len(inst)
+            self.desc.meshes = C.cast(self.meshes, C.POINTER(_abi.MeshDesc))
+            self.desc.mesh_material_offsets = self.offsets.ctypes.data
+            self.desc.instances = C.cast(self.inst, C.POINTER(_abi.InstanceDesc))
+            self.desc.mesh_count = len(scene.meshes)
 
     def ptr(self):
         return C.byref(self.desc)

@@ -114,6 +114,40 @@ class Scene:
         return h.hexdigest()[:16]
 
 
+@dataclass
+class InstancedScene(Scene):
+    """A two-level scene: meshes (dicts of positions, normals, texcoords, indices, material_indices),
+    a material offset per mesh (the reference's MaterialOffsets) and instances (mesh index, 3x4
+    object-to-world rows (r | t)). The one-mesh fields hold mesh 0."""
+
+    meshes: list = field(default_factory=list)
+    mesh_material_offsets: np.ndarray | None = None
+    instances: list = field(default_factory=list)
+
+    @property
+    def triangle_count(self) -> int:
+        return int(sum(m["indices"].shape[0] for m in self.meshes))
+
+    def digest(self) -> str:
+        h = hashlib.sha256(super().digest().encode())
+        for m in self.meshes:
+            for k in ("positions", "normals", "texcoords", "indices", "material_indices"):
+                if m.get(k) is not None:
+                    h.update(np.ascontiguousarray(m[k]).tobytes())
+        h.update(np.ascontiguousarray(self.mesh_material_offsets, np.uint32).tobytes())
+        for mi, xf in self.instances:
+            h.update(np.uint32(mi).tobytes())
+            h.update(np.asarray(xf, np.float32).tobytes())
+        return h.hexdigest()[:16]
+
+
+def placement(cos_y: float = 1.0, sin_y: float = 0.0, scale: float = 1.0, translate=(0.0, 0.0, 0.0)):
+    """Rows (r | t) of a rotation about y (cos, sin given), a uniform scale and a translation."""
+    c, s_, k = np.float32(cos_y), np.float32(sin_y), np.float32(scale)
+    tx, ty, tz = (np.float32(v) for v in translate)
+    return np.array([[k * c, 0, k * s_, tx], [0, k, 0, ty], [-k * s_, 0, k * c, tz]], np.float32)
+
+
 class _Builder:
     def __init__(self):
         self.pos, self.nrm, self.uv, self.idx, self.mat = [], [], [], [], []
@@ -197,6 +231,72 @@ def cornell_box(seed: int = 1, width: int = 256, height: int = 256, spp: int = 1
         mats["closure"] = TR_CLOSURE_LAMBERT
     return Scene("cornell_box", pos, nrm, uv, idx, mat, mats, CameraSpec(), width, height, spp, max_depth, 1 << 30,
                  seed)
+
+
+def instanced_cornell(seed: int = 3, width: int = 64, height: int = 48, spp: int = 4, max_depth: int = 5,
+                      wall_closure: int = TR_CLOSURE_DIFFUSE) -> InstancedScene:
+    """A two-level Cornell box: the room (5 quads, identity instance), two unit-box meshes placed
+    three times (rotated about y, scaled, translated), a sphere mesh placed twice and a quad light
+    mesh placed twice (translations only: the reference places light triangles with the transpose
+    of the instance rotation, Scene.cpp:288-291, which agrees with the geometry only then)."""
+    rng = np.random.default_rng(seed)
+    mats = []
+    meshes = []
+    offsets = []
+
+    def mesh_from(builder, local_mats):
+        pos, nrm, uv, idx, mat = builder.arrays()
+        offsets.append(len(mats))
+        mats.extend(local_mats)
+        meshes.append(dict(positions=pos, normals=nrm, texcoords=uv, indices=idx, material_indices=mat))
+
+    room = _Builder()
+    walls = [
+        ([(-1, -1, -1), (1, -1, -1), (1, -1, 1), (-1, -1, 1)], (0, 1, 0)),
+        ([(-1, 1, 1), (1, 1, 1), (1, 1, -1), (-1, 1, -1)], (0, -1, 0)),
+        ([(-1, -1, 1), (1, -1, 1), (1, 1, 1), (-1, 1, 1)], (0, 0, -1)),
+        ([(-1, -1, -1), (-1, -1, 1), (-1, 1, 1), (-1, 1, -1)], (1, 0, 0)),
+        ([(1, -1, 1), (1, -1, -1), (1, 1, -1), (1, 1, 1)], (-1, 0, 0)),
+    ]
+    wall_mats = []
+    for k, (corners, normal) in enumerate(walls):
+        wall_mats.append(material(diffuse=rng.uniform(0.2, 0.8, 3).astype(np.float32), closure=wall_closure))
+        room.quad(corners, normal, k)
+    mesh_from(room, wall_mats)
+    for closure, kw in ((wall_closure, dict(diffuse=rng.uniform(0.2, 0.8, 3).astype(np.float32))),
+                        (TR_CLOSURE_DISNEY, dict(diffuse=(0.95, 0.64, 0.54), metallic=1.0, roughness=0.3,
+                                                 specular=0.5))):
+        box = _Builder()
+        box.box((0.0, 0.0, 0.0), (1.0, 1.0, 1.0), 1.0, 0.0, 0)
+        mesh_from(box, [material(closure=closure, **kw)])
+    sp_p, sp_i = _octahedron_sphere(6)
+    mat_s = material(diffuse=rng.uniform(0.3, 0.9, 3).astype(np.float32), closure=TR_CLOSURE_DISNEY,
+                     roughness=0.5, metallic=0.2, specular=0.5)
+    mats_before = len(mats)
+    offsets.append(mats_before)
+    mats.append(mat_s)
+    meshes.append(dict(positions=sp_p, normals=sp_p.copy(), texcoords=None, indices=sp_i,
+                       material_indices=np.zeros(sp_i.shape[0], np.uint32)))
+    light = _Builder()
+    light.quad([(-0.12, 0.0, -0.12), (0.12, 0.0, -0.12), (0.12, 0.0, 0.12), (-0.12, 0.0, 0.12)], (0, -1, 0), 0)
+    mesh_from(light, [material(diffuse=(1, 1, 1), emissive=(20, 20, 20), closure=TR_CLOSURE_DIFFUSE)])
+    instances = [
+        (0, placement()),
+        (1, placement(0.9553365, -0.29552022, 0.6, (0.35, -0.7, -0.1))),
+        (1, placement(0.8775826, 0.47942555, 0.3, (-0.55, -0.85, -0.45))),
+        (2, placement(0.9553365, 0.29552022, 0.6, (-0.35, -0.4, 0.35))),
+        (3, placement(1.0, 0.0, 0.2, (0.45, -0.25, 0.3))),
+        (3, placement(0.0, 1.0, 0.12, (-0.1, -0.88, -0.5))),
+        (4, placement(translate=(-0.3, 0.99, 0.0))),
+        (4, placement(translate=(0.3, 0.99, 0.1))),
+    ]
+    mats = np.array(mats, MATERIAL_DTYPE)
+    if wall_closure == TR_CLOSURE_LAMBERT:
+        mats["closure"] = TR_CLOSURE_LAMBERT
+    m0 = meshes[0]
+    return InstancedScene("instanced_cornell", m0["positions"], m0["normals"], m0["texcoords"], m0["indices"],
+                          m0["material_indices"], mats, CameraSpec(), width, height, spp, max_depth, 1 << 30, seed,
+                          meshes=meshes, mesh_material_offsets=np.array(offsets, np.uint32), instances=instances)
 
 
 def _value_noise(n: int, rng: np.random.Generator, octaves: int = 6, base: int = 4) -> np.ndarray:
