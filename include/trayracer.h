@@ -379,7 +379,8 @@ tr_status tr_autotune(void* ctx, void* stream, uint32_t flags, tr_tune_report* r
  * consecutive (item, sample) units. A path's random numbers are keyed as in
  * tr_render_frame (pixel, sample, bounce, seed), so an item whose samples fit
  * in one wave renders the image tr_render_frame gives for that scene with
- * multi_sample = spp from a reset accumulator, bit for bit. */
+ * multi_sample = spp from a reset accumulator (to a few ulps: the batch
+ * kernels are separate instances the compiler may contract differently). */
 typedef struct tr_batch_item {
     const tr_scene_desc* scene;     /* read during tr_batch_create only */
     tr_camera camera;

@@ -1,8 +1,10 @@
 """Batched rendering (tr_batch_*): many scenes of different size, resolution and
 sample count in one wavefront, checked against rendering each scene on its own
 through tr_render_frame. Random numbers are keyed by (pixel, sample, bounce,
-seed) in both, and each item keeps its own BVH, so the images agree bit for
-bit when the accumulation order is the same."""
+seed) in both and each item keeps its own BVH, so every path takes the same
+decisions; the batch kernels are separate template instances whose multiply-adds
+the compiler may contract differently, so images agree to a few ulps (2e-6
+relative) when the accumulation order is the same."""
 import numpy as np
 import pytest
 
@@ -64,7 +66,7 @@ def test_batch_equals_single_scene_renders():
             want, n = _single(s, s.spp, st)
             rays += n
             got = b.Image(i)
-            np.testing.assert_array_equal(got, want)
+            np.testing.assert_allclose(got, want, rtol=2e-6, atol=1e-7)
         assert stats["extend_rays"] + stats["shadow_rays"] == rays
 
 
@@ -81,7 +83,7 @@ def test_batch_split_into_waves_equals_frame_sequence():
         for i, s in enumerate(scenes):
             np.testing.assert_array_equal(b.Image(i), imgs[i])
             want, _ = _single(s, s.spp, st, frames=s.spp)
-            np.testing.assert_array_equal(imgs[i], want)
+            np.testing.assert_allclose(imgs[i], want, rtol=2e-6, atol=1e-7)
 
 
 def test_batch_uneven_waves_close_to_single():
