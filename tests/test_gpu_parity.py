@@ -67,8 +67,10 @@ def shade_sensitivity(o, st, b, W, H, state, hits, ext64, sh64):
         D = state[1].copy()
         D[:, :3] = (D[:, :3].astype(np.float64) * (1.0 + pat * 2.0 ** -21)).astype(np.float32)
         e, _, sh, _, _ = o.shade(st, b, 0, W, H, state[0], D, state[2], hits, fp64=True)
-        sens_e = np.maximum(sens_e, np.abs(e.astype(np.float64) - ext64))
-        sens_s = np.maximum(sens_s, np.abs(sh.astype(np.float64) - sh64))
+        with np.errstate(invalid="ignore"):
+            # entries without an extend / shadow ray may hold NaN: fmax keeps the other value
+            sens_e = np.fmax(sens_e, np.abs(e.astype(np.float64) - ext64))
+            sens_s = np.fmax(sens_s, np.abs(sh.astype(np.float64) - sh64))
     return sens_e, sens_s
 
 
