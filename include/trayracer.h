@@ -352,6 +352,19 @@ tr_status tr_adjoint_frame(void* ctx, void* stream, const float* pixel_grad, flo
  * contexts) race. Guide buffers (TR_FLAG_WRITE_AOVS) are not written. */
 tr_status tr_render_frame_noalloc(void* ctx, void* stream, float* accumulator, float* colors, uint32_t sample_count);
 
+/* ---- render modes ----
+ * ≙ the renderMode / renderFlags arguments of DeviceRenderer::RenderFrame
+ * (DeviceRenderer.cpp:97-106) and KernelSettings::aoDist / zDepthMax: mode is a
+ * RenderModes value (CommonStructs.h:110-125: 0 AmbientOcclusion,
+ * 1 AmbientOcclusionShading, 2 Bitangent, 3 GeometricNormal, 4 MaterialID,
+ * 5 MaterialProperty, 6 ObjectID, 7 PathTracing (default), 8 ShadingNormal,
+ * 9 Tangent, 10 TextureCoordinate, 11 Wireframe, 12 ZDepth); flags selects the
+ * MaterialPropertyIds value of mode 5. Modes other than 7 run the reference's
+ * other shade kernels (Tracer/CUDA/GPU/Shade/*.h) through tr_render_frame; the
+ * per-stage entries accept mode 7 only. Changing the mode resets the
+ * accumulation. */
+tr_status tr_set_render_mode(void* ctx, uint32_t mode, uint32_t flags, float ao_dist, float z_depth_max);
+
 /* ---- tuning ----
  * No counterpart in the reference (OptiX picks its own launch shapes). */
 #define TR_TUNE_SKIP_BVH (1u << 0)  /* tr_autotune: keep the BVH leaf size */

@@ -232,6 +232,7 @@ class Reference:
             lib.ref_render_frame.argtypes = [_P, _P, _P, _U, _U, _U, _P, _P, _P]
             lib.ref_closure.argtypes = [C.c_int, _P, _P]
             lib.ref_rng.argtypes = [_U, _U, _U, _P]
+            lib.ref_set_render_mode.argtypes = [_U, _U, C.c_float, C.c_float]
             cls._lib = lib
         return cls._lib
 
@@ -260,6 +261,11 @@ class Reference:
         if getattr(self, "_c", None) and self._lib is not None:
             self._lib.ref_destroy(self._c)
             self._c = None
+
+    @classmethod
+    def set_render_mode(cls, mode: int, flags: int = 0, ao_dist: float = 1.0, z_depth_max: float = 1.0):
+        """RenderModes value, MaterialPropertyIds flags, aoDist, zDepthMax for the following frames."""
+        cls.lib().ref_set_render_mode(int(mode), int(flags), float(ao_dist), float(z_depth_max))
 
     def render_frame(self, cam: CameraSpec, settings, width, height, sample_count, accumulator):
         """One DeviceRenderer::RenderFrame; accumulator (H*W, 4) float32 is updated in place."""

@@ -19,7 +19,8 @@ struct RefSceneBuffers {
 void refk_set_scene(const RefSceneBuffers& b);
 void refk_set_frame(const LaunchParams* params, const RayCounters* counters);
 void refk_shade(uint32_t pathCount, float4* accumulator, float4* albedo, float4* normals, float4* pathStates,
-                uint4* hitData, float4* shadowRays, int resX, int resY, uint32_t stride, uint32_t pathLength);
+                uint4* hitData, float4* shadowRays, int resX, int resY, uint32_t stride, uint32_t pathLength,
+                uint32_t renderMode, uint32_t renderFlags);
 
 void refo_set_params(const LaunchParams& p);
 void refo_launch(uint32_t w, uint32_t h, uint32_t d);

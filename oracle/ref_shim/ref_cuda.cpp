@@ -8,7 +8,19 @@ uint3 threadIdx, blockIdx, blockDim;
 
 #include "CudaLights.h"
 #include "CudaMaterial.h"
+#include "Shade/AmbientOcclusion.h"
+#include "Shade/AmbientOcclusionShading.h"
+#include "Shade/Bitangent.h"
+#include "Shade/GeometricNormal.h"
+#include "Shade/MaterialID.h"
+#include "Shade/MaterialProperty.h"
+#include "Shade/ObjectID.h"
 #include "Shade/PathTracing.h"
+#include "Shade/ShadingNormal.h"
+#include "Shade/Tangent.h"
+#include "Shade/TextureCoordinate.h"
+#include "Shade/Wireframe.h"
+#include "Shade/ZDepth.h"
 
 #include "ref_api.h"
 
@@ -31,10 +43,11 @@ void refk_set_frame(const LaunchParams* params, const RayCounters* counters)
     SetCudaCounters(counters);
 }
 
-// Shade(RenderModes::PathTracing, ...) of Tracer/CUDA/GPU/cuda.cu:57-59 with the
+// Shade(renderMode, ...) of Tracer/CUDA/GPU/cuda.cu:23-85 with the
 // <<<ceil(n/128), 128>>> grid walked one thread at a time.
 void refk_shade(uint32_t pathCount, float4* accumulator, float4* albedo, float4* normals, float4* pathStates,
-                uint4* hitData, float4* shadowRays, int resX, int resY, uint32_t stride, uint32_t pathLength)
+                uint4* hitData, float4* shadowRays, int resX, int resY, uint32_t stride, uint32_t pathLength,
+                uint32_t renderMode, uint32_t renderFlags)
 {
     blockDim = make_uint3(128, 1, 1);
     const uint32_t blocks = (pathCount + 127) / 128;
@@ -42,8 +55,25 @@ void refk_shade(uint32_t pathCount, float4* accumulator, float4* albedo, float4*
         blockIdx = make_uint3(b, 0, 0);
         for (uint32_t t = 0; t < 128; ++t) {
             threadIdx = make_uint3(t, 0, 0);
-            PathTracingKernel(pathCount, accumulator, albedo, normals, pathStates, hitData, shadowRays, resX, resY,
-                              stride, pathLength, 0);
+#define REF_ARGS pathCount, accumulator, albedo, normals, pathStates, hitData, shadowRays, resX, resY, stride, \
+                 pathLength, renderFlags
+            switch (static_cast<RenderModes>(renderMode)) {
+            case RenderModes::AmbientOcclusion: AmbientOcclusionKernel(REF_ARGS); break;
+            case RenderModes::AmbientOcclusionShading: AmbientOcclusionShadingKernel(REF_ARGS); break;
+            case RenderModes::Bitangent: BitangentKernel(REF_ARGS); break;
+            case RenderModes::GeometricNormal: GeometricNormalKernel(REF_ARGS); break;
+            case RenderModes::MaterialID: MaterialIDKernel(REF_ARGS); break;
+            case RenderModes::MaterialProperty: MaterialPropertyKernel(REF_ARGS); break;
+            case RenderModes::ObjectID: ObjectIDKernel(REF_ARGS); break;
+            case RenderModes::PathTracing: PathTracingKernel(REF_ARGS); break;
+            case RenderModes::ShadingNormal: ShadingNormalKernel(REF_ARGS); break;
+            case RenderModes::Tangent: TangentKernel(REF_ARGS); break;
+            case RenderModes::TextureCoordinate: TextureCoordinateKernel(REF_ARGS); break;
+            case RenderModes::Wireframe: WireframeKernel(REF_ARGS); break;
+            case RenderModes::ZDepth: ZDepthKernel(REF_ARGS); break;
+            default: break;
+            }
+#undef REF_ARGS
         }
     }
 }

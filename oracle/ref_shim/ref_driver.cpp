@@ -31,6 +31,11 @@ struct RefCtx {
 
 RefCtx* g_ctx = nullptr;
 
+// render mode of the next frames (DeviceRenderer::RenderFrame's renderMode / renderFlags)
+uint32_t g_renderMode = uint32_t(RenderModes::PathTracing);
+uint32_t g_renderFlags = 0;
+float g_aoDist = 1.f, g_zDepthMax = 1.f;
+
 // The reference's float3x4 (Tracer/Utility/LinearMath.h:205-210: float3 x; tx; y; ty; z; tz)
 // with its inverse (:472-506) and transform (:274-281), restated here because that
 // header's host intrinsics collide with this shim's.
@@ -111,12 +116,13 @@ void set_frame_params(RefCtx* c, const tr_camera* cam, const tr_kernel_settings*
     lp.pathStates = states;
     lp.hitData = hits;
     lp.shadowRays = shadow;
-    lp.renderMode = RenderModes::PathTracing;
+    lp.renderMode = static_cast<RenderModes>(g_renderMode);
+    lp.renderFlags = g_renderFlags;
     lp.kernelSettings.multiSample = st->multi_sample;
     lp.kernelSettings.maxDepth = st->max_depth;
     lp.kernelSettings.seed = st->seed;
-    lp.kernelSettings.aoDist = 1.f;
-    lp.kernelSettings.zDepthMax = 1.f;
+    lp.kernelSettings.aoDist = g_aoDist;
+    lp.kernelSettings.zDepthMax = g_zDepthMax;
     lp.kernelSettings.rayEpsilon = st->ray_epsilon;
     g_ctx = c;
     refk_set_frame(&c->lp, &c->counters);
@@ -150,6 +156,14 @@ void ref_host_trace(float3 O, float3 D, float tmin, float tmax, bool anyHit, uin
 }
 
 extern "C" {
+
+void ref_set_render_mode(uint32_t mode, uint32_t flags, float aoDist, float zDepthMax)
+{
+    g_renderMode = mode;
+    g_renderFlags = flags;
+    g_aoDist = aoDist;
+    g_zDepthMax = zDepthMax;
+}
 
 void* ref_create(const tr_scene_desc* desc)
 {
@@ -341,7 +355,7 @@ void ref_shade(void* ctx, const tr_camera* cam, const tr_kernel_settings* st, ui
     const uint32_t stride = W * H * st->multi_sample;
     refk_shade(pathCount, reinterpret_cast<float4*>(accumulator), reinterpret_cast<float4*>(albedo),
                reinterpret_cast<float4*>(normals), reinterpret_cast<float4*>(states), reinterpret_cast<uint4*>(hits),
-               reinterpret_cast<float4*>(shadow), int(W), int(H), stride, pathLength);
+               reinterpret_cast<float4*>(shadow), int(W), int(H), stride, pathLength, g_renderMode, g_renderFlags);
     counters[0] = c->counters.extendRays;
     counters[1] = c->counters.shadowRays;
 }

@@ -7,7 +7,8 @@ and its raygen + path-tracing kernels (Tracer/Optix/GPU/optix.cu,
 Tracer/CUDA/GPU/Shade/PathTracing.h), compiled as host C++, produce the
 expected values; nothing here is written from memory.
 
-    python tests/golden/make_golden.py
+    python tests/golden/make_golden.py              # every fixture
+    python tests/golden/make_golden.py debug_modes  # only ref_debug_modes.npz
 """
 from __future__ import annotations
 
@@ -102,7 +103,36 @@ def cornell_reference_frames(width=32, height=32, ms=1, seed=5, frames=2):
     )
 
 
+DEBUG_MODES = [(0, 0), (1, 0), (2, 0), (3, 0), (4, 0), (5, 3), (5, 4), (5, 6), (5, 7), (6, 0), (8, 0), (9, 0),
+               (10, 0), (11, 0), (12, 0)]
+
+
+def debug_mode_frames(width=40, height=30, seed=5, ao_dist=0.6, z_depth_max=3.0):
+    """One frame of every other render mode (RenderModes 0-12 except 7; MaterialProperty with
+    MaterialPropertyIds Diffuse, Emissive, Normal, Roughness) on the two-level Cornell box, by the
+    reference's raygen programs and shade kernels (Tracer/CUDA/GPU/Shade/*.h)."""
+    scene = tr.instanced_cornell(width=width, height=height)
+    st = KernelSettings(multiSample=1, maxDepth=2, seed=seed, rrStart=1,
+                        flags=tr.TR_FLAG_REFERENCE_SAMPLING | tr._abi.TR_FLAG_REFERENCE_DRAW_RTL)
+    ref = Reference(scene)
+    out = dict(digest=np.array(scene.digest()), width=width, height=height, seed=seed, ao_dist=ao_dist,
+               z_depth_max=z_depth_max, modes=np.array(DEBUG_MODES, np.uint32))
+    for mode, flags in DEBUG_MODES:
+        Reference.set_render_mode(mode, flags, ao_dist, z_depth_max)
+        acc = np.zeros((width * height, 4), np.float32)
+        ref.render_frame(scene.camera, st, width, height, 0, acc)
+        out[f"mode_{mode}_{flags}"] = acc
+    Reference.set_render_mode(7)
+    return out
+
+
 def main():
+    if sys.argv[1:] == ["debug_modes"]:
+        build.build_oracle()
+        if build.build_reference() is None:
+            raise SystemExit("reference sources not found")
+        np.savez_compressed(OUT / "ref_debug_modes.npz", **debug_mode_frames())
+        return
     build.build_oracle()
     if build.build_reference() is None:
         raise SystemExit("reference sources not found: the golden fixtures come from the reference's own code")
@@ -121,6 +151,8 @@ def main():
     # frames
     np.savez_compressed(OUT / "ref_cornell_32x32_ms1.npz", **cornell_reference_frames(ms=1))
     np.savez_compressed(OUT / "ref_cornell_24x16_ms2.npz", **cornell_reference_frames(24, 16, ms=2, seed=9))
+    # the other render modes
+    np.savez_compressed(OUT / "ref_debug_modes.npz", **debug_mode_frames())
     for p in sorted(OUT.glob("*.npz")):
         print(p.name, p.stat().st_size)
 

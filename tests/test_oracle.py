@@ -135,6 +135,27 @@ def test_oracle_matches_reference_kernels_two_level():
         assert acc[:, :3].max() > 0
 
 
+@pytest.mark.skipif(not reference_available(), reason="reference host build absent (sources not present)")
+def test_debug_mode_fixture_reproduced_by_reference():
+    """ref_debug_modes.npz is what the reference's other shade kernels make today."""
+    import importlib.util
+
+    spec = importlib.util.spec_from_file_location("make_golden", GOLDEN / "make_golden.py")
+    mg = importlib.util.module_from_spec(spec)
+    spec.loader.exec_module(mg)
+    g = np.load(GOLDEN / "ref_debug_modes.npz")
+    try:
+        fresh = mg.debug_mode_frames(int(g["width"]), int(g["height"]), int(g["seed"]), float(g["ao_dist"]),
+                                     float(g["z_depth_max"]))
+    finally:
+        Reference.set_render_mode(7)
+    for mode, flags in g["modes"]:
+        key = f"mode_{mode}_{flags}"
+        np.testing.assert_array_equal(fresh[key], g[key], err_msg=key)
+    # the modes are not all alike: normals, IDs and depth differ from one another
+    assert len({g[f"mode_{m}_{f}"].tobytes() for m, f in g["modes"]}) >= 12
+
+
 def test_counter_rng_properties():
     u = np.concatenate([Oracle.counter_rng(p, s, b, 1, 8) for p in range(64) for s in range(4) for b in range(3)])
     assert u.min() >= 0.0 and u.max() < 1.0

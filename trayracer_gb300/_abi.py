@@ -266,6 +266,7 @@ FUNCTIONS = {
     "tr_update_materials": (C.c_int, [_V, C.POINTER(MaterialDesc), _U]),
     "tr_adjoint_frame": (C.c_int, [_V, _V, _V, C.c_float, _V]),
     "tr_render_frame_noalloc": (C.c_int, [_V, _V, _V, _V, _U]),
+    "tr_set_render_mode": (C.c_int, [_V, _U, _U, C.c_float, C.c_float]),
     "tr_get_tuning": (C.c_int, [_V, C.POINTER(Tuning)]),
     "tr_set_tuning": (C.c_int, [_V, C.POINTER(Tuning)]),
     "tr_autotune": (C.c_int, [_V, _V, _U, C.POINTER(TuneReport)]),

@@ -128,6 +128,12 @@ struct Context {
     cudaGraph_t graph = nullptr;
     cudaGraphExec_t graphExec = nullptr;
     bool graphValid = false;
+
+    // render mode (RenderModes; debug modes run the reference's other shade kernels)
+    uint32_t renderMode = kModePathTracing;
+    uint32_t renderFlags = 0;
+    float aoDist = 1.f;
+    float zDepthMax = 1.f;
 };
 
 tr_status fail(Context* c, tr_status st, const std::string& msg)
@@ -332,6 +338,28 @@ tr_status enqueue_frame(Context* c, cudaStream_t s, bool timed)
         return st;
     if (timed)
         TR_CUDA(c, cudaEventRecord(c->evStart, s));
+    if (c->renderMode != kModePathTracing) {
+        Settings st = c->settings;
+        st.renderMode = c->renderMode;
+        st.renderFlags = c->renderFlags;
+        st.aoDist = c->aoDist;
+        st.zDepthMax = c->zDepthMax;
+        TR_CUDA(c, launch_generate(c->frame, c->camera, st, s));
+        if (timed)
+            TR_CUDA(c, cudaEventRecord(c->evGenerate, s));
+        for (uint32_t b = 0; b < st.maxDepth; ++b) {
+            TR_CUDA(c, launch_debug_bounce(c->scene, c->frame, c->camera, st, b, c->shape, s));
+            if (timed) {
+                TR_CUDA(c, cudaEventRecord(c->evExtend[b], s));
+                TR_CUDA(c, cudaEventRecord(c->evShade[b], s));
+                TR_CUDA(c, cudaEventRecord(c->evConnect[b], s));
+            }
+        }
+        TR_CUDA(c, launch_finalize(c->frame, c->settings, s));
+        if (timed)
+            TR_CUDA(c, cudaEventRecord(c->evFinal, s));
+        return TR_OK;
+    }
     // default sampling mode: the camera rays are made inside the first extend launch
     const bool fused = (c->settings.flags & TR_FLAG_REFERENCE_SAMPLING) == 0;
     if (!fused)
@@ -427,6 +455,9 @@ bool convert_settings(const tr_kernel_settings& s, Settings* out, std::string* e
     k.rrStart = s.rr_start;
     k.flags = s.flags;
     k.maxColor = s.max_color > 0.f ? s.max_color : 10.f;
+    k.renderMode = kModePathTracing;
+    k.aoDist = 1.f;
+    k.zDepthMax = 1.f;
     *out = k;
     return true;
 }
@@ -760,6 +791,28 @@ tr_status tr_adjoint_frame(void* ctx, void* stream, const float* pixel_grad, flo
     return TR_OK;
 }
 
+tr_status tr_set_render_mode(void* ctx, uint32_t mode, uint32_t flags, float ao_dist, float z_depth_max)
+{
+    if (!ctx)
+        return TR_ERR_INVALID_ARGUMENT;
+    Context* c = static_cast<Context*>(ctx);
+    if (mode > kModeZDepth)
+        return fail(c, TR_ERR_INVALID_ARGUMENT, "unknown render mode");
+    if (!(ao_dist > 0.f) || !(z_depth_max > 0.f))
+        return fail(c, TR_ERR_INVALID_ARGUMENT, "ao_dist and z_depth_max must be > 0");
+    const bool changed = mode != c->renderMode || flags != c->renderFlags || ao_dist != c->aoDist ||
+                         z_depth_max != c->zDepthMax;
+    c->renderMode = mode;
+    c->renderFlags = flags;
+    c->aoDist = ao_dist;
+    c->zDepthMax = z_depth_max;
+    if (changed) {
+        invalidate_graph(c);
+        return tr_reset(ctx);
+    }
+    return TR_OK;
+}
+
 tr_status tr_get_tuning(void* ctx, tr_tuning* out)
 {
     if (!ctx || !out)
@@ -1019,6 +1072,9 @@ tr_status tr_extend(void* ctx, void* stream, uint32_t bounce)
     Context* c = static_cast<Context*>(ctx);
     if (bounce >= TR_MAX_DEPTH)
         return fail(c, TR_ERR_INVALID_ARGUMENT, "bounce out of range");
+    if (c->renderMode != kModePathTracing)
+        return fail(c, TR_ERR_INVALID_ARGUMENT, "the stage entries drive the path-tracing mode; render other modes "
+                                                "with tr_render_frame");
     tr_status st = check_ready(c);
     if (st != TR_OK)
         return st;
@@ -1035,6 +1091,9 @@ tr_status tr_shade(void* ctx, void* stream, uint32_t bounce)
     Context* c = static_cast<Context*>(ctx);
     if (bounce >= TR_MAX_DEPTH)
         return fail(c, TR_ERR_INVALID_ARGUMENT, "bounce out of range");
+    if (c->renderMode != kModePathTracing)
+        return fail(c, TR_ERR_INVALID_ARGUMENT, "the stage entries drive the path-tracing mode; render other modes "
+                                                "with tr_render_frame");
     tr_status st = check_ready(c);
     if (st != TR_OK)
         return st;
@@ -1049,6 +1108,9 @@ tr_status tr_connect(void* ctx, void* stream, uint32_t bounce)
     Context* c = static_cast<Context*>(ctx);
     if (bounce >= TR_MAX_DEPTH)
         return fail(c, TR_ERR_INVALID_ARGUMENT, "bounce out of range");
+    if (c->renderMode != kModePathTracing)
+        return fail(c, TR_ERR_INVALID_ARGUMENT, "the stage entries drive the path-tracing mode; render other modes "
+                                                "with tr_render_frame");
     tr_status st = check_ready(c);
     if (st != TR_OK)
         return st;

@@ -214,7 +214,17 @@ struct Settings {
     uint32_t flags;
     float maxColor;
     uint32_t refillBelow;  // persistent traversal warps refill lanes below this many active (set per launch)
+    uint32_t renderMode;   // RenderModes (Tracer/Common/CommonStructs.h:110-125); 7 = path tracing
+    uint32_t renderFlags;  // MaterialPropertyIds for the material-property mode
+    float aoDist;          // KernelSettings::aoDist (ambient occlusion modes)
+    float zDepthMax;       // KernelSettings::zDepthMax (depth mode)
 };
+
+// RenderModes, Tracer/Common/CommonStructs.h:110-125
+constexpr uint32_t kModeAO = 0, kModeAOShading = 1, kModeBitangent = 2, kModeGeometricNormal = 3,
+                   kModeMaterialID = 4, kModeMaterialProperty = 5, kModeObjectID = 6, kModePathTracing = 7,
+                   kModeShadingNormal = 8, kModeTangent = 9, kModeTextureCoordinate = 10, kModeWireframe = 11,
+                   kModeZDepth = 12;
 
 // Device counter words: per bounce the extend queue length, the shadow queue
 // length, the work-fetch cursors of the persistent extend and connect launches,

@@ -938,6 +938,206 @@ __global__ void __launch_bounds__(256) finalize_kernel(FrameView f, Settings st)
     f.colors[p] = make_float4(acc.x / n, acc.y / n, acc.z / n, acc.w / n);
 }
 
+// ------------------------------------------------------------------ debug render modes
+// The reference's other shade kernels (Tracer/CUDA/GPU/Shade/*.h except
+// PathTracing.h), run over the whole bounce queue with hits stored by queue
+// slot (no compaction: the ambient-occlusion and wireframe modes act on
+// missed rays too). Each path sets its radiance (one contribution per path).
+
+// Closest hit of every ray of the bounce's queue (state[bounce & 1]); the
+// wireframe mode re-aims secondary rays at a jittered point of the pixel as
+// the Secondary raygen program does (optix.cu:292-300).
+__global__ void __launch_bounds__(128) debug_extend_kernel(SceneView s, FrameView f, Camera cam, Settings st,
+                                                           uint32_t bounce)
+{
+    const uint32_t count = queue_length(f, bounce);
+    float4* q = f.state[bounce & 1u];
+    const uint32_t cap = f.capacity;
+    const uint32_t sc = *f.sampleCount;
+    for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < count; i += gridDim.x * blockDim.x) {
+        const float4 O4 = q[i];
+        float3 O = f3(O4), D = f3(q[i + cap]);
+        const uint32_t pathIx = path_ix(__float_as_uint(O4.w));
+        if (st.renderMode == kModeWireframe && bounce > 0) {
+            const uint32_t wh = f.resX * f.resY;
+            const uint32_t pixelIx = pathIx % wh;
+            RefRng rng{tea2(st.seed + pathIx, (sc << 1) | 1u)};
+            float T;
+            camera_ray(cam, f.resX, f.resY, pixelIx % f.resX, pixelIx / f.resX, rng,
+                       (st.flags & TR_FLAG_REFERENCE_DRAW_RTL) != 0, O, D, T);
+        }
+        float tmax = kDstMax;
+        uint32_t slot = 0xffffffffu, inst = 0;
+        float u = 0.f, v = 0.f;
+        if (!traverse<false>(s, O, D, st.rayEpsilon, tmax, slot, u, v, nullptr, &inst))
+            atomicOr(f.errorFlag, 1u);
+        f.hits[i] = slot != 0xffffffffu
+                        ? make_uint4(encode_bary(u, v), inst, __float_as_uint(__ldg(s.bvhTris + 3u * slot).w),
+                                     __float_as_uint(tmax))
+                        : make_uint4(0u, 0xffffffffu, 0xffffffffu, __float_as_uint(kDstMax));
+    }
+}
+
+// OrthonormalBase + SampleCosineHemisphere (CudaUtility.h:182-199, 271-292)
+__device__ __forceinline__ float3 cosine_hemisphere(const float3& n, float r0, float r1)
+{
+    float3 b = fabsf(n.x) > fabsf(n.y) ? make_float3(-n.y, n.x, 0.f) : make_float3(0.f, -n.z, n.y);
+    b = normalize(b);
+    const float3 t = cross(b, n);
+    float sinPhi, cosPhi;
+    sincosf(2.0f * kPi * r0, &sinPhi, &cosPhi);
+    const float rb = sqrtf(1.f - r1);
+    const float3 l = make_float3(cosPhi * rb, sinPhi * rb, sqrtf(r1));
+    return l.x * t + l.y * b + l.z * n;
+}
+
+// IdToColor (CudaUtility.h:14-27): bits of id spread over the three channels
+__device__ __forceinline__ float3 id_to_color(uint32_t id)
+{
+    uint32_t c[3];
+    for (uint32_t i = 0; i < 3; ++i) {
+        c[i] = (id >> i) & 0x249249u;
+        c[i] = ((c[i] << 1) | (c[i] >> 3)) & 0x0C30C3u;
+        c[i] = ((c[i] << 2) | (c[i] >> 6)) & 0x00F00Fu;
+        c[i] = ((c[i] << 4) | (c[i] >> 12)) & 0x0000FFu;
+    }
+    return make_float3(c[0] * (1.f / 255.f), c[1] * (1.f / 255.f), c[2] * (1.f / 255.f));
+}
+
+__global__ void __launch_bounds__(128) debug_shade_kernel(SceneView s, FrameView f, Camera cam, Settings st,
+                                                          uint32_t bounce)
+{
+    const uint32_t count = queue_length(f, bounce);
+    const float4* in = f.state[bounce & 1u];
+    float4* out = f.state[(bounce + 1u) & 1u];
+    const uint32_t cap = f.capacity;
+    const uint32_t sc = *f.sampleCount;
+    const uint32_t wh = f.resX * f.resY;
+    const bool rtl = (st.flags & TR_FLAG_REFERENCE_DRAW_RTL) != 0;
+    const bool aov = (st.flags & TR_FLAG_WRITE_AOVS) != 0;
+    uint32_t* extCounter = f.counters + bounce + 1u;
+    const uint32_t mode = st.renderMode;
+    const bool ao = mode == kModeAO || mode == kModeAOShading;
+    for (uint32_t base = (blockIdx.x * blockDim.x + threadIdx.x) & ~31u; base < count;
+         base += gridDim.x * blockDim.x) {
+        const uint32_t i = base + lane_id();
+        bool wantExt = false;
+        float4 ext[3];
+        if (i < count) {
+            const float4 O4 = in[i];
+            const float4 D4 = in[i + cap];
+            const uint4 hd = f.hits[i];
+            const uint32_t pathIx = path_ix(__float_as_uint(O4.w));
+            const uint32_t pixelIx = pathIx % wh;
+            const bool hit = hd.z != 0xffffffffu;
+            const float tmax = __uint_as_float(hd.w);
+            float3 c = f3(0.f);
+            bool set = false;
+            if (ao && bounce > 0) {
+                // the occlusion ray: 1 beyond aoDist (or on a miss), else tmax / aoDist
+                const float z = tmax > st.aoDist ? 1.f : tmax / st.aoDist;
+                c = mode == kModeAO ? make_float3(z, z, z) : f3(in[i + 2 * cap]) * z;
+                set = true;
+            } else if (mode == kModeWireframe) {
+                if (bounce == 0) {
+                    // trace a second, jittered ray; keep this hit's primitive
+                    wantExt = true;
+                    ext[0] = f4(f3(O4), __uint_as_float(pack_path(pathIx, 0)));
+                    ext[1] = f4(f3(D4), 0.f);
+                    ext[2] = make_float4(0.f, 0.f, 0.f, __uint_as_float(hd.z));
+                } else if (__float_as_uint(in[i + 2 * cap].w) == hd.z) {
+                    c = make_float3(1.f, 1.f, 1.f);
+                    set = true;
+                }
+            } else if (mode == kModeZDepth) {
+                if (hit) {
+                    const float z = fminf(fmaxf(tmax * dot(f3(D4), cam.forward) / st.zDepthMax, 0.f), 1.f);
+                    c = make_float3(z, z, z);
+                    set = true;
+                }
+            } else if (mode == kModeObjectID) {
+                if (hit) {
+                    c = id_to_color(hd.y + 1u);
+                    set = true;
+                }
+            } else if (hit && bounce == 0) {
+                const float2 bary = decode_bary(hd.x);
+                const bool fix = ao;
+                const Surface sf = surface_at(s, hd.y, hd.z, bary, fix ? f3(D4) : f3(0.f));
+                uint32_t closure, emissiveFlag;
+                const HitMat m = load_material(s.materials, sf.matIx, closure, emissiveFlag);
+                if (ao) {
+                    uint32_t seed = tea2(st.seed + pathIx, mode == kModeAO ? bounce + 1u : sc + bounce + 1u);
+                    if (mode == kModeAO)
+                        seed ^= sc;  // rot_seed (random.h:69-72)
+                    RefRng rng{seed};
+                    float r0, r1;
+                    draw2(rng, rtl, r0, r1);
+                    const float3 I = f3(O4) + f3(D4) * tmax;
+                    wantExt = true;
+                    ext[0] = f4(I, __uint_as_float(pack_path(pathIx, 0)));
+                    ext[1] = f4(cosine_hemisphere(sf.N, r0, r1), 0.f);
+                    const float3 T = mode == kModeAO ? make_float3(1.f, 1.f, 1.f) : m.diffuse;
+                    ext[2] = f4(T, 0.f);
+                    c = T;  // the value of an occlusion ray that escapes
+                    set = true;
+                    if (aov && pathIx < wh) {
+                        f.albedo[pixelIx] = f4(mode == kModeAO ? make_float3(1.f, 1.f, 1.f) : m.diffuse, 0.f);
+                        f.normals[pixelIx] = f4(sf.N, 0.f);
+                    }
+                } else {
+                    set = true;
+                    switch (mode) {
+                    case kModeBitangent: c = (sf.B + make_float3(1.f, 1.f, 1.f)) * 0.5f; break;
+                    case kModeGeometricNormal: c = (sf.Ng + make_float3(1.f, 1.f, 1.f)) * 0.5f; break;
+                    case kModeShadingNormal: c = (sf.N + make_float3(1.f, 1.f, 1.f)) * 0.5f; break;
+                    case kModeTangent: c = (sf.T + make_float3(1.f, 1.f, 1.f)) * 0.5f; break;
+                    case kModeMaterialID: c = id_to_color(sf.matIx + 1u); break;
+                    case kModeTextureCoordinate: {
+                        const uint32_t ti = (s.instInfo ? __ldg(&s.instInfo[hd.y].y) : 0u) + hd.z;
+                        const TriShade& tri = s.tris[ti];
+                        const float2 u0 = make_float2(h2f(tri.uv0x), h2f(tri.uv0y));
+                        const float2 u1 = make_float2(h2f(tri.uv1x), h2f(tri.uv1y));
+                        const float2 u2 = make_float2(h2f(tri.uv2x), h2f(tri.uv2y));
+                        const float2 uv = make_float2(u0.x + ((u1.x - u0.x) * bary.x) + ((u2.x - u0.x) * bary.y),
+                                                      u0.y + ((u1.y - u0.y) * bary.x) + ((u2.y - u0.y) * bary.y));
+                        c = make_float3(uv.x, uv.y, 0.f);
+                        break;
+                    }
+                    case kModeMaterialProperty:
+                        switch (st.renderFlags) {  // MaterialPropertyIds
+                        case 0: c = make_float3(m.anisotropic, m.anisotropic, m.anisotropic); break;
+                        case 1: c = make_float3(m.clearcoat, m.clearcoat, m.clearcoat); break;
+                        case 2: c = make_float3(m.clearcoatGloss, m.clearcoatGloss, m.clearcoatGloss); break;
+                        case 3: c = m.diffuse; break;
+                        case 4: c = m.emissive; break;
+                        case 5: c = make_float3(m.metallic, m.metallic, m.metallic); break;
+                        case 6: c = make_float3(1.f, 1.f, 1.f); break;  // no normal map: GetColor's default
+                        case 7: c = make_float3(m.roughness, m.roughness, m.roughness); break;
+                        case 8: c = make_float3(m.sheen, m.sheen, m.sheen); break;
+                        case 9: c = make_float3(m.sheenTint, m.sheenTint, m.sheenTint); break;
+                        case 10: c = make_float3(m.specular, m.specular, m.specular); break;
+                        case 11: c = make_float3(m.specularTint, m.specularTint, m.specularTint); break;
+                        case 12: c = make_float3(m.subsurface, m.subsurface, m.subsurface); break;
+                        default: c = make_float3(1.f, 0.f, 1.f); break;
+                        }
+                        break;
+                    default: set = false; break;
+                    }
+                }
+            }
+            if (set)
+                f.radiance[pathIx] = f4(safe_color(c, st.maxColor), 0.f);
+        }
+        const uint32_t slot = warp_append(extCounter, wantExt);
+        if (wantExt) {
+            out[slot] = ext[0];
+            out[slot + cap] = ext[1];
+            out[slot + 2 * cap] = ext[2];
+        }
+    }
+}
+
 // Batched rendering: sums each pixel's samples of the wave in sample order
 // and adds them to the item's pixel of the batch accumulator (zeroed before
 // the first wave; waves run in order, and an item has at most one segment per
@@ -1511,6 +1711,15 @@ cudaError_t launch_adjoint(const SceneView& s, const FrameView& f, const Camera&
         else
             nee_grad_kernel<false><<<gradBlocks, kAdjointThreads, 0, stream>>>(s, f, bounce, a);
     }
+    return cudaGetLastError();
+}
+
+cudaError_t launch_debug_bounce(const SceneView& s, const FrameView& f, const Camera& cam, const Settings& st,
+                                uint32_t bounce, const LaunchShape& shape, cudaStream_t stream)
+{
+    const uint32_t blocks = shape.sms * 8u;
+    debug_extend_kernel<<<blocks, 128, 0, stream>>>(s, f, cam, st, bounce);
+    debug_shade_kernel<<<blocks, 128, 0, stream>>>(s, f, cam, st, bounce);
     return cudaGetLastError();
 }
 

@@ -37,6 +37,10 @@ cudaError_t launch_shade(const SceneView& s, const FrameView& f, const Settings&
 cudaError_t launch_connect(const SceneView& s, const FrameView& f, const Settings& st, uint32_t bounce,
                            const LaunchShape& shape, cudaStream_t stream);
 cudaError_t launch_finalize(const FrameView& f, const Settings& st, cudaStream_t stream);
+// One bounce of a debug render mode (Settings::renderMode != path tracing):
+// closest hit of every ray of queue state[bounce & 1], then the mode's shade.
+cudaError_t launch_debug_bounce(const SceneView& s, const FrameView& f, const Camera& cam, const Settings& st,
+                                uint32_t bounce, const LaunchShape& shape, cudaStream_t stream);
 // Counting sort of the bounce's hit queue by material into sv.order (shade
 // reads the queue through it when FrameView::hitOrder = sv.order).
 cudaError_t launch_sort_hits(const SceneView& s, const FrameView& f, const SortView& sv, uint32_t bounce,

@@ -27,7 +27,8 @@ class TracerError(RuntimeError):
 
 
 class RenderModes(enum.IntEnum):
-    """Tracer/Common/CommonStructs.h:110-125; only PathTracing is the hot path."""
+    """Tracer/Common/CommonStructs.h:110-125; PathTracing is the hot path, the other modes run the
+    reference's other shade kernels (tr_set_render_mode)."""
 
     AmbientOcclusion = 0
     AmbientOcclusionShading = 1
@@ -202,10 +203,11 @@ class DeviceRenderer:
     def RenderFrame(self, kernelSettings: KernelSettings | None = None,
                     renderMode: RenderModes = RenderModes.PathTracing, renderFlags: int = 0, stream: int = 0,
                     use_graph: bool = False):
-        if renderMode != RenderModes.PathTracing:
-            raise TracerError(1, "RenderFrame", f"render mode {renderMode.name} is not part of this hot path")
         if kernelSettings is not None:
             self.SetSettings(kernelSettings)
+        ks = kernelSettings or self._settings
+        self._check(self._lib.tr_set_render_mode(self._ctx, int(renderMode), int(renderFlags), float(ks.aoDist),
+                                                 float(ks.zDepthMax)), "tr_set_render_mode")
         self._check(self._lib.tr_render_frame(self._ctx, C.c_void_p(stream or None), int(use_graph)),
                     "tr_render_frame")
 
