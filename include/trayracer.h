@@ -365,6 +365,27 @@ tr_status tr_render_frame_noalloc(void* ctx, void* stream, float* accumulator, f
  * accumulation. */
 tr_status tr_set_render_mode(void* ctx, uint32_t mode, uint32_t flags, float ao_dist, float z_depth_max);
 
+/* ---- ray pick ----
+ * ≙ RayPickResult (CommonStructs.h:132-141): the camera position, the direction
+ * of the picked pixel's camera ray, and what the ray hit first (instance and
+ * mesh-local triangle, ~0u both on a miss; tmax = the hit distance, 1e30 on a
+ * miss). */
+typedef struct tr_ray_pick_result {
+    float ray_origin[3];
+    uint32_t inst_ix;
+    float ray_dir[3];
+    uint32_t prim_ix;
+    float tmax;
+} tr_ray_pick_result;
+
+/* ≙ DeviceRenderer::PickRay (DeviceRenderer.cpp:71-92) with the RayPick raygen
+ * (optix.cu:345-377): one camera ray through pixel (x, y) counted from the top
+ * row (the ray takes row height - y, as the reference does), random stream
+ * seeded 0, closest hit with the scene's ray epsilon. Runs on stream and waits
+ * for it; any pixel coordinates are accepted (outside the image the ray leaves
+ * the frustum). Needs a scene, a camera and a resolution. */
+tr_status tr_pick_ray(void* ctx, void* stream, int32_t x, int32_t y, tr_ray_pick_result* out);
+
 /* ---- tuning ----
  * No counterpart in the reference (OptiX picks its own launch shapes). */
 #define TR_TUNE_SKIP_BVH (1u << 0)  /* tr_autotune: keep the BVH leaf size */

@@ -55,6 +55,7 @@ class Oracle:
             lib.orc_trace_closest.argtypes = [_P, _P, _P, _U, C.c_float, _P]
             lib.orc_trace_ray.restype = C.c_int
             lib.orc_trace_ray.argtypes = [_P, _P, _P, C.c_float, C.c_float, C.c_int, _P, _P, _P, _P, _P]
+            lib.orc_pick_ray.argtypes = [_P, _P, _P, _U, _U, C.c_int32, C.c_int32, _P]
             lib.orc_ties.restype = _U
             lib.orc_ties.argtypes = [_P, _P, _P, C.c_float, C.c_float, C.c_float, _P, _U, _P]
             lib.orc_trace_any.argtypes = [_P, _P, _P, _U, C.c_float, _P]
@@ -101,6 +102,14 @@ class Oracle:
         self._lib.orc_generate(self._s, C.addressof(cc), C.addressof(st), width, height, sample_count, first, n,
                                _ptr(O), _ptr(D), _ptr(T))
         return O, D, T
+
+    def pick_ray(self, cam: CameraSpec, settings, width, height, x, y) -> np.ndarray:
+        """RayPickResult of pixel (x, y) as 9 float32 words (instIx, primIx as bit patterns)."""
+        out = np.zeros(9, np.float32)
+        cc = camera_to_c(cam)
+        st = settings.to_c()
+        self._lib.orc_pick_ray(self._s, C.addressof(cc), C.addressof(st), width, height, int(x), int(y), _ptr(out))
+        return out
 
     def trace_closest(self, O: np.ndarray, D: np.ndarray, tmin: float) -> np.ndarray:
         O = np.ascontiguousarray(O, np.float32)
@@ -233,6 +242,7 @@ class Reference:
             lib.ref_closure.argtypes = [C.c_int, _P, _P]
             lib.ref_rng.argtypes = [_U, _U, _U, _P]
             lib.ref_set_render_mode.argtypes = [_U, _U, C.c_float, C.c_float]
+            lib.ref_pick_ray.argtypes = [_P, _P, _P, _U, _U, C.c_int32, C.c_int32, _P]
             cls._lib = lib
         return cls._lib
 
@@ -276,6 +286,14 @@ class Reference:
         self._lib.ref_render_frame(self._c, C.addressof(cc), C.addressof(st), width, height, sample_count,
                                    _ptr(accumulator), _ptr(ext), _ptr(sh))
         return ext, sh
+
+    def pick_ray(self, cam: CameraSpec, settings, width, height, x, y) -> np.ndarray:
+        """DeviceRenderer::PickRay through the RayPick raygen: RayPickResult as 9 float32 words."""
+        out = np.zeros(9, np.float32)
+        cc = camera_to_c(cam)
+        st = settings.to_c()
+        self._lib.ref_pick_ray(self._c, C.addressof(cc), C.addressof(st), width, height, int(x), int(y), _ptr(out))
+        return out
 
     def primary(self, cam, settings, width, height, sample_count, accumulator):
         stride = width * height * settings.multiSample

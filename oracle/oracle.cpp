@@ -1078,7 +1078,7 @@ template <class T, class Rng> void sample_disk(Rng& rng, T& x, T& y)
 
 // GenerateCameraRay, optix.cu:142-174 (with SampleBokeh :93-112, Distort :117-138)
 template <class T, class Rng>
-void camera_ray(const tr_camera& cam, T tanFov2, uint32_t W, uint32_t H, uint32_t ix, uint32_t iy, Rng& rng,
+void camera_ray(const tr_camera& cam, T tanFov2, uint32_t W, uint32_t H, int ix, int iy, Rng& rng,
                 V3<T>& O, V3<T>& D, T& Tv)
 {
     const V3<T> pos = v3(T(cam.position[0]), T(cam.position[1]), T(cam.position[2]));
@@ -1907,6 +1907,33 @@ void orc_generate(const orc_scene* s, const tr_camera* cam, const tr_kernel_sett
         std::memcpy(D4 + 4 * size_t(k), d, 16);
         std::memcpy(T4 + 4 * size_t(k), t, 16);
     }
+}
+
+// RayPick raygen, optix.cu:345-377 (DeviceRenderer::PickRay, DeviceRenderer.cpp:71-92): the
+// camera ray of pixel (x, H - y) with the LCG state 0, closest hit; out = RayPickResult words.
+void orc_pick_ray(const orc_scene* s, const tr_camera* cam, const tr_kernel_settings* st, uint32_t W, uint32_t H,
+                  int32_t x, int32_t y, float* out)
+{
+    const float tanFov2 = std::tan(cam->fov / 2.0f);
+    RefRng rng{0u};
+    V3<float> O, D;
+    float Tv;
+    camera_ray<float>(*cam, tanFov2, W, H, x, int(H) - y, rng, O, D, Tv);
+    uint32_t inst = 0xffffffffu, prim = 0xffffffffu;
+    float tmax = kDstMax;
+    if (Tv > 0) {
+        const float Oa[3] = {O.x, O.y, O.z}, Da[3] = {D.x, D.y, D.z};
+        float t = kDstMax, u = 0, v = 0;
+        uint32_t p = 0xffffffffu, in = 0;
+        if (trace<float>(*s, Oa, Da, st->ray_epsilon, t, false, p, u, v, &in)) {
+            inst = in;
+            prim = s->twoLevel ? p - s->meshTriBase[s->instMesh[in]] : p;
+            tmax = t;
+        }
+    }
+    const float r[9] = {cam->position[0], cam->position[1], cam->position[2], u2f(inst), D.x, D.y, D.z, u2f(prim),
+                        tmax};
+    std::memcpy(out, r, sizeof(r));
 }
 
 void orc_trace_closest(const orc_scene* s, const float* O4, const float* D4, uint32_t n, float tmin, uint32_t* hits)

@@ -53,6 +53,9 @@ void orc_trace_closest(const orc_scene* s, const float* O4, const float* D4, uin
 
 /* One ray over [tmin, tmax]: closest hit (any = 0) or first hit (any = 1).
  * Returns 1 on a hit with prim, t and barycentrics (u, v) set. */
+// RayPickResult (9 words) of the RayPick raygen for pixel (x, y).
+void orc_pick_ray(const orc_scene* s, const tr_camera* cam, const tr_kernel_settings* st, uint32_t width,
+                  uint32_t height, int32_t x, int32_t y, float* out);
 int orc_trace_ray(const orc_scene* s, const float* O, const float* D, float tmin, float tmax, int any, uint32_t* prim,
                   float* t, float* u, float* v, uint32_t* inst);
 

@@ -372,6 +372,25 @@ void ref_shadow(void* ctx, const tr_camera* cam, const tr_kernel_settings* st, u
     refo_launch(shadowCount, 1, 1);
 }
 
+// DeviceRenderer::PickRay (DeviceRenderer.cpp:71-92): the RayPick raygen (optix.cu:345-377) for
+// one pixel; out = the RayPickResult's 9 words.
+void ref_pick_ray(void* ctx, const tr_camera* cam, const tr_kernel_settings* st, uint32_t W, uint32_t H, int32_t x,
+                  int32_t y, float* out)
+{
+    RefCtx* c = static_cast<RefCtx*>(ctx);
+    bind_scene(c);
+    set_frame_params(c, cam, st, W, H, 0, nullptr, nullptr, nullptr, nullptr);
+    RayPickResult r{};
+    c->lp.rayGenMode = RayGenModes::RayPick;
+    c->lp.rayPickPixel = make_int2(x, y);
+    c->lp.rayPickResult = &r;
+    refo_set_params(c->lp);
+    refo_launch(1, 1, 1);
+    c->lp.rayPickResult = nullptr;
+    static_assert(sizeof(RayPickResult) == 9 * sizeof(float), "RayPickResult is 9 words");
+    std::memcpy(out, &r, sizeof(r));
+}
+
 // DeviceRenderer::RenderFrame (DeviceRenderer.cpp:97-133) for one frame:
 // accumulator in/out (float4 per pixel); ext/shadow ray counts per bounce.
 void ref_render_frame(void* ctx, const tr_camera* cam, const tr_kernel_settings* st, uint32_t W, uint32_t H,

@@ -9,9 +9,11 @@ expected values; nothing here is written from memory.
 
     python tests/golden/make_golden.py              # every fixture
     python tests/golden/make_golden.py debug_modes  # only ref_debug_modes.npz
+    python tests/golden/make_golden.py ray_picks    # only ref_ray_pick.npz
 """
 from __future__ import annotations
 
+import dataclasses
 import sys
 from pathlib import Path
 
@@ -126,12 +128,55 @@ def debug_mode_frames(width=40, height=30, seed=5, ao_dist=0.6, z_depth_max=3.0)
     return out
 
 
+PICK_CAMERA_FIELDS = ("position", "target", "up", "fov", "aperture", "distortion", "focal_dist", "bokeh_side_count",
+                      "bokeh_rotation")
+
+
+def pick_cases():
+    """(name, scene, camera) triples of the ray-pick fixture: the Cornell box, the two-level Cornell
+    box and a heightfield seen through a six-bladed aperture with lens distortion (misses included)."""
+    hf = tr.heightfield(n=16, width=32, height=32)
+    lens = dataclasses.replace(hf.camera, aperture=0.05, focal_dist=12.0, bokeh_side_count=6, bokeh_rotation=0.3,
+                               distortion=0.1)
+    return [("cornell", tr.cornell_box(width=40, height=30), None),
+            ("instanced_cornell", tr.instanced_cornell(width=40, height=30), None),
+            ("heightfield_lens", hf, lens)]
+
+
+def pick_pixels(w, h):
+    """Every third column and second row plus a margin of two pixels outside the image."""
+    return np.array([(x, y) for x in range(-2, w + 2, 3) for y in range(-2, h + 3, 2)], np.int32)
+
+
+def ray_picks():
+    """DeviceRenderer::PickRay results (RayPickResult words, as uint32) by the reference's RayPick
+    raygen (optix.cu:345-377) compiled as host C++."""
+    out = {}
+    st = KernelSettings(flags=tr.TR_FLAG_REFERENCE_SAMPLING | tr._abi.TR_FLAG_REFERENCE_DRAW_RTL)
+    for name, scene, cam in pick_cases():
+        cam = cam or scene.camera
+        ref = Reference(scene)
+        px = pick_pixels(scene.width, scene.height)
+        res = np.stack([ref.pick_ray(cam, st, scene.width, scene.height, x, y) for x, y in px])
+        out[f"{name}_digest"] = np.array(scene.digest())
+        out[f"{name}_camera"] = np.array([float(np.asarray(getattr(cam, f), np.float64).ravel()[i])
+                                          for f in PICK_CAMERA_FIELDS
+                                          for i in range(np.asarray(getattr(cam, f)).size)], np.float64)
+        out[f"{name}_size"] = np.array([scene.width, scene.height], np.int32)
+        out[f"{name}_pixels"] = px
+        out[f"{name}_result"] = res.view(np.uint32)
+    return out
+
+
 def main():
-    if sys.argv[1:] == ["debug_modes"]:
+    if sys.argv[1:] in (["debug_modes"], ["ray_picks"]):
         build.build_oracle()
         if build.build_reference() is None:
             raise SystemExit("reference sources not found")
-        np.savez_compressed(OUT / "ref_debug_modes.npz", **debug_mode_frames())
+        if sys.argv[1] == "debug_modes":
+            np.savez_compressed(OUT / "ref_debug_modes.npz", **debug_mode_frames())
+        else:
+            np.savez_compressed(OUT / "ref_ray_pick.npz", **ray_picks())
         return
     build.build_oracle()
     if build.build_reference() is None:
@@ -153,6 +198,8 @@ def main():
     np.savez_compressed(OUT / "ref_cornell_24x16_ms2.npz", **cornell_reference_frames(24, 16, ms=2, seed=9))
     # the other render modes
     np.savez_compressed(OUT / "ref_debug_modes.npz", **debug_mode_frames())
+    # ray picks
+    np.savez_compressed(OUT / "ref_ray_pick.npz", **ray_picks())
     for p in sorted(OUT.glob("*.npz")):
         print(p.name, p.stat().st_size)
 

@@ -52,6 +52,7 @@ def test_struct_layouts_match_ctypes(tmp_path):
         "tr_batch_item": _abi.BatchItem,
         "tr_batch_info": _abi.BatchInfo,
         "tr_batch_statistics": _abi.BatchStatistics,
+        "tr_ray_pick_result": _abi.RayPickResult,
     }
     lines = ['#include <stdio.h>', '#include <stddef.h>', f'#include "{HEADER}"', "int main(void){"]
     for cname, py in structs.items():

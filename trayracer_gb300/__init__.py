@@ -10,7 +10,8 @@ from ._abi import (  # noqa: F401
     TR_MAX_DEPTH,
     load_library,
 )
-from .renderer import BatchRenderer, DeviceRenderer, KernelSettings, RenderModes, TracerError, camera_to_c, settings_for  # noqa: F401
+from .renderer import (BatchRenderer, DeviceRenderer, KernelSettings, RayPickResult, RenderModes,  # noqa: F401
+                       TracerError, camera_to_c, settings_for)
 from .scenes import (  # noqa: F401
     CameraSpec,
     Scene,

@@ -181,6 +181,18 @@ class Tuning(C.Structure):
     ]
 
 
+class RayPickResult(C.Structure):
+    """tr_ray_pick_result (RayPickResult, CommonStructs.h:132-141)."""
+
+    _fields_ = [
+        ("ray_origin", C.c_float * 3),
+        ("inst_ix", C.c_uint32),
+        ("ray_dir", C.c_float * 3),
+        ("prim_ix", C.c_uint32),
+        ("tmax", C.c_float),
+    ]
+
+
 class TuneReport(C.Structure):
     _fields_ = [
         ("chosen", Tuning),
@@ -267,6 +279,7 @@ FUNCTIONS = {
     "tr_adjoint_frame": (C.c_int, [_V, _V, _V, C.c_float, _V]),
     "tr_render_frame_noalloc": (C.c_int, [_V, _V, _V, _V, _U]),
     "tr_set_render_mode": (C.c_int, [_V, _U, _U, C.c_float, C.c_float]),
+    "tr_pick_ray": (C.c_int, [_V, _V, C.c_int32, C.c_int32, C.POINTER(RayPickResult)]),
     "tr_get_tuning": (C.c_int, [_V, C.POINTER(Tuning)]),
     "tr_set_tuning": (C.c_int, [_V, C.POINTER(Tuning)]),
     "tr_autotune": (C.c_int, [_V, _V, _U, C.POINTER(TuneReport)]),

@@ -116,6 +116,7 @@ struct Context {
     LaunchShape shape{};
     uint32_t sampleCount = 0;
     uint32_t* hostCounters = nullptr;  // pinned
+    float* pickResult = nullptr;       // 9 words of the frame arena (tr_pick_ray)
 
     // timing
     cudaEvent_t evStart = nullptr, evGenerate = nullptr, evFinal = nullptr;
@@ -278,6 +279,7 @@ tr_status ensure_frame(Context* c)
     const size_t oTrav = take(4 * sizeof(unsigned long long));
     const size_t oKeys = take(cap * sizeof(uint32_t));
     const size_t oOrder = take(cap * sizeof(uint32_t));
+    const size_t oPick = take(16 * sizeof(float));
     void* base = nullptr;
     const cudaError_t e = cudaMalloc(&base, off);
     if (e != cudaSuccess)
@@ -301,6 +303,7 @@ tr_status ensure_frame(Context* c)
     f.traversal = reinterpret_cast<unsigned long long*>(b + oTrav);
     c->sort.keys = reinterpret_cast<uint32_t*>(b + oKeys);
     c->sort.order = reinterpret_cast<uint32_t*>(b + oOrder);
+    c->pickResult = reinterpret_cast<float*>(b + oPick);
     f.capacity = uint32_t(cap);
     f.resX = c->width;
     f.resY = c->height;
@@ -810,6 +813,26 @@ tr_status tr_set_render_mode(void* ctx, uint32_t mode, uint32_t flags, float ao_
         invalidate_graph(c);
         return tr_reset(ctx);
     }
+    return TR_OK;
+}
+
+tr_status tr_pick_ray(void* ctx, void* stream, int32_t x, int32_t y, tr_ray_pick_result* out)
+{
+    if (!ctx || !out)
+        return TR_ERR_INVALID_ARGUMENT;
+    Context* c = static_cast<Context*>(ctx);
+    cudaSetDevice(c->device);
+    tr_status st = check_ready(c);
+    if (st != TR_OK)
+        return st;
+    cudaStream_t s = pick_stream(c, stream);
+    TR_CUDA(c, launch_pick_ray(c->scene, c->camera, c->settings, c->width, c->height, x, y, c->pickResult,
+                               c->frame.errorFlag, s));
+    float r[9];
+    TR_CUDA(c, cudaMemcpyAsync(r, c->pickResult, sizeof(r), cudaMemcpyDeviceToHost, s));
+    TR_CUDA(c, cudaStreamSynchronize(s));
+    static_assert(sizeof(tr_ray_pick_result) == sizeof(r), "tr_ray_pick_result is 9 words");
+    std::memcpy(out, r, sizeof(r));
     return TR_OK;
 }
 

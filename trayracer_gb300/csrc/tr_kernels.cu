@@ -155,7 +155,7 @@ __device__ __forceinline__ bool distort(float2& lens, float tanFov2, float disto
 
 // GenerateCameraRay, optix.cu:142-174
 template <class Rng>
-__device__ __forceinline__ void camera_ray(const Camera& cam, uint32_t resX, uint32_t resY, uint32_t ix, uint32_t iy,
+__device__ __forceinline__ void camera_ray(const Camera& cam, uint32_t resX, uint32_t resY, int ix, int iy,
                                            Rng& rng, bool rtl, float3& O, float3& D, float& T)
 {
     O = cam.pos;
@@ -978,6 +978,41 @@ __global__ void __launch_bounds__(128) debug_extend_kernel(SceneView s, FrameVie
     }
 }
 
+// RayPick raygen (optix.cu:345-377): the camera ray of pixel (x, resY - y) with the
+// random stream seeded 0, traced closest-hit; result = RayPickResult (7 words:
+// camera position, instIx, direction, primIx, tmax).
+__global__ void __launch_bounds__(32) pick_ray_kernel(SceneView s, Camera cam, Settings st, uint32_t resX,
+                                                      uint32_t resY, int x, int y, float* result, uint32_t* errorFlag)
+{
+    if (threadIdx.x != 0)
+        return;
+    RefRng rng{0u};
+    float3 O, D;
+    float T;
+    camera_ray(cam, resX, resY, x, int(resY) - y, rng, (st.flags & TR_FLAG_REFERENCE_DRAW_RTL) != 0, O, D, T);
+    uint32_t inst = 0xffffffffu, prim = 0xffffffffu;
+    float tmax = kDstMax;
+    if (T > 0.f) {
+        uint32_t slot = 0xffffffffu, hitInst = 0;
+        float u = 0.f, v = 0.f;
+        if (!traverse<false>(s, O, D, st.rayEpsilon, tmax, slot, u, v, nullptr, &hitInst))
+            atomicOr(errorFlag, 1u);
+        if (slot != 0xffffffffu) {
+            inst = hitInst;
+            prim = __float_as_uint(__ldg(s.bvhTris + 3u * slot).w);
+        }
+    }
+    result[0] = cam.pos.x;
+    result[1] = cam.pos.y;
+    result[2] = cam.pos.z;
+    result[3] = __uint_as_float(inst);
+    result[4] = D.x;
+    result[5] = D.y;
+    result[6] = D.z;
+    result[7] = __uint_as_float(prim);
+    result[8] = tmax;
+}
+
 // OrthonormalBase + SampleCosineHemisphere (CudaUtility.h:182-199, 271-292)
 __device__ __forceinline__ float3 cosine_hemisphere(const float3& n, float r0, float r1)
 {
@@ -1720,6 +1755,13 @@ cudaError_t launch_debug_bounce(const SceneView& s, const FrameView& f, const Ca
     const uint32_t blocks = shape.sms * 8u;
     debug_extend_kernel<<<blocks, 128, 0, stream>>>(s, f, cam, st, bounce);
     debug_shade_kernel<<<blocks, 128, 0, stream>>>(s, f, cam, st, bounce);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_pick_ray(const SceneView& s, const Camera& cam, const Settings& st, uint32_t resX, uint32_t resY,
+                            int x, int y, float* result, uint32_t* errorFlag, cudaStream_t stream)
+{
+    pick_ray_kernel<<<1, 32, 0, stream>>>(s, cam, st, resX, resY, x, y, result, errorFlag);
     return cudaGetLastError();
 }
 

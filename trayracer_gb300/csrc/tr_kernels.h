@@ -41,6 +41,10 @@ cudaError_t launch_finalize(const FrameView& f, const Settings& st, cudaStream_t
 // closest hit of every ray of queue state[bounce & 1], then the mode's shade.
 cudaError_t launch_debug_bounce(const SceneView& s, const FrameView& f, const Camera& cam, const Settings& st,
                                 uint32_t bounce, const LaunchShape& shape, cudaStream_t stream);
+// RayPick: one camera ray through pixel (x, resY - y), closest hit; result holds
+// 9 words laid out as tr_ray_pick_result.
+cudaError_t launch_pick_ray(const SceneView& s, const Camera& cam, const Settings& st, uint32_t resX, uint32_t resY,
+                            int x, int y, float* result, uint32_t* errorFlag, cudaStream_t stream);
 // Counting sort of the bounce's hit queue by material into sv.order (shade
 // reads the queue through it when FrameView::hitOrder = sv.order).
 cudaError_t launch_sort_hits(const SceneView& s, const FrameView& f, const SortView& sv, uint32_t bounce,

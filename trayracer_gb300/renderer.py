@@ -2,7 +2,7 @@
 
 ``DeviceRenderer`` follows Tracer::DeviceRenderer (Tracer/Renderer/DeviceRenderer.h:21-67):
 RenderFrame(kernelSettings, renderMode, renderFlags), Reset, SetCamera, Resize,
-Statistics, SampleCount, Resolution, Accumulator/ColorBuffer; ``UpdateScene``
+Statistics, SampleCount, Resolution, Accumulator/ColorBuffer, PickRay; ``UpdateScene``
 follows Renderer::UpdateScene (Tracer/Renderer/Renderer.h:49). Where the
 reference calls FatalError -> exit (Tracer/CUDA/CudaError.cpp:13-25) these
 methods raise ``TracerError`` with the C status.
@@ -64,6 +64,21 @@ class KernelSettings:
     def to_c(self) -> _abi.KernelSettings:
         return _abi.KernelSettings(self.multiSample, self.maxDepth, self.seed & 0xFFFFFFFF, self.rayEpsilon,
                                    min(self.rrStart, 0xFFFFFFFF), self.flags, self.maxColor, 0)
+
+
+@dataclass(frozen=True)
+class RayPickResult:
+    """RayPickResult (CommonStructs.h:132-141); instIx and primIx are 0xFFFFFFFF on a miss."""
+
+    rayOrigin: tuple
+    instIx: int
+    rayDir: tuple
+    primIx: int
+    tmax: float
+
+    @property
+    def hit(self) -> bool:
+        return self.primIx != 0xFFFFFFFF
 
 
 def camera_to_c(cam: CameraSpec) -> _abi.Camera:
@@ -259,6 +274,15 @@ class DeviceRenderer:
         chosen = {f: getattr(rep.chosen, f) for f, _ in rep.chosen._fields_ if f != "reserved"}
         return {"chosen": chosen, "frame_ms_default": rep.frame_ms_default, "frame_ms_tuned": rep.frame_ms_tuned,
                 "trials": rep.trials}
+
+    def PickRay(self, pixelIndex, stream: int = 0) -> RayPickResult:
+        """DeviceRenderer::PickRay (DeviceRenderer.cpp:71-92): what the camera ray through pixel
+        (x, y) hits first; waits for the result."""
+        x, y = pixelIndex
+        r = _abi.RayPickResult()
+        self._check(self._lib.tr_pick_ray(self._ctx, C.c_void_p(stream or None), int(x), int(y), C.byref(r)),
+                    "tr_pick_ray")
+        return RayPickResult(tuple(r.ray_origin), int(r.inst_ix), tuple(r.ray_dir), int(r.prim_ix), float(r.tmax))
 
     def Synchronize(self, stream: int = 0):
         self._check(self._lib.tr_synchronize(self._ctx, C.c_void_p(stream or None)), "tr_synchronize")
