@@ -365,6 +365,25 @@ tr_status tr_render_frame_noalloc(void* ctx, void* stream, float* accumulator, f
  * accumulation. */
 tr_status tr_set_render_mode(void* ctx, uint32_t mode, uint32_t flags, float ao_dist, float z_depth_max);
 
+/* ---- sky ----
+ * ≙ Tracer::Sky (Tracer/Renderer/Sky.h:16-67, Sky.cpp): the Preetham sky that a
+ * path sees when it leaves the scene (SampleSky, CudaSky.h:105-156, called by
+ * PathTracing.h:40-55). A context starts with the sky disabled (misses are
+ * black); the reference's Scene starts with Sky's defaults (enabled, sun
+ * straight up, 32 arc minutes, intensity 1000, turbidity 4, bias 1). */
+typedef struct tr_sky_desc {
+    uint32_t enabled;
+    uint32_t draw_sun;            /* the sun disc is seen by camera and specular paths */
+    float sun_dir[3];             /* normalised on set (Sky::SetSunDir) */
+    float sun_angular_diameter;   /* arc minutes */
+    float sun_intensity;
+    float turbidity;              /* clamped to [1, 10] (Sky::SetTurbidity) */
+    float selection_bias;         /* Sky::SetSelectionBias: scales the sun's NEE energy */
+} tr_sky_desc;
+
+/* Sets (or with sky = NULL disables) the sky; resets the accumulation. */
+tr_status tr_set_sky(void* ctx, const tr_sky_desc* sky);
+
 /* ---- ray pick ----
  * ≙ RayPickResult (CommonStructs.h:132-141): the camera position, the direction
  * of the picked pixel's camera ray, and what the ray hit first (instance and

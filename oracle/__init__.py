@@ -56,6 +56,7 @@ class Oracle:
             lib.orc_trace_ray.restype = C.c_int
             lib.orc_trace_ray.argtypes = [_P, _P, _P, C.c_float, C.c_float, C.c_int, _P, _P, _P, _P, _P]
             lib.orc_pick_ray.argtypes = [_P, _P, _P, _U, _U, C.c_int32, C.c_int32, _P]
+            lib.orc_set_sky.argtypes = [_P, _P]
             lib.orc_ties.restype = _U
             lib.orc_ties.argtypes = [_P, _P, _P, C.c_float, C.c_float, C.c_float, _P, _U, _P]
             lib.orc_trace_any.argtypes = [_P, _P, _P, _U, C.c_float, _P]
@@ -102,6 +103,11 @@ class Oracle:
         self._lib.orc_generate(self._s, C.addressof(cc), C.addressof(st), width, height, sample_count, first, n,
                                _ptr(O), _ptr(D), _ptr(T))
         return O, D, T
+
+    def set_sky(self, sky):
+        """Sky seen by paths that leave the scene (a trayracer_gb300 SkySettings, or None: disabled)."""
+        self._sky = sky.to_c() if sky is not None else None
+        self._lib.orc_set_sky(self._s, C.addressof(self._sky) if self._sky is not None else None)
 
     def pick_ray(self, cam: CameraSpec, settings, width, height, x, y) -> np.ndarray:
         """RayPickResult of pixel (x, y) as 9 float32 words (instIx, primIx as bit patterns)."""
@@ -243,6 +249,7 @@ class Reference:
             lib.ref_rng.argtypes = [_U, _U, _U, _P]
             lib.ref_set_render_mode.argtypes = [_U, _U, C.c_float, C.c_float]
             lib.ref_pick_ray.argtypes = [_P, _P, _P, _U, _U, C.c_int32, C.c_int32, _P]
+            lib.ref_set_sky.argtypes = [_P, _P]
             cls._lib = lib
         return cls._lib
 
@@ -286,6 +293,11 @@ class Reference:
         self._lib.ref_render_frame(self._c, C.addressof(cc), C.addressof(st), width, height, sample_count,
                                    _ptr(accumulator), _ptr(ext), _ptr(sh))
         return ext, sh
+
+    def set_sky(self, sky):
+        """The SkyData of a Tracer::Sky with these settings (None: disabled)."""
+        self._sky = sky.to_c() if sky is not None else None
+        self._lib.ref_set_sky(self._c, C.addressof(self._sky) if self._sky is not None else None)
 
     def pick_ray(self, cam: CameraSpec, settings, width, height, x, y) -> np.ndarray:
         """DeviceRenderer::PickRay through the RayPick raygen: RayPickResult as 9 float32 words."""

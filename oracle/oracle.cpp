@@ -254,6 +254,15 @@ struct orc_scene {
     std::vector<float> instInv;
     std::vector<std::vector<Node>> meshNodes;
     std::vector<std::vector<uint32_t>> meshRefs;
+    // Sky::Build (Sky.cpp): the SkyData fields SampleSky reads; disabled by default
+    struct {
+        float sunDir[3] = {0.f, 1.f, 0.f};
+        int enabled = 0;
+        float drawSun = 0.f;
+        float cosSunAngularDiameter = 1.f;
+        float sunIntensity = 0.f;
+        float turbidity = 4.f;
+    } sky;
 };
 
 namespace {
@@ -1328,6 +1337,70 @@ V3<T> sample_light(const orc_scene& S, Rng& rng, V3<T> I, V3<T> N, T& prob, T& p
     return -Ld;
 }
 
+// SampleSky, CudaSky.h:105-156 (Preetham sky), every term evaluated per call in T
+// as the reference does; black when the sky is disabled.
+template <class T>
+V3<T> sample_sky(const orc_scene& S, V3<T> D, bool drawSun)
+{
+    using std::acos;
+    using std::cos;
+    using std::exp;
+    using std::pow;
+    const auto& k = S.sky;
+    if (k.enabled == 0)
+        return v3s(T(0));
+    const T Pi = K<T>::Pi;
+    const V3<T> sunDir = v3(T(k.sunDir[0]), T(k.sunDir[1]), T(k.sunDir[2]));
+    const T cosAD = T(k.cosSunAngularDiameter);
+    const V3<T> up = v3(T(0), T(1), T(0));
+    const T cosSunUp = dot(sunDir, up);
+    auto sat = [](T x) { return x < T(0) ? T(0) : (x > T(1) ? T(1) : x); };
+    T sunfade = T(1) - sat(T(1) - exp(-sunDir.z / T(500)));
+    const T rayleigh = T(2.5f) - (T(1) * (T(1) - sunfade));
+    const T lambda[3] = {T(620e-9f), T(492e-9f), T(390e-9f)};
+    const T K[3] = {T(0.686f), T(0.678f), T(0.666f)};
+    const T num = T(8) * pow(Pi, T(3)) * pow(pow(T(1.0003f), T(2)) - T(1), T(2)) * (T(6) + T(3) * T(0.031f));
+    const T c = T(0.2f) * T(k.turbidity) * T(10e-18f);
+    T bR[3], bM[3];
+    for (int i = 0; i < 3; ++i) {
+        bR[i] = (num / ((T(3) * T(2.545e25f)) * pow(lambda[i], T(4)) * (T(6) - T(7) * T(0.031f)))) * rayleigh;
+        bM[i] = (T(0.434f) * c * Pi * pow((T(2) * Pi) / lambda[i], T(4) - T(2)) * K[i]) * T(0.005f);
+    }
+    const T zenith = acos(std::max(dot(up, D), T(0)));
+    const T denom = cos(zenith) + T(0.15f) * pow(T(93.885f) - ((zenith * T(180)) / Pi), T(-1.253f));
+    const T sR = T(8.4e3f) / denom, sM = T(1.25e3f) / denom;
+    const T cosTheta = dot(D, sunDir);
+    const T rPhase = (T(3) / (T(16) * Pi)) * (T(1) + pow(cosTheta * T(0.5f) + T(0.5f), T(2)));
+    const T g = T(0.80f);
+    const T hg = (T(1) / (T(4) * Pi)) * ((T(1) - pow(g, T(2))) / pow(T(1) - T(2) * g * cosTheta + pow(g, T(2)), T(1.5f)));
+    const T sunE = T(k.sunIntensity) *
+                   std::max(T(0), T(1) - exp(-(((Pi / T(1.95f)) - acos(cosSunUp)) / T(1.5f))));
+    const T hmix = sat(pow(T(1) - cosSunUp, T(5)));
+    const T e0 = cosAD, e1 = cosAD + T(2e-5f);
+    const T y = std::max(T(0), std::min((cosTheta - e0) / (e1 - e0), T(1)));
+    const T sundisk = y * y * (T(3) - (T(2) * y));
+    T Fex[3], Lin[3], L0[3];
+    for (int i = 0; i < 3; ++i) {
+        Fex[i] = exp(-(bR[i] * sR + bM[i] * sM));
+        const T ratio = ((bR[i] * rPhase) + (bM[i] * hg)) / (bR[i] + bM[i]);
+        Lin[i] = pow((sunE * ratio) * (T(1) - Fex[i]), T(1.5f));
+        Lin[i] = Lin[i] * ((T(1) * (T(1) - hmix)) + (pow((sunE * ratio) * Fex[i], T(0.5f)) * hmix));
+        L0[i] = (T(0.1f) * Fex[i]) + ((((sunE * T(19000)) * Fex[i]) * sundisk) * (drawSun ? T(1) : T(0)));
+    }
+    const T luma = L0[0] * T(0.299f) + L0[1] * T(0.587f) + L0[2] * T(0.114f);
+    const T t = std::max(sunDir.y, T(0));
+    sunfade = sunfade * ((T(1) * (T(1) - t)) + (T(0.9f) * t));
+    const T expo = T(1) / (T(1) + sunfade);
+    T out[3];
+    for (int i = 0; i < 3; ++i) {
+        const T l0 = (luma * (T(1) - T(0.5f))) + (L0[i] * T(0.5f));
+        const T cc = Lin[i] + l0;
+        const T tm = (cc * (T(1) + cc / T(1000))) / (cc + T(128));
+        out[i] = pow(std::max(T(0), tm), expo);
+    }
+    return v3(out[0], out[1], out[2]);
+}
+
 // PathTracingKernel body, PathTracing.h:15-174
 template <class T, bool REF, class Rng>
 ShadeOut<T> shade_one(const orc_scene& S, const tr_kernel_settings& st, uint32_t bounce, V3<T> O, V3<T> D,
@@ -1337,8 +1410,14 @@ ShadeOut<T> shade_one(const orc_scene& S, const tr_kernel_settings& st, uint32_t
     ShadeOut<T> out;
     const T maxColor = T(st.max_color > 0.f ? st.max_color : 10.f);
     const V3<T> I = O + D * tmax;
-    if (primIx == 0xffffffffu)
-        return out;  // sky disabled: black
+    if (primIx == 0xffffffffu) {
+        // PathTracing.h:40-55: T * SampleSky, the sun disc for camera and specular paths
+        if (S.sky.enabled) {
+            const bool sun = S.sky.drawSun != 0.f && (bounce == 0 || (flags & 1u));
+            out.add = safe_color<T>(Tp * sample_sky<T>(S, D, sun), maxColor);
+        }
+        return out;
+    }
     const Surface<T> sf = surface_at<T>(S, primIx, bu, bv, D, inst);
     const HitMat<T> m = hit_material<T>(S.mats[sf.matIx]);
     out.hit = true;
@@ -1878,6 +1957,25 @@ orc_scene* orc_scene_create(const tr_scene_desc* desc)
 }
 
 void orc_scene_destroy(orc_scene* s) { delete s; }
+
+// Sky::SetSunDir (normalised with helper_math's normalize), SetTurbidity (clamp to
+// [1, 10]) and Sky::Build (cos of the angular diameter in radians); NULL disables.
+void orc_set_sky(orc_scene* s, const tr_sky_desc* sky)
+{
+    if (!sky) {
+        s->sky.enabled = 0;
+        return;
+    }
+    const float* d = sky->sun_dir;
+    const float inv = 1.0f / std::sqrt(d[0] * d[0] + d[1] * d[1] + d[2] * d[2]);
+    for (int i = 0; i < 3; ++i)
+        s->sky.sunDir[i] = d[i] * inv;
+    s->sky.enabled = sky->enabled ? 1 : 0;
+    s->sky.drawSun = sky->draw_sun ? 1.f : 0.f;
+    s->sky.cosSunAngularDiameter = std::cos(sky->sun_angular_diameter * K<float>::Pi / (60.f * 180.f));
+    s->sky.sunIntensity = sky->sun_intensity;
+    s->sky.turbidity = std::fmin(std::fmax(sky->turbidity, 1.f), 10.f);
+}
 uint32_t orc_light_count(const orc_scene* s) { return uint32_t(s->lights.size()); }
 float orc_light_energy(const orc_scene* s, int total) { return total ? s->lightEnergyTotal : s->lightEnergy; }
 

@@ -53,6 +53,8 @@ void orc_trace_closest(const orc_scene* s, const float* O4, const float* D4, uin
 
 /* One ray over [tmin, tmax]: closest hit (any = 0) or first hit (any = 1).
  * Returns 1 on a hit with prim, t and barycentrics (u, v) set. */
+// Sky seen by paths that leave the scene (NULL: disabled, the default).
+void orc_set_sky(orc_scene* s, const tr_sky_desc* sky);
 // RayPickResult (9 words) of the RayPick raygen for pixel (x, y).
 void orc_pick_ray(const orc_scene* s, const tr_camera* cam, const tr_kernel_settings* st, uint32_t width,
                   uint32_t height, int32_t x, int32_t y, float* out);

@@ -372,6 +372,29 @@ void ref_shadow(void* ctx, const tr_camera* cam, const tr_kernel_settings* st, u
     refo_launch(shadowCount, 1, 1);
 }
 
+// Sky::SetSunDir / SetTurbidity / Build (Sky.cpp): the SkyData the reference's SampleSky
+// reads (NULL: disabled, as a context starts).
+void ref_set_sky(void* ctx, const tr_sky_desc* sky)
+{
+    RefCtx* c = static_cast<RefCtx*>(ctx);
+    c->sky = SkyData{};
+    if (!sky)
+        return;
+    const float3 dir = normalize(make_float3(sky->sun_dir[0], sky->sun_dir[1], sky->sun_dir[2]));
+    constexpr float Pi = 3.1415926535897932f;  // LinearMath.h:16
+    const float diameter = sky->sun_angular_diameter * Pi / (60.f * 180.f);
+    const float radius = diameter * .5f;
+    c->sky.sunDir = dir;
+    c->sky.skyEnabled = sky->enabled ? 1 : 0;
+    c->sky.drawSun = sky->draw_sun ? 1.f : 0.f;
+    c->sky.sunArea = Pi * radius * radius;
+    c->sky.cosSunAngularDiameter = cosf(diameter);
+    c->sky.sunIntensity = sky->sun_intensity;
+    c->sky.turbidity = clamp(sky->turbidity, 1.f, 10.f);
+    c->sky.selectionBias = sky->selection_bias;
+    c->sky.sunEnergy = sky->enabled ? sky->sun_intensity * sky->selection_bias : 0.f;
+}
+
 // DeviceRenderer::PickRay (DeviceRenderer.cpp:71-92): the RayPick raygen (optix.cu:345-377) for
 // one pixel; out = the RayPickResult's 9 words.
 void ref_pick_ray(void* ctx, const tr_camera* cam, const tr_kernel_settings* st, uint32_t W, uint32_t H, int32_t x,

@@ -10,6 +10,7 @@ expected values; nothing here is written from memory.
     python tests/golden/make_golden.py              # every fixture
     python tests/golden/make_golden.py debug_modes  # only ref_debug_modes.npz
     python tests/golden/make_golden.py ray_picks    # only ref_ray_pick.npz
+    python tests/golden/make_golden.py sky          # only ref_sky.npz
 """
 from __future__ import annotations
 
@@ -168,15 +169,38 @@ def ray_picks():
     return out
 
 
+SKY_CASES = {
+    "sun_high": dict(sunDir=(0.2, 0.9, 0.4)),
+    "sun_low": dict(sunDir=(0.4, 0.15, 0.8), turbidity=6.5, sunAngularDiameter=300.0),
+    "sun_set": dict(sunDir=(0.0, -0.2, 1.0), drawSun=False),
+}
+
+
+def sky_frames(width=32, height=24, seed=3, max_depth=4):
+    """One frame of the outdoor heightfield (Lambert) under three skies by the reference's
+    kernels (SampleSky, CudaSky.h:105-156, on every path that leaves the scene)."""
+    scene = tr.outdoor_heightfield(width=width, height=height, lambert=True)
+    st = KernelSettings(multiSample=1, maxDepth=max_depth, seed=seed, rrStart=1,
+                        flags=tr.TR_FLAG_REFERENCE_SAMPLING | tr._abi.TR_FLAG_REFERENCE_DRAW_RTL)
+    out = dict(digest=np.array(scene.digest()), width=width, height=height, seed=seed, max_depth=max_depth)
+    for name, kw in SKY_CASES.items():
+        ref = Reference(scene)
+        ref.set_sky(tr.SkySettings(**kw))
+        acc = np.zeros((width * height, 4), np.float32)
+        ref.render_frame(scene.camera, st, width, height, 0, acc)
+        out[f"{name}_acc"] = acc
+    return out
+
+
 def main():
-    if sys.argv[1:] in (["debug_modes"], ["ray_picks"]):
+    single = {"debug_modes": ("ref_debug_modes.npz", debug_mode_frames), "ray_picks": ("ref_ray_pick.npz", ray_picks),
+              "sky": ("ref_sky.npz", sky_frames)}
+    if len(sys.argv) == 2 and sys.argv[1] in single:
         build.build_oracle()
         if build.build_reference() is None:
             raise SystemExit("reference sources not found")
-        if sys.argv[1] == "debug_modes":
-            np.savez_compressed(OUT / "ref_debug_modes.npz", **debug_mode_frames())
-        else:
-            np.savez_compressed(OUT / "ref_ray_pick.npz", **ray_picks())
+        name, make = single[sys.argv[1]]
+        np.savez_compressed(OUT / name, **make())
         return
     build.build_oracle()
     if build.build_reference() is None:
@@ -200,6 +224,8 @@ def main():
     np.savez_compressed(OUT / "ref_debug_modes.npz", **debug_mode_frames())
     # ray picks
     np.savez_compressed(OUT / "ref_ray_pick.npz", **ray_picks())
+    # the sky
+    np.savez_compressed(OUT / "ref_sky.npz", **sky_frames())
     for p in sorted(OUT.glob("*.npz")):
         print(p.name, p.stat().st_size)
 

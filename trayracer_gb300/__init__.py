@@ -11,7 +11,7 @@ from ._abi import (  # noqa: F401
     load_library,
 )
 from .renderer import (BatchRenderer, DeviceRenderer, KernelSettings, RayPickResult, RenderModes,  # noqa: F401
-                       TracerError, camera_to_c, settings_for)
+                       SkySettings, TracerError, camera_to_c, settings_for)
 from .scenes import (  # noqa: F401
     CameraSpec,
     Scene,
@@ -19,6 +19,7 @@ from .scenes import (  # noqa: F401
     displaced_spheres,
     heightfield,
     instanced_cornell,
+    outdoor_heightfield,
     sphere_batch,
     sphere_scene,
 )

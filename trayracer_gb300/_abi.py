@@ -181,6 +181,20 @@ class Tuning(C.Structure):
     ]
 
 
+class SkyDesc(C.Structure):
+    """tr_sky_desc (Tracer::Sky settings, Sky.h:16-67)."""
+
+    _fields_ = [
+        ("enabled", C.c_uint32),
+        ("draw_sun", C.c_uint32),
+        ("sun_dir", C.c_float * 3),
+        ("sun_angular_diameter", C.c_float),
+        ("sun_intensity", C.c_float),
+        ("turbidity", C.c_float),
+        ("selection_bias", C.c_float),
+    ]
+
+
 class RayPickResult(C.Structure):
     """tr_ray_pick_result (RayPickResult, CommonStructs.h:132-141)."""
 
@@ -280,6 +294,7 @@ FUNCTIONS = {
     "tr_render_frame_noalloc": (C.c_int, [_V, _V, _V, _V, _U]),
     "tr_set_render_mode": (C.c_int, [_V, _U, _U, C.c_float, C.c_float]),
     "tr_pick_ray": (C.c_int, [_V, _V, C.c_int32, C.c_int32, C.POINTER(RayPickResult)]),
+    "tr_set_sky": (C.c_int, [_V, C.POINTER(SkyDesc)]),
     "tr_get_tuning": (C.c_int, [_V, C.POINTER(Tuning)]),
     "tr_set_tuning": (C.c_int, [_V, C.POINTER(Tuning)]),
     "tr_autotune": (C.c_int, [_V, _V, _U, C.POINTER(TuneReport)]),

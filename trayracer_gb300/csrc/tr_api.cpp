@@ -23,6 +23,7 @@
 #include "tr_accel.h"
 #include "tr_bvh.h"
 #include "tr_kernels.h"
+#include "tr_sky.h"
 #include "tr_scene.h"
 
 namespace {
@@ -748,6 +749,8 @@ tr_status tr_adjoint_frame(void* ctx, void* stream, const float* pixel_grad, flo
         return fail(c, TR_ERR_INVALID_ARGUMENT, "null gradient buffer");
     if (c->settings.flags & TR_FLAG_REFERENCE_SAMPLING)
         return fail(c, TR_ERR_INVALID_ARGUMENT, "the adjoint differentiates the default sampling mode only");
+    if (c->scene.sky.enabled)
+        return fail(c, TR_ERR_INVALID_ARGUMENT, "the adjoint differentiates scenes without a sky");
     tr_status st = check_ready(c);
     if (st != TR_OK)
         return st;
@@ -814,6 +817,27 @@ tr_status tr_set_render_mode(void* ctx, uint32_t mode, uint32_t flags, float ao_
         return tr_reset(ctx);
     }
     return TR_OK;
+}
+
+tr_status tr_set_sky(void* ctx, const tr_sky_desc* sky)
+{
+    if (!ctx)
+        return TR_ERR_INVALID_ARGUMENT;
+    Context* c = static_cast<Context*>(ctx);
+    if (sky) {
+        const float* d = sky->sun_dir;
+        if (!std::isfinite(d[0]) || !std::isfinite(d[1]) || !std::isfinite(d[2]) ||
+            !(d[0] * d[0] + d[1] * d[1] + d[2] * d[2] > 0.f))
+            return fail(c, TR_ERR_INVALID_ARGUMENT, "sun_dir must be a finite non-zero vector");
+        if (!std::isfinite(sky->sun_angular_diameter) || !std::isfinite(sky->sun_intensity) ||
+            !std::isfinite(sky->turbidity) || !std::isfinite(sky->selection_bias))
+            return fail(c, TR_ERR_INVALID_ARGUMENT, "sky parameters must be finite");
+        c->scene.sky = make_sky(*sky);
+    } else {
+        c->scene.sky = SkyView{};
+    }
+    invalidate_graph(c);
+    return tr_reset(ctx);
 }
 
 tr_status tr_pick_ray(void* ctx, void* stream, int32_t x, int32_t y, tr_ray_pick_result* out)

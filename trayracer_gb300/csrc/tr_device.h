@@ -85,6 +85,23 @@ struct alignas(16) CwbvhNode {
 static_assert(sizeof(CwbvhNode) == 80, "CwbvhNode must stay 80 bytes");
 
 // Scene as seen by the kernels (constant for one uploaded scene).
+// Preetham sky (CudaSky.h:105-156) with every term that does not depend on the
+// ray direction evaluated once on the host (tr_sky.h make_sky).
+struct SkyView {
+    float3 sunDir;
+    uint32_t enabled;
+    float3 betaR;          // TotalRayleigh * rayleigh coefficient
+    float drawSun;         // 1 or 0
+    float3 betaM;          // TotalMie * mie coefficient
+    float sunE;            // SunIntensity(cos sun-up angle)
+    float3 betaSum;        // betaR + betaM
+    float cosSunAngularDiameter;
+    float horizonMix;      // saturate((1 - cos sun-up angle)^5)
+    float exponent;        // 1 / (1 + sunfade)
+    float sunEnergy;       // Sky::SunEnergy (NEE pick weight)
+    float sunArea;
+};
+
 struct SceneView {
     const CwbvhNode* nodes;
     const float4* bvhTris;      // 3 float4 per triangle in BVH order: (v0, bits(primIx)), (e1, 0), (e2, 0)
@@ -105,6 +122,7 @@ struct SceneView {
     uint32_t nodeCount;
     uint32_t triCount;
     uint32_t pad;
+    SkyView sky;
 };
 
 struct BatchItem;

@@ -20,6 +20,7 @@
 //               PathTracing.h:45,90 and optix.cu:340).
 // Queue appends use one warp ballot + one atomicAdd per warp.
 #include "tr_kernels.h"
+#include "tr_sky.h"
 
 #include "tr_bsdf.cuh"
 #include "tr_bsdf_dual.cuh"
@@ -294,6 +295,25 @@ constexpr uint32_t kRefillBelow = 24;
 // rendered as a whole, default sampling mode) computes each path's camera ray
 // in place of reading a generated queue, and clears the path's radiance: the
 // primary rays never go through memory.
+// A path that leaves the scene sees the sky (PathTracing.h:40-55): T * SampleSky,
+// with the sun disc for camera and specular paths; a primary miss writes the sky
+// as its albedo guide. Out of line so that the traversal loop keeps its registers.
+__device__ __noinline__ void sky_miss(const SceneView& s, const FrameView& f, const Settings& st, uint32_t bounce,
+                                      float4 O4, float4 D4, float4 T4, bool aov)
+{
+    const uint32_t data = __float_as_uint(O4.w);
+    const uint32_t pathIx = path_ix(data);
+    const bool sun = s.sky.drawSun != 0.f && (bounce == 0 || (path_flags(data) & kFlagSpecular));
+    const float3 sky = sky_radiance(s.sky, f3(D4), sun);
+    const float3 add = safe_color(f3(T4) * sky, st.maxColor);
+    const float4 r = f.radiance[pathIx];
+    f.radiance[pathIx] = make_float4(r.x + add.x, r.y + add.y, r.z + add.z, r.w);
+    if (aov && pathIx < f.resX * f.resY) {
+        f.albedo[pathIx] = f4(sky, 0.f);
+        f.normals[pathIx] = make_float4(0.f, 0.f, 0.f, 0.f);
+    }
+}
+
 template <bool COUNT, bool BATCH, bool PRIMARY, bool TL>
 __global__ void __launch_bounds__(128, 8) extend_kernel(SceneView s, FrameView f, Settings st, uint32_t bounce,
                                                      Camera cam)
@@ -364,8 +384,10 @@ __global__ void __launch_bounds__(128, 8) extend_kernel(SceneView s, FrameView f
                     __stcs(hq + slot + 2 * cap, T4);
                     __stcs(f.hits + slot, make_uint4(encode_bary(base(t).u, base(t).v), hit_instance(t), prim,
                                                      __float_as_uint(base(t).tmax)));
+                } else if (s.sky.enabled) {
+                    sky_miss(s, f, st, bounce, O4, D4, T4, aov);
                 } else if (aov) {
-                    // a primary miss sees the (disabled) sky: black guide values (PathTracing.h:48-52)
+                    // a primary miss sees the disabled sky: black guide values (PathTracing.h:48-52)
                     const uint32_t pathIx = path_ix(__float_as_uint(O4.w));
                     if (pathIx < wh) {
                         f.albedo[pathIx] = make_float4(0.f, 0.f, 0.f, 0.f);
@@ -595,7 +617,8 @@ __device__ __forceinline__ void shade_path(const SceneView& s, const FrameView& 
     const float3 I = O + D * tmax;
 
     if (primIx == 0xffffffffu) {
-        // miss: the sky is disabled, SampleSky returns black (CudaSky.h:108-109)
+        // miss: only the adjoint replay comes here (the extend kernel shades misses, sky_miss),
+        // and it takes scenes without a sky, where SampleSky returns black (CudaSky.h:108-109)
         if (aov) {
             f.albedo[pixelIx] = make_float4(0.f, 0.f, 0.f, 0.f);
             f.normals[pixelIx] = make_float4(0.f, 0.f, 0.f, 0.f);

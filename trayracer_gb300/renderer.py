@@ -66,6 +66,24 @@ class KernelSettings:
                                    min(self.rrStart, 0xFFFFFFFF), self.flags, self.maxColor, 0)
 
 
+@dataclass
+class SkySettings:
+    """Tracer::Sky (Tracer/Renderer/Sky.h:16-67) with its defaults: the Preetham sky seen by
+    paths that leave the scene (SampleSky, CudaSky.h:105-156)."""
+
+    enabled: bool = True
+    drawSun: bool = True
+    sunDir: tuple = (0.0, 1.0, 0.0)
+    sunAngularDiameter: float = 32.0   # arc minutes
+    sunIntensity: float = 1000.0
+    turbidity: float = 4.0
+    selectionBias: float = 1.0
+
+    def to_c(self) -> _abi.SkyDesc:
+        return _abi.SkyDesc(int(bool(self.enabled)), int(bool(self.drawSun)), (C.c_float * 3)(*self.sunDir),
+                            self.sunAngularDiameter, self.sunIntensity, self.turbidity, self.selectionBias)
+
+
 @dataclass(frozen=True)
 class RayPickResult:
     """RayPickResult (CommonStructs.h:132-141); instIx and primIx are 0xFFFFFFFF on a miss."""
@@ -274,6 +292,11 @@ class DeviceRenderer:
         chosen = {f: getattr(rep.chosen, f) for f, _ in rep.chosen._fields_ if f != "reserved"}
         return {"chosen": chosen, "frame_ms_default": rep.frame_ms_default, "frame_ms_tuned": rep.frame_ms_tuned,
                 "trials": rep.trials}
+
+    def SetSky(self, sky: SkySettings | None):
+        """Scene::GetSky settings (None disables the sky, the state a context starts in)."""
+        d = sky.to_c() if sky is not None else None
+        self._check(self._lib.tr_set_sky(self._ctx, C.byref(d) if d is not None else None), "tr_set_sky")
 
     def PickRay(self, pixelIndex, stream: int = 0) -> RayPickResult:
         """DeviceRenderer::PickRay (DeviceRenderer.cpp:71-92): what the camera ray through pixel

@@ -7,6 +7,7 @@ bit-identical on every platform numpy runs on.
 """
 from __future__ import annotations
 
+import dataclasses
 import hashlib
 from dataclasses import dataclass, field
 
@@ -394,6 +395,18 @@ def heightfield(n: int = 1024, seed: int = 1, width: int = 1920, height: int = 1
                      fov=float(np.float32(60.0 * np.pi / 180.0)))
     return Scene(f"heightfield_{n}", pos, nrm, uv, idx, mat, np.array(mats, MATERIAL_DTYPE), cam, width, height,
                  spp, max_depth, rr_start, seed)
+
+
+def outdoor_heightfield(n: int = 16, width: int = 32, height: int = 24, n_lights: int = 4,
+                        lambert: bool = False) -> Scene:
+    """The heightfield seen toward its horizon, so that paths leave it and see the sky; with
+    lambert=True every material uses the reference's live Lambert closure."""
+    sc = heightfield(n=n, width=width, height=height, n_lights=n_lights)
+    sc.name = f"outdoor_heightfield_{n}"
+    sc.camera = dataclasses.replace(sc.camera, target=(0.0, 4.0, 0.0))
+    if lambert:
+        sc.materials["closure"] = TR_CLOSURE_LAMBERT
+    return sc
 
 
 def random_soup(n_tris: int = 2000, seed: int = 7, extent: float = 1.0) -> Scene:
