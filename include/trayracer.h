@@ -48,7 +48,7 @@
 extern "C" {
 #endif
 
-#define TR_ABI_VERSION 1u
+#define TR_ABI_VERSION 2u
 
 /* Maximum path length; the reference's DeviceRenderer::MaxTraceDepth
  * (Tracer/Renderer/DeviceRenderer.h:29). */
@@ -173,6 +173,37 @@ typedef struct tr_instance_desc {
     float transform[12];           /* object -> world, 3 rows (r.x, r.y, r.z, t) as OptixInstance::transform */
 } tr_instance_desc;
 
+/* Material property slots (≙ MaterialPropertyIds, CommonStructs.h:78-96), the
+ * order of tr_scene_desc.material_textures. */
+enum {
+    TR_PROP_ANISOTROPIC = 0,
+    TR_PROP_CLEARCOAT = 1,
+    TR_PROP_CLEARCOAT_GLOSS = 2,
+    TR_PROP_DIFFUSE = 3,
+    TR_PROP_EMISSIVE = 4,       /* takes no texture (Material.cpp: Emissive is colour only) */
+    TR_PROP_METALLIC = 5,
+    TR_PROP_NORMAL = 6,         /* texture only: a normal map */
+    TR_PROP_ROUGHNESS = 7,
+    TR_PROP_SHEEN = 8,
+    TR_PROP_SHEEN_TINT = 9,
+    TR_PROP_SPECULAR = 10,
+    TR_PROP_SPECULAR_TINT = 11,
+    TR_PROP_SUBSURFACE = 12,
+    TR_PROP_COUNT = 13
+};
+#define TR_NO_TEXTURE 0xFFFFFFFFu
+
+/* ≙ Texture (Tracer/Resources/Texture.cpp:83-139): width x height RGBA texels
+ * as IEEE binary16 bits, row by row, sampled as the reference's texture
+ * objects are (bilinear filtering, wrap addressing, normalised coordinates).
+ * A property with a texture is its colour times the texture's RGB at the hit's
+ * texture coordinate (GetColor, CudaMaterial.h:77-95). */
+typedef struct tr_texture_desc {
+    uint32_t width;
+    uint32_t height;
+    const uint16_t* texels;        /* 4 x width x height */
+} tr_texture_desc;
+
 typedef struct tr_scene_desc {
     const tr_mesh_desc* mesh;      /* one mesh, one identity instance (when instance_count == 0) */
     const tr_material_desc* materials;
@@ -186,7 +217,9 @@ typedef struct tr_scene_desc {
     const uint32_t* mesh_material_offsets; /* per mesh, added to its material indices (≙ MaterialOffsets); NULL = 0 */
     const tr_instance_desc* instances;
     uint32_t mesh_count;
-    uint32_t reserved;
+    uint32_t texture_count;
+    const tr_texture_desc* textures;
+    const uint32_t* material_textures; /* material_count x TR_PROP_COUNT texture indices or TR_NO_TEXTURE; NULL = none */
 } tr_scene_desc;
 
 typedef struct tr_config {

@@ -57,6 +57,7 @@ class Oracle:
             lib.orc_trace_ray.argtypes = [_P, _P, _P, C.c_float, C.c_float, C.c_int, _P, _P, _P, _P, _P]
             lib.orc_pick_ray.argtypes = [_P, _P, _P, _U, _U, C.c_int32, C.c_int32, _P]
             lib.orc_set_sky.argtypes = [_P, _P]
+            lib.orc_texture_sample.argtypes = [_P, _U, C.c_float, C.c_float, _P]
             lib.orc_ties.restype = _U
             lib.orc_ties.argtypes = [_P, _P, _P, C.c_float, C.c_float, C.c_float, _P, _U, _P]
             lib.orc_trace_any.argtypes = [_P, _P, _P, _U, C.c_float, _P]
@@ -103,6 +104,12 @@ class Oracle:
         self._lib.orc_generate(self._s, C.addressof(cc), C.addressof(st), width, height, sample_count, first, n,
                                _ptr(O), _ptr(D), _ptr(T))
         return O, D, T
+
+    def texture_sample(self, texture: int, u: float, v: float) -> np.ndarray:
+        """tex2D<float4> of one of the scene's textures at (u, v), as the texture unit filters it."""
+        out = np.zeros(4, np.float32)
+        self._lib.orc_texture_sample(self._s, int(texture), float(u), float(v), _ptr(out))
+        return out
 
     def set_sky(self, sky):
         """Sky seen by paths that leave the scene (a trayracer_gb300 SkySettings, or None: disabled)."""

@@ -218,6 +218,10 @@ struct MatRaw {            // fp16-rounded properties (Material::Property::Build
         clearcoatGloss;
     uint32_t closure;
 };
+struct Texture {            // RGBA binary16 texels, row by row
+    uint32_t w = 0, h = 0;
+    std::vector<uint16_t> texels;
+};
 struct Light {
     float V0[3], V1[3], V2[3], N[3];
     float area, energy, radiance[3], sumEnergy;
@@ -241,6 +245,8 @@ struct orc_scene {
     std::vector<double> geoD;    // 9 doubles per triangle: v0, e1, e2 (exact)
     std::vector<uint32_t> matIdx;
     std::vector<MatRaw> mats;
+    std::vector<Texture> textures;
+    std::vector<int32_t> matTex;   // TR_PROP_COUNT texture indices per material (-1: none); empty: no textures
     std::vector<Light> lights;
     std::vector<Alias> alias;
     float lightEnergy = 0.f;
@@ -1141,11 +1147,72 @@ void camera_ray(const tr_camera& cam, T tanFov2, uint32_t W, uint32_t H, int ix,
 }
 
 // ---------------------------------------------------------------- shade
+// tex2D<float4> of a texture described as the reference's (Texture.cpp:107-139):
+// bilinear filtering, wrap addressing, normalised coordinates. Restated from the
+// CUDA C++ Programming Guide ("Texture Fetching", linear filtering): the
+// coordinate is wrapped to [0, 1), scaled by the size, shifted by half a texel;
+// the neighbouring texels wrap around the edges and the fractional weights are
+// held in fixed point with 8 fractional bits.
+void texture_sample(const Texture& t, float u, float v, float out[4])
+{
+    auto wrap = [](float x) { return std::isfinite(x) ? x - std::floor(x) : 0.f; };
+    const float x = wrap(u) * float(t.w) - 0.5f;
+    const float y = wrap(v) * float(t.h) - 0.5f;
+    const float fx = std::floor(x), fy = std::floor(y);
+    const float a = std::nearbyint((x - fx) * 256.f) * (1.f / 256.f);
+    const float b = std::nearbyint((y - fy) * 256.f) * (1.f / 256.f);
+    const int64_t W = t.w, H = t.h;
+    const int64_t i0 = ((int64_t(fx) % W) + W) % W, j0 = ((int64_t(fy) % H) + H) % H;
+    const int64_t i1 = (i0 + 1) % W, j1 = (j0 + 1) % H;
+    auto texel = [&](int64_t i, int64_t j, int c) { return hval(t.texels[4 * size_t(j * W + i) + size_t(c)]); };
+    for (int c = 0; c < 4; ++c)
+        out[c] = ((1.f - a) * (1.f - b)) * texel(i0, j0, c) + (a * (1.f - b)) * texel(i1, j0, c) +
+                 ((1.f - a) * b) * texel(i0, j1, c) + (a * b) * texel(i1, j1, c);
+}
+
+int32_t material_texture(const orc_scene& S, uint32_t matIx, uint32_t prop)
+{
+    return S.matTex.empty() ? -1 : S.matTex[size_t(matIx) * TR_PROP_COUNT + prop];
+}
+
+// GetColor (CudaMaterial.h:77-95) for the properties with a texture: the stored
+// colour times the texture's RGB at uv, in float.
+MatRaw textured_raw(const orc_scene& S, uint32_t matIx, float u, float v)
+{
+    MatRaw r = S.mats[matIx];
+    auto tex = [&](uint32_t p, float rgb[3]) {
+        const int32_t ti = material_texture(S, matIx, p);
+        if (ti < 0)
+            return false;
+        float o[4];
+        texture_sample(S.textures[size_t(ti)], u, v, o);
+        rgb[0] = o[0];
+        rgb[1] = o[1];
+        rgb[2] = o[2];
+        return true;
+    };
+    float c[3];
+    if (tex(TR_PROP_DIFFUSE, c))
+        for (int k = 0; k < 3; ++k)
+            r.diffuse[k] = r.diffuse[k] * c[k];
+    const std::pair<uint32_t, float*> scalars[] = {
+        {TR_PROP_ANISOTROPIC, &r.anisotropic}, {TR_PROP_CLEARCOAT, &r.clearcoat},
+        {TR_PROP_CLEARCOAT_GLOSS, &r.clearcoatGloss}, {TR_PROP_METALLIC, &r.metallic},
+        {TR_PROP_ROUGHNESS, &r.roughness}, {TR_PROP_SHEEN, &r.sheen}, {TR_PROP_SHEEN_TINT, &r.sheenTint},
+        {TR_PROP_SPECULAR, &r.specular}, {TR_PROP_SPECULAR_TINT, &r.specularTint},
+        {TR_PROP_SUBSURFACE, &r.subsurface}};
+    for (const auto& sc : scalars)
+        if (tex(sc.first, c))
+            *sc.second = *sc.second * c[0];
+    return r;
+}
+
 template <class T>
 struct Surface {
     V3<T> N, Ng, Tn, B;
     T area;
     uint32_t matIx;
+    float u, v;   // texture coordinate (float, as the reference interpolates it)
 };
 
 // GetIntersectionAttributes + FixNormals, CudaMaterial.h:102-212. prim is the
@@ -1166,6 +1233,28 @@ template <class T> Surface<T> surface_at(const orc_scene& S, uint32_t prim, T bu
         n[k] = v3(T(hval(t.n[k][0])), T(hval(t.n[k][1])), T(hval(t.n[k][2])));
     sf.N = normalize(n[0] + ((n[1] - n[0]) * bu) + ((n[2] - n[0]) * bv));
     sf.Ng = v3(T(hval(t.N[0])), T(hval(t.N[1])), T(hval(t.N[2])));
+    // texcoord: Barycentric of the fp16 texcoords, in float (CudaMaterial.h:131-135)
+    {
+        const float fu = float(bu), fv = float(bv);
+        float uv[3][2];
+        for (int k = 0; k < 3; ++k) {
+            uv[k][0] = hval(t.uv[k][0]);
+            uv[k][1] = hval(t.uv[k][1]);
+        }
+        sf.u = uv[0][0] + ((uv[1][0] - uv[0][0]) * fu) + ((uv[2][0] - uv[0][0]) * fv);
+        sf.v = uv[0][1] + ((uv[1][1] - uv[0][1]) * fu) + ((uv[2][1] - uv[0][1]) * fv);
+    }
+    const int32_t normalTex = material_texture(S, sf.matIx, TR_PROP_NORMAL);
+    if (normalTex >= 0) {
+        // normal map applied before the tangent frame exists (CudaMaterial.h:185-191 with the
+        // zero tangent and bitangent of a zero-initialised Intersection)
+        float o[4];
+        texture_sample(S.textures[size_t(normalTex)], sf.u, sf.v, o);
+        const V3<T> nm = v3(T(o[0]), T(o[1]), T(o[2]));
+        const V3<T> norMap = (nm * T(2)) - v3s(T(1));
+        const V3<T> zero = v3s(T(0));
+        sf.N = normalize(zero * norMap.x + zero * norMap.y + sf.N * norMap.z);
+    }
     // texcoord differences are taken in fp16 (half subtraction)
     const T s1 = T(hround(hval(t.uv[1][0]) - hval(t.uv[0][0])));
     const T t1 = T(hround(hval(t.uv[1][1]) - hval(t.uv[0][1])));
@@ -1419,7 +1508,8 @@ ShadeOut<T> shade_one(const orc_scene& S, const tr_kernel_settings& st, uint32_t
         return out;
     }
     const Surface<T> sf = surface_at<T>(S, primIx, bu, bv, D, inst);
-    const HitMat<T> m = hit_material<T>(S.mats[sf.matIx]);
+    const HitMat<T> m = S.matTex.empty() ? hit_material<T>(S.mats[sf.matIx])
+                                         : hit_material<T>(textured_raw(S, sf.matIx, sf.u, sf.v));
     out.hit = true;
     out.matIx = sf.matIx;
     if (m.emissive.x + m.emissive.y + m.emissive.z > T(kEps)) {
@@ -1807,6 +1897,21 @@ orc_scene* orc_scene_create(const tr_scene_desc* desc)
     S->geo.resize(9 * size_t(total));
     S->geoD.resize(9 * size_t(total));
     S->matIdx.resize(total);
+    for (uint32_t i = 0; i < desc->texture_count; ++i) {
+        const tr_texture_desc& td = desc->textures[i];
+        Texture t;
+        t.w = td.width;
+        t.h = td.height;
+        t.texels.assign(td.texels, td.texels + 4 * size_t(td.width) * td.height);
+        S->textures.push_back(std::move(t));
+    }
+    if (desc->material_textures && desc->texture_count > 0) {
+        S->matTex.resize(size_t(desc->material_count) * TR_PROP_COUNT);
+        for (size_t k = 0; k < S->matTex.size(); ++k) {
+            const uint32_t ti = desc->material_textures[k];
+            S->matTex[k] = ti == TR_NO_TEXTURE ? -1 : int32_t(ti);
+        }
+    }
     S->mats.resize(desc->material_count);
     for (uint32_t i = 0; i < desc->material_count; ++i) {
         const tr_material_desc& d = desc->materials[i];
@@ -1957,6 +2062,11 @@ orc_scene* orc_scene_create(const tr_scene_desc* desc)
 }
 
 void orc_scene_destroy(orc_scene* s) { delete s; }
+
+void orc_texture_sample(const orc_scene* s, uint32_t texture, float u, float v, float* out)
+{
+    texture_sample(s->textures[texture], u, v, out);
+}
 
 // Sky::SetSunDir (normalised with helper_math's normalize), SetTurbidity (clamp to
 // [1, 10]) and Sky::Build (cos of the angular diameter in radians); NULL disables.

@@ -53,6 +53,9 @@ void orc_trace_closest(const orc_scene* s, const float* O4, const float* D4, uin
 
 /* One ray over [tmin, tmax]: closest hit (any = 0) or first hit (any = 1).
  * Returns 1 on a hit with prim, t and barycentrics (u, v) set. */
+// tex2D<float4> of texture `texture` at (u, v) as the device samples it (bilinear,
+// wrap, normalised coordinates, 8-bit fractional weights).
+void orc_texture_sample(const orc_scene* s, uint32_t texture, float u, float v, float* out);
 // Sky seen by paths that leave the scene (NULL: disabled, the default).
 void orc_set_sky(orc_scene* s, const tr_sky_desc* sky);
 // RayPickResult (9 words) of the RayPick raygen for pixel (x, y).

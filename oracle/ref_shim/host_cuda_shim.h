@@ -23,7 +23,15 @@ static inline float __saturatef(float x) { return x < 0.f ? 0.f : (x > 1.f ? 1.f
 static inline void __threadfence() {}
 // kernels run one job at a time on one host thread
 static inline uint32_t atomicAdd(uint32_t* p, uint32_t v) { const uint32_t o = *p; *p = o + v; return o; }
-template <class T> static inline T tex2D(cudaTextureObject_t, float, float) { return T{1.f, 1.f, 1.f, 1.f}; }
+// tex2D<float4>: texture object = texture index + 1 of the bound scene, sampled as the
+// device does (bilinear, wrap, normalised coordinates), by the oracle's sampler
+void ref_tex2d(cudaTextureObject_t t, float x, float y, float* out);
+template <class T> static inline T tex2D(cudaTextureObject_t t, float x, float y)
+{
+    float o[4];
+    ref_tex2d(t, x, y, o);
+    return T{o[0], o[1], o[2], o[3]};
+}
 
 #undef __launch_bounds__
 #define __launch_bounds__(...)

@@ -155,6 +155,11 @@ void ref_host_trace(float3 O, float3 D, float tmin, float tmax, bool anyHit, uin
     p3 = __float_as_uint(t);
 }
 
+void ref_tex2d(cudaTextureObject_t t, float x, float y, float* out)
+{
+    orc_texture_sample(g_ctx->orc, uint32_t(t - 1u), x, y, out);
+}
+
 extern "C" {
 
 void ref_set_render_mode(uint32_t mode, uint32_t flags, float aoDist, float zDepthMax)
@@ -270,6 +275,8 @@ void* ref_create(const tr_scene_desc* desc)
     for (uint32_t i = 0; i < desc->material_count; ++i) {
         const tr_material_desc& d = desc->materials[i];
         CudaMatarial& cm = c->mats[i];
+        // Material::Property::Build (Material.cpp:56-78): textureMap = the texture object
+        // (here its index + 1) where the property has a texture
         auto f = [&](MaterialPropertyIds id, float v) { cm.properties[size_t(id)] = prop(v, 0.f, 0.f, 1, 1); };
         f(MaterialPropertyIds::Anisotropic, d.anisotropic);
         f(MaterialPropertyIds::Clearcoat, d.clearcoat);
@@ -284,6 +291,12 @@ void* ref_create(const tr_scene_desc* desc)
         f(MaterialPropertyIds::Specular, d.specular);
         f(MaterialPropertyIds::SpecularTint, d.specular_tint);
         f(MaterialPropertyIds::Subsurface, d.subsurface);
+        if (desc->material_textures && desc->texture_count > 0)
+            for (uint32_t p = 0; p < TR_PROP_COUNT; ++p) {
+                const uint32_t ti = desc->material_textures[size_t(i) * TR_PROP_COUNT + p];
+                if (ti != TR_NO_TEXTURE)
+                    cm.properties[p].textureMap = cudaTextureObject_t(ti) + 1u;
+            }
     }
     c->sky.skyEnabled = 0;
     c->sky.drawSun = 0;

@@ -11,6 +11,7 @@ expected values; nothing here is written from memory.
     python tests/golden/make_golden.py debug_modes  # only ref_debug_modes.npz
     python tests/golden/make_golden.py ray_picks    # only ref_ray_pick.npz
     python tests/golden/make_golden.py sky          # only ref_sky.npz
+    python tests/golden/make_golden.py textures     # only ref_textures.npz
 """
 from __future__ import annotations
 
@@ -192,9 +193,35 @@ def sky_frames(width=32, height=24, seed=3, max_depth=4):
     return out
 
 
+TEXTURE_MODES = [(5, 3), (5, 5), (5, 6), (5, 7), (8, 0)]
+
+
+def texture_frames(width=32, height=24, seed=11):
+    """The textured Cornell box (Lambert) by the reference's kernels with their tex2D fetches
+    served by the oracle's restatement of the texture unit's bilinear filter: one path-traced
+    frame (reference sampling) and the material-property / shading-normal images of
+    TEXTURE_MODES."""
+    scene = tr.textured_cornell(width=width, height=height, wall_closure=tr.TR_CLOSURE_LAMBERT)
+    st = KernelSettings(multiSample=1, maxDepth=5, seed=seed, rrStart=1,
+                        flags=tr.TR_FLAG_REFERENCE_SAMPLING | tr._abi.TR_FLAG_REFERENCE_DRAW_RTL)
+    out = dict(digest=np.array(scene.digest()), width=width, height=height, seed=seed,
+               modes=np.array(TEXTURE_MODES, np.uint32))
+    ref = Reference(scene)
+    acc = np.zeros((width * height, 4), np.float32)
+    ref.render_frame(scene.camera, st, width, height, 0, acc)
+    out["frame"] = acc
+    for mode, flags in TEXTURE_MODES:
+        Reference.set_render_mode(mode, flags, 1.0, 1.0)
+        acc = np.zeros((width * height, 4), np.float32)
+        ref.render_frame(scene.camera, st, width, height, 0, acc)
+        out[f"mode_{mode}_{flags}"] = acc
+    Reference.set_render_mode(7)
+    return out
+
+
 def main():
     single = {"debug_modes": ("ref_debug_modes.npz", debug_mode_frames), "ray_picks": ("ref_ray_pick.npz", ray_picks),
-              "sky": ("ref_sky.npz", sky_frames)}
+              "sky": ("ref_sky.npz", sky_frames), "textures": ("ref_textures.npz", texture_frames)}
     if len(sys.argv) == 2 and sys.argv[1] in single:
         build.build_oracle()
         if build.build_reference() is None:
@@ -226,6 +253,8 @@ def main():
     np.savez_compressed(OUT / "ref_ray_pick.npz", **ray_picks())
     # the sky
     np.savez_compressed(OUT / "ref_sky.npz", **sky_frames())
+    # textures
+    np.savez_compressed(OUT / "ref_textures.npz", **texture_frames())
     for p in sorted(OUT.glob("*.npz")):
         print(p.name, p.stat().st_size)
 

@@ -22,4 +22,5 @@ from .scenes import (  # noqa: F401
     outdoor_heightfield,
     sphere_batch,
     sphere_scene,
+    textured_cornell,
 )

@@ -5,7 +5,7 @@ import ctypes as C
 from pathlib import Path
 
 TR_MAX_DEPTH = 16
-TR_ABI_VERSION = 1
+TR_ABI_VERSION = 2
 TR_FLAG_REFERENCE_SAMPLING = 1 << 0
 TR_FLAG_WRITE_AOVS = 1 << 1
 TR_FLAG_REFERENCE_DRAW_RTL = 1 << 2
@@ -93,6 +93,15 @@ class InstanceDesc(C.Structure):
     ]
 
 
+TR_PROP_COUNT = 13
+TR_PROP_DIFFUSE = 3
+TR_PROP_EMISSIVE = 4
+TR_PROP_METALLIC = 5
+TR_PROP_NORMAL = 6
+TR_PROP_ROUGHNESS = 7
+TR_NO_TEXTURE = 0xFFFFFFFF
+
+
 class SceneDesc(C.Structure):
     _fields_ = [
         ("mesh", C.POINTER(MeshDesc)),
@@ -105,8 +114,16 @@ class SceneDesc(C.Structure):
         ("mesh_material_offsets", C.c_void_p),
         ("instances", C.POINTER(InstanceDesc)),
         ("mesh_count", C.c_uint32),
-        ("reserved", C.c_uint32),
+        ("texture_count", C.c_uint32),
+        ("textures", C.c_void_p),
+        ("material_textures", C.c_void_p),
     ]
+
+
+class TextureDesc(C.Structure):
+    """tr_texture_desc: RGBA binary16 texels."""
+
+    _fields_ = [("width", C.c_uint32), ("height", C.c_uint32), ("texels", C.c_void_p)]
 
 
 class Config(C.Structure):

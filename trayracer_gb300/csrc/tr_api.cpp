@@ -119,6 +119,12 @@ struct Context {
     uint32_t* hostCounters = nullptr;  // pinned
     float* pickResult = nullptr;       // 9 words of the frame arena (tr_pick_ray)
 
+    // textures of the scene: one CUDA array and texture object each, and the
+    // per-material slots as uploaded (kept to rewrite their emissive colour)
+    std::vector<cudaArray_t> texArrays;
+    std::vector<cudaTextureObject_t> texObjects;
+    std::vector<TexSlots> texSlotsHost;
+
     // timing
     cudaEvent_t evStart = nullptr, evGenerate = nullptr, evFinal = nullptr;
     cudaEvent_t evExtend[TR_MAX_DEPTH] = {}, evShade[TR_MAX_DEPTH] = {}, evConnect[TR_MAX_DEPTH] = {};
@@ -175,6 +181,44 @@ void invalidate_graph(Context* c)
     c->graphExec = nullptr;
     c->graph = nullptr;
     c->graphValid = false;
+}
+
+void release_textures(Context* c)
+{
+    for (cudaTextureObject_t t : c->texObjects)
+        cudaDestroyTextureObject(t);
+    for (cudaArray_t a : c->texArrays)
+        cudaFreeArray(a);
+    c->texObjects.clear();
+    c->texArrays.clear();
+    c->texSlotsHost.clear();
+}
+
+// Texture::Upload (Texture.cpp:83-139): RGBA binary16 texels in a CUDA array,
+// sampled with bilinear filtering, wrap addressing and normalised coordinates
+// (the same texture description as the reference's, so a texel fetch filters
+// the same way).
+tr_status upload_texture(Context* c, const tr_texture_desc& t)
+{
+    const cudaChannelFormatDesc cd = cudaCreateChannelDescHalf4();
+    cudaArray_t arr = nullptr;
+    TR_CUDA(c, cudaMallocArray(&arr, &cd, t.width, t.height));
+    c->texArrays.push_back(arr);
+    const size_t pitch = size_t(t.width) * 4 * sizeof(uint16_t);
+    TR_CUDA(c, cudaMemcpy2DToArray(arr, 0, 0, t.texels, pitch, pitch, t.height, cudaMemcpyHostToDevice));
+    cudaResourceDesc rd{};
+    rd.resType = cudaResourceTypeArray;
+    rd.res.array.array = arr;
+    cudaTextureDesc td{};
+    td.addressMode[0] = cudaAddressModeWrap;
+    td.addressMode[1] = cudaAddressModeWrap;
+    td.filterMode = cudaFilterModeLinear;
+    td.readMode = cudaReadModeElementType;
+    td.normalizedCoords = 1;
+    cudaTextureObject_t obj = 0;
+    TR_CUDA(c, cudaCreateTextureObject(&obj, &rd, &td, nullptr));
+    c->texObjects.push_back(obj);
+    return TR_OK;
 }
 
 // Uploads the acceleration structures into their own arena and points the
@@ -548,6 +592,7 @@ tr_status tr_destroy(void* ctx)
     c->bvhArena.release();
     c->frameArena.release();
     c->adjointArena.release();
+    release_textures(c);
     if (c->hostCounters)
         cudaFreeHost(c->hostCounters);
     cudaEvent_t* evs[] = {&c->evStart, &c->evGenerate, &c->evFinal};
@@ -600,13 +645,28 @@ tr_status tr_scene_upload(void* ctx, const tr_scene_desc* desc)
     const size_t oAlias = take(fs.alias.size() * sizeof(AliasEntry));
     const size_t oXf = take(fs.invTransforms.size() * sizeof(float4));
     const size_t oBins = take(2 * size_t(desc->material_count) * sizeof(uint32_t));  // sort counts + cursors
+    const size_t oTex = take(fs.texSlots.size() * sizeof(TexSlots));
 
     if (c->stream)
         cudaStreamSynchronize(c->stream);
     invalidate_graph(c);
     c->sceneArena.release();
     c->bvhArena.release();
+    release_textures(c);
     c->hasScene = false;
+    if (!fs.texSlots.empty()) {
+        for (uint32_t i = 0; i < desc->texture_count; ++i) {
+            const tr_status ts = upload_texture(c, desc->textures[i]);
+            if (ts != TR_OK) {
+                release_textures(c);
+                return ts;
+            }
+        }
+        for (TexSlots& slot : fs.texSlots)
+            for (uint32_t p = 0; p < TR_PROP_COUNT; ++p)
+                if (slot.tex[p])
+                    slot.tex[p] = c->texObjects[size_t(slot.tex[p] - 1u)];
+    }
     void* base = nullptr;
     cudaError_t e = cudaMalloc(&base, off);
     if (e != cudaSuccess)
@@ -626,6 +686,7 @@ tr_status tr_scene_upload(void* ctx, const tr_scene_desc* desc)
         up(oLights, fs.lights.data(), fs.lights.size() * sizeof(LightTri)),
         up(oAlias, fs.alias.data(), fs.alias.size() * sizeof(AliasEntry)),
         up(oXf, fs.invTransforms.data(), fs.invTransforms.size() * sizeof(float4)),
+        up(oTex, fs.texSlots.data(), fs.texSlots.size() * sizeof(TexSlots)),
     };
     for (cudaError_t x : es)
         if (x != cudaSuccess) {
@@ -646,6 +707,8 @@ tr_status tr_scene_upload(void* ctx, const tr_scene_desc* desc)
     s.lights = reinterpret_cast<const LightTri*>(b + oLights);
     s.alias = reinterpret_cast<const AliasEntry*>(b + oAlias);
     s.invTransforms = reinterpret_cast<const float4*>(b + oXf);
+    s.texSlots = fs.texSlots.empty() ? nullptr : reinterpret_cast<const TexSlots*>(b + oTex);
+    c->texSlotsHost = fs.texSlots;
     TR_CUDA(c, cudaMemset(b + oBins, 0, 2 * size_t(desc->material_count) * sizeof(uint32_t)));
     c->sort.counts = reinterpret_cast<uint32_t*>(b + oBins);
     c->sort.cursor = c->sort.counts + desc->material_count;
@@ -705,6 +768,15 @@ tr_status tr_update_materials(void* ctx, const tr_material_desc* materials, uint
     std::vector<Material> mats(count);
     for (uint32_t i = 0; i < count; ++i)
         mats[i] = resolve_material(materials[i]);
+    // the textures stay assigned; the textured resolution reads the new emissive colour
+    std::vector<TexSlots> slots = c->texSlotsHost;
+    for (uint32_t i = 0; i < count && !slots.empty(); ++i) {
+        for (uint32_t p = 0; p < TR_PROP_COUNT; ++p)
+            if (slots[i].tex[p])
+                mats[i].texMask |= 1u << p;
+        for (int k = 0; k < 3; ++k)
+            slots[i].emissive[k] = round_to_half(materials[i].emissive[k]);
+    }
     std::vector<LightTri> lights = c->hostLights;
     std::vector<double> energies(lights.size());
     float sumEnergy = 0.f;
@@ -726,6 +798,11 @@ tr_status tr_update_materials(void* ctx, const tr_material_desc* materials, uint
         TR_CUDA(c, cudaStreamSynchronize(c->stream));
     TR_CUDA(c, cudaMemcpy(const_cast<Material*>(c->scene.materials), mats.data(), mats.size() * sizeof(Material),
                           cudaMemcpyHostToDevice));
+    if (!slots.empty()) {
+        TR_CUDA(c, cudaMemcpy(const_cast<TexSlots*>(c->scene.texSlots), slots.data(), slots.size() * sizeof(TexSlots),
+                              cudaMemcpyHostToDevice));
+        c->texSlotsHost = slots;
+    }
     if (!lights.empty()) {
         TR_CUDA(c, cudaMemcpy(const_cast<LightTri*>(c->scene.lights), lights.data(), lights.size() * sizeof(LightTri),
                               cudaMemcpyHostToDevice));
@@ -751,6 +828,8 @@ tr_status tr_adjoint_frame(void* ctx, void* stream, const float* pixel_grad, flo
         return fail(c, TR_ERR_INVALID_ARGUMENT, "the adjoint differentiates the default sampling mode only");
     if (c->scene.sky.enabled)
         return fail(c, TR_ERR_INVALID_ARGUMENT, "the adjoint differentiates scenes without a sky");
+    if (c->scene.texSlots)
+        return fail(c, TR_ERR_INVALID_ARGUMENT, "the adjoint differentiates untextured materials only");
     tr_status st = check_ready(c);
     if (st != TR_OK)
         return st;

@@ -285,8 +285,8 @@ tr_status tr_batch_create(const tr_config* config, const tr_batch_item* items, u
             return TR_ERR_INVALID_ARGUMENT;
         if (uint64_t(it.width) * it.height > cap)
             return TR_ERR_LIMIT;
-        if (!validate_scene(*it.scene).empty() || it.scene->instance_count)
-            return TR_ERR_INVALID_ARGUMENT;  // one-mesh scenes only
+        if (!validate_scene(*it.scene).empty() || it.scene->instance_count || it.scene->material_textures)
+            return TR_ERR_INVALID_ARGUMENT;  // one-mesh untextured scenes only
         pixels += uint64_t(it.width) * it.height;
         paths += uint64_t(it.width) * it.height * it.spp;
     }

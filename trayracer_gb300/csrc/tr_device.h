@@ -43,9 +43,19 @@ struct alignas(16) Material {
     float luminance;
     uint32_t closure;
     uint32_t isEmissive;   // emissive.x + .y + .z > Epsilon (PathTracing.h:73)
-    uint32_t pad0, pad1;
+    uint32_t texMask;      // bit TR_PROP_* set: that property has a texture (TexSlots)
+    uint32_t pad1;
 };
 static_assert(sizeof(Material) == 96, "Material must stay 96 bytes");
+
+// Textures of one material, read only when its texMask is non-zero: the texture
+// object of each property (0 = none) and the fp16-rounded Emissive colour, which
+// the per-hit resolution multiplies with the textured diffuse (CudaMaterial.h:158).
+struct alignas(16) TexSlots {
+    unsigned long long tex[TR_PROP_COUNT];  // cudaTextureObject_t
+    float emissive[3];
+    uint32_t pad;
+};
 
 // Emissive triangle in world space: same fields and 80-byte layout as the
 // reference's LightTriangle (Tracer/Common/CommonStructs.h:257-273).
@@ -122,6 +132,7 @@ struct SceneView {
     uint32_t nodeCount;
     uint32_t triCount;
     uint32_t pad;
+    const TexSlots* texSlots;   // per material, null when the scene has no textures
     SkyView sky;
 };
 

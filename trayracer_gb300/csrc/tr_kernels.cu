@@ -493,9 +493,19 @@ struct Surface {
     float3 B;   // bitangent
     float area;
     uint32_t matIx;
+    float2 uv;  // texture coordinate
 };
 
-// GetIntersectionAttributes + FixNormals, CudaMaterial.h:117-212
+// tex2D of a property's texture: its RGB (GetColor, CudaMaterial.h:89-92)
+__device__ __forceinline__ float3 tex_rgb(unsigned long long t, const float2& uv)
+{
+    const float4 c = tex2D<float4>(t, uv.x, uv.y);
+    return make_float3(c.x, c.y, c.z);
+}
+
+// GetIntersectionAttributes + FixNormals, CudaMaterial.h:117-212 (TEX: the scene has
+// textures, so a normal map may apply)
+template <bool TEX = false>
 __device__ __forceinline__ Surface surface_at(const SceneView& s, uint32_t instIx, uint32_t primIx, float2 bary,
                                               const float3& D)
 {
@@ -515,6 +525,20 @@ __device__ __forceinline__ Surface surface_at(const SceneView& s, uint32_t instI
     const float3 N2 = make_float3(h2f(tri.N2x), h2f(tri.N2y), h2f(tri.N2z));
     sf.N = normalize(N0 + ((N1 - N0) * bary.x) + ((N2 - N0) * bary.y));
     sf.Ng = make_float3(h2f(tri.Nx), h2f(tri.Ny), h2f(tri.Nz));
+    const float2 uv0 = make_float2(h2f(tri.uv0x), h2f(tri.uv0y));
+    const float2 uv1 = make_float2(h2f(tri.uv1x), h2f(tri.uv1y));
+    const float2 uv2 = make_float2(h2f(tri.uv2x), h2f(tri.uv2y));
+    sf.uv = make_float2(uv0.x + ((uv1.x - uv0.x) * bary.x) + ((uv2.x - uv0.x) * bary.y),
+                        uv0.y + ((uv1.y - uv0.y) * bary.x) + ((uv2.y - uv0.y) * bary.y));
+    if (TEX && (__ldg(&s.materials[sf.matIx].texMask) & (1u << TR_PROP_NORMAL))) {
+        // normal map (CudaMaterial.h:185-191), applied where the reference applies it: before
+        // the tangent frame is computed, so with the zero tangent and bitangent of its
+        // zero-initialised Intersection; the map can only keep or flip the normal
+        const float3 nm = tex_rgb(__ldg(&s.texSlots[sf.matIx].tex[TR_PROP_NORMAL]), sf.uv);
+        const float3 norMap = (nm * 2.f) - f3(1.f);
+        const float3 zero = f3(0.f);
+        sf.N = normalize(norMap.x * zero + norMap.y * zero + norMap.z * sf.N);
+    }
 
     // tangents from texcoord derivatives (differences taken in fp16)
     const __half u0x = __ushort_as_half(tri.uv0x), u0y = __ushort_as_half(tri.uv0y);
@@ -549,7 +573,7 @@ __device__ __forceinline__ Surface surface_at(const SceneView& s, uint32_t instI
 }
 
 __device__ __forceinline__ HitMat load_material(const Material* __restrict__ mats, uint32_t ix, uint32_t& closure,
-                                                uint32_t& emissiveFlag)
+                                                uint32_t& emissiveFlag, uint32_t* texMask = nullptr)
 {
     const float4* p = reinterpret_cast<const float4*>(mats + ix);
     const float4 a = __ldg(p + 0), b = __ldg(p + 1), c = __ldg(p + 2), d = __ldg(p + 3), e = __ldg(p + 4);
@@ -571,7 +595,40 @@ __device__ __forceinline__ HitMat load_material(const Material* __restrict__ mat
     m.luminance = e.w;
     closure = g.x;
     emissiveFlag = g.y;
+    if (texMask)
+        *texMask = g.z;
     return m;
+}
+
+// GetIntersectionAttributes' material part (CudaMaterial.h:153-183) for a material
+// with textures: each textured property is its colour times the texture's RGB at
+// the hit, then emissive = Emissive * diffuse, tint and luminance from the
+// textured diffuse, and the emissive test of PathTracing.h:73 per hit.
+__device__ __forceinline__ void apply_textures(const SceneView& s, uint32_t matIx, uint32_t mask, float2 uv, HitMat& m,
+                                            uint32_t& emissiveFlag)
+{
+    const TexSlots& t = s.texSlots[matIx];
+    auto scalar = [&](uint32_t p, float& v) {
+        if (mask & (1u << p))
+            v = v * tex_rgb(__ldg(&t.tex[p]), uv).x;
+    };
+    if (mask & (1u << TR_PROP_DIFFUSE))
+        m.diffuse = m.diffuse * tex_rgb(__ldg(&t.tex[TR_PROP_DIFFUSE]), uv);
+    const float3 tintXYZ = linear_to_xyz(m.diffuse);
+    scalar(TR_PROP_METALLIC, m.metallic);
+    m.emissive = make_float3(__ldg(&t.emissive[0]), __ldg(&t.emissive[1]), __ldg(&t.emissive[2])) * m.diffuse;
+    scalar(TR_PROP_SUBSURFACE, m.subsurface);
+    m.tint = tintXYZ.y > 0 ? xyz_to_linear(tintXYZ * (1.f / tintXYZ.y)) : f3(1.f);
+    scalar(TR_PROP_SPECULAR, m.specular);
+    scalar(TR_PROP_ROUGHNESS, m.roughness);
+    scalar(TR_PROP_SPECULAR_TINT, m.specularTint);
+    scalar(TR_PROP_ANISOTROPIC, m.anisotropic);
+    scalar(TR_PROP_SHEEN, m.sheen);
+    scalar(TR_PROP_SHEEN_TINT, m.sheenTint);
+    scalar(TR_PROP_CLEARCOAT, m.clearcoat);
+    scalar(TR_PROP_CLEARCOAT_GLOSS, m.clearcoatGloss);
+    m.luminance = tintXYZ.y;
+    emissiveFlag = (m.emissive.x + m.emissive.y + m.emissive.z > kEpsilon) ? 1u : 0u;
 }
 
 // What the path-replay adjoint needs to know about one shaded vertex.
@@ -591,7 +648,7 @@ struct VertexInfo {
 // One PathTracingKernel step (PathTracing.h:15-174) for one queue entry. With
 // vi == nullptr (the shade kernel) it adds emitted radiance and writes the
 // guide buffers; the adjoint replay passes vi and gets the vertex instead.
-template <bool REF, class Rng>
+template <bool REF, class Rng, bool TEX = false>
 __device__ __forceinline__ void shade_path(const SceneView& s, const FrameView& f, const Settings& st, uint32_t bounce,
                                            uint32_t sc, const float4& O4, const float4& D4, const float4& T4,
                                            const uint4& hd, Rng& rng, bool& wantExt, float4 (&ext)[3],
@@ -626,9 +683,11 @@ __device__ __forceinline__ void shade_path(const SceneView& s, const FrameView& 
         return;
     }
 
-    const Surface sf = surface_at(s, instIx, primIx, bary, D);
-    uint32_t closure, emissiveFlag;
-    const HitMat m = load_material(s.materials, sf.matIx, closure, emissiveFlag);
+    const Surface sf = surface_at<TEX>(s, instIx, primIx, bary, D);
+    uint32_t closure, emissiveFlag, texMask;
+    HitMat m = load_material(s.materials, sf.matIx, closure, emissiveFlag, &texMask);
+    if (TEX && texMask)
+        apply_textures(s, sf.matIx, texMask, sf.uv, m, emissiveFlag);
     if (vi) {
         vi->hit = true;
         vi->matIx = sf.matIx;
@@ -727,7 +786,7 @@ __device__ __forceinline__ void shade_path(const SceneView& s, const FrameView& 
     }
 }
 
-template <bool REF, bool BATCH>
+template <bool REF, bool BATCH, bool TEX = false>
 __global__ void __launch_bounds__(128) shade_kernel(SceneView s, FrameView f, Settings st, uint32_t bounce)
 {
     const uint32_t count = __ldcg(f.counters + kHitCounterBase + bounce);
@@ -762,11 +821,12 @@ __global__ void __launch_bounds__(128) shade_kernel(SceneView s, FrameView f, Se
                 shade_path<false>(si, f, st, bounce, sc, O4, D4, T4, hd, rng, wantExt, ext, wantShadow, sh);
             } else if (REF) {
                 RefRng rng{tea2(st.seed + pathIx, sc + bounce + 1u)};
-                shade_path<REF>(s, f, st, bounce, sc, O4, D4, T4, hd, rng, wantExt, ext, wantShadow, sh);
+                shade_path<REF, RefRng, TEX>(s, f, st, bounce, sc, O4, D4, T4, hd, rng, wantExt, ext, wantShadow, sh);
             } else {
                 CounterRng rng;
                 rng.init(pathIx % wh, sc + pathIx / wh, bounce + 1u, st.seed);
-                shade_path<REF>(s, f, st, bounce, sc, O4, D4, T4, hd, rng, wantExt, ext, wantShadow, sh);
+                shade_path<REF, CounterRng, TEX>(s, f, st, bounce, sc, O4, D4, T4, hd, rng, wantExt, ext, wantShadow,
+                                                 sh);
             }
         }
         const uint32_t shSlot = warp_append(shCounter, wantShadow);
@@ -1121,9 +1181,11 @@ __global__ void __launch_bounds__(128) debug_shade_kernel(SceneView s, FrameView
             } else if (hit && bounce == 0) {
                 const float2 bary = decode_bary(hd.x);
                 const bool fix = ao;
-                const Surface sf = surface_at(s, hd.y, hd.z, bary, fix ? f3(D4) : f3(0.f));
-                uint32_t closure, emissiveFlag;
-                const HitMat m = load_material(s.materials, sf.matIx, closure, emissiveFlag);
+                const Surface sf = surface_at<true>(s, hd.y, hd.z, bary, fix ? f3(D4) : f3(0.f));
+                uint32_t closure, emissiveFlag, texMask;
+                HitMat m = load_material(s.materials, sf.matIx, closure, emissiveFlag, &texMask);
+                if (texMask)
+                    apply_textures(s, sf.matIx, texMask, sf.uv, m, emissiveFlag);
                 if (ao) {
                     uint32_t seed = tea2(st.seed + pathIx, mode == kModeAO ? bounce + 1u : sc + bounce + 1u);
                     if (mode == kModeAO)
@@ -1170,7 +1232,11 @@ __global__ void __launch_bounds__(128) debug_shade_kernel(SceneView s, FrameView
                         case 3: c = m.diffuse; break;
                         case 4: c = m.emissive; break;
                         case 5: c = make_float3(m.metallic, m.metallic, m.metallic); break;
-                        case 6: c = make_float3(1.f, 1.f, 1.f); break;  // no normal map: GetColor's default
+                        case 6:  // GetColor(Normal): the map's RGB, else GetColor's default
+                            c = (texMask & (1u << TR_PROP_NORMAL))
+                                    ? tex_rgb(__ldg(&s.texSlots[sf.matIx].tex[TR_PROP_NORMAL]), sf.uv)
+                                    : make_float3(1.f, 1.f, 1.f);
+                            break;
                         case 7: c = make_float3(m.roughness, m.roughness, m.roughness); break;
                         case 8: c = make_float3(m.sheen, m.sheen, m.sheen); break;
                         case 9: c = make_float3(m.sheenTint, m.sheenTint, m.sheenTint); break;
@@ -1676,9 +1742,14 @@ cudaError_t launch_extend(const SceneView& s, const FrameView& f, const Settings
 cudaError_t launch_shade(const SceneView& s, const FrameView& f, const Settings& st, uint32_t bounce,
                          const LaunchShape& shape, cudaStream_t stream)
 {
+    const bool ref = (st.flags & TR_FLAG_REFERENCE_SAMPLING) != 0;
     if (f.segments)
         shade_kernel<false, true><<<shape.shadeBlocks, 128, 0, stream>>>(s, f, st, bounce);
-    else if (st.flags & TR_FLAG_REFERENCE_SAMPLING)
+    else if (s.texSlots && ref)
+        shade_kernel<true, false, true><<<shape.shadeBlocks, 128, 0, stream>>>(s, f, st, bounce);
+    else if (s.texSlots)
+        shade_kernel<false, false, true><<<shape.shadeBlocks, 128, 0, stream>>>(s, f, st, bounce);
+    else if (ref)
         shade_kernel<true, false><<<shape.shadeBlocks, 128, 0, stream>>>(s, f, st, bounce);
     else
         shade_kernel<false, false><<<shape.shadeBlocks, 128, 0, stream>>>(s, f, st, bounce);

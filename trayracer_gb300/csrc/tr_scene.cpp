@@ -59,6 +59,25 @@ std::string validate_scene(const tr_scene_desc& desc)
             return "material " + std::to_string(i) + " has an unknown closure";
     if (desc.bvh_leaf_size > 3)
         return "bvh_leaf_size must be 0..3";
+    if (desc.texture_count > 0 && !desc.textures)
+        return "texture array missing";
+    for (uint32_t i = 0; i < desc.texture_count; ++i) {
+        const tr_texture_desc& t = desc.textures[i];
+        if (t.width == 0 || t.height == 0 || t.width > kMaxTextureSize || t.height > kMaxTextureSize || !t.texels)
+            return "texture " + std::to_string(i) + " must have texels and a size in [1, 32768]";
+    }
+    if (desc.material_textures) {
+        for (uint32_t i = 0; i < desc.material_count; ++i)
+            for (uint32_t p = 0; p < TR_PROP_COUNT; ++p) {
+                const uint32_t ti = desc.material_textures[size_t(i) * TR_PROP_COUNT + p];
+                if (ti == TR_NO_TEXTURE)
+                    continue;
+                if (ti >= desc.texture_count)
+                    return "material " + std::to_string(i) + " names a missing texture";
+                if (p == TR_PROP_EMISSIVE)
+                    return "material " + std::to_string(i) + ": the emissive property takes no texture";
+            }
+    }
     return std::string();
 }
 
@@ -172,6 +191,26 @@ FlatScene flatten_scene(const tr_scene_desc& desc)
     fs.materials.resize(desc.material_count);
     for (uint32_t i = 0; i < desc.material_count; ++i)
         fs.materials[i] = resolve_material(desc.materials[i]);
+    // textures per material (texture index + 1 until the upload puts the texture objects in)
+    if (desc.material_textures && desc.texture_count > 0) {
+        fs.texSlots.assign(desc.material_count, TexSlots{});
+        bool any = false;
+        for (uint32_t i = 0; i < desc.material_count; ++i) {
+            TexSlots& ts = fs.texSlots[i];
+            for (uint32_t p = 0; p < TR_PROP_COUNT; ++p) {
+                const uint32_t ti = desc.material_textures[size_t(i) * TR_PROP_COUNT + p];
+                if (ti != TR_NO_TEXTURE) {
+                    ts.tex[p] = uint64_t(ti) + 1u;
+                    fs.materials[i].texMask |= 1u << p;
+                    any = true;
+                }
+            }
+            for (int k = 0; k < 3; ++k)
+                ts.emissive[k] = round_to_half(desc.materials[i].emissive[k]);
+        }
+        if (!any)
+            fs.texSlots.clear();
+    }
     const bool twoLevel = desc.instance_count > 0;
     const uint32_t meshCount = scene_mesh_count(desc);
 

@@ -15,6 +15,7 @@ struct FlatScene {
     std::vector<uint32_t> meshTriBase; // two-level: first triangle of each mesh
     std::vector<uint32_t> instMesh;    // two-level: mesh of each instance
     std::vector<Material> materials;
+    std::vector<TexSlots> texSlots;    // per material when any material has a texture (tex = index + 1)
     std::vector<LightTri> lights;
     std::vector<AliasEntry> alias;
     std::vector<float4> invTransforms; // 3 per instance
@@ -22,6 +23,9 @@ struct FlatScene {
     float lightEnergyTotal = 0.f;
     float bounds[6] = {0, 0, 0, 0, 0, 0};
 };
+
+// Largest texture side accepted.
+constexpr uint32_t kMaxTextureSize = 32768;
 
 // Validates the description; returns an empty string when it is usable.
 std::string validate_scene(const tr_scene_desc& desc);

@@ -137,6 +137,16 @@ class SceneDescHolder:
         )
         self.desc = _abi.SceneDesc(C.pointer(self.mesh), C.cast(self.mats.ctypes.data, C.POINTER(_abi.MaterialDesc)),
                                    self.mats.shape[0], leaf_size, build_threads, 0)
+        if scene.material_textures is not None and len(scene.textures) > 0:
+            self.tex_arrays = [np.ascontiguousarray(t, np.float16) for t in scene.textures]
+            self.tex = (_abi.TextureDesc * len(self.tex_arrays))()
+            for i, t in enumerate(self.tex_arrays):
+                assert t.ndim == 3 and t.shape[2] == 4, "textures are (H, W, 4) RGBA"
+                self.tex[i] = _abi.TextureDesc(t.shape[1], t.shape[0], t.ctypes.data)
+            self.mat_tex = np.ascontiguousarray(scene.material_textures, np.uint32)
+            self.desc.texture_count = len(self.tex_arrays)
+            self.desc.textures = C.cast(self.tex, C.c_void_p)
+            self.desc.material_textures = self.mat_tex.ctypes.data
         inst = getattr(scene, "instances", None)
         if inst is not None:
             # two-level scene: meshes placed by instances

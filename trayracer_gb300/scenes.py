@@ -102,6 +102,10 @@ class Scene:
     max_depth: int = 5
     rr_start: int = 1 << 30
     seed: int = 1
+    # textures: (H, W, 4) float16 RGBA arrays; material_textures: (M, 13) texture index per
+    # MaterialPropertyIds slot (0xFFFFFFFF: none), or None
+    textures: list = field(default_factory=list)
+    material_textures: np.ndarray | None = None
 
     @property
     def triangle_count(self) -> int:
@@ -112,6 +116,10 @@ class Scene:
         for a in (self.positions, self.normals, self.texcoords, self.indices, self.material_indices, self.materials):
             if a is not None:
                 h.update(np.ascontiguousarray(a).tobytes())
+        if self.material_textures is not None:
+            h.update(np.ascontiguousarray(self.material_textures, np.uint32).tobytes())
+            for t in self.textures:
+                h.update(np.ascontiguousarray(t, np.float16).tobytes())
         return h.hexdigest()[:16]
 
 
@@ -232,6 +240,43 @@ def cornell_box(seed: int = 1, width: int = 256, height: int = 256, spp: int = 1
         mats["closure"] = TR_CLOSURE_LAMBERT
     return Scene("cornell_box", pos, nrm, uv, idx, mat, mats, CameraSpec(), width, height, spp, max_depth, 1 << 30,
                  seed)
+
+
+def textured_cornell(seed: int = 5, width: int = 48, height: int = 48, spp: int = 4, max_depth: int = 5,
+                     wall_closure: int = TR_CLOSURE_DIFFUSE, tex_size: int = 16) -> Scene:
+    """The Cornell box with textures: texture coordinates are a planar projection of the vertex
+    positions (ranging beyond [0, 1], so the wrap addressing matters); the walls and the short box
+    carry a random diffuse texture, the floor also a roughness, metallic and a normal map whose
+    blue channel falls below one half on some texels (the reference applies normal maps before
+    its tangent frame exists, so such texels flip the normal), and the light's diffuse is
+    textured too (its emission is Emissive times the textured diffuse)."""
+    sc = cornell_box(seed=seed, width=width, height=height, spp=spp, max_depth=max_depth, wall_closure=wall_closure)
+    rng = np.random.default_rng(seed + 100)
+    p = sc.positions
+    sc.texcoords = np.stack([p[:, 0] * np.float32(0.73) + p[:, 2] * np.float32(0.41) + np.float32(0.2),
+                             p[:, 1] * np.float32(0.67) - p[:, 2] * np.float32(0.29) + np.float32(0.1)],
+                            axis=-1).astype(np.float32)
+
+    def tex(lo, hi, shape=(tex_size, tex_size)):
+        t = rng.uniform(lo, hi, shape + (4,)).astype(np.float16)
+        t[..., 3] = np.float16(1.0)
+        return t
+
+    normal = tex(0.0, 1.0)
+    normal[..., 2] = np.where(rng.random((tex_size, tex_size)) < 0.2, np.float16(0.3), np.float16(0.9))
+    sc.textures = [tex(0.2, 1.0), tex(0.3, 1.0, (8, 12)), tex(0.0, 1.0, (5, 7)), normal]
+    mt = np.full((sc.materials.shape[0], 13), 0xFFFFFFFF, np.uint32)
+    diffuse, roughness, metallic, nrm = 3, 7, 5, 6
+    for m in range(sc.materials.shape[0]):
+        if m != 6:  # not the tall conductor box
+            mt[m, diffuse] = 0
+    mt[0, roughness] = 1   # floor
+    mt[0, metallic] = 2
+    mt[0, nrm] = 3
+    mt[5, nrm] = 3         # short box
+    sc.material_textures = mt
+    sc.name = "textured_cornell"
+    return sc
 
 
 def instanced_cornell(seed: int = 3, width: int = 64, height: int = 48, spp: int = 4, max_depth: int = 5,
