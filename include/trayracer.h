@@ -417,6 +417,57 @@ typedef struct tr_sky_desc {
 /* Sets (or with sky = NULL disables) the sky; resets the accumulation. */
 tr_status tr_set_sky(void* ctx, const tr_sky_desc* sky);
 
+/* ---- scene files ----
+ * ≙ SceneFile::Load (Tracer/FileIO/SceneFile.cpp:89-436, 680-723) with
+ * ModelFile::Import / TextureFile::Import (ModelFile.cpp:50-160, 330-449,
+ * TextureFile.cpp:30-150): the reference's scene JSON ("models", "instances",
+ * "materials", "camera", "renderer", "sky"; "post" is ignored) read into a
+ * two-level tr_scene_desc. Models load from the reference's model cache format
+ * ("MDL" version 2: the file itself, or the cache file the reference keeps for
+ * it, cache/<hash of its path>.bin) or from Wavefront OBJ; textures from the
+ * reference's texture cache format ("TEX" version 2, likewise). Relative paths
+ * resolve against base_dir (NULL: the current directory, as the reference
+ * resolves them). Meshes are ordered by first use among the instances and
+ * materials concatenated per mesh, as Renderer::BuildMaterials orders them;
+ * every material takes TR_CLOSURE_LAMBERT, the closure the reference shades
+ * with. */
+typedef struct tr_scene_file_info {
+    const tr_scene_desc* scene;     /* NULL when the file places no instance */
+    tr_camera camera;               /* "camera" (CameraNode defaults when absent) */
+    float camera_target[3];
+    float camera_up[3];
+    tr_kernel_settings settings;    /* "renderer" over Renderer::DefaultSettings (flags 0) */
+    float ao_dist;
+    float z_depth_max;
+    tr_sky_desc sky;                /* "sky" over Sky's defaults (enabled) */
+    uint32_t mesh_count;
+    uint32_t instance_count;
+    const char* const* mesh_names;      /* model name per mesh */
+    const char* const* instance_names;  /* per instance */
+    const char* const* material_names;  /* per material */
+    const char* warnings;           /* one line per model or texture that could not be read ("" if none);
+                                       as in the reference, their instances or textures are left out */
+} tr_scene_file_info;
+
+/* Loads a scene file; *out_file owns every array the info points at. */
+tr_status tr_scene_file_load(const char* path, const char* base_dir, void** out_file);
+tr_status tr_scene_file_get_info(void* file, tr_scene_file_info* out);
+tr_status tr_scene_file_free(void* file);
+/* Message of the last failed scene-file or cache call on this thread. */
+const char* tr_scene_file_last_error(void);
+
+/* ≙ SaveToCache of ModelFile.cpp:50-93: writes a mesh and its materials in
+ * the reference's model cache format (a mesh without normals gets smooth
+ * vertex normals, as the reference's importer generates them; without
+ * texcoords, zeros). material_names: material_count names;
+ * texture_paths: NULL or material_count x TR_PROP_COUNT paths (NULL or "" for
+ * none) stored with the texture-enabled properties. */
+tr_status tr_model_cache_write(const char* path, const tr_mesh_desc* mesh, const tr_material_desc* materials,
+                               const char* const* material_names, const char* const* texture_paths,
+                               uint32_t material_count);
+/* ≙ SaveToCache of TextureFile.cpp:30-45: RGBA binary16 texels. */
+tr_status tr_texture_cache_write(const char* path, uint32_t width, uint32_t height, const uint16_t* texels);
+
 /* ---- ray pick ----
  * ≙ RayPickResult (CommonStructs.h:132-141): the camera position, the direction
  * of the picked pixel's camera ray, and what the ray hit first (instance and

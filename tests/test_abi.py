@@ -53,6 +53,9 @@ def test_struct_layouts_match_ctypes(tmp_path):
         "tr_batch_info": _abi.BatchInfo,
         "tr_batch_statistics": _abi.BatchStatistics,
         "tr_ray_pick_result": _abi.RayPickResult,
+        "tr_sky_desc": _abi.SkyDesc,
+        "tr_texture_desc": _abi.TextureDesc,
+        "tr_scene_file_info": _abi.SceneFileInfo,
     }
     lines = ['#include <stdio.h>', '#include <stddef.h>', f'#include "{HEADER}"', "int main(void){"]
     for cname, py in structs.items():

@@ -24,3 +24,4 @@ from .scenes import (  # noqa: F401
     sphere_scene,
     textured_cornell,
 )
+from .scenefile import SceneFile, load_scene_file, write_model_cache, write_texture_cache  # noqa: F401,E402

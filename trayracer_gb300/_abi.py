@@ -278,6 +278,27 @@ class BatchStatistics(C.Structure):
 
 
 # name -> (restype, argtypes) for every function include/trayracer.h declares
+class SceneFileInfo(C.Structure):
+    """tr_scene_file_info."""
+
+    _fields_ = [
+        ("scene", C.POINTER(SceneDesc)),
+        ("camera", Camera),
+        ("camera_target", C.c_float * 3),
+        ("camera_up", C.c_float * 3),
+        ("settings", KernelSettings),
+        ("ao_dist", C.c_float),
+        ("z_depth_max", C.c_float),
+        ("sky", SkyDesc),
+        ("mesh_count", C.c_uint32),
+        ("instance_count", C.c_uint32),
+        ("mesh_names", C.POINTER(C.c_char_p)),
+        ("instance_names", C.POINTER(C.c_char_p)),
+        ("material_names", C.POINTER(C.c_char_p)),
+        ("warnings", C.c_char_p),
+    ]
+
+
 _V = C.c_void_p
 _U = C.c_uint32
 FUNCTIONS = {
@@ -312,6 +333,12 @@ FUNCTIONS = {
     "tr_set_render_mode": (C.c_int, [_V, _U, _U, C.c_float, C.c_float]),
     "tr_pick_ray": (C.c_int, [_V, _V, C.c_int32, C.c_int32, C.POINTER(RayPickResult)]),
     "tr_set_sky": (C.c_int, [_V, C.POINTER(SkyDesc)]),
+    "tr_scene_file_load": (C.c_int, [C.c_char_p, C.c_char_p, C.POINTER(_V)]),
+    "tr_scene_file_get_info": (C.c_int, [_V, C.POINTER(SceneFileInfo)]),
+    "tr_scene_file_free": (C.c_int, [_V]),
+    "tr_scene_file_last_error": (C.c_char_p, []),
+    "tr_model_cache_write": (C.c_int, [C.c_char_p, C.POINTER(MeshDesc), _V, _V, _V, _U]),
+    "tr_texture_cache_write": (C.c_int, [C.c_char_p, _U, _U, _V]),
     "tr_get_tuning": (C.c_int, [_V, C.POINTER(Tuning)]),
     "tr_set_tuning": (C.c_int, [_V, C.POINTER(Tuning)]),
     "tr_autotune": (C.c_int, [_V, _V, _U, C.POINTER(TuneReport)]),
