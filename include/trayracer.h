@@ -418,9 +418,9 @@ typedef struct tr_sky_desc {
 tr_status tr_set_sky(void* ctx, const tr_sky_desc* sky);
 
 /* ---- scene files ----
- * ≙ SceneFile::Load (Tracer/FileIO/SceneFile.cpp:89-436, 680-723) with
- * ModelFile::Import / TextureFile::Import (ModelFile.cpp:50-160, 330-449,
- * TextureFile.cpp:30-150): the reference's scene JSON ("models", "instances",
+ * ≙ SceneFile::Load (Tracer/FileIO/SceneFile.cpp:89-441, 683-730) with
+ * ModelFile::Import / TextureFile::Import (ModelFile.cpp:53-160, 331-449,
+ * TextureFile.cpp:33-175): the reference's scene JSON ("models", "instances",
  * "materials", "camera", "renderer", "sky"; "post" is ignored) read into a
  * two-level tr_scene_desc. Models load from the reference's model cache format
  * ("MDL" version 2: the file itself, or the cache file the reference keeps for
@@ -456,7 +456,7 @@ tr_status tr_scene_file_free(void* file);
 /* Message of the last failed scene-file or cache call on this thread. */
 const char* tr_scene_file_last_error(void);
 
-/* ≙ SaveToCache of ModelFile.cpp:50-93: writes a mesh and its materials in
+/* ≙ SaveToCache of ModelFile.cpp:53-95: writes a mesh and its materials in
  * the reference's model cache format (a mesh without normals gets smooth
  * vertex normals, as the reference's importer generates them; without
  * texcoords, zeros). material_names: material_count names;
@@ -465,7 +465,7 @@ const char* tr_scene_file_last_error(void);
 tr_status tr_model_cache_write(const char* path, const tr_mesh_desc* mesh, const tr_material_desc* materials,
                                const char* const* material_names, const char* const* texture_paths,
                                uint32_t material_count);
-/* ≙ SaveToCache of TextureFile.cpp:30-45: RGBA binary16 texels. */
+/* ≙ SaveToCache of TextureFile.cpp:33-48: RGBA binary16 texels. */
 tr_status tr_texture_cache_write(const char* path, uint32_t width, uint32_t height, const uint16_t* texels);
 
 /* ---- ray pick ----

@@ -89,7 +89,7 @@ std::string lower(std::string s)
     return s;
 }
 
-// BinaryFile::CachedFilePath (BinaryFile.cpp:58-62): "cache/" + std::hash of the
+// BinaryFile::CachedFilePath (BinaryFile.cpp:67-71): "cache/" + std::hash of the
 // path + ".bin". The reference is built with MSVC, whose std::hash of a string
 // is 64-bit FNV-1a over its bytes (Fowler, Noll, Vo).
 uint64_t fnv1a64(const std::string& s)
@@ -291,7 +291,7 @@ struct ModelData {
     std::vector<MaterialRec> mats;
 };
 
-// LoadFromCache (ModelFile.cpp:97-160): header, vertices, normals, texcoords,
+// LoadFromCache (ModelFile.cpp:98-160): header, vertices, normals, texcoords,
 // indices, material indices, then the materials with their property values and
 // texture paths in MaterialPropertyIds order.
 bool read_model_cache(const std::vector<char>& buf, ModelData& m, std::string& err)
@@ -362,7 +362,7 @@ struct TextureData {
     std::vector<uint16_t> texels;   // RGBA binary16
 };
 
-// Texture LoadFromCache (TextureFile.cpp:47-75): header, int2 resolution, half4 pixels.
+// Texture LoadFromCache (TextureFile.cpp:52-80): header, int2 resolution, half4 pixels.
 bool read_texture_cache(const std::vector<char>& buf, TextureData& t, std::string& err)
 {
     if (!header_is(buf, kTextureId, kCacheVersion)) {
@@ -416,7 +416,7 @@ void smooth_normals(const std::vector<float>& pos, const std::vector<uint32_t>& 
 
 // ------------------------------------------------------------------ Wavefront OBJ
 // Stands in for the reference's Assimp import of OBJ models (ModelFile.cpp:
-// 330-449): polygons become triangle fans, each distinct (position, texcoord,
+// 331-449): polygons become triangle fans, each distinct (position, texcoord,
 // normal) triple one vertex; vertices without a normal take the normalised sum
 // of the unit normals of the faces around their position. Materials come from
 // the mtllib files: Kd, Ke, map_Kd (diffuse), map_Ks (specular), norm / map_Bump /
@@ -717,7 +717,7 @@ struct SceneFileObj {
     tr_scene_desc desc{};
     tr_scene_file_info info{};
 
-    // TextureFile::Import (TextureFile.cpp:107-150): one texture per global path;
+    // TextureFile::Import (TextureFile.cpp:120-175): one texture per global path;
     // the texture cache format is read from the file itself or from its cache
     // file. Returns the texture's index, or -1 when it cannot be read (the
     // property then has no texture, as when the reference's image import fails).
@@ -746,7 +746,7 @@ struct SceneFileObj {
         return int32_t(textures.size() - 1);
     }
 
-    // ModelFile::Import (ModelFile.cpp:330-449): the model cache format from the
+    // ModelFile::Import (ModelFile.cpp:331-449): the model cache format from the
     // file itself or its cache file (LoadFromCache's write-time rule), else OBJ.
     bool model(const std::string& path, ModelData& m, std::string& err)
     {
@@ -786,7 +786,7 @@ tr_status load_scene(const std::string& path, const std::string& base, SceneFile
                        "\"" + path + "\" does not contain valid json" + (err.empty() ? "" : ": " + err));
     S.base = base;
 
-    // ParseModels (SceneFile.cpp:237-265): name -> path, the last declaration wins
+    // ParseModels (SceneFile.cpp:256-284): name -> path, the last declaration wins
     std::map<std::string, std::string> declared;
     if (const json::Value* ms = doc.find("models"); ms && ms->is_array())
         for (const json::Value& m : ms->items) {
@@ -839,7 +839,7 @@ tr_status load_scene(const std::string& path, const std::string& base, SceneFile
             insts.push_back(in);
         }
 
-    // ImportModels (SceneFile.cpp:412-441): every declared model an instance names;
+    // ImportModels (SceneFile.cpp:413-441): every declared model an instance names;
     // instances of undeclared or unreadable models are left out
     std::map<std::string, ModelData> imported;
     std::set<std::string> failed;
@@ -859,7 +859,7 @@ tr_status load_scene(const std::string& path, const std::string& base, SceneFile
         imported.emplace(in.model, std::move(m));
     }
 
-    // ParseMaterials (SceneFile.cpp:192-233): per model, per material name, the
+    // ParseMaterials (SceneFile.cpp:195-252): per model, per material name, the
     // properties by lower-case MaterialPropertyIds name and "<name>Map" textures
     if (const json::Value* mm = doc.find("materials"); mm && mm->is_array())
         for (const json::Value& jm : mm->items) {
@@ -1011,7 +1011,7 @@ tr_status load_scene(const std::string& path, const std::string& base, SceneFile
     std::copy(target, target + 3, info.camera_target);
     std::copy(up, up + 3, info.camera_up);
 
-    // ParseRenderSettings (SceneFile.cpp:358-380) over Renderer::DefaultSettings
+    // ParseRenderSettings (SceneFile.cpp:351-376) over Renderer::DefaultSettings
     tr_kernel_settings& st = info.settings;
     st = tr_kernel_settings{1u, TR_MAX_DEPTH, 0u, 1e-3f, 1u, 0u, 10.f, 0u};
     info.ao_dist = 1.f;
@@ -1027,7 +1027,7 @@ tr_status load_scene(const std::string& path, const std::string& base, SceneFile
         read_number(*r, "ray-epsilon", st.ray_epsilon);
     }
 
-    // ParseSkySettings (SceneFile.cpp:384-410) over Sky's defaults (Sky.h:55-67)
+    // ParseSkySettings (SceneFile.cpp:380-409) over Sky's defaults (Sky.h:55-67)
     tr_sky_desc& sky = info.sky;
     sky = tr_sky_desc{1u, 1u, {0.f, 1.f, 0.f}, 32.f, 1000.f, 4.f, 1.f};
     if (const json::Value* j = doc.find("sky")) {
