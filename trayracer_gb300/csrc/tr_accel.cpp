@@ -16,9 +16,7 @@ SceneAccel build_accel(const tr_scene_desc& desc, const std::vector<uint32_t>& m
     std::vector<Aabb> meshBox(meshCount);
     for (uint32_t mi = 0; mi < meshCount; ++mi) {
         const tr_mesh_desc& m = scene_mesh(desc, mi);
-        const BinaryBvh bin = build_binary_bvh(m.positions, m.indices, m.triangle_count, opt);
-        const Cwbvh wide = collapse_to_cwbvh(bin, m.positions, m.indices);
-        meshBox[mi] = bin.nodes[0].box;
+        const Cwbvh wide = build_cwbvh(m.positions, m.indices, m.triangle_count, opt, &meshBox[mi]);
         const uint32_t nodeBase = uint32_t(out.nodes.size());
         const uint32_t slotBase = uint32_t(out.tris.size() / 3);
         out.meshRoot.push_back(nodeBase);

@@ -152,8 +152,7 @@ std::vector<ItemBuild> build_items(const tr_batch_item* items, uint32_t count, u
                 opt.maxLeafSize = d.bvh_leaf_size ? d.bvh_leaf_size : leafSize;
                 opt.threads = 1;
                 const tr_mesh_desc& m = *d.mesh;
-                const BinaryBvh bin = build_binary_bvh(m.positions, m.indices, m.triangle_count, opt);
-                r.bvh = collapse_to_cwbvh(bin, m.positions, m.indices);
+                r.bvh = build_cwbvh(m.positions, m.indices, m.triangle_count, opt);
                 r.triangles = m.triangle_count;
             } catch (const std::exception& e) {
                 r.error = e.what();

@@ -1,6 +1,6 @@
-// Host BVH builder: binned SAH over triangle bounds, then a greedy collapse to
-// an 8-wide compressed BVH (CWBVH) with octant-ordered child slots and 8-bit
-// quantized child boxes (Ylitie, Karras, Laine, HPG 2017).
+// Host BVH builder: binned SAH over triangle bounds, then a collapse (SAH-optimal
+// or greedy) to an 8-wide compressed BVH (CWBVH) with octant-ordered child slots
+// and 8-bit quantized child boxes (Ylitie, Karras, Laine, HPG 2017).
 #include "tr_bvh.h"
 
 #include <algorithm>
@@ -191,6 +191,125 @@ inline void set_byte(uint32_t* words, int i, uint32_t v)
     words[i >> 2] |= (v & 0xffu) << ((i & 3) * 8);
 }
 
+// A child of a wide node: binary subtree `bin`, either a leaf holding its
+// `count` triangles (primRefs[first, first + count)) or an internal wide node.
+struct Kid {
+    uint32_t bin;
+    bool leaf;
+    uint32_t first;
+    uint32_t count;
+};
+
+// SAH-optimal collapse of a binary BVH into 8-wide nodes (Ylitie, Karras, Laine,
+// HPG 2017, section 3.1): for every binary node n and i = 1..8, the least SAH
+// cost of representing n's subtree by at most i children of a wide node, where a
+// child is a leaf of up to maxLeaf triangles (cost: area x kPrim per triangle) or
+// an internal wide node (area x kNode, plus the cost of its own up-to-8 children).
+struct SahCollapse {
+    std::vector<float> cost;       // 8 per binary node
+    std::vector<uint8_t> choice;   // 8 per node: [0] 0 leaf / 1 internal; [i] 0xff like i-1, else slots k of the left child
+    std::vector<uint8_t> split8;   // slots of the left child in the node's own 8 children
+    std::vector<uint32_t> first, prims;
+
+    SahCollapse() = default;
+    SahCollapse(const BinaryBvh& bvh, uint32_t maxLeaf)
+    {
+        // a triangle test weighed as a node visit: with these kernels a node test (80 bytes,
+        // eight slabs) and a triangle test (48 bytes) cost about alike, and this weight gave
+        // the fewest node visits and triangle tests together on the benchmark heightfield
+        constexpr float kNode = 1.f, kPrim = 1.f;
+        const std::vector<BinaryNode>& bn = bvh.nodes;
+        const size_t n = bn.size();
+        cost.assign(8 * n, 0.f);
+        choice.assign(8 * n, 0);
+        split8.assign(n, 0);
+        first.assign(n, 0);
+        prims.assign(n, 0);
+        // children are allocated after their parent: reverse index order is bottom-up
+        for (size_t x = n; x-- > 0;) {
+            const BinaryNode& b = bn[x];
+            const float area = box_area(b.box);
+            float* c = &cost[8 * x];
+            uint8_t* ch = &choice[8 * x];
+            if (b.count > 0) {
+                first[x] = b.left;
+                prims[x] = b.count;
+                const float leaf = b.count <= maxLeaf ? area * kPrim * float(b.count) : INFINITY;
+                for (int i = 0; i < 8; ++i) {
+                    c[i] = leaf;
+                    ch[i] = i == 0 ? 0 : 0xff;
+                }
+                continue;
+            }
+            const uint32_t l = b.left, r = b.left + 1;
+            first[x] = first[l];
+            prims[x] = prims[l] + prims[r];
+            const float* cl = &cost[8 * l];
+            const float* cr = &cost[8 * r];
+            float dist[9];
+            uint8_t distK[9];
+            for (int j = 2; j <= 8; ++j) {
+                dist[j] = INFINITY;
+                distK[j] = 1;
+                for (int k = 1; k < j; ++k) {
+                    const float v = cl[k - 1] + cr[j - k - 1];
+                    if (v < dist[j]) {
+                        dist[j] = v;
+                        distK[j] = uint8_t(k);
+                    }
+                }
+            }
+            split8[x] = distK[8];
+            const float internal = area * kNode + dist[8];
+            const float leaf = prims[x] <= maxLeaf ? area * kPrim * float(prims[x]) : INFINITY;
+            c[0] = leaf <= internal ? leaf : internal;
+            ch[0] = leaf <= internal ? 0 : 1;
+            for (int i = 1; i < 8; ++i) {
+                if (dist[i + 1] < c[i - 1]) {
+                    c[i] = dist[i + 1];
+                    ch[i] = distK[i + 1];
+                } else {
+                    c[i] = c[i - 1];
+                    ch[i] = 0xff;
+                }
+            }
+        }
+    }
+
+    // the children representing node x's subtree in at most i + 1 slots
+    void gather(const std::vector<BinaryNode>& bn, uint32_t x, int i, Kid* out, int& count) const
+    {
+        while (i > 0 && choice[8 * size_t(x) + size_t(i)] == 0xff)
+            --i;
+        if (bn[x].count > 0) {
+            out[count++] = Kid{x, true, bn[x].left, bn[x].count};
+            return;
+        }
+        if (i == 0) {
+            const bool leaf = choice[8 * size_t(x)] == 0;
+            out[count++] = Kid{x, leaf, first[x], prims[x]};
+            return;
+        }
+        const int k = choice[8 * size_t(x) + size_t(i)];
+        gather(bn, bn[x].left, k - 1, out, count);
+        gather(bn, bn[x].left + 1, i - k, out, count);
+    }
+
+    // the children of the wide node made for binary node x
+    int children(const std::vector<BinaryNode>& bn, uint32_t x, Kid* out) const
+    {
+        int count = 0;
+        if (bn[x].count > 0 || choice[8 * size_t(x)] == 0) {
+            out[count++] = Kid{x, true, first[x], prims[x]};  // the whole subtree is one leaf
+            return count;
+        }
+        const int k = split8[x];
+        gather(bn, bn[x].left, k - 1, out, count);
+        gather(bn, bn[x].left + 1, 8 - k - 1, out, count);
+        return count;
+    }
+};
+
 } // namespace
 
 namespace {
@@ -240,6 +359,19 @@ BinaryBvh build_binary_bvh(const float* positions, const uint32_t* indices, uint
     return build_from_prims(prims, options);
 }
 
+Cwbvh build_cwbvh(const float* positions, const uint32_t* indices, uint32_t triCount, const BvhBuildOptions& opt,
+                  Aabb* bounds)
+{
+    BvhBuildOptions o = opt;
+    const uint32_t leaf = std::max(1u, std::min(opt.maxLeafSize, 3u));
+    if (opt.sahCollapse)
+        o.maxLeafSize = 1;
+    const BinaryBvh bin = build_binary_bvh(positions, indices, triCount, o);
+    if (bounds)
+        *bounds = bin.nodes[0].box;
+    return collapse_to_cwbvh(bin, positions, indices, opt.sahCollapse ? leaf : 0u);
+}
+
 BinaryBvh build_binary_bvh_boxes(const Aabb* boxes, uint32_t count, const BvhBuildOptions& options)
 {
     std::vector<PrimInfo> prims(count);
@@ -252,8 +384,9 @@ BinaryBvh build_binary_bvh_boxes(const Aabb* boxes, uint32_t count, const BvhBui
     return build_from_prims(prims, options);
 }
 
-Cwbvh collapse_to_cwbvh(const BinaryBvh& bvh, const float* positions, const uint32_t* indices)
+Cwbvh collapse_to_cwbvh(const BinaryBvh& bvh, const float* positions, const uint32_t* indices, uint32_t sahMaxLeaf)
 {
+    const SahCollapse sah = sahMaxLeaf && !bvh.primRefs.empty() ? SahCollapse(bvh, sahMaxLeaf) : SahCollapse();
     Cwbvh out;
     const std::vector<BinaryNode>& bn = bvh.nodes;
     out.nodes.reserve(bn.size() / 4 + 1);
@@ -271,42 +404,52 @@ Cwbvh collapse_to_cwbvh(const BinaryBvh& bvh, const float* positions, const uint
     };
     std::deque<Task> tasks;
     tasks.push_back({0, 0});
+    const SahCollapse* dp = sah.cost.empty() ? nullptr : &sah;
     while (!tasks.empty()) {
         const Task task = tasks.front();
         tasks.pop_front();
 
-        // gather up to 8 children by repeatedly opening the largest internal child
-        uint32_t kids[8];
+        // the up to 8 children of the wide node: binary subtrees, each a leaf
+        // (its triangles tested together) or an internal wide node
+        Kid kids[8];
         int kidCount = 0;
-        if (bn[task.bin].count > 0) {
-            kids[kidCount++] = task.bin;  // a leaf root
+        if (dp) {
+            kidCount = dp->children(bn, task.bin, kids);
         } else {
-            kids[kidCount++] = bn[task.bin].left;
-            kids[kidCount++] = bn[task.bin].left + 1;
-        }
-        while (kidCount < 8) {
-            int best = -1;
-            float bestArea = -1.f;
-            for (int k = 0; k < kidCount; ++k) {
-                if (bn[kids[k]].count == 0) {
-                    const float a = box_area(bn[kids[k]].box);
-                    if (a > bestArea) {
-                        bestArea = a;
-                        best = k;
+            // greedy: repeatedly open the largest internal child
+            uint32_t bins[8];
+            if (bn[task.bin].count > 0) {
+                bins[kidCount++] = task.bin;  // a leaf root
+            } else {
+                bins[kidCount++] = bn[task.bin].left;
+                bins[kidCount++] = bn[task.bin].left + 1;
+            }
+            while (kidCount < 8) {
+                int best = -1;
+                float bestArea = -1.f;
+                for (int k = 0; k < kidCount; ++k) {
+                    if (bn[bins[k]].count == 0) {
+                        const float a = box_area(bn[bins[k]].box);
+                        if (a > bestArea) {
+                            bestArea = a;
+                            best = k;
+                        }
                     }
                 }
+                if (best < 0)
+                    break;
+                const uint32_t opened = bins[best];
+                bins[best] = bn[opened].left;
+                bins[kidCount++] = bn[opened].left + 1;
             }
-            if (best < 0)
-                break;
-            const uint32_t opened = kids[best];
-            kids[best] = bn[opened].left;
-            kids[kidCount++] = bn[opened].left + 1;
+            for (int k = 0; k < kidCount; ++k)
+                kids[k] = Kid{bins[k], bn[bins[k]].count > 0, bn[bins[k]].left, bn[bins[k]].count};
         }
 
         Aabb nodeBox;
         box_empty(nodeBox);
         for (int k = 0; k < kidCount; ++k)
-            box_grow(nodeBox, bn[kids[k]].box.lo, bn[kids[k]].box.hi);
+            box_grow(nodeBox, bn[kids[k].bin].box.lo, bn[kids[k].bin].box.hi);
 
         // slot assignment: slot s holds the child nearest for rays of octant s
         // (octant bit a set = negative direction along axis a)
@@ -321,7 +464,7 @@ Cwbvh collapse_to_cwbvh(const BinaryBvh& bvh, const float* positions, const uint
             for (int k = 0; k < kidCount; ++k) {
                 float c[3];
                 for (int a = 0; a < 3; ++a)
-                    c[a] = 0.5f * (bn[kids[k]].box.lo[a] + bn[kids[k]].box.hi[a]) - pc[a];
+                    c[a] = 0.5f * (bn[kids[k].bin].box.lo[a] + bn[kids[k].bin].box.hi[a]) - pc[a];
                 for (int s = 0; s < 8; ++s) {
                     const float dx = (s & 1) ? -1.f : 1.f, dy = (s & 2) ? -1.f : 1.f, dz = (s & 4) ? -1.f : 1.f;
                     cost[k][s] = c[0] * dx + c[1] * dy + c[2] * dz;
@@ -378,7 +521,8 @@ Cwbvh collapse_to_cwbvh(const BinaryBvh& bvh, const float* positions, const uint
         for (int s = 0; s < 8; ++s) {
             if (slotKid[s] < 0)
                 continue;
-            const BinaryNode& kid = bn[kids[slotKid[s]]];
+            const Kid& kk = kids[slotKid[s]];
+            const BinaryNode& kid = bn[kk.bin];
             for (int a = 0; a < 3; ++a) {
                 const double lo = (double(kid.box.lo[a]) - double(nodeBox.lo[a])) / scale[a];
                 const double hi = (double(kid.box.hi[a]) - double(nodeBox.lo[a])) / scale[a];
@@ -387,17 +531,17 @@ Cwbvh collapse_to_cwbvh(const BinaryBvh& bvh, const float* positions, const uint
                 set_byte(q[a], s, uint32_t(qlo));
                 set_byte(q[3 + a], s, uint32_t(qhi));
             }
-            if (kid.count == 0) {
+            if (!kk.leaf) {
                 imask |= 1u << s;
                 set_byte(meta, s, 0x20u | (24u + uint32_t(s)));
-                tasks.push_back({kids[slotKid[s]], childBase + internalCount});
+                tasks.push_back({kk.bin, childBase + internalCount});
                 internalCount++;
             } else {
                 const uint32_t offset = uint32_t(out.triPrim.size()) - triBase;
-                const uint32_t unary = (1u << kid.count) - 1u;
+                const uint32_t unary = (1u << kk.count) - 1u;
                 set_byte(meta, s, (unary << 5) | offset);
-                for (uint32_t i = 0; i < kid.count; ++i) {
-                    const uint32_t prim = bvh.primRefs[kid.left + i];
+                for (uint32_t i = 0; i < kk.count; ++i) {
+                    const uint32_t prim = bvh.primRefs[kk.first + i];
                     if (!positions) {  // a BVH over boxes: the leaf slot only names the primitive
                         out.triPrim.push_back(prim);
                         continue;

@@ -25,6 +25,9 @@ struct BinaryNode {
 
 struct BvhBuildOptions {
     uint32_t maxLeafSize = 3;   // 1..3 (the CWBVH leaf encoding holds up to 3)
+    // true: the binary BVH is built down to one triangle per leaf and the wide leaves
+    // (up to maxLeafSize triangles) are chosen by the SAH-optimal collapse
+    bool sahCollapse = true;
     uint32_t bins = 16;
     uint32_t threads = 0;       // 0 = hardware concurrency
 };
@@ -41,6 +44,7 @@ struct Cwbvh {
 };
 
 // Builds a binary BVH over triangles given as positions (float3 per vertex)
+// (leaves of up to maxLeafSize triangles, or of one when sahCollapse)
 // and indices (uint3 per triangle).
 BinaryBvh build_binary_bvh(const float* positions, const uint32_t* indices, uint32_t triCount,
                            const BvhBuildOptions& options);
@@ -52,7 +56,16 @@ BinaryBvh build_binary_bvh_boxes(const Aabb* boxes, uint32_t count, const BvhBui
 // Collapses a binary BVH into the 8-wide compressed layout and packs the
 // traversal triangles (v0, e1 = v1 - v0, e2 = v2 - v0). positions == nullptr
 // (a BVH over boxes): no triangles, triPrim names the primitive of each leaf
-// slot.
-Cwbvh collapse_to_cwbvh(const BinaryBvh& bvh, const float* positions, const uint32_t* indices);
+// slot. sahMaxLeaf = 0: greedy collapse (open the largest internal child until
+// 8); 1..3: SAH-optimal collapse with leaves of up to sahMaxLeaf triangles.
+Cwbvh collapse_to_cwbvh(const BinaryBvh& bvh, const float* positions, const uint32_t* indices,
+                        uint32_t sahMaxLeaf = 0);
 
 } // namespace tr
+
+namespace tr {
+// The 8-wide BVH of one mesh as the options ask: binary build, then the
+// SAH-optimal or the greedy collapse.
+Cwbvh build_cwbvh(const float* positions, const uint32_t* indices, uint32_t triCount, const BvhBuildOptions& opt,
+                  Aabb* bounds = nullptr);
+}  // namespace tr
