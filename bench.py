@@ -672,6 +672,26 @@ def main():
                 except ValueError:
                     traffic = None
 
+    # --- the other stages by the same fixed byte formulas (per step). Shade: 140 B read per
+    # shaded hit (state 48 + hit 16 + shading record 72 + material index 4) plus 48 B per
+    # extend and per shadow ray written; connect: 48 B per shadow ray plus its traversal
+    # bytes; finalize: per pixel the multi_sample path radiances (16 B each), the
+    # accumulator read and written and the colour written (16 B each). The radiance
+    # read-modify-writes of emissive hits and visible shadow rays are not in the counters, so
+    # the shade and connect figures are lower bounds.
+    secondary = ext_rays - int(ext_per_bounce[0])
+    stage_bytes = {
+        "shade": hit_rays * 140 + (secondary + sh_rays) * 48,
+        "connect": sh_rays * 48 + cs["traversal_connect_nodes"] * NODE_BYTES + cs["traversal_connect_tris"] * TRI_BYTES,
+        "finalize": frames_per_step * scene.width * scene.height * (16 * args.ms + 48),
+    }
+    stage_roofline = {}
+    for k, b in stage_bytes.items():
+        sec = stage_ms[k] / 1e3
+        gbs = b / sec / 1e9 if sec > 0 else None
+        stage_roofline[k] = {"bytes_per_step": int(b), "achieved_gbs": None if gbs is None else round(gbs, 1),
+                             "frac": None if gbs is None else round(gbs / peak, 4)}
+
     # --- image accuracy on a pixel band against the FP64 oracle
     rmse = None
     cpu = None
@@ -755,6 +775,7 @@ def main():
                 "connect_nodes_per_ray": round(cs["traversal_connect_nodes"] / max(1, sh_rays), 3),
                 "connect_tris_per_ray": round(cs["traversal_connect_tris"] / max(1, sh_rays), 3),
             },
+            "stage_roofline": stage_roofline,  # lower bounds for shade and connect (see above)
             "cpu_baseline": cpu,
             "clocks": clocks.summary(),
             "e2e": {
