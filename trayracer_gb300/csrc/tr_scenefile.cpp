@@ -1,8 +1,6 @@
 // Scene files: the reference's scene JSON (Tracer/FileIO/SceneFile.cpp), its
 // model and texture cache formats (ModelFile.cpp / TextureFile.cpp over
 // BinaryFile.h/.inl) and Wavefront OBJ, read into a two-level tr_scene_desc.
-#include <cuda_fp16.h>
-
 #include <algorithm>
 #include <array>
 #include <cmath>
