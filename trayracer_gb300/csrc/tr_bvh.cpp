@@ -8,6 +8,7 @@
 #include <cmath>
 #include <cstring>
 #include <deque>
+#include <memory>
 #include <thread>
 
 namespace tr {
@@ -206,72 +207,99 @@ struct Kid {
 // child is a leaf of up to maxLeaf triangles (cost: area x kPrim per triangle) or
 // an internal wide node (area x kNode, plus the cost of its own up-to-8 children).
 struct SahCollapse {
-    std::vector<float> cost;       // 8 per binary node
-    std::vector<uint8_t> choice;   // 8 per node: [0] 0 leaf / 1 internal; [i] 0xff like i-1, else slots k of the left child
-    std::vector<uint8_t> split8;   // slots of the left child in the node's own 8 children
-    std::vector<uint32_t> first, prims;
+    // tables written before they are read (children before parents), so left uninitialised
+    std::unique_ptr<float[]> cost;       // 8 per binary node
+    std::unique_ptr<uint8_t[]> choice;   // 8 per node: [0] 0 leaf / 1 internal; [i] 0xff like i-1, else slots k of the left child
+    std::unique_ptr<uint8_t[]> split8;   // slots of the left child in the node's own 8 children
+    std::unique_ptr<uint32_t[]> first, prims;
+    const std::vector<BinaryNode>* bn = nullptr;
+    uint32_t maxLeaf = 3;
+    int spawnDepth = 0;
 
     SahCollapse() = default;
-    SahCollapse(const BinaryBvh& bvh, uint32_t maxLeaf)
+    SahCollapse(const BinaryBvh& bvh, uint32_t maxLeaf) : bn(&bvh.nodes), maxLeaf(maxLeaf)
+    {
+        const size_t n = bvh.nodes.size();
+        cost.reset(new float[8 * n]);
+        choice.reset(new uint8_t[8 * n]);
+        split8.reset(new uint8_t[n]);
+        first.reset(new uint32_t[n]);
+        prims.reset(new uint32_t[n]);
+        const unsigned hw = std::max(1u, std::thread::hardware_concurrency());
+        while ((1u << spawnDepth) < hw)
+            ++spawnDepth;
+        solve(0, 0);
+    }
+    bool empty() const { return !cost; }
+
+    // the table of node x after those of its subtree; the top levels split across threads
+    void solve(uint32_t x, int depth)
+    {
+        const BinaryNode& b = (*bn)[x];
+        if (b.count == 0) {
+            const uint32_t l = b.left;
+            if (depth < spawnDepth) {
+                std::thread t([this, l, depth] { solve(l, depth + 1); });
+                solve(l + 1, depth + 1);
+                t.join();
+            } else {
+                solve(l, depth + 1);
+                solve(l + 1, depth + 1);
+            }
+        }
+        node(x);
+    }
+
+    void node(uint32_t x)
     {
         // a triangle test weighed as a node visit: with these kernels a node test (80 bytes,
         // eight slabs) and a triangle test (48 bytes) cost about alike, and this weight gave
         // the fewest node visits and triangle tests together on the benchmark heightfield
         constexpr float kNode = 1.f, kPrim = 1.f;
-        const std::vector<BinaryNode>& bn = bvh.nodes;
-        const size_t n = bn.size();
-        cost.assign(8 * n, 0.f);
-        choice.assign(8 * n, 0);
-        split8.assign(n, 0);
-        first.assign(n, 0);
-        prims.assign(n, 0);
-        // children are allocated after their parent: reverse index order is bottom-up
-        for (size_t x = n; x-- > 0;) {
-            const BinaryNode& b = bn[x];
-            const float area = box_area(b.box);
-            float* c = &cost[8 * x];
-            uint8_t* ch = &choice[8 * x];
-            if (b.count > 0) {
-                first[x] = b.left;
-                prims[x] = b.count;
-                const float leaf = b.count <= maxLeaf ? area * kPrim * float(b.count) : INFINITY;
-                for (int i = 0; i < 8; ++i) {
-                    c[i] = leaf;
-                    ch[i] = i == 0 ? 0 : 0xff;
-                }
-                continue;
+        const BinaryNode& b = (*bn)[x];
+        const float area = box_area(b.box);
+        float* c = &cost[8 * size_t(x)];
+        uint8_t* ch = &choice[8 * size_t(x)];
+        if (b.count > 0) {
+            first[x] = b.left;
+            prims[x] = b.count;
+            const float leaf = b.count <= maxLeaf ? area * kPrim * float(b.count) : INFINITY;
+            for (int i = 0; i < 8; ++i) {
+                c[i] = leaf;
+                ch[i] = i == 0 ? 0 : 0xff;
             }
-            const uint32_t l = b.left, r = b.left + 1;
-            first[x] = first[l];
-            prims[x] = prims[l] + prims[r];
-            const float* cl = &cost[8 * l];
-            const float* cr = &cost[8 * r];
-            float dist[9];
-            uint8_t distK[9];
-            for (int j = 2; j <= 8; ++j) {
-                dist[j] = INFINITY;
-                distK[j] = 1;
-                for (int k = 1; k < j; ++k) {
-                    const float v = cl[k - 1] + cr[j - k - 1];
-                    if (v < dist[j]) {
-                        dist[j] = v;
-                        distK[j] = uint8_t(k);
-                    }
+            split8[x] = 0;
+            return;
+        }
+        first[x] = first[b.left];
+        prims[x] = prims[b.left] + prims[b.left + 1];
+        const float leaf = prims[x] <= maxLeaf ? area * kPrim * float(prims[x]) : INFINITY;
+        const float* cl = &cost[8 * size_t(b.left)];
+        const float* cr = &cost[8 * size_t(b.left + 1)];
+        float dist[9];
+        uint8_t distK[9];
+        for (int j = 2; j <= 8; ++j) {
+            dist[j] = INFINITY;
+            distK[j] = 1;
+            for (int k = 1; k < j; ++k) {
+                const float v = cl[k - 1] + cr[j - k - 1];
+                if (v < dist[j]) {
+                    dist[j] = v;
+                    distK[j] = uint8_t(k);
                 }
             }
-            split8[x] = distK[8];
-            const float internal = area * kNode + dist[8];
-            const float leaf = prims[x] <= maxLeaf ? area * kPrim * float(prims[x]) : INFINITY;
-            c[0] = leaf <= internal ? leaf : internal;
-            ch[0] = leaf <= internal ? 0 : 1;
-            for (int i = 1; i < 8; ++i) {
-                if (dist[i + 1] < c[i - 1]) {
-                    c[i] = dist[i + 1];
-                    ch[i] = distK[i + 1];
-                } else {
-                    c[i] = c[i - 1];
-                    ch[i] = 0xff;
-                }
+        }
+        split8[x] = distK[8];
+        const float internal = area * kNode + dist[8];
+        c[0] = leaf <= internal ? leaf : internal;
+        ch[0] = leaf <= internal ? 0 : 1;
+        for (int i = 1; i < 8; ++i) {
+            if (dist[i + 1] < c[i - 1]) {
+                c[i] = dist[i + 1];
+                ch[i] = distK[i + 1];
+            } else {
+                c[i] = c[i - 1];
+                ch[i] = 0xff;
             }
         }
     }
@@ -404,7 +432,7 @@ Cwbvh collapse_to_cwbvh(const BinaryBvh& bvh, const float* positions, const uint
     };
     std::deque<Task> tasks;
     tasks.push_back({0, 0});
-    const SahCollapse* dp = sah.cost.empty() ? nullptr : &sah;
+    const SahCollapse* dp = sah.empty() ? nullptr : &sah;
     while (!tasks.empty()) {
         const Task task = tasks.front();
         tasks.pop_front();
