@@ -246,6 +246,26 @@ __device__ __forceinline__ void primary_ray(const FrameView& f, const Camera& ca
     }
 }
 
+// Work item i of a launch that makes its camera rays -> the path it traces:
+// pixels taken in 8 x 4 tiles, samples in order, so that the rays a warp starts
+// leave the camera through one compact tile. A permutation of [0, W*H*ms) when
+// the film is a whole number of tiles; otherwise the identity. The order in which
+// paths are traced changes no path's result (radiance and random numbers are
+// keyed by the path index).
+constexpr bool kTiledCameraOrder = true;
+__device__ __forceinline__ uint32_t camera_order(const FrameView& f, uint32_t i)
+{
+    const uint32_t W = f.resX, H = f.resY;
+    if (!kTiledCameraOrder || (W & 7u) || (H & 3u))
+        return i;
+    const uint32_t wh = W * H;
+    const uint32_t sample = i / wh, r = i - sample * wh;
+    const uint32_t tile = r >> 5, within = r & 31u;
+    const uint32_t tilesX = W >> 3;
+    const uint32_t ty = tile / tilesX, tx = tile - ty * tilesX;
+    return sample * wh + ((ty << 2) | (within >> 3)) * W + ((tx << 3) | (within & 7u));
+}
+
 template <bool REF, bool BATCH>
 __global__ void __launch_bounds__(256) generate_kernel(FrameView f, Camera cam, Settings st)
 {
@@ -347,11 +367,12 @@ __global__ void __launch_bounds__(128, 8) extend_kernel(SceneView s, FrameView f
                     if (PRIMARY) {
                         float3 O, D;
                         float T;
-                        primary_ray<false, BATCH>(f, cam, st, i, sc, O, D, T);
-                        O4 = f4(O, u2f(pack_path(i, 0)));
+                        const uint32_t pathIx = BATCH ? i : camera_order(f, i);
+                        primary_ray<false, BATCH>(f, cam, st, pathIx, sc, O, D, T);
+                        O4 = f4(O, u2f(pack_path(pathIx, 0)));
                         D4 = f4(D, 0.f);
                         T4 = make_float4(T, T, T, 1.f);
-                        f.radiance[i] = make_float4(0.f, 0.f, 0.f, 0.f);
+                        f.radiance[pathIx] = make_float4(0.f, 0.f, 0.f, 0.f);
                     } else {
                         O4 = __ldcs(in + i);
                         D4 = __ldcs(in + i + cap);
