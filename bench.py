@@ -784,9 +784,11 @@ def main():
                 "h2d_bytes_per_step": 72 + 32,
                 "d2h_bytes_per_step": scene.width * scene.height * 16,
             },
-            # per frame: extend, shade and connect per bounce, then finalize and advance (the
-            # launch list of profiles/heightfield_960x540_ms4_launches.md: 26 for 8 bounces)
-            "gpu_launches": args.steps * frames_per_step * (3 * st.maxDepth + 2),
+            # per frame: extend, shade and connect per bounce (and the three kernels of the hit
+            # sort when the tuning turned it on), then finalize and advance (the launch list of
+            # profiles/heightfield_960x540_ms4_launches.md: 26 for 8 bounces)
+            "gpu_launches": args.steps * frames_per_step * ((3 + (3 if r.Tuning().get("sort_hits") else 0))
+                                                            * st.maxDepth + 2),
             "scene_upload_s": round(upload_s, 2),
             "tuning": tune,
         }
