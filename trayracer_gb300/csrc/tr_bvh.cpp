@@ -417,29 +417,44 @@ Cwbvh collapse_to_cwbvh(const BinaryBvh& bvh, const float* positions, const uint
     const SahCollapse sah = sahMaxLeaf && !bvh.primRefs.empty() ? SahCollapse(bvh, sahMaxLeaf) : SahCollapse();
     Cwbvh out;
     const std::vector<BinaryNode>& bn = bvh.nodes;
-    out.nodes.reserve(bn.size() / 4 + 1);
-    out.tris.reserve(bvh.primRefs.size() * 3);
-    out.triPrim.reserve(bvh.primRefs.size());
     out.nodes.push_back(CwbvhNode{});
     if (bvh.primRefs.empty()) {
         // empty scene: a root without children never reports a hit
         return out;
     }
 
+    // Layout pass (breadth first, sequential): the children of every wide node,
+    // their slots, and where its internal children and leaf triangles go. Internal
+    // children take consecutive wide indices in slot order, leaf triangles
+    // consecutive slots in slot order.
+    struct WideRec {
+        uint32_t wide;
+        uint32_t childBase;
+        uint32_t triBase;
+        int kidCount;
+        Kid kids[8];
+        int slotKid[8];
+        Aabb box;
+    };
     struct Task {
         uint32_t bin;
         uint32_t wide;
     };
+    std::vector<WideRec> recs;
+    recs.reserve(bn.size() / 4 + 1);
     std::deque<Task> tasks;
     tasks.push_back({0, 0});
+    uint32_t nextWide = 1, nextTri = 0;
     const SahCollapse* dp = sah.empty() ? nullptr : &sah;
     while (!tasks.empty()) {
         const Task task = tasks.front();
         tasks.pop_front();
+        WideRec rec;
+        rec.wide = task.wide;
 
         // the up to 8 children of the wide node: binary subtrees, each a leaf
         // (its triangles tested together) or an internal wide node
-        Kid kids[8];
+        Kid* kids = rec.kids;
         int kidCount = 0;
         if (dp) {
             kidCount = dp->children(bn, task.bin, kids);
@@ -473,17 +488,18 @@ Cwbvh collapse_to_cwbvh(const BinaryBvh& bvh, const float* positions, const uint
             for (int k = 0; k < kidCount; ++k)
                 kids[k] = Kid{bins[k], bn[bins[k]].count > 0, bn[bins[k]].left, bn[bins[k]].count};
         }
+        rec.kidCount = kidCount;
 
-        Aabb nodeBox;
+        Aabb& nodeBox = rec.box;
         box_empty(nodeBox);
         for (int k = 0; k < kidCount; ++k)
             box_grow(nodeBox, bn[kids[k].bin].box.lo, bn[kids[k].bin].box.hi);
 
         // slot assignment: slot s holds the child nearest for rays of octant s
         // (octant bit a set = negative direction along axis a)
-        int slotKid[8];
-        for (int s = 0; s < 8; ++s)
-            slotKid[s] = -1;
+        int* slotKid = rec.slotKid;
+        for (int sl = 0; sl < 8; ++sl)
+            slotKid[sl] = -1;
         {
             float cost[8][8];
             float pc[3];
@@ -493,9 +509,9 @@ Cwbvh collapse_to_cwbvh(const BinaryBvh& bvh, const float* positions, const uint
                 float c[3];
                 for (int a = 0; a < 3; ++a)
                     c[a] = 0.5f * (bn[kids[k].bin].box.lo[a] + bn[kids[k].bin].box.hi[a]) - pc[a];
-                for (int s = 0; s < 8; ++s) {
-                    const float dx = (s & 1) ? -1.f : 1.f, dy = (s & 2) ? -1.f : 1.f, dz = (s & 4) ? -1.f : 1.f;
-                    cost[k][s] = c[0] * dx + c[1] * dy + c[2] * dz;
+                for (int sl = 0; sl < 8; ++sl) {
+                    const float dx = (sl & 1) ? -1.f : 1.f, dy = (sl & 2) ? -1.f : 1.f, dz = (sl & 4) ? -1.f : 1.f;
+                    cost[k][sl] = c[0] * dx + c[1] * dy + c[2] * dz;
                 }
             }
             bool kidDone[8] = {};
@@ -505,13 +521,13 @@ Cwbvh collapse_to_cwbvh(const BinaryBvh& bvh, const float* positions, const uint
                 for (int k = 0; k < kidCount; ++k) {
                     if (kidDone[k])
                         continue;
-                    for (int s = 0; s < 8; ++s) {
-                        if (slotKid[s] >= 0)
+                    for (int sl = 0; sl < 8; ++sl) {
+                        if (slotKid[sl] >= 0)
                             continue;
-                        if (cost[k][s] < bc || bk < 0) {
-                            bc = cost[k][s];
+                        if (cost[k][sl] < bc || bk < 0) {
+                            bc = cost[k][sl];
                             bk = k;
-                            bs = s;
+                            bs = sl;
                         }
                     }
                 }
@@ -520,8 +536,28 @@ Cwbvh collapse_to_cwbvh(const BinaryBvh& bvh, const float* positions, const uint
             }
         }
 
-        // quantization frame
-        CwbvhNode node{};
+        rec.childBase = nextWide;
+        rec.triBase = nextTri;
+        for (int sl = 0; sl < 8; ++sl) {
+            if (slotKid[sl] < 0)
+                continue;
+            const Kid& kk = kids[slotKid[sl]];
+            if (!kk.leaf)
+                tasks.push_back({kk.bin, nextWide++});
+            else
+                nextTri += kk.count;
+        }
+        recs.push_back(rec);
+    }
+    out.nodes.resize(nextWide);
+    out.triPrim.resize(nextTri);
+    if (positions)
+        out.tris.resize(3 * size_t(nextTri));
+
+    // Encoding pass (parallel over wide nodes): quantized child boxes, meta bytes,
+    // the node words and the traversal triangles of its leaves.
+    auto encode = [&](const WideRec& rec) {
+        const Aabb& nodeBox = rec.box;
         uint32_t w0[4] = {0, 0, 0, 0};
         uint32_t meta[2] = {0, 0};
         uint32_t q[6][2] = {};  // qlo.x, qlo.y, qlo.z, qhi.x, qhi.y, qhi.z
@@ -543,59 +579,69 @@ Cwbvh collapse_to_cwbvh(const BinaryBvh& bvh, const float* positions, const uint
         w0[3] = uint32_t(biased[0]) | (uint32_t(biased[1]) << 8) | (uint32_t(biased[2]) << 16);
 
         uint32_t imask = 0;
-        const uint32_t triBase = uint32_t(out.triPrim.size());
-        const uint32_t childBase = uint32_t(out.nodes.size());
         uint32_t internalCount = 0;
-        for (int s = 0; s < 8; ++s) {
-            if (slotKid[s] < 0)
+        uint32_t triCount = 0;
+        for (int sl = 0; sl < 8; ++sl) {
+            if (rec.slotKid[sl] < 0)
                 continue;
-            const Kid& kk = kids[slotKid[s]];
+            const Kid& kk = rec.kids[rec.slotKid[sl]];
             const BinaryNode& kid = bn[kk.bin];
             for (int a = 0; a < 3; ++a) {
                 const double lo = (double(kid.box.lo[a]) - double(nodeBox.lo[a])) / scale[a];
                 const double hi = (double(kid.box.hi[a]) - double(nodeBox.lo[a])) / scale[a];
                 const int qlo = std::max(0, std::min(255, int(std::floor(lo))));
                 const int qhi = std::max(0, std::min(255, int(std::ceil(hi))));
-                set_byte(q[a], s, uint32_t(qlo));
-                set_byte(q[3 + a], s, uint32_t(qhi));
+                set_byte(q[a], sl, uint32_t(qlo));
+                set_byte(q[3 + a], sl, uint32_t(qhi));
             }
             if (!kk.leaf) {
-                imask |= 1u << s;
-                set_byte(meta, s, 0x20u | (24u + uint32_t(s)));
-                tasks.push_back({kk.bin, childBase + internalCount});
+                imask |= 1u << sl;
+                set_byte(meta, sl, 0x20u | (24u + uint32_t(sl)));
                 internalCount++;
             } else {
-                const uint32_t offset = uint32_t(out.triPrim.size()) - triBase;
                 const uint32_t unary = (1u << kk.count) - 1u;
-                set_byte(meta, s, (unary << 5) | offset);
+                set_byte(meta, sl, (unary << 5) | triCount);
                 for (uint32_t i = 0; i < kk.count; ++i) {
                     const uint32_t prim = bvh.primRefs[kk.first + i];
-                    if (!positions) {  // a BVH over boxes: the leaf slot only names the primitive
-                        out.triPrim.push_back(prim);
+                    const size_t slot = size_t(rec.triBase) + triCount + i;
+                    out.triPrim[slot] = prim;
+                    if (!positions)  // a BVH over boxes: the leaf slot only names the primitive
                         continue;
-                    }
                     const float* p0 = positions + 3 * indices[3 * prim + 0];
                     const float* p1 = positions + 3 * indices[3 * prim + 1];
                     const float* p2 = positions + 3 * indices[3 * prim + 2];
-                    out.tris.push_back(make_float4(p0[0], p0[1], p0[2], u2f(prim)));
-                    out.tris.push_back(make_float4(p1[0] - p0[0], p1[1] - p0[1], p1[2] - p0[2], 0.f));
-                    out.tris.push_back(make_float4(p2[0] - p0[0], p2[1] - p0[1], p2[2] - p0[2], 0.f));
-                    out.triPrim.push_back(prim);
+                    out.tris[3 * slot + 0] = make_float4(p0[0], p0[1], p0[2], u2f(prim));
+                    out.tris[3 * slot + 1] = make_float4(p1[0] - p0[0], p1[1] - p0[1], p1[2] - p0[2], 0.f);
+                    out.tris[3 * slot + 2] = make_float4(p2[0] - p0[0], p2[1] - p0[1], p2[2] - p0[2], 0.f);
                 }
+                triCount += kk.count;
             }
         }
+        (void)internalCount;
         w0[3] |= imask << 24;
-        for (uint32_t i = 0; i < internalCount; ++i)
-            out.nodes.push_back(CwbvhNode{});
-
+        CwbvhNode node{};
         node.w[0] = make_uint4(w0[0], w0[1], w0[2], w0[3]);
-        node.w[1] = make_uint4(childBase, triBase, meta[0], meta[1]);
+        node.w[1] = make_uint4(rec.childBase, rec.triBase, meta[0], meta[1]);
         node.w[2] = make_uint4(q[0][0], q[0][1], q[1][0], q[1][1]);
         node.w[3] = make_uint4(q[2][0], q[2][1], q[3][0], q[3][1]);
         node.w[4] = make_uint4(q[4][0], q[4][1], q[5][0], q[5][1]);
-        out.nodes[task.wide] = node;
-    }
+        out.nodes[rec.wide] = node;
+    };
+    const unsigned hw = std::max(1u, std::thread::hardware_concurrency());
+    const unsigned workers = recs.size() > 4096 ? hw : 1u;
+    std::atomic<size_t> next{0};
+    auto run = [&] {
+        constexpr size_t kChunk = 256;
+        for (size_t b0 = next.fetch_add(kChunk); b0 < recs.size(); b0 = next.fetch_add(kChunk))
+            for (size_t i = b0; i < std::min(recs.size(), b0 + kChunk); ++i)
+                encode(recs[i]);
+    };
+    std::vector<std::thread> pool;
+    for (unsigned w = 1; w < workers; ++w)
+        pool.emplace_back(run);
+    run();
+    for (std::thread& t : pool)
+        t.join();
     return out;
 }
-
 } // namespace tr
