@@ -246,20 +246,22 @@ __device__ __forceinline__ void primary_ray(const FrameView& f, const Camera& ca
     }
 }
 
-// Work item i of a launch that makes its camera rays -> the path it traces:
-// pixels taken in 8 x 4 tiles, samples in order, so that the rays a warp starts
-// leave the camera through one compact tile. A permutation of [0, W*H*ms) when
-// the film is a whole number of tiles; otherwise the identity. The order in which
-// paths are traced changes no path's result (radiance and random numbers are
-// keyed by the path index).
-constexpr bool kTiledCameraOrder = true;
+// Work item i of a launch that makes its camera rays -> the path it traces: the
+// samples of a pixel are consecutive, and the pixels are taken in 8 x 4 tiles,
+// so that a warp starts the nearly identical camera rays of one or two pixels
+// (its 32 lanes hold 32 / multi_sample pixels) and the rest of the frame keeps
+// that coherence: their hits, shadow rays and bounce rays sit together in the
+// queues. A permutation of [0, W*H*ms) when the film is a whole number of tiles;
+// otherwise the identity. The order in which paths are traced changes no path's
+// result (radiance and random numbers are keyed by the path index).
 __device__ __forceinline__ uint32_t camera_order(const FrameView& f, uint32_t i)
 {
     const uint32_t W = f.resX, H = f.resY;
-    if (!kTiledCameraOrder || (W & 7u) || (H & 3u))
+    if ((W & 7u) || (H & 3u))
         return i;
     const uint32_t wh = W * H;
-    const uint32_t sample = i / wh, r = i - sample * wh;
+    const uint32_t ms = f.pathCount / wh;
+    const uint32_t sample = i % ms, r = i / ms;
     const uint32_t tile = r >> 5, within = r & 31u;
     const uint32_t tilesX = W >> 3;
     const uint32_t ty = tile / tilesX, tx = tile - ty * tilesX;
