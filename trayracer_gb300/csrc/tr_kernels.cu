@@ -268,6 +268,16 @@ __device__ __forceinline__ uint32_t camera_order(const FrameView& f, uint32_t i)
     return sample * wh + ((ty << 2) | (within >> 3)) * W + ((tx << 3) | (within & 7u));
 }
 
+// The same for a batched wave: within each segment (one item's samples in the
+// wave) the samples of a pixel are consecutive.
+__device__ __forceinline__ uint32_t batch_camera_order(const FrameView& f, uint32_t i)
+{
+    const BatchSegment sg = f.segments[batch_segment(f, i)];
+    const uint32_t rel = i - sg.pathBase;
+    const uint32_t pixel = rel / sg.samples, sample = rel - pixel * sg.samples;
+    return sg.pathBase + sample * sg.pixels + pixel;
+}
+
 template <bool REF, bool BATCH>
 __global__ void __launch_bounds__(256) generate_kernel(FrameView f, Camera cam, Settings st)
 {
@@ -369,7 +379,7 @@ __global__ void __launch_bounds__(128, 8) extend_kernel(SceneView s, FrameView f
                     if (PRIMARY) {
                         float3 O, D;
                         float T;
-                        const uint32_t pathIx = BATCH ? i : camera_order(f, i);
+                        const uint32_t pathIx = BATCH ? batch_camera_order(f, i) : camera_order(f, i);
                         primary_ray<false, BATCH>(f, cam, st, pathIx, sc, O, D, T);
                         O4 = f4(O, u2f(pack_path(pathIx, 0)));
                         D4 = f4(D, 0.f);
