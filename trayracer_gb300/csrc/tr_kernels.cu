@@ -251,17 +251,17 @@ __device__ __forceinline__ void primary_ray(const FrameView& f, const Camera& ca
 // so that a warp starts the nearly identical camera rays of one or two pixels
 // (its 32 lanes hold 32 / multi_sample pixels) and the rest of the frame keeps
 // that coherence: their hits, shadow rays and bounce rays sit together in the
-// queues. A permutation of [0, W*H*ms) when the film is a whole number of tiles;
-// otherwise the identity. The order in which paths are traced changes no path's
-// result (radiance and random numbers are keyed by the path index).
+// queues. A permutation of [0, W*H*ms); a film that is not a whole number of
+// tiles takes its pixels row by row. The order in which paths are traced changes
+// no path's result (radiance and random numbers are keyed by the path index).
 __device__ __forceinline__ uint32_t camera_order(const FrameView& f, uint32_t i)
 {
     const uint32_t W = f.resX, H = f.resY;
-    if ((W & 7u) || (H & 3u))
-        return i;
     const uint32_t wh = W * H;
     const uint32_t ms = f.pathCount / wh;
     const uint32_t sample = i % ms, r = i / ms;
+    if ((W & 7u) || (H & 3u))
+        return sample * wh + r;
     const uint32_t tile = r >> 5, within = r & 31u;
     const uint32_t tilesX = W >> 3;
     const uint32_t ty = tile / tilesX, tx = tile - ty * tilesX;
