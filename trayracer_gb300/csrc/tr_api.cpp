@@ -1035,7 +1035,7 @@ tr_status tr_autotune(void* ctx, void* stream, uint32_t flags, tr_tune_report* r
         }
         return TR_OK;
     };
-    const uint32_t refills[] = {12, 16, 20, 24, 28, 32};
+    const uint32_t refills[] = {6, 8, 10, 12, 16, 20, 24, 28, 32};
     for (uint32_t v : refills) {
         tr_tuning t = best;
         t.refill_below = v;
