@@ -1,6 +1,7 @@
 """Scene files (SceneFile::Load, Tracer/FileIO/SceneFile.cpp) and the model / texture cache formats
-(ModelFile.cpp, TextureFile.cpp, BinaryFile.inl) read by the library into a two-level scene. Synthetic
-scene files only: the reference's own scene files name models that are not present."""
+(ModelFile.cpp, TextureFile.cpp, BinaryFile.inl) read by the library into a two-level scene. Scenes
+are rendered from synthetic scene files; the reference's own scene files, where its sources are
+present, are only parsed (the models they name are not present)."""
 import json
 import struct
 from pathlib import Path
