@@ -368,19 +368,13 @@ TR_HD bool node_step(Traversal& t, uint2* stack, const CwbvhNode* __restrict__ n
 }
 
 // Tests the triangles of a leaf group. Returns 2 when an any-hit ray found
-// its hit, 1 when a closer hit was recorded, 0 otherwise.
-template <bool ANY, bool COUNT>
+// its hit, 1 when a closer hit was recorded, 0 otherwise. PAIR (closest hit
+// only) fetches two triangles before testing either.
+template <bool ANY, bool COUNT, bool PAIR = false>
 TR_HD int leaf_triangles(Traversal& t, uint2 tris, const SceneView& s, TraversalCounts* cnt)
 {
     int found = 0;
-    while (tris.y != 0u) {
-        const uint32_t k = ffs32(tris.y) - 1u;
-        tris.y &= tris.y - 1u;
-        const uint32_t slot = tris.x + k;
-        const float4* tp = s.bvhTris + 3u * slot;
-        const float4 a = ldg(tp + 0);
-        const float4 b = ldg(tp + 1);
-        const float4 c = ldg(tp + 2);
+    auto test = [&](uint32_t slot, const float4& a, const float4& b, const float4& c) -> bool {
         if (COUNT)
             cnt->tris++;
         float tt, uu, vv;
@@ -388,7 +382,7 @@ TR_HD int leaf_triangles(Traversal& t, uint2 tris, const SceneView& s, Traversal
             if (ANY) {
                 t.tmax = tt;
                 t.hitSlot = slot;
-                return 2;
+                return true;
             }
             if (tt < t.tmax || t.hitSlot == 0xffffffffu) {
                 t.tmax = tt;
@@ -398,6 +392,37 @@ TR_HD int leaf_triangles(Traversal& t, uint2 tris, const SceneView& s, Traversal
                 found = 1;
             }
         }
+        return false;
+    };
+    if (ANY || !PAIR) {
+        // one triangle at a time (any hit: a second fetch in flight costs the
+        // shadow kernel registers and occupancy, and the first hit ends the ray;
+        // two-level traversal: it would spill)
+        while (tris.y != 0u) {
+            const uint32_t k = ffs32(tris.y) - 1u;
+            tris.y &= tris.y - 1u;
+            const float4* tp = s.bvhTris + 3u * (tris.x + k);
+            if (test(tris.x + k, ldg(tp + 0), ldg(tp + 1), ldg(tp + 2)))
+                return 2;
+        }
+        return found;
+    }
+    // closest hit: two triangles per iteration, both fetched before either is
+    // tested (the second fetch repeats the first when only one is left); tested
+    // in bit order, so the result is that of the one-at-a-time loop
+    while (tris.y != 0u) {
+        const uint32_t k0 = ffs32(tris.y) - 1u;
+        tris.y &= tris.y - 1u;
+        const bool two = tris.y != 0u;
+        const uint32_t k1 = two ? ffs32(tris.y) - 1u : k0;
+        tris.y &= tris.y - 1u;
+        const float4* p0 = s.bvhTris + 3u * (tris.x + k0);
+        const float4* p1 = s.bvhTris + 3u * (tris.x + k1);
+        const float4 a0 = ldg(p0 + 0), b0 = ldg(p0 + 1), c0 = ldg(p0 + 2);
+        const float4 a1 = ldg(p1 + 0), b1 = ldg(p1 + 1), c1 = ldg(p1 + 2);
+        test(tris.x + k0, a0, b0, c0);
+        if (two)
+            test(tris.x + k1, a1, b1, c1);
     }
     return found;
 }
@@ -412,7 +437,7 @@ TR_HD bool traversal_step(Traversal& t, uint2* stack, const SceneView& s, Traver
     uint2 tris;
     if (!node_step<COUNT>(t, stack, s.nodes, cnt, tris))
         return true;
-    if (leaf_triangles<ANY, COUNT>(t, tris, s, cnt) == 2)
+    if (leaf_triangles<ANY, COUNT, !ANY>(t, tris, s, cnt) == 2)
         return true;
     if (t.group.y <= 0x00ffffffu) {
         if (t.sp == 0)
