@@ -39,6 +39,16 @@ __device__ __forceinline__ float h2f(uint16_t h) { return __half2float(__ushort_
 
 __device__ __forceinline__ uint32_t lane_id() { return threadIdx.x & 31u; }
 
+// 16-byte asynchronous global -> shared copy (L2 only), its commit and the wait
+// for all of this thread's committed copies.
+__device__ __forceinline__ void cp_async16(void* smem, const void* gmem)
+{
+    const uint32_t a = static_cast<uint32_t>(__cvta_generic_to_shared(smem));
+    asm volatile("cp.async.cg.shared.global [%0], [%1], 16;" ::"r"(a), "l"(gmem) : "memory");
+}
+__device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commit_group;" ::: "memory"); }
+__device__ __forceinline__ void cp_async_wait_all() { asm volatile("cp.async.wait_group 0;" ::: "memory"); }
+
 // Appends the lanes with pred set to a queue; one atomic per warp.
 __device__ __forceinline__ uint32_t warp_append(uint32_t* counter, bool pred)
 {
@@ -833,17 +843,39 @@ __global__ void __launch_bounds__(128) shade_kernel(SceneView s, FrameView f, Se
     const uint32_t lane = lane_id();
     const uint32_t warpGlobal = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
     const uint32_t warpStride = (gridDim.x * blockDim.x) >> 5;
+    // The next item's path state and hit record are copied (cp.async) while
+    // this item is shaded. Two buffers: the one refilled was read an iteration
+    // earlier, by loads whose values that iteration's shading consumed, so the
+    // copy cannot overtake them.
+    __shared__ float4 stage[2][4][128];
+    const uint32_t tid = threadIdx.x;
+    uint32_t buf = 0;
+    auto fetch = [&](uint32_t k, uint32_t b) {
+        const uint32_t i = f.hitOrder ? __ldcs(f.hitOrder + k) : k;
+        cp_async16(&stage[b][0][tid], in + i);
+        cp_async16(&stage[b][1][tid], in + i + cap);
+        cp_async16(&stage[b][2][tid], in + i + 2 * cap);
+        cp_async16(&stage[b][3][tid], f.hits + i);
+        cp_async_commit();
+    };
+    if (warpGlobal * 32u + lane < count)
+        fetch(warpGlobal * 32u + lane, 0u);
 
     for (uint32_t base = warpGlobal * 32u; base < count; base += warpStride * 32u) {
         const uint32_t k = base + lane;
         bool wantExt = false, wantShadow = false;
         float4 ext[3], sh[3];
         if (k < count) {
-            const uint32_t i = f.hitOrder ? __ldcs(f.hitOrder + k) : k;
-            const float4 O4 = __ldcs(in + i);
-            const float4 D4 = __ldcs(in + i + cap);
-            const float4 T4 = __ldcs(in + i + 2 * cap);
-            const uint4 hd = __ldcs(f.hits + i);
+            cp_async_wait_all();
+            const float4 O4 = stage[buf][0][tid];
+            const float4 D4 = stage[buf][1][tid];
+            const float4 T4 = stage[buf][2][tid];
+            const float4 h = stage[buf][3][tid];
+            const uint4 hd = make_uint4(__float_as_uint(h.x), __float_as_uint(h.y), __float_as_uint(h.z),
+                                        __float_as_uint(h.w));
+            buf ^= 1u;
+            if (k + warpStride * 32u < count)
+                fetch(k + warpStride * 32u, buf);
             const uint32_t pathIx = path_ix(__float_as_uint(O4.w));
             if (BATCH) {
                 const BatchSegment sg = f.segments[batch_segment(f, pathIx)];
