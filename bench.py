@@ -53,7 +53,7 @@ def parse():
     p.add_argument("--height", type=int, default=1080)
     p.add_argument("--spp", type=int, default=64)
     p.add_argument("--ms", type=int, default=16, help="samples per pixel per wavefront frame")
-    p.add_argument("--cpu-seconds", type=float, default=12.0, help="target CPU work of the CPU baseline sample")
+    p.add_argument("--cpu-seconds", type=float, default=20.0, help="target CPU work of the CPU baseline sample")
     p.add_argument("--no-cpu-baseline", action="store_true")
     p.add_argument("--profile", action="store_true",
                    help="render one eager frame of the workload and exit (the case the ncu captures use)")
