@@ -66,6 +66,8 @@ def parse():
     p.add_argument("--rmse-spp", type=int, default=1024,
                    help="plain workload: also compare a render of this many spp against the FP64 oracle")
     p.add_argument("--batch-count", type=int, default=64)
+    p.add_argument("--no-extra", action="store_true",
+                   help="plain workload: skip the batched and differentiation measurements after the timed region")
     p.add_argument("--wave-paths", type=int, default=0, help="batched waves: paths per wave (0: library default)")
     return p.parse_args()
 
@@ -177,7 +179,71 @@ def cpu_baseline(scene, args, seconds: float, oracle=None):
         "sample": f"{n} pixels x {4 * frames} spp of the {scene.width}x{scene.height} image (rows from the "
                   f"centre), 8 bounces, {rays} rays in {dt:.1f} s",
         "samples_per_s": n * 4 * frames / dt,
+        "traversal": "the oracle's median-split binary BVH (up to 4 triangles per leaf), not the GPU's "
+                     "SAH-built 8-wide BVH",
     }
+
+
+def band_accuracy(r, scene, args, frames, sptr, rows=16, spp_long=1024, rows_long=2):
+    """Relative image RMSE of the step's 64-spp image on `rows` image rows spread over the frame,
+    against the FP64 oracle and against the fp32 oracle (same sample keys on all sides), the fp32
+    oracle against the FP64 one, and the fraction of the last frame's paths whose radiance is
+    within 1e-4 of the fp32 oracle's. The difference to FP64 is fp32 against fp64 arithmetic:
+    it shows as noise where a path's fp32 and fp64 continuations part (near-specular lobes,
+    Russian roulette and lobe choices on a last-bit difference) and falls as 1/sqrt(spp). Then
+    the same against FP64 at spp_long samples per pixel on rows_long rows."""
+    import trayracer_gb300 as tr
+    from oracle import Oracle
+
+    W, H, ms = scene.width, scene.height, args.ms
+    st = tr.settings_for(scene, multi_sample=ms)
+    threads = os.cpu_count() or 1
+    orc = Oracle(scene)
+    img = r.ColorBuffer()
+    buf = r.Buffers()
+    ys = [(k * H) // rows + H // (2 * rows) for k in range(rows)]
+    g_img, o32, o64, ok = [], [], [], []
+    for y in ys:
+        first = y * W
+        a32, p32, _ = orc.render(scene.camera, st, W, H, frames=frames, first_pixel=first, pixel_count=W,
+                                 want_paths=True, threads=threads)
+        a64, _, _ = orc.render(scene.camera, st, W, H, frames=frames, first_pixel=first, pixel_count=W,
+                               use_double=True, threads=threads)
+        rad = np.stack([r.read_device(buf["radiance"] + 16 * (first + smp * W * H), np.float32, 4 * W)
+                        .reshape(W, 4) for smp in range(ms)])[..., :3].astype(np.float64)
+        p = p32[..., :3]
+        ok.append((np.abs(rad - p) <= 1e-4 * np.maximum(1.0, np.abs(p)) + 1e-6).all(-1).ravel())
+        g_img.append(img.reshape(-1, 4)[first:first + W, :3].astype(np.float64))
+        o32.append(a32[:, :3] / a32[:, 3:4])
+        o64.append(a64[:, :3] / a64[:, 3:4])
+    g, i32, i64 = (np.concatenate(x) for x in (g_img, o32, o64))
+
+    def rel(a, b):
+        return float(np.sqrt(np.mean((a - b) ** 2)) / max(1e-12, np.sqrt(np.mean(b ** 2))))
+
+    out = {
+        "rows": ys,
+        "spp": frames * ms,
+        "rmse_gpu_vs_fp64": rel(g, i64),
+        "rmse_gpu_vs_fp32_oracle": rel(g, i32),
+        "rmse_fp32_oracle_vs_fp64": rel(i32, i64),
+        "paths_compared": int(sum(x.size for x in ok)),
+        "paths_within_1e-4_of_fp32_oracle": float(np.concatenate(ok).mean()),
+    }
+    if spp_long > frames * ms:
+        long_frames = spp_long // ms
+        r.Reset()
+        for _ in range(long_frames):
+            r.RenderFrame(stream=sptr, use_graph=True)
+        img = r.ColorBuffer()
+        band0 = (H // 2) * W
+        nb = rows_long * W
+        a64, _, _ = orc.render(scene.camera, st, W, H, frames=long_frames, first_pixel=band0, pixel_count=nb,
+                               use_double=True, threads=threads)
+        out[f"rmse_gpu_vs_fp64_spp_{long_frames * ms}"] = rel(img.reshape(-1, 4)[band0:band0 + nb, :3]
+                                                              .astype(np.float64), a64[:, :3] / a64[:, 3:4])
+        out["rows_long"] = list(range(H // 2, H // 2 + rows_long))
+    return out
 
 
 def run_reference(args):
@@ -215,7 +281,7 @@ def run_reference(args):
         "data": "synthetic",
         "config": config_dict(args, scene),
         "cpu_baseline": {"value": round(value, 4), "unit": "Mrays/s", "cores": last["cores"], "kind": "port",
-                         "sample": last["sample"]},
+                         "sample": last["sample"], "traversal": last["traversal"]},
         "e2e": {"value": round(value, 4), "unit": "Mrays/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
         "note": "the reference's own code path is OptiX/RT-core + Windows only; the timed CPU implementation is "
                 "the restated reference path (oracle/), each step a bounded pixel sample",
@@ -237,7 +303,7 @@ def config_dict(args, scene):
     }
 
 
-def run_batch(args):
+def measure_batch(args, steps, warmup, with_ms1=True):
     """The batching mix: 64 seeded sphere scenes (1k-500k triangles, 128^2-1024^2, 4/16/64 spp,
     1-16 lights, 6 bounces, RR from bounce 3) rendered by one wavefront (all waves in one CUDA
     graph) against the same scenes rendered one after the other through tr_render_frame
@@ -264,15 +330,15 @@ def run_batch(args):
     info = b.Info()
     if args.profile:
         b.Render(st, stream=sptr, use_graph=False)
-        print(json.dumps({"batch": b.Statistics(), "info": b.Info()}))
+        out = {"batch": b.Statistics(), "info": b.Info()}
         b.close()
-        return
-    for _ in range(args.warmup):
+        return out
+    for _ in range(warmup):
         b.Render(st, stream=sptr)
     torch.cuda.synchronize()
     times = []
     with ClockSampler(0) as clocks:
-        for _ in range(args.steps):
+        for _ in range(steps):
             flush.fill_(1.0)
             e0 = torch.cuda.Event(enable_timing=True)
             e1 = torch.cuda.Event(enable_timing=True)
@@ -295,36 +361,65 @@ def run_batch(args):
 
     def per_scene(max_ms):
         total_ms, total_rays, n_launch = 0.0, 0, 0
-        for s in scenes:
-            ms = min(s.spp, max_ms)
-            frames = s.spp // ms
-            r.UpdateScene(s)
-            r.SetCamera(s.camera)
-            r.Resize((s.width, s.height))
-            r.SetSettings(KernelSettings(**{**st.__dict__, "multiSample": ms}))
-            elapsed = None
-            for _ in range(2):  # the first pass allocates and captures the graph
+        with ClockSampler(0) as pclocks:
+            for s in scenes:
+                ms = min(s.spp, max_ms)
+                frames = s.spp // ms
+                r.UpdateScene(s)
+                r.SetCamera(s.camera)
+                r.Resize((s.width, s.height))
+                r.SetSettings(KernelSettings(**{**st.__dict__, "multiSample": ms}))
+                elapsed = None
+                for _ in range(2):  # the first pass allocates and captures the graph
+                    r.Reset()
+                    flush.fill_(1.0)
+                    e0 = torch.cuda.Event(enable_timing=True)
+                    e1 = torch.cuda.Event(enable_timing=True)
+                    e0.record(stream)
+                    for _ in range(frames):
+                        r.RenderFrame(stream=sptr, use_graph=True)
+                    e1.record(stream)
+                    e1.synchronize()
+                    elapsed = e0.elapsed_time(e1)
+                total_ms += elapsed
                 r.Reset()
-                flush.fill_(1.0)
-                e0 = torch.cuda.Event(enable_timing=True)
-                e1 = torch.cuda.Event(enable_timing=True)
-                e0.record(stream)
                 for _ in range(frames):
-                    r.RenderFrame(stream=sptr, use_graph=True)
-                e1.record(stream)
-                e1.synchronize()
-                elapsed = e0.elapsed_time(e1)
-            total_ms += elapsed
-            r.Reset()
-            for _ in range(frames):
-                r.RenderFrame(stream=sptr, use_graph=False)
-                total_rays += r.Statistics()["path_count"]
-            n_launch += frames * (3 * st.maxDepth + 3)
-        return total_ms, total_rays, n_launch
+                    r.RenderFrame(stream=sptr, use_graph=False)
+                    total_rays += r.Statistics()["path_count"]
+                n_launch += frames * (3 * st.maxDepth + 3)
+        return total_ms, total_rays, n_launch, pclocks.summary()
 
-    plain_ms, plain_rays, launches = per_scene(16)
-    ms1_ms, ms1_rays, ms1_launches = per_scene(1)
+    plain_ms, plain_rays, launches, plain_clocks = per_scene(16)
+    out = {
+        "samples": samples,
+        "batch_ms": batch_ms,
+        "batch_rays": int(rays),
+        "info": info,
+        "clocks": clocks.summary(),
+        "per_scene": {"ms": round(plain_ms, 3), "samples_per_s": round(samples / (plain_ms / 1e3), 1),
+                      "mrays_per_s": round(plain_rays / (plain_ms / 1e3) / 1e6, 1), "gpu_launches": launches,
+                      "clocks": plain_clocks},
+        "rays_per_scene": int(plain_rays),
+        "speedup_vs_per_scene": round(plain_ms / batch_ms, 3),
+        "scene_generation_s": round(gen_s, 2),
+        "batch_build_s": round(build_s, 2),
+    }
+    if with_ms1:
+        ms1_ms, ms1_rays, ms1_launches, ms1_clocks = per_scene(1)
+        out["per_scene_ms1"] = {"ms": round(ms1_ms, 3), "samples_per_s": round(samples / (ms1_ms / 1e3), 1),
+                                "mrays_per_s": round(ms1_rays / (ms1_ms / 1e3) / 1e6, 1),
+                                "gpu_launches": ms1_launches, "clocks": ms1_clocks}
+        out["speedup_vs_per_scene_ms1"] = round(ms1_ms / batch_ms, 3)
     r.close()
+    return out
+
+
+def run_batch(args):
+    m = measure_batch(args, args.steps, args.warmup)
+    if args.profile:
+        print(json.dumps(m))
+        return
+    info, samples, batch_ms = m["info"], m["samples"], m["batch_ms"]
     line = {
         "metric": "samples/s",
         "value": round(samples / (batch_ms / 1e3), 1),
@@ -338,31 +433,38 @@ def run_batch(args):
         "vs_baseline": None,
         "dtype": "f32",
         "data": "synthetic",
-        "config": {"workload": f"{len(scenes)} sphere scenes, {info['triangle_count']} tris, "
+        "config": {"workload": f"{args.batch_count} sphere scenes, {info['triangle_count']} tris, "
                                f"{info['pixel_count']} pixels, {samples} samples, 6 bounces, RR from 3",
                    "waves": info["wave_count"], "wave_paths": info["wave_paths"],
                    "l2": "flushed before each timed render (256 MiB write)"},
-        "mrays_per_s": round(rays / (batch_ms / 1e3) / 1e6, 1),
+        "mrays_per_s": round(m["batch_rays"] / (batch_ms / 1e3) / 1e6, 1),
         "gpu_launches": info["launches"],
-        "per_scene": {"ms": round(plain_ms, 3), "samples_per_s": round(samples / (plain_ms / 1e3), 1),
-                      "mrays_per_s": round(plain_rays / (plain_ms / 1e3) / 1e6, 1), "gpu_launches": launches},
-        "per_scene_ms1": {"ms": round(ms1_ms, 3), "samples_per_s": round(samples / (ms1_ms / 1e3), 1),
-                          "mrays_per_s": round(ms1_rays / (ms1_ms / 1e3) / 1e6, 1), "gpu_launches": ms1_launches},
-        "speedup_vs_per_scene": round(plain_ms / batch_ms, 3),
-        "speedup_vs_per_scene_ms1": round(ms1_ms / batch_ms, 3),
-        "rays_batch": int(rays),
-        "rays_per_scene": int(plain_rays),
-        "scene_generation_s": round(gen_s, 2),
-        "batch_build_s": round(build_s, 2),
-        "clocks": clocks.summary(),
+        **{k: m[k] for k in ("per_scene", "per_scene_ms1", "speedup_vs_per_scene", "speedup_vs_per_scene_ms1",
+                             "rays_per_scene", "scene_generation_s", "batch_build_s", "clocks")},
+        "rays_batch": m["batch_rays"],
     }
     print(json.dumps(line), flush=True)
 
 
-def run_adjoint(args):
-    """Differentiation scene (the Cornell box with Disney walls, 512^2, 32 spp, 6 bounces, no RR):
-    one forward frame (graph) and its path-replay adjoint for the L2 loss against a black target
-    (so every path that carried radiance is replayed); reports both times and their ratio."""
+def perturbed_materials(materials, seed=2, sigma=0.05):
+    """The differentiation target's parameters: every Disney parameter (base colour, roughness,
+    metallic, specular) of every material + N(0, sigma), clipped to [0, 1]."""
+    rng = np.random.default_rng(seed)
+    m = materials.copy()
+    for key, shape in (("diffuse", (3,)), ("roughness", ()), ("metallic", ()), ("specular", ())):
+        v = m[key].astype(np.float64) + rng.normal(0.0, sigma, m[key].shape)
+        m[key] = np.clip(v, 0.0, 1.0).astype(np.float32)
+    emissive = materials["emissive"].max(axis=-1) > 0
+    m[emissive] = materials[emissive]  # lights keep their colour; their radiance is a parameter, not perturbed
+    return m
+
+
+def measure_adjoint(args, steps, warmup):
+    """Differentiation: the Cornell box with Disney walls, 512^2, 32 spp, 6 bounces, no RR. One
+    forward frame (graph replay) and the path-replay adjoint of the L2 loss 0.5 |img - target|^2
+    against a target rendered with the Disney parameters perturbed by N(0, 0.05) (clipped to
+    [0, 1]); gradients of all 9 parameters of the 8 materials. CUDA events on the launch stream,
+    L2 flushed before the forward frame and before the adjoint."""
     import torch
 
     import trayracer_gb300 as tr
@@ -373,65 +475,87 @@ def run_adjoint(args):
     sptr = stream.cuda_stream
     flush = torch.empty(256 * 1024 * 1024 // 4, dtype=torch.float32, device="cuda")
     W = H = 512
+    spp = 32
     scene = tr.cornell_box(width=W, height=H, wall_closure=tr.TR_CLOSURE_DISNEY, max_depth=6)
-    st = KernelSettings(multiSample=32, maxDepth=6, seed=1, rrStart=1 << 30)
+    st = KernelSettings(multiSample=spp, maxDepth=6, seed=1, rrStart=1 << 30)
     r = tr.DeviceRenderer(0)
     r.UpdateScene(scene)
     r.SetCamera(scene.camera)
     r.Resize((W, H))
+    # the target: perturbed parameters, another seed
+    r.UpdateMaterials(perturbed_materials(scene.materials))
+    r.SetSettings(KernelSettings(**{**st.__dict__, "seed": 7}))
+    r.RenderFrame(stream=sptr, use_graph=False)
+    target = torch.from_numpy(r.ColorBuffer().copy()).cuda()
+    r.UpdateMaterials(scene.materials)
     r.SetSettings(st)
-    target = torch.zeros((H, W, 4), dtype=torch.float32, device="cuda")
     grad = torch.zeros((scene.materials.shape[0], 9), dtype=torch.float32, device="cuda")
     if args.profile:
         r.RenderFrame(stream=sptr, use_graph=False)
         pg = torch.from_numpy(r.ColorBuffer()).cuda() - target  # dL/dcolor of 0.5 |img - target|^2
-        r.AdjointFrame(pg.data_ptr(), 1.0 / 32, grad.data_ptr(), stream=sptr)
+        r.AdjointFrame(pg.data_ptr(), 1.0 / spp, grad.data_ptr(), stream=sptr)
         torch.cuda.synchronize()
-        print(json.dumps({"grad_norm": float(grad.norm())}))
         r.close()
-        return
+        return {"grad_norm": float(grad.norm())}
     fwd, adj = [], []
-    for i in range(args.warmup + args.steps):
-        flush.fill_(1.0)
-        e0, e1, e2 = (torch.cuda.Event(enable_timing=True) for _ in range(3))
-        r.Reset()
-        e0.record(stream)
-        r.RenderFrame(stream=sptr, use_graph=True)
-        e1.record(stream)
-        # dL/dcolor of 0.5 * |img - target|^2 over the image, then the adjoint of that frame
-        img = torch.from_numpy(r.ColorBuffer()).cuda() if i == 0 else img
-        pg = img - target
-        flush.fill_(1.0)
-        e1b = torch.cuda.Event(enable_timing=True)
-        e1b.record(stream)
-        r.AdjointFrame(pg.data_ptr(), 1.0 / 32, grad.data_ptr(), stream=sptr)
-        e2.record(stream)
-        e2.synchronize()
-        if i >= args.warmup:
-            fwd.append(e0.elapsed_time(e1))
-            adj.append(e1b.elapsed_time(e2))
+    img = None
+    with ClockSampler(0) as clocks:
+        for i in range(warmup + steps):
+            flush.fill_(1.0)
+            e0, e1, e2, e3 = (torch.cuda.Event(enable_timing=True) for _ in range(4))
+            r.Reset()
+            e0.record(stream)
+            r.RenderFrame(stream=sptr, use_graph=True)
+            e1.record(stream)
+            if img is None:
+                img = torch.from_numpy(r.ColorBuffer()).cuda()
+                pg = img - target
+            flush.fill_(1.0)
+            e2.record(stream)
+            r.AdjointFrame(pg.data_ptr(), 1.0 / spp, grad.data_ptr(), stream=sptr)
+            e3.record(stream)
+            e3.synchronize()
+            if i >= warmup:
+                fwd.append(e0.elapsed_time(e1))
+                adj.append(e2.elapsed_time(e3))
     stats = r.Statistics()
     r.close()
     f_ms, a_ms = float(statistics.median(fwd)), float(statistics.median(adj))
+    return {
+        "forward_ms": round(f_ms, 3),
+        "adjoint_ms": round(a_ms, 3),
+        "adjoint_over_forward": round(a_ms / f_ms, 3),
+        "forward_mrays_per_s": round(stats["path_count"] / (f_ms / 1e3) / 1e6, 1),
+        "samples_per_s": round(W * H * spp / (f_ms / 1e3), 1),
+        "adjoint_samples_per_s": round(W * H * spp / (a_ms / 1e3), 1),
+        "gradient_norm": float(grad.norm()),
+        "clocks": clocks.summary(),
+    }
+
+
+def run_adjoint(args):
+    m = measure_adjoint(args, args.steps, args.warmup)
+    if args.profile:
+        print(json.dumps(m))
+        return
     line = {
         "metric": "adjoint/forward time",
-        "value": round(a_ms / f_ms, 3),
+        "value": m["adjoint_over_forward"],
         "unit": "ratio",
         "n_gpus": 1,
         "steps": args.steps,
         "warmup": args.warmup,
-        "ms_per_step": round(f_ms + a_ms, 3),
+        "ms_per_step": round(m["forward_ms"] + m["adjoint_ms"], 3),
         "higher_is_better": False,
         "scaling": "weak",
         "vs_baseline": None,
         "dtype": "f32",
         "data": "synthetic",
-        "config": {"workload": "Cornell box with Disney walls, 512x512, 32 spp, 6 bounces, no RR; "
-                               "gradients of 9 parameters for each of the 8 materials",
+        "config": {"workload": "Cornell box with Disney walls, 512x512, 32 spp, 6 bounces, no RR; L2 loss "
+                               "against a target rendered with the Disney parameters + N(0, 0.05); gradients of "
+                               "9 parameters for each of the 8 materials",
                    "l2": "flushed before the forward frame and before the adjoint (256 MiB write)"},
-        "forward_ms": round(f_ms, 3),
-        "adjoint_ms": round(a_ms, 3),
-        "forward_mrays_per_s": round(stats["path_count"] / (f_ms / 1e3) / 1e6, 1),
+        **m,
     }
     print(json.dumps(line), flush=True)
 
@@ -665,15 +789,18 @@ def main():
     launches = frames_per_step * st.maxDepth
     achieved = ext_bytes / ext_s / 1e9
     compulsory = (ext_rays * EXTEND_BYTES_PER_RAY + hit_rays * EXTEND_BYTES_PER_HIT) / ext_s / 1e9
-    traffic = None
-    # DRAM bytes per extend ray from the ncu capture summarised in profiles/ (a text line
-    # "dram_bytes_per_extend_ray: <value>"), scaled to this run's average launch
-    prof = ROOT / "profiles" / "extend_kernel_heightfield_1920x1080_traffic.md"
+    # DRAM bytes per extend ray measured by ncu on the 960x540 case of this workload (4 spp per
+    # frame, a few extend launches captured), scaled to this run's average launch by its extend
+    # rays; labelled with its source in the line, not measured in this run
+    traffic, traffic_source = None, None
+    prof = ROOT / "profiles" / "extend_kernel_heightfield_960x540_traffic.txt"
     if prof.exists():
         for line in prof.read_text().splitlines():
             if line.strip().startswith("dram_bytes_per_extend_ray:"):
                 try:
                     traffic = float(line.split(":", 1)[1]) * ext_rays / launches
+                    traffic_source = ("ncu dram__bytes_read.sum + dram__bytes_write.sum of the 960x540 case, "
+                                      "per extend ray, scaled to this run's extend rays per launch")
                 except ValueError:
                     traffic = None
 
@@ -697,49 +824,41 @@ def main():
         stage_roofline[k] = {"bytes_per_step": int(b), "achieved_gbs": None if gbs is None else round(gbs, 1),
                              "frac": None if gbs is None else round(gbs / peak, 4)}
 
-    # --- image accuracy on a pixel band against the FP64 oracle
-    rmse = None
+    # --- image accuracy on 16 image rows spread over the frame, against the oracle
+    accuracy = None
     cpu = None
     if rank == 0 and not args.no_cpu_baseline:
         try:
+            accuracy = band_accuracy(r, scene, args, frames_per_step, sptr, spp_long=args.rmse_spp)
             from oracle import Oracle
 
-            # Same sample keys on both sides, so the difference is fp32 vs fp64 arithmetic only; it
-            # shows as noise where a path's fp32 and fp64 continuations part (near-specular lobes,
-            # Russian roulette and lobe choices on a last-bit difference) and falls as 1/sqrt(spp).
-            band0 = (scene.height // 2) * scene.width
-            nb = 2 * scene.width
-            orc = Oracle(scene)
-
-            def band_rmse(img, frames, use_double=True):
-                acc, _, _ = orc.render(scene.camera, tr.settings_for(scene, multi_sample=args.ms), scene.width,
-                                       scene.height, frames=frames, first_pixel=band0, pixel_count=nb,
-                                       use_double=use_double, threads=os.cpu_count() or 1)
-                ref = acc[:, :3] / acc[:, 3:4]
-                got = img.reshape(-1, 4)[band0:band0 + nb, :3].astype(np.float64)
-                return float(np.sqrt(np.mean((got - ref) ** 2)) / max(1e-12, np.sqrt(np.mean(ref ** 2))))
-
-            img = r.ColorBuffer()
-            rmse = {"spp_%d" % args.spp: band_rmse(img, frames_per_step)}
-            # the fp32 oracle against the FP64 oracle: the same divergence without the GPU
-            acc32, _, _ = orc.render(scene.camera, tr.settings_for(scene, multi_sample=args.ms), scene.width,
-                                     scene.height, frames=frames_per_step, first_pixel=band0, pixel_count=nb,
-                                     use_double=False, threads=os.cpu_count() or 1)
-            acc64, _, _ = orc.render(scene.camera, tr.settings_for(scene, multi_sample=args.ms), scene.width,
-                                     scene.height, frames=frames_per_step, first_pixel=band0, pixel_count=nb,
-                                     use_double=True, threads=os.cpu_count() or 1)
-            r32, r64 = acc32[:, :3] / acc32[:, 3:4], acc64[:, :3] / acc64[:, 3:4]
-            rmse["fp32_oracle_spp_%d" % args.spp] = float(np.sqrt(np.mean((r32 - r64) ** 2)) /
-                                                          max(1e-12, np.sqrt(np.mean(r64 ** 2))))
-            if args.rmse_spp > args.spp:
-                frames = args.rmse_spp // args.ms
-                r.Reset()
-                for _ in range(frames):
-                    r.RenderFrame(stream=sptr, use_graph=True)
-                rmse["spp_%d" % (frames * args.ms)] = band_rmse(r.ColorBuffer(), frames)
-            cpu = cpu_baseline(scene, args, args.cpu_seconds, orc)
+            cpu = cpu_baseline(scene, args, args.cpu_seconds, Oracle(scene))
         except Exception as e:  # the checker is optional; the GPU numbers stand
             cpu = {"value": None, "unavailable": str(e)}
+
+    # --- the batched and differentiation configurations, measured in the same process after
+    # the plain timed region (their own timed regions, CUDA events, L2 flushed)
+    batch = adjoint = None
+    if rank == 0 and ws == 1 and not args.no_extra:
+        adjoint = measure_adjoint(args, steps=5, warmup=3)
+        m = measure_batch(args, steps=3, warmup=3, with_ms1=False)
+        batch = {
+            "batched_over_per_scene": m["speedup_vs_per_scene"],
+            "batched_ms": round(m["batch_ms"], 3),
+            "per_scene_ms": m["per_scene"]["ms"],
+            "batched_samples_per_s": round(m["samples"] / (m["batch_ms"] / 1e3), 1),
+            "per_scene_samples_per_s": m["per_scene"]["samples_per_s"],
+            "batched_mrays_per_s": round(m["batch_rays"] / (m["batch_ms"] / 1e3) / 1e6, 1),
+            "per_scene_mrays_per_s": m["per_scene"]["mrays_per_s"],
+            "samples": m["samples"],
+            "waves": m["info"]["wave_count"],
+            "gpu_launches": m["info"]["launches"],
+            "workload": f"{args.batch_count} sphere scenes ({m['info']['triangle_count']} tris, "
+                        f"{m['info']['pixel_count']} pixels, 4/16/64 spp, 6 bounces, RR from 3); per scene: "
+                        f"tr_render_frame graph frames at multi_sample min(spp, 16)",
+            "clocks": m["clocks"],
+            "per_scene_clocks": m["per_scene"]["clocks"],
+        }
 
     if rank == 0:
         line = {
@@ -762,7 +881,7 @@ def main():
             "shadow_rays_per_step": int(sh_rays),
             "hit_rays_per_step": int(hit_rays),
             "stage_ms_per_step": {k: round(v, 3) for k, v in stage_ms.items()},
-            "rmse_vs_fp64_band": rmse,  # relative RMSE on 2 image rows, by samples per pixel
+            "accuracy": accuracy,
             "roofline": {
                 "kernel": "extend_kernel (CWBVH closest hit)",
                 "bound": "hbm",
@@ -772,6 +891,7 @@ def main():
                 "unit": "GB/s",
                 "frac": round(achieved / peak, 4),
                 "traffic": traffic,
+                "traffic_source": traffic_source,
                 "bytes_per_launch": int(ext_bytes / launches),
                 "avg_launch_ms": round(stage_ms["extend"] / launches, 4),
                 "compulsory_frac": round(compulsory / peak, 4),
@@ -790,12 +910,13 @@ def main():
                 "d2h_bytes_per_step": scene.width * scene.height * 16,
             },
             # per frame: extend, shade and connect per bounce (and the three kernels of the hit
-            # sort when the tuning turned it on), then finalize and advance (the launch list of
-            # profiles/heightfield_960x540_ms4_launches.md: 26 for 8 bounces)
+            # sort when the tuning turned it on), then finalize and advance: 26 for 8 bounces
             "gpu_launches": args.steps * frames_per_step * ((3 + (3 if r.Tuning().get("sort_hits") else 0))
                                                             * st.maxDepth + 2),
             "scene_upload_s": round(upload_s, 2),
             "tuning": tune,
+            "adjoint": adjoint,
+            "batched": batch,
         }
         print(json.dumps(line), flush=True)
     r.close()

@@ -117,7 +117,10 @@ typedef struct tr_kernel_settings {
     uint32_t rr_start;       /* first path length with Russian roulette (reference: 1); >= max_depth disables */
     uint32_t flags;          /* TR_FLAG_* */
     float max_color;         /* firefly clamp of SafeColor (CudaUtility.h:91); <= 0 selects 10 */
-    uint32_t reserved;
+    uint32_t traversal_step_limit; /* bound on the BVH node visits of one ray's traversal; 0 selects 2^22.
+                                      A ray that runs out ends with the hit found so far and sets
+                                      tr_statistics.device_error (the reference has no bound: OptiX
+                                      traversal is opaque) */
 } tr_kernel_settings;
 
 /* ≙ the camera fields of LaunchParams (Tracer/Common/CommonStructs.h:170-184). */
@@ -245,7 +248,8 @@ typedef struct tr_statistics {
     float connect_time_ms;
     float finalize_time_ms;
     uint32_t sample_count;          /* accumulated samples per pixel */
-    uint32_t device_error;          /* nonzero: a kernel recorded a bounded-loop overrun */
+    uint32_t device_error;          /* nonzero: a kernel recorded a bounded-loop overrun (traversal stack
+                                       depth or traversal_step_limit) since the last tr_reset */
     /* with TR_FLAG_COUNT_TRAVERSAL, summed over the frames since tr_reset */
     uint64_t traversal_extend_nodes;
     uint64_t traversal_extend_tris;
@@ -380,9 +384,17 @@ tr_status tr_adjoint_frame(void* ctx, void* stream, const float* pixel_grad, flo
  * come from the context (set up beforehand; tr_scene_upload allocates). The
  * first call on a device looks up the array's device address (which loads the
  * library's device image there); make that first call before any stream
- * capture. Every call shares the array and rewrites what it must start from:
- * calls that overlap on the GPU (other streams, other threads, other
- * contexts) race. Guide buffers (TR_FLAG_WRITE_AOVS) are not written. */
+ * capture. The address is kept for the life of the process and does not
+ * survive a cudaDeviceReset of that device. Every call shares the array and
+ * rewrites what it must start from: calls that overlap on the GPU (other
+ * streams, other threads, other contexts) race. Guide buffers
+ * (TR_FLAG_WRITE_AOVS) are not written. The path-tracing render mode only
+ * (TR_ERR_INVALID_ARGUMENT after tr_set_render_mode to another mode). The
+ * launch shapes are the context's tuning (tr_set_tuning / tr_autotune) without
+ * the hit sort. tr_get_statistics after this call reports this frame (ray
+ * counts, device_error) from the shared array, so a call that overlaps it
+ * races with that read too. The calling thread's current device is restored
+ * on return. */
 tr_status tr_render_frame_noalloc(void* ctx, void* stream, float* accumulator, float* colors, uint32_t sample_count);
 
 /* ---- render modes ----

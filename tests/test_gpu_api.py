@@ -61,6 +61,40 @@ def test_errors_are_statuses():
     r.close()
 
 
+@pytest.mark.parametrize("use_graph", [False, True])
+def test_traversal_bound_is_a_status_and_clears_on_reset(use_graph):
+    """A traversal that runs out of its node-visit bound ends the ray with the hit found so far
+    and raises the device error word; the call still returns TR_OK, tr_get_statistics reports
+    the error until tr_reset, and the next frames are clean. (The reference exits the process on
+    any CUDA error, Tracer/CUDA/CudaError.cpp:13-25.)"""
+    import dataclasses
+
+    scene = tr.heightfield(n=128, width=64, height=36, spp=2)
+    st = tr.settings_for(scene, multi_sample=2)
+    r = renderer(scene, st)
+    r.RenderFrame(use_graph=use_graph)
+    want = r.ColorBuffer().copy()
+    assert r.Statistics()["device_error"] == 0
+    r.SetSettings(dataclasses.replace(st, traversalStepLimit=2))  # resets the accumulation
+    r.RenderFrame(use_graph=use_graph)
+    s = r.Statistics()
+    assert s["device_error"] != 0
+    assert np.isfinite(r.ColorBuffer()).all()
+    # the per-stage entries run into the same bound
+    r.Reset()
+    assert r.Statistics()["device_error"] == 0
+    r.BeginFrame()
+    r.Generate()
+    r.Extend(0)
+    assert r.Statistics()["device_error"] != 0
+    # back to the default bound: clean frames equal to the first one
+    r.SetSettings(st)
+    assert r.Statistics()["device_error"] == 0
+    r.RenderFrame(use_graph=use_graph)
+    assert r.Statistics()["device_error"] == 0
+    np.testing.assert_array_equal(r.ColorBuffer(), want)
+    r.close()
+
 @pytest.mark.parametrize("reference", [False, True])
 def test_graph_equals_eager_and_is_deterministic(reference):
     scene = tr.heightfield(n=96, width=96, height=54, rr_start=2)

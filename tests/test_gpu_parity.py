@@ -105,8 +105,8 @@ def check_hits(o, O, D, got, eps):
         tg = float(got[i, 3].view(np.float32))
         tw = float(want[i, 3].view(np.float32))
         assert abs(tg - tw) <= 1e-6 * abs(tw), f"ray {i}: gpu {got[i]} oracle {want[i]}"
-        ties = o.ties(O[i], D[i], eps, tw, with_instances=True)
-        assert (int(got[i, 1]), int(got[i, 2])) in ties, f"ray {i}: {got[i]} is no near tie of {want[i]}"
+        near = o.ties(O[i], D[i], eps, tw, with_instances=True)
+        assert (int(got[i, 1]), int(got[i, 2])) in near, f"ray {i}: {got[i]} is no near tie of {want[i]}"
         ties += 1
     return ties
 
@@ -253,6 +253,9 @@ def test_frame_parity_per_path(reference, two_level):
 
 
 def test_image_rmse_against_fp64_oracle():
+    """The GPU image against the FP64 oracle's with the same sample keys: no further from it than
+    the fp32 oracle is (the residual is fp32 against fp64 path divergence, which falls as
+    1/sqrt(spp))."""
     scene = tr.cornell_box(width=48, height=48)
     st = tr.settings_for(scene, multi_sample=8)
     r = make_renderer(scene, st)
@@ -260,11 +263,18 @@ def test_image_rmse_against_fp64_oracle():
         r.RenderFrame()
     img = r.ColorBuffer()
     r.close()
-    acc64, _, _ = Oracle(scene).render(scene.camera, st, 48, 48, frames=2, use_double=True)
+    o = Oracle(scene)
+    acc64, _, _ = o.render(scene.camera, st, 48, 48, frames=2, use_double=True)
+    acc32, _, _ = o.render(scene.camera, st, 48, 48, frames=2)
     ref = (acc64[:, :3] / acc64[:, 3:4]).reshape(48, 48, 3)
-    rel_rmse = np.sqrt(np.mean((img[..., :3] - ref) ** 2)) / np.sqrt(np.mean(ref ** 2))
-    print(f"relative image RMSE vs FP64 oracle: {rel_rmse:.3e}")
-    assert rel_rmse < 1e-3 * 30, rel_rmse
+    ref32 = (acc32[:, :3] / acc32[:, 3:4]).reshape(48, 48, 3)
+
+    def rel(a, b):
+        return np.sqrt(np.mean((a - b) ** 2)) / np.sqrt(np.mean(b ** 2))
+
+    rel_rmse, rel32 = rel(img[..., :3], ref), rel(ref32, ref)
+    print(f"relative image RMSE vs FP64 oracle: GPU {rel_rmse:.3e}, fp32 oracle {rel32:.3e}")
+    assert rel_rmse <= 1.5 * rel32 + 1e-5, (rel_rmse, rel32)
 
 
 @pytest.mark.parametrize("fixture", ["ref_cornell_32x32_ms1.npz", "ref_cornell_24x16_ms2.npz"])

@@ -11,10 +11,13 @@ import pytest
 
 import trayracer_gb300 as tr
 from oracle import Oracle
+from oracle.build import reference_root
 from trayracer_gb300.scenefile import load_scene_file, write_model_cache, write_texture_cache
 from trayracer_gb300.scenes import MATERIAL_DTYPE, material
 
-REFERENCE_SCENES = Path("/root/reference/Resources/scenes")
+# the reference's own scene files, where its sources are present (oracle.build.reference_root)
+_REF = reference_root()
+REFERENCE_SCENES = _REF / "Resources" / "scenes" if _REF is not None else Path("/nonexistent")
 
 
 def _box(lo, hi):

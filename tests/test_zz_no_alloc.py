@@ -5,6 +5,9 @@ owns all device memory). Checked against tr_render_frame, which renders the
 same frame from the context's own buffers, on two calls in a row.
 
 Named to run last: it loads the library's device scratch array on the GPU."""
+import ctypes as C
+import dataclasses
+
 import numpy as np
 import pytest
 
@@ -49,6 +52,26 @@ def test_noalloc_matches_render_frame_on_two_calls():
     assert _close(got1, want1).all()
     assert _close(got2, want2).all()
     assert np.array_equal(acc.cpu().numpy()[..., 3], np.full((48, 64), 4.0, np.float32))
+    # the statistics of a no-allocation frame come from the shared array
+    s = r.Statistics()
+    assert s["device_error"] == 0 and s["extend_rays"][0] == 64 * 48 * 2 and s["sample_count"] == 4
+
+    # a traversal that runs out of its bound is reported through tr_get_statistics; the next
+    # call starts clean
+    r.SetSettings(dataclasses.replace(st, traversalStepLimit=2))
+    assert lib.tr_render_frame_noalloc(r.handle, None, acc.data_ptr(), col.data_ptr(), 0) == 0
+    assert r.Statistics()["device_error"] != 0
+    r.SetSettings(st)
+    assert lib.tr_render_frame_noalloc(r.handle, None, acc.data_ptr(), col.data_ptr(), 0) == 0
+    assert r.Statistics()["device_error"] == 0
+    torch.cuda.synchronize()
+    assert _close(col.cpu().numpy(), want1).all()
+
+    # other render modes are refused, not path-traced
+    assert lib.tr_set_render_mode(r.handle, 0, 0, C.c_float(1.0), C.c_float(1.0)) == 0  # ambient occlusion
+    assert lib.tr_render_frame_noalloc(r.handle, None, acc.data_ptr(), col.data_ptr(), 0) == 1
+    assert b"path-tracing" in lib.tr_last_error(r.handle)
+    assert lib.tr_set_render_mode(r.handle, 7, 0, C.c_float(1.0), C.c_float(1.0)) == 0
 
     # beyond the scratch array: rejected with a status, nothing launched
     r.Resize((512, 512))

@@ -36,7 +36,7 @@ class KernelSettings(C.Structure):
         ("rr_start", C.c_uint32),
         ("flags", C.c_uint32),
         ("max_color", C.c_float),
-        ("reserved", C.c_uint32),
+        ("traversal_step_limit", C.c_uint32),
     ]
 
 

@@ -116,7 +116,6 @@ struct Context {
     uint32_t frameW = 0, frameH = 0, frameMs = 0;
     LaunchShape shape{};
     uint32_t sampleCount = 0;
-    uint32_t* hostCounters = nullptr;  // pinned
     float* pickResult = nullptr;       // 9 words of the frame arena (tr_pick_ray)
 
     // textures of the scene: one CUDA array and texture object each, and the
@@ -136,6 +135,14 @@ struct Context {
     cudaGraph_t graph = nullptr;
     cudaGraphExec_t graphExec = nullptr;
     bool graphValid = false;
+
+    // frames rendered by tr_render_frame_noalloc: the launch shape for their
+    // capacity and tuning, and whether the last frame was one of them
+    LaunchShape noallocShape{};
+    uint32_t noallocShapeCap = 0;
+    tr_tuning noallocShapeTuning{};
+    bool lastFrameNoalloc = false;
+    uint32_t noallocPaths = 0;
 
     // render mode (RenderModes; debug modes run the reference's other shade kernels)
     uint32_t renderMode = kModePathTracing;
@@ -455,7 +462,31 @@ tr_status context_views(void* ctx, ContextViews* out)
     out->settings = c->settings;
     out->width = c->width;
     out->height = c->height;
+    out->renderMode = c->renderMode;
     return TR_OK;
+}
+
+tr_status context_launch_shape(void* ctx, uint32_t capacity, LaunchShape* out)
+{
+    if (!ctx || !out)
+        return TR_ERR_INVALID_ARGUMENT;
+    Context* c = static_cast<Context*>(ctx);
+    if (c->noallocShapeCap != capacity || std::memcmp(&c->noallocShapeTuning, &c->tuning, sizeof(tr_tuning)) != 0) {
+        c->noallocShape = tuned_launch_shape(c->device, capacity, c->tuning);
+        c->noallocShape.sortHits = 0;
+        c->noallocShapeCap = capacity;
+        c->noallocShapeTuning = c->tuning;
+    }
+    *out = c->noallocShape;
+    return TR_OK;
+}
+
+void context_note_noalloc_frame(void* ctx, uint32_t paths)
+{
+    Context* c = static_cast<Context*>(ctx);
+    c->lastFrameNoalloc = true;
+    c->noallocPaths = paths;
+    c->timedFrame = false;
 }
 
 tr_status context_fail(void* ctx, tr_status st, const std::string& msg)
@@ -506,6 +537,7 @@ bool convert_settings(const tr_kernel_settings& s, Settings* out, std::string* e
     k.renderMode = kModePathTracing;
     k.aoDist = 1.f;
     k.zDepthMax = 1.f;
+    k.stepLimit = s.traversal_step_limit ? s.traversal_step_limit : kMaxTraversalSteps;
     *out = k;
     return true;
 }
@@ -568,8 +600,6 @@ tr_status tr_create(const tr_config* config, void** out_ctx)
     for (uint32_t i = 0; ok && i < TR_MAX_DEPTH; ++i)
         ok = cudaEventCreate(&c->evExtend[i]) == cudaSuccess && cudaEventCreate(&c->evShade[i]) == cudaSuccess &&
              cudaEventCreate(&c->evConnect[i]) == cudaSuccess;
-    ok = ok && cudaMallocHost(reinterpret_cast<void**>(&c->hostCounters), kCounterWords * 2 * sizeof(uint32_t)) ==
-                   cudaSuccess;
     if (!ok) {
         cudaGetLastError();
         tr_destroy(c);
@@ -593,8 +623,6 @@ tr_status tr_destroy(void* ctx)
     c->frameArena.release();
     c->adjointArena.release();
     release_textures(c);
-    if (c->hostCounters)
-        cudaFreeHost(c->hostCounters);
     cudaEvent_t* evs[] = {&c->evStart, &c->evGenerate, &c->evFinal};
     for (cudaEvent_t* e : evs)
         if (*e)
@@ -1160,6 +1188,7 @@ tr_status tr_reset(void* ctx)
         cudaSetDevice(c->device);
         TR_CUDA(c, cudaMemsetAsync(c->frame.sampleCount, 0, sizeof(uint32_t), c->stream));
         TR_CUDA(c, cudaMemsetAsync(c->frame.traversal, 0, 4 * sizeof(unsigned long long), c->stream));
+        TR_CUDA(c, cudaMemsetAsync(c->frame.errorFlag, 0, sizeof(uint32_t), c->stream));
         TR_CUDA(c, cudaStreamSynchronize(c->stream));
     }
     return TR_OK;
@@ -1175,6 +1204,7 @@ tr_status tr_begin_frame(void* ctx, void* stream)
     if (st != TR_OK)
         return st;
     c->timedFrame = false;
+    c->lastFrameNoalloc = false;
     c->lastStream = pick_stream(c, stream);
     return enqueue_begin(c, c->lastStream);
 }
@@ -1268,6 +1298,7 @@ tr_status tr_render_frame(void* ctx, void* stream, int32_t use_graph)
         return st;
     cudaStream_t s = pick_stream(c, stream);
     c->lastStream = s;
+    c->lastFrameNoalloc = false;
     if (use_graph) {
         if (!c->graphValid) {
             // capture on the context stream (the legacy default stream cannot be captured)
@@ -1314,22 +1345,33 @@ tr_status tr_get_statistics(void* ctx, tr_statistics* out)
     if (!ctx || !out)
         return TR_ERR_INVALID_ARGUMENT;
     Context* c = static_cast<Context*>(ctx);
-    if (!c->frameArena.base)
+    FrameWords words{c->frame.counters, c->frame.sampleCount, c->frame.errorFlag, c->frame.traversal};
+    uint32_t primary = c->frame.pathCount;
+    if (c->lastFrameNoalloc) {
+        // the last frame came from tr_render_frame_noalloc: its words live in the shared scratch
+        std::string err;
+        const tr_status st = noalloc_frame_words(c->device, &words, err);
+        if (st != TR_OK)
+            return fail(c, st, err);
+        primary = c->noallocPaths;
+    } else if (!c->frameArena.base) {
         return fail(c, TR_ERR_NOT_READY, "no frame rendered");
+    }
     cudaSetDevice(c->device);
     TR_CUDA(c, cudaDeviceSynchronize());
-    TR_CUDA(c, cudaMemcpy(c->hostCounters, c->frame.counters, kCounterWords * sizeof(uint32_t), cudaMemcpyDeviceToHost));
+    uint32_t counters[kCounterWords];
+    TR_CUDA(c, cudaMemcpy(counters, words.counters, sizeof(counters), cudaMemcpyDeviceToHost));
     uint32_t err = 0, sc = 0;
     unsigned long long trav[4] = {0, 0, 0, 0};
-    TR_CUDA(c, cudaMemcpy(trav, c->frame.traversal, sizeof(trav), cudaMemcpyDeviceToHost));
-    TR_CUDA(c, cudaMemcpy(&err, c->frame.errorFlag, sizeof(uint32_t), cudaMemcpyDeviceToHost));
-    TR_CUDA(c, cudaMemcpy(&sc, c->frame.sampleCount, sizeof(uint32_t), cudaMemcpyDeviceToHost));
+    TR_CUDA(c, cudaMemcpy(trav, words.traversal, sizeof(trav), cudaMemcpyDeviceToHost));
+    TR_CUDA(c, cudaMemcpy(&err, words.errorFlag, sizeof(uint32_t), cudaMemcpyDeviceToHost));
+    TR_CUDA(c, cudaMemcpy(&sc, words.sampleCount, sizeof(uint32_t), cudaMemcpyDeviceToHost));
     tr_statistics s{};
     const uint32_t depth = c->settings.maxDepth;
     for (uint32_t b = 0; b < depth; ++b) {
-        s.extend_rays[b] = b == 0 ? c->frame.pathCount : c->hostCounters[b];
-        s.shadow_rays[b] = c->hostCounters[kShadowCounterBase + b];
-        s.hit_rays[b] = c->hostCounters[kHitCounterBase + b];
+        s.extend_rays[b] = b == 0 ? primary : counters[b];
+        s.shadow_rays[b] = counters[kShadowCounterBase + b];
+        s.hit_rays[b] = counters[kHitCounterBase + b];
         s.path_count += s.extend_rays[b] + s.shadow_rays[b];
         s.shadow_ray_count += s.shadow_rays[b];
         if (b == 0)

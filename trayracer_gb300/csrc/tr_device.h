@@ -112,6 +112,10 @@ struct SkyView {
     float sunArea;
 };
 
+// Default bound on the node visits (internal and leaf groups) of one ray's
+// traversal; a ray that runs out sets the frame's device error word.
+constexpr uint32_t kMaxTraversalSteps = 1u << 22;
+
 struct SceneView {
     const CwbvhNode* nodes;
     const float4* bvhTris;      // 3 float4 per triangle in BVH order: (v0, bits(primIx)), (e1, 0), (e2, 0)
@@ -131,7 +135,7 @@ struct SceneView {
     float lightEnergyTotal;     // sum of all light energies
     uint32_t nodeCount;
     uint32_t triCount;
-    uint32_t pad;
+    uint32_t stepLimit = kMaxTraversalSteps;  // bound on node visits of one ray (Settings::stepLimit per launch)
     const TexSlots* texSlots;   // per material, null when the scene has no textures
     SkyView sky;
 };
@@ -247,6 +251,7 @@ struct Settings {
     uint32_t renderFlags;  // MaterialPropertyIds for the material-property mode
     float aoDist;          // KernelSettings::aoDist (ambient occlusion modes)
     float zDepthMax;       // KernelSettings::zDepthMax (depth mode)
+    uint32_t stepLimit;    // bound on the BVH node visits of one ray (tr_kernel_settings.traversal_step_limit)
 };
 
 // RenderModes, Tracer/Common/CommonStructs.h:110-125

@@ -1754,6 +1754,17 @@ __global__ void advance_kernel(FrameView f, Settings st)
 } // namespace
 
 // ------------------------------------------------------------------ launchers
+namespace {
+// The scene as a traversal launch sees it: with the settings' bound on the
+// node visits of one ray.
+SceneView traced(const SceneView& s, const Settings& st)
+{
+    SceneView v = s;
+    v.stepLimit = st.stepLimit ? st.stepLimit : kMaxTraversalSteps;
+    return v;
+}
+} // namespace
+
 cudaError_t launch_generate(const FrameView& f, const Camera& cam, const Settings& st, cudaStream_t stream)
 {
     if (f.pathCount == 0)
@@ -1769,9 +1780,10 @@ cudaError_t launch_generate(const FrameView& f, const Camera& cam, const Setting
 }
 
 template <bool PRIMARY>
-void launch_extend_variant(const SceneView& s, const FrameView& f, const Settings& st, uint32_t bounce,
+void launch_extend_variant(const SceneView& s0, const FrameView& f, const Settings& st, uint32_t bounce,
                            const Camera& cam, const LaunchShape& shape, cudaStream_t stream)
 {
+    const SceneView s = traced(s0, st);
     const bool count = (st.flags & TR_FLAG_COUNT_TRAVERSAL) != 0;
     const uint32_t g = shape.extendBlocks;
     if (f.segments) {
@@ -1821,9 +1833,10 @@ cudaError_t launch_shade(const SceneView& s, const FrameView& f, const Settings&
     return cudaGetLastError();
 }
 
-cudaError_t launch_connect(const SceneView& s, const FrameView& f, const Settings& st0, uint32_t bounce,
+cudaError_t launch_connect(const SceneView& s0, const FrameView& f, const Settings& st0, uint32_t bounce,
                            const LaunchShape& shape, cudaStream_t stream)
 {
+    const SceneView s = traced(s0, st0);
     Settings st = st0;
     st.refillBelow = shape.refillBelow;
     const bool count = (st.flags & TR_FLAG_COUNT_TRAVERSAL) != 0;
@@ -1857,9 +1870,10 @@ cudaError_t launch_finalize(const FrameView& f, const Settings& st, cudaStream_t
     return cudaGetLastError();
 }
 
-cudaError_t launch_adjoint(const SceneView& s, const FrameView& f, const Camera& cam, const Settings& st,
+cudaError_t launch_adjoint(const SceneView& s0, const FrameView& f, const Camera& cam, const Settings& st,
                            const AdjointView& a, const LaunchShape& shape, cudaStream_t stream)
 {
+    const SceneView s = traced(s0, st);
     if (f.pathCount == 0)
         return cudaSuccess;
     cudaError_t e = cudaMemsetAsync(f.counters, 0, kCounterWords * sizeof(uint32_t), stream);
@@ -1908,9 +1922,10 @@ cudaError_t launch_adjoint(const SceneView& s, const FrameView& f, const Camera&
     return cudaGetLastError();
 }
 
-cudaError_t launch_debug_bounce(const SceneView& s, const FrameView& f, const Camera& cam, const Settings& st,
+cudaError_t launch_debug_bounce(const SceneView& s0, const FrameView& f, const Camera& cam, const Settings& st,
                                 uint32_t bounce, const LaunchShape& shape, cudaStream_t stream)
 {
+    const SceneView s = traced(s0, st);
     const uint32_t blocks = shape.sms * 8u;
     debug_extend_kernel<<<blocks, 128, 0, stream>>>(s, f, cam, st, bounce);
     debug_shade_kernel<<<blocks, 128, 0, stream>>>(s, f, cam, st, bounce);
@@ -1920,7 +1935,7 @@ cudaError_t launch_debug_bounce(const SceneView& s, const FrameView& f, const Ca
 cudaError_t launch_pick_ray(const SceneView& s, const Camera& cam, const Settings& st, uint32_t resX, uint32_t resY,
                             int x, int y, float* result, uint32_t* errorFlag, cudaStream_t stream)
 {
-    pick_ray_kernel<<<1, 32, 0, stream>>>(s, cam, st, resX, resY, x, y, result, errorFlag);
+    pick_ray_kernel<<<1, 32, 0, stream>>>(traced(s, st), cam, st, resX, resY, x, y, result, errorFlag);
     return cudaGetLastError();
 }
 

@@ -36,6 +36,24 @@ constexpr int kMaxDevices = 64;
 std::mutex g_setupMutex;
 void* g_scratchAddress[kMaxDevices] = {};
 
+// Makes `device` current for the guard's lifetime and restores the calling
+// thread's previous device afterwards.
+struct DeviceGuard {
+    int previous = -1;
+    bool ok = false;
+    explicit DeviceGuard(int device)
+    {
+        if (cudaGetDevice(&previous) != cudaSuccess)
+            previous = -1;
+        ok = previous == device || cudaSetDevice(device) == cudaSuccess;
+    }
+    ~DeviceGuard()
+    {
+        if (previous >= 0)
+            cudaSetDevice(previous);
+    }
+};
+
 // Clears what a frame expects to start at zero and sets the frame's sample count.
 __global__ void noalloc_begin_kernel(uint32_t* counters, uint32_t* sampleCount, uint32_t* errorFlag,
                                      unsigned long long* traversal, uint32_t sc)
@@ -73,7 +91,42 @@ tr_status scratch_address(int device, void** out, std::string& err)
     return TR_OK;
 }
 
+// Where the frame's buffers sit in the scratch array at `base` for `cap` paths.
+FrameView scratch_frame(char* base, size_t cap)
+{
+    FrameView f{};
+    f.state[0] = reinterpret_cast<float4*>(base);
+    f.state[1] = reinterpret_cast<float4*>(base + 3 * cap * 16);
+    f.hits = reinterpret_cast<uint4*>(base + 6 * cap * 16);
+    f.shadow = reinterpret_cast<float4*>(base + 7 * cap * 16);
+    f.radiance = reinterpret_cast<float4*>(base + 10 * cap * 16);
+    char* tail = base + size_t(kNoAllocMaxPaths) * kNoAllocPathBytes;
+    f.counters = reinterpret_cast<uint32_t*>(tail);
+    f.sampleCount = reinterpret_cast<uint32_t*>(tail + kCounterWords * 4);
+    f.errorFlag = reinterpret_cast<uint32_t*>(tail + kCounterWords * 4 + 4);
+    f.traversal = reinterpret_cast<unsigned long long*>(tail + 512);
+    f.capacity = uint32_t(cap);
+    return f;
+}
+
 } // namespace
+
+tr_status noalloc_frame_words(int device, FrameWords* out, std::string& err)
+{
+    DeviceGuard guard(device);
+    if (!guard.ok) {
+        err = "cudaSetDevice failed";
+        return TR_ERR_CUDA;
+    }
+    void* base = nullptr;
+    const tr_status st = scratch_address(device, &base, err);
+    if (st != TR_OK)
+        return st;
+    const FrameView f = scratch_frame(static_cast<char*>(base), 0);
+    *out = FrameWords{f.counters, f.sampleCount, f.errorFlag, f.traversal};
+    return TR_OK;
+}
+
 } // namespace tr
 
 using namespace tr;
@@ -87,13 +140,18 @@ extern "C" tr_status tr_render_frame_noalloc(void* ctx, void* stream, float* acc
         return st;
     if (!accumulator || !colors)
         return context_fail(ctx, TR_ERR_INVALID_ARGUMENT, "accumulator and colors must be device pointers");
+    if (v.renderMode != kModePathTracing)
+        return context_fail(ctx, TR_ERR_INVALID_ARGUMENT,
+                            "tr_render_frame_noalloc renders the path-tracing mode only; render other modes "
+                            "with tr_render_frame");
     const uint64_t wh = uint64_t(v.width) * v.height;
     const uint64_t paths = wh * v.settings.multiSample;
     if (paths == 0 || paths > kNoAllocMaxPaths)
         return context_fail(ctx, TR_ERR_LIMIT,
                             "tr_render_frame_noalloc holds at most 131072 paths in flight "
                             "(width * height * multi_sample)");
-    if (cudaSetDevice(v.device) != cudaSuccess)
+    DeviceGuard guard(v.device);
+    if (!guard.ok)
         return context_fail(ctx, TR_ERR_CUDA, "cudaSetDevice failed");
     void* base = nullptr;
     std::string err;
@@ -102,30 +160,22 @@ extern "C" tr_status tr_render_frame_noalloc(void* ctx, void* stream, float* acc
         return context_fail(ctx, st, err);
 
     const size_t cap = size_t(paths);
-    char* b = static_cast<char*>(base);
-    FrameView f{};
-    f.state[0] = reinterpret_cast<float4*>(b);
-    f.state[1] = reinterpret_cast<float4*>(b + 3 * cap * 16);
-    f.hits = reinterpret_cast<uint4*>(b + 6 * cap * 16);
-    f.shadow = reinterpret_cast<float4*>(b + 7 * cap * 16);
-    f.radiance = reinterpret_cast<float4*>(b + 10 * cap * 16);
-    char* tail = b + size_t(kNoAllocMaxPaths) * kNoAllocPathBytes;
-    f.counters = reinterpret_cast<uint32_t*>(tail);
-    f.sampleCount = reinterpret_cast<uint32_t*>(tail + kCounterWords * 4);
-    f.errorFlag = reinterpret_cast<uint32_t*>(tail + kCounterWords * 4 + 4);
-    f.traversal = reinterpret_cast<unsigned long long*>(tail + 512);
+    FrameView f = scratch_frame(static_cast<char*>(base), cap);
     f.accumulator = reinterpret_cast<float4*>(accumulator);
     f.colors = reinterpret_cast<float4*>(colors);
     f.albedo = nullptr;
     f.normals = nullptr;
-    f.capacity = uint32_t(cap);
     f.resX = v.width;
     f.resY = v.height;
     f.pathCount = uint32_t(paths);
+    f.hitOrder = nullptr;
 
     Settings s = v.settings;
     s.flags &= ~uint32_t(TR_FLAG_WRITE_AOVS);  // no guide buffers on this path
-    const LaunchShape shape = default_launch_shape(v.device, uint32_t(cap));
+    LaunchShape shape;
+    st = context_launch_shape(ctx, uint32_t(cap), &shape);
+    if (st != TR_OK)
+        return st;
     cudaStream_t cs = stream ? static_cast<cudaStream_t>(stream) : v.stream;
 
     noalloc_begin_kernel<<<1, 128, 0, cs>>>(f.counters, f.sampleCount, f.errorFlag, f.traversal, sample_count);
@@ -143,5 +193,6 @@ extern "C" tr_status tr_render_frame_noalloc(void* ctx, void* stream, float* acc
         e = launch_finalize(f, s, cs);
     if (e != cudaSuccess)
         return context_fail(ctx, TR_ERR_CUDA, std::string("tr_render_frame_noalloc: ") + cudaGetErrorString(e));
+    context_note_noalloc_frame(ctx, uint32_t(paths));
     return TR_OK;
 }

@@ -104,7 +104,6 @@ struct TraversalCounts {
 };
 
 constexpr int kTraversalStack = 32;
-constexpr uint32_t kMaxTraversalSteps = 1u << 22;  // bound on node + leaf visits of one ray
 
 struct TriHit {
     float t;
@@ -336,8 +335,8 @@ TR_HD void traversal_begin(Traversal& t, const float3& O, const float3& D, float
 // stack); returns its leaf group (base, bits). Returns false when a bound ran
 // out (t.ok cleared).
 template <bool COUNT>
-TR_HD bool node_step(Traversal& t, uint2* stack, const CwbvhNode* __restrict__ nodes, TraversalCounts* cnt,
-                     uint2& leaves)
+TR_HD bool node_step(Traversal& t, uint2* stack, const CwbvhNode* __restrict__ nodes, uint32_t stepLimit,
+                     TraversalCounts* cnt, uint2& leaves)
 {
     leaves = make_uint2(0u, 0u);
     if (t.group.y <= 0x00ffffffu)
@@ -360,7 +359,7 @@ TR_HD bool node_step(Traversal& t, uint2* stack, const CwbvhNode* __restrict__ n
         cnt->nodes++;
     t.group = make_uint2(childBase, (hm & 0xff000000u) | imask);
     leaves = make_uint2(triBase, hm & 0x00ffffffu);
-    if (++t.steps > kMaxTraversalSteps) {
+    if (++t.steps > stepLimit) {
         t.ok = false;
         return false;
     }
@@ -435,7 +434,7 @@ template <bool ANY, bool COUNT>
 TR_HD bool traversal_step(Traversal& t, uint2* stack, const SceneView& s, TraversalCounts* cnt)
 {
     uint2 tris;
-    if (!node_step<COUNT>(t, stack, s.nodes, cnt, tris))
+    if (!node_step<COUNT>(t, stack, s.nodes, s.stepLimit, cnt, tris))
         return true;
     if (leaf_triangles<ANY, COUNT, !ANY>(t, tris, s, cnt) == 2)
         return true;
@@ -531,7 +530,7 @@ TR_HD bool traversal_step(TraversalTL& r, uint2* stack, const SceneView& s, Trav
         r.inst = id;
         r.instSp = t.sp;
         t.group = make_uint2(ldg(&s.instInfo[id].x), 0x80000000u);
-        if (++t.steps > kMaxTraversalSteps) {
+        if (++t.steps > s.stepLimit) {
             t.ok = false;
             return true;
         }
@@ -539,7 +538,7 @@ TR_HD bool traversal_step(TraversalTL& r, uint2* stack, const SceneView& s, Trav
     }
     const bool top = r.inst == kNoInstance;
     uint2 leaves;
-    if (!node_step<COUNT>(t, stack, top ? s.tlasNodes : s.nodes, cnt, leaves))
+    if (!node_step<COUNT>(t, stack, top ? s.tlasNodes : s.nodes, s.stepLimit, cnt, leaves))
         return true;
     if (top) {
         r.leafGroup = leaves;  // entered one by one in the next steps

@@ -60,10 +60,12 @@ class KernelSettings:
     rrStart: int = 1           # PathTracing.h:149 (pathLength > 0)
     flags: int = 0
     maxColor: float = 10.0     # gMaxColorIntensity, CudaUtility.h:91
+    traversalStepLimit: int = 0  # bound on BVH node visits per ray (0: 2^22); no reference counterpart
 
     def to_c(self) -> _abi.KernelSettings:
         return _abi.KernelSettings(self.multiSample, self.maxDepth, self.seed & 0xFFFFFFFF, self.rayEpsilon,
-                                   min(self.rrStart, 0xFFFFFFFF), self.flags, self.maxColor, 0)
+                                   min(self.rrStart, 0xFFFFFFFF), self.flags, self.maxColor,
+                                   self.traversalStepLimit)
 
 
 @dataclass
