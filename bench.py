@@ -446,19 +446,6 @@ def run_batch(args):
     print(json.dumps(line), flush=True)
 
 
-def perturbed_materials(materials, seed=2, sigma=0.05):
-    """The differentiation target's parameters: every Disney parameter (base colour, roughness,
-    metallic, specular) of every material + N(0, sigma), clipped to [0, 1]."""
-    rng = np.random.default_rng(seed)
-    m = materials.copy()
-    for key, shape in (("diffuse", (3,)), ("roughness", ()), ("metallic", ()), ("specular", ())):
-        v = m[key].astype(np.float64) + rng.normal(0.0, sigma, m[key].shape)
-        m[key] = np.clip(v, 0.0, 1.0).astype(np.float32)
-    emissive = materials["emissive"].max(axis=-1) > 0
-    m[emissive] = materials[emissive]  # lights keep their colour; their radiance is a parameter, not perturbed
-    return m
-
-
 def measure_adjoint(args, steps, warmup):
     """Differentiation: the Cornell box with Disney walls, 512^2, 32 spp, 6 bounces, no RR. One
     forward frame (graph replay) and the path-replay adjoint of the L2 loss 0.5 |img - target|^2
@@ -483,7 +470,7 @@ def measure_adjoint(args, steps, warmup):
     r.SetCamera(scene.camera)
     r.Resize((W, H))
     # the target: perturbed parameters, another seed
-    r.UpdateMaterials(perturbed_materials(scene.materials))
+    r.UpdateMaterials(tr.perturbed_materials(scene.materials))
     r.SetSettings(KernelSettings(**{**st.__dict__, "seed": 7}))
     r.RenderFrame(stream=sptr, use_graph=False)
     target = torch.from_numpy(r.ColorBuffer().copy()).cuda()

@@ -1,7 +1,11 @@
 """The GPU path-replay adjoint: against the FP64 oracle's gradient of the same
-estimator, against central finite differences of GPU renders (parameters
-whose change leaves the sampled paths fixed), and through the libtorch
-autograd function. Firefly clamp off (its scale is not differentiated)."""
+estimator (relative 1e-4; with Russian roulette and 12 bounces too), against
+central finite differences of GPU renders (parameters whose change leaves the
+sampled paths fixed: within 1e-2; roughness, metallic and specular, which move
+the sampled directions: statistically over seeds), on the differentiation
+configuration (512 x 512, 32 spp, L2 loss against a perturbed target), and
+through the libtorch autograd function. Firefly clamp off (its scale is not
+differentiated)."""
 import numpy as np
 import pytest
 
@@ -28,8 +32,14 @@ def diff_scene(w, h):
     return scene
 
 
-def settings(spp, depth=6):
-    return KernelSettings(multiSample=spp, maxDepth=depth, seed=3, rrStart=1 << 30, maxColor=1e30)
+def settings(spp, depth=6, rr_start=1 << 30):
+    return KernelSettings(multiSample=spp, maxDepth=depth, seed=3, rrStart=rr_start, maxColor=1e30)
+
+
+def rel_difference(g, want):
+    """Relative L2 difference over the entries above 1 % of the largest."""
+    big = np.abs(want) > 1e-2 * np.abs(want).max()
+    return float(np.linalg.norm(g[big] - want[big]) / np.linalg.norm(want[big]))
 
 
 def gpu_adjoint(scene, st, weights):
@@ -57,10 +67,36 @@ def test_gpu_adjoint_matches_fp64_oracle():
     w[:, 3] = 0
     g_gpu = gpu_adjoint(scene, st, w)
     g_cpu = Oracle(scene).adjoint(scene.camera, st, 32, 32, 0, w, scale=1.0 / st.multiSample, use_double=True)
-    big = np.abs(g_cpu) > 1e-2 * np.abs(g_cpu).max()
-    rel = np.linalg.norm(g_gpu[big] - g_cpu[big]) / np.linalg.norm(g_cpu[big])
+    rel = rel_difference(g_gpu, g_cpu)
     print(f"relative gradient difference GPU vs FP64 oracle: {rel:.2e}")
-    assert rel < 2e-2, rel
+    assert rel < 1e-4, rel
+
+
+def test_gpu_adjoint_with_russian_roulette_deep_paths():
+    """12 bounces with Russian roulette from bounce 3 (the large configuration's depth): the
+    replay carries each path's remaining radiance forward, so no per-bounce state is kept
+    however deep the path; the survival factor 1/rr (Shade/PathTracing.h:149-155) is held fixed
+    like the sampling pdfs (detached), which keeps the gradient estimator unbiased:
+    E[d(g)/rr 1{u < rr}] = d(g) for any rr. Against the oracle's adjoint of the same estimator
+    (fp32: the same Russian-roulette decisions; FP64: decisions may flip on a last-bit
+    difference)."""
+    scene = diff_scene(32, 32)
+    st = settings(16, depth=12, rr_start=3)
+    rng = np.random.default_rng(3)
+    w = rng.uniform(-1, 1, (32 * 32, 4)).astype(np.float32)
+    w[:, 3] = 0
+    g_gpu = gpu_adjoint(scene, st, w)
+    o = Oracle(scene)
+    g32 = o.adjoint(scene.camera, st, 32, 32, 0, w, scale=1.0 / st.multiSample, use_double=False)
+    g64 = o.adjoint(scene.camera, st, 32, 32, 0, w, scale=1.0 / st.multiSample, use_double=True)
+    rel32, rel64, rel_o = rel_difference(g_gpu, g32), rel_difference(g_gpu, g64), rel_difference(g32, g64)
+    print(f"RR adjoint, 12 bounces: GPU vs fp32 oracle {rel32:.2e}, vs FP64 oracle {rel64:.2e}, "
+          f"fp32 vs FP64 oracle {rel_o:.2e}")
+    assert rel32 < 1e-4, rel32
+    assert rel64 < 1e-2 and rel64 <= 1.5 * rel_o + 1e-4, (rel64, rel_o)
+    # deep paths exist: the gradient differs from a 6-bounce frame's
+    g6 = gpu_adjoint(scene, settings(16, depth=6, rr_start=3), w)
+    assert rel_difference(g6, g_gpu) > 1e-4
 
 
 def _fd_renderer(scene, st):
@@ -79,14 +115,20 @@ def _fd(r, scene, w, m, field, c, h):
         img = r.ColorBuffer().reshape(-1, 4).astype(np.float64)
         return float((img[:, :3] * w[:, :3]).sum())
 
+    # material values are stored as fp16 on upload: step to fp16 values and divide by the step
+    # that remains
     mp, mm = scene.materials.copy(), scene.materials.copy()
     if c is None:
-        mp[m][field] += h
-        mm[m][field] -= h
+        p0 = float(mp[m][field])
+        mp[m][field] = np.float32(np.float16(p0 + h))
+        mm[m][field] = np.float32(np.float16(p0 - h))
+        step = float(mp[m][field]) - float(mm[m][field])
     else:
-        mp[m][field][c] += h
-        mm[m][field][c] -= h
-    return (loss(mp) - loss(mm)) / (2 * h)
+        p0 = float(mp[m][field][c])
+        mp[m][field][c] = np.float32(np.float16(p0 + h))
+        mm[m][field][c] = np.float32(np.float16(p0 - h))
+        step = float(mp[m][field][c]) - float(mm[m][field][c])
+    return (loss(mp) - loss(mm)) / step
 
 
 def test_gpu_adjoint_matches_finite_differences():
@@ -116,34 +158,103 @@ def test_gpu_adjoint_matches_finite_differences():
     assert not bad, bad
 
 
-def test_gpu_adjoint_roughness_statistically_consistent_with_fd():
-    """Roughness moves the sampled GGX directions (and rays across geometric edges), so the
-    fixed-seed finite difference is a noisy estimator of the derivative while the
-    detached-sampling adjoint is not. Over independent seeds (batch means) the two must agree
-    within three standard errors of their difference."""
-    scene = diff_scene(128, 128)
+@pytest.mark.parametrize("field,slot,materials,h", [("roughness", 3, (0, 2, 6), 2.0 ** -8),
+                                                     ("metallic", 4, (0, 2, 3), 2.0 ** -6),
+                                                     ("specular", 5, (0, 2, 3), 2.0 ** -6)])
+def test_gpu_adjoint_statistically_consistent_with_fd(field, slot, materials, h):
+    """Roughness, metallic and specular move the sampled directions (the GGX lobe's shape, the
+    lobe-selection weights) and so rays across geometric edges: the fixed-seed finite difference
+    is a noisy estimator of the derivative while the detached-sampling adjoint is not. Over
+    independent seeds (batch means) the two must agree within three standard errors of their
+    difference; and at least one of them must be resolved (adjoint mean above three standard
+    errors), so that a wrong gradient would show. Metallic and specular are checked on walls whose
+    values lie inside [h, 1 - h] (metallic 0.12-0.27, specular 0.23-0.80)."""
+    scene = diff_scene(256, 256)
     rng = np.random.default_rng(4)
-    w = rng.uniform(0.0, 1.0, (128 * 128, 4)).astype(np.float32)
+    w = rng.uniform(0.0, 1.0, (256 * 256, 4)).astype(np.float32)
     w[:, 3] = 0
-    h = 2.0 ** -8
     rows = []
-    for mi in (0, 2, 6):
+    for mi in materials:
+        p0 = float(scene.materials[mi][field])
+        assert h <= p0 <= 1.0 - h or field == "roughness"
         diffs = []
-        for seed in range(12):
+        for seed in range(16):
             st = settings(16)
             st.seed = 1000 + seed
             g = gpu_adjoint(scene, st, w)
             r = _fd_renderer(scene, st)
-            fd = _fd(r, scene, w, mi, "roughness", None, h)
+            fd = _fd(r, scene, w, mi, field, None, h)
             r.close()
-            diffs.append((fd, float(g[mi, 3])))
+            diffs.append((fd, float(g[mi, slot])))
         d = np.array(diffs)
         delta = d[:, 0] - d[:, 1]
         se = delta.std(ddof=1) / np.sqrt(len(delta))
         rows.append((mi, d[:, 0].mean(), d[:, 1].mean(), delta.mean(), se))
-    print("roughness gradient (material, fd mean, adjoint mean, mean difference, standard error):", rows)
+    print(f"{field} gradient (material, fd mean, adjoint mean, mean difference, standard error):", rows)
     for mi, fdm, adm, dm, se in rows:
         assert abs(dm) <= 3.0 * se + 1e-3 * abs(adm), rows
+    assert any(abs(adm) > 3.0 * se for _, _, adm, _, se in rows), "no material with a resolved gradient"
+
+
+def test_differentiation_configuration():
+    """The differentiation configuration: the closed box (diffuse walls and short box, GGX
+    conductor) at 512 x 512, 32 spp, 6 bounces, no Russian roulette; L2 loss
+    0.5 |img - target|^2 against a target rendered with every Disney parameter + N(0, 0.05)
+    (clipped to [0, 1]). Every parameter whose change leaves the sampled paths fixed (the base
+    colours of the diffuse materials and of the metallic conductor, the light's emission) is
+    checked against central differences of GPU renders with common random numbers, h = 1e-3
+    relative to max(1, |p|), divided by the change that remains after the fp16 rounding of
+    material values on upload; within 1e-2. The whole gradient table against the FP64 oracle's."""
+    W = H = 512
+    scene = tr.cornell_box(width=W, height=H, max_depth=6)
+    m = scene.materials.copy()
+    for f in ("diffuse", "emissive", "metallic", "roughness", "specular"):
+        m[f] = m[f].astype(np.float16).astype(np.float32)
+    scene.materials = m
+    st = settings(32)
+    r = _fd_renderer(scene, st)
+    r.UpdateMaterials(tr.perturbed_materials(m))
+    r.SetSettings(KernelSettings(**{**st.__dict__, "seed": 7}))
+    r.RenderFrame()
+    target = r.ColorBuffer().reshape(-1, 4).astype(np.float64)
+    r.UpdateMaterials(m)
+    r.SetSettings(st)
+    r.RenderFrame()
+    img = r.ColorBuffer().reshape(-1, 4).astype(np.float64)
+    w = (img - target).astype(np.float32)
+    w[:, 3] = 0
+    g = gpu_adjoint(scene, st, w)
+
+    def loss(mats):
+        r.UpdateMaterials(mats)
+        r.RenderFrame()
+        x = r.ColorBuffer().reshape(-1, 4).astype(np.float64)
+        return 0.5 * float(((x[:, :3] - target[:, :3]) ** 2).sum())
+
+    light = int(np.where(m["emissive"].sum(1) > 0)[0][0])
+    checks = [(mi, "diffuse", c, c) for mi in range(7) for c in range(3)]
+    checks += [(light, "emissive", c, 6 + c) for c in range(3)]
+    rows, bad = [], []
+    gmax = np.abs(g).max()
+    for mi, field, c, slot in checks:
+        p0 = float(m[mi][field][c])
+        h = 1e-3 * max(1.0, abs(p0))
+        mp, mm = m.copy(), m.copy()
+        mp[mi][field][c] = np.float32(np.float16(p0 + h))
+        mm[mi][field][c] = np.float32(np.float16(p0 - h))
+        step = float(mp[mi][field][c]) - float(mm[mi][field][c])
+        assert step > 0
+        fd = (loss(mp) - loss(mm)) / step
+        rows.append((mi, field, c, fd, float(g[mi, slot])))
+        if abs(fd - g[mi, slot]) > 1e-2 * abs(fd) + 1e-5 * gmax:
+            bad.append(rows[-1])
+    r.close()
+    print("differentiation configuration (material, field, channel, fd, adjoint):", rows)
+    assert not bad, bad
+    g64 = Oracle(scene).adjoint(scene.camera, st, W, H, 0, w, scale=1.0 / st.multiSample, use_double=True)
+    rel = rel_difference(g, g64)
+    print(f"differentiation configuration: GPU vs FP64 oracle gradient {rel:.2e}")
+    assert rel < 1e-4, rel
 
 
 def test_torch_autograd_function():

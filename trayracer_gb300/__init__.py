@@ -20,6 +20,7 @@ from .scenes import (  # noqa: F401
     heightfield,
     instanced_cornell,
     outdoor_heightfield,
+    perturbed_materials,
     sphere_batch,
     sphere_scene,
     textured_cornell,

@@ -242,6 +242,20 @@ def cornell_box(seed: int = 1, width: int = 256, height: int = 256, spp: int = 1
                  seed)
 
 
+def perturbed_materials(materials: np.ndarray, seed: int = 2, sigma: float = 0.05) -> np.ndarray:
+    """The differentiation target's parameters: every Disney parameter (base colour, roughness,
+    metallic, specular) of every non-emissive material + N(0, sigma), clipped to [0, 1]; emitters
+    keep theirs."""
+    rng = np.random.default_rng(seed)
+    m = np.array(materials, MATERIAL_DTYPE, copy=True)
+    for key in ("diffuse", "roughness", "metallic", "specular"):
+        v = m[key].astype(np.float64) + rng.normal(0.0, sigma, m[key].shape)
+        m[key] = np.clip(v, 0.0, 1.0).astype(np.float32)
+    emissive = np.asarray(materials["emissive"]).max(axis=-1) > 0
+    m[emissive] = np.asarray(materials)[emissive]
+    return m
+
+
 def textured_cornell(seed: int = 5, width: int = 48, height: int = 48, spp: int = 4, max_depth: int = 5,
                      wall_closure: int = TR_CLOSURE_DIFFUSE, tex_size: int = 16) -> Scene:
     """The Cornell box with textures: texture coordinates are a planar projection of the vertex
