@@ -1065,6 +1065,42 @@ template <class T, bool REF> Lobe<T> d_sample(V3<T> wo, const HitMat<T>& m, T r0
     return r;
 }
 
+// The default sampling mode's Disney closure (the reference's sampling with its
+// quirks fixed): the lobe that r0 falls in picks the extend direction (r0
+// rescaled into the lobe's interval), and the light direction and the extend
+// direction are both evaluated over all lobes - value = sum of the lobe values,
+// pdf = sum of weight x lobe pdf, each lobe term as in d_evaluate<T, false>
+// (Disney.h:401-470). Same estimator as Disney::Sample + Disney::Evaluate
+// (Disney.h:473-565) without their REF quirks.
+template <class T> Clos<T> d_closure_default(V3<T> wo, V3<T> wi, V3<T> Tp, const HitMat<T>& m, T r0, T r1)
+{
+    Lobe<T> e{wi, T(0), v3s(T(0)), 0};
+    Lobe<T> s{v3(T(0), T(0), T(1)), T(0), v3s(T(0)), 0};
+    T wd, ws, wsp, wc;
+    if (d_weights(m, wd, ws, wsp, wc)) {
+        T ax, ay;
+        alpha_xy(m.roughness, m.anisotropic, ax, ay);
+        const T cd = wd, cs = cd + ws, csp = cs + wsp;
+        V3<T> d = v3(T(0), T(0), T(1));
+        if (r0 < cd) {
+            d = cos_hemi(r0 / wd, r1);
+        } else if (r0 < cs) {
+            d = cos_hemi((r0 - cd) / ws, r1);
+        } else if (wo.z != T(0)) {
+            const V3<T> h = r0 < csp ? ggx_sample_m(wo, fmn((r0 - cs) / wsp, T(0.99999994f)), r1, ax, ay)
+                                     : gtr1_sample_m(fmn((r0 - csp) / wc, T(0.99999994f)), r1, cc_alpha(m));
+            d = reflect(-wo, h);
+            force_above(d);
+        }
+        e = d_evaluate<T, false>(wo, wi, m);
+        const Lobe<T> q = d_evaluate<T, false>(wo, d, m);
+        s.wi = d;
+        s.pdf = q.pdf > T(1e-6f) ? q.pdf : T(0);
+        s.Tv = q.Tv;
+    }
+    return finalize(Tp, e, s);
+}
+
 // ---------------------------------------------------------------- camera
 template <class T, class Rng> void sample_disk(Rng& rng, T& x, T& y)
 {
@@ -1549,7 +1585,8 @@ ShadeOut<T> shade_one(const orc_scene& S, const tr_kernel_settings& st, uint32_t
     const T r1 = T(u1);
     Clos<T> c;
     if (m.closure == TR_CLOSURE_DISNEY)
-        c = finalize(Tp, d_evaluate<T, REF>(wo, wi, m), d_sample<T, REF>(wo, m, r0, r1));
+        c = REF ? finalize(Tp, d_evaluate<T, true>(wo, wi, m), d_sample<T, true>(wo, m, r0, r1))
+                : d_closure_default<T>(wo, wi, Tp, m, r0, r1);
     else if (m.closure == TR_CLOSURE_DIFFUSE)
         c = diffuse(wo, wi, Tp, m, r0, r1);
     else
@@ -2342,7 +2379,7 @@ void orc_closure(int type, int reference, int use_double, const float* in, float
         Clos<T> c;
         if (type == TR_CLOSURE_DISNEY)
             c = reference ? finalize(Tp, d_evaluate<T, true>(wo, wi, m), d_sample<T, true>(wo, m, r0, r1))
-                          : finalize(Tp, d_evaluate<T, false>(wo, wi, m), d_sample<T, false>(wo, m, r0, r1));
+                          : d_closure_default<T>(wo, wi, Tp, m, r0, r1);
         else if (type == TR_CLOSURE_DIFFUSE)
             c = diffuse(wo, wi, Tp, m, r0, r1);
         else

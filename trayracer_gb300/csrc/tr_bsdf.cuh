@@ -19,7 +19,10 @@
 //     next emissive hit.
 // REF = false sums all lobe values, rescales r0 into the chosen lobe's
 // interval, includes the clearcoat pdf and flags no Disney lobe as specular
-// (none is a delta lobe), so NEE and BSDF sampling always combine by MIS.
+// (none is a delta lobe), so NEE and BSDF sampling always combine by MIS; the
+// chosen lobe only picks the direction, which is then evaluated over all lobes
+// like the light direction (so a clearcoat sample carries the clearcoat
+// Fresnel, where Disney.h:337-366 weights it with the specular one).
 // Values the reference leaves unset on early returns are zero in both modes.
 #pragma once
 
@@ -547,12 +550,180 @@ __device__ __forceinline__ Lobe sample(const float3& wo, const HitMat& mat, floa
 
 } // namespace disney
 
+// ---------------------------------------------------------------- Disney, default sampling mode
+// The default mode's closure: the sampled lobe only chooses the direction, and
+// the light direction and the sampled direction are both evaluated over all
+// lobes (value = sum of the lobe values, pdf = sum of weight x lobe pdf), so
+// the extend direction's value is the closure value that the path-replay
+// adjoint differentiates. The terms that depend on the material and wo alone
+// (lobe weights, alphas, the Smith Lambda of wo, the GTR1 normalisation) are
+// computed once per hit; each term is the same arithmetic as in
+// disney::evaluate<false>.
+namespace disney {
+
+struct Prep {
+    float wd, ws, wsp, wc;  // lobe selection weights
+    float ax, ay;           // GGX alphas (Microfacet.h:33-49)
+    float lamO;             // GGX Lambda(wo)
+    float ccA;              // GTR1 alpha before its clamp
+    float ccA2;             // clamped GTR1 alpha squared
+    float ccLogA2;          // log(ccA2)
+    float ccNorm;           // (a2 - 1) / (pi log a2) of GTR1's D
+    float ccLamO;           // GTR1 Lambda(wo)
+};
+
+__device__ __forceinline__ float gtr1_lambda_c(const float3& v, float a2, float logA2)
+{
+    const float c = v.z;
+    if (c == 0.0f)
+        return 0.0f;
+    const float c2 = square(c);
+    const float s = sqrtf(fmaxf(0.0f, 1.0f - c2));
+    if (s == 0.0f)
+        return 0.0f;
+    const float cot2 = c2 / square(s);
+    const float cot = sqrtf(cot2);
+    const float a = sqrtf(cot2 + a2);
+    const float b = sqrtf(cot2 + 1.0f);
+    const float lc = logf(cot + b);
+    const float ld = logf(cot + a);
+    return (a - b + cot * (lc - ld)) / (cot * logA2);
+}
+
+__device__ __forceinline__ bool prepare(const HitMat& mat, const float3& wo, Prep& p)
+{
+    if (!weights(mat, p.wd, p.ws, p.wsp, p.wc))
+        return false;
+    mf::alpha_xy(mat.roughness, mat.anisotropic, p.ax, p.ay);
+    p.lamO = p.wsp > 0 ? mf::ggx_lambda(wo, p.ax, p.ay) : 0.f;
+    p.ccA = clearcoat_alpha(mat);
+    if (p.wc > 0) {
+        const float alpha = clampf(p.ccA, 0.001f, 0.999f);
+        p.ccA2 = square(alpha);
+        p.ccLogA2 = logf(p.ccA2);
+        p.ccNorm = (p.ccA2 - 1.0f) / (kPi * p.ccLogA2);
+        p.ccLamO = gtr1_lambda_c(wo, p.ccA2, p.ccLogA2);
+    }
+    return true;
+}
+
+// ggx_eval with Lambda(wo) and D computed once
+__device__ __forceinline__ float ggx_eval_p(const Prep& p, const HitMat& mat, const float3& wo, const float3& wi,
+                                            float3& value)
+{
+    if (wo.z == 0.0f || wi.z == 0.0f)
+        return 0.0f;
+    const float3 m = normalize(wi + wo);
+    const float coh = dot(wo, m);
+    if (coh == 0.0f)
+        return 0.0f;
+    const float D = mf::ggx_D(m, p.ax, p.ay);
+    const float G = 1.0f / (1.0f + p.lamO + mf::ggx_lambda(wi, p.ax, p.ay));
+    value = spec_fresnel(mat, wo, m);
+    value *= D * G / fabsf(4.0f * wo.z * wi.z);
+    const float G1 = 1.0f / (1.0f + p.lamO);
+    return (G1 * fabsf(coh) * D / fabsf(wo.z)) / fabsf(4.0f * coh);
+}
+
+// gtr1_eval with the GTR1 normalisation, Lambda(wo) and D computed once
+__device__ __forceinline__ float gtr1_eval_p(const Prep& p, const HitMat& mat, const float3& wo, const float3& wi,
+                                             float3& value)
+{
+    if (wo.z == 0.0f || wi.z == 0.0f)
+        return 0.0f;
+    const float3 m = normalize(wi + wo);
+    const float coh = dot(wo, m);
+    if (coh == 0.0f)
+        return 0.0f;
+    const float D = p.ccNorm * (1.0f / (1.0f + (p.ccA2 - 1.0f) * square(m.z)));
+    const float G = 1.0f / (1.0f + p.ccLamO + gtr1_lambda_c(wi, p.ccA2, p.ccLogA2));
+    value = clearcoat_fresnel(mat, wo, m);
+    value *= D * G / fabsf(4.0f * wo.z * wi.z);
+    return (D * fabsf(m.y)) / fabsf(4.0f * coh);
+}
+
+// All lobes at wi: returns sum(weight x pdf), value = sum of the lobe values (evaluate<false>).
+__device__ __forceinline__ float eval_all(const Prep& p, const HitMat& mat, const float3& wo, const float3& wi,
+                                          float3& value)
+{
+    float pdf = 0.f;
+    value = f3(0.f);
+    float3 v = f3(0.f);
+    if (p.wd > 0) {
+        pdf += p.wd * diffuse_eval(mat, wo, wi, v);
+        value += v;
+    }
+    if (p.ws > 0) {
+        pdf += p.ws * sheen_eval(mat, wo, wi, v);
+        value += v;
+    }
+    if (p.wsp > 0) {
+        v = f3(0.f);
+        const float q = ggx_eval_p(p, mat, wo, wi, v);
+        if (q > 0) {
+            pdf += p.wsp * q;
+            value += v;
+        }
+    }
+    if (p.wc > 0) {
+        v = f3(0.f);
+        const float q = gtr1_eval_p(p, mat, wo, wi, v);
+        if (q > 0) {
+            pdf += p.wc * q;
+            value += v;
+        }
+    }
+    return pdf;
+}
+
+// The sampled direction: the lobe r0 falls in, with r0 rescaled into its interval.
+__device__ __forceinline__ float3 sample_direction(const Prep& p, const float3& wo, float r0, float r1)
+{
+    const float cd = p.wd, cs = cd + p.ws, csp = cs + p.wsp;
+    float3 wi = make_float3(0.f, 0.f, 1.f);
+    if (r0 < cd) {
+        wi = cos_hemisphere(r0 / p.wd, r1);
+    } else if (r0 < cs) {
+        wi = cos_hemisphere((r0 - cd) / p.ws, r1);
+    } else if (wo.z != 0.0f) {
+        float3 m;
+        if (r0 < csp)
+            m = mf::ggx_sample(wo, fminf_((r0 - cs) / p.wsp, 0.99999994f), r1, p.ax, p.ay);
+        else
+            m = mf::gtr1_sample(fminf_((r0 - csp) / p.wc, 0.99999994f), r1, p.ccA);
+        wi = reflect(-wo, m);
+        force_above(wi);
+    }
+    return wi;
+}
+
+} // namespace disney
+
 template <bool REF>
 __device__ __forceinline__ ClosureResult disney_closure(const float3& wo, const float3& wi, const float3& T,
                                                         const HitMat& m, float r0, float r1)
 {
-    const Lobe e = disney::evaluate<REF>(wo, wi, m);
-    const Lobe s = disney::sample<REF>(wo, m, r0, r1);
+    if (REF) {
+        const Lobe e = disney::evaluate<REF>(wo, wi, m);
+        const Lobe s = disney::sample<REF>(wo, m, r0, r1);
+        return finalize_closure(T, e, s);
+    }
+    Lobe e, s;
+    e.wi = wi;
+    e.pdf = 0.f;
+    e.T = f3(0.f);
+    e.flags = 0;
+    s.wi = make_float3(0.f, 0.f, 1.f);
+    s.pdf = 0.f;
+    s.T = f3(0.f);
+    s.flags = 0;
+    disney::Prep p;
+    if (disney::prepare(m, wo, p)) {
+        e.pdf = disney::eval_all(p, m, wo, wi, e.T);
+        s.wi = disney::sample_direction(p, wo, r0, r1);
+        const float q = disney::eval_all(p, m, wo, s.wi, s.T);
+        s.pdf = q > 1e-6f ? q : 0.f;
+    }
     return finalize_closure(T, e, s);
 }
 
