@@ -99,10 +99,10 @@ __device__ __forceinline__ ClosureResult lambert_closure(const float3& wo, const
     if (r0 < specProb) {
         s.wi = make_float3(-wo.x, -wo.y, wo.z);  // reflect(-wo, z)
         s.pdf = 1.f;
-        s.T = f3(1.f / s.wi.z) * m.diffuse;
+        s.T = f3(fdiv(1.f, s.wi.z)) * m.diffuse;
         s.flags = kFlagSpecular;
     } else {
-        s.wi = cos_hemisphere((specProb - r0) / (1.f - specProb), r1);
+        s.wi = cos_hemisphere(fdiv(specProb - r0, 1.f - specProb), r1);
         s.pdf = kRcpPi * s.wi.z;
         s.T = f3(kRcpPi) * m.diffuse;
         s.flags = 0;
@@ -134,22 +134,22 @@ __device__ __forceinline__ void alpha_xy(float roughness, float aniso, float& ax
 {
     const float r2 = square(roughness);
     const float aspect = sqrtf(1.0f + aniso * (aniso < 0 ? 0.9f : -0.9f));
-    ax = fmaxf(0.001f, r2 / aspect);
+    ax = fmaxf(0.001f, fdiv(r2, aspect));
     ay = fmaxf(0.001f, r2 * aspect);
 }
 
 __device__ __forceinline__ float stretched_roughness(const float3& m, float sinT, float ax, float ay)
 {
     if (ax == ay || sinT == 0.0f)
-        return 1.0f / square(ax);
-    return square(m.x / (sinT * ax)) + square(m.z / (sinT * ay));
+        return fdiv(1.0f, square(ax));
+    return square(fdiv(m.x, sinT * ax)) + square(fdiv(m.z, sinT * ay));
 }
 
 __device__ __forceinline__ float projected_roughness(const float3& m, float sinT, float ax, float ay)
 {
     if (ax == ay || sinT == 0.0f)
         return ax;
-    return sqrtf(square((m.x * ax) / sinT) + square((m.y * ay) / sinT));
+    return sqrtf(square(fdiv(m.x * ax, sinT)) + square(fdiv(m.y * ay, sinT)));
 }
 
 __device__ __forceinline__ float ggx_lambda(const float3& v, float ax, float ay)
@@ -160,7 +160,7 @@ __device__ __forceinline__ float ggx_lambda(const float3& v, float ax, float ay)
     const float c2 = square(c);
     const float s = sqrtf(fmaxf(0.0f, 1.0f - c2));
     const float a = projected_roughness(v, s, ax, ay);
-    const float t2 = square(s) / c2;
+    const float t2 = fdiv(square(s), c2);
     return (-1.0f + sqrtf(1.0f + square(a) * t2)) * 0.5f;
 }
 
@@ -172,23 +172,23 @@ __device__ __forceinline__ float ggx_D(const float3& m, float ax, float ay)
     const float c2 = square(c);
     const float s = sqrtf(fmaxf(0.0f, 1.0f - c2));
     const float c4 = square(c2);
-    const float t2 = (1.0f - c2) / c2;
+    const float t2 = fdiv(1.0f - c2, c2);
     const float A = stretched_roughness(m, s, ax, ay);
     const float tmp = 1.0f + t2 * A;
-    return 1.0f / (kPi * ax * ay * c4 * square(tmp));
+    return fdiv(1.0f, kPi * ax * ay * c4 * square(tmp));
 }
 
 __device__ __forceinline__ float ggx_G(const float3& wi, const float3& wo, float ax, float ay)
 {
-    return 1.0f / (1.0f + ggx_lambda(wo, ax, ay) + ggx_lambda(wi, ax, ay));
+    return fdiv(1.0f, 1.0f + ggx_lambda(wo, ax, ay) + ggx_lambda(wi, ax, ay));
 }
 
 __device__ __forceinline__ float ggx_pdf(const float3& v, const float3& m, float ax, float ay)
 {
     if (v.z == 0.0f)
         return 0.0f;
-    const float G1 = 1.0f / (1.0f + ggx_lambda(v, ax, ay));
-    return G1 * fabsf(dot(v, m)) * ggx_D(m, ax, ay) / fabsf(v.z);
+    const float G1 = fdiv(1.0f, 1.0f + ggx_lambda(v, ax, ay));
+    return fdiv(G1 * fabsf(dot(v, m)) * ggx_D(m, ax, ay), fabsf(v.z));
 }
 
 // visible-normal sample (Heitz 2017), Microfacet.h:172-210
@@ -198,9 +198,9 @@ __device__ __forceinline__ float3 ggx_sample(const float3& v, float r0, float r1
     const float3 st = normalize(make_float3(sgn * v.x * ax, sgn * v.y * ay, sgn * v.z));
     const float3 t1 = v.y < 0.9999f ? normalize(cross(st, make_float3(0.f, 0.f, 1.f))) : make_float3(1.f, 0.f, 0.f);
     const float3 t2 = cross(t1, st);
-    const float a = 1.0f / (1.0f + st.z);
+    const float a = fdiv(1.0f, 1.0f + st.z);
     const float r = sqrtf(r0);
-    const float phi = r1 < a ? r1 / a * kPi : kPi + (r1 - a) / (1.0f - a) * kPi;
+    const float phi = r1 < a ? fdiv(r1, a) * kPi : kPi + fdiv(r1 - a, 1.0f - a) * kPi;
     float sp, cp;
     sincosf(phi, &sp, &cp);
     const float p1 = r * cp;
@@ -218,7 +218,7 @@ __device__ __forceinline__ float gtr1_lambda(const float3& v, float ax)
     const float s = sqrtf(fmaxf(0.0f, 1.0f - c2));
     if (s == 0.0f)
         return 0.0f;
-    const float cot2 = c2 / square(s);
+    const float cot2 = fdiv(c2, square(s));
     const float cot = sqrtf(cot2);
     const float alpha = clampf(ax, 0.001f, 0.999f);
     const float a2 = square(alpha);
@@ -226,7 +226,7 @@ __device__ __forceinline__ float gtr1_lambda(const float3& v, float ax)
     const float b = sqrtf(cot2 + 1.0f);
     const float lc = logf(cot + b);
     const float ld = logf(cot + a);
-    return (a - b + cot * (lc - ld)) / (cot * logf(a2));
+    return fdiv(a - b + cot * (lc - ld), cot * logf(a2));
 }
 
 __device__ __forceinline__ float gtr1_D(const float3& m, float ax)
@@ -234,14 +234,14 @@ __device__ __forceinline__ float gtr1_D(const float3& m, float ax)
     const float alpha = clampf(ax, 0.001f, 0.999f);
     const float a2 = square(alpha);
     const float c2 = square(m.z);
-    const float a = (a2 - 1.0f) / (kPi * logf(a2));
-    const float b = 1.0f / (1.0f + (a2 - 1.0f) * c2);
+    const float a = fdiv(a2 - 1.0f, kPi * logf(a2));
+    const float b = fdiv(1.0f, 1.0f + (a2 - 1.0f) * c2);
     return a * b;
 }
 
 __device__ __forceinline__ float gtr1_G(const float3& wi, const float3& wo, float ax)
 {
-    return 1.0f / (1.0f + gtr1_lambda(wo, ax) + gtr1_lambda(wi, ax));
+    return fdiv(1.0f, 1.0f + gtr1_lambda(wo, ax) + gtr1_lambda(wi, ax));
 }
 
 // GTR1 pdf as stated in the reference (Microfacet.h:320-323; uses |m.y|)
@@ -252,7 +252,7 @@ __device__ __forceinline__ float3 gtr1_sample(float r0, float r1, float ax)
     const float alpha = clampf(ax, 0.001f, 0.999f);
     const float a2 = square(alpha);
     const float a = 1.0f - powf(a2, 1.0f - r0);
-    const float c2 = a / (1.0f - a2);
+    const float c2 = fdiv(a, 1.0f - a2);
     const float c = sqrtf(c2);
     const float s = sqrtf(fmaxf(0.0f, 1.0f - c2));
     float sp, cp;
@@ -309,7 +309,7 @@ __device__ __forceinline__ float diffuse_eval(const HitMat& mat, const float3& w
     if (mat.subsurface > 0.0f) {
         const float fss90 = square(cih) * mat.roughness;
         const float fss = mix(1.0f, fss90, fl) * mix(1.0f, fss90, fv);
-        const float ss = 1.25f * (fss * (1.0f / (fabsf(con) + fabsf(cin)) - 0.5f) + 0.5f);
+        const float ss = 1.25f * (fss * (fdiv(1.0f, fabsf(con) + fabsf(cin)) - 0.5f) + 0.5f);
         fd = mix(fd, ss, mat.subsurface);
     }
     value = mat.diffuse;
@@ -338,8 +338,8 @@ __device__ __forceinline__ float ggx_eval(float ax, float ay, const HitMat& mat,
     const float D = mf::ggx_D(m, ax, ay);
     const float G = mf::ggx_G(wi, wo, ax, ay);
     value = spec_fresnel(mat, wo, m);
-    value *= D * G / fabsf(4.0f * wo.z * wi.z);
-    return mf::ggx_pdf(wo, m, ax, ay) / fabsf(4.0f * coh);
+    value *= fdiv(D * G, fabsf(4.0f * wo.z * wi.z));
+    return fdiv(mf::ggx_pdf(wo, m, ax, ay), fabsf(4.0f * coh));
 }
 
 __device__ __forceinline__ void ggx_sample(float ax, float ay, const HitMat& mat, float r0, float r1, const float3& wo,
@@ -354,13 +354,13 @@ __device__ __forceinline__ void ggx_sample(float ax, float ay, const HitMat& mat
     if (wi.z == 0.0f)
         return;
     const float coh = dot(wo, m);
-    pdf = mf::ggx_pdf(wo, m, ax, ay) / fabsf(4.0f * coh);
+    pdf = fdiv(mf::ggx_pdf(wo, m, ax, ay), fabsf(4.0f * coh));
     if (pdf < 1e-6f)
         return;
     const float D = mf::ggx_D(m, ax, ay);
     const float G = mf::ggx_G(wi, wo, ax, ay);
     value = spec_fresnel(mat, wo, m);
-    value *= D * G / fabsf(4.0f * wo.z * wi.z);
+    value *= fdiv(D * G, fabsf(4.0f * wo.z * wi.z));
 }
 
 __device__ __forceinline__ float gtr1_eval(float a, const HitMat& mat, const float3& wo, const float3& wi, float3& value)
@@ -374,8 +374,8 @@ __device__ __forceinline__ float gtr1_eval(float a, const HitMat& mat, const flo
     const float D = mf::gtr1_D(m, a);
     const float G = mf::gtr1_G(wi, wo, a);
     value = clearcoat_fresnel(mat, wo, m);
-    value *= D * G / fabsf(4.0f * wo.z * wi.z);
-    return mf::gtr1_pdf(m, a) / fabsf(4.0f * coh);
+    value *= fdiv(D * G, fabsf(4.0f * wo.z * wi.z));
+    return fdiv(mf::gtr1_pdf(m, a), fabsf(4.0f * coh));
 }
 
 // Disney.h:337-366: the clearcoat sample is weighted with the specular Fresnel
@@ -391,13 +391,13 @@ __device__ __forceinline__ void gtr1_sample(float a, const HitMat& mat, float r0
     if (wi.z == 0.0f)
         return;
     const float coh = dot(wo, m);
-    pdf = mf::gtr1_pdf(m, a) / fabsf(4.0f * coh);
+    pdf = fdiv(mf::gtr1_pdf(m, a), fabsf(4.0f * coh));
     if (pdf < 1e-6f)
         return;
     const float D = mf::gtr1_D(m, a);
     const float G = mf::gtr1_G(wi, wo, a);
     value = spec_fresnel(mat, wo, m);
-    value *= D * G / fabsf(4.0f * wo.z * wi.z);
+    value *= fdiv(D * G, fabsf(4.0f * wo.z * wi.z));
 }
 
 __device__ __forceinline__ bool weights(const HitMat& mat, float& wd, float& ws, float& wsp, float& wc)
@@ -409,7 +409,7 @@ __device__ __forceinline__ bool weights(const HitMat& mat, float& wd, float& ws,
     const float total = wd + ws + wsp + wc;
     if (total == 0.0f)
         return false;
-    const float rcp = 1.f / total;
+    const float rcp = fdiv(1.f, total);
     wd *= rcp;
     ws *= rcp;
     wsp *= rcp;
@@ -490,20 +490,20 @@ __device__ __forceinline__ Lobe sample(const float3& wo, const HitMat& mat, floa
     float3 value = f3(0.f);
     uint32_t flags = 0;
     if (r0 < cd) {
-        const float u = REF ? r0 : r0 / wd;
+        const float u = REF ? r0 : fdiv(r0, wd);
         wi = cos_hemisphere(u, r1);
         cpdf = diffuse_eval(mat, wo, wi, value);
         prob = wd * cpdf;
         wd = 0;
     } else if (r0 < cs) {
-        const float u = REF ? r0 : (r0 - cd) / ws;
+        const float u = REF ? r0 : fdiv(r0 - cd, ws);
         wi = cos_hemisphere(u, r1);
         cpdf = sheen_eval(mat, wo, wi, value);
         prob = ws * cpdf;
         ws = 0;
         flags |= REF ? kFlagSpecular : 0u;
     } else if (r0 < csp) {
-        const float u = REF ? r0 : fminf_((r0 - cs) / wsp, 0.99999994f);
+        const float u = REF ? r0 : fminf_(fdiv(r0 - cs, wsp), 0.99999994f);
         float ax, ay;
         mf::alpha_xy(mat.roughness, mat.anisotropic, ax, ay);
         ggx_sample(ax, ay, mat, u, r1, wo, wi, cpdf, value);
@@ -511,7 +511,7 @@ __device__ __forceinline__ Lobe sample(const float3& wo, const HitMat& mat, floa
         wsp = 0;
         flags |= REF ? kFlagSpecular : 0u;
     } else {
-        const float u = REF ? r0 : fminf_((r0 - csp) / wc, 0.99999994f);
+        const float u = REF ? r0 : fminf_(fdiv(r0 - csp, wc), 0.99999994f);
         gtr1_sample(clearcoat_alpha(mat), mat, u, r1, wo, wi, cpdf, value);
         prob = wc * cpdf;
         wc = 0;
@@ -581,13 +581,13 @@ __device__ __forceinline__ float gtr1_lambda_c(const float3& v, float a2, float 
     const float s = sqrtf(fmaxf(0.0f, 1.0f - c2));
     if (s == 0.0f)
         return 0.0f;
-    const float cot2 = c2 / square(s);
+    const float cot2 = fdiv(c2, square(s));
     const float cot = sqrtf(cot2);
     const float a = sqrtf(cot2 + a2);
     const float b = sqrtf(cot2 + 1.0f);
     const float lc = logf(cot + b);
     const float ld = logf(cot + a);
-    return (a - b + cot * (lc - ld)) / (cot * logA2);
+    return fdiv(a - b + cot * (lc - ld), cot * logA2);
 }
 
 __device__ __forceinline__ bool prepare(const HitMat& mat, const float3& wo, Prep& p)
@@ -601,7 +601,7 @@ __device__ __forceinline__ bool prepare(const HitMat& mat, const float3& wo, Pre
         const float alpha = clampf(p.ccA, 0.001f, 0.999f);
         p.ccA2 = square(alpha);
         p.ccLogA2 = logf(p.ccA2);
-        p.ccNorm = (p.ccA2 - 1.0f) / (kPi * p.ccLogA2);
+        p.ccNorm = fdiv(p.ccA2 - 1.0f, kPi * p.ccLogA2);
         p.ccLamO = gtr1_lambda_c(wo, p.ccA2, p.ccLogA2);
     }
     return true;
@@ -618,11 +618,11 @@ __device__ __forceinline__ float ggx_eval_p(const Prep& p, const HitMat& mat, co
     if (coh == 0.0f)
         return 0.0f;
     const float D = mf::ggx_D(m, p.ax, p.ay);
-    const float G = 1.0f / (1.0f + p.lamO + mf::ggx_lambda(wi, p.ax, p.ay));
+    const float G = fdiv(1.0f, 1.0f + p.lamO + mf::ggx_lambda(wi, p.ax, p.ay));
     value = spec_fresnel(mat, wo, m);
-    value *= D * G / fabsf(4.0f * wo.z * wi.z);
-    const float G1 = 1.0f / (1.0f + p.lamO);
-    return (G1 * fabsf(coh) * D / fabsf(wo.z)) / fabsf(4.0f * coh);
+    value *= fdiv(D * G, fabsf(4.0f * wo.z * wi.z));
+    const float G1 = fdiv(1.0f, 1.0f + p.lamO);
+    return fdiv(fdiv(G1 * fabsf(coh) * D, fabsf(wo.z)), fabsf(4.0f * coh));
 }
 
 // gtr1_eval with the GTR1 normalisation, Lambda(wo) and D computed once
@@ -635,11 +635,11 @@ __device__ __forceinline__ float gtr1_eval_p(const Prep& p, const HitMat& mat, c
     const float coh = dot(wo, m);
     if (coh == 0.0f)
         return 0.0f;
-    const float D = p.ccNorm * (1.0f / (1.0f + (p.ccA2 - 1.0f) * square(m.z)));
-    const float G = 1.0f / (1.0f + p.ccLamO + gtr1_lambda_c(wi, p.ccA2, p.ccLogA2));
+    const float D = p.ccNorm * fdiv(1.0f, 1.0f + (p.ccA2 - 1.0f) * square(m.z));
+    const float G = fdiv(1.0f, 1.0f + p.ccLamO + gtr1_lambda_c(wi, p.ccA2, p.ccLogA2));
     value = clearcoat_fresnel(mat, wo, m);
-    value *= D * G / fabsf(4.0f * wo.z * wi.z);
-    return (D * fabsf(m.y)) / fabsf(4.0f * coh);
+    value *= fdiv(D * G, fabsf(4.0f * wo.z * wi.z));
+    return fdiv(D * fabsf(m.y), fabsf(4.0f * coh));
 }
 
 // All lobes at wi: returns sum(weight x pdf), value = sum of the lobe values (evaluate<false>).
@@ -682,15 +682,15 @@ __device__ __forceinline__ float3 sample_direction(const Prep& p, const float3& 
     const float cd = p.wd, cs = cd + p.ws, csp = cs + p.wsp;
     float3 wi = make_float3(0.f, 0.f, 1.f);
     if (r0 < cd) {
-        wi = cos_hemisphere(r0 / p.wd, r1);
+        wi = cos_hemisphere(fdiv(r0, p.wd), r1);
     } else if (r0 < cs) {
-        wi = cos_hemisphere((r0 - cd) / p.ws, r1);
+        wi = cos_hemisphere(fdiv(r0 - cd, p.ws), r1);
     } else if (wo.z != 0.0f) {
         float3 m;
         if (r0 < csp)
-            m = mf::ggx_sample(wo, fminf_((r0 - cs) / p.wsp, 0.99999994f), r1, p.ax, p.ay);
+            m = mf::ggx_sample(wo, fminf_(fdiv(r0 - cs, p.wsp), 0.99999994f), r1, p.ax, p.ay);
         else
-            m = mf::gtr1_sample(fminf_((r0 - csp) / p.wc, 0.99999994f), r1, p.ccA);
+            m = mf::gtr1_sample(fminf_(fdiv(r0 - csp, p.wc), 0.99999994f), r1, p.ccA);
         wi = reflect(-wo, m);
         force_above(wi);
     }

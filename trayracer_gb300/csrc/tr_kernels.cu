@@ -64,6 +64,28 @@ __device__ __forceinline__ uint32_t warp_append(uint32_t* counter, bool pred)
     return base + __popc(mask & ((1u << lane) - 1u));
 }
 
+// Two appends at once (one atomic per warp and queue, both in flight before
+// either result is read): slot0 / slot1 of the lanes with pred0 / pred1.
+__device__ __forceinline__ void warp_append2(uint32_t* counter0, bool pred0, uint32_t& slot0, uint32_t* counter1,
+                                             bool pred1, uint32_t& slot1)
+{
+    const uint32_t m0 = __ballot_sync(kFull, pred0);
+    const uint32_t m1 = __ballot_sync(kFull, pred1);
+    const uint32_t lane = lane_id();
+    const uint32_t l0 = m0 ? __ffs(m0) - 1u : 0u;
+    const uint32_t l1 = m1 ? __ffs(m1) - 1u : 0u;
+    uint32_t b0 = 0, b1 = 0;
+    if (m0 && lane == l0)
+        b0 = atomicAdd(counter0, __popc(m0));
+    if (m1 && lane == l1)
+        b1 = atomicAdd(counter1, __popc(m1));
+    b0 = __shfl_sync(kFull, b0, l0);
+    b1 = __shfl_sync(kFull, b1, l1);
+    const uint32_t below = (1u << lane) - 1u;
+    slot0 = b0 + __popc(m0 & below);
+    slot1 = b1 + __popc(m1 & below);
+}
+
 // SafeColor = fixnan(clamp_scaled(c, max)), CudaUtility.h:95-99 and
 // CudaLinearMath.h:127-142.
 __device__ __forceinline__ float3 safe_color(const float3& c, float maxValue)
@@ -515,9 +537,9 @@ __device__ __forceinline__ float3 sample_light(const SceneView& s, Rng& rng, boo
     const float sqDist = dot(Ld, Ld);
     Ld = normalize(Ld);
     const float LNdotL = dot(L.N, Ld);
-    prob = L.energy / total;
+    prob = fdiv(L.energy, total);
     const bool facing = REF ? (dot(N, Ld) != 0.f) : (dot(N, Ld) < 0.f);
-    pdf = (LNdotL > 0 && facing) ? sqDist / (L.area * LNdotL) : 0;
+    pdf = (LNdotL > 0 && facing) ? fdiv(sqDist, L.area * LNdotL) : 0;
     dist = sqrtf(sqDist);
     radiance = L.radiance;
     return -Ld;
@@ -594,18 +616,22 @@ __device__ __forceinline__ Surface surface_at(const SceneView& s, uint32_t instI
         sf.B = normalize(cross(sf.N, e1));
         sf.T = normalize(cross(sf.N, sf.B));
     } else {
-        const float rr = 1.f / r;
+        const float rr = fdiv(1.f, r);
         const float3 tv = ((s1 * e2) - (s2 * e1)) * rr;
         sf.B = normalize(tv - sf.N * dot(sf.N, tv));
         sf.T = normalize(cross(sf.N, sf.B));
     }
-    const float4 tx = __ldg(s.invTransforms + instIx * 3 + 0);
-    const float4 ty = __ldg(s.invTransforms + instIx * 3 + 1);
-    const float4 tz = __ldg(s.invTransforms + instIx * 3 + 2);
-    sf.N = normalize(xform(tx, ty, tz, sf.N));
-    sf.Ng = normalize(xform(tx, ty, tz, sf.Ng));
-    sf.B = normalize(xform(tx, ty, tz, sf.B));
-    sf.T = normalize(xform(tx, ty, tz, sf.T));
+    if (s.instInfo) {
+        // two-level scenes: the frame to world space by the inverse-transpose
+        // instance transform (one mesh: the identity, skipped)
+        const float4 tx = __ldg(s.invTransforms + instIx * 3 + 0);
+        const float4 ty = __ldg(s.invTransforms + instIx * 3 + 1);
+        const float4 tz = __ldg(s.invTransforms + instIx * 3 + 2);
+        sf.N = normalize(xform(tx, ty, tz, sf.N));
+        sf.Ng = normalize(xform(tx, ty, tz, sf.Ng));
+        sf.B = normalize(xform(tx, ty, tz, sf.B));
+        sf.T = normalize(xform(tx, ty, tz, sf.T));
+    }
     if (dot(D, sf.N) > 0) {
         sf.Ng = -sf.Ng;
         sf.N = -sf.N;
@@ -747,17 +773,17 @@ __device__ __forceinline__ void shade_path(const SceneView& s, const FrameView& 
         if (bounce == 0 || (flags & kFlagSpecular)) {
             contrib = m.emissive;
         } else {
-            const float lightPdf = (tmax * tmax) / (fabsf(dot(D, sf.N)) * sf.area);
+            const float lightPdf = fdiv(tmax * tmax, fabsf(dot(D, sf.N)) * sf.area);
             const float3 en = m.emissive * sf.area;
             const float total = REF ? s.lightEnergy : s.lightEnergyTotal;
-            const float pick = (en.x + en.y + en.z) / total;
+            const float pick = fdiv(en.x + en.y + en.z, total);
             const float denom = extendPdf + lightPdf * pick;
             if (REF) {
                 if (denom > 0)
-                    contrib = T * m.diffuse * (1.0f / denom);
+                    contrib = T * m.diffuse * fdiv(1.0f, denom);
             } else {
                 if (denom > 0)
-                    contrib = T * m.emissive * (extendPdf / denom);
+                    contrib = T * m.emissive * fdiv(extendPdf, denom);
             }
         }
         float3 add = safe_color(contrib, st.maxColor);
@@ -800,7 +826,7 @@ __device__ __forceinline__ void shade_path(const SceneView& s, const FrameView& 
         c = lambert_closure(wo, wi, T, m, r0, r1);
 
     if ((lightPdf > kEpsilon) && (c.shPdf > kEpsilon) && ((c.extFlags & kFlagSpecular) == 0)) {
-        const float3 shadowT = (c.shT * lightRadiance) / (lightProb * lightPdf + c.shPdf);
+        const float3 shadowT = (c.shT * lightRadiance) * fdiv(1.f, lightProb * lightPdf + c.shPdf);
         wantShadow = true;
         sh[0] = f4(I, __uint_as_float(pathIx));
         sh[1] = f4(L, lightDist);
@@ -810,12 +836,12 @@ __device__ __forceinline__ void shade_path(const SceneView& s, const FrameView& 
     if (vi)
         vi->wiExt = c.extWi;
     if (c.extPdf > kEpsilon) {
-        float3 tp = c.extT / fabsf(c.extPdf);
+        float3 tp = c.extT * fdiv(1.f, fabsf(c.extPdf));
         if (bounce >= st.rrStart) {
             const float rr = fminf(1.0f, fmaxf(tp.x, fmaxf(tp.y, tp.z)));
             if (rr < rng.next())
                 return;
-            tp *= 1.f / rr;
+            tp *= fdiv(1.f, rr);
         }
         const float3 nd = normalize((c.extWi.x * sf.T) + (c.extWi.y * sf.B) + (c.extWi.z * sf.N));
         if (c.extFlags & kFlagSpecular)
@@ -830,7 +856,7 @@ __device__ __forceinline__ void shade_path(const SceneView& s, const FrameView& 
 }
 
 template <bool REF, bool BATCH, bool TEX = false>
-__global__ void __launch_bounds__(128) shade_kernel(SceneView s, FrameView f, Settings st, uint32_t bounce)
+__global__ void __launch_bounds__(128, 5) shade_kernel(SceneView s, FrameView f, Settings st, uint32_t bounce)
 {
     const uint32_t count = __ldcg(f.counters + kHitCounterBase + bounce);
     const float4* __restrict__ in = f.state[1];
@@ -894,13 +920,13 @@ __global__ void __launch_bounds__(128) shade_kernel(SceneView s, FrameView f, Se
                                                  sh);
             }
         }
-        const uint32_t shSlot = warp_append(shCounter, wantShadow);
+        uint32_t shSlot, exSlot;
+        warp_append2(shCounter, wantShadow, shSlot, extCounter, wantExt, exSlot);
         if (wantShadow) {
             __stcs(f.shadow + shSlot, sh[0]);
             __stcs(f.shadow + shSlot + cap, sh[1]);
             __stcs(f.shadow + shSlot + 2 * cap, sh[2]);
         }
-        const uint32_t exSlot = warp_append(extCounter, wantExt);
         if (wantExt) {
             __stcs(out + exSlot, ext[0]);
             __stcs(out + exSlot + cap, ext[1]);

@@ -66,6 +66,16 @@ TR_HD float rsqrt_(float x)
 #endif
 }
 TR_HD float3 normalize(const float3& v) { return v * rsqrt_(dot(v, v)); }
+// a / b for shading arithmetic: the device's fast division (within 2 ulp; the
+// traversal keeps its correctly rounded operations), plain division on the host
+TR_HD float fdiv(float a, float b)
+{
+#if defined(__CUDA_ARCH__)
+    return __fdividef(a, b);
+#else
+    return a / b;
+#endif
+}
 TR_HD float2 normalize(const float2& v) { return v * rsqrt_(v.x * v.x + v.y * v.y); }
 TR_HD float fminf_(float a, float b) { return a < b ? a : b; }
 TR_HD float fmaxf_(float a, float b) { return a > b ? a : b; }
