@@ -69,6 +69,8 @@ def parse():
     p.add_argument("--no-extra", action="store_true",
                    help="plain workload: skip the batched and differentiation measurements after the timed region")
     p.add_argument("--wave-paths", type=int, default=0, help="batched waves: paths per wave (0: library default)")
+    p.add_argument("--no-ms1", action="store_true",
+                   help="batch workload: skip the per-scene baseline at the reference's multi_sample = 1")
     return p.parse_args()
 
 
@@ -415,7 +417,7 @@ def measure_batch(args, steps, warmup, with_ms1=True):
 
 
 def run_batch(args):
-    m = measure_batch(args, args.steps, args.warmup)
+    m = measure_batch(args, args.steps, args.warmup, with_ms1=not args.no_ms1)
     if args.profile:
         print(json.dumps(m))
         return
@@ -439,8 +441,8 @@ def run_batch(args):
                    "l2": "flushed before each timed render (256 MiB write)"},
         "mrays_per_s": round(m["batch_rays"] / (batch_ms / 1e3) / 1e6, 1),
         "gpu_launches": info["launches"],
-        **{k: m[k] for k in ("per_scene", "per_scene_ms1", "speedup_vs_per_scene", "speedup_vs_per_scene_ms1",
-                             "rays_per_scene", "scene_generation_s", "batch_build_s", "clocks")},
+        **{k: m.get(k) for k in ("per_scene", "per_scene_ms1", "speedup_vs_per_scene", "speedup_vs_per_scene_ms1",
+                                 "rays_per_scene", "scene_generation_s", "batch_build_s", "clocks")},
         "rays_batch": m["batch_rays"],
     }
     print(json.dumps(line), flush=True)
@@ -792,16 +794,17 @@ def main():
                     traffic = None
 
     # --- the other stages by the same fixed byte formulas (per step). Shade: 140 B read per
-    # shaded hit (state 48 + hit 16 + shading record 72 + material index 4) plus 48 B per
-    # extend and per shadow ray written; connect: 48 B per shadow ray plus its traversal
-    # bytes; finalize: per pixel the multi_sample path radiances (16 B each), the
-    # accumulator read and written and the colour written (16 B each). The radiance
-    # read-modify-writes of emissive hits and visible shadow rays are not in the counters, so
-    # the shade and connect figures are lower bounds.
+    # shaded hit (state 48 + hit 16 + shading record 72 + material index 4), 48 B per extend
+    # and per shadow ray written and 32 B per radiance read-modify-write (emissive hits);
+    # connect: 48 B per shadow ray, its traversal bytes and 32 B per radiance
+    # read-modify-write (unoccluded shadow rays); finalize: per pixel the multi_sample path
+    # radiances (16 B each), the accumulator read and written and the colour written (16 B
+    # each). The radiance updates come from the counting pass.
     secondary = ext_rays - int(ext_per_bounce[0])
     stage_bytes = {
-        "shade": hit_rays * 140 + (secondary + sh_rays) * 48,
-        "connect": sh_rays * 48 + cs["traversal_connect_nodes"] * NODE_BYTES + cs["traversal_connect_tris"] * TRI_BYTES,
+        "shade": hit_rays * 140 + (secondary + sh_rays) * 48 + cs["radiance_updates_shade"] * 32,
+        "connect": sh_rays * 48 + cs["traversal_connect_nodes"] * NODE_BYTES + cs["traversal_connect_tris"] * TRI_BYTES
+        + cs["radiance_updates_connect"] * 32,
         "finalize": frames_per_step * scene.width * scene.height * (16 * args.ms + 48),
     }
     stage_roofline = {}
@@ -887,7 +890,7 @@ def main():
                 "connect_nodes_per_ray": round(cs["traversal_connect_nodes"] / max(1, sh_rays), 3),
                 "connect_tris_per_ray": round(cs["traversal_connect_tris"] / max(1, sh_rays), 3),
             },
-            "stage_roofline": stage_roofline,  # lower bounds for shade and connect (see above)
+            "stage_roofline": stage_roofline,
             "cpu_baseline": cpu,
             "clocks": clocks.summary(),
             "e2e": {

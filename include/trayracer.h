@@ -48,7 +48,7 @@
 extern "C" {
 #endif
 
-#define TR_ABI_VERSION 2u
+#define TR_ABI_VERSION 3u
 
 /* Maximum path length; the reference's DeviceRenderer::MaxTraceDepth
  * (Tracer/Renderer/DeviceRenderer.h:29). */
@@ -256,6 +256,10 @@ typedef struct tr_statistics {
     uint64_t traversal_connect_nodes;
     uint64_t traversal_connect_tris;
     uint32_t hit_rays[TR_MAX_DEPTH];    /* extend rays per bounce that hit something */
+    /* with TR_FLAG_COUNT_TRAVERSAL, summed over the frames since tr_reset: path radiance
+     * read-modify-writes by shade (emissive hits) and by connect (unoccluded shadow rays) */
+    uint64_t radiance_updates_shade;
+    uint64_t radiance_updates_connect;
 } tr_statistics;
 
 /* Scene numbers: triangle/light/BVH sizes and the host build time. */

@@ -172,6 +172,10 @@ def test_counts_and_aovs():
     assert all(s["shadow_rays"][i] <= ext[i] for i in range(st.maxDepth))
     assert s["path_count"] == sum(ext) + sum(s["shadow_rays"])
     assert s["traversal_extend_nodes"] >= sum(ext)
+    # radiance updates: one per emissive hit in shade (camera rays see the light), one per
+    # unoccluded shadow ray in connect
+    assert 0 < s["radiance_updates_shade"] <= sum(s["hit_rays"])
+    assert 0 < s["radiance_updates_connect"] <= sum(s["shadow_rays"])
     assert (albedo[..., :3] > 0).any()
     assert s["render_time_ms"] > 0 and s["extend_time_ms"] > 0
 

@@ -5,7 +5,7 @@ import ctypes as C
 from pathlib import Path
 
 TR_MAX_DEPTH = 16
-TR_ABI_VERSION = 2
+TR_ABI_VERSION = 3
 TR_FLAG_REFERENCE_SAMPLING = 1 << 0
 TR_FLAG_WRITE_AOVS = 1 << 1
 TR_FLAG_REFERENCE_DRAW_RTL = 1 << 2
@@ -152,6 +152,8 @@ class Statistics(C.Structure):
         ("traversal_connect_nodes", C.c_uint64),
         ("traversal_connect_tris", C.c_uint64),
         ("hit_rays", C.c_uint32 * TR_MAX_DEPTH),
+        ("radiance_updates_shade", C.c_uint64),
+        ("radiance_updates_connect", C.c_uint64),
     ]
 
 

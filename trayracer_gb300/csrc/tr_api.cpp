@@ -328,7 +328,7 @@ tr_status ensure_frame(Context* c)
     const size_t oCnt = take(kCounterWords * sizeof(uint32_t));
     const size_t oSc = take(sizeof(uint32_t));
     const size_t oErr = take(sizeof(uint32_t));
-    const size_t oTrav = take(4 * sizeof(unsigned long long));
+    const size_t oTrav = take(kTraversalCounters * sizeof(unsigned long long));
     const size_t oKeys = take(cap * sizeof(uint32_t));
     const size_t oOrder = take(cap * sizeof(uint32_t));
     const size_t oPick = take(16 * sizeof(float));
@@ -1187,7 +1187,7 @@ tr_status tr_reset(void* ctx)
     if (c->frame.sampleCount && c->frameArena.base) {
         cudaSetDevice(c->device);
         TR_CUDA(c, cudaMemsetAsync(c->frame.sampleCount, 0, sizeof(uint32_t), c->stream));
-        TR_CUDA(c, cudaMemsetAsync(c->frame.traversal, 0, 4 * sizeof(unsigned long long), c->stream));
+        TR_CUDA(c, cudaMemsetAsync(c->frame.traversal, 0, kTraversalCounters * sizeof(unsigned long long), c->stream));
         TR_CUDA(c, cudaMemsetAsync(c->frame.errorFlag, 0, sizeof(uint32_t), c->stream));
         TR_CUDA(c, cudaStreamSynchronize(c->stream));
     }
@@ -1362,7 +1362,7 @@ tr_status tr_get_statistics(void* ctx, tr_statistics* out)
     uint32_t counters[kCounterWords];
     TR_CUDA(c, cudaMemcpy(counters, words.counters, sizeof(counters), cudaMemcpyDeviceToHost));
     uint32_t err = 0, sc = 0;
-    unsigned long long trav[4] = {0, 0, 0, 0};
+    unsigned long long trav[kTraversalCounters] = {};
     TR_CUDA(c, cudaMemcpy(trav, words.traversal, sizeof(trav), cudaMemcpyDeviceToHost));
     TR_CUDA(c, cudaMemcpy(&err, words.errorFlag, sizeof(uint32_t), cudaMemcpyDeviceToHost));
     TR_CUDA(c, cudaMemcpy(&sc, words.sampleCount, sizeof(uint32_t), cudaMemcpyDeviceToHost));
@@ -1406,6 +1406,8 @@ tr_status tr_get_statistics(void* ctx, tr_statistics* out)
     s.traversal_extend_tris = trav[1];
     s.traversal_connect_nodes = trav[2];
     s.traversal_connect_tris = trav[3];
+    s.radiance_updates_shade = trav[4];
+    s.radiance_updates_connect = trav[5];
     *out = s;
     return TR_OK;
 }

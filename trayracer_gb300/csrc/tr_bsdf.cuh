@@ -699,9 +699,11 @@ __device__ __forceinline__ float3 sample_direction(const Prep& p, const float3& 
 
 } // namespace disney
 
+// evalLight = false (default mode): the light direction is not evaluated (its
+// result would be discarded: the light sample has no density there).
 template <bool REF>
 __device__ __forceinline__ ClosureResult disney_closure(const float3& wo, const float3& wi, const float3& T,
-                                                        const HitMat& m, float r0, float r1)
+                                                        const HitMat& m, float r0, float r1, bool evalLight = true)
 {
     if (REF) {
         const Lobe e = disney::evaluate<REF>(wo, wi, m);
@@ -719,7 +721,8 @@ __device__ __forceinline__ ClosureResult disney_closure(const float3& wo, const 
     s.flags = 0;
     disney::Prep p;
     if (disney::prepare(m, wo, p)) {
-        e.pdf = disney::eval_all(p, m, wo, wi, e.T);
+        if (evalLight)
+            e.pdf = disney::eval_all(p, m, wo, wi, e.T);
         s.wi = disney::sample_direction(p, wo, r0, r1);
         const float q = disney::eval_all(p, m, wo, s.wi, s.T);
         s.pdf = q > 1e-6f ? q : 0.f;

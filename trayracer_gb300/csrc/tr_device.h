@@ -112,6 +112,9 @@ struct SkyView {
     float sunArea;
 };
 
+// Counters of the counting launches (TR_FLAG_COUNT_TRAVERSAL), FrameView::traversal.
+constexpr uint32_t kTraversalCounters = 6;
+
 // Default bound on the node visits (internal and leaf groups) of one ray's
 // traversal; a ray that runs out sets the frame's device error word.
 constexpr uint32_t kMaxTraversalSteps = 1u << 22;
@@ -170,7 +173,8 @@ struct FrameView {
     uint32_t* counters;    // kCounterWords words, layout above
     uint32_t* sampleCount; // device copy of the accumulated sample count
     uint32_t* errorFlag;   // set by bounded loops that ran out
-    unsigned long long* traversal;  // extend nodes, extend tris, connect nodes, connect tris (counting launches)
+    unsigned long long* traversal;  // kTraversalCounters words (counting launches): extend nodes, extend tris,
+                                    // connect nodes, connect tris, shade and connect radiance updates
     uint32_t capacity;
     uint32_t resX, resY;
     uint32_t pathCount;    // resX * resY * multiSample (batched: the paths of the wave)

@@ -333,6 +333,16 @@ __device__ __forceinline__ uint32_t queue_length(const FrameView& f, uint32_t bo
 }
 
 // Sums per-thread traversal work into a device counter, one atomic per warp.
+// Adds the warp's sum of v to *dst (one atomic per warp).
+__device__ __forceinline__ void add_count(unsigned long long* dst, uint32_t v)
+{
+    unsigned long long n = v;
+    for (int o = 16; o > 0; o >>= 1)
+        n += __shfl_down_sync(kFull, n, o);
+    if (lane_id() == 0 && n)
+        atomicAdd(dst, n);
+}
+
 __device__ __forceinline__ void add_counts(unsigned long long* dst, const TraversalCounts& c)
 {
     unsigned long long n = c.nodes, t = c.tris;
@@ -717,8 +727,9 @@ struct VertexInfo {
 // One PathTracingKernel step (PathTracing.h:15-174) for one queue entry. With
 // vi == nullptr (the shade kernel) it adds emitted radiance and writes the
 // guide buffers; the adjoint replay passes vi and gets the vertex instead.
+// Returns true when it added emitted radiance to the path's radiance.
 template <bool REF, class Rng, bool TEX = false>
-__device__ __forceinline__ void shade_path(const SceneView& s, const FrameView& f, const Settings& st, uint32_t bounce,
+__device__ __forceinline__ bool shade_path(const SceneView& s, const FrameView& f, const Settings& st, uint32_t bounce,
                                            uint32_t sc, const float4& O4, const float4& D4, const float4& T4,
                                            const uint4& hd, Rng& rng, bool& wantExt, float4 (&ext)[3],
                                            bool& wantShadow, float4 (&sh)[3], VertexInfo* vi = nullptr)
@@ -749,7 +760,7 @@ __device__ __forceinline__ void shade_path(const SceneView& s, const FrameView& 
             f.albedo[pixelIx] = make_float4(0.f, 0.f, 0.f, 0.f);
             f.normals[pixelIx] = make_float4(0.f, 0.f, 0.f, 0.f);
         }
-        return;
+        return false;
     }
 
     const Surface sf = surface_at<TEX>(s, instIx, primIx, bary, D);
@@ -792,11 +803,11 @@ __device__ __forceinline__ void shade_path(const SceneView& s, const FrameView& 
         if (vi) {
             vi->emissive = true;
             vi->emitted = add;
-            return;
+            return false;
         }
         float4 r = f.radiance[pathIx];
         f.radiance[pathIx] = make_float4(r.x + add.x, r.y + add.y, r.z + add.z, r.w);
-        return;
+        return true;
     }
 
     float lightProb, lightPdf, lightDist;
@@ -819,7 +830,7 @@ __device__ __forceinline__ void shade_path(const SceneView& s, const FrameView& 
     draw2(rng, rtl, r0, r1);
     ClosureResult c;
     if (closure == TR_CLOSURE_DISNEY)
-        c = disney_closure<REF>(wo, wi, T, m, r0, r1);
+        c = disney_closure<REF>(wo, wi, T, m, r0, r1, lightPdf > kEpsilon);
     else if (closure == TR_CLOSURE_DIFFUSE)
         c = diffuse_closure(wo, wi, T, m, r0, r1);
     else
@@ -840,7 +851,7 @@ __device__ __forceinline__ void shade_path(const SceneView& s, const FrameView& 
         if (bounce >= st.rrStart) {
             const float rr = fminf(1.0f, fmaxf(tp.x, fmaxf(tp.y, tp.z)));
             if (rr < rng.next())
-                return;
+                return false;
             tp *= fdiv(1.f, rr);
         }
         const float3 nd = normalize((c.extWi.x * sf.T) + (c.extWi.y * sf.B) + (c.extWi.z * sf.N));
@@ -853,6 +864,7 @@ __device__ __forceinline__ void shade_path(const SceneView& s, const FrameView& 
         ext[1] = f4(nd, __uint_as_float(pack_normal(sf.N)));
         ext[2] = f4(fixnan(tp), c.extPdf);
     }
+    return false;
 }
 
 template <bool REF, bool BATCH, bool TEX = false>
@@ -889,7 +901,7 @@ __global__ void __launch_bounds__(128, 5) shade_kernel(SceneView s, FrameView f,
 
     for (uint32_t base = warpGlobal * 32u; base < count; base += warpStride * 32u) {
         const uint32_t k = base + lane;
-        bool wantExt = false, wantShadow = false;
+        bool wantExt = false, wantShadow = false, emitted = false;
         float4 ext[3], sh[3];
         if (k < count) {
             cp_async_wait_all();
@@ -909,17 +921,20 @@ __global__ void __launch_bounds__(128, 5) shade_kernel(SceneView s, FrameView f,
                 const SceneView si = item_scene(s, f.items[sg.item]);
                 CounterRng rng;
                 rng.init(rel % sg.pixels, sg.sampleBase + rel / sg.pixels, bounce + 1u, st.seed);
-                shade_path<false>(si, f, st, bounce, sc, O4, D4, T4, hd, rng, wantExt, ext, wantShadow, sh);
+                emitted = shade_path<false>(si, f, st, bounce, sc, O4, D4, T4, hd, rng, wantExt, ext, wantShadow, sh);
             } else if (REF) {
                 RefRng rng{tea2(st.seed + pathIx, sc + bounce + 1u)};
-                shade_path<REF, RefRng, TEX>(s, f, st, bounce, sc, O4, D4, T4, hd, rng, wantExt, ext, wantShadow, sh);
+                emitted = shade_path<REF, RefRng, TEX>(s, f, st, bounce, sc, O4, D4, T4, hd, rng, wantExt, ext,
+                                                       wantShadow, sh);
             } else {
                 CounterRng rng;
                 rng.init(pathIx % wh, sc + pathIx / wh, bounce + 1u, st.seed);
-                shade_path<REF, CounterRng, TEX>(s, f, st, bounce, sc, O4, D4, T4, hd, rng, wantExt, ext, wantShadow,
-                                                 sh);
+                emitted = shade_path<REF, CounterRng, TEX>(s, f, st, bounce, sc, O4, D4, T4, hd, rng, wantExt, ext,
+                                                           wantShadow, sh);
             }
         }
+        if (st.flags & TR_FLAG_COUNT_TRAVERSAL)
+            add_count(f.traversal + 4, emitted ? 1u : 0u);
         uint32_t shSlot, exSlot;
         warp_append2(shCounter, wantShadow, shSlot, extCounter, wantExt, exSlot);
         if (wantShadow) {
@@ -1042,6 +1057,7 @@ __global__ void __launch_bounds__(128) connect_kernel(SceneView s, FrameView f, 
     uint32_t* work = f.counters + kConnectWorkBase + bounce;
     const uint32_t lane = lane_id();
     TraversalCounts cnt{0, 0};
+    uint32_t visibleCnt = 0;
     typename TravOf<TL>::type t;
     uint2 stack[kTraversalStack];
     uint32_t ray = 0, pathIx = 0;
@@ -1080,14 +1096,18 @@ __global__ void __launch_bounds__(128) connect_kernel(SceneView s, FrameView f, 
                     const float4 T4 = __ldcs(f.shadow + ray + 2 * cap);
                     float4 r = f.radiance[pathIx];
                     f.radiance[pathIx] = make_float4(r.x + T4.x, r.y + T4.y, r.z + T4.z, r.w);
+                    if (COUNT)
+                        ++visibleCnt;
                 }
                 alive = false;
             }
             active = __ballot_sync(kFull, alive);
         } while (uint32_t(__popc(active)) >= st.refillBelow);
     }
-    if (COUNT)
+    if (COUNT) {
         add_counts(f.traversal + 2, cnt);
+        add_count(f.traversal + 5, visibleCnt);
+    }
 }
 
 // Sums each pixel's samples in sample order into the accumulator and writes

@@ -28,7 +28,8 @@ constexpr uint32_t kNoAllocMaxPaths = 1u << 17;
 constexpr size_t kNoAllocPathBytes = 2 * 3 * 16 + 16 + 3 * 16 + 16;
 constexpr size_t kNoAllocTailBytes = 1024;  // counters, sample count, error word, traversal counters
 constexpr size_t kNoAllocScratchBytes = size_t(kNoAllocMaxPaths) * kNoAllocPathBytes + kNoAllocTailBytes;
-static_assert(kCounterWords * 4 + 4 + 4 <= 512 && 512 + 32 <= kNoAllocTailBytes, "scratch tail too small");
+static_assert(kCounterWords * 4 + 4 + 4 <= 512 && 512 + kTraversalCounters * 8 <= kNoAllocTailBytes,
+              "scratch tail too small");
 
 __device__ __align__(256) unsigned char g_noallocScratch[kNoAllocScratchBytes];
 
@@ -63,7 +64,7 @@ __global__ void noalloc_begin_kernel(uint32_t* counters, uint32_t* sampleCount, 
     if (threadIdx.x == 0) {
         *sampleCount = sc;
         *errorFlag = 0u;
-        for (int k = 0; k < 4; ++k)
+        for (uint32_t k = 0; k < kTraversalCounters; ++k)
             traversal[k] = 0ull;
     }
 }
