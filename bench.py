@@ -68,7 +68,8 @@ def parse():
     p.add_argument("--batch-count", type=int, default=64)
     p.add_argument("--no-extra", action="store_true",
                    help="plain workload: skip the batched and differentiation measurements after the timed region")
-    p.add_argument("--wave-paths", type=int, default=0, help="batched waves: paths per wave (0: library default)")
+    p.add_argument("--pool-paths", type=int, default=0,
+                   help="batched rendering: path slots of the continuous wavefront (0: library default)")
     p.add_argument("--no-ms1", action="store_true",
                    help="batch workload: skip the per-scene baseline at the reference's multi_sample = 1")
     return p.parse_args()
@@ -307,8 +308,8 @@ def config_dict(args, scene):
 
 def measure_batch(args, steps, warmup, with_ms1=True):
     """The batching mix: 64 seeded sphere scenes (1k-500k triangles, 128^2-1024^2, 4/16/64 spp,
-    1-16 lights, 6 bounces, RR from bounce 3) rendered by one wavefront (all waves in one CUDA
-    graph) against the same scenes rendered one after the other through tr_render_frame
+    1-16 lights, 6 bounces, RR from bounce 3) rendered by one continuous wavefront (a pool of path
+    slots refilled from a device cursor, the iterations a CUDA graph while loop) against the same scenes rendered one after the other through tr_render_frame
     (graph per frame, multi_sample = min(spp, 16), the reference's largest multi-sample)."""
     import torch
 
@@ -325,9 +326,9 @@ def measure_batch(args, steps, warmup, with_ms1=True):
     st = KernelSettings(multiSample=1, maxDepth=6, seed=1, rrStart=3)
     samples = sum(s.width * s.height * s.spp for s in scenes)
 
-    # batched: one wavefront, all waves replayed from one graph
+    # batched: one continuous wavefront, one graph launch
     t = time.perf_counter()
-    b = tr.BatchRenderer(scenes, wave_paths=args.wave_paths)
+    b = tr.BatchRenderer(scenes, pool_paths=args.pool_paths)
     build_s = time.perf_counter() - t
     info = b.Info()
     if args.profile:
@@ -393,6 +394,8 @@ def measure_batch(args, steps, warmup, with_ms1=True):
 
     plain_ms, plain_rays, launches, plain_clocks = per_scene(16)
     out = {
+        "iterations": bstats["iterations"],
+        "launches": bstats["launches"],
         "samples": samples,
         "batch_ms": batch_ms,
         "batch_rays": int(rays),
@@ -437,10 +440,10 @@ def run_batch(args):
         "data": "synthetic",
         "config": {"workload": f"{args.batch_count} sphere scenes, {info['triangle_count']} tris, "
                                f"{info['pixel_count']} pixels, {samples} samples, 6 bounces, RR from 3",
-                   "waves": info["wave_count"], "wave_paths": info["wave_paths"],
+                   "pool_paths": info["pool_paths"], "iterations": m["iterations"],
                    "l2": "flushed before each timed render (256 MiB write)"},
         "mrays_per_s": round(m["batch_rays"] / (batch_ms / 1e3) / 1e6, 1),
-        "gpu_launches": info["launches"],
+        "gpu_launches": m["launches"],
         **{k: m.get(k) for k in ("per_scene", "per_scene_ms1", "speedup_vs_per_scene", "speedup_vs_per_scene_ms1",
                                  "rays_per_scene", "scene_generation_s", "batch_build_s", "clocks")},
         "rays_batch": m["batch_rays"],
@@ -841,8 +844,9 @@ def main():
             "batched_mrays_per_s": round(m["batch_rays"] / (m["batch_ms"] / 1e3) / 1e6, 1),
             "per_scene_mrays_per_s": m["per_scene"]["mrays_per_s"],
             "samples": m["samples"],
-            "waves": m["info"]["wave_count"],
-            "gpu_launches": m["info"]["launches"],
+            "iterations": m["iterations"],
+            "pool_paths": m["info"]["pool_paths"],
+            "gpu_launches": m["launches"],
             "workload": f"{args.batch_count} sphere scenes ({m['info']['triangle_count']} tris, "
                         f"{m['info']['pixel_count']} pixels, 4/16/64 spp, 6 bounces, RR from 3); per scene: "
                         f"tr_render_frame graph frames at multi_sample min(spp, 16)",

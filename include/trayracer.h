@@ -523,17 +523,21 @@ tr_status tr_autotune(void* ctx, void* stream, uint32_t flags, tr_tune_report* r
 
 /* ---- batched rendering ----
  * Many independent scenes of uneven triangle count, resolution and sample
- * count rendered by one wavefront. No counterpart in the reference (one
- * DeviceRenderer renders one scene, Tracer/Renderer/DeviceRenderer.cpp:97-133);
- * the per-stage kernels are the ones behind tr_extend / tr_shade /
- * tr_connect. Each item's scene gets its own BVH; the buffers are
- * concatenated on the device and all items' paths run through the same
- * launches in waves of at most wave_paths paths (0: 2^25), made of
- * consecutive (item, sample) units. A path's random numbers are keyed as in
- * tr_render_frame (pixel, sample, bounce, seed), so an item whose samples fit
- * in one wave renders the image tr_render_frame gives for that scene with
- * multi_sample = spp from a reset accumulator (to a few ulps: the batch
- * kernels are separate instances the compiler may contract differently). */
+ * count rendered by one continuous wavefront. No counterpart in the reference
+ * (one DeviceRenderer renders one scene with a host bounce loop,
+ * Tracer/Renderer/DeviceRenderer.cpp:97-133); the per-stage kernels are the
+ * ones behind tr_extend / tr_shade / tr_connect. Each item's scene gets its
+ * own BVH; the buffers are concatenated on the device. All items' samples are
+ * fed from a device cursor into a pool of pool_paths path slots (0: 2^25):
+ * every iteration traces the paths carried over from the last one and starts
+ * new samples in the slots that finished paths left, so the pool stays full
+ * until the last samples drain. With use_graph the iterations run as a CUDA
+ * graph while loop whose condition the device sets. A path's random numbers
+ * are keyed as in tr_render_frame (pixel, sample, bounce, seed) and each
+ * pixel's samples are summed in sample order, so every item renders the image
+ * tr_render_frame gives for that scene with multi_sample = spp from a reset
+ * accumulator (to a few ulps: the batch kernels are separate instances the
+ * compiler may contract differently). */
 typedef struct tr_batch_item {
     const tr_scene_desc* scene;     /* read during tr_batch_create only */
     tr_camera camera;
@@ -545,19 +549,19 @@ typedef struct tr_batch_item {
 
 typedef struct tr_batch_info {
     uint32_t item_count;
-    uint32_t wave_count;
+    uint32_t round_count;           /* item ranges that share the per-sample radiance buffer (2^30 samples) */
     uint64_t path_count;            /* sum of width * height * spp */
     uint64_t pixel_count;           /* sum of width * height */
     uint64_t triangle_count;
     uint64_t device_bytes;
-    uint32_t wave_paths;            /* largest wave */
-    uint32_t launches;              /* kernels launched by one tr_batch_render (last settings) */
+    uint32_t pool_paths;            /* path slots of the wavefront */
+    uint32_t reserved;
     float build_time_ms;            /* host flattening + BVH builds */
     float upload_time_ms;
 } tr_batch_info;
 
 typedef struct tr_batch_statistics {
-    uint64_t extend_rays;           /* over all waves and bounces of the last render */
+    uint64_t extend_rays;           /* over all iterations of the last render */
     uint64_t shadow_rays;
     uint64_t hit_rays;
     float render_time_ms;           /* CUDA events around the last render */
@@ -566,12 +570,15 @@ typedef struct tr_batch_statistics {
     uint64_t traversal_extend_tris;
     uint64_t traversal_connect_nodes;
     uint64_t traversal_connect_tris;
+    uint32_t iterations;            /* wavefront iterations that traced rays */
+    uint32_t launches;              /* kernels of the last render (4 per iteration, per round 2 + 4) */
 } tr_batch_statistics;
 
 /* Builds and uploads all items (host threads build the BVHs). Items are
- * one-mesh scenes (instance_count 0). TR_ERR_LIMIT when an item's width *
- * height exceeds wave_paths. */
-tr_status tr_batch_create(const tr_config* config, const tr_batch_item* items, uint32_t count, uint64_t wave_paths,
+ * one-mesh scenes (instance_count 0). Device memory: 160 B per path slot,
+ * 16 B per sample of the largest round, 32 B per pixel. TR_ERR_LIMIT when an
+ * item has more than 2^30 samples or pool_paths >= 2^28. */
+tr_status tr_batch_create(const tr_config* config, const tr_batch_item* items, uint32_t count, uint64_t pool_paths,
                           void** out_batch);
 tr_status tr_batch_destroy(void* batch);
 const char* tr_batch_last_error(void* batch);
@@ -579,8 +586,9 @@ tr_status tr_batch_get_info(void* batch, tr_batch_info* info);
 /* Renders every item's spp samples from a zeroed accumulator. settings:
  * max_depth, seed, ray_epsilon, rr_start, max_color as for tr_set_settings;
  * multi_sample is ignored; TR_FLAG_REFERENCE_SAMPLING, TR_FLAG_WRITE_AOVS and
- * TR_FLAG_REFERENCE_DRAW_RTL are rejected. use_graph: all waves replay from
- * one CUDA graph, captured again when the settings change. */
+ * TR_FLAG_REFERENCE_DRAW_RTL are rejected. use_graph: one CUDA graph (a while
+ * loop per round), captured again when the settings change; without it the
+ * host runs the iterations, reading the queue length back after each. */
 tr_status tr_batch_render(void* batch, void* stream, const tr_kernel_settings* settings, int32_t use_graph);
 tr_status tr_batch_get_statistics(void* batch, tr_batch_statistics* stats);
 /* Device pointer to an item's colors (float4 per pixel, row-major). */

@@ -1,10 +1,12 @@
 """Batched rendering (tr_batch_*): many scenes of different size, resolution and
-sample count in one wavefront, checked against rendering each scene on its own
-through tr_render_frame. Random numbers are keyed by (pixel, sample, bounce,
-seed) in both and each item keeps its own BVH, so every path takes the same
-decisions; the batch kernels are separate template instances whose multiply-adds
-the compiler may contract differently, so images agree to a few ulps (2e-6
-relative) when the accumulation order is the same."""
+sample count in one continuous wavefront (a pool of path slots refilled with new
+samples as paths end), checked against rendering each scene on its own through
+tr_render_frame with multi_sample = spp. Random numbers are keyed by (pixel,
+sample, bounce, seed) in both, each item keeps its own BVH and each pixel's
+samples are summed in sample order, so every path takes the same decisions and
+the images agree to a few ulps (2e-6 relative: the batch kernels are separate
+template instances whose multiply-adds the compiler may contract differently),
+whatever the pool size."""
 import numpy as np
 import pytest
 
@@ -51,16 +53,23 @@ def _single(scene, spp, st, frames=1):
     return img, rays
 
 
-def test_batch_equals_single_scene_renders():
+@pytest.mark.parametrize("pool", [0, 5000, 700])
+def test_batch_equals_single_scene_renders(pool):
+    """Default pool (larger than the batch: one iteration per bounce), and pools smaller than
+    one item's pixels (many iterations, paths of different bounces in one queue)."""
     scenes = _scenes()
     st = _settings()
-    with tr.BatchRenderer(scenes) as b:
+    with tr.BatchRenderer(scenes, pool_paths=pool) as b:
         info = b.Info()
-        assert info["wave_count"] == 1 and info["item_count"] == len(scenes)
-        assert info["path_count"] == sum(s.width * s.height * s.spp for s in scenes)
+        total = sum(s.width * s.height * s.spp for s in scenes)
+        assert info["round_count"] == 1 and info["item_count"] == len(scenes)
+        assert info["path_count"] == total
+        assert info["pool_paths"] == (min(pool, total) if pool else total)
         b.Render(st)
         stats = b.Statistics()
         assert stats["device_error"] == 0
+        if pool:
+            assert stats["iterations"] > total // pool
         rays = 0
         for i, s in enumerate(scenes):
             want, n = _single(s, s.spp, st)
@@ -68,35 +77,26 @@ def test_batch_equals_single_scene_renders():
             got = b.Image(i)
             np.testing.assert_allclose(got, want, rtol=2e-6, atol=1e-7)
         assert stats["extend_rays"] + stats["shadow_rays"] == rays
+        assert stats["launches"] == 2 + 4 * (stats["iterations"] + 1)
 
 
-def test_batch_split_into_waves_equals_frame_sequence():
-    # one sample of one item per wave: the batch adds samples in the order a
-    # sequence of one-sample frames does
+def test_batch_graph_equals_eager():
+    # the graph's device-driven while loop and the host-driven iterations run the same launches
     scenes = _scenes(res=(32, 24))
     st = _settings(seed=9)
-    with tr.BatchRenderer(scenes, wave_paths=32 * 24) as b:
-        assert b.Info()["wave_count"] == sum(s.spp for s in scenes)
+    with tr.BatchRenderer(scenes, pool_paths=1000) as b:
         b.Render(st, use_graph=True)
         imgs = [b.Image(i).copy() for i in range(len(scenes))]
-        b.Render(st, use_graph=False)  # eager replay of the same launches
-        for i, s in enumerate(scenes):
+        g = b.Statistics()
+        b.Render(st, use_graph=False)
+        e = b.Statistics()
+        for i in range(len(scenes)):
             np.testing.assert_array_equal(b.Image(i), imgs[i])
-            want, _ = _single(s, s.spp, st, frames=s.spp)
-            np.testing.assert_allclose(imgs[i], want, rtol=2e-6, atol=1e-7)
-
-
-def test_batch_uneven_waves_close_to_single():
-    # waves that cut items at arbitrary sample counts: same samples, another summation order
-    scenes = _scenes()
-    st = _settings(seed=4)
-    with tr.BatchRenderer(scenes, wave_paths=5000) as b:
-        assert b.Info()["wave_count"] > 2
-        b.Render(st)
-        for i, s in enumerate(scenes):
-            want, _ = _single(s, s.spp, st)
-            got = b.Image(i)
-            assert np.allclose(got, want, rtol=1e-5, atol=1e-6)
+        assert (g["iterations"], g["extend_rays"], g["shadow_rays"]) == (e["iterations"], e["extend_rays"],
+                                                                          e["shadow_rays"])
+        b.Render(st, use_graph=True)  # replay
+        for i in range(len(scenes)):
+            np.testing.assert_array_equal(b.Image(i), imgs[i])
 
 
 def test_batch_counting_and_errors():
@@ -115,5 +115,5 @@ def test_batch_counting_and_errors():
         assert lib.tr_batch_download(b._b, None, len(scenes), buf.ctypes.data, buf.nbytes) == 1
         assert lib.tr_batch_download(b._b, None, 0, buf.ctypes.data, buf.nbytes) == 1  # buffer too small
     with pytest.raises(tr.TracerError) as e:
-        tr.BatchRenderer(scenes, wave_paths=100)  # an item larger than a wave
+        tr.BatchRenderer(scenes, pool_paths=1 << 28)  # more path slots than path indices
     assert e.value.status == 6

@@ -253,13 +253,13 @@ class BatchItem(C.Structure):
 class BatchInfo(C.Structure):
     _fields_ = [
         ("item_count", C.c_uint32),
-        ("wave_count", C.c_uint32),
+        ("round_count", C.c_uint32),
         ("path_count", C.c_uint64),
         ("pixel_count", C.c_uint64),
         ("triangle_count", C.c_uint64),
         ("device_bytes", C.c_uint64),
-        ("wave_paths", C.c_uint32),
-        ("launches", C.c_uint32),
+        ("pool_paths", C.c_uint32),
+        ("reserved", C.c_uint32),
         ("build_time_ms", C.c_float),
         ("upload_time_ms", C.c_float),
     ]
@@ -276,6 +276,8 @@ class BatchStatistics(C.Structure):
         ("traversal_extend_tris", C.c_uint64),
         ("traversal_connect_nodes", C.c_uint64),
         ("traversal_connect_tris", C.c_uint64),
+        ("iterations", C.c_uint32),
+        ("launches", C.c_uint32),
     ]
 
 

@@ -1,19 +1,23 @@
 // Batched rendering: many independent scenes of uneven triangle count,
-// resolution and sample count rendered by one wavefront. No counterpart in
-// the reference, whose DeviceRenderer renders one scene at a time
-// (Tracer/Renderer/DeviceRenderer.cpp:97-133).
+// resolution and sample count rendered by one continuous wavefront. No
+// counterpart in the reference, whose DeviceRenderer renders one scene at a
+// time with a host bounce loop (Tracer/Renderer/DeviceRenderer.cpp:97-133,
+// with a blocking counter download per bounce at :255-257).
 //
 // Every item's scene is flattened and given its own 8-wide BVH (built on host
 // threads, one item per thread); the buffers are concatenated into one device
 // arena with node, triangle, material and light indices rebased, so a ray
-// only needs its item's root node. The items' paths are cut into waves of at
-// most `wave_paths` paths made of consecutive (item, sample) units; each wave
-// runs the same generate / extend / shade / connect launches as one scene,
-// with the item of a path looked up from the wave's segment table, and adds
-// its samples to the batch accumulator. Two waves are in flight at a time, on
-// two streams with their own buffers, so one wave's short late bounces overlap
-// the other wave's long early ones; only the waves' accumulator updates are
-// ordered. One tr_batch_render replays all waves from one CUDA graph.
+// only needs its item's root node. All items' samples are numbered (a sample
+// id: item by item, pixel by pixel, the samples of a pixel consecutive) and
+// fed to a pool of path slots from a device cursor: each iteration traces the
+// paths the last one carried over plus new samples in the slots that ended
+// paths left, so the pool stays full until the last samples drain, with no
+// per-scene or per-wave tail. The iterations run as a CUDA graph while loop
+// whose condition a device plan kernel sets (queue not empty), so one
+// tr_batch_render is one graph launch with no host round trip. Each sample's
+// radiance lands in a per-sample buffer, summed per pixel in sample order at
+// the end; items whose samples exceed that buffer's budget go to the next
+// round (the rounds run one after the other in the same graph).
 #include <cuda_runtime.h>
 
 #include <algorithm>
@@ -35,14 +39,17 @@ namespace {
 
 using namespace tr;
 
-constexpr uint64_t kDefaultWavePaths = 1ull << 25;
-constexpr uint32_t kWaveSets = 2;  // waves in flight, each with its own buffers and stream
+constexpr uint64_t kDefaultPoolPaths = 1ull << 25;
+// Samples of one round: the per-sample radiance buffer holds this many float4.
+constexpr uint64_t kRoundSamples = 1ull << 30;
 
-struct Wave {
-    uint32_t segmentOffset = 0;
-    uint32_t segmentCount = 0;
-    uint32_t paths = 0;
-    uint32_t pixels = 0;
+// Consecutive items whose samples share one per-sample radiance buffer.
+struct Round {
+    uint32_t firstItem = 0;
+    uint32_t itemCount = 0;
+    uint32_t samples = 0;     // sample ids [0, samples) of the round
+    uint32_t pixelBegin = 0;  // the round's pixels in the batch accumulator
+    uint32_t pixelEnd = 0;
 };
 
 struct ItemBuild {
@@ -60,16 +67,14 @@ struct Batch {
     void* sceneArena = nullptr;
     void* frameArena = nullptr;
     SceneView scene{};
-    FrameView frame[kWaveSets]{};    // wave buffers of each set; segments, counts and counters set per wave
-    cudaStream_t lanes[kWaveSets] = {};
-    cudaEvent_t evFork = nullptr;
-    std::vector<cudaEvent_t> evFinal; // per wave: its samples are in the accumulator
-    std::vector<Wave> waves;
+    FrameView frame{};               // pool buffers; items, item count and state set per round
+    std::vector<Round> rounds;
     std::vector<BatchItem> items;
-    BatchSegment* segments = nullptr;
-    uint32_t* counters = nullptr;    // kCounterWords per wave
+    BatchItem* itemsDevice = nullptr;
+    BatchState* states = nullptr;    // one per round
     float4* accumulator = nullptr;
     float4* colors = nullptr;
+    uint32_t pool = 0;               // path slots
     LaunchShape shape{};
     tr_batch_info info{};
 
@@ -78,7 +83,6 @@ struct Batch {
     cudaGraphExec_t graphExec = nullptr;
     bool graphValid = false;
     cudaEvent_t evStart = nullptr, evStop = nullptr;
-    bool timed = false;
     Settings lastSettings{};
     bool rendered = false;
 };
@@ -111,12 +115,20 @@ tr_status cuda_fail(Batch* b, cudaError_t e, const char* what)
 
 inline size_t align256(size_t x) { return (x + 255) & ~size_t(255); }
 
-void release(Batch* b)
+void release_graph(Batch* b)
 {
     if (b->graphExec)
         cudaGraphExecDestroy(b->graphExec);
     if (b->graph)
         cudaGraphDestroy(b->graph);
+    b->graphExec = nullptr;
+    b->graph = nullptr;
+    b->graphValid = false;
+}
+
+void release(Batch* b)
+{
+    release_graph(b);
     if (b->evStart)
         cudaEventDestroy(b->evStart);
     if (b->evStop)
@@ -125,14 +137,6 @@ void release(Batch* b)
         cudaFree(b->sceneArena);
     if (b->frameArena)
         cudaFree(b->frameArena);
-    for (cudaEvent_t e : b->evFinal)
-        if (e)
-            cudaEventDestroy(e);
-    if (b->evFork)
-        cudaEventDestroy(b->evFork);
-    for (cudaStream_t l : b->lanes)
-        if (l)
-            cudaStreamDestroy(l);
     if (b->stream)
         cudaStreamDestroy(b->stream);
 }
@@ -170,96 +174,68 @@ std::vector<ItemBuild> build_items(const tr_batch_item* items, uint32_t count, u
     return out;
 }
 
-// Consecutive (item, sample) units into waves of at most `cap` paths.
-void plan_waves(const std::vector<BatchItem>& items, uint64_t cap, std::vector<Wave>& waves,
-                std::vector<BatchSegment>& segs)
+// Items in order into rounds of at most kRoundSamples samples; sample ids
+// (BatchItem::sampleBase) count from each round's first item.
+bool plan_rounds(std::vector<BatchItem>& items, std::vector<Round>& rounds)
 {
-    Wave w{};
-    w.segmentOffset = 0;
-    auto close = [&]() {
-        if (w.segmentCount) {
-            waves.push_back(w);
-            w = Wave{};
-            w.segmentOffset = uint32_t(segs.size());
-        }
-    };
+    Round r{};
+    uint64_t samples = 0;
     for (uint32_t i = 0; i < items.size(); ++i) {
-        const uint64_t px = uint64_t(items[i].width) * items[i].height;
-        uint32_t done = 0;
-        while (done < items[i].spp) {
-            uint64_t fit = (cap - w.paths) / px;
-            if (fit == 0) {
-                close();
-                fit = cap / px;
-            }
-            const uint32_t k = uint32_t(std::min<uint64_t>(fit, items[i].spp - done));
-            BatchSegment sg{};
-            sg.pathBase = w.paths;
-            sg.pixelBase = w.pixels;
-            sg.item = i;
-            sg.sampleBase = done;
-            sg.pixels = uint32_t(px);
-            sg.samples = k;
-            segs.push_back(sg);
-            w.segmentCount++;
-            w.paths += uint32_t(k * px);
-            w.pixels += uint32_t(px);
-            done += k;
+        const uint64_t n = uint64_t(items[i].width) * items[i].height * items[i].spp;
+        if (n > kRoundSamples)
+            return false;
+        if (samples + n > kRoundSamples) {
+            r.samples = uint32_t(samples);
+            rounds.push_back(r);
+            r = Round{};
+            r.firstItem = i;
+            r.pixelBegin = items[i].pixelBase;
+            samples = 0;
         }
+        items[i].sampleBase = uint32_t(samples);
+        samples += n;
+        r.itemCount++;
+        r.pixelEnd = items[i].pixelBase + items[i].width * items[i].height;
     }
-    close();
+    if (r.itemCount) {
+        r.samples = uint32_t(samples);
+        rounds.push_back(r);
+    }
+    return true;
 }
 
-FrameView wave_view(const Batch* b, uint32_t w)
+FrameView round_view(const Batch* b, uint32_t k)
 {
-    FrameView f = b->frame[w % kWaveSets];
-    const Wave& wv = b->waves[w];
-    f.segments = b->segments + wv.segmentOffset;
-    f.segmentCount = wv.segmentCount;
-    f.pathCount = wv.paths;
-    f.counters = b->counters + size_t(w) * kCounterWords;
+    FrameView f = b->frame;
+    const Round& r = b->rounds[k];
+    f.items = b->itemsDevice + r.firstItem;
+    f.itemCount = r.itemCount;
+    f.batch = b->states + k;
     return f;
 }
 
-cudaError_t enqueue(Batch* b, const Settings& st, cudaStream_t s)
+// One iteration of round k: plan, extend (carried paths + new samples), shade,
+// connect.
+cudaError_t enqueue_iteration(Batch* b, uint32_t k, const Settings& st, cudaGraphConditionalHandle loop,
+                              bool useLoop, cudaStream_t s)
 {
-    cudaError_t e = cudaMemsetAsync(b->accumulator, 0, size_t(b->info.pixel_count) * sizeof(float4), s);
+    const FrameView f = round_view(b, k);  // each path uses its item's camera
+    const uint64_t bound = uint64_t(b->rounds[k].samples) * st.maxDepth + 4u;
+    const uint32_t limit = bound < 0xffffffffull ? uint32_t(bound) : 0xffffffffu;
+    cudaError_t e = launch_batch_plan(f.batch, b->pool, b->rounds[k].samples, limit, f.errorFlag, loop, useLoop, s);
     if (e == cudaSuccess)
-        e = cudaMemsetAsync(b->counters, 0, b->waves.size() * kCounterWords * sizeof(uint32_t), s);
-    const Camera noCamera{};  // each path uses its item's camera
+        e = launch_extend(b->scene, f, st, 0u, b->shape, s, nullptr);
     if (e == cudaSuccess)
-        e = cudaEventRecord(b->evFork, s);
-    for (uint32_t k = 0; e == cudaSuccess && k < kWaveSets; ++k)
-        e = cudaStreamWaitEvent(b->lanes[k], b->evFork, 0);
-    for (uint32_t w = 0; e == cudaSuccess && w < b->waves.size(); ++w) {
-        // a set's stream runs its waves in order, so a wave reuses the buffers of the
-        // wave two before it only after that one finished
-        cudaStream_t ls = b->lanes[w % kWaveSets];
-        const FrameView f = wave_view(b, w);
-        // the camera rays are made inside the first extend launch
-        for (uint32_t bounce = 0; e == cudaSuccess && bounce < st.maxDepth; ++bounce) {
-            e = launch_extend(b->scene, f, st, bounce, b->shape, ls, &noCamera);
-            if (e == cudaSuccess)
-                e = launch_shade(b->scene, f, st, bounce, b->shape, ls);
-            if (e == cudaSuccess)
-                e = launch_connect(b->scene, f, st, bounce, b->shape, ls);
-        }
-        // accumulator updates in wave order: an item split over two waves adds to the same pixels
-        if (e == cudaSuccess && w > 0)
-            e = cudaStreamWaitEvent(ls, b->evFinal[w - 1], 0);
-        if (e == cudaSuccess)
-            e = launch_batch_finalize(f, b->waves[w].pixels, ls);
-        if (e == cudaSuccess)
-            e = cudaEventRecord(b->evFinal[w], ls);
-    }
-    // the last wave's accumulator update follows every earlier one and its own wave
-    if (e == cudaSuccess && !b->waves.empty())
-        e = cudaStreamWaitEvent(s, b->evFinal[b->waves.size() - 1], 0);
-    for (uint32_t k = 1; e == cudaSuccess && k < kWaveSets && k < b->waves.size(); ++k)
-        e = cudaStreamWaitEvent(s, b->evFinal[b->waves.size() - 1 - k], 0);
+        e = launch_shade(b->scene, f, st, 0u, b->shape, s);
     if (e == cudaSuccess)
-        e = launch_batch_resolve(b->accumulator, b->colors, uint32_t(b->info.pixel_count), s);
+        e = launch_connect(b->scene, f, st, 0u, b->shape, s);
     return e;
+}
+
+// Starting state of a round: everything zero (the plan kernel sets its end).
+cudaError_t enqueue_round_start(Batch* b, uint32_t k, cudaStream_t s)
+{
+    return cudaMemsetAsync(b->states + k, 0, sizeof(BatchState), s);
 }
 
 } // namespace
@@ -267,22 +243,22 @@ cudaError_t enqueue(Batch* b, const Settings& st, cudaStream_t s)
 extern "C" {
 
 tr_status tr_batch_create(const tr_config* config, const tr_batch_item* items, uint32_t count,
-                          uint64_t wave_paths, void** out_batch)
+                          uint64_t pool_paths, void** out_batch)
 {
     if (!config || !out_batch || !items || count == 0)
         return TR_ERR_INVALID_ARGUMENT;
     *out_batch = nullptr;
     if (config->abi_version != TR_ABI_VERSION)
         return TR_ERR_INVALID_ARGUMENT;
-    const uint64_t cap = wave_paths ? wave_paths : kDefaultWavePaths;
-    if (cap >= TR_MAX_PATHS)
+    const uint64_t poolCap = pool_paths ? pool_paths : kDefaultPoolPaths;
+    if (poolCap >= TR_MAX_PATHS)
         return TR_ERR_LIMIT;
     uint64_t pixels = 0, paths = 0;
     for (uint32_t i = 0; i < count; ++i) {
         const tr_batch_item& it = items[i];
         if (!it.scene || it.width == 0 || it.height == 0 || it.spp == 0)
             return TR_ERR_INVALID_ARGUMENT;
-        if (uint64_t(it.width) * it.height > cap)
+        if (uint64_t(it.width) * it.height * it.spp > kRoundSamples)
             return TR_ERR_LIMIT;
         if (!validate_scene(*it.scene).empty() || it.scene->instance_count || it.scene->material_textures)
             return TR_ERR_INVALID_ARGUMENT;  // one-mesh untextured scenes only
@@ -304,13 +280,9 @@ tr_status tr_batch_create(const tr_config* config, const tr_batch_item* items, u
         return st;
     };
     // a blocking stream, like the context's: work on it is ordered with the legacy default stream
-    if (cudaStreamCreate(&b->stream) != cudaSuccess ||
-        cudaEventCreate(&b->evStart) != cudaSuccess || cudaEventCreate(&b->evStop) != cudaSuccess ||
-        cudaEventCreateWithFlags(&b->evFork, cudaEventDisableTiming) != cudaSuccess)
+    if (cudaStreamCreate(&b->stream) != cudaSuccess || cudaEventCreate(&b->evStart) != cudaSuccess ||
+        cudaEventCreate(&b->evStop) != cudaSuccess)
         return bail(TR_ERR_CUDA);
-    for (uint32_t k = 0; k < kWaveSets; ++k)
-        if (cudaStreamCreateWithFlags(&b->lanes[k], cudaStreamNonBlocking) != cudaSuccess)
-            return bail(TR_ERR_CUDA);
 
     const auto t0 = std::chrono::steady_clock::now();
     std::vector<ItemBuild> built = build_items(items, count, 3u);
@@ -380,9 +352,11 @@ tr_status tr_batch_create(const tr_config* config, const tr_batch_item* items, u
     built.clear();
     const float4 identity[3] = {make_float4(1.f, 0.f, 0.f, 0.f), make_float4(0.f, 1.f, 0.f, 0.f),
                                 make_float4(0.f, 0.f, 1.f, 0.f)};
-    std::vector<Wave> waves;
-    std::vector<BatchSegment> segs;
-    plan_waves(b->items, cap, waves, segs);
+    if (!plan_rounds(b->items, b->rounds))
+        return bail(TR_ERR_LIMIT);
+    uint32_t roundSamples = 0;
+    for (const Round& r : b->rounds)
+        roundSamples = std::max(roundSamples, r.samples);
     const auto t1 = std::chrono::steady_clock::now();
 
     // scene arena
@@ -435,81 +409,67 @@ tr_status tr_batch_create(const tr_config* config, const tr_batch_item* items, u
     sv.nodeCount = uint32_t(nodes.size());
     sv.triCount = uint32_t(tris.size());
 
-    // frame arena: wave buffers, batch accumulator and colors, tables
-    uint32_t capPaths = 0;
-    for (const Wave& w : waves)
-        capPaths = std::max(capPaths, w.paths);
-    const size_t capN = capPaths;
+    // frame arena: the pool's queues, the per-sample radiance of a round, the
+    // batch accumulator and colors, items and round states
+    const uint32_t pool = uint32_t(std::min<uint64_t>(poolCap, std::max<uint64_t>(1, roundSamples)));
+    const size_t capN = pool;
     off = 0;
-    size_t oS0[kWaveSets], oS1[kWaveSets], oHits[kWaveSets], oShadow[kWaveSets], oRad[kWaveSets];
-    const uint32_t sets = uint32_t(std::min<size_t>(kWaveSets, waves.size()));
-    for (uint32_t k = 0; k < sets; ++k) {
-        oS0[k] = take(3 * capN * sizeof(float4));
-        oS1[k] = take(3 * capN * sizeof(float4));
-        oHits[k] = take(capN * sizeof(uint4));
-        oShadow[k] = take(3 * capN * sizeof(float4));
-        oRad[k] = take(capN * sizeof(float4));
-    }
+    const size_t oS0 = take(3 * capN * sizeof(float4));
+    const size_t oS1 = take(3 * capN * sizeof(float4));
+    const size_t oHits = take(capN * sizeof(uint4));
+    const size_t oShadow = take(3 * capN * sizeof(float4));
+    const size_t oRad = take(size_t(roundSamples) * sizeof(float4));
     const size_t oAcc = take(pixels * sizeof(float4));
     const size_t oCol = take(pixels * sizeof(float4));
-    const size_t oCnt = take(waves.size() * kCounterWords * sizeof(uint32_t));
-    const size_t oSeg = take(segs.size() * sizeof(BatchSegment));
     const size_t oItems = take(b->items.size() * sizeof(BatchItem));
+    const size_t oStates = take(b->rounds.size() * sizeof(BatchState));
     const size_t oWords = take(2 * sizeof(uint32_t));
-    const size_t oTrav = take(4 * sizeof(unsigned long long));
+    const size_t oTrav = take(kTraversalCounters * sizeof(unsigned long long));
     e = cudaMalloc(&b->frameArena, off);
     if (e != cudaSuccess) {
         cudaGetLastError();
         return bail(e == cudaErrorMemoryAllocation ? TR_ERR_OUT_OF_MEMORY : TR_ERR_CUDA);
     }
     char* fb = static_cast<char*>(b->frameArena);
-    if (cudaMemset(fb, 0, off) != cudaSuccess ||
-        cudaMemcpy(fb + oSeg, segs.data(), segs.size() * sizeof(BatchSegment), cudaMemcpyHostToDevice) !=
-            cudaSuccess ||
+    if (cudaMemset(fb + oAcc, 0, oItems - oAcc) != cudaSuccess ||
+        cudaMemset(fb + oStates, 0, off - oStates) != cudaSuccess ||
         cudaMemcpy(fb + oItems, b->items.data(), b->items.size() * sizeof(BatchItem), cudaMemcpyHostToDevice) !=
             cudaSuccess)
         return bail(TR_ERR_CUDA);
-    FrameView f{};
+    FrameView& f = b->frame;
+    f = FrameView{};
+    f.state[0] = reinterpret_cast<float4*>(fb + oS0);
+    f.state[1] = reinterpret_cast<float4*>(fb + oS1);
+    f.hits = reinterpret_cast<uint4*>(fb + oHits);
+    f.shadow = reinterpret_cast<float4*>(fb + oShadow);
+    f.radiance = reinterpret_cast<float4*>(fb + oRad);
     f.accumulator = reinterpret_cast<float4*>(fb + oAcc);
     f.colors = reinterpret_cast<float4*>(fb + oCol);
     f.albedo = nullptr;
     f.normals = nullptr;
-    f.sampleCount = reinterpret_cast<uint32_t*>(fb + oWords);      // stays 0: samples are keyed per segment
+    f.sampleCount = reinterpret_cast<uint32_t*>(fb + oWords);  // stays 0: samples are keyed per item
     f.errorFlag = reinterpret_cast<uint32_t*>(fb + oWords) + 1;
     f.traversal = reinterpret_cast<unsigned long long*>(fb + oTrav);
-    f.capacity = capPaths;
+    f.capacity = pool;
     f.resX = 1;
     f.resY = 1;
-    f.items = reinterpret_cast<const BatchItem*>(fb + oItems);
-    for (uint32_t k = 0; k < kWaveSets; ++k) {
-        const uint32_t j = k < sets ? k : 0u;
-        b->frame[k] = f;
-        b->frame[k].state[0] = reinterpret_cast<float4*>(fb + oS0[j]);
-        b->frame[k].state[1] = reinterpret_cast<float4*>(fb + oS1[j]);
-        b->frame[k].hits = reinterpret_cast<uint4*>(fb + oHits[j]);
-        b->frame[k].shadow = reinterpret_cast<float4*>(fb + oShadow[j]);
-        b->frame[k].radiance = reinterpret_cast<float4*>(fb + oRad[j]);
-    }
-    b->evFinal.assign(waves.size(), nullptr);
-    for (cudaEvent_t& ev : b->evFinal)
-        if (cudaEventCreateWithFlags(&ev, cudaEventDisableTiming) != cudaSuccess)
-            return bail(TR_ERR_CUDA);
-    b->segments = reinterpret_cast<BatchSegment*>(fb + oSeg);
-    b->counters = reinterpret_cast<uint32_t*>(fb + oCnt);
+    f.pathCount = pool;
+    b->itemsDevice = reinterpret_cast<BatchItem*>(fb + oItems);
+    b->states = reinterpret_cast<BatchState*>(fb + oStates);
     b->accumulator = f.accumulator;
     b->colors = f.colors;
-    b->waves = waves;
-    b->shape = default_launch_shape(b->device, capPaths);
+    b->pool = pool;
+    b->shape = default_launch_shape(b->device, pool);
     const auto t2 = std::chrono::steady_clock::now();
 
     tr_batch_info& in = b->info;
     in.item_count = count;
-    in.wave_count = uint32_t(waves.size());
+    in.round_count = uint32_t(b->rounds.size());
     in.path_count = paths;
     in.pixel_count = pixels;
     in.triangle_count = triTotal;
     in.device_bytes = sceneBytes + off;
-    in.wave_paths = capPaths;
+    in.pool_paths = pool;
     in.build_time_ms = std::chrono::duration<float, std::milli>(t1 - t0).count();
     in.upload_time_ms = std::chrono::duration<float, std::milli>(t2 - t1).count();
     *out_batch = b;
@@ -538,11 +498,110 @@ tr_status tr_batch_get_info(void* batch, tr_batch_info* out)
 {
     if (!batch || !out)
         return TR_ERR_INVALID_ARGUMENT;
-    Batch* b = static_cast<Batch*>(batch);
-    *out = b->info;
-    out->launches = uint32_t(b->waves.size()) * (1u + 3u * b->lastSettings.maxDepth) + 1u;
+    *out = static_cast<Batch*>(batch)->info;
     return TR_OK;
 }
+
+} // extern "C"
+
+namespace {
+
+// Captures body() on the batch's stream into graph `into` after `deps`; *tail
+// (optional) gets the last node captured.
+template <class Body>
+cudaError_t capture_into(Batch* b, cudaGraph_t into, const cudaGraphNode_t* deps, size_t nDeps, Body&& body,
+                         cudaGraphNode_t* tail)
+{
+    cudaError_t e =
+        cudaStreamBeginCaptureToGraph(b->stream, into, deps, nullptr, nDeps, cudaStreamCaptureModeThreadLocal);
+    if (e != cudaSuccess)
+        return e;
+    e = body();
+    if (e == cudaSuccess && tail) {
+        cudaStreamCaptureStatus cs;
+        const cudaGraphNode_t* d = nullptr;
+        size_t n = 0;
+        e = cudaStreamGetCaptureInfo(b->stream, &cs, nullptr, nullptr, &d, nullptr, &n);
+        if (e == cudaSuccess)
+            *tail = n ? d[n - 1] : nullptr;
+    }
+    cudaGraph_t out = into;
+    const cudaError_t ee = cudaStreamEndCapture(b->stream, &out);
+    return e != cudaSuccess ? e : ee;
+}
+
+// The batch as one graph: per round its start, a while loop over iterations
+// whose condition the plan kernel sets, and its finalize.
+tr_status capture_graph(Batch* b, const Settings& st)
+{
+    release_graph(b);
+    cudaGraph_t g = nullptr;
+    TR_BCUDA(b, cudaGraphCreate(&g, 0));
+    auto fail_graph = [&](cudaError_t e, const char* what) {
+        cudaGraphDestroy(g);
+        return cuda_fail(b, e, what);
+    };
+    cudaGraphNode_t last = nullptr;
+    for (uint32_t k = 0; k < b->rounds.size(); ++k) {
+        cudaGraphNode_t start = nullptr;
+        cudaError_t e = capture_into(b, g, last ? &last : nullptr, last ? 1 : 0,
+                                     [&]() { return enqueue_round_start(b, k, b->stream); }, &start);
+        if (e != cudaSuccess || !start)
+            return fail_graph(e != cudaSuccess ? e : cudaErrorUnknown, "batch graph: round start");
+        cudaGraphConditionalHandle loop;
+        e = cudaGraphConditionalHandleCreate(&loop, g, 1u, cudaGraphCondAssignDefault);
+        if (e != cudaSuccess)
+            return fail_graph(e, "cudaGraphConditionalHandleCreate");
+        cudaGraphNodeParams cp{};
+        cp.type = cudaGraphNodeTypeConditional;
+        cp.conditional.handle = loop;
+        cp.conditional.type = cudaGraphCondTypeWhile;
+        cp.conditional.size = 1;
+        cudaGraphNode_t whileNode = nullptr;
+        e = cudaGraphAddNode(&whileNode, g, &start, nullptr, 1, &cp);
+        if (e != cudaSuccess)
+            return fail_graph(e, "cudaGraphAddNode(while)");
+        cudaGraph_t body = cp.conditional.phGraph_out[0];
+        e = capture_into(b, body, nullptr, 0, [&]() { return enqueue_iteration(b, k, st, loop, true, b->stream); },
+                         nullptr);
+        if (e != cudaSuccess)
+            return fail_graph(e, "batch graph: iteration");
+        const FrameView f = round_view(b, k);
+        const Round& r = b->rounds[k];
+        e = capture_into(b, g, &whileNode, 1,
+                         [&]() { return launch_batch_finalize(f, r.pixelBegin, r.pixelEnd, b->stream); }, &last);
+        if (e != cudaSuccess || !last)
+            return fail_graph(e != cudaSuccess ? e : cudaErrorUnknown, "batch graph: finalize");
+    }
+    b->graph = g;
+    TR_BCUDA(b, cudaGraphInstantiate(&b->graphExec, g, 0));
+    b->graphValid = true;
+    return TR_OK;
+}
+
+// Without a graph: the host runs the iterations of each round until a plan
+// finds nothing left to trace (one small read-back per iteration).
+tr_status enqueue_eager(Batch* b, const Settings& st, cudaStream_t s)
+{
+    for (uint32_t k = 0; k < b->rounds.size(); ++k) {
+        TR_BCUDA(b, enqueue_round_start(b, k, s));
+        while (true) {
+            TR_BCUDA(b, enqueue_iteration(b, k, st, cudaGraphConditionalHandle{}, false, s));
+            uint32_t queue = 0;
+            TR_BCUDA(b, cudaMemcpyAsync(&queue, &b->states[k].queue, sizeof(uint32_t), cudaMemcpyDeviceToHost, s));
+            TR_BCUDA(b, cudaStreamSynchronize(s));
+            if (queue == 0)
+                break;
+        }
+        const Round& r = b->rounds[k];
+        TR_BCUDA(b, launch_batch_finalize(round_view(b, k), r.pixelBegin, r.pixelEnd, s));
+    }
+    return TR_OK;
+}
+
+} // namespace
+
+extern "C" {
 
 tr_status tr_batch_render(void* batch, void* stream, const tr_kernel_settings* settings, int32_t use_graph)
 {
@@ -559,35 +618,25 @@ tr_status tr_batch_render(void* batch, void* stream, const tr_kernel_settings* s
     st.multiSample = 1;  // unused: each item renders its own spp
     cudaSetDevice(b->device);
     cudaStream_t s = stream ? static_cast<cudaStream_t>(stream) : b->stream;
+    if (use_graph && !(st.flags & TR_FLAG_COUNT_TRAVERSAL) &&
+        (!b->graphValid || std::memcmp(&st, &b->graphSettings, sizeof(Settings)) != 0)) {
+        // captured on the batch's own stream, which must be idle
+        TR_BCUDA(b, cudaStreamSynchronize(b->stream));
+        const tr_status cs = capture_graph(b, st);
+        if (cs != TR_OK)
+            return cs;
+        b->graphSettings = st;
+    }
     TR_BCUDA(b, cudaEventRecord(b->evStart, s));
+    TR_BCUDA(b, cudaMemsetAsync(b->frame.errorFlag, 0, sizeof(uint32_t), s));
     if (use_graph && !(st.flags & TR_FLAG_COUNT_TRAVERSAL)) {
-        if (!b->graphValid || std::memcmp(&st, &b->graphSettings, sizeof(Settings)) != 0) {
-            if (b->graphExec)
-                cudaGraphExecDestroy(b->graphExec);
-            if (b->graph)
-                cudaGraphDestroy(b->graph);
-            b->graphExec = nullptr;
-            b->graph = nullptr;
-            b->graphValid = false;
-            TR_BCUDA(b, cudaStreamBeginCapture(b->stream, cudaStreamCaptureModeThreadLocal));
-            const cudaError_t ec = enqueue(b, st, b->stream);
-            cudaGraph_t g = nullptr;
-            const cudaError_t ee = cudaStreamEndCapture(b->stream, &g);
-            if (ec != cudaSuccess || ee != cudaSuccess) {
-                if (g)
-                    cudaGraphDestroy(g);
-                return cuda_fail(b, ec != cudaSuccess ? ec : ee, "batch graph capture");
-            }
-            b->graph = g;
-            TR_BCUDA(b, cudaGraphInstantiate(&b->graphExec, g, 0));
-            b->graphSettings = st;
-            b->graphValid = true;
-        }
         TR_BCUDA(b, cudaGraphLaunch(b->graphExec, s));
     } else {
         if (st.flags & TR_FLAG_COUNT_TRAVERSAL)
-            TR_BCUDA(b, cudaMemsetAsync(b->frame[0].traversal, 0, 4 * sizeof(unsigned long long), s));
-        TR_BCUDA(b, enqueue(b, st, s));
+            TR_BCUDA(b, cudaMemsetAsync(b->frame.traversal, 0, kTraversalCounters * sizeof(unsigned long long), s));
+        const tr_status es = enqueue_eager(b, st, s);
+        if (es != TR_OK)
+            return es;
     }
     TR_BCUDA(b, cudaEventRecord(b->evStop, s));
     b->lastSettings = st;
@@ -604,21 +653,23 @@ tr_status tr_batch_get_statistics(void* batch, tr_batch_statistics* out)
         return fail(b, TR_ERR_NOT_READY, "no batch rendered");
     cudaSetDevice(b->device);
     TR_BCUDA(b, cudaEventSynchronize(b->evStop));
-    std::vector<uint32_t> cnt(b->waves.size() * kCounterWords);
-    TR_BCUDA(b, cudaMemcpy(cnt.data(), b->counters, cnt.size() * sizeof(uint32_t), cudaMemcpyDeviceToHost));
+    std::vector<BatchState> states(b->rounds.size());
+    TR_BCUDA(b, cudaMemcpy(states.data(), b->states, states.size() * sizeof(BatchState), cudaMemcpyDeviceToHost));
     uint32_t err = 0;
-    unsigned long long trav[4] = {0, 0, 0, 0};
-    TR_BCUDA(b, cudaMemcpy(&err, b->frame[0].errorFlag, sizeof(uint32_t), cudaMemcpyDeviceToHost));
-    TR_BCUDA(b, cudaMemcpy(trav, b->frame[0].traversal, sizeof(trav), cudaMemcpyDeviceToHost));
+    unsigned long long trav[kTraversalCounters] = {};
+    TR_BCUDA(b, cudaMemcpy(&err, b->frame.errorFlag, sizeof(uint32_t), cudaMemcpyDeviceToHost));
+    TR_BCUDA(b, cudaMemcpy(trav, b->frame.traversal, sizeof(trav), cudaMemcpyDeviceToHost));
     tr_batch_statistics s{};
-    for (size_t w = 0; w < b->waves.size(); ++w) {
-        const uint32_t* c = cnt.data() + w * kCounterWords;
-        for (uint32_t bounce = 0; bounce < b->lastSettings.maxDepth; ++bounce) {
-            s.extend_rays += bounce == 0 ? b->waves[w].paths : c[bounce];
-            s.shadow_rays += c[kShadowCounterBase + bounce];
-            s.hit_rays += c[kHitCounterBase + bounce];
-        }
+    for (const BatchState& bs : states) {
+        // the last plan of a round added its final iteration's counts
+        s.extend_rays += bs.extendRays;
+        s.shadow_rays += bs.shadowRays;
+        s.hit_rays += bs.hitRays;
+        s.iterations += bs.iterations;
     }
+    // per round: start, finalize, and plan + extend + shade + connect per iteration (the last
+    // iteration of a round finds nothing to trace)
+    s.launches = uint32_t(b->rounds.size()) * 2u + 4u * (s.iterations + uint32_t(b->rounds.size()));
     float ms = 0.f;
     cudaEventElapsedTime(&ms, b->evStart, b->evStop);
     s.render_time_ms = ms;

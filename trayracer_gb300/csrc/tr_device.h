@@ -145,18 +145,27 @@ struct SceneView {
 
 struct BatchItem;
 
-// Batched rendering: one wavefront over the paths of many scenes whose
-// buffers are concatenated (node, triangle, material and light indices
-// rebased). A wave holds consecutive (item, sample) units of width * height
-// paths; a segment is the run of one item's samples inside one wave.
-struct BatchSegment {
-    uint32_t pathBase;    // first path index of the segment in the wave
-    uint32_t pixelBase;   // first pixel of the segment among the wave's segments
-    uint32_t item;
-    uint32_t sampleBase;  // sample index of the segment's first unit
-    uint32_t pixels;      // width * height of the item
-    uint32_t samples;     // units (samples per pixel) of the item in the segment
-    uint32_t pad0, pad1;
+// Batched rendering: one continuous wavefront over the samples of many scenes
+// whose buffers are concatenated (node, triangle, material and light indices
+// rebased). A sample is identified by its sample id: the items' samples are
+// numbered item by item, and within an item pixel by pixel with the samples of
+// a pixel consecutive (id = item.sampleBase + pixel * spp + sample). A pool of
+// path slots is kept full: every iteration traces the paths carried over from
+// the last one and starts new samples in the slots that paths left.
+struct BatchState {
+    uint32_t cursor;       // next sample id to start
+    uint32_t end;          // one past the last sample id
+    uint32_t queue;        // extend queue length of the current iteration
+    uint32_t carried;      // extend queue entries [0, carried) are carried-over paths; the rest start now
+    uint32_t freshBase;    // sample id of extend queue entry `carried`
+    uint32_t survivors;    // paths the current iteration carries over (shade's extend-queue appends)
+    uint32_t hits;         // hit queue length
+    uint32_t shadows;      // shadow queue length
+    uint32_t extendWork;   // work cursors of the persistent extend / connect launches
+    uint32_t connectWork;
+    uint32_t iterations;   // iterations that traced rays
+    uint32_t pad;
+    unsigned long long extendRays, shadowRays, hitRays;  // totals over the iterations
 };
 
 // Per-frame constants of the wavefront (constant between resizes / setting
@@ -177,13 +186,14 @@ struct FrameView {
                                     // connect nodes, connect tris, shade and connect radiance updates
     uint32_t capacity;
     uint32_t resX, resY;
-    uint32_t pathCount;    // resX * resY * multiSample (batched: the paths of the wave)
+    uint32_t pathCount;    // resX * resY * multiSample (batched: the pool's path slots)
     // material order of the hit queue (null: shade in queue order)
     const uint32_t* hitOrder;
-    // batched rendering only (null / 0 for one scene)
-    const BatchSegment* segments;
+    // batched rendering only (null / 0 for one scene): the iteration state and
+    // the items of the round being rendered (sample ids count from its first item)
+    BatchState* batch;
     const BatchItem* items;
-    uint32_t segmentCount;
+    uint32_t itemCount;
     uint32_t pad;
 };
 
@@ -202,8 +212,8 @@ struct Camera {
     float pad;
 };
 
-// One scene of a batch: its camera and film, BVH root, light range and
-// pixel range in the batch accumulator.
+// One scene of a batch: its camera and film, BVH root, light range, pixel
+// range in the batch accumulator and sample-id range in its round.
 struct BatchItem {
     Camera camera;
     uint32_t width, height;
@@ -214,7 +224,8 @@ struct BatchItem {
     float lightEnergyTotal;
     uint32_t pixelBase;     // first pixel in the batch accumulator
     uint32_t spp;
-    uint32_t pad0, pad1, pad2;
+    uint32_t sampleBase;    // first sample id (counted from the first item of the item's round)
+    uint32_t pad1, pad2;
 };
 
 // Scratch and parameters of the path-replay adjoint (by path index, plane

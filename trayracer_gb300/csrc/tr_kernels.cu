@@ -212,13 +212,13 @@ __device__ __forceinline__ void camera_ray(const Camera& cam, uint32_t resX, uin
     T = v2 * v2;
 }
 
-// Batched rendering: the segment of a wave path (segments sorted by pathBase).
-__device__ __forceinline__ uint32_t batch_segment(const FrameView& f, uint32_t pathIx)
+// Batched rendering: the item of a sample id (items sorted by sampleBase).
+__device__ __forceinline__ uint32_t batch_item(const FrameView& f, uint32_t id)
 {
-    uint32_t lo = 0, hi = f.segmentCount;
+    uint32_t lo = 0, hi = f.itemCount;
     while (hi - lo > 1u) {
         const uint32_t mid = (lo + hi) >> 1;
-        if (__ldg(&f.segments[mid].pathBase) <= pathIx)
+        if (__ldg(&f.items[mid].sampleBase) <= id)
             lo = mid;
         else
             hi = mid;
@@ -226,13 +226,38 @@ __device__ __forceinline__ uint32_t batch_segment(const FrameView& f, uint32_t p
     return lo;
 }
 
-// BVH root of the scene a path belongs to (node 0 for one scene).
+// Item, pixel and sample index of a batch sample id.
+struct BatchSample {
+    uint32_t item;
+    uint32_t pixel;
+    uint32_t sample;
+};
+__device__ __forceinline__ BatchSample batch_sample(const FrameView& f, uint32_t id)
+{
+    BatchSample b;
+    b.item = batch_item(f, id);
+    const uint32_t local = id - __ldg(&f.items[b.item].sampleBase);
+    const uint32_t spp = __ldg(&f.items[b.item].spp);
+    b.pixel = local / spp;
+    b.sample = local - b.pixel * spp;
+    return b;
+}
+
+// BVH root of the scene a path belongs to (node 0 for one scene; a batch path
+// is given by its sample id).
 template <bool BATCH>
-__device__ __forceinline__ uint32_t path_root(const FrameView& f, uint32_t pathIx)
+__device__ __forceinline__ uint32_t path_root(const FrameView& f, uint32_t id)
 {
     if (!BATCH)
         return 0u;
-    return __ldg(&f.items[__ldg(&f.segments[batch_segment(f, pathIx)].item)].root);
+    return __ldg(&f.items[batch_item(f, id)].root);
+}
+
+// Per-path bounce and flags of a batched path, kept in D.w (the packed normal
+// of one-scene paths, which nothing reads): bounce << 4 | flags.
+__device__ __forceinline__ uint32_t batch_pack(uint32_t bounce, uint32_t flags)
+{
+    return (bounce << kPathIxShift) | (flags & kFlagsMask);
 }
 
 // The scene view of a batch item: the concatenated buffers with the item's
@@ -259,14 +284,13 @@ __device__ __forceinline__ void primary_ray(const FrameView& f, const Camera& ca
     const uint32_t pixelIx = pathIx % wh;
     const uint32_t sampleIx = pathIx / wh;
     if (BATCH) {
-        // the item's camera and film; the counter RNG keyed as for one scene
-        const BatchSegment sg = f.segments[batch_segment(f, pathIx)];
-        const uint32_t rel = pathIx - sg.pathBase;
-        const uint32_t pixel = rel % sg.pixels;
-        const BatchItem& it = f.items[sg.item];
+        // pathIx is the sample id: the item's camera and film, the counter RNG
+        // keyed as for one scene
+        const BatchSample bs = batch_sample(f, pathIx);
+        const BatchItem& it = f.items[bs.item];
         CounterRng rng;
-        rng.init(pixel, sg.sampleBase + rel / sg.pixels, 0u, st.seed);
-        camera_ray(it.camera, it.width, it.height, pixel % it.width, pixel / it.width, rng, false, O, D, T);
+        rng.init(bs.pixel, bs.sample, 0u, st.seed);
+        camera_ray(it.camera, it.width, it.height, bs.pixel % it.width, bs.pixel / it.width, rng, false, O, D, T);
     } else if (REF) {
         RefRng rng{tea2(st.seed + pathIx, sc << 1)};
         const bool rtl = (st.flags & TR_FLAG_REFERENCE_DRAW_RTL) != 0;
@@ -298,16 +322,6 @@ __device__ __forceinline__ uint32_t camera_order(const FrameView& f, uint32_t i)
     const uint32_t tilesX = W >> 3;
     const uint32_t ty = tile / tilesX, tx = tile - ty * tilesX;
     return sample * wh + ((ty << 2) | (within >> 3)) * W + ((tx << 3) | (within & 7u));
-}
-
-// The same for a batched wave: within each segment (one item's samples in the
-// wave) the samples of a pixel are consecutive.
-__device__ __forceinline__ uint32_t batch_camera_order(const FrameView& f, uint32_t i)
-{
-    const BatchSegment sg = f.segments[batch_segment(f, i)];
-    const uint32_t rel = i - sg.pathBase;
-    const uint32_t pixel = rel / sg.samples, sample = rel - pixel * sg.samples;
-    return sg.pathBase + sample * sg.pixels + pixel;
 }
 
 template <bool REF, bool BATCH>
@@ -388,16 +402,21 @@ __device__ __noinline__ void sky_miss(const SceneView& s, const FrameView& f, co
     }
 }
 
+// BATCH: the extend queue of a batch iteration - entries [0, carried) are
+// paths carried over from the last iteration, the entries after them start
+// new samples (their camera rays are made here), so the pool stays full.
 template <bool COUNT, bool BATCH, bool PRIMARY, bool TL>
 __global__ void __launch_bounds__(128, 8) extend_kernel(SceneView s, FrameView f, Settings st, uint32_t bounce,
                                                      Camera cam)
 {
-    const uint32_t count = queue_length(f, bounce);
+    const uint32_t count = BATCH ? __ldcg(&f.batch->queue) : queue_length(f, bounce);
+    const uint32_t carried = BATCH ? __ldcg(&f.batch->carried) : 0u;
+    const uint32_t freshBase = BATCH ? __ldcg(&f.batch->freshBase) : 0u;
     const float4* __restrict__ in = f.state[0];
     float4* __restrict__ hq = f.state[1];
     const uint32_t cap = f.capacity;
-    uint32_t* work = f.counters + kExtendWorkBase + bounce;
-    uint32_t* hitCounter = f.counters + kHitCounterBase + bounce;
+    uint32_t* work = BATCH ? &f.batch->extendWork : f.counters + kExtendWorkBase + bounce;
+    uint32_t* hitCounter = BATCH ? &f.batch->hits : f.counters + kHitCounterBase + bounce;
     const uint32_t lane = lane_id();
     const bool aov = (st.flags & TR_FLAG_WRITE_AOVS) && bounce == 0;
     const uint32_t wh = f.resX * f.resY;
@@ -418,12 +437,13 @@ __global__ void __launch_bounds__(128, 8) extend_kernel(SceneView s, FrameView f
             if (!alive && more) {
                 const uint32_t i = base + __popc(idle & ((1u << lane) - 1u));
                 if (i < count) {
-                    if (PRIMARY) {
+                    if (BATCH ? i >= carried : PRIMARY) {
                         float3 O, D;
                         float T;
-                        const uint32_t pathIx = BATCH ? batch_camera_order(f, i) : camera_order(f, i);
+                        const uint32_t pathIx = BATCH ? freshBase + (i - carried) : camera_order(f, i);
                         primary_ray<false, BATCH>(f, cam, st, pathIx, sc, O, D, T);
-                        O4 = f4(O, u2f(pack_path(pathIx, 0)));
+                        // a batch path keeps its sample id in O.w and bounce | flags in D.w
+                        O4 = f4(O, u2f(BATCH ? pathIx : pack_path(pathIx, 0)));
                         D4 = f4(D, 0.f);
                         T4 = make_float4(T, T, T, 1.f);
                         f.radiance[pathIx] = make_float4(0.f, 0.f, 0.f, 0.f);
@@ -432,8 +452,8 @@ __global__ void __launch_bounds__(128, 8) extend_kernel(SceneView s, FrameView f
                         D4 = __ldcs(in + i + cap);
                         T4 = __ldcs(in + i + 2 * cap);
                     }
-                    traversal_begin(t, f3(O4), f3(D4), st.rayEpsilon, kDstMax,
-                                    path_root<BATCH>(f, path_ix(__float_as_uint(O4.w))));
+                    const uint32_t id = BATCH ? __float_as_uint(O4.w) : path_ix(__float_as_uint(O4.w));
+                    traversal_begin(t, f3(O4), f3(D4), st.rayEpsilon, kDstMax, path_root<BATCH>(f, id));
                     alive = true;
                 } else {
                     more = false;
@@ -727,8 +747,10 @@ struct VertexInfo {
 // One PathTracingKernel step (PathTracing.h:15-174) for one queue entry. With
 // vi == nullptr (the shade kernel) it adds emitted radiance and writes the
 // guide buffers; the adjoint replay passes vi and gets the vertex instead.
-// Returns true when it added emitted radiance to the path's radiance.
-template <bool REF, class Rng, bool TEX = false>
+// Returns true when it added emitted radiance to the path's radiance. BATCH:
+// the path's sample id is O.w, its bounce and flags are in D.w, and its last
+// bounce (max_depth - 1) makes no extend ray.
+template <bool REF, class Rng, bool TEX = false, bool BATCH = false>
 __device__ __forceinline__ bool shade_path(const SceneView& s, const FrameView& f, const Settings& st, uint32_t bounce,
                                            uint32_t sc, const float4& O4, const float4& D4, const float4& T4,
                                            const uint4& hd, Rng& rng, bool& wantExt, float4 (&ext)[3],
@@ -737,11 +759,11 @@ __device__ __forceinline__ bool shade_path(const SceneView& s, const FrameView& 
     const uint32_t wh = f.resX * f.resY;
     const float3 O = f3(O4), D = f3(D4), T = f3(T4);
     const uint32_t data = __float_as_uint(O4.w);
-    const uint32_t pathIx = path_ix(data);
-    uint32_t flags = path_flags(data);
+    const uint32_t pathIx = BATCH ? data : path_ix(data);
+    uint32_t flags = BATCH ? (__float_as_uint(D4.w) & kFlagsMask) : path_flags(data);
     const float extendPdf = T4.w;
     const uint32_t pixelIx = pathIx % wh;
-    const bool aov = vi == nullptr && (st.flags & TR_FLAG_WRITE_AOVS) && bounce == 0 && pathIx < wh;
+    const bool aov = !BATCH && vi == nullptr && (st.flags & TR_FLAG_WRITE_AOVS) && bounce == 0 && pathIx < wh;
     if (vi) {
         vi->hit = false;
         vi->emissive = false;
@@ -846,7 +868,7 @@ __device__ __forceinline__ bool shade_path(const SceneView& s, const FrameView& 
 
     if (vi)
         vi->wiExt = c.extWi;
-    if (c.extPdf > kEpsilon) {
+    if (c.extPdf > kEpsilon && (!BATCH || bounce + 1u < st.maxDepth)) {
         float3 tp = c.extT * fdiv(1.f, fabsf(c.extPdf));
         if (bounce >= st.rrStart) {
             const float rr = fminf(1.0f, fmaxf(tp.x, fmaxf(tp.y, tp.z)));
@@ -860,8 +882,8 @@ __device__ __forceinline__ bool shade_path(const SceneView& s, const FrameView& 
         else
             flags &= ~kFlagSpecular;
         wantExt = true;
-        ext[0] = f4(I, __uint_as_float(pack_path(pathIx, flags)));
-        ext[1] = f4(nd, __uint_as_float(pack_normal(sf.N)));
+        ext[0] = f4(I, __uint_as_float(BATCH ? pathIx : pack_path(pathIx, flags)));
+        ext[1] = f4(nd, __uint_as_float(BATCH ? batch_pack(bounce + 1u, flags) : pack_normal(sf.N)));
         ext[2] = f4(fixnan(tp), c.extPdf);
     }
     return false;
@@ -870,14 +892,14 @@ __device__ __forceinline__ bool shade_path(const SceneView& s, const FrameView& 
 template <bool REF, bool BATCH, bool TEX = false>
 __global__ void __launch_bounds__(128, 5) shade_kernel(SceneView s, FrameView f, Settings st, uint32_t bounce)
 {
-    const uint32_t count = __ldcg(f.counters + kHitCounterBase + bounce);
+    const uint32_t count = BATCH ? __ldcg(&f.batch->hits) : __ldcg(f.counters + kHitCounterBase + bounce);
     const float4* __restrict__ in = f.state[1];
     float4* __restrict__ out = f.state[0];
     const uint32_t cap = f.capacity;
     const uint32_t sc = *f.sampleCount;
     const uint32_t wh = f.resX * f.resY;
-    uint32_t* extCounter = f.counters + bounce + 1u;
-    uint32_t* shCounter = f.counters + kShadowCounterBase + bounce;
+    uint32_t* extCounter = BATCH ? &f.batch->survivors : f.counters + bounce + 1u;
+    uint32_t* shCounter = BATCH ? &f.batch->shadows : f.counters + kShadowCounterBase + bounce;
     const uint32_t lane = lane_id();
     const uint32_t warpGlobal = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
     const uint32_t warpStride = (gridDim.x * blockDim.x) >> 5;
@@ -916,12 +938,15 @@ __global__ void __launch_bounds__(128, 5) shade_kernel(SceneView s, FrameView f,
                 fetch(k + warpStride * 32u, buf);
             const uint32_t pathIx = path_ix(__float_as_uint(O4.w));
             if (BATCH) {
-                const BatchSegment sg = f.segments[batch_segment(f, pathIx)];
-                const uint32_t rel = pathIx - sg.pathBase;
-                const SceneView si = item_scene(s, f.items[sg.item]);
+                // O.w is the sample id, D.w the path's bounce and flags
+                const uint32_t id = __float_as_uint(O4.w);
+                const uint32_t pathBounce = __float_as_uint(D4.w) >> kPathIxShift;
+                const BatchSample bs = batch_sample(f, id);
+                const SceneView si = item_scene(s, f.items[bs.item]);
                 CounterRng rng;
-                rng.init(rel % sg.pixels, sg.sampleBase + rel / sg.pixels, bounce + 1u, st.seed);
-                emitted = shade_path<false>(si, f, st, bounce, sc, O4, D4, T4, hd, rng, wantExt, ext, wantShadow, sh);
+                rng.init(bs.pixel, bs.sample, pathBounce + 1u, st.seed);
+                emitted = shade_path<false, CounterRng, false, true>(si, f, st, pathBounce, sc, O4, D4, T4, hd, rng,
+                                                                     wantExt, ext, wantShadow, sh);
             } else if (REF) {
                 RefRng rng{tea2(st.seed + pathIx, sc + bounce + 1u)};
                 emitted = shade_path<REF, RefRng, TEX>(s, f, st, bounce, sc, O4, D4, T4, hd, rng, wantExt, ext,
@@ -1052,9 +1077,9 @@ __global__ void __launch_bounds__(256) sort_scatter_kernel(FrameView f, SortView
 template <bool COUNT, bool BATCH, bool TL>
 __global__ void __launch_bounds__(128) connect_kernel(SceneView s, FrameView f, Settings st, uint32_t bounce)
 {
-    const uint32_t count = __ldcg(f.counters + kShadowCounterBase + bounce);
+    const uint32_t count = BATCH ? __ldcg(&f.batch->shadows) : __ldcg(f.counters + kShadowCounterBase + bounce);
     const uint32_t cap = f.capacity;
-    uint32_t* work = f.counters + kConnectWorkBase + bounce;
+    uint32_t* work = BATCH ? &f.batch->connectWork : f.counters + kConnectWorkBase + bounce;
     const uint32_t lane = lane_id();
     TraversalCounts cnt{0, 0};
     uint32_t visibleCnt = 0;
@@ -1373,45 +1398,74 @@ __global__ void __launch_bounds__(128) debug_shade_kernel(SceneView s, FrameView
     }
 }
 
-// Batched rendering: sums each pixel's samples of the wave in sample order
-// and adds them to the item's pixel of the batch accumulator (zeroed before
-// the first wave; waves run in order, and an item has at most one segment per
-// wave, so no two threads add to one pixel).
-__global__ void __launch_bounds__(256) batch_finalize_kernel(FrameView f, uint32_t wavePixels)
+// Batched rendering: one iteration's plan. Sums the iteration that ended into
+// the totals, carries its surviving paths over (the first `carried` entries of
+// the extend queue) and fills the rest of the pool with new samples from the
+// cursor; with a conditional handle (graph replay) the batch's while loop goes
+// on as long as the new iteration has rays to trace. Every path ends within
+// max_depth iterations, so a round needs at most samples * max_depth
+// iterations; `limit` (above that) ends the loop with the error word set
+// should the counts ever say otherwise.
+__global__ void batch_plan_kernel(BatchState* __restrict__ bs, uint32_t pool, uint32_t end, uint32_t limit,
+                                  uint32_t* __restrict__ errorFlag, cudaGraphConditionalHandle loop, int32_t useLoop)
 {
-    const uint32_t q = blockIdx.x * blockDim.x + threadIdx.x;
-    if (q >= wavePixels)
+    if (threadIdx.x != 0 || blockIdx.x != 0)
         return;
-    uint32_t lo = 0, hi = f.segmentCount;
+    BatchState s = *bs;
+    s.end = end;
+    s.extendRays += s.queue;
+    s.shadowRays += s.shadows;
+    s.hitRays += s.hits;
+    const uint32_t carried = s.survivors;  // <= the last queue length <= pool
+    const uint32_t room = pool - carried;
+    const uint32_t left = s.end - s.cursor;
+    const uint32_t fresh = left < room ? left : room;
+    s.carried = carried;
+    s.freshBase = s.cursor;
+    s.cursor += fresh;
+    s.queue = carried + fresh;
+    if (s.queue && s.iterations >= limit) {
+        s.queue = 0;
+        atomicOr(errorFlag, 2u);
+    }
+    s.survivors = 0;
+    s.hits = 0;
+    s.shadows = 0;
+    s.extendWork = 0;
+    s.connectWork = 0;
+    if (s.queue)
+        s.iterations++;
+    *bs = s;
+    if (useLoop)
+        cudaGraphSetConditional(loop, s.queue ? 1u : 0u);
+}
+
+// Batched rendering: every pixel of the round's items, its samples summed in
+// sample order (as finalize_kernel sums one frame's multi_sample samples), into
+// the batch accumulator (sum, spp) and colors = accumulator / spp.
+__global__ void __launch_bounds__(256) batch_finalize_kernel(FrameView f, uint32_t pixelBegin, uint32_t pixelEnd)
+{
+    const uint32_t p = pixelBegin + blockIdx.x * blockDim.x + threadIdx.x;
+    if (p >= pixelEnd)
+        return;
+    uint32_t lo = 0, hi = f.itemCount;
     while (hi - lo > 1u) {
         const uint32_t mid = (lo + hi) >> 1;
-        if (__ldg(&f.segments[mid].pixelBase) <= q)
+        if (__ldg(&f.items[mid].pixelBase) <= p)
             lo = mid;
         else
             hi = mid;
     }
-    const BatchSegment sg = f.segments[lo];
-    const uint32_t p = q - sg.pixelBase;
+    const BatchItem& it = f.items[lo];
+    const uint32_t spp = it.spp;
+    const float4* r = f.radiance + it.sampleBase + size_t(p - it.pixelBase) * spp;
     float3 sum = f3(0.f);
-    for (uint32_t k = 0; k < sg.samples; ++k) {
-        const float4 r = f.radiance[sg.pathBase + k * sg.pixels + p];
-        sum = sum + f3(r);
-    }
-    float4* a = f.accumulator + f.items[sg.item].pixelBase + p;
-    const float4 acc = *a;
-    *a = make_float4(acc.x + sum.x, acc.y + sum.y, acc.z + sum.z, acc.w + float(sg.samples));
-}
-
-// colors = accumulator / samples, over all pixels of a batch.
-__global__ void __launch_bounds__(256) batch_resolve_kernel(const float4* __restrict__ acc, float4* __restrict__ colors,
-                                                            uint32_t pixels)
-{
-    const uint32_t p = blockIdx.x * blockDim.x + threadIdx.x;
-    if (p >= pixels)
-        return;
-    const float4 a = acc[p];
-    const float n = a.w;
-    colors[p] = n > 0.f ? make_float4(a.x / n, a.y / n, a.z / n, a.w / n) : make_float4(0.f, 0.f, 0.f, 0.f);
+    for (uint32_t k = 0; k < spp; ++k)
+        sum = sum + f3(__ldcs(r + k));
+    const float4 acc = make_float4(0.f + sum.x, 0.f + sum.y, 0.f + sum.z, 0.f + float(spp));
+    f.accumulator[p] = acc;
+    const float n = float(spp);
+    f.colors[p] = make_float4(acc.x / n, acc.y / n, acc.z / n, acc.w / n);
 }
 
 // Adds each lane's gradient slots [first, last) to the row of its key
@@ -1816,9 +1870,7 @@ cudaError_t launch_generate(const FrameView& f, const Camera& cam, const Setting
     if (f.pathCount == 0)
         return cudaSuccess;
     const uint32_t blocks = (f.pathCount + 255u) / 256u;
-    if (f.segments)
-        generate_kernel<false, true><<<blocks, 256, 0, stream>>>(f, cam, st);
-    else if (st.flags & TR_FLAG_REFERENCE_SAMPLING)
+    if (st.flags & TR_FLAG_REFERENCE_SAMPLING)
         generate_kernel<true, false><<<blocks, 256, 0, stream>>>(f, cam, st);
     else
         generate_kernel<false, false><<<blocks, 256, 0, stream>>>(f, cam, st);
@@ -1832,7 +1884,7 @@ void launch_extend_variant(const SceneView& s0, const FrameView& f, const Settin
     const SceneView s = traced(s0, st);
     const bool count = (st.flags & TR_FLAG_COUNT_TRAVERSAL) != 0;
     const uint32_t g = shape.extendBlocks;
-    if (f.segments) {
+    if (f.batch) {
         if (count)
             extend_kernel<true, true, PRIMARY, false><<<g, 128, 0, stream>>>(s, f, st, bounce, cam);
         else
@@ -1866,7 +1918,7 @@ cudaError_t launch_shade(const SceneView& s, const FrameView& f, const Settings&
                          const LaunchShape& shape, cudaStream_t stream)
 {
     const bool ref = (st.flags & TR_FLAG_REFERENCE_SAMPLING) != 0;
-    if (f.segments)
+    if (f.batch)
         shade_kernel<false, true><<<shape.shadeBlocks, 128, 0, stream>>>(s, f, st, bounce);
     else if (s.texSlots && ref)
         shade_kernel<true, false, true><<<shape.shadeBlocks, 128, 0, stream>>>(s, f, st, bounce);
@@ -1887,7 +1939,7 @@ cudaError_t launch_connect(const SceneView& s0, const FrameView& f, const Settin
     st.refillBelow = shape.refillBelow;
     const bool count = (st.flags & TR_FLAG_COUNT_TRAVERSAL) != 0;
     const uint32_t g = shape.connectBlocks;
-    if (f.segments) {
+    if (f.batch) {
         if (count)
             connect_kernel<true, true, false><<<g, 128, 0, stream>>>(s, f, st, bounce);
         else
@@ -1995,19 +2047,18 @@ cudaError_t launch_sort_hits(const SceneView& s, const FrameView& f, const SortV
     return cudaGetLastError();
 }
 
-cudaError_t launch_batch_finalize(const FrameView& f, uint32_t wavePixels, cudaStream_t stream)
+cudaError_t launch_batch_plan(BatchState* state, uint32_t pool, uint32_t end, uint32_t limit, uint32_t* errorFlag,
+                              cudaGraphConditionalHandle loop, bool useLoop, cudaStream_t stream)
 {
-    if (wavePixels == 0)
-        return cudaSuccess;
-    batch_finalize_kernel<<<(wavePixels + 255u) / 256u, 256, 0, stream>>>(f, wavePixels);
+    batch_plan_kernel<<<1, 32, 0, stream>>>(state, pool, end, limit, errorFlag, loop, useLoop ? 1 : 0);
     return cudaGetLastError();
 }
 
-cudaError_t launch_batch_resolve(const float4* accumulator, float4* colors, uint32_t pixels, cudaStream_t stream)
+cudaError_t launch_batch_finalize(const FrameView& f, uint32_t pixelBegin, uint32_t pixelEnd, cudaStream_t stream)
 {
-    if (pixels == 0)
+    if (pixelEnd <= pixelBegin)
         return cudaSuccess;
-    batch_resolve_kernel<<<(pixels + 255u) / 256u, 256, 0, stream>>>(accumulator, colors, pixels);
+    batch_finalize_kernel<<<(pixelEnd - pixelBegin + 255u) / 256u, 256, 0, stream>>>(f, pixelBegin, pixelEnd);
     return cudaGetLastError();
 }
 

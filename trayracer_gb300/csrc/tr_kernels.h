@@ -49,10 +49,14 @@ cudaError_t launch_pick_ray(const SceneView& s, const Camera& cam, const Setting
 // reads the queue through it when FrameView::hitOrder = sv.order).
 cudaError_t launch_sort_hits(const SceneView& s, const FrameView& f, const SortView& sv, uint32_t bounce,
                              const LaunchShape& shape, cudaStream_t stream);
-// Batched rendering: adds a wave's samples to the batch accumulator; then
-// colors = accumulator / samples over all batch pixels.
-cudaError_t launch_batch_finalize(const FrameView& f, uint32_t wavePixels, cudaStream_t stream);
-cudaError_t launch_batch_resolve(const float4* accumulator, float4* colors, uint32_t pixels, cudaStream_t stream);
+// Batched rendering: the plan of one iteration of the continuous wavefront
+// (with useLoop, it sets the conditional of the graph's while loop: 1 while
+// there are rays to trace; a round stops after `limit` iterations with the
+// error word set), and the accumulator and colors of a round's
+// pixels [pixelBegin, pixelEnd) from its per-sample radiance.
+cudaError_t launch_batch_plan(BatchState* state, uint32_t pool, uint32_t end, uint32_t limit, uint32_t* errorFlag,
+                              cudaGraphConditionalHandle loop, bool useLoop, cudaStream_t stream);
+cudaError_t launch_batch_finalize(const FrameView& f, uint32_t pixelBegin, uint32_t pixelEnd, cudaStream_t stream);
 // Path-replay adjoint of the frame `f` (its per-path radiance and sample
 // count are the forward frame's; its queues are overwritten, its counters
 // are the adjoint's own).

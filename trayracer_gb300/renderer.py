@@ -392,10 +392,11 @@ def settings_for(scene: Scene, multi_sample: int = 1, reference: bool = False, s
 
 
 class BatchRenderer:
-    """Many independent scenes rendered by one wavefront (tr_batch_*): each item is
-    (scene, spp) with the scene's own camera and resolution."""
+    """Many independent scenes rendered by one continuous wavefront (tr_batch_*): each item
+    is (scene, spp) with the scene's own camera and resolution; pool_paths path slots (0: the
+    library's default) are kept full with the items' samples."""
 
-    def __init__(self, scenes, spp=None, wave_paths: int = 0, device: int = 0):
+    def __init__(self, scenes, spp=None, pool_paths: int = 0, device: int = 0):
         self._lib = _abi.load_library()
         self._b = C.c_void_p()
         self.scenes = list(scenes)
@@ -409,7 +410,7 @@ class BatchRenderer:
             items[i].height = s.height
             items[i].spp = self.spp[i]
         cfg = _abi.Config(device, _abi.TR_ABI_VERSION)
-        st = self._lib.tr_batch_create(C.byref(cfg), items, len(self.scenes), int(wave_paths), C.byref(self._b))
+        st = self._lib.tr_batch_create(C.byref(cfg), items, len(self.scenes), int(pool_paths), C.byref(self._b))
         if st != 0:
             raise TracerError(st, "tr_batch_create")
 
@@ -442,7 +443,7 @@ class BatchRenderer:
     def Info(self) -> dict:
         i = _abi.BatchInfo()
         self._check(self._lib.tr_batch_get_info(self._b, C.byref(i)), "tr_batch_get_info")
-        return {f: getattr(i, f) for f, _ in i._fields_}
+        return {f: getattr(i, f) for f, _ in i._fields_ if f != "reserved"}
 
     def Statistics(self) -> dict:
         s = _abi.BatchStatistics()
