@@ -126,6 +126,10 @@ struct Context {
 
     // timing
     cudaEvent_t evStart = nullptr, evGenerate = nullptr, evFinal = nullptr;
+    // captured frames trace bounce b's shadow rays on this stream while bounce
+    // b + 1's extend rays run on the frame's stream (fork / join)
+    cudaStream_t side = nullptr;
+    cudaEvent_t evFork = nullptr, evJoin = nullptr;
     cudaEvent_t evExtend[TR_MAX_DEPTH] = {}, evShade[TR_MAX_DEPTH] = {}, evConnect[TR_MAX_DEPTH] = {};
     bool timedFrame = false;
     uint32_t timedDepth = 0;
@@ -421,19 +425,38 @@ tr_status enqueue_frame(Context* c, cudaStream_t s, bool timed)
         TR_CUDA(c, launch_generate(c->frame, c->camera, c->settings, s));
     if (timed)
         TR_CUDA(c, cudaEventRecord(c->evGenerate, s));
+    // Untimed (captured) frames overlap bounce b's connect with bounce b + 1's
+    // extend: connect reads the shadow queue and adds to the radiance of paths
+    // in flight, extend reads the extend queue and writes the hit queue, so they
+    // share nothing; shade b + 1 (which rewrites the shadow queue and adds
+    // emission to the same radiance) waits for both. Not with a sky: extend
+    // adds the sky to the radiance of missed paths. Timed frames keep the
+    // stages in sequence for their per-stage events.
+    const bool overlap = !timed && !c->scene.sky.enabled;
     for (uint32_t b = 0; b < c->settings.maxDepth; ++b) {
         TR_CUDA(c, launch_extend(c->scene, c->frame, c->settings, b, c->shape, s, fused ? &c->camera : nullptr));
         if (c->shape.sortHits)
             TR_CUDA(c, launch_sort_hits(c->scene, c->frame, c->sort, b, c->shape, s));
         if (timed)
             TR_CUDA(c, cudaEventRecord(c->evExtend[b], s));
+        if (overlap && b > 0)
+            TR_CUDA(c, cudaStreamWaitEvent(s, c->evJoin, 0));
         TR_CUDA(c, launch_shade(c->scene, c->frame, c->settings, b, c->shape, s));
         if (timed)
             TR_CUDA(c, cudaEventRecord(c->evShade[b], s));
-        TR_CUDA(c, launch_connect(c->scene, c->frame, c->settings, b, c->shape, s));
+        if (overlap) {
+            TR_CUDA(c, cudaEventRecord(c->evFork, s));
+            TR_CUDA(c, cudaStreamWaitEvent(c->side, c->evFork, 0));
+            TR_CUDA(c, launch_connect(c->scene, c->frame, c->settings, b, c->shape, c->side));
+            TR_CUDA(c, cudaEventRecord(c->evJoin, c->side));
+        } else {
+            TR_CUDA(c, launch_connect(c->scene, c->frame, c->settings, b, c->shape, s));
+        }
         if (timed)
             TR_CUDA(c, cudaEventRecord(c->evConnect[b], s));
     }
+    if (overlap)
+        TR_CUDA(c, cudaStreamWaitEvent(s, c->evJoin, 0));
     TR_CUDA(c, launch_finalize(c->frame, c->settings, s));
     if (timed)
         TR_CUDA(c, cudaEventRecord(c->evFinal, s));
@@ -595,6 +618,9 @@ tr_status tr_create(const tr_config* config, void** out_ctx)
     c->settings.flags = 0;
     c->settings.maxColor = 10.f;
     bool ok = cudaStreamCreate(&c->stream) == cudaSuccess;
+    ok = ok && cudaStreamCreateWithFlags(&c->side, cudaStreamNonBlocking) == cudaSuccess;
+    ok = ok && cudaEventCreateWithFlags(&c->evFork, cudaEventDisableTiming) == cudaSuccess &&
+         cudaEventCreateWithFlags(&c->evJoin, cudaEventDisableTiming) == cudaSuccess;
     ok = ok && cudaEventCreate(&c->evStart) == cudaSuccess && cudaEventCreate(&c->evGenerate) == cudaSuccess &&
          cudaEventCreate(&c->evFinal) == cudaSuccess;
     for (uint32_t i = 0; ok && i < TR_MAX_DEPTH; ++i)
@@ -623,7 +649,7 @@ tr_status tr_destroy(void* ctx)
     c->frameArena.release();
     c->adjointArena.release();
     release_textures(c);
-    cudaEvent_t* evs[] = {&c->evStart, &c->evGenerate, &c->evFinal};
+    cudaEvent_t* evs[] = {&c->evStart, &c->evGenerate, &c->evFinal, &c->evFork, &c->evJoin};
     for (cudaEvent_t* e : evs)
         if (*e)
             cudaEventDestroy(*e);
@@ -632,6 +658,8 @@ tr_status tr_destroy(void* ctx)
         if (c->evShade[i]) cudaEventDestroy(c->evShade[i]);
         if (c->evConnect[i]) cudaEventDestroy(c->evConnect[i]);
     }
+    if (c->side)
+        cudaStreamDestroy(c->side);
     if (c->stream)
         cudaStreamDestroy(c->stream);
     delete c;

@@ -62,6 +62,10 @@ struct ItemBuild {
 struct Batch {
     int device = 0;
     cudaStream_t stream = nullptr;
+    // a captured iteration traces the last iteration's shadow rays on `side`
+    // while its extend runs on `stream` (fork / join)
+    cudaStream_t side = nullptr;
+    cudaEvent_t evFork = nullptr, evJoin = nullptr;
     std::string lastError;
 
     void* sceneArena = nullptr;
@@ -137,6 +141,12 @@ void release(Batch* b)
         cudaFree(b->sceneArena);
     if (b->frameArena)
         cudaFree(b->frameArena);
+    if (b->evFork)
+        cudaEventDestroy(b->evFork);
+    if (b->evJoin)
+        cudaEventDestroy(b->evJoin);
+    if (b->side)
+        cudaStreamDestroy(b->side);
     if (b->stream)
         cudaStreamDestroy(b->stream);
 }
@@ -214,21 +224,41 @@ FrameView round_view(const Batch* b, uint32_t k)
     return f;
 }
 
-// One iteration of round k: plan, extend (carried paths + new samples), shade,
-// connect.
+// One iteration of round k: plan, connect of the last iteration's shadow rays
+// and extend (carried paths + new samples), shade. Connect adds to the
+// radiance of paths in flight and reads the shadow queue, extend reads the
+// extend queue and starts new samples: they share nothing, so with `overlap`
+// connect runs on the side stream beside extend; shade (which rewrites the
+// shadow queue and adds emission to the same radiance) waits for both. The
+// last iteration of a round traces nothing new and runs the final connect.
 cudaError_t enqueue_iteration(Batch* b, uint32_t k, const Settings& st, cudaGraphConditionalHandle loop,
-                              bool useLoop, cudaStream_t s)
+                              bool useLoop, cudaStream_t s, bool overlap)
 {
     const FrameView f = round_view(b, k);  // each path uses its item's camera
     const uint64_t bound = uint64_t(b->rounds[k].samples) * st.maxDepth + 4u;
     const uint32_t limit = bound < 0xffffffffull ? uint32_t(bound) : 0xffffffffu;
     cudaError_t e = launch_batch_plan(f.batch, b->pool, b->rounds[k].samples, limit, f.errorFlag, loop, useLoop, s);
-    if (e == cudaSuccess)
-        e = launch_extend(b->scene, f, st, 0u, b->shape, s, nullptr);
+    if (overlap) {
+        if (e == cudaSuccess)
+            e = cudaEventRecord(b->evFork, s);
+        if (e == cudaSuccess)
+            e = cudaStreamWaitEvent(b->side, b->evFork, 0);
+        if (e == cudaSuccess)
+            e = launch_connect(b->scene, f, st, 0u, b->shape, b->side);
+        if (e == cudaSuccess)
+            e = cudaEventRecord(b->evJoin, b->side);
+        if (e == cudaSuccess)
+            e = launch_extend(b->scene, f, st, 0u, b->shape, s, nullptr);
+        if (e == cudaSuccess)
+            e = cudaStreamWaitEvent(s, b->evJoin, 0);
+    } else {
+        if (e == cudaSuccess)
+            e = launch_connect(b->scene, f, st, 0u, b->shape, s);
+        if (e == cudaSuccess)
+            e = launch_extend(b->scene, f, st, 0u, b->shape, s, nullptr);
+    }
     if (e == cudaSuccess)
         e = launch_shade(b->scene, f, st, 0u, b->shape, s);
-    if (e == cudaSuccess)
-        e = launch_connect(b->scene, f, st, 0u, b->shape, s);
     return e;
 }
 
@@ -281,7 +311,10 @@ tr_status tr_batch_create(const tr_config* config, const tr_batch_item* items, u
     };
     // a blocking stream, like the context's: work on it is ordered with the legacy default stream
     if (cudaStreamCreate(&b->stream) != cudaSuccess || cudaEventCreate(&b->evStart) != cudaSuccess ||
-        cudaEventCreate(&b->evStop) != cudaSuccess)
+        cudaEventCreate(&b->evStop) != cudaSuccess ||
+        cudaStreamCreateWithFlags(&b->side, cudaStreamNonBlocking) != cudaSuccess ||
+        cudaEventCreateWithFlags(&b->evFork, cudaEventDisableTiming) != cudaSuccess ||
+        cudaEventCreateWithFlags(&b->evJoin, cudaEventDisableTiming) != cudaSuccess)
         return bail(TR_ERR_CUDA);
 
     const auto t0 = std::chrono::steady_clock::now();
@@ -562,8 +595,8 @@ tr_status capture_graph(Batch* b, const Settings& st)
         if (e != cudaSuccess)
             return fail_graph(e, "cudaGraphAddNode(while)");
         cudaGraph_t body = cp.conditional.phGraph_out[0];
-        e = capture_into(b, body, nullptr, 0, [&]() { return enqueue_iteration(b, k, st, loop, true, b->stream); },
-                         nullptr);
+        e = capture_into(
+            b, body, nullptr, 0, [&]() { return enqueue_iteration(b, k, st, loop, true, b->stream, true); }, nullptr);
         if (e != cudaSuccess)
             return fail_graph(e, "batch graph: iteration");
         const FrameView f = round_view(b, k);
@@ -586,7 +619,7 @@ tr_status enqueue_eager(Batch* b, const Settings& st, cudaStream_t s)
     for (uint32_t k = 0; k < b->rounds.size(); ++k) {
         TR_BCUDA(b, enqueue_round_start(b, k, s));
         while (true) {
-            TR_BCUDA(b, enqueue_iteration(b, k, st, cudaGraphConditionalHandle{}, false, s));
+            TR_BCUDA(b, enqueue_iteration(b, k, st, cudaGraphConditionalHandle{}, false, s, false));
             uint32_t queue = 0;
             TR_BCUDA(b, cudaMemcpyAsync(&queue, &b->states[k].queue, sizeof(uint32_t), cudaMemcpyDeviceToHost, s));
             TR_BCUDA(b, cudaStreamSynchronize(s));

@@ -160,11 +160,11 @@ struct BatchState {
     uint32_t freshBase;    // sample id of extend queue entry `carried`
     uint32_t survivors;    // paths the current iteration carries over (shade's extend-queue appends)
     uint32_t hits;         // hit queue length
-    uint32_t shadows;      // shadow queue length
+    uint32_t shadows;      // shadow queue length (written by this iteration's shade)
     uint32_t extendWork;   // work cursors of the persistent extend / connect launches
     uint32_t connectWork;
     uint32_t iterations;   // iterations that traced rays
-    uint32_t pad;
+    uint32_t connectQueue; // shadow rays of the last iteration, traced by this iteration's connect
     unsigned long long extendRays, shadowRays, hitRays;  // totals over the iterations
 };
 

@@ -1077,7 +1077,7 @@ __global__ void __launch_bounds__(256) sort_scatter_kernel(FrameView f, SortView
 template <bool COUNT, bool BATCH, bool TL>
 __global__ void __launch_bounds__(128) connect_kernel(SceneView s, FrameView f, Settings st, uint32_t bounce)
 {
-    const uint32_t count = BATCH ? __ldcg(&f.batch->shadows) : __ldcg(f.counters + kShadowCounterBase + bounce);
+    const uint32_t count = BATCH ? __ldcg(&f.batch->connectQueue) : __ldcg(f.counters + kShadowCounterBase + bounce);
     const uint32_t cap = f.capacity;
     uint32_t* work = BATCH ? &f.batch->connectWork : f.counters + kConnectWorkBase + bounce;
     const uint32_t lane = lane_id();
@@ -1399,9 +1399,9 @@ __global__ void __launch_bounds__(128) debug_shade_kernel(SceneView s, FrameView
 }
 
 // Batched rendering: one iteration's plan. Sums the iteration that ended into
-// the totals, carries its surviving paths over (the first `carried` entries of
-// the extend queue) and fills the rest of the pool with new samples from the
-// cursor; with a conditional handle (graph replay) the batch's while loop goes
+// the totals, hands its shadow rays to this iteration's connect, carries its
+// surviving paths over (the first `carried` entries of the extend queue) and
+// fills the rest of the pool with new samples from the cursor; with a conditional handle (graph replay) the batch's while loop goes
 // on as long as the new iteration has rays to trace. Every path ends within
 // max_depth iterations, so a round needs at most samples * max_depth
 // iterations; `limit` (above that) ends the loop with the error word set
@@ -1416,6 +1416,7 @@ __global__ void batch_plan_kernel(BatchState* __restrict__ bs, uint32_t pool, ui
     s.extendRays += s.queue;
     s.shadowRays += s.shadows;
     s.hitRays += s.hits;
+    s.connectQueue = s.shadows;
     const uint32_t carried = s.survivors;  // <= the last queue length <= pool
     const uint32_t room = pool - carried;
     const uint32_t left = s.end - s.cursor;
