@@ -552,7 +552,7 @@ def run_adjoint(args):
     print(json.dumps(line), flush=True)
 
 
-def run_large(args):
+def measure_large(args, steps, warmup):
     """The large configuration: 4096 displaced spheres (20.48 M triangles, 100k emissive), 4096
     materials, 3840x2160, 16 spp in one frame (132.7 M paths in flight), 12 bounces, RR from bounce
     3; a forward frame (graph) and the path-replay adjoint of the L2 loss against a black target
@@ -581,44 +581,33 @@ def run_large(args):
     grad = torch.zeros((scene.materials.shape[0], 9), dtype=torch.float32, device="cuda")
     fwd, adj, rays = [], [], 0
     pg = None
-    for i in range(args.warmup + args.steps):
-        flush.fill_(1.0)
-        e0, e1, e2, e3 = (torch.cuda.Event(enable_timing=True) for _ in range(4))
-        r.Reset()
-        e0.record(stream)
-        r.RenderFrame(stream=sptr, use_graph=True)
-        e1.record(stream)
-        if pg is None:
-            pg = torch.from_numpy(r.ColorBuffer()).cuda()  # dL/dcolor of 0.5 |img|^2
-            rays = r.Statistics()["path_count"]
-        flush.fill_(1.0)
-        e2.record(stream)
-        r.AdjointFrame(pg.data_ptr(), 1.0 / scene.spp, grad.data_ptr(), stream=sptr)
-        e3.record(stream)
-        e3.synchronize()
-        if i >= args.warmup:
-            fwd.append(e0.elapsed_time(e1))
-            adj.append(e2.elapsed_time(e3))
+    with ClockSampler(0) as clocks:
+        for i in range(warmup + steps):
+            flush.fill_(1.0)
+            e0, e1, e2, e3 = (torch.cuda.Event(enable_timing=True) for _ in range(4))
+            r.Reset()
+            e0.record(stream)
+            r.RenderFrame(stream=sptr, use_graph=True)
+            e1.record(stream)
+            if pg is None:
+                pg = torch.from_numpy(r.ColorBuffer()).cuda()  # dL/dcolor of 0.5 |img|^2
+                rays = r.Statistics()["path_count"]
+            flush.fill_(1.0)
+            e2.record(stream)
+            r.AdjointFrame(pg.data_ptr(), 1.0 / scene.spp, grad.data_ptr(), stream=sptr)
+            e3.record(stream)
+            e3.synchronize()
+            if i >= warmup:
+                fwd.append(e0.elapsed_time(e1))
+                adj.append(e2.elapsed_time(e3))
     stats = r.Statistics()
     assert stats["device_error"] == 0
     r.close()
     f_ms, a_ms = float(statistics.median(fwd)), float(statistics.median(adj))
-    line = {
-        "metric": "Mrays/s",
-        "value": round(rays / (f_ms / 1e3) / 1e6, 1),
-        "unit": "Mrays/s",
-        "n_gpus": 1,
-        "steps": args.steps,
-        "warmup": args.warmup,
-        "ms_per_step": round(f_ms + a_ms, 3),
-        "higher_is_better": True,
-        "scaling": "weak",
-        "vs_baseline": None,
-        "dtype": "f32",
-        "data": "synthetic",
-        "config": {"workload": f"{info['triangle_count']} triangles (4096 displaced spheres, 100k emissive), "
-                               f"4096 materials, {W}x{H}, {scene.spp} spp, 12 bounces, RR from 3",
-                   "l2": "flushed before the forward frame and before the adjoint (256 MiB write)"},
+    return {
+        "workload": f"{info['triangle_count']} triangles (4096 displaced spheres, 100k emissive), "
+                    f"4096 materials, {W}x{H}, {scene.spp} spp, 12 bounces, RR from 3",
+        "mrays_per_s": round(rays / (f_ms / 1e3) / 1e6, 1),
         "samples_per_s": round(W * H * scene.spp / (f_ms / 1e3), 1),
         "forward_ms": round(f_ms, 3),
         "adjoint_ms": round(a_ms, 3),
@@ -628,7 +617,30 @@ def run_large(args):
         "scene_upload_s": round(upload_s, 2),
         "scene_device_bytes": int(info["device_bytes"]),
         "gradient_norm": float(grad.norm()),
+        "clocks": clocks.summary(),
     }
+
+
+def run_large(args):
+    m = measure_large(args, args.steps, args.warmup)
+    line = {
+        "metric": "Mrays/s",
+        "value": None,
+        "unit": "Mrays/s",
+        "n_gpus": 1,
+        "steps": args.steps,
+        "warmup": args.warmup,
+        "ms_per_step": round(m["forward_ms"] + m["adjoint_ms"], 3),
+        "higher_is_better": True,
+        "scaling": "weak",
+        "vs_baseline": None,
+        "dtype": "f32",
+        "data": "synthetic",
+        "config": {"workload": m["workload"],
+                   "l2": "flushed before the forward frame and before the adjoint (256 MiB write)"},
+        **{k: v for k, v in m.items() if k != "workload"},
+    }
+    line["value"] = m["mrays_per_s"]
     print(json.dumps(line), flush=True)
 
 
@@ -831,7 +843,7 @@ def main():
 
     # --- the batched and differentiation configurations, measured in the same process after
     # the plain timed region (their own timed regions, CUDA events, L2 flushed)
-    batch = adjoint = None
+    batch = adjoint = large = None
     if rank == 0 and ws == 1 and not args.no_extra:
         adjoint = measure_adjoint(args, steps=5, warmup=3)
         m = measure_batch(args, steps=3, warmup=3, with_ms1=False)
@@ -853,6 +865,7 @@ def main():
             "clocks": m["clocks"],
             "per_scene_clocks": m["per_scene"]["clocks"],
         }
+        large = measure_large(args, steps=2, warmup=1)
 
     if rank == 0:
         line = {
@@ -911,6 +924,7 @@ def main():
             "tuning": tune,
             "adjoint": adjoint,
             "batched": batch,
+            "large": large,
         }
         print(json.dumps(line), flush=True)
     r.close()

@@ -316,7 +316,8 @@ typedef struct tr_tuning {
     uint32_t connect_blocks_per_sm; /* persistent connect grid, 1..occupancy */
     uint32_t shade_waves;           /* shade grid cap in waves of resident blocks, 1..64 */
     uint32_t sort_hits;             /* 1: counting sort of each bounce's hits by material before shade */
-    uint32_t reserved[2];
+    uint32_t traversal_threads;     /* threads per block of the extend / connect launches: 64 or 128 */
+    uint32_t shade_threads;         /* threads per block of the shade launches: 64 or 128 */
 } tr_tuning;
 
 typedef struct tr_tune_report {

@@ -232,6 +232,16 @@ def test_tuning_keeps_images_and_autotune_picks_fastest():
     t = r.Tuning()
     assert t["refill_below"] == 12 and t["extend_blocks_per_sm"] == 2 and t["shade_waves"] == 1
     assert t["sort_hits"] == 1
+    # block sizes of the traversal and shade launches
+    r.SetTuning(traversal_threads=64, shade_threads=64, refill_below=12)
+    r.Reset()
+    r.RenderFrame(use_graph=True)
+    np.testing.assert_array_equal(r.ColorBuffer(), want)
+    t = r.Tuning()
+    assert t["traversal_threads"] == 64 and t["shade_threads"] == 64 and t["extend_blocks_per_sm"] >= 8
+    with pytest.raises(TracerError):
+        r.SetTuning(traversal_threads=256)
+    r.SetTuning(refill_below=12, extend_blocks_per_sm=2, connect_blocks_per_sm=3, shade_waves=1, sort_hits=1)
     # the per-stage entry points sort too when the sort is on
     r.Reset()
     r.BeginFrame()

@@ -196,7 +196,8 @@ class Tuning(C.Structure):
         ("connect_blocks_per_sm", C.c_uint32),
         ("shade_waves", C.c_uint32),
         ("sort_hits", C.c_uint32),
-        ("reserved", C.c_uint32 * 2),
+        ("traversal_threads", C.c_uint32),
+        ("shade_threads", C.c_uint32),
     ]
 
 

@@ -1008,6 +1008,8 @@ tr_status tr_get_tuning(void* ctx, tr_tuning* out)
         t.connect_blocks_per_sm = c->shape.connectBlocks / c->shape.sms;
         t.shade_waves = c->shape.shadeWaves;
         t.sort_hits = c->shape.sortHits;
+        t.traversal_threads = c->shape.traversalThreads;
+        t.shade_threads = c->shape.shadeThreads;
     }
     *out = t;
     return TR_OK;
@@ -1018,8 +1020,11 @@ tr_status tr_set_tuning(void* ctx, const tr_tuning* t)
     if (!ctx || !t)
         return TR_ERR_INVALID_ARGUMENT;
     Context* c = static_cast<Context*>(ctx);
-    if (t->bvh_leaf_size > 3 || t->refill_below > 32 || t->shade_waves > 64 || t->sort_hits > 1)
-        return fail(c, TR_ERR_INVALID_ARGUMENT, "tuning out of range (leaf size <= 3, refill <= 32, shade waves <= 64)");
+    auto threadsOk = [](uint32_t v) { return v == 0 || v == 64 || v == 128; };
+    if (t->bvh_leaf_size > 3 || t->refill_below > 32 || t->shade_waves > 64 || t->sort_hits > 1 ||
+        !threadsOk(t->traversal_threads) || !threadsOk(t->shade_threads))
+        return fail(c, TR_ERR_INVALID_ARGUMENT, "tuning out of range (leaf size <= 3, refill <= 32, shade waves <= 64, "
+                                                "block sizes 64 or 128)");
     cudaSetDevice(c->device);
     if (t->bvh_leaf_size && c->hasScene) {
         const tr_status st = rebuild_bvh(c, t->bvh_leaf_size);
@@ -1073,7 +1078,6 @@ tr_status tr_autotune(void* ctx, void* stream, uint32_t flags, tr_tune_report* r
     };
     tr_tuning best{};
     tr_get_tuning(ctx, &best);
-    const LaunchShape def = default_launch_shape(c->device, uint32_t(c->frame.capacity));
     float bestMs = 0.f, defaultMs = 0.f;
     st = timeFrames(&bestMs);
     defaultMs = bestMs;
@@ -1091,6 +1095,21 @@ tr_status tr_autotune(void* ctx, void* stream, uint32_t flags, tr_tune_report* r
         }
         return TR_OK;
     };
+    // block sizes first: the grids below are counted in blocks of the chosen size
+    for (uint32_t v : {64u}) {
+        tr_tuning t = best;
+        t.traversal_threads = v;
+        t.extend_blocks_per_sm = 0;
+        t.connect_blocks_per_sm = 0;
+        if (st == TR_OK && v != best.traversal_threads)
+            st = tryTuning(t);
+    }
+    for (uint32_t v : {64u}) {
+        tr_tuning t = best;
+        t.shade_threads = v;
+        if (st == TR_OK && v != best.shade_threads)
+            st = tryTuning(t);
+    }
     const uint32_t refills[] = {6, 8, 10, 12, 16, 20, 24, 28, 32};
     for (uint32_t v : refills) {
         tr_tuning t = best;
@@ -1098,6 +1117,10 @@ tr_status tr_autotune(void* ctx, void* stream, uint32_t flags, tr_tune_report* r
         if (st == TR_OK && v != best.refill_below)
             st = tryTuning(t);
     }
+    tr_tuning sized = best;
+    sized.extend_blocks_per_sm = 0;
+    sized.connect_blocks_per_sm = 0;
+    const LaunchShape def = tuned_launch_shape(c->device, uint32_t(c->frame.capacity), sized);
     for (uint32_t d : {def.extendPerSm / 2, def.extendPerSm * 3 / 4}) {
         tr_tuning t = best;
         t.extend_blocks_per_sm = d;

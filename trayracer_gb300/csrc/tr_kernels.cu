@@ -372,8 +372,9 @@ __device__ __forceinline__ void add_counts(unsigned long long* dst, const Traver
 
 // Persistent warps refill a lane with the next ray of the queue when fewer
 // than st.refillBelow of its 32 rays are still traversing (incoherent
-// secondary rays end at very different times); tuned per scene, 24 by default.
-constexpr uint32_t kRefillBelow = 24;
+// secondary rays end at very different times); tuned per scene, 10 by default
+// (what the autotuner picks on the benchmark heightfield, 8 to 10).
+constexpr uint32_t kRefillBelow = 10;
 
 // Closest hit of the bounce's extend queue. Rays that hit are appended (one
 // warp ballot and one atomic per step) to the hit queue with their full path
@@ -405,6 +406,8 @@ __device__ __noinline__ void sky_miss(const SceneView& s, const FrameView& f, co
 // BATCH: the extend queue of a batch iteration - entries [0, carried) are
 // paths carried over from the last iteration, the entries after them start
 // new samples (their camera rays are made here), so the pool stays full.
+// Blocks of 64 or 128 threads (a launch parameter, LaunchShape::traversalThreads):
+// the kernel works per warp; 64 registers, 32 resident warps per SM.
 template <bool COUNT, bool BATCH, bool PRIMARY, bool TL>
 __global__ void __launch_bounds__(128, 8) extend_kernel(SceneView s, FrameView f, Settings st, uint32_t bounce,
                                                      Camera cam)
@@ -889,6 +892,12 @@ __device__ __forceinline__ bool shade_path(const SceneView& s, const FrameView& 
     return false;
 }
 
+// Dynamic shared memory of the shade kernel per thread: two staging buffers of
+// the path state's three planes and the hit record.
+constexpr uint32_t kShadeStageBytes = 2u * 4u * sizeof(float4);
+
+// Blocks of 64 or 128 threads (LaunchShape::shadeThreads; dynamic shared memory
+// of kShadeStageBytes per thread for the input staging), at most 96 registers.
 template <bool REF, bool BATCH, bool TEX = false>
 __global__ void __launch_bounds__(128, 5) shade_kernel(SceneView s, FrameView f, Settings st, uint32_t bounce)
 {
@@ -907,15 +916,19 @@ __global__ void __launch_bounds__(128, 5) shade_kernel(SceneView s, FrameView f,
     // this item is shaded. Two buffers: the one refilled was read an iteration
     // earlier, by loads whose values that iteration's shading consumed, so the
     // copy cannot overtake them.
-    __shared__ float4 stage[2][4][128];
+    // stage[(b * 4 + plane) * blockDim.x + thread]: two buffers of the state's
+    // three planes and the hit record
+    extern __shared__ float4 stage[];
     const uint32_t tid = threadIdx.x;
+    const uint32_t bd = blockDim.x;
     uint32_t buf = 0;
+    auto at = [&](uint32_t b, uint32_t plane) -> float4* { return stage + (b * 4u + plane) * bd + tid; };
     auto fetch = [&](uint32_t k, uint32_t b) {
         const uint32_t i = f.hitOrder ? __ldcs(f.hitOrder + k) : k;
-        cp_async16(&stage[b][0][tid], in + i);
-        cp_async16(&stage[b][1][tid], in + i + cap);
-        cp_async16(&stage[b][2][tid], in + i + 2 * cap);
-        cp_async16(&stage[b][3][tid], f.hits + i);
+        cp_async16(at(b, 0), in + i);
+        cp_async16(at(b, 1), in + i + cap);
+        cp_async16(at(b, 2), in + i + 2 * cap);
+        cp_async16(at(b, 3), f.hits + i);
         cp_async_commit();
     };
     if (warpGlobal * 32u + lane < count)
@@ -927,10 +940,10 @@ __global__ void __launch_bounds__(128, 5) shade_kernel(SceneView s, FrameView f,
         float4 ext[3], sh[3];
         if (k < count) {
             cp_async_wait_all();
-            const float4 O4 = stage[buf][0][tid];
-            const float4 D4 = stage[buf][1][tid];
-            const float4 T4 = stage[buf][2][tid];
-            const float4 h = stage[buf][3][tid];
+            const float4 O4 = *at(buf, 0);
+            const float4 D4 = *at(buf, 1);
+            const float4 T4 = *at(buf, 2);
+            const float4 h = *at(buf, 3);
             const uint4 hd = make_uint4(__float_as_uint(h.x), __float_as_uint(h.y), __float_as_uint(h.z),
                                         __float_as_uint(h.w));
             buf ^= 1u;
@@ -1074,6 +1087,7 @@ __global__ void __launch_bounds__(256) sort_scatter_kernel(FrameView f, SortView
 
 // Any hit of the bounce's shadow queue over [eps, dist - 2 eps]; an unoccluded
 // ray adds its radiance to its path. Same lane refill as extend_kernel.
+// Blocks of 64 or 128 threads (LaunchShape::traversalThreads): the kernel works per warp.
 template <bool COUNT, bool BATCH, bool TL>
 __global__ void __launch_bounds__(128) connect_kernel(SceneView s, FrameView f, Settings st, uint32_t bounce)
 {
@@ -1887,19 +1901,19 @@ void launch_extend_variant(const SceneView& s0, const FrameView& f, const Settin
     const uint32_t g = shape.extendBlocks;
     if (f.batch) {
         if (count)
-            extend_kernel<true, true, PRIMARY, false><<<g, 128, 0, stream>>>(s, f, st, bounce, cam);
+            extend_kernel<true, true, PRIMARY, false><<<g, shape.traversalThreads, 0, stream>>>(s, f, st, bounce, cam);
         else
-            extend_kernel<false, true, PRIMARY, false><<<g, 128, 0, stream>>>(s, f, st, bounce, cam);
+            extend_kernel<false, true, PRIMARY, false><<<g, shape.traversalThreads, 0, stream>>>(s, f, st, bounce, cam);
     } else if (s.tlasNodes) {
         if (count)
-            extend_kernel<true, false, PRIMARY, true><<<g, 128, 0, stream>>>(s, f, st, bounce, cam);
+            extend_kernel<true, false, PRIMARY, true><<<g, shape.traversalThreads, 0, stream>>>(s, f, st, bounce, cam);
         else
-            extend_kernel<false, false, PRIMARY, true><<<g, 128, 0, stream>>>(s, f, st, bounce, cam);
+            extend_kernel<false, false, PRIMARY, true><<<g, shape.traversalThreads, 0, stream>>>(s, f, st, bounce, cam);
     } else {
         if (count)
-            extend_kernel<true, false, PRIMARY, false><<<g, 128, 0, stream>>>(s, f, st, bounce, cam);
+            extend_kernel<true, false, PRIMARY, false><<<g, shape.traversalThreads, 0, stream>>>(s, f, st, bounce, cam);
         else
-            extend_kernel<false, false, PRIMARY, false><<<g, 128, 0, stream>>>(s, f, st, bounce, cam);
+            extend_kernel<false, false, PRIMARY, false><<<g, shape.traversalThreads, 0, stream>>>(s, f, st, bounce, cam);
     }
 }
 
@@ -1919,16 +1933,17 @@ cudaError_t launch_shade(const SceneView& s, const FrameView& f, const Settings&
                          const LaunchShape& shape, cudaStream_t stream)
 {
     const bool ref = (st.flags & TR_FLAG_REFERENCE_SAMPLING) != 0;
+    const size_t smem = size_t(shape.shadeThreads) * kShadeStageBytes;
     if (f.batch)
-        shade_kernel<false, true><<<shape.shadeBlocks, 128, 0, stream>>>(s, f, st, bounce);
+        shade_kernel<false, true><<<shape.shadeBlocks, shape.shadeThreads, smem, stream>>>(s, f, st, bounce);
     else if (s.texSlots && ref)
-        shade_kernel<true, false, true><<<shape.shadeBlocks, 128, 0, stream>>>(s, f, st, bounce);
+        shade_kernel<true, false, true><<<shape.shadeBlocks, shape.shadeThreads, smem, stream>>>(s, f, st, bounce);
     else if (s.texSlots)
-        shade_kernel<false, false, true><<<shape.shadeBlocks, 128, 0, stream>>>(s, f, st, bounce);
+        shade_kernel<false, false, true><<<shape.shadeBlocks, shape.shadeThreads, smem, stream>>>(s, f, st, bounce);
     else if (ref)
-        shade_kernel<true, false><<<shape.shadeBlocks, 128, 0, stream>>>(s, f, st, bounce);
+        shade_kernel<true, false><<<shape.shadeBlocks, shape.shadeThreads, smem, stream>>>(s, f, st, bounce);
     else
-        shade_kernel<false, false><<<shape.shadeBlocks, 128, 0, stream>>>(s, f, st, bounce);
+        shade_kernel<false, false><<<shape.shadeBlocks, shape.shadeThreads, smem, stream>>>(s, f, st, bounce);
     return cudaGetLastError();
 }
 
@@ -1942,19 +1957,19 @@ cudaError_t launch_connect(const SceneView& s0, const FrameView& f, const Settin
     const uint32_t g = shape.connectBlocks;
     if (f.batch) {
         if (count)
-            connect_kernel<true, true, false><<<g, 128, 0, stream>>>(s, f, st, bounce);
+            connect_kernel<true, true, false><<<g, shape.traversalThreads, 0, stream>>>(s, f, st, bounce);
         else
-            connect_kernel<false, true, false><<<g, 128, 0, stream>>>(s, f, st, bounce);
+            connect_kernel<false, true, false><<<g, shape.traversalThreads, 0, stream>>>(s, f, st, bounce);
     } else if (s.tlasNodes) {
         if (count)
-            connect_kernel<true, false, true><<<g, 128, 0, stream>>>(s, f, st, bounce);
+            connect_kernel<true, false, true><<<g, shape.traversalThreads, 0, stream>>>(s, f, st, bounce);
         else
-            connect_kernel<false, false, true><<<g, 128, 0, stream>>>(s, f, st, bounce);
+            connect_kernel<false, false, true><<<g, shape.traversalThreads, 0, stream>>>(s, f, st, bounce);
     } else {
         if (count)
-            connect_kernel<true, false, false><<<g, 128, 0, stream>>>(s, f, st, bounce);
+            connect_kernel<true, false, false><<<g, shape.traversalThreads, 0, stream>>>(s, f, st, bounce);
         else
-            connect_kernel<false, false, false><<<g, 128, 0, stream>>>(s, f, st, bounce);
+            connect_kernel<false, false, false><<<g, shape.traversalThreads, 0, stream>>>(s, f, st, bounce);
     }
     return cudaGetLastError();
 }
@@ -1988,17 +2003,19 @@ cudaError_t launch_adjoint(const SceneView& s0, const FrameView& f, const Camera
     if (e != cudaSuccess)
         return e;
     const uint32_t gradBlocks = shape.sms * uint32_t(perSm > 0 ? perSm : 1);
+    // the replay's connect runs 128-thread blocks: as many threads as the forward connect grid
+    const uint32_t connectBlocks128 = (shape.connectBlocks * shape.traversalThreads + 127u) / 128u;
     Settings fwd = st;
     fwd.flags &= ~uint32_t(TR_FLAG_COUNT_TRAVERSAL | TR_FLAG_WRITE_AOVS);
     fwd.refillBelow = shape.refillBelow;
     adjoint_generate_kernel<<<(f.pathCount + 255u) / 256u, 256, 0, stream>>>(f, cam, fwd, a);
     for (uint32_t bounce = 0; bounce < st.maxDepth; ++bounce) {
         if (s.tlasNodes)
-            extend_kernel<false, false, false, true><<<shape.extendBlocks, 128, 0, stream>>>(s, f, fwd, bounce,
-                                                                                          Camera{});
+            extend_kernel<false, false, false, true><<<shape.extendBlocks, shape.traversalThreads, 0, stream>>>(
+                s, f, fwd, bounce, Camera{});
         else
-            extend_kernel<false, false, false, false><<<shape.extendBlocks, 128, 0, stream>>>(s, f, fwd, bounce,
-                                                                                           Camera{});
+            extend_kernel<false, false, false, false><<<shape.extendBlocks, shape.traversalThreads, 0, stream>>>(
+                s, f, fwd, bounce, Camera{});
         if (bounce > 0) {
             if (useSmem)
                 ext_grad_kernel<true><<<gradBlocks, kAdjointThreads, smem, stream>>>(s, f, bounce, a);
@@ -2010,9 +2027,9 @@ cudaError_t launch_adjoint(const SceneView& s0, const FrameView& f, const Camera
         else
             adjoint_shade_kernel<false><<<gradBlocks, kAdjointThreads, 0, stream>>>(s, f, fwd, bounce, a);
         if (s.tlasNodes)
-            adjoint_connect_kernel<true><<<shape.connectBlocks, 128, 0, stream>>>(s, f, fwd, bounce, a);
+            adjoint_connect_kernel<true><<<connectBlocks128, 128, 0, stream>>>(s, f, fwd, bounce, a);
         else
-            adjoint_connect_kernel<false><<<shape.connectBlocks, 128, 0, stream>>>(s, f, fwd, bounce, a);
+            adjoint_connect_kernel<false><<<connectBlocks128, 128, 0, stream>>>(s, f, fwd, bounce, a);
         if (useSmem)
             nee_grad_kernel<true><<<gradBlocks, kAdjointThreads, smem, stream>>>(s, f, bounce, a);
         else
@@ -2063,29 +2080,48 @@ cudaError_t launch_batch_finalize(const FrameView& f, uint32_t pixelBegin, uint3
     return cudaGetLastError();
 }
 
+namespace {
+// Resident blocks per SM of `kernel` at `threads` per block (4 when the query fails).
+template <class Kernel>
+uint32_t resident(Kernel kernel, uint32_t threads, size_t smem)
+{
+    int perSm = 0;
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&perSm, kernel, int(threads), smem);
+    return uint32_t(perSm > 0 ? perSm : 4);
+}
+
+// Block sizes the traversal and shade kernels take: their register budgets are
+// set for blocks of at most 128 threads.
+bool valid_threads(uint32_t t) { return t == 64u || t == 128u; }
+
+// Grids of a shape for its block sizes: the persistent traversal kernels at
+// their occupancy limit, shade capped at shadeWaves waves of resident blocks.
+void size_grids(LaunchShape& shape, uint32_t capacity)
+{
+    shape.extendPerSm = resident(extend_kernel<false, false, false, false>, shape.traversalThreads, 0);
+    shape.connectPerSm = resident(connect_kernel<false, false, false>, shape.traversalThreads, 0);
+    shape.extendBlocks = shape.sms * shape.extendPerSm;
+    shape.connectBlocks = shape.sms * shape.connectPerSm;
+    const uint32_t maxShade = shape.sms *
+                              resident(shade_kernel<false, false>, shape.shadeThreads,
+                                       size_t(shape.shadeThreads) * kShadeStageBytes) *
+                              shape.shadeWaves;
+    const uint32_t need = (capacity + shape.shadeThreads - 1u) / shape.shadeThreads;
+    shape.shadeBlocks = need < maxShade ? (need > 0 ? need : 1u) : maxShade;
+}
+} // namespace
+
 LaunchShape default_launch_shape(int device, uint32_t capacity)
 {
     LaunchShape shape;
     int sms = 0;
     cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, device);
-    if (sms <= 0)
-        sms = 1;
-    int perSm = 0;
-    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&perSm, extend_kernel<false, false, false, false>, 128, 0);
-    shape.extendBlocks = uint32_t(sms) * uint32_t(perSm > 0 ? perSm : 4);
-    perSm = 0;
-    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&perSm, connect_kernel<false, false, false>, 128, 0);
-    shape.connectBlocks = uint32_t(sms) * uint32_t(perSm > 0 ? perSm : 4);
-    perSm = 0;
-    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&perSm, shade_kernel<false, false>, 128, 0);
-    const uint32_t maxShade = uint32_t(sms) * uint32_t(perSm > 0 ? perSm : 4) * 4u;
-    const uint32_t need = (capacity + 127u) / 128u;
-    shape.shadeBlocks = need < maxShade ? (need > 0 ? need : 1u) : maxShade;
-    shape.sms = uint32_t(sms);
+    shape.sms = uint32_t(sms > 0 ? sms : 1);
     shape.refillBelow = kRefillBelow;
-    shape.extendPerSm = uint32_t(shape.extendBlocks / shape.sms);
-    shape.connectPerSm = uint32_t(shape.connectBlocks / shape.sms);
     shape.shadeWaves = 4;
+    shape.traversalThreads = 128;
+    shape.shadeThreads = 128;
+    size_grids(shape, capacity);
     return shape;
 }
 
@@ -2094,19 +2130,18 @@ LaunchShape tuned_launch_shape(int device, uint32_t capacity, const tr_tuning& t
     LaunchShape shape = default_launch_shape(device, capacity);
     if (t.refill_below >= 1 && t.refill_below <= 32)
         shape.refillBelow = t.refill_below;
+    if (t.shade_waves >= 1 && t.shade_waves <= 64)
+        shape.shadeWaves = t.shade_waves;
+    if (valid_threads(t.traversal_threads))
+        shape.traversalThreads = t.traversal_threads;
+    if (valid_threads(t.shade_threads))
+        shape.shadeThreads = t.shade_threads;
+    size_grids(shape, capacity);
     if (t.extend_blocks_per_sm >= 1 && t.extend_blocks_per_sm <= shape.extendPerSm)
         shape.extendBlocks = shape.sms * t.extend_blocks_per_sm;
     if (t.connect_blocks_per_sm >= 1 && t.connect_blocks_per_sm <= shape.connectPerSm)
         shape.connectBlocks = shape.sms * t.connect_blocks_per_sm;
     shape.sortHits = t.sort_hits ? 1u : 0u;
-    if (t.shade_waves >= 1 && t.shade_waves <= 64) {
-        int perSm = 0;
-        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&perSm, shade_kernel<false, false>, 128, 0);
-        const uint32_t maxShade = shape.sms * uint32_t(perSm > 0 ? perSm : 4) * t.shade_waves;
-        const uint32_t need = (capacity + 127u) / 128u;
-        shape.shadeBlocks = need < maxShade ? (need > 0 ? need : 1u) : maxShade;
-        shape.shadeWaves = t.shade_waves;
-    }
     return shape;
 }
 

@@ -16,11 +16,13 @@ struct LaunchShape {
     uint32_t connectBlocks = 0;
     uint32_t shadeBlocks = 0;
     uint32_t sms = 0;
-    uint32_t refillBelow = 24;   // lane refill threshold of the persistent traversal warps
+    uint32_t refillBelow = 10;   // lane refill threshold of the persistent traversal warps
     uint32_t extendPerSm = 0;    // resident extend / connect blocks per SM (occupancy limit by default)
     uint32_t connectPerSm = 0;
     uint32_t shadeWaves = 4;     // shade grid cap, in waves of resident blocks
     uint32_t sortHits = 0;       // 1: counting sort of each bounce's hit queue by material before shade
+    uint32_t traversalThreads = 128;  // block size of the extend and connect launches (64 or 128)
+    uint32_t shadeThreads = 128;      // block size of the shade launches (64 or 128)
 };
 
 LaunchShape default_launch_shape(int device, uint32_t capacity);
