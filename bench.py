@@ -6,10 +6,12 @@ value-noise heightfield (2,093,058 triangles) + 64 emissive triangles
 materials on 64 x 64 tiles, 1920 x 1080, 64 samples per pixel, 8 bounces,
 Russian roulette from bounce 3, counter-based RNG, fp32. Synthetic, seeded.
 
-One step = one full 64-spp frame set of that image: reset, then 64 / ms
-wavefront frames of ms samples per pixel (ms = 16: 33.2 M paths in flight),
-each frame a captured CUDA graph of generate, 8 x (extend, shade, connect),
-finalize. The metric is the reference's Mrays/s = (extend + shadow rays) /
+One step = all 64 samples per pixel of that image: reset, then one
+tr_render_samples call that renders them as one continuous wavefront through
+the frame's 1920 x 1080 x ms path slots (ms = 16: 33.2 M paths in flight),
+refilled with the next samples as paths end; its iterations (plan, connect,
+extend, shade) run as one CUDA graph with a device-driven while loop. The
+per-stage figures come from eager frames of the same samples. The metric is the reference's Mrays/s = (extend + shadow rays) /
 time (Tracer/GUI/MainGui.cpp:97-100,801-805); samples/s is reported beside it.
 
     python bench.py [--steps K] [--warmup W] [--gpus N] [--impl reference]
@@ -202,7 +204,11 @@ def band_accuracy(r, scene, args, frames, sptr, rows=16, spp_long=1024, rows_lon
     st = tr.settings_for(scene, multi_sample=ms)
     threads = os.cpu_count() or 1
     orc = Oracle(scene)
-    img = r.ColorBuffer()
+    img = r.ColorBuffer()  # the benchmark step's image (one continuous wavefront of all samples)
+    # the same samples frame by frame, for the per-path radiance of the last frame
+    r.Reset()
+    for _ in range(frames):
+        r.RenderFrame(stream=sptr, use_graph=True)
     buf = r.Buffers()
     ys = [(k * H) // rows + H // (2 * rows) for k in range(rows)]
     g_img, o32, o64, ok = [], [], [], []
@@ -694,9 +700,9 @@ def main():
     flush = torch.empty(256 * 1024 * 1024 // 4, dtype=torch.float32, device=f"cuda:{local}")
 
     def step(use_graph=True):
+        # all spp samples as one continuous wavefront through the frame's path slots
         r.Reset()
-        for _ in range(frames_per_step):
-            r.RenderFrame(stream=sptr, use_graph=use_graph)
+        r.RenderSamples(args.spp, stream=sptr, use_graph=use_graph)
 
     # --- autotuner (launch shapes, BVH leaf size) on this workload, outside the timed region
     tune = None
@@ -763,6 +769,10 @@ def main():
         total_ms = max_over_ranks(total_ms, device=f"cuda:{local}")
     final = r.Statistics()
     assert final["device_error"] == 0
+    # the rays of one step as the continuous wavefront traced them (the counting pass above
+    # renders the same samples frame by frame, for the per-stage figures)
+    frame_rays_per_step = rays_per_step
+    rays_per_step = final["path_count"]
 
     # --- end to end through the public API, host buffers: per step the camera
     # and settings are handed over from host structs, the frame set is rendered
@@ -916,10 +926,11 @@ def main():
                 "h2d_bytes_per_step": 72 + 32,
                 "d2h_bytes_per_step": scene.width * scene.height * 16,
             },
-            # per frame: extend, shade and connect per bounce (and the three kernels of the hit
-            # sort when the tuning turned it on), then finalize and advance: 26 for 8 bounces
-            "gpu_launches": args.steps * frames_per_step * ((3 + (3 if r.Tuning().get("sort_hits") else 0))
-                                                            * st.maxDepth + 2),
+            # per step: the continuous wavefront's plan, connect, extend and shade per iteration
+            # plus its start, finalize and advance
+            "gpu_launches": args.steps * final["launches"],
+            "iterations_per_step": final["iterations"],
+            "frame_rays_per_step": int(frame_rays_per_step),
             "scene_upload_s": round(upload_s, 2),
             "tuning": tune,
             "adjoint": adjoint,

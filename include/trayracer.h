@@ -260,6 +260,8 @@ typedef struct tr_statistics {
      * read-modify-writes by shade (emissive hits) and by connect (unoccluded shadow rays) */
     uint64_t radiance_updates_shade;
     uint64_t radiance_updates_connect;
+    uint32_t iterations;            /* after tr_render_samples: continuous-wavefront iterations that traced rays */
+    uint32_t launches;              /* after tr_render_samples: kernels of that render */
 } tr_statistics;
 
 /* Scene numbers: triangle/light/BVH sizes and the host build time. */
@@ -362,6 +364,25 @@ tr_status tr_finalize(void* ctx, void* stream);
  * round trips; with use_graph != 0 it is captured once per configuration into
  * a CUDA graph and replayed. */
 tr_status tr_render_frame(void* ctx, void* stream, int32_t use_graph);
+
+/* spp samples per pixel (a multiple of multi_sample) added to the
+ * accumulation, as spp / multi_sample calls of tr_render_frame would add them
+ * (the same sample keys), but rendered as one continuous wavefront: the
+ * frame's width * height * multi_sample path slots are kept full from a device
+ * sample cursor, each path regenerated with the next sample as soon as it
+ * ends, so the frames' late bounces do not leave the GPU idle between frames;
+ * with use_graph the iterations run as a CUDA graph while loop. The image
+ * equals the frame sequence's up to the order of the per-pixel sums (all spp
+ * samples summed in sample order, not frame by frame). Allocates 16 B per
+ * sample for the per-sample radiance. Where the continuous kernels do not
+ * apply (TR_FLAG_REFERENCE_SAMPLING, TR_FLAG_WRITE_AOVS, two-level or
+ * textured scenes, other render modes, more than 2^30 samples) it renders the
+ * frames. After it, tr_get_statistics reports totals: path_count,
+ * shadow_ray_count, primary_path_count (width * height * spp) and
+ * secondary_path_count (every other extend ray); the per-bounce arrays and
+ * stage times are zero. No reference counterpart (DeviceRenderer renders one
+ * frame per call, Tracer/Renderer/DeviceRenderer.cpp:97-133). */
+tr_status tr_render_samples(void* ctx, void* stream, uint32_t spp, int32_t use_graph);
 
 /* Path-replay adjoint (Vicini, Speierer, Jakob, SIGGRAPH 2021) of the last
  * rendered frame: adds to param_grad (device, material_count x 9 floats:

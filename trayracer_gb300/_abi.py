@@ -154,6 +154,8 @@ class Statistics(C.Structure):
         ("hit_rays", C.c_uint32 * TR_MAX_DEPTH),
         ("radiance_updates_shade", C.c_uint64),
         ("radiance_updates_connect", C.c_uint64),
+        ("iterations", C.c_uint32),
+        ("launches", C.c_uint32),
     ]
 
 
@@ -324,6 +326,7 @@ FUNCTIONS = {
     "tr_connect": (C.c_int, [_V, _V, _U]),
     "tr_finalize": (C.c_int, [_V, _V]),
     "tr_render_frame": (C.c_int, [_V, _V, C.c_int32]),
+    "tr_render_samples": (C.c_int, [_V, _V, _U, C.c_int32]),
     "tr_synchronize": (C.c_int, [_V, _V]),
     "tr_get_statistics": (C.c_int, [_V, C.POINTER(Statistics)]),
     "tr_get_buffers": (C.c_int, [_V, C.POINTER(Buffers)]),

@@ -22,6 +22,7 @@
 #include "tr_api_internal.h"
 #include "tr_accel.h"
 #include "tr_bvh.h"
+#include "tr_continuous.h"
 #include "tr_kernels.h"
 #include "tr_sky.h"
 #include "tr_scene.h"
@@ -140,6 +141,21 @@ struct Context {
     cudaGraphExec_t graphExec = nullptr;
     bool graphValid = false;
 
+    // tr_render_samples: per-sample radiance, the one item and the iteration
+    // state of the continuous wavefront, and its graph (per sample count)
+    DeviceArena samplesArena;
+    uint64_t samplesCapacity = 0;      // per-sample radiance entries the arena holds
+    float4* sampleRadiance = nullptr;
+    BatchItem* samplesItem = nullptr;
+    BatchState* samplesState = nullptr;
+    BatchItem samplesItemHost{};       // what samplesItem holds
+    bool samplesItemValid = false;
+    cudaGraph_t samplesGraph = nullptr;
+    cudaGraphExec_t samplesExec = nullptr;
+    uint32_t samplesGraphSpp = 0;
+    bool lastSamples = false;          // the last render was tr_render_samples' continuous wavefront
+    uint32_t lastSamplesPaths = 0;
+
     // frames rendered by tr_render_frame_noalloc: the launch shape for their
     // capacity and tuning, and whether the last frame was one of them
     LaunchShape noallocShape{};
@@ -192,6 +208,14 @@ void invalidate_graph(Context* c)
     c->graphExec = nullptr;
     c->graph = nullptr;
     c->graphValid = false;
+    if (c->samplesExec)
+        cudaGraphExecDestroy(c->samplesExec);
+    if (c->samplesGraph)
+        cudaGraphDestroy(c->samplesGraph);
+    c->samplesExec = nullptr;
+    c->samplesGraph = nullptr;
+    c->samplesGraphSpp = 0;
+    c->samplesItemValid = false;
 }
 
 void release_textures(Context* c)
@@ -313,6 +337,8 @@ tr_status ensure_frame(Context* c)
     invalidate_graph(c);
     c->frameArena.release();
     c->adjointArena.release();
+    c->samplesArena.release();
+    c->samplesCapacity = 0;
     const size_t cap = size_t(paths);
     size_t off = 0;
     auto take = [&](size_t bytes) {
@@ -508,6 +534,7 @@ void context_note_noalloc_frame(void* ctx, uint32_t paths)
 {
     Context* c = static_cast<Context*>(ctx);
     c->lastFrameNoalloc = true;
+    c->lastSamples = false;
     c->noallocPaths = paths;
     c->timedFrame = false;
 }
@@ -648,6 +675,7 @@ tr_status tr_destroy(void* ctx)
     c->bvhArena.release();
     c->frameArena.release();
     c->adjointArena.release();
+    c->samplesArena.release();
     release_textures(c);
     cudaEvent_t* evs[] = {&c->evStart, &c->evGenerate, &c->evFinal, &c->evFork, &c->evJoin};
     for (cudaEvent_t* e : evs)
@@ -1256,6 +1284,7 @@ tr_status tr_begin_frame(void* ctx, void* stream)
         return st;
     c->timedFrame = false;
     c->lastFrameNoalloc = false;
+    c->lastSamples = false;
     c->lastStream = pick_stream(c, stream);
     return enqueue_begin(c, c->lastStream);
 }
@@ -1350,6 +1379,7 @@ tr_status tr_render_frame(void* ctx, void* stream, int32_t use_graph)
     cudaStream_t s = pick_stream(c, stream);
     c->lastStream = s;
     c->lastFrameNoalloc = false;
+    c->lastSamples = false;
     if (use_graph) {
         if (!c->graphValid) {
             // capture on the context stream (the legacy default stream cannot be captured)
@@ -1378,6 +1408,112 @@ tr_status tr_render_frame(void* ctx, void* stream, int32_t use_graph)
         c->timedDepth = c->settings.maxDepth;
     }
     c->sampleCount += c->settings.multiSample;
+    return TR_OK;
+}
+
+// tr_render_samples: one continuous wavefront of width * height * spp samples
+// through the frame's path slots (the batch kernels with one item), or, where
+// those kernels do not apply, spp / multi_sample frames.
+tr_status tr_render_samples(void* ctx, void* stream, uint32_t spp, int32_t use_graph)
+{
+    if (!ctx)
+        return TR_ERR_INVALID_ARGUMENT;
+    Context* c = static_cast<Context*>(ctx);
+    cudaSetDevice(c->device);
+    tr_status st = check_ready(c);
+    if (st != TR_OK)
+        return st;
+    const uint32_t ms = c->settings.multiSample;
+    if (spp == 0 || spp % ms != 0)
+        return fail(c, TR_ERR_INVALID_ARGUMENT, "spp must be a positive multiple of multi_sample");
+    const uint64_t wh = uint64_t(c->width) * c->height;
+    const uint64_t samples = wh * spp;
+    const uint32_t flags = c->settings.flags;
+    const bool continuous = c->renderMode == kModePathTracing &&
+                            (flags & (TR_FLAG_REFERENCE_SAMPLING | TR_FLAG_WRITE_AOVS)) == 0 && !c->scene.tlasNodes &&
+                            !c->scene.texSlots && samples <= (1ull << 30);
+    if (!continuous) {
+        for (uint32_t k = 0; k < spp / ms && st == TR_OK; ++k)
+            st = tr_render_frame(ctx, stream, use_graph);
+        return st;
+    }
+    // per-sample radiance, the item and the iteration state
+    if (c->samplesCapacity < samples) {
+        invalidate_graph(c);
+        c->samplesArena.release();
+        c->samplesCapacity = 0;
+        const size_t oRad = 0;
+        const size_t oItem = align256(size_t(samples) * sizeof(float4));
+        const size_t oState = align256(oItem + sizeof(BatchItem));
+        const size_t bytes = align256(oState + sizeof(BatchState));
+        void* base = nullptr;
+        const cudaError_t e = cudaMalloc(&base, bytes);
+        if (e != cudaSuccess)
+            return cuda_fail(c, e, "cudaMalloc(sample radiance)");
+        c->samplesArena.base = base;
+        c->samplesArena.bytes = bytes;
+        char* b = static_cast<char*>(base);
+        c->sampleRadiance = reinterpret_cast<float4*>(b + oRad);
+        c->samplesItem = reinterpret_cast<BatchItem*>(b + oItem);
+        c->samplesState = reinterpret_cast<BatchState*>(b + oState);
+        c->samplesCapacity = samples;
+    }
+    BatchItem it{};
+    it.camera = c->camera;
+    it.width = c->width;
+    it.height = c->height;
+    it.root = 0;
+    it.lightBase = 0;
+    it.lightCount = c->scene.lightCount;
+    it.lightEnergy = c->scene.lightEnergy;
+    it.lightEnergyTotal = c->scene.lightEnergyTotal;
+    it.pixelBase = 0;
+    it.spp = spp;
+    it.sampleBase = 0;
+    cudaStream_t s = pick_stream(c, stream);
+    if (!c->samplesItemValid || std::memcmp(&it, &c->samplesItemHost, sizeof(BatchItem)) != 0) {
+        c->samplesItemHost = it;
+        TR_CUDA(c, cudaMemcpy(c->samplesItem, &c->samplesItemHost, sizeof(BatchItem), cudaMemcpyHostToDevice));
+        c->samplesItemValid = true;
+    }
+    FrameView f = c->frame;
+    f.radiance = c->sampleRadiance;
+    f.batch = c->samplesState;
+    f.items = c->samplesItem;
+    f.itemCount = 1;
+    f.hitOrder = nullptr;
+    f.pathCount = uint32_t(c->frameCapacity);
+    LaunchShape shape = c->shape;
+    shape.sortHits = 0;
+    const ContinuousLaunch L{c->scene, c->settings, shape, uint32_t(c->frameCapacity), c->side, c->evFork,
+                             c->evJoin};
+    const std::vector<ContinuousRound> rounds{ContinuousRound{f, uint32_t(samples), 0u, uint32_t(wh)}};
+    if (use_graph && (flags & TR_FLAG_COUNT_TRAVERSAL) == 0) {
+        if (!c->samplesExec || c->samplesGraphSpp != spp) {
+            if (c->samplesExec)
+                cudaGraphExecDestroy(c->samplesExec);
+            if (c->samplesGraph)
+                cudaGraphDestroy(c->samplesGraph);
+            c->samplesExec = nullptr;
+            c->samplesGraph = nullptr;
+            // captured on the context's own stream, which must be idle
+            TR_CUDA(c, cudaStreamSynchronize(c->stream));
+            cudaGraph_t g = nullptr;
+            TR_CUDA(c, capture_continuous(L, rounds, spp, c->stream, &g));
+            c->samplesGraph = g;
+            TR_CUDA(c, cudaGraphInstantiate(&c->samplesExec, g, 0));
+            c->samplesGraphSpp = spp;
+        }
+        TR_CUDA(c, cudaGraphLaunch(c->samplesExec, s));
+    } else {
+        TR_CUDA(c, run_continuous_eager(L, rounds, spp, s));
+    }
+    c->lastStream = s;
+    c->timedFrame = false;
+    c->lastFrameNoalloc = false;
+    c->lastSamples = true;
+    c->lastSamplesPaths = uint32_t(samples);
+    c->sampleCount += spp;
     return TR_OK;
 }
 
@@ -1418,6 +1554,29 @@ tr_status tr_get_statistics(void* ctx, tr_statistics* out)
     TR_CUDA(c, cudaMemcpy(&err, words.errorFlag, sizeof(uint32_t), cudaMemcpyDeviceToHost));
     TR_CUDA(c, cudaMemcpy(&sc, words.sampleCount, sizeof(uint32_t), cudaMemcpyDeviceToHost));
     tr_statistics s{};
+    if (c->lastSamples) {
+        // the continuous wavefront keeps totals, not per-bounce queue lengths
+        BatchState bs{};
+        TR_CUDA(c, cudaMemcpy(&bs, c->samplesState, sizeof(bs), cudaMemcpyDeviceToHost));
+        s.primary_path_count = c->lastSamplesPaths;
+        s.secondary_path_count = bs.extendRays - c->lastSamplesPaths;
+        s.shadow_ray_count = bs.shadowRays;
+        s.path_count = bs.extendRays + bs.shadowRays;
+        s.sample_count = sc;
+        s.device_error = err;
+        s.traversal_extend_nodes = trav[0];
+        s.traversal_extend_tris = trav[1];
+        s.traversal_connect_nodes = trav[2];
+        s.traversal_connect_tris = trav[3];
+        s.radiance_updates_shade = trav[4];
+        s.radiance_updates_connect = trav[5];
+        s.iterations = bs.iterations;
+        // start, finalize, advance, and plan + connect + extend + shade per iteration (the
+        // last finds nothing to trace)
+        s.launches = 3u + 4u * (bs.iterations + 1u);
+        *out = s;
+        return TR_OK;
+    }
     const uint32_t depth = c->settings.maxDepth;
     for (uint32_t b = 0; b < depth; ++b) {
         s.extend_rays[b] = b == 0 ? primary : counters[b];

@@ -32,6 +32,7 @@
 #include "../../include/trayracer.h"
 #include "tr_api_internal.h"
 #include "tr_bvh.h"
+#include "tr_continuous.h"
 #include "tr_kernels.h"
 #include "tr_scene.h"
 
@@ -224,48 +225,20 @@ FrameView round_view(const Batch* b, uint32_t k)
     return f;
 }
 
-// One iteration of round k: plan, connect of the last iteration's shadow rays
-// and extend (carried paths + new samples), shade. Connect adds to the
-// radiance of paths in flight and reads the shadow queue, extend reads the
-// extend queue and starts new samples: they share nothing, so with `overlap`
-// connect runs on the side stream beside extend; shade (which rewrites the
-// shadow queue and adds emission to the same radiance) waits for both. The
-// last iteration of a round traces nothing new and runs the final connect.
-cudaError_t enqueue_iteration(Batch* b, uint32_t k, const Settings& st, cudaGraphConditionalHandle loop,
-                              bool useLoop, cudaStream_t s, bool overlap)
+// The rounds as the continuous wavefront runs them.
+std::vector<ContinuousRound> continuous_rounds(const Batch* b)
 {
-    const FrameView f = round_view(b, k);  // each path uses its item's camera
-    const uint64_t bound = uint64_t(b->rounds[k].samples) * st.maxDepth + 4u;
-    const uint32_t limit = bound < 0xffffffffull ? uint32_t(bound) : 0xffffffffu;
-    cudaError_t e = launch_batch_plan(f.batch, b->pool, b->rounds[k].samples, limit, f.errorFlag, loop, useLoop, s);
-    if (overlap) {
-        if (e == cudaSuccess)
-            e = cudaEventRecord(b->evFork, s);
-        if (e == cudaSuccess)
-            e = cudaStreamWaitEvent(b->side, b->evFork, 0);
-        if (e == cudaSuccess)
-            e = launch_connect(b->scene, f, st, 0u, b->shape, b->side);
-        if (e == cudaSuccess)
-            e = cudaEventRecord(b->evJoin, b->side);
-        if (e == cudaSuccess)
-            e = launch_extend(b->scene, f, st, 0u, b->shape, s, nullptr);
-        if (e == cudaSuccess)
-            e = cudaStreamWaitEvent(s, b->evJoin, 0);
-    } else {
-        if (e == cudaSuccess)
-            e = launch_connect(b->scene, f, st, 0u, b->shape, s);
-        if (e == cudaSuccess)
-            e = launch_extend(b->scene, f, st, 0u, b->shape, s, nullptr);
+    std::vector<ContinuousRound> out;
+    for (uint32_t k = 0; k < b->rounds.size(); ++k) {
+        const Round& r = b->rounds[k];
+        out.push_back(ContinuousRound{round_view(b, k), r.samples, r.pixelBegin, r.pixelEnd});
     }
-    if (e == cudaSuccess)
-        e = launch_shade(b->scene, f, st, 0u, b->shape, s);
-    return e;
+    return out;
 }
 
-// Starting state of a round: everything zero (the plan kernel sets its end).
-cudaError_t enqueue_round_start(Batch* b, uint32_t k, cudaStream_t s)
+ContinuousLaunch continuous_launch(const Batch* b, const Settings& st)
 {
-    return cudaMemsetAsync(b->states + k, 0, sizeof(BatchState), s);
+    return ContinuousLaunch{b->scene, st, b->shape, b->pool, b->side, b->evFork, b->evJoin};
 }
 
 } // namespace
@@ -537,103 +510,6 @@ tr_status tr_batch_get_info(void* batch, tr_batch_info* out)
 
 } // extern "C"
 
-namespace {
-
-// Captures body() on the batch's stream into graph `into` after `deps`; *tail
-// (optional) gets the last node captured.
-template <class Body>
-cudaError_t capture_into(Batch* b, cudaGraph_t into, const cudaGraphNode_t* deps, size_t nDeps, Body&& body,
-                         cudaGraphNode_t* tail)
-{
-    cudaError_t e =
-        cudaStreamBeginCaptureToGraph(b->stream, into, deps, nullptr, nDeps, cudaStreamCaptureModeThreadLocal);
-    if (e != cudaSuccess)
-        return e;
-    e = body();
-    if (e == cudaSuccess && tail) {
-        cudaStreamCaptureStatus cs;
-        const cudaGraphNode_t* d = nullptr;
-        size_t n = 0;
-        e = cudaStreamGetCaptureInfo(b->stream, &cs, nullptr, nullptr, &d, nullptr, &n);
-        if (e == cudaSuccess)
-            *tail = n ? d[n - 1] : nullptr;
-    }
-    cudaGraph_t out = into;
-    const cudaError_t ee = cudaStreamEndCapture(b->stream, &out);
-    return e != cudaSuccess ? e : ee;
-}
-
-// The batch as one graph: per round its start, a while loop over iterations
-// whose condition the plan kernel sets, and its finalize.
-tr_status capture_graph(Batch* b, const Settings& st)
-{
-    release_graph(b);
-    cudaGraph_t g = nullptr;
-    TR_BCUDA(b, cudaGraphCreate(&g, 0));
-    auto fail_graph = [&](cudaError_t e, const char* what) {
-        cudaGraphDestroy(g);
-        return cuda_fail(b, e, what);
-    };
-    cudaGraphNode_t last = nullptr;
-    for (uint32_t k = 0; k < b->rounds.size(); ++k) {
-        cudaGraphNode_t start = nullptr;
-        cudaError_t e = capture_into(b, g, last ? &last : nullptr, last ? 1 : 0,
-                                     [&]() { return enqueue_round_start(b, k, b->stream); }, &start);
-        if (e != cudaSuccess || !start)
-            return fail_graph(e != cudaSuccess ? e : cudaErrorUnknown, "batch graph: round start");
-        cudaGraphConditionalHandle loop;
-        e = cudaGraphConditionalHandleCreate(&loop, g, 1u, cudaGraphCondAssignDefault);
-        if (e != cudaSuccess)
-            return fail_graph(e, "cudaGraphConditionalHandleCreate");
-        cudaGraphNodeParams cp{};
-        cp.type = cudaGraphNodeTypeConditional;
-        cp.conditional.handle = loop;
-        cp.conditional.type = cudaGraphCondTypeWhile;
-        cp.conditional.size = 1;
-        cudaGraphNode_t whileNode = nullptr;
-        e = cudaGraphAddNode(&whileNode, g, &start, nullptr, 1, &cp);
-        if (e != cudaSuccess)
-            return fail_graph(e, "cudaGraphAddNode(while)");
-        cudaGraph_t body = cp.conditional.phGraph_out[0];
-        e = capture_into(
-            b, body, nullptr, 0, [&]() { return enqueue_iteration(b, k, st, loop, true, b->stream, true); }, nullptr);
-        if (e != cudaSuccess)
-            return fail_graph(e, "batch graph: iteration");
-        const FrameView f = round_view(b, k);
-        const Round& r = b->rounds[k];
-        e = capture_into(b, g, &whileNode, 1,
-                         [&]() { return launch_batch_finalize(f, r.pixelBegin, r.pixelEnd, b->stream); }, &last);
-        if (e != cudaSuccess || !last)
-            return fail_graph(e != cudaSuccess ? e : cudaErrorUnknown, "batch graph: finalize");
-    }
-    b->graph = g;
-    TR_BCUDA(b, cudaGraphInstantiate(&b->graphExec, g, 0));
-    b->graphValid = true;
-    return TR_OK;
-}
-
-// Without a graph: the host runs the iterations of each round until a plan
-// finds nothing left to trace (one small read-back per iteration).
-tr_status enqueue_eager(Batch* b, const Settings& st, cudaStream_t s)
-{
-    for (uint32_t k = 0; k < b->rounds.size(); ++k) {
-        TR_BCUDA(b, enqueue_round_start(b, k, s));
-        while (true) {
-            TR_BCUDA(b, enqueue_iteration(b, k, st, cudaGraphConditionalHandle{}, false, s, false));
-            uint32_t queue = 0;
-            TR_BCUDA(b, cudaMemcpyAsync(&queue, &b->states[k].queue, sizeof(uint32_t), cudaMemcpyDeviceToHost, s));
-            TR_BCUDA(b, cudaStreamSynchronize(s));
-            if (queue == 0)
-                break;
-        }
-        const Round& r = b->rounds[k];
-        TR_BCUDA(b, launch_batch_finalize(round_view(b, k), r.pixelBegin, r.pixelEnd, s));
-    }
-    return TR_OK;
-}
-
-} // namespace
-
 extern "C" {
 
 tr_status tr_batch_render(void* batch, void* stream, const tr_kernel_settings* settings, int32_t use_graph)
@@ -655,9 +531,12 @@ tr_status tr_batch_render(void* batch, void* stream, const tr_kernel_settings* s
         (!b->graphValid || std::memcmp(&st, &b->graphSettings, sizeof(Settings)) != 0)) {
         // captured on the batch's own stream, which must be idle
         TR_BCUDA(b, cudaStreamSynchronize(b->stream));
-        const tr_status cs = capture_graph(b, st);
-        if (cs != TR_OK)
-            return cs;
+        release_graph(b);
+        cudaGraph_t g = nullptr;
+        TR_BCUDA(b, capture_continuous(continuous_launch(b, st), continuous_rounds(b), 0u, b->stream, &g));
+        b->graph = g;
+        TR_BCUDA(b, cudaGraphInstantiate(&b->graphExec, g, 0));
+        b->graphValid = true;
         b->graphSettings = st;
     }
     TR_BCUDA(b, cudaEventRecord(b->evStart, s));
@@ -667,9 +546,7 @@ tr_status tr_batch_render(void* batch, void* stream, const tr_kernel_settings* s
     } else {
         if (st.flags & TR_FLAG_COUNT_TRAVERSAL)
             TR_BCUDA(b, cudaMemsetAsync(b->frame.traversal, 0, kTraversalCounters * sizeof(unsigned long long), s));
-        const tr_status es = enqueue_eager(b, st, s);
-        if (es != TR_OK)
-            return es;
+        TR_BCUDA(b, run_continuous_eager(continuous_launch(b, st), continuous_rounds(b), 0u, s));
     }
     TR_BCUDA(b, cudaEventRecord(b->evStop, s));
     b->lastSettings = st;

@@ -289,7 +289,7 @@ __device__ __forceinline__ void primary_ray(const FrameView& f, const Camera& ca
         const BatchSample bs = batch_sample(f, pathIx);
         const BatchItem& it = f.items[bs.item];
         CounterRng rng;
-        rng.init(bs.pixel, bs.sample, 0u, st.seed);
+        rng.init(bs.pixel, sc + bs.sample, 0u, st.seed);
         camera_ray(it.camera, it.width, it.height, bs.pixel % it.width, bs.pixel / it.width, rng, false, O, D, T);
     } else if (REF) {
         RefRng rng{tea2(st.seed + pathIx, sc << 1)};
@@ -387,12 +387,17 @@ constexpr uint32_t kRefillBelow = 10;
 // A path that leaves the scene sees the sky (PathTracing.h:40-55): T * SampleSky,
 // with the sun disc for camera and specular paths; a primary miss writes the sky
 // as its albedo guide. Out of line so that the traversal loop keeps its registers.
+// BATCH: the path's sample id is O.w, its bounce and flags are in D.w.
+template <bool BATCH>
 __device__ __noinline__ void sky_miss(const SceneView& s, const FrameView& f, const Settings& st, uint32_t bounce,
                                       float4 O4, float4 D4, float4 T4, bool aov)
 {
     const uint32_t data = __float_as_uint(O4.w);
-    const uint32_t pathIx = path_ix(data);
-    const bool sun = s.sky.drawSun != 0.f && (bounce == 0 || (path_flags(data) & kFlagSpecular));
+    const uint32_t pathIx = BATCH ? data : path_ix(data);
+    const uint32_t flags = BATCH ? (__float_as_uint(D4.w) & kFlagsMask) : path_flags(data);
+    if (BATCH)
+        bounce = __float_as_uint(D4.w) >> kPathIxShift;
+    const bool sun = s.sky.drawSun != 0.f && (bounce == 0 || (flags & kFlagSpecular));
     const float3 sky = sky_radiance(s.sky, f3(D4), sun);
     const float3 add = safe_color(f3(T4) * sky, st.maxColor);
     const float4 r = f.radiance[pathIx];
@@ -427,7 +432,7 @@ __global__ void __launch_bounds__(128, 8) extend_kernel(SceneView s, FrameView f
     typename TravOf<TL>::type t;
     uint2 stack[kTraversalStack];
     float4 O4 = make_float4(0.f, 0.f, 0.f, 0.f), D4 = O4, T4 = O4;
-    const uint32_t sc = PRIMARY ? *f.sampleCount : 0u;
+    const uint32_t sc = (PRIMARY || BATCH) ? *f.sampleCount : 0u;
     bool alive = false, more = true;
     while (true) {
         const uint32_t idle = __ballot_sync(kFull, !alive && more);
@@ -483,7 +488,7 @@ __global__ void __launch_bounds__(128, 8) extend_kernel(SceneView s, FrameView f
                     __stcs(f.hits + slot, make_uint4(encode_bary(base(t).u, base(t).v), hit_instance(t), prim,
                                                      __float_as_uint(base(t).tmax)));
                 } else if (s.sky.enabled) {
-                    sky_miss(s, f, st, bounce, O4, D4, T4, aov);
+                    sky_miss<BATCH>(s, f, st, bounce, O4, D4, T4, aov);
                 } else if (aov) {
                     // a primary miss sees the disabled sky: black guide values (PathTracing.h:48-52)
                     const uint32_t pathIx = path_ix(__float_as_uint(O4.w));
@@ -957,7 +962,7 @@ __global__ void __launch_bounds__(128, 5) shade_kernel(SceneView s, FrameView f,
                 const BatchSample bs = batch_sample(f, id);
                 const SceneView si = item_scene(s, f.items[bs.item]);
                 CounterRng rng;
-                rng.init(bs.pixel, bs.sample, pathBounce + 1u, st.seed);
+                rng.init(bs.pixel, sc + bs.sample, pathBounce + 1u, st.seed);
                 emitted = shade_path<false, CounterRng, false, true>(si, f, st, pathBounce, sc, O4, D4, T4, hd, rng,
                                                                      wantExt, ext, wantShadow, sh);
             } else if (REF) {
@@ -1456,8 +1461,9 @@ __global__ void batch_plan_kernel(BatchState* __restrict__ bs, uint32_t pool, ui
 }
 
 // Batched rendering: every pixel of the round's items, its samples summed in
-// sample order (as finalize_kernel sums one frame's multi_sample samples), into
-// the batch accumulator (sum, spp) and colors = accumulator / spp.
+// sample order (as finalize_kernel sums one frame's multi_sample samples), added
+// to the accumulator (which the first samples overwrite: *f.sampleCount == 0)
+// and colors = accumulator / (samples before + spp).
 __global__ void __launch_bounds__(256) batch_finalize_kernel(FrameView f, uint32_t pixelBegin, uint32_t pixelEnd)
 {
     const uint32_t p = pixelBegin + blockIdx.x * blockDim.x + threadIdx.x;
@@ -1477,9 +1483,11 @@ __global__ void __launch_bounds__(256) batch_finalize_kernel(FrameView f, uint32
     float3 sum = f3(0.f);
     for (uint32_t k = 0; k < spp; ++k)
         sum = sum + f3(__ldcs(r + k));
-    const float4 acc = make_float4(0.f + sum.x, 0.f + sum.y, 0.f + sum.z, 0.f + float(spp));
+    const uint32_t sc = *f.sampleCount;
+    float4 acc = sc == 0 ? make_float4(0.f, 0.f, 0.f, 0.f) : f.accumulator[p];
+    acc = make_float4(acc.x + sum.x, acc.y + sum.y, acc.z + sum.z, acc.w + float(spp));
     f.accumulator[p] = acc;
-    const float n = float(spp);
+    const float n = float(sc + spp);
     f.colors[p] = make_float4(acc.x / n, acc.y / n, acc.z / n, acc.w / n);
 }
 
@@ -1971,6 +1979,14 @@ cudaError_t launch_connect(const SceneView& s0, const FrameView& f, const Settin
         else
             connect_kernel<false, false, false><<<g, shape.traversalThreads, 0, stream>>>(s, f, st, bounce);
     }
+    return cudaGetLastError();
+}
+
+cudaError_t launch_advance(const FrameView& f, uint32_t samples, cudaStream_t stream)
+{
+    Settings st{};
+    st.multiSample = samples;
+    advance_kernel<<<1, 32, 0, stream>>>(f, st);
     return cudaGetLastError();
 }
 

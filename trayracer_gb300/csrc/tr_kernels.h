@@ -39,6 +39,8 @@ cudaError_t launch_shade(const SceneView& s, const FrameView& f, const Settings&
 cudaError_t launch_connect(const SceneView& s, const FrameView& f, const Settings& st, uint32_t bounce,
                            const LaunchShape& shape, cudaStream_t stream);
 cudaError_t launch_finalize(const FrameView& f, const Settings& st, cudaStream_t stream);
+// Adds `samples` to the frame's device sample count.
+cudaError_t launch_advance(const FrameView& f, uint32_t samples, cudaStream_t stream);
 // One bounce of a debug render mode (Settings::renderMode != path tracing):
 // closest hit of every ray of queue state[bounce & 1], then the mode's shade.
 cudaError_t launch_debug_bounce(const SceneView& s, const FrameView& f, const Camera& cam, const Settings& st,

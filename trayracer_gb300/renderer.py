@@ -256,6 +256,12 @@ class DeviceRenderer:
         self._check(self._lib.tr_render_frame(self._ctx, C.c_void_p(stream or None), int(use_graph)),
                     "tr_render_frame")
 
+    def RenderSamples(self, spp: int, stream: int = 0, use_graph: bool = True):
+        """tr_render_samples: spp samples per pixel (a multiple of multi_sample) added to the
+        accumulation as one continuous wavefront (same samples as spp / multi_sample frames)."""
+        self._check(self._lib.tr_render_samples(self._ctx, C.c_void_p(stream or None), int(spp), int(use_graph)),
+                    "tr_render_samples")
+
     def BeginFrame(self, stream: int = 0):
         self._check(self._lib.tr_begin_frame(self._ctx, C.c_void_p(stream or None)), "tr_begin_frame")
 
