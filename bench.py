@@ -58,7 +58,8 @@ def parse():
     p.add_argument("--cpu-seconds", type=float, default=20.0, help="target CPU work of the CPU baseline sample")
     p.add_argument("--no-cpu-baseline", action="store_true")
     p.add_argument("--profile", action="store_true",
-                   help="render one eager frame of the workload and exit (the case the ncu captures use)")
+                   help="render one eager step of the workload (spp samples as one continuous wavefront) and "
+                        "exit (the case the ncu captures use)")
     p.add_argument("--workload", default="plain", choices=["plain", "batch", "adjoint", "large"],
                    help="plain: the heightfield (default); batch: the 64-scene mix in one wavefront against "
                         "per-scene renders; adjoint: forward frame and path-replay adjoint of the "
@@ -690,9 +691,10 @@ def main():
     stream = torch.cuda.current_stream()
     sptr = stream.cuda_stream
     if args.profile:
-        r.RenderFrame(stream=sptr, use_graph=False)
+        r.RenderSamples(args.spp, stream=sptr, use_graph=False)
         s = r.Statistics()
-        print(json.dumps({k: s[k] for k in ("path_count", "extend_rays", "hit_rays", "shadow_rays",
+        print(json.dumps({k: s[k] for k in ("path_count", "primary_path_count", "secondary_path_count",
+                                             "shadow_ray_count", "hit_ray_count", "iterations", "launches",
                                              "extend_time_ms", "shade_time_ms", "connect_time_ms",
                                              "device_error")}))
         r.close()
@@ -710,43 +712,36 @@ def main():
         tune = r.Autotune(stream=sptr)
         torch.cuda.synchronize()
 
-    # --- counting pass (rays per step, traversal work), outside the timed region
-    stage_ms = {"generate": 0.0, "extend": 0.0, "shade": 0.0, "connect": 0.0, "finalize": 0.0}
-    ext_rays = sh_rays = 0
-    hit_rays = 0
-    ext_per_bounce = np.zeros(16, np.int64)
-    r.Reset()
-    for _ in range(frames_per_step):
-        r.RenderFrame(stream=sptr, use_graph=False)
-        s = r.Statistics()
-        ext_rays += sum(s["extend_rays"])
-        sh_rays += sum(s["shadow_rays"])
-        hit_rays += sum(s["hit_rays"])
-        ext_per_bounce += np.array(s["extend_rays"], np.int64)
-    rays_per_step = ext_rays + sh_rays
+    # --- counting pass (rays and traversal work of one step), outside the timed region: the
+    # same step rendered eagerly with the traversal counters on
     cnt_settings = tr.settings_for(scene, multi_sample=args.ms)
     cnt_settings.seed = st.seed
     cnt_settings.flags |= TR_FLAG_COUNT_TRAVERSAL
     r.SetSettings(cnt_settings)
     r.Reset()
-    for _ in range(frames_per_step):
-        r.RenderFrame(stream=sptr, use_graph=False)
+    r.RenderSamples(args.spp, stream=sptr, use_graph=False)
     cs = r.Statistics()
     r.SetSettings(st)
     assert cs["device_error"] == 0, "traversal bound exceeded"
+    ext_rays = cs["primary_path_count"] + cs["secondary_path_count"]
+    sh_rays = cs["shadow_ray_count"]
+    hit_rays = cs["hit_ray_count"]
+    primary_rays = cs["primary_path_count"]
 
     # --- warm-up
     for _ in range(args.warmup):
         step()
     torch.cuda.synchronize()
 
-    # --- per-stage timing of one eager step (CUDA events per stage, on the launch stream)
+    # --- per-stage timing of one eager step: the same continuous wavefront run from a host loop
+    # with the stages in sequence (no connect/extend overlap), CUDA events around every launch
+    # on the launch stream, summed over the iterations; "generate" is the plan kernels,
+    # "finalize" the round start, finalize and sample-count advance
     r.Reset()
-    for _ in range(frames_per_step):
-        r.RenderFrame(stream=sptr, use_graph=False)
-        s = r.Statistics()
-        for k in stage_ms:
-            stage_ms[k] += s[f"{k}_time_ms"]
+    r.RenderSamples(args.spp, stream=sptr, use_graph=False)
+    s = r.Statistics()
+    stage_ms = {k: s[f"{k}_time_ms"] for k in ("generate", "extend", "shade", "connect", "finalize")}
+    stage_launches = s["iterations"] + 1  # per stage: one per iteration, the last finds nothing
 
     # --- timed region: K steps, graph replay, L2 flushed between steps
     times = []
@@ -769,9 +764,6 @@ def main():
         total_ms = max_over_ranks(total_ms, device=f"cuda:{local}")
     final = r.Statistics()
     assert final["device_error"] == 0
-    # the rays of one step as the continuous wavefront traced them (the counting pass above
-    # renders the same samples frame by frame, for the per-stage figures)
-    frame_rays_per_step = rays_per_step
     rays_per_step = final["path_count"]
 
     # --- end to end through the public API, host buffers: per step the camera
@@ -800,7 +792,7 @@ def main():
                  + cs["traversal_extend_nodes"] * NODE_BYTES
                  + cs["traversal_extend_tris"] * TRI_BYTES)
     ext_s = stage_ms["extend"] / 1e3
-    launches = frames_per_step * st.maxDepth
+    launches = stage_launches
     achieved = ext_bytes / ext_s / 1e9
     compulsory = (ext_rays * EXTEND_BYTES_PER_RAY + hit_rays * EXTEND_BYTES_PER_HIT) / ext_s / 1e9
     # DRAM bytes per extend ray measured by ncu on the 960x540 case of this workload (4 spp per
@@ -822,15 +814,15 @@ def main():
     # shaded hit (state 48 + hit 16 + shading record 72 + material index 4), 48 B per extend
     # and per shadow ray written and 32 B per radiance read-modify-write (emissive hits);
     # connect: 48 B per shadow ray, its traversal bytes and 32 B per radiance
-    # read-modify-write (unoccluded shadow rays); finalize: per pixel the multi_sample path
+    # read-modify-write (unoccluded shadow rays); finalize: per pixel its spp sample
     # radiances (16 B each), the accumulator read and written and the colour written (16 B
     # each). The radiance updates come from the counting pass.
-    secondary = ext_rays - int(ext_per_bounce[0])
+    secondary = ext_rays - primary_rays
     stage_bytes = {
         "shade": hit_rays * 140 + (secondary + sh_rays) * 48 + cs["radiance_updates_shade"] * 32,
         "connect": sh_rays * 48 + cs["traversal_connect_nodes"] * NODE_BYTES + cs["traversal_connect_tris"] * TRI_BYTES
         + cs["radiance_updates_connect"] * 32,
-        "finalize": frames_per_step * scene.width * scene.height * (16 * args.ms + 48),
+        "finalize": scene.width * scene.height * (16 * args.spp + 48),
     }
     stage_roofline = {}
     for k, b in stage_bytes.items():
@@ -930,7 +922,9 @@ def main():
             # plus its start, finalize and advance
             "gpu_launches": args.steps * final["launches"],
             "iterations_per_step": final["iterations"],
-            "frame_rays_per_step": int(frame_rays_per_step),
+            "stage_source": "one eager step of the same samples (continuous wavefront, stages in sequence, "
+                            "CUDA events per launch); the timed steps are graph launches with connect beside "
+                            "extend",
             "scene_upload_s": round(upload_s, 2),
             "tuning": tune,
             "adjoint": adjoint,

@@ -262,6 +262,7 @@ typedef struct tr_statistics {
     uint64_t radiance_updates_connect;
     uint32_t iterations;            /* after tr_render_samples: continuous-wavefront iterations that traced rays */
     uint32_t launches;              /* after tr_render_samples: kernels of that render */
+    uint64_t hit_ray_count;         /* extend rays that hit something (the sum of hit_rays) */
 } tr_statistics;
 
 /* Scene numbers: triangle/light/BVH sizes and the host build time. */
@@ -378,9 +379,13 @@ tr_status tr_render_frame(void* ctx, void* stream, int32_t use_graph);
  * apply (TR_FLAG_REFERENCE_SAMPLING, TR_FLAG_WRITE_AOVS, two-level or
  * textured scenes, other render modes, more than 2^30 samples) it renders the
  * frames. After it, tr_get_statistics reports totals: path_count,
- * shadow_ray_count, primary_path_count (width * height * spp) and
- * secondary_path_count (every other extend ray); the per-bounce arrays and
- * stage times are zero. No reference counterpart (DeviceRenderer renders one
+ * shadow_ray_count, hit_ray_count, primary_path_count (width * height * spp)
+ * and secondary_path_count (every other extend ray), iterations and launches;
+ * the per-bounce arrays are zero. An eager render (use_graph = 0) also
+ * reports its stage times, summed over the iterations: generate_time_ms the
+ * plan kernels, extend_time_ms (with the camera rays of new samples),
+ * shade_time_ms, connect_time_ms, finalize_time_ms the round starts,
+ * finalize and sample-count advance. No reference counterpart (DeviceRenderer renders one
  * frame per call, Tracer/Renderer/DeviceRenderer.cpp:97-133). */
 tr_status tr_render_samples(void* ctx, void* stream, uint32_t spp, int32_t use_graph);
 

@@ -126,3 +126,37 @@ def test_samples_errors():
     r.RenderSamples(8)
     assert r.Statistics()["device_error"] != 0
     r.close()
+
+
+def test_samples_statistics():
+    """Totals of a continuous render against the same samples as frames, the stage times of an
+    eager render (zero after a graph render), and the launch count."""
+    scene = SCENES["heightfield"]()
+    st = tr.settings_for(scene, multi_sample=2)
+    r = renderer(scene, st)
+    hits = ext = shadow = 0
+    for _ in range(3):
+        r.RenderFrame(use_graph=False)
+        f = r.Statistics()
+        assert f["hit_ray_count"] == sum(f["hit_rays"])
+        hits += f["hit_ray_count"]
+        ext += f["primary_path_count"] + f["secondary_path_count"] + f["deep_path_count"]
+        shadow += f["shadow_ray_count"]
+    for graph in (False, True):
+        r.Reset()
+        r.RenderSamples(6, use_graph=graph)
+        s = r.Statistics()
+        assert s["device_error"] == 0 and s["iterations"] >= 3  # the pool holds a third of the samples
+        assert s["launches"] == 3 + 4 * (s["iterations"] + 1)
+        n = s["primary_path_count"] + s["secondary_path_count"]
+        assert s["primary_path_count"] == scene.width * scene.height * 6
+        assert s["path_count"] == n + s["shadow_ray_count"]
+        for got, want in ((n, ext), (s["shadow_ray_count"], shadow), (s["hit_ray_count"], hits)):
+            assert abs(got - want) <= 1e-3 * want
+        times = [s[f"{k}_time_ms"] for k in ("generate", "extend", "shade", "connect", "finalize")]
+        if graph:
+            assert all(t == 0 for t in times)
+        else:
+            assert all(t > 0 for t in times)
+            assert s["render_time_ms"] == pytest.approx(sum(times), rel=1e-5)
+    r.close()

@@ -156,6 +156,7 @@ class Statistics(C.Structure):
         ("radiance_updates_connect", C.c_uint64),
         ("iterations", C.c_uint32),
         ("launches", C.c_uint32),
+        ("hit_ray_count", C.c_uint64),
     ]
 
 

@@ -155,6 +155,8 @@ struct Context {
     uint32_t samplesGraphSpp = 0;
     bool lastSamples = false;          // the last render was tr_render_samples' continuous wavefront
     uint32_t lastSamplesPaths = 0;
+    bool samplesTimed = false;         // ... rendered eagerly, with its stage times
+    StageTimes samplesTimes{};
 
     // frames rendered by tr_render_frame_noalloc: the launch shape for their
     // capacity and tuning, and whether the last frame was one of them
@@ -1505,8 +1507,13 @@ tr_status tr_render_samples(void* ctx, void* stream, uint32_t spp, int32_t use_g
             c->samplesGraphSpp = spp;
         }
         TR_CUDA(c, cudaGraphLaunch(c->samplesExec, s));
+        c->samplesTimed = false;
     } else {
-        TR_CUDA(c, run_continuous_eager(L, rounds, spp, s));
+        // eager: stage by stage with a host loop, each stage timed by CUDA events
+        c->samplesTimes = StageTimes{};
+        c->samplesTimed = false;
+        TR_CUDA(c, run_continuous_eager(L, rounds, spp, s, &c->samplesTimes));
+        c->samplesTimed = true;
     }
     c->lastStream = s;
     c->timedFrame = false;
@@ -1570,10 +1577,20 @@ tr_status tr_get_statistics(void* ctx, tr_statistics* out)
         s.traversal_connect_tris = trav[3];
         s.radiance_updates_shade = trav[4];
         s.radiance_updates_connect = trav[5];
+        s.hit_ray_count = bs.hitRays;
         s.iterations = bs.iterations;
         // start, finalize, advance, and plan + connect + extend + shade per iteration (the
         // last finds nothing to trace)
         s.launches = 3u + 4u * (bs.iterations + 1u);
+        if (c->samplesTimed) {
+            const StageTimes& t = c->samplesTimes;
+            s.generate_time_ms = t.plan;
+            s.extend_time_ms = t.extend;
+            s.shade_time_ms = t.shade;
+            s.connect_time_ms = t.connect;
+            s.finalize_time_ms = t.end;
+            s.render_time_ms = t.plan + t.extend + t.shade + t.connect + t.end;
+        }
         *out = s;
         return TR_OK;
     }
@@ -1584,6 +1601,7 @@ tr_status tr_get_statistics(void* ctx, tr_statistics* out)
         s.hit_rays[b] = counters[kHitCounterBase + b];
         s.path_count += s.extend_rays[b] + s.shadow_rays[b];
         s.shadow_ray_count += s.shadow_rays[b];
+        s.hit_ray_count += s.hit_rays[b];
         if (b == 0)
             s.primary_path_count = s.extend_rays[b];
         else if (b == 1)

@@ -35,6 +35,16 @@ struct ContinuousLaunch {
     cudaEvent_t join;
 };
 
+// Device time per stage of an eager run, summed over its iterations (CUDA
+// events around each stage on the launch stream; the stages run in sequence).
+struct StageTimes {
+    float plan = 0.f;     // plan kernels (totals, queue hand-over, new samples taken)
+    float connect = 0.f;  // shadow rays
+    float extend = 0.f;   // carried paths and the camera rays of new samples
+    float shade = 0.f;
+    float end = 0.f;      // round starts, finalize and the sample count advance
+};
+
 // One iteration of a round: plan, connect of the last iteration's shadow rays
 // and extend (carried paths + new samples), shade. With `overlap`, connect
 // runs on the side stream beside extend: connect reads the shadow queue and
@@ -42,9 +52,11 @@ struct ContinuousLaunch {
 // starts new samples, so they share nothing; shade (which rewrites the shadow
 // queue and adds emission to the same radiance) waits for both. Not with a
 // sky, whose misses extend adds to the radiance of carried paths.
+// `marks` (optional, without overlap): four events recorded after plan,
+// connect, extend and shade.
 cudaError_t enqueue_continuous_iteration(const ContinuousLaunch& L, const ContinuousRound& r,
                                          cudaGraphConditionalHandle loop, bool useLoop, cudaStream_t s,
-                                         bool overlap);
+                                         bool overlap, const cudaEvent_t* marks = nullptr);
 
 // A graph of all rounds in order: per round its start, a while loop over its
 // iterations (condition set by the plan kernel on the device) and its
@@ -54,8 +66,10 @@ cudaError_t capture_continuous(const ContinuousLaunch& L, const std::vector<Cont
                                uint32_t advance, cudaStream_t s, cudaGraph_t* out);
 
 // The same launches from a host loop that reads each round's queue length
-// back after every iteration (no graph).
+// back after every iteration (no graph), stages in sequence. With `times`, the
+// device time of each stage is summed into it (the call then returns with the
+// stream idle).
 cudaError_t run_continuous_eager(const ContinuousLaunch& L, const std::vector<ContinuousRound>& rounds,
-                                 uint32_t advance, cudaStream_t s);
+                                 uint32_t advance, cudaStream_t s, StageTimes* times = nullptr);
 
 } // namespace tr
