@@ -795,18 +795,19 @@ def main():
     launches = stage_launches
     achieved = ext_bytes / ext_s / 1e9
     compulsory = (ext_rays * EXTEND_BYTES_PER_RAY + hit_rays * EXTEND_BYTES_PER_HIT) / ext_s / 1e9
-    # DRAM bytes per extend ray measured by ncu on the 960x540 case of this workload (4 spp per
-    # frame, a few extend launches captured), scaled to this run's average launch by its extend
-    # rays; labelled with its source in the line, not measured in this run
+    # DRAM bytes per extend ray measured by ncu over all extend launches of one eager step of
+    # this workload (one pass), scaled to this run's average launch by its extend rays; labelled
+    # with its source in the line, not measured in this run
     traffic, traffic_source = None, None
-    prof = ROOT / "profiles" / "extend_kernel_heightfield_960x540_traffic.txt"
+    prof = ROOT / "profiles" / "extend_kernel_heightfield_1920x1080_traffic.txt"
     if prof.exists():
         for line in prof.read_text().splitlines():
             if line.strip().startswith("dram_bytes_per_extend_ray:"):
                 try:
                     traffic = float(line.split(":", 1)[1]) * ext_rays / launches
-                    traffic_source = ("ncu dram__bytes_read.sum + dram__bytes_write.sum of the 960x540 case, "
-                                      "per extend ray, scaled to this run's extend rays per launch")
+                    traffic_source = ("ncu dram__bytes_read.sum + dram__bytes_write.sum over the 15 extend "
+                                      "launches of one eager step of this workload, per extend ray, scaled to "
+                                      "this run's extend rays per launch")
                 except ValueError:
                     traffic = None
 

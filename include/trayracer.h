@@ -385,8 +385,10 @@ tr_status tr_render_frame(void* ctx, void* stream, int32_t use_graph);
  * reports its stage times, summed over the iterations: generate_time_ms the
  * plan kernels, extend_time_ms (with the camera rays of new samples),
  * shade_time_ms, connect_time_ms, finalize_time_ms the round starts,
- * finalize and sample-count advance. No reference counterpart (DeviceRenderer renders one
- * frame per call, Tracer/Renderer/DeviceRenderer.cpp:97-133). */
+ * finalize and sample-count advance. Replaces n accumulating frames of the
+ * reference's application loop (Tracer/App/RunApp.cpp:144, one
+ * DeviceRenderer::RenderFrame per displayed frame,
+ * Tracer/Renderer/DeviceRenderer.cpp:97-133). */
 tr_status tr_render_samples(void* ctx, void* stream, uint32_t spp, int32_t use_graph);
 
 /* Path-replay adjoint (Vicini, Speierer, Jakob, SIGGRAPH 2021) of the last
