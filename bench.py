@@ -66,6 +66,8 @@ def parse():
                         "differentiation scene; large: the 20.5M-triangle displaced-sphere scene at 3840x2160, "
                         "16 spp, 12 bounces, forward frame and adjoint over its 4096 materials")
     p.add_argument("--no-autotune", action="store_true", help="plain workload: keep the default launch shapes")
+    p.add_argument("--tune-on", default="samples", choices=["samples", "frames"],
+                   help="plain workload: what the autotuner times (continuous renders, as the step, or frames)")
     p.add_argument("--rmse-spp", type=int, default=1024,
                    help="plain workload: also compare a render of this many spp against the FP64 oracle")
     p.add_argument("--batch-count", type=int, default=64)
@@ -709,7 +711,8 @@ def main():
     # --- autotuner (launch shapes, BVH leaf size) on this workload, outside the timed region
     tune = None
     if not args.no_autotune:
-        tune = r.Autotune(stream=sptr)
+        tune = r.Autotune(stream=sptr, samples=args.tune_on == "samples")
+        tune["timed"] = args.tune_on
         torch.cuda.synchronize()
 
     # --- counting pass (rays and traversal work of one step), outside the timed region: the

@@ -537,17 +537,23 @@ tr_status tr_pick_ray(void* ctx, void* stream, int32_t x, int32_t y, tr_ray_pick
 /* ---- tuning ----
  * No counterpart in the reference (OptiX picks its own launch shapes). */
 #define TR_TUNE_SKIP_BVH (1u << 0)  /* tr_autotune: keep the BVH leaf size */
+#define TR_TUNE_SAMPLES (1u << 1)   /* tr_autotune: time continuous renders (tr_render_samples of
+                                       4 x multi_sample samples per pixel) instead of frames */
 /* Current tuning (after the first frame: the launch shapes in use). */
 tr_status tr_get_tuning(void* ctx, tr_tuning* tuning);
 /* Applies a tuning; a new bvh_leaf_size rebuilds the BVH from the host copy of
  * the mesh kept since tr_scene_upload. Zero fields take the defaults. */
 tr_status tr_set_tuning(void* ctx, const tr_tuning* tuning);
 /* Times graph-replayed frames of the current scene, camera, settings and
- * resolution (one warm-up + two timed frames per configuration) over the
- * lane refill threshold, the persistent extend / connect grids, the shade grid
- * cap, the material sort of the hits and (unless TR_TUNE_SKIP_BVH) the BVH leaf
- * size, one parameter at a time,
- * keeps the fastest and resets the accumulation. */
+ * resolution (one warm-up + two timed frames per configuration; with
+ * TR_TUNE_SAMPLES one warm-up + one timed continuous render of 4 x
+ * multi_sample samples per pixel, and no material sort, which the continuous
+ * kernels do not use) over the block sizes of the traversal and shade
+ * launches, the lane refill threshold, the persistent extend / connect grids,
+ * the shade grid cap, the material sort of the hits and (unless
+ * TR_TUNE_SKIP_BVH) the BVH leaf size, one parameter at a time, keeps the
+ * fastest and resets the accumulation. The report's frame_ms_* are per frame,
+ * or per continuous render with TR_TUNE_SAMPLES. */
 tr_status tr_autotune(void* ctx, void* stream, uint32_t flags, tr_tune_report* report);
 
 /* ---- batched rendering ----

@@ -160,3 +160,20 @@ def test_samples_statistics():
             assert all(t > 0 for t in times)
             assert s["render_time_ms"] == pytest.approx(sum(times), rel=1e-5)
     r.close()
+
+
+def test_autotune_on_continuous_renders():
+    """tr_autotune with TR_TUNE_SAMPLES times continuous renders; the chosen tuning is applied,
+    the accumulation reset, and the continuous render afterwards matches the frames it replaces."""
+    scene = tr.cornell_box(width=64, height=48)
+    st = tr.settings_for(scene, multi_sample=2)
+    r = renderer(scene, st)
+    rep = r.Autotune(skip_bvh=True, samples=True)
+    assert rep["trials"] >= 10
+    assert rep["frame_ms_tuned"] <= rep["frame_ms_default"]
+    assert rep["chosen"] == r.Tuning() and r.SampleCount() == 0
+    r.RenderSamples(4)
+    got = r.ColorBuffer().copy()
+    r.close()
+    want, _, _ = frames(scene, st, 2)
+    np.testing.assert_allclose(got, want, rtol=1e-5, atol=1e-7)

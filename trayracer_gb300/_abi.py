@@ -241,6 +241,7 @@ class TuneReport(C.Structure):
 
 
 TR_TUNE_SKIP_BVH = 1 << 0
+TR_TUNE_SAMPLES = 1 << 1
 
 
 class BatchItem(C.Structure):

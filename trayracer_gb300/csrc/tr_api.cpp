@@ -1090,19 +1090,23 @@ tr_status tr_autotune(void* ctx, void* stream, uint32_t flags, tr_tune_report* r
     TR_CUDA(c, cudaEventCreate(&e0));
     TR_CUDA(c, cudaEventCreate(&e1));
     uint32_t trials = 0;
+    const bool samples = (flags & TR_TUNE_SAMPLES) != 0;
+    const uint32_t spp = 4u * c->settings.multiSample;
     auto timeFrames = [&](float* ms) -> tr_status {
-        tr_status r = tr_render_frame(ctx, stream, 1);
+        const int timed = samples ? 1 : 2;
+        auto render = [&]() { return samples ? tr_render_samples(ctx, stream, spp, 1) : tr_render_frame(ctx, stream, 1); };
+        tr_status r = render();
         if (r != TR_OK)
             return r;
         TR_CUDA(c, cudaEventRecord(e0, s));
-        for (int i = 0; i < 2 && r == TR_OK; ++i)
-            r = tr_render_frame(ctx, stream, 1);
+        for (int i = 0; i < timed && r == TR_OK; ++i)
+            r = render();
         if (r != TR_OK)
             return r;
         TR_CUDA(c, cudaEventRecord(e1, s));
         TR_CUDA(c, cudaEventSynchronize(e1));
         TR_CUDA(c, cudaEventElapsedTime(ms, e0, e1));
-        *ms *= 0.5f;
+        *ms /= float(timed);
         ++trials;
         return TR_OK;
     };
@@ -1169,7 +1173,7 @@ tr_status tr_autotune(void* ctx, void* stream, uint32_t flags, tr_tune_report* r
         if (st == TR_OK && w != best.shade_waves)
             st = tryTuning(t);
     }
-    {
+    if (!samples) {
         tr_tuning t = best;
         t.sort_hits = best.sort_hits ? 0u : 1u;
         if (st == TR_OK)

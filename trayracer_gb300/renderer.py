@@ -302,11 +302,13 @@ class DeviceRenderer:
             setattr(t, k, int(v))
         self._check(self._lib.tr_set_tuning(self._ctx, C.byref(t)), "tr_set_tuning")
 
-    def Autotune(self, stream: int = 0, skip_bvh: bool = False) -> dict:
-        """tr_autotune: times launch shapes (and BVH leaf sizes) on the current frame setup."""
+    def Autotune(self, stream: int = 0, skip_bvh: bool = False, samples: bool = False) -> dict:
+        """tr_autotune: times launch shapes (and BVH leaf sizes) on the current frame setup; with
+        samples=True on continuous renders of 4 x multi_sample samples per pixel (RenderSamples)."""
         rep = _abi.TuneReport()
-        self._check(self._lib.tr_autotune(self._ctx, C.c_void_p(stream or None),
-                                          _abi.TR_TUNE_SKIP_BVH if skip_bvh else 0, C.byref(rep)), "tr_autotune")
+        flags = (_abi.TR_TUNE_SKIP_BVH if skip_bvh else 0) | (_abi.TR_TUNE_SAMPLES if samples else 0)
+        self._check(self._lib.tr_autotune(self._ctx, C.c_void_p(stream or None), flags, C.byref(rep)),
+                    "tr_autotune")
         chosen = {f: getattr(rep.chosen, f) for f, _ in rep.chosen._fields_ if f != "reserved"}
         return {"chosen": chosen, "frame_ms_default": rep.frame_ms_default, "frame_ms_tuned": rep.frame_ms_tuned,
                 "trials": rep.trials}
