@@ -612,7 +612,7 @@ typedef struct tr_batch_statistics {
 /* Builds and uploads all items (host threads build the BVHs). Items are
  * one-mesh scenes (instance_count 0). Device memory: 160 B per path slot,
  * 16 B per sample of the largest round, 32 B per pixel. TR_ERR_LIMIT when an
- * item has more than 2^30 samples or pool_paths >= 2^28. */
+ * item has more than 2^30 samples, pool_paths >= 2^28 or count >= 2^24. */
 tr_status tr_batch_create(const tr_config* config, const tr_batch_item* items, uint32_t count, uint64_t pool_paths,
                           void** out_batch);
 tr_status tr_batch_destroy(void* batch);

@@ -254,7 +254,7 @@ tr_status tr_batch_create(const tr_config* config, const tr_batch_item* items, u
     if (config->abi_version != TR_ABI_VERSION)
         return TR_ERR_INVALID_ARGUMENT;
     const uint64_t poolCap = pool_paths ? pool_paths : kDefaultPoolPaths;
-    if (poolCap >= TR_MAX_PATHS)
+    if (poolCap >= TR_MAX_PATHS || count >= (1u << 24))  // a path keeps its item in 24 bits
         return TR_ERR_LIMIT;
     uint64_t pixels = 0, paths = 0;
     for (uint32_t i = 0; i < count; ++i) {

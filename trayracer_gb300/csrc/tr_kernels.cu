@@ -243,22 +243,31 @@ __device__ __forceinline__ BatchSample batch_sample(const FrameView& f, uint32_t
     return b;
 }
 
-// BVH root of the scene a path belongs to (node 0 for one scene; a batch path
-// is given by its sample id).
-template <bool BATCH>
-__device__ __forceinline__ uint32_t path_root(const FrameView& f, uint32_t id)
+// Per-path item, bounce and flags of a batched path, kept in D.w (the packed
+// normal of one-scene paths, which nothing reads): item << 8 | bounce << 4 |
+// flags, so that no stage searches the items for a path's sample id again.
+constexpr uint32_t kBatchItemShift = 8;
+__device__ __forceinline__ uint32_t batch_pack(uint32_t bounce, uint32_t flags, uint32_t item)
 {
-    if (!BATCH)
-        return 0u;
-    return __ldg(&f.items[batch_item(f, id)].root);
+    return (item << kBatchItemShift) | ((bounce & 0xfu) << kPathIxShift) | (flags & kFlagsMask);
+}
+__device__ __forceinline__ uint32_t batch_bounce(uint32_t packed) { return (packed >> kPathIxShift) & 0xfu; }
+__device__ __forceinline__ uint32_t batch_item_of(uint32_t packed) { return packed >> kBatchItemShift; }
+
+// Pixel and sample index of a batch sample id of a known item.
+__device__ __forceinline__ BatchSample batch_sample_in(const FrameView& f, uint32_t id, uint32_t item)
+{
+    BatchSample b;
+    b.item = item;
+    const uint32_t local = id - __ldg(&f.items[item].sampleBase);
+    const uint32_t spp = __ldg(&f.items[item].spp);
+    b.pixel = local / spp;
+    b.sample = local - b.pixel * spp;
+    return b;
 }
 
-// Per-path bounce and flags of a batched path, kept in D.w (the packed normal
-// of one-scene paths, which nothing reads): bounce << 4 | flags.
-__device__ __forceinline__ uint32_t batch_pack(uint32_t bounce, uint32_t flags)
-{
-    return (bounce << kPathIxShift) | (flags & kFlagsMask);
-}
+// BVH root of a batch item.
+__device__ __forceinline__ uint32_t item_root(const FrameView& f, uint32_t item) { return __ldg(&f.items[item].root); }
 
 // The scene view of a batch item: the concatenated buffers with the item's
 // light range.
@@ -278,7 +287,7 @@ __device__ __forceinline__ SceneView item_scene(const SceneView& s, const BatchI
 // optix.cu:235-276): sc = samples accumulated before this frame.
 template <bool REF, bool BATCH>
 __device__ __forceinline__ void primary_ray(const FrameView& f, const Camera& cam, const Settings& st, uint32_t pathIx,
-                                            uint32_t sc, float3& O, float3& D, float& T)
+                                            uint32_t sc, float3& O, float3& D, float& T, uint32_t* itemOut = nullptr)
 {
     const uint32_t wh = f.resX * f.resY;
     const uint32_t pixelIx = pathIx % wh;
@@ -288,6 +297,8 @@ __device__ __forceinline__ void primary_ray(const FrameView& f, const Camera& ca
         // keyed as for one scene
         const BatchSample bs = batch_sample(f, pathIx);
         const BatchItem& it = f.items[bs.item];
+        if (itemOut)
+            *itemOut = bs.item;
         CounterRng rng;
         rng.init(bs.pixel, sc + bs.sample, 0u, st.seed);
         camera_ray(it.camera, it.width, it.height, bs.pixel % it.width, bs.pixel / it.width, rng, false, O, D, T);
@@ -396,7 +407,7 @@ __device__ __noinline__ void sky_miss(const SceneView& s, const FrameView& f, co
     const uint32_t pathIx = BATCH ? data : path_ix(data);
     const uint32_t flags = BATCH ? (__float_as_uint(D4.w) & kFlagsMask) : path_flags(data);
     if (BATCH)
-        bounce = __float_as_uint(D4.w) >> kPathIxShift;
+        bounce = batch_bounce(__float_as_uint(D4.w));
     const bool sun = s.sky.drawSun != 0.f && (bounce == 0 || (flags & kFlagSpecular));
     const float3 sky = sky_radiance(s.sky, f3(D4), sun);
     const float3 add = safe_color(f3(T4) * sky, st.maxColor);
@@ -448,11 +459,12 @@ __global__ void __launch_bounds__(128, 8) extend_kernel(SceneView s, FrameView f
                     if (BATCH ? i >= carried : PRIMARY) {
                         float3 O, D;
                         float T;
+                        uint32_t item = 0;
                         const uint32_t pathIx = BATCH ? freshBase + (i - carried) : camera_order(f, i);
-                        primary_ray<false, BATCH>(f, cam, st, pathIx, sc, O, D, T);
-                        // a batch path keeps its sample id in O.w and bounce | flags in D.w
+                        primary_ray<false, BATCH>(f, cam, st, pathIx, sc, O, D, T, &item);
+                        // a batch path keeps its sample id in O.w and item | bounce | flags in D.w
                         O4 = f4(O, u2f(BATCH ? pathIx : pack_path(pathIx, 0)));
-                        D4 = f4(D, 0.f);
+                        D4 = f4(D, BATCH ? u2f(batch_pack(0u, 0u, item)) : 0.f);
                         T4 = make_float4(T, T, T, 1.f);
                         f.radiance[pathIx] = make_float4(0.f, 0.f, 0.f, 0.f);
                     } else {
@@ -460,8 +472,8 @@ __global__ void __launch_bounds__(128, 8) extend_kernel(SceneView s, FrameView f
                         D4 = __ldcs(in + i + cap);
                         T4 = __ldcs(in + i + 2 * cap);
                     }
-                    const uint32_t id = BATCH ? __float_as_uint(O4.w) : path_ix(__float_as_uint(O4.w));
-                    traversal_begin(t, f3(O4), f3(D4), st.rayEpsilon, kDstMax, path_root<BATCH>(f, id));
+                    traversal_begin(t, f3(O4), f3(D4), st.rayEpsilon, kDstMax,
+                                    BATCH ? item_root(f, batch_item_of(__float_as_uint(D4.w))) : 0u);
                     alive = true;
                 } else {
                     more = false;
@@ -871,7 +883,9 @@ __device__ __forceinline__ bool shade_path(const SceneView& s, const FrameView& 
         wantShadow = true;
         sh[0] = f4(I, __uint_as_float(pathIx));
         sh[1] = f4(L, lightDist);
-        sh[2] = f4(safe_color(shadowT, st.maxColor), 0.f);
+        // a batch shadow ray carries its item's BVH root in T.w
+        sh[2] = f4(safe_color(shadowT, st.maxColor),
+                   BATCH ? u2f(item_root(f, batch_item_of(__float_as_uint(D4.w)))) : 0.f);
     }
 
     if (vi)
@@ -891,7 +905,8 @@ __device__ __forceinline__ bool shade_path(const SceneView& s, const FrameView& 
             flags &= ~kFlagSpecular;
         wantExt = true;
         ext[0] = f4(I, __uint_as_float(BATCH ? pathIx : pack_path(pathIx, flags)));
-        ext[1] = f4(nd, __uint_as_float(BATCH ? batch_pack(bounce + 1u, flags) : pack_normal(sf.N)));
+        ext[1] = f4(nd, __uint_as_float(BATCH ? batch_pack(bounce + 1u, flags, batch_item_of(__float_as_uint(D4.w)))
+                                              : pack_normal(sf.N)));
         ext[2] = f4(fixnan(tp), c.extPdf);
     }
     return false;
@@ -958,8 +973,8 @@ __global__ void __launch_bounds__(128, 5) shade_kernel(SceneView s, FrameView f,
             if (BATCH) {
                 // O.w is the sample id, D.w the path's bounce and flags
                 const uint32_t id = __float_as_uint(O4.w);
-                const uint32_t pathBounce = __float_as_uint(D4.w) >> kPathIxShift;
-                const BatchSample bs = batch_sample(f, id);
+                const uint32_t pathBounce = batch_bounce(__float_as_uint(D4.w));
+                const BatchSample bs = batch_sample_in(f, id, batch_item_of(__float_as_uint(D4.w)));
                 const SceneView si = item_scene(s, f.items[bs.item]);
                 CounterRng rng;
                 rng.init(bs.pixel, sc + bs.sample, pathBounce + 1u, st.seed);
@@ -1121,8 +1136,10 @@ __global__ void __launch_bounds__(128) connect_kernel(SceneView s, FrameView f, 
                     const float4 L4 = __ldcs(f.shadow + i + cap);
                     ray = i;
                     pathIx = __float_as_uint(O4.w);
-                    traversal_begin(t, f3(O4), f3(L4), st.rayEpsilon, L4.w - (2 * st.rayEpsilon),
-                                    path_root<BATCH>(f, pathIx));
+                    const uint32_t root =
+                        BATCH ? __float_as_uint(__ldcs(reinterpret_cast<const float*>(f.shadow + i + 2 * cap) + 3))
+                              : 0u;
+                    traversal_begin(t, f3(O4), f3(L4), st.rayEpsilon, L4.w - (2 * st.rayEpsilon), root);
                     alive = true;
                 } else {
                     more = false;
