@@ -1497,9 +1497,19 @@ __global__ void __launch_bounds__(256) batch_finalize_kernel(FrameView f, uint32
     const BatchItem& it = f.items[lo];
     const uint32_t spp = it.spp;
     const float4* r = f.radiance + it.sampleBase + size_t(p - it.pixelBase) * spp;
+    // in sample order; a thread's samples are consecutive, the lanes of a warp
+    // spp float4 apart, so two loads in flight per step and the lines kept in L1
+    // for the thread's next samples
     float3 sum = f3(0.f);
-    for (uint32_t k = 0; k < spp; ++k)
-        sum = sum + f3(__ldcs(r + k));
+    uint32_t k = 0;
+    for (; k + 1u < spp; k += 2u) {
+        const float4 a = __ldg(r + k);
+        const float4 b = __ldg(r + k + 1u);
+        sum = sum + f3(a);
+        sum = sum + f3(b);
+    }
+    if (k < spp)
+        sum = sum + f3(__ldg(r + k));
     const uint32_t sc = *f.sampleCount;
     float4 acc = sc == 0 ? make_float4(0.f, 0.f, 0.f, 0.f) : f.accumulator[p];
     acc = make_float4(acc.x + sum.x, acc.y + sum.y, acc.z + sum.z, acc.w + float(spp));
