@@ -38,7 +38,7 @@ sys.path.insert(0, str(ROOT))
 
 EXTEND_BYTES_PER_RAY = 48      # path state in (O, D, T: 48 B)
 EXTEND_BYTES_PER_HIT = 64      # path state (48 B) + hit record (16 B) appended to the hit queue
-NODE_BYTES = 80                # one CWBVH node
+NODE_BYTES = 80                # per node visit: the fixed algorithmic figure of a compressed 8-wide node
 TRI_BYTES = 48                 # one traversal triangle (v0, e1, e2)
 SHADE_BYTES_FIXED = 140        # state 48 + hit 16 + triangle record 72 + material index 4
 L2_BYTES = 129 * 1024 * 1024

@@ -270,7 +270,7 @@ typedef struct tr_scene_info {
     uint32_t triangle_count;
     uint32_t light_count;
     uint32_t material_count;
-    uint32_t bvh_node_count;        /* 8-wide compressed nodes (80 B each) */
+    uint32_t bvh_node_count;        /* 8-wide nodes (208 B with fp32 child boxes, 80 B quantized) */
     uint64_t device_bytes;          /* scene bytes resident on the device */
     float light_energy;             /* total emitted energy used for light picks */
     float build_time_ms;            /* host flattening + BVH build */
@@ -321,6 +321,10 @@ typedef struct tr_tuning {
     uint32_t sort_hits;             /* 1: counting sort of each bounce's hits by material before shade */
     uint32_t traversal_threads;     /* threads per block of the extend / connect launches: 64 or 128 */
     uint32_t shade_threads;         /* threads per block of the shade launches: 64 or 128 */
+    uint32_t bvh_nodes;             /* node layout: 0 auto (fp32 child boxes while the nodes fit 64 MB and
+                                       the scene has one level, else 8-bit quantized), 1 fp32 (208 B a
+                                       node), 2 quantized (80 B); tr_get_tuning reports the layout in use
+                                       (1 or 2) */
 } tr_tuning;
 
 typedef struct tr_tune_report {
@@ -646,13 +650,14 @@ tr_status tr_download_accumulator(void* ctx, void* stream, float* host_rgba, uin
 tr_status tr_copy_from_device(void* ctx, void* host_dst, const void* device_src, uint64_t bytes);
 tr_status tr_copy_to_device(void* ctx, void* device_dst, const void* host_src, uint64_t bytes);
 
-/* Host-side check of the acceleration structure: builds the 8-wide compressed
- * BVH of `scene` on the host and traverses n rays (float4 O, float4 D) with
- * the traversal source of tr_extend / tr_connect compiled for the CPU.
- * any_hit = 0: closest hit over [tmin, 1e30], hits as tr_extend writes them
- * (uint4: bary 16:16, instIx, primIx, bits(t)). any_hit = 1: first hit over
- * [tmin, D.w]; hits[4i+2] = primIx or ~0. counts (optional): uint2 per ray =
- * (nodes visited, triangles tested). No context or GPU needed. */
+/* Host-side check of the acceleration structure: builds the 8-wide BVH of
+ * `scene` on the host and traverses n rays (float4 O, float4 D) with the
+ * traversal source of tr_extend / tr_connect compiled for the CPU.
+ * any_hit bit 0 clear: closest hit over [tmin, 1e30], hits as tr_extend writes
+ * them (uint4: bary 16:16, instIx, primIx, bits(t)); set: first hit over
+ * [tmin, D.w]; hits[4i+2] = primIx or ~0. any_hit bit 1: the BVHs with
+ * 8-bit quantized child boxes instead of fp32 ones. counts (optional): uint2 per ray = (nodes visited, triangles tested).
+ * No context or GPU needed. */
 tr_status tr_trace_host(const tr_scene_desc* scene, const float* O4, const float* D4, uint32_t n, float tmin,
                         int32_t any_hit, uint32_t* hits, uint32_t* counts);
 

@@ -99,13 +99,14 @@ def _rays(scene, n, seed):
     return O, D
 
 
-def _host_trace(scene, O, D, any_hit=False, leaf=0, tmin=1e-3):
+def _host_trace(scene, O, D, any_hit=False, leaf=0, tmin=1e-3, quant=False):
     lib = _abi.load_library()
     h = SceneDescHolder(scene, leaf_size=leaf)
     n = O.shape[0]
     hits = np.zeros((n, 4), np.uint32)
     counts = np.zeros((n, 2), np.uint32)
-    st = lib.tr_trace_host(C.byref(h.desc), O.ctypes.data, D.ctypes.data, n, tmin, int(any_hit), hits.ctypes.data,
+    flags = int(any_hit) | (2 if quant else 0)  # bit 1: 8-bit quantized child boxes
+    st = lib.tr_trace_host(C.byref(h.desc), O.ctypes.data, D.ctypes.data, n, tmin, flags, hits.ctypes.data,
                            counts.ctypes.data)
     assert st == 0
     return hits, counts
@@ -125,28 +126,42 @@ def _check_closest(scene, O, D, hits):
     return same.mean()
 
 
+@pytest.mark.parametrize("quant", [False, True], ids=["fp32", "quantized"])
 @pytest.mark.parametrize("leaf", [1, 2, 3])
-def test_host_cwbvh_closest_hit_matches_oracle(leaf):
+def test_host_cwbvh_closest_hit_matches_oracle(leaf, quant):
     scene = random_soup(4000, seed=leaf)
     O, D = _rays(scene, 8000, seed=leaf)
-    hits, counts = _host_trace(scene, O, D, leaf=leaf)
+    hits, counts = _host_trace(scene, O, D, leaf=leaf, quant=quant)
     assert _check_closest(scene, O, D, hits) == 1.0
     assert counts[:, 0].min() >= 1
 
 
-def test_host_cwbvh_cornell_and_heightfield():
+@pytest.mark.parametrize("quant", [False, True], ids=["fp32", "quantized"])
+def test_host_cwbvh_cornell_and_heightfield(quant):
     for scene in (tr.cornell_box(), tr.heightfield(n=96, width=8, height=8)):
         O, D = _rays(scene, 6000, seed=3)
-        hits, _ = _host_trace(scene, O, D)
+        hits, _ = _host_trace(scene, O, D, quant=quant)
         # coplanar faces (box bottoms on the floor) are the only ties
         assert _check_closest(scene, O, D, hits) > 0.99
 
 
-def test_host_cwbvh_any_hit_matches_oracle():
+def test_host_node_layouts_visit_counts():
+    """Exact fp32 child boxes are never larger than their outward-rounded 8-bit
+    quantization, so no ray visits more nodes with them."""
+    scene = tr.heightfield(n=96, width=8, height=8)
+    O, D = _rays(scene, 6000, seed=7)
+    _, c32 = _host_trace(scene, O, D)
+    _, c8 = _host_trace(scene, O, D, quant=True)
+    assert (c32[:, 0] <= c8[:, 0]).all()
+    assert c32[:, 0].sum() < c8[:, 0].sum()
+
+
+@pytest.mark.parametrize("quant", [False, True], ids=["fp32", "quantized"])
+def test_host_cwbvh_any_hit_matches_oracle(quant):
     scene = random_soup(3000, seed=9)
     O, D = _rays(scene, 6000, seed=4)
     D[:, 3] = np.random.default_rng(5).uniform(0.05, 2.0, 6000).astype(np.float32)
-    hits, _ = _host_trace(scene, O, D, any_hit=True)
+    hits, _ = _host_trace(scene, O, D, any_hit=True, quant=quant)
     occluded_host = hits[:, 2] != 0xFFFFFFFF
     L = D.copy()
     L[:, 3] = D[:, 3] + 2e-3  # orc_trace_any uses tmax = dist - 2 eps

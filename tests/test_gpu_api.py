@@ -265,3 +265,33 @@ def test_tuning_keeps_images_and_autotune_picks_fastest():
     with pytest.raises(TracerError):
         r.SetTuning(bvh_leaf_size=4)
     r.close()
+
+
+@pytest.mark.parametrize("name", ["heightfield", "cornell", "instanced"])
+def test_node_layouts_render_the_same_image(name):
+    """fp32 and 8-bit quantized child boxes (tr_tuning.bvh_nodes 1 / 2) give the same
+    closest hits, so the same image up to hits on near ties; the default layout is
+    fp32 for a small one-level scene and quantized for a two-level one."""
+    scene = {"heightfield": lambda: tr.heightfield(n=128, width=64, height=36, rr_start=2),
+             "cornell": lambda: tr.cornell_box(width=48, height=40),
+             "instanced": lambda: tr.instanced_cornell(width=48, height=40)}[name]()
+    st = tr.settings_for(scene, multi_sample=2)
+    r = tr.DeviceRenderer(0)
+    r.UpdateScene(scene)
+    r.SetCamera(scene.camera)
+    r.Resize((scene.width, scene.height))
+    r.SetSettings(st)
+    assert r.Tuning()["bvh_nodes"] == (2 if name == "instanced" else 1)
+    imgs = {}
+    for layout in (1, 2):
+        r.SetTuning(bvh_nodes=layout)
+        assert r.Tuning()["bvh_nodes"] == layout
+        r.Reset()
+        r.RenderSamples(4)
+        imgs[layout] = r.ColorBuffer().copy()
+        assert r.Statistics()["device_error"] == 0
+    with pytest.raises(TracerError):
+        r.SetTuning(bvh_nodes=3)
+    r.close()
+    same = np.isclose(imgs[1], imgs[2], rtol=1e-5, atol=1e-7).all(-1).mean()
+    assert same >= 0.995, same

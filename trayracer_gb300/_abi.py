@@ -201,6 +201,7 @@ class Tuning(C.Structure):
         ("sort_hits", C.c_uint32),
         ("traversal_threads", C.c_uint32),
         ("shade_threads", C.c_uint32),
+        ("bvh_nodes", C.c_uint32),
     ]
 
 

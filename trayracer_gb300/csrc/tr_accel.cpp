@@ -20,9 +20,9 @@ SceneAccel build_accel(const tr_scene_desc& desc, const std::vector<uint32_t>& m
         const uint32_t nodeBase = uint32_t(out.nodes.size());
         const uint32_t slotBase = uint32_t(out.tris.size() / 3);
         out.meshRoot.push_back(nodeBase);
-        for (CwbvhNode n : wide.nodes) {
-            n.w[1].x += nodeBase;
-            n.w[1].y += slotBase;
+        for (WideNode n : wide.nodes) {
+            n.hdr.x += nodeBase;
+            n.hdr.y += slotBase;
             out.nodes.push_back(n);
         }
         out.tris.insert(out.tris.end(), wide.tris.begin(), wide.tris.end());

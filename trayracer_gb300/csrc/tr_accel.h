@@ -13,10 +13,10 @@
 namespace tr {
 
 struct SceneAccel {
-    std::vector<CwbvhNode> nodes;      // every mesh's BVH, child and triangle bases rebased
+    std::vector<WideNode> nodes;      // every mesh's BVH, child and triangle bases rebased
     std::vector<float4> tris;          // traversal triangles; v0.w = the mesh's own triangle index
     std::vector<uint32_t> meshRoot;    // first node of each mesh's BVH
-    std::vector<CwbvhNode> tlasNodes;  // two-level scenes: BVH over the instances' world boxes
+    std::vector<WideNode> tlasNodes;  // two-level scenes: BVH over the instances' world boxes
     std::vector<uint32_t> tlasInst;    // instance of each leaf slot of tlasNodes
     std::vector<uint2> instInfo;       // per instance: (BVH root node, first triangle of its mesh)
 };

@@ -92,6 +92,7 @@ struct Context {
     OwnedGeometry geom;            // host copy of the meshes and instances, for BVH rebuilds
     std::vector<uint32_t> meshTriBase;
     uint32_t leafSize = 3;
+    uint32_t nodeMode = 0;         // tr_tuning.bvh_nodes: 0 auto, 1 fp32, 2 quantized
     tr_tuning tuning{};
     SceneView scene{};
     tr_scene_info info{};
@@ -262,15 +263,23 @@ tr_status upload_texture(Context* c, const tr_texture_desc& t)
 // scene view at them.
 tr_status upload_bvh(Context* c, const SceneAccel& acc)
 {
+    const bool quant = quantized_nodes(acc.nodes.size() + acc.tlasNodes.size(), c->nodeMode, !acc.tlasNodes.empty());
+    const std::vector<QuantNode> qnodes = quant ? quantize_nodes(acc.nodes) : std::vector<QuantNode>{};
+    const std::vector<QuantNode> qtlas = quant ? quantize_nodes(acc.tlasNodes) : std::vector<QuantNode>{};
+    const void* nodeSrc = quant ? static_cast<const void*>(qnodes.data()) : static_cast<const void*>(acc.nodes.data());
+    const void* tlasSrc = quant ? static_cast<const void*>(qtlas.data()) : static_cast<const void*>(acc.tlasNodes.data());
+    const size_t nodeSize = quant ? sizeof(QuantNode) : sizeof(WideNode);
+    const size_t nodeBytes = acc.nodes.size() * nodeSize;
+    const size_t tlasBytes = acc.tlasNodes.size() * nodeSize;
     size_t off = 0;
     auto take = [&](size_t bytes) {
         const size_t o = off;
         off = align256(off + std::max<size_t>(bytes, 16));
         return o;
     };
-    const size_t oN = take(acc.nodes.size() * sizeof(CwbvhNode));
+    const size_t oN = take(nodeBytes);
     const size_t oT = take(acc.tris.size() * sizeof(float4));
-    const size_t oTl = take(acc.tlasNodes.size() * sizeof(CwbvhNode));
+    const size_t oTl = take(tlasBytes);
     const size_t oTi = take(acc.tlasInst.size() * sizeof(uint32_t));
     const size_t oIi = take(acc.instInfo.size() * sizeof(uint2));
     void* base = nullptr;
@@ -282,9 +291,9 @@ tr_status upload_bvh(Context* c, const SceneAccel& acc)
         return bytes ? cudaMemcpy(b + o, src, bytes, cudaMemcpyHostToDevice) : cudaSuccess;
     };
     const cudaError_t es[] = {
-        up(oN, acc.nodes.data(), acc.nodes.size() * sizeof(CwbvhNode)),
+        up(oN, nodeSrc, nodeBytes),
         up(oT, acc.tris.data(), acc.tris.size() * sizeof(float4)),
-        up(oTl, acc.tlasNodes.data(), acc.tlasNodes.size() * sizeof(CwbvhNode)),
+        up(oTl, tlasSrc, tlasBytes),
         up(oTi, acc.tlasInst.data(), acc.tlasInst.size() * sizeof(uint32_t)),
         up(oIi, acc.instInfo.data(), acc.instInfo.size() * sizeof(uint2)),
     };
@@ -296,22 +305,26 @@ tr_status upload_bvh(Context* c, const SceneAccel& acc)
     c->bvhArena.release();
     c->bvhArena.base = base;
     c->bvhArena.bytes = off;
-    c->scene.nodes = reinterpret_cast<const CwbvhNode*>(b + oN);
+    c->scene.nodes = b + oN;
+    c->scene.quantNodes = quant ? 1u : 0u;
     c->scene.bvhTris = reinterpret_cast<const float4*>(b + oT);
     c->scene.nodeCount = uint32_t(acc.nodes.size());
     const bool twoLevel = !acc.tlasNodes.empty();
-    c->scene.tlasNodes = twoLevel ? reinterpret_cast<const CwbvhNode*>(b + oTl) : nullptr;
+    c->scene.tlasNodes = twoLevel ? static_cast<const void*>(b + oTl) : nullptr;
     c->scene.tlasInst = twoLevel ? reinterpret_cast<const uint32_t*>(b + oTi) : nullptr;
     c->scene.instInfo = twoLevel ? reinterpret_cast<const uint2*>(b + oIi) : nullptr;
     c->info.bvh_node_count = uint32_t(acc.nodes.size() + acc.tlasNodes.size());
     return TR_OK;
 }
 
-// Rebuilds the BVH from the host copy of the geometry with another leaf size.
-tr_status rebuild_bvh(Context* c, uint32_t leafSize)
+// Rebuilds the BVH from the host copy of the geometry with another leaf size
+// or node layout.
+tr_status rebuild_bvh(Context* c, uint32_t leafSize, uint32_t nodeMode)
 {
-    if (leafSize == c->leafSize)
+    if (leafSize == c->leafSize && nodeMode == c->nodeMode)
         return TR_OK;
+    const uint32_t oldMode = c->nodeMode;
+    c->nodeMode = nodeMode;
     BvhBuildOptions opt;
     opt.maxLeafSize = leafSize;
     const SceneAccel wide = build_accel(c->geom.desc, c->meshTriBase, opt);
@@ -322,6 +335,8 @@ tr_status rebuild_bvh(Context* c, uint32_t leafSize)
     const tr_status st = upload_bvh(c, wide);
     if (st == TR_OK)
         c->leafSize = leafSize;
+    else
+        c->nodeMode = oldMode;
     return st;
 }
 
@@ -1032,6 +1047,7 @@ tr_status tr_get_tuning(void* ctx, tr_tuning* out)
     Context* c = static_cast<Context*>(ctx);
     tr_tuning t = c->tuning;
     t.bvh_leaf_size = c->leafSize;
+    t.bvh_nodes = c->hasScene ? (c->scene.quantNodes ? 2u : 1u) : c->nodeMode;
     if (c->shape.sms) {
         t.refill_below = c->shape.refillBelow;
         t.extend_blocks_per_sm = c->shape.extendBlocks / c->shape.sms;
@@ -1052,14 +1068,16 @@ tr_status tr_set_tuning(void* ctx, const tr_tuning* t)
     Context* c = static_cast<Context*>(ctx);
     auto threadsOk = [](uint32_t v) { return v == 0 || v == 64 || v == 128; };
     if (t->bvh_leaf_size > 3 || t->refill_below > 32 || t->shade_waves > 64 || t->sort_hits > 1 ||
-        !threadsOk(t->traversal_threads) || !threadsOk(t->shade_threads))
+        !threadsOk(t->traversal_threads) || !threadsOk(t->shade_threads) || t->bvh_nodes > 2)
         return fail(c, TR_ERR_INVALID_ARGUMENT, "tuning out of range (leaf size <= 3, refill <= 32, shade waves <= 64, "
-                                                "block sizes 64 or 128)");
+                                                "block sizes 64 or 128, node layout <= 2)");
     cudaSetDevice(c->device);
-    if (t->bvh_leaf_size && c->hasScene) {
-        const tr_status st = rebuild_bvh(c, t->bvh_leaf_size);
+    if (c->hasScene) {
+        const tr_status st = rebuild_bvh(c, t->bvh_leaf_size ? t->bvh_leaf_size : c->leafSize, t->bvh_nodes);
         if (st != TR_OK)
             return st;
+    } else {
+        c->nodeMode = t->bvh_nodes;
     }
     c->tuning = *t;
     c->tuning.bvh_leaf_size = c->leafSize;
@@ -1179,13 +1197,19 @@ tr_status tr_autotune(void* ctx, void* stream, uint32_t flags, tr_tune_report* r
         if (st == TR_OK)
             st = tryTuning(t);
     }
-    if ((flags & TR_TUNE_SKIP_BVH) == 0)
+    if ((flags & TR_TUNE_SKIP_BVH) == 0) {
         for (uint32_t leaf : {1u, 2u, 3u}) {
             tr_tuning t = best;
             t.bvh_leaf_size = leaf;
             if (st == TR_OK && leaf != best.bvh_leaf_size)
                 st = tryTuning(t);
         }
+        // the other node layout (fp32 or quantized child boxes)
+        tr_tuning t = best;
+        t.bvh_nodes = c->scene.quantNodes ? 1u : 2u;
+        if (st == TR_OK)
+            st = tryTuning(t);
+    }
     if (st == TR_OK)
         st = tr_set_tuning(ctx, &best);
     cudaEventDestroy(e0);

@@ -297,7 +297,7 @@ tr_status tr_batch_create(const tr_config* config, const tr_batch_item* items, u
             return bail(TR_ERR_INVALID_ARGUMENT);
 
     // concatenated host buffers with rebased indices
-    std::vector<CwbvhNode> nodes;
+    std::vector<WideNode> nodes;
     std::vector<float4> btris;
     std::vector<TriShade> tris;
     std::vector<uint32_t> matIdx;
@@ -313,9 +313,9 @@ tr_status tr_batch_create(const tr_config* config, const tr_batch_item* items, u
         const uint32_t primBase = uint32_t(tris.size());
         const uint32_t matBase = uint32_t(materials.size());
         const uint32_t lightBase = uint32_t(lights.size());
-        for (CwbvhNode n : r.bvh.nodes) {
-            n.w[1].x += nodeBase;
-            n.w[1].y += slotBase;
+        for (WideNode n : r.bvh.nodes) {
+            n.hdr.x += nodeBase;
+            n.hdr.y += slotBase;
             nodes.push_back(n);
         }
         for (size_t k = 0; k < r.bvh.tris.size(); ++k) {
@@ -372,7 +372,12 @@ tr_status tr_batch_create(const tr_config* config, const tr_batch_item* items, u
         off = align256(off + std::max<size_t>(bytes, 16));
         return o;
     };
-    const size_t oNodes = take(nodes.size() * sizeof(CwbvhNode));
+    // the node layout of the concatenated BVHs (fp32 child boxes while they fit L2)
+    const bool quant = quantized_nodes(nodes.size(), 0u);
+    const std::vector<QuantNode> qnodes = quant ? quantize_nodes(nodes) : std::vector<QuantNode>{};
+    const void* nodeSrc = quant ? static_cast<const void*>(qnodes.data()) : static_cast<const void*>(nodes.data());
+    const size_t nodeBytes = nodes.size() * (quant ? sizeof(QuantNode) : sizeof(WideNode));
+    const size_t oNodes = take(nodeBytes);
     const size_t oBTris = take(btris.size() * sizeof(float4));
     const size_t oTris = take(tris.size() * sizeof(TriShade));
     const size_t oMat = take(matIdx.size() * sizeof(uint32_t));
@@ -391,7 +396,7 @@ tr_status tr_batch_create(const tr_config* config, const tr_batch_item* items, u
         return bytes ? cudaMemcpy(sb + o, src, bytes, cudaMemcpyHostToDevice) : cudaSuccess;
     };
     const cudaError_t es[] = {
-        up(oNodes, nodes.data(), nodes.size() * sizeof(CwbvhNode)),
+        up(oNodes, nodeSrc, nodeBytes),
         up(oBTris, btris.data(), btris.size() * sizeof(float4)),
         up(oTris, tris.data(), tris.size() * sizeof(TriShade)),
         up(oMat, matIdx.data(), matIdx.size() * sizeof(uint32_t)),
@@ -404,7 +409,8 @@ tr_status tr_batch_create(const tr_config* config, const tr_batch_item* items, u
         if (x != cudaSuccess)
             return bail(TR_ERR_CUDA);
     SceneView& sv = b->scene;
-    sv.nodes = reinterpret_cast<const CwbvhNode*>(sb + oNodes);
+    sv.nodes = sb + oNodes;
+    sv.quantNodes = quant ? 1u : 0u;
     sv.bvhTris = reinterpret_cast<const float4*>(sb + oBTris);
     sv.tris = reinterpret_cast<const TriShade*>(sb + oTris);
     sv.matIdx = reinterpret_cast<const uint32_t*>(sb + oMat);

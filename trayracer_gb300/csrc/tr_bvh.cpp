@@ -417,7 +417,7 @@ Cwbvh collapse_to_cwbvh(const BinaryBvh& bvh, const float* positions, const uint
     const SahCollapse sah = sahMaxLeaf && !bvh.primRefs.empty() ? SahCollapse(bvh, sahMaxLeaf) : SahCollapse();
     Cwbvh out;
     const std::vector<BinaryNode>& bn = bvh.nodes;
-    out.nodes.push_back(CwbvhNode{});
+    out.nodes.push_back(WideNode{});
     if (bvh.primRefs.empty()) {
         // empty scene: a root without children never reports a hit
         return out;
@@ -554,32 +554,16 @@ Cwbvh collapse_to_cwbvh(const BinaryBvh& bvh, const float* positions, const uint
     if (positions)
         out.tris.resize(3 * size_t(nextTri));
 
-    // Encoding pass (parallel over wide nodes): quantized child boxes, meta bytes,
-    // the node words and the traversal triangles of its leaves.
+    // Encoding pass (parallel over wide nodes): child boxes, meta bytes, the
+    // node header and the traversal triangles of its leaves.
     auto encode = [&](const WideRec& rec) {
-        const Aabb& nodeBox = rec.box;
-        uint32_t w0[4] = {0, 0, 0, 0};
-        uint32_t meta[2] = {0, 0};
-        uint32_t q[6][2] = {};  // qlo.x, qlo.y, qlo.z, qhi.x, qhi.y, qhi.z
-        double scale[3];
-        int biased[3];
-        for (int a = 0; a < 3; ++a) {
-            const double extent = double(nodeBox.hi[a]) - double(nodeBox.lo[a]);
-            int e = -100;
-            if (extent > 0.0) {
-                int ex;
-                std::frexp(extent / 255.0, &ex);
-                e = ex;
+        WideNode node{};
+        for (int a = 0; a < 3; ++a)
+            for (int sl = 0; sl < 8; ++sl) {
+                node.lo[a][sl] = INFINITY;
+                node.hi[a][sl] = -INFINITY;
             }
-            e = std::max(-126, std::min(e, 127));
-            biased[a] = e + 127;
-            scale[a] = std::ldexp(1.0, e);
-            w0[a] = f2u(nodeBox.lo[a]);
-        }
-        w0[3] = uint32_t(biased[0]) | (uint32_t(biased[1]) << 8) | (uint32_t(biased[2]) << 16);
-
-        uint32_t imask = 0;
-        uint32_t internalCount = 0;
+        uint32_t meta[2] = {0, 0};
         uint32_t triCount = 0;
         for (int sl = 0; sl < 8; ++sl) {
             if (rec.slotKid[sl] < 0)
@@ -587,17 +571,11 @@ Cwbvh collapse_to_cwbvh(const BinaryBvh& bvh, const float* positions, const uint
             const Kid& kk = rec.kids[rec.slotKid[sl]];
             const BinaryNode& kid = bn[kk.bin];
             for (int a = 0; a < 3; ++a) {
-                const double lo = (double(kid.box.lo[a]) - double(nodeBox.lo[a])) / scale[a];
-                const double hi = (double(kid.box.hi[a]) - double(nodeBox.lo[a])) / scale[a];
-                const int qlo = std::max(0, std::min(255, int(std::floor(lo))));
-                const int qhi = std::max(0, std::min(255, int(std::ceil(hi))));
-                set_byte(q[a], sl, uint32_t(qlo));
-                set_byte(q[3 + a], sl, uint32_t(qhi));
+                node.lo[a][sl] = kid.box.lo[a];
+                node.hi[a][sl] = kid.box.hi[a];
             }
             if (!kk.leaf) {
-                imask |= 1u << sl;
                 set_byte(meta, sl, 0x20u | (24u + uint32_t(sl)));
-                internalCount++;
             } else {
                 const uint32_t unary = (1u << kk.count) - 1u;
                 set_byte(meta, sl, (unary << 5) | triCount);
@@ -617,14 +595,7 @@ Cwbvh collapse_to_cwbvh(const BinaryBvh& bvh, const float* positions, const uint
                 triCount += kk.count;
             }
         }
-        (void)internalCount;
-        w0[3] |= imask << 24;
-        CwbvhNode node{};
-        node.w[0] = make_uint4(w0[0], w0[1], w0[2], w0[3]);
-        node.w[1] = make_uint4(rec.childBase, rec.triBase, meta[0], meta[1]);
-        node.w[2] = make_uint4(q[0][0], q[0][1], q[1][0], q[1][1]);
-        node.w[3] = make_uint4(q[2][0], q[2][1], q[3][0], q[3][1]);
-        node.w[4] = make_uint4(q[4][0], q[4][1], q[5][0], q[5][1]);
+        node.hdr = make_uint4(rec.childBase, rec.triBase, meta[0], meta[1]);
         out.nodes[rec.wide] = node;
     };
     const unsigned hw = std::max(1u, std::thread::hardware_concurrency());
@@ -644,4 +615,65 @@ Cwbvh collapse_to_cwbvh(const BinaryBvh& bvh, const float* positions, const uint
         t.join();
     return out;
 }
+std::vector<QuantNode> quantize_nodes(const std::vector<WideNode>& nodes)
+{
+    std::vector<QuantNode> out(nodes.size());
+    for (size_t n = 0; n < nodes.size(); ++n) {
+        const WideNode& w = nodes[n];
+        const uint32_t meta[2] = {w.hdr.z, w.hdr.w};
+        auto metaOf = [&](int sl) { return (meta[sl >> 2] >> (8 * (sl & 3))) & 0xffu; };
+        Aabb box;
+        for (int a = 0; a < 3; ++a) {
+            box.lo[a] = INFINITY;
+            box.hi[a] = -INFINITY;
+        }
+        for (int sl = 0; sl < 8; ++sl)
+            if (metaOf(sl))
+                for (int a = 0; a < 3; ++a) {
+                    box.lo[a] = std::min(box.lo[a], w.lo[a][sl]);
+                    box.hi[a] = std::max(box.hi[a], w.hi[a][sl]);
+                }
+        uint32_t w0[4] = {0, 0, 0, 0};
+        uint32_t q[6][2] = {};  // qlo.x, qlo.y, qlo.z, qhi.x, qhi.y, qhi.z
+        double scale[3];
+        for (int a = 0; a < 3; ++a) {
+            if (!(box.lo[a] <= box.hi[a]))
+                box.lo[a] = box.hi[a] = 0.f;  // no child
+            const double extent = double(box.hi[a]) - double(box.lo[a]);
+            int e = -100;
+            if (extent > 0.0) {
+                int ex;
+                std::frexp(extent / 255.0, &ex);
+                e = ex;
+            }
+            e = std::max(-126, std::min(e, 127));
+            scale[a] = std::ldexp(1.0, e);
+            w0[a] = f2u(box.lo[a]);
+            w0[3] |= uint32_t(e + 127) << (8 * a);
+        }
+        uint32_t imask = 0;
+        for (int sl = 0; sl < 8; ++sl) {
+            const uint32_t m = metaOf(sl);
+            if (!m)
+                continue;
+            if ((m & 0x1fu) >= 24u)
+                imask |= 1u << sl;
+            for (int a = 0; a < 3; ++a) {
+                const double lo = (double(w.lo[a][sl]) - double(box.lo[a])) / scale[a];
+                const double hi = (double(w.hi[a][sl]) - double(box.lo[a])) / scale[a];
+                set_byte(q[a], sl, uint32_t(std::max(0, std::min(255, int(std::floor(lo))))));
+                set_byte(q[3 + a], sl, uint32_t(std::max(0, std::min(255, int(std::ceil(hi))))));
+            }
+        }
+        w0[3] |= imask << 24;
+        QuantNode& o = out[n];
+        o.w[0] = make_uint4(w0[0], w0[1], w0[2], w0[3]);
+        o.w[1] = w.hdr;
+        o.w[2] = make_uint4(q[0][0], q[0][1], q[1][0], q[1][1]);
+        o.w[3] = make_uint4(q[2][0], q[2][1], q[3][0], q[3][1]);
+        o.w[4] = make_uint4(q[4][0], q[4][1], q[5][0], q[5][1]);
+    }
+    return out;
+}
+
 } // namespace tr

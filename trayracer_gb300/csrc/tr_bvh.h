@@ -38,7 +38,7 @@ struct BinaryBvh {
 };
 
 struct Cwbvh {
-    std::vector<CwbvhNode> nodes;
+    std::vector<WideNode> nodes;
     std::vector<float4> tris;          // 3 float4 per triangle slot
     std::vector<uint32_t> triPrim;     // triangle index per slot
 };
@@ -60,6 +60,21 @@ BinaryBvh build_binary_bvh_boxes(const Aabb* boxes, uint32_t count, const BvhBui
 // 8); 1..3: SAH-optimal collapse with leaves of up to sahMaxLeaf triangles.
 Cwbvh collapse_to_cwbvh(const BinaryBvh& bvh, const float* positions, const uint32_t* indices,
                         uint32_t sahMaxLeaf = 0);
+
+// The same nodes with 8-bit quantized child boxes (rounded outwards against
+// each node's box, the union of its children's).
+std::vector<QuantNode> quantize_nodes(const std::vector<WideNode>& nodes);
+
+// Node layout of an uploaded BVH: mode 0 (auto) keeps fp32 child boxes while the
+// nodes fit kWideNodeBudget (they then stay in L2 beside the wavefront
+// buffers) and the scene has one level (the two-level traversal holds more
+// state, and fp32 nodes make it spill), 1 always fp32, 2 always quantized.
+// Returns true for quantized.
+constexpr size_t kWideNodeBudget = size_t(64) << 20;
+inline bool quantized_nodes(size_t nodeCount, uint32_t mode, bool twoLevel = false)
+{
+    return mode == 2u || (mode == 0u && (twoLevel || nodeCount * sizeof(WideNode) > kWideNodeBudget));
+}
 
 } // namespace tr
 

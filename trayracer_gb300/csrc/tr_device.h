@@ -79,20 +79,37 @@ struct AliasEntry {
     uint32_t alias;  // bucket taken otherwise
 };
 
-// 8-wide compressed BVH node (Ylitie, Karras, Laine, "Efficient Incoherent Ray
-// Traversal on GPUs Through Compressed Wide BVHs", HPG 2017), 80 bytes:
+// 8-wide BVH nodes with the child and leaf encoding of the compressed wide BVH
+// (Ylitie, Karras, Laine, "Efficient Incoherent Ray Traversal on GPUs Through
+// Compressed Wide BVHs", HPG 2017), in two layouts.
+// meta: 0 empty; internal child = 0x20 | (24 + slot); leaf = (unary triangle
+// count << 5) | triangle offset from tri_base. The internal children (the
+// node's imask) are the meta bytes whose low five bits are 24 or more.
+//
+// WideNode, child boxes in fp32, 208 bytes:
+//   hdr: child_base, tri_base, meta[0..3], meta[4..7]
+//   lo[a][slot], hi[a][slot]: the child boxes per axis (empty slot: +inf / -inf)
+// No per-child byte unpacking in the traversal, whose issue slots bound it;
+// used while the nodes stay L2-resident (the heightfield's 214k nodes: 45 MB).
+struct alignas(16) WideNode {
+    uint4 hdr;
+    float lo[3][8];
+    float hi[3][8];
+};
+static_assert(sizeof(WideNode) == 208, "WideNode must stay 208 bytes");
+
+// QuantNode, child boxes 8-bit quantized (the paper's layout), 80 bytes:
 //   w0: p.x, p.y, p.z (float bits), e.x | e.y<<8 | e.z<<16 | imask<<24
 //   w1: child_base, tri_base, meta[0..3], meta[4..7]
 //   w2: qlo.x[0..7], qlo.y[0..7]
 //   w3: qlo.z[0..7], qhi.x[0..7]
 //   w4: qhi.y[0..7], qhi.z[0..7]
-// e are biased exponents (scale = 2^(e-127)); a child box is
-// p + q * scale. meta: 0 empty; internal child = 0x20 | (24 + slot);
-// leaf = (unary triangle count << 5) | triangle offset from tri_base.
-struct alignas(16) CwbvhNode {
+// e are biased exponents (scale = 2^(e-127)); a child box is p + q * scale,
+// rounded outwards. For BVHs too large for L2.
+struct alignas(16) QuantNode {
     uint4 w[5];
 };
-static_assert(sizeof(CwbvhNode) == 80, "CwbvhNode must stay 80 bytes");
+static_assert(sizeof(QuantNode) == 80, "QuantNode must stay 80 bytes");
 
 // Scene as seen by the kernels (constant for one uploaded scene).
 // Preetham sky (CudaSky.h:105-156) with every term that does not depend on the
@@ -120,7 +137,7 @@ constexpr uint32_t kTraversalCounters = 6;
 constexpr uint32_t kMaxTraversalSteps = 1u << 22;
 
 struct SceneView {
-    const CwbvhNode* nodes;
+    const void* nodes;          // WideNode, or QuantNode when quantNodes
     const float4* bvhTris;      // 3 float4 per triangle in BVH order: (v0, bits(primIx)), (e1, 0), (e2, 0)
     const TriShade* tris;       // by primIx
     const uint32_t* matIdx;     // by primIx
@@ -130,7 +147,7 @@ struct SceneView {
     const float4* invTransforms; // 3 float4 per instance (inverse instance transform rows)
     // two-level scenes (null for one mesh): BVH over the instances, the instance
     // of each of its leaf slots, and per instance (BVH root node, first triangle)
-    const CwbvhNode* tlasNodes;
+    const void* tlasNodes;      // the same layout as nodes
     const uint32_t* tlasInst;
     const uint2* instInfo;
     int32_t lightCount;
@@ -139,6 +156,7 @@ struct SceneView {
     uint32_t nodeCount;
     uint32_t triCount;
     uint32_t stepLimit = kMaxTraversalSteps;  // bound on node visits of one ray (Settings::stepLimit per launch)
+    uint32_t quantNodes = 0;    // nodes and tlasNodes are QuantNode arrays (else WideNode)
     const TexSlots* texSlots;   // per material, null when the scene has no textures
     SkyView sky;
 };

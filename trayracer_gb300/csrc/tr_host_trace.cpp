@@ -1,5 +1,5 @@
-// Host-side run of the CWBVH build + traversal code of the extend/connect
-// kernels (tr_trace_host): the same node encoding and the same traversal
+// Host-side run of the 8-wide BVH build + traversal code of the extend/connect
+// kernels (tr_trace_host): the same node layouts and the same traversal
 // source (one or two levels), compiled for the CPU, so the BVH can be checked
 // without a GPU and the traversal work per ray (nodes visited, triangles
 // tested) can be counted.
@@ -28,14 +28,19 @@ extern "C" tr_status tr_trace_host(const tr_scene_desc* desc, const float* O4, c
     opt.threads = desc->build_threads;
     const FlatScene fs = flatten_scene(*desc);
     const SceneAccel acc = build_accel(*desc, fs.meshTriBase, opt);
+    const bool quant = (any_hit & 2) != 0;
+    any_hit &= 1;
+    const std::vector<QuantNode> qnodes = quant ? quantize_nodes(acc.nodes) : std::vector<QuantNode>{};
+    const std::vector<QuantNode> qtlas = quant ? quantize_nodes(acc.tlasNodes) : std::vector<QuantNode>{};
     SceneView s{};
-    s.nodes = acc.nodes.data();
+    s.nodes = quant ? static_cast<const void*>(qnodes.data()) : static_cast<const void*>(acc.nodes.data());
+    s.quantNodes = quant ? 1u : 0u;
     s.bvhTris = acc.tris.data();
     s.nodeCount = uint32_t(acc.nodes.size());
     s.triCount = uint32_t(fs.tris.size());
     s.invTransforms = fs.invTransforms.data();
     if (!acc.tlasNodes.empty()) {
-        s.tlasNodes = acc.tlasNodes.data();
+        s.tlasNodes = quant ? static_cast<const void*>(qtlas.data()) : static_cast<const void*>(acc.tlasNodes.data());
         s.tlasInst = acc.tlasInst.data();
         s.instInfo = acc.instInfo.data();
     }

@@ -22,6 +22,8 @@
 #include "tr_kernels.h"
 #include "tr_sky.h"
 
+#include <type_traits>
+
 #include "tr_bsdf.cuh"
 #include "tr_bsdf_dual.cuh"
 #include "tr_rng.h"
@@ -424,7 +426,7 @@ __device__ __noinline__ void sky_miss(const SceneView& s, const FrameView& f, co
 // new samples (their camera rays are made here), so the pool stays full.
 // Blocks of 64 or 128 threads (a launch parameter, LaunchShape::traversalThreads):
 // the kernel works per warp; 64 registers, 32 resident warps per SM.
-template <bool COUNT, bool BATCH, bool PRIMARY, bool TL>
+template <bool COUNT, bool BATCH, bool PRIMARY, bool TL, int LAYOUT = kLayoutScene>
 __global__ void __launch_bounds__(128, 8) extend_kernel(SceneView s, FrameView f, Settings st, uint32_t bounce,
                                                      Camera cam)
 {
@@ -486,7 +488,7 @@ __global__ void __launch_bounds__(128, 8) extend_kernel(SceneView s, FrameView f
         do {
             bool done = false;
             if (alive)
-                done = traversal_step<false, COUNT>(t, stack, s, &cnt);
+                done = traversal_step<false, COUNT, LAYOUT>(t, stack, s, &cnt);
             const bool hit = done && base(t).hitSlot != 0xffffffffu;
             const uint32_t slot = warp_append(hitCounter, hit);
             if (done) {
@@ -1108,7 +1110,7 @@ __global__ void __launch_bounds__(256) sort_scatter_kernel(FrameView f, SortView
 // Any hit of the bounce's shadow queue over [eps, dist - 2 eps]; an unoccluded
 // ray adds its radiance to its path. Same lane refill as extend_kernel.
 // Blocks of 64 or 128 threads (LaunchShape::traversalThreads): the kernel works per warp.
-template <bool COUNT, bool BATCH, bool TL>
+template <bool COUNT, bool BATCH, bool TL, int LAYOUT = kLayoutScene>
 __global__ void __launch_bounds__(128) connect_kernel(SceneView s, FrameView f, Settings st, uint32_t bounce)
 {
     const uint32_t count = BATCH ? __ldcg(&f.batch->connectQueue) : __ldcg(f.counters + kShadowCounterBase + bounce);
@@ -1150,7 +1152,7 @@ __global__ void __launch_bounds__(128) connect_kernel(SceneView s, FrameView f, 
             break;
         uint32_t active;
         do {
-            if (alive && traversal_step<true, COUNT>(t, stack, s, &cnt)) {
+            if (alive && traversal_step<true, COUNT, LAYOUT>(t, stack, s, &cnt)) {
                 if (!base(t).ok)
                     atomicOr(f.errorFlag, 1u);
                 if (base(t).hitSlot == 0xffffffffu) {
@@ -1934,21 +1936,36 @@ void launch_extend_variant(const SceneView& s0, const FrameView& f, const Settin
     const SceneView s = traced(s0, st);
     const bool count = (st.flags & TR_FLAG_COUNT_TRAVERSAL) != 0;
     const uint32_t g = shape.extendBlocks;
+    const uint32_t b = shape.traversalThreads;
+    // one-level scenes: an instance per node layout
+    auto oneLevel = [&](auto batchTag) {
+        constexpr bool BATCH = decltype(batchTag)::value;
+        if (s.quantNodes) {
+            if (count)
+                extend_kernel<true, BATCH, PRIMARY, false, kLayoutQuant><<<g, b, 0, stream>>>(s, f, st, bounce, cam);
+            else
+                extend_kernel<false, BATCH, PRIMARY, false, kLayoutQuant><<<g, b, 0, stream>>>(s, f, st, bounce, cam);
+        } else {
+            if (count)
+                extend_kernel<true, BATCH, PRIMARY, false, kLayoutWide><<<g, b, 0, stream>>>(s, f, st, bounce, cam);
+            else
+                extend_kernel<false, BATCH, PRIMARY, false, kLayoutWide><<<g, b, 0, stream>>>(s, f, st, bounce, cam);
+        }
+    };
     if (f.batch) {
+        oneLevel(std::true_type{});
+    } else if (s.tlasNodes && !s.quantNodes) {
         if (count)
-            extend_kernel<true, true, PRIMARY, false><<<g, shape.traversalThreads, 0, stream>>>(s, f, st, bounce, cam);
+            extend_kernel<true, false, PRIMARY, true, kLayoutWide><<<g, b, 0, stream>>>(s, f, st, bounce, cam);
         else
-            extend_kernel<false, true, PRIMARY, false><<<g, shape.traversalThreads, 0, stream>>>(s, f, st, bounce, cam);
+            extend_kernel<false, false, PRIMARY, true, kLayoutWide><<<g, b, 0, stream>>>(s, f, st, bounce, cam);
     } else if (s.tlasNodes) {
         if (count)
-            extend_kernel<true, false, PRIMARY, true><<<g, shape.traversalThreads, 0, stream>>>(s, f, st, bounce, cam);
+            extend_kernel<true, false, PRIMARY, true, kLayoutQuant><<<g, b, 0, stream>>>(s, f, st, bounce, cam);
         else
-            extend_kernel<false, false, PRIMARY, true><<<g, shape.traversalThreads, 0, stream>>>(s, f, st, bounce, cam);
+            extend_kernel<false, false, PRIMARY, true, kLayoutQuant><<<g, b, 0, stream>>>(s, f, st, bounce, cam);
     } else {
-        if (count)
-            extend_kernel<true, false, PRIMARY, false><<<g, shape.traversalThreads, 0, stream>>>(s, f, st, bounce, cam);
-        else
-            extend_kernel<false, false, PRIMARY, false><<<g, shape.traversalThreads, 0, stream>>>(s, f, st, bounce, cam);
+        oneLevel(std::false_type{});
     }
 }
 
@@ -1990,21 +2007,36 @@ cudaError_t launch_connect(const SceneView& s0, const FrameView& f, const Settin
     st.refillBelow = shape.refillBelow;
     const bool count = (st.flags & TR_FLAG_COUNT_TRAVERSAL) != 0;
     const uint32_t g = shape.connectBlocks;
+    const uint32_t b = shape.traversalThreads;
+    // one-level scenes: an instance per node layout
+    auto oneLevel = [&](auto batchTag) {
+        constexpr bool BATCH = decltype(batchTag)::value;
+        if (s.quantNodes) {
+            if (count)
+                connect_kernel<true, BATCH, false, kLayoutQuant><<<g, b, 0, stream>>>(s, f, st, bounce);
+            else
+                connect_kernel<false, BATCH, false, kLayoutQuant><<<g, b, 0, stream>>>(s, f, st, bounce);
+        } else {
+            if (count)
+                connect_kernel<true, BATCH, false, kLayoutWide><<<g, b, 0, stream>>>(s, f, st, bounce);
+            else
+                connect_kernel<false, BATCH, false, kLayoutWide><<<g, b, 0, stream>>>(s, f, st, bounce);
+        }
+    };
     if (f.batch) {
+        oneLevel(std::true_type{});
+    } else if (s.tlasNodes && !s.quantNodes) {
         if (count)
-            connect_kernel<true, true, false><<<g, shape.traversalThreads, 0, stream>>>(s, f, st, bounce);
+            connect_kernel<true, false, true, kLayoutWide><<<g, b, 0, stream>>>(s, f, st, bounce);
         else
-            connect_kernel<false, true, false><<<g, shape.traversalThreads, 0, stream>>>(s, f, st, bounce);
+            connect_kernel<false, false, true, kLayoutWide><<<g, b, 0, stream>>>(s, f, st, bounce);
     } else if (s.tlasNodes) {
         if (count)
-            connect_kernel<true, false, true><<<g, shape.traversalThreads, 0, stream>>>(s, f, st, bounce);
+            connect_kernel<true, false, true, kLayoutQuant><<<g, b, 0, stream>>>(s, f, st, bounce);
         else
-            connect_kernel<false, false, true><<<g, shape.traversalThreads, 0, stream>>>(s, f, st, bounce);
+            connect_kernel<false, false, true, kLayoutQuant><<<g, b, 0, stream>>>(s, f, st, bounce);
     } else {
-        if (count)
-            connect_kernel<true, false, false><<<g, shape.traversalThreads, 0, stream>>>(s, f, st, bounce);
-        else
-            connect_kernel<false, false, false><<<g, shape.traversalThreads, 0, stream>>>(s, f, st, bounce);
+        oneLevel(std::false_type{});
     }
     return cudaGetLastError();
 }
@@ -2053,12 +2085,18 @@ cudaError_t launch_adjoint(const SceneView& s0, const FrameView& f, const Camera
     fwd.refillBelow = shape.refillBelow;
     adjoint_generate_kernel<<<(f.pathCount + 255u) / 256u, 256, 0, stream>>>(f, cam, fwd, a);
     for (uint32_t bounce = 0; bounce < st.maxDepth; ++bounce) {
-        if (s.tlasNodes)
-            extend_kernel<false, false, false, true><<<shape.extendBlocks, shape.traversalThreads, 0, stream>>>(
-                s, f, fwd, bounce, Camera{});
+        if (s.tlasNodes && !s.quantNodes)
+            extend_kernel<false, false, false, true, kLayoutWide>
+                <<<shape.extendBlocks, shape.traversalThreads, 0, stream>>>(s, f, fwd, bounce, Camera{});
+        else if (s.tlasNodes)
+            extend_kernel<false, false, false, true, kLayoutQuant>
+                <<<shape.extendBlocks, shape.traversalThreads, 0, stream>>>(s, f, fwd, bounce, Camera{});
+        else if (s.quantNodes)
+            extend_kernel<false, false, false, false, kLayoutQuant>
+                <<<shape.extendBlocks, shape.traversalThreads, 0, stream>>>(s, f, fwd, bounce, Camera{});
         else
-            extend_kernel<false, false, false, false><<<shape.extendBlocks, shape.traversalThreads, 0, stream>>>(
-                s, f, fwd, bounce, Camera{});
+            extend_kernel<false, false, false, false, kLayoutWide>
+                <<<shape.extendBlocks, shape.traversalThreads, 0, stream>>>(s, f, fwd, bounce, Camera{});
         if (bounce > 0) {
             if (useSmem)
                 ext_grad_kernel<true><<<gradBlocks, kAdjointThreads, smem, stream>>>(s, f, bounce, a);
@@ -2141,8 +2179,8 @@ bool valid_threads(uint32_t t) { return t == 64u || t == 128u; }
 // their occupancy limit, shade capped at shadeWaves waves of resident blocks.
 void size_grids(LaunchShape& shape, uint32_t capacity)
 {
-    shape.extendPerSm = resident(extend_kernel<false, false, false, false>, shape.traversalThreads, 0);
-    shape.connectPerSm = resident(connect_kernel<false, false, false>, shape.traversalThreads, 0);
+    shape.extendPerSm = resident(extend_kernel<false, false, false, false, kLayoutWide>, shape.traversalThreads, 0);
+    shape.connectPerSm = resident(connect_kernel<false, false, false, kLayoutWide>, shape.traversalThreads, 0);
     shape.extendBlocks = shape.sms * shape.extendPerSm;
     shape.connectBlocks = shape.sms * shape.connectPerSm;
     const uint32_t maxShade = shape.sms *

@@ -190,6 +190,18 @@ __device__ __forceinline__ unsigned long long byte_pair(uint32_t lo, uint32_t hi
     asm("mov.b64 %0, {%1, %2};" : "=l"(d) : "r"(a), "r"(b));
     return d;
 }
+__device__ __forceinline__ unsigned long long sub2(unsigned long long a, unsigned long long b)
+{
+    unsigned long long d;
+    asm("sub.rn.f32x2 %0, %1, %2;" : "=l"(d) : "l"(a), "l"(b));
+    return d;
+}
+__device__ __forceinline__ unsigned long long mul2(unsigned long long a, unsigned long long b)
+{
+    unsigned long long d;
+    asm("mul.rn.f32x2 %0, %1, %2;" : "=l"(d) : "l"(a), "l"(b));
+    return d;
+}
 __device__ __forceinline__ float max3(float a, float b, float c)
 {
     float d;
@@ -206,8 +218,99 @@ __device__ __forceinline__ float min3(float a, float b, float c)
 
 // Intersects the 8 children of a node; returns the hit mask: bits 24..31 for
 // internal children (position 24 + (slot ^ (7 - octant))), bits 0..23 for
-// leaf triangles (offset from the node's triangle base).
-TR_HD uint32_t intersect_node(const CwbvhNode* __restrict__ nodes, uint32_t nodeIx,
+// leaf triangles (offset from the node's triangle base). imask gets the
+// node's internal children (bit per slot). A child plane's distance is
+// (plane - O) * invD with each operation rounded (the slab test of Ize,
+// "Robust BVH Ray Traversal", JCGT 2013: the far distance is scaled by
+// 1 + 2^-21.3 before the comparison to cover the rounding of both distances).
+TR_HD uint32_t intersect_wnode(const WideNode* __restrict__ nodes, uint32_t nodeIx,
+                                                   const float3& O, const float3& invD, uint32_t octInv, float tmin,
+                                                   float tmax, uint32_t& childBase, uint32_t& triBase,
+                                                   uint32_t& imask)
+{
+    const WideNode* node = nodes + nodeIx;
+    const uint4 h = ldg(&node->hdr);
+    childBase = h.x;
+    triBase = h.y;
+    // the near plane is hi on axes the ray walks backwards
+    const bool nx = invD.x < 0.f, ny = invD.y < 0.f, nz = invD.z < 0.f;
+    const float* nearX = nx ? node->hi[0] : node->lo[0];
+    const float* farX = nx ? node->lo[0] : node->hi[0];
+    const float* nearY = ny ? node->hi[1] : node->lo[1];
+    const float* farY = ny ? node->lo[1] : node->hi[1];
+    const float* nearZ = nz ? node->hi[2] : node->lo[2];
+    const float* farZ = nz ? node->lo[2] : node->hi[2];
+#ifdef __CUDA_ARCH__
+    const unsigned long long ox2 = pack2(O.x, O.x), oy2 = pack2(O.y, O.y), oz2 = pack2(O.z, O.z);
+    const unsigned long long ix2 = pack2(invD.x, invD.x), iy2 = pack2(invD.y, invD.y), iz2 = pack2(invD.z, invD.z);
+#endif
+
+    // Per byte of meta: the hit-mask bit position (internal children, whose
+    // low five bits are >= 24, are re-ordered by the ray octant) and the bits
+    // to set there (the unary triangle count, or one bit for an internal
+    // child; zero for an empty slot, so empty slots need no branch).
+    const uint32_t octInv4 = octInv * 0x01010101u;
+    uint32_t hitmask = 0;
+    imask = 0;
+#pragma unroll
+    for (int half = 0; half < 2; ++half) {
+        const uint32_t meta4 = half == 0 ? h.z : h.w;
+        const uint32_t inner4 = ((meta4 & (meta4 << 1)) & 0x10101010u) >> 4;  // 1 per internal child
+        // the four 0/1 bytes gathered into bits 28..31 by one multiply
+        imask |= ((inner4 * 0x10204080u) >> 28) << (4 * half);
+        const uint32_t bitIndex4 = (meta4 ^ (octInv4 & (inner4 * 0xffu))) & 0x1f1f1f1fu;
+        const uint32_t childBits4 = (meta4 >> 5) & 0x07070707u;
+        float t0x[4], t1x[4], t0y[4], t1y[4], t0z[4], t1z[4];
+#ifdef __CUDA_ARCH__
+        const float4 nX = ldg(reinterpret_cast<const float4*>(nearX) + half);
+        const float4 fX = ldg(reinterpret_cast<const float4*>(farX) + half);
+        const float4 nY = ldg(reinterpret_cast<const float4*>(nearY) + half);
+        const float4 fY = ldg(reinterpret_cast<const float4*>(farY) + half);
+        const float4 nZ = ldg(reinterpret_cast<const float4*>(nearZ) + half);
+        const float4 fZ = ldg(reinterpret_cast<const float4*>(farZ) + half);
+        // two children per packed subtract and multiply (each lane rounds as the
+        // scalar sub_rn / mul_rn do)
+        auto slab = [&](const float4& p, unsigned long long o2, unsigned long long i2, float (&t)[4]) {
+            unpack2(mul2(sub2(pack2(p.x, p.y), o2), i2), t[0], t[1]);
+            unpack2(mul2(sub2(pack2(p.z, p.w), o2), i2), t[2], t[3]);
+        };
+        slab(nX, ox2, ix2, t0x);
+        slab(fX, ox2, ix2, t1x);
+        slab(nY, oy2, iy2, t0y);
+        slab(fY, oy2, iy2, t1y);
+        slab(nZ, oz2, iz2, t0z);
+        slab(fZ, oz2, iz2, t1z);
+#else
+        for (int j = 0; j < 4; ++j) {
+            const int sl = 4 * half + j;
+            t0x[j] = mul_rn(sub_rn(nearX[sl], O.x), invD.x);
+            t1x[j] = mul_rn(sub_rn(farX[sl], O.x), invD.x);
+            t0y[j] = mul_rn(sub_rn(nearY[sl], O.y), invD.y);
+            t1y[j] = mul_rn(sub_rn(farY[sl], O.y), invD.y);
+            t0z[j] = mul_rn(sub_rn(nearZ[sl], O.z), invD.z);
+            t1z[j] = mul_rn(sub_rn(farZ[sl], O.z), invD.z);
+        }
+#endif
+#pragma unroll
+        for (int j = 0; j < 4; ++j) {
+#ifdef __CUDA_ARCH__
+            const float tn = max3(t0x[j], t0y[j], fmaxf(t0z[j], tmin));
+            const float tf = min3(t1x[j], t1y[j], fminf(t1z[j], tmax));
+#else
+            const float tn = fmaxf(fmaxf(t0x[j], t0y[j]), fmaxf(t0z[j], tmin));
+            const float tf = fminf(fminf(t1x[j], t1y[j]), fminf(t1z[j], tmax));
+#endif
+            if (tn <= tf * 1.0000004f)
+                hitmask |= ((childBits4 >> (8 * j)) & 7u) << ((bitIndex4 >> (8 * j)) & 31u);
+        }
+    }
+    return hitmask;
+}
+
+// The same for a node with 8-bit quantized child boxes (the compressed wide BVH
+// of Ylitie et al.): a child plane is p + q * 2^e of the node's origin and
+// exponents, its distance one fused multiply-add of the byte.
+TR_HD uint32_t intersect_qnode(const QuantNode* __restrict__ nodes, uint32_t nodeIx,
                                                    const float3& O, const float3& invD, uint32_t octInv, float tmin,
                                                    float tmax, uint32_t& childBase, uint32_t& triBase,
                                                    uint32_t& imask)
@@ -334,8 +437,12 @@ TR_HD void traversal_begin(Traversal& t, const float3& O, const float3& D, float
 // becomes its internal children (the rest of the old group waits on the
 // stack); returns its leaf group (base, bits). Returns false when a bound ran
 // out (t.ok cleared).
-template <bool COUNT>
-TR_HD bool node_step(Traversal& t, uint2* stack, const CwbvhNode* __restrict__ nodes, uint32_t stepLimit,
+// Node layout a traversal is compiled for: the scene's (a uniform branch per
+// node on SceneView::quantNodes), or fixed to fp32 or quantized child boxes.
+enum : int { kLayoutScene = 0, kLayoutWide = 1, kLayoutQuant = 2 };
+
+template <bool COUNT, int LAYOUT = kLayoutScene>
+TR_HD bool node_step(Traversal& t, uint2* stack, const void* __restrict__ nodes, bool quant, uint32_t stepLimit,
                      TraversalCounts* cnt, uint2& leaves)
 {
     leaves = make_uint2(0u, 0u);
@@ -354,7 +461,14 @@ TR_HD bool node_step(Traversal& t, uint2* stack, const CwbvhNode* __restrict__ n
             t.ok = false;
     }
     uint32_t childBase, triBase, imask;
-    const uint32_t hm = intersect_node(nodes, nodeIx, t.O, t.invD, t.octInv, t.tmin, t.tmax, childBase, triBase, imask);
+    // the node layout is the same for every ray of a launch (a uniform branch
+    // when it is not fixed at compile time)
+    const bool q = LAYOUT == kLayoutQuant || (LAYOUT == kLayoutScene && quant);
+    const uint32_t hm =
+        q ? intersect_qnode(static_cast<const QuantNode*>(nodes), nodeIx, t.O, t.invD, t.octInv, t.tmin, t.tmax,
+                                childBase, triBase, imask)
+              : intersect_wnode(static_cast<const WideNode*>(nodes), nodeIx, t.O, t.invD, t.octInv, t.tmin, t.tmax,
+                                childBase, triBase, imask);
     if (COUNT)
         cnt->nodes++;
     t.group = make_uint2(childBase, (hm & 0xff000000u) | imask);
@@ -393,7 +507,7 @@ TR_HD int leaf_triangles(Traversal& t, uint2 tris, const SceneView& s, Traversal
         }
         return false;
     };
-    if (ANY || !PAIR) {
+    if constexpr (ANY || !PAIR) {
         // one triangle at a time (any hit: a second fetch in flight costs the
         // shadow kernel registers and occupancy, and the first hit ends the ray;
         // two-level traversal: it would spill)
@@ -405,36 +519,37 @@ TR_HD int leaf_triangles(Traversal& t, uint2 tris, const SceneView& s, Traversal
                 return 2;
         }
         return found;
+    } else {
+        // closest hit: two triangles per iteration, both fetched before either is
+        // tested (the second fetch repeats the first when only one is left); tested
+        // in bit order, so the result is that of the one-at-a-time loop
+        while (tris.y != 0u) {
+            const uint32_t k0 = ffs32(tris.y) - 1u;
+            tris.y &= tris.y - 1u;
+            const bool two = tris.y != 0u;
+            const uint32_t k1 = two ? ffs32(tris.y) - 1u : k0;
+            tris.y &= tris.y - 1u;
+            const float4* p0 = s.bvhTris + 3u * (tris.x + k0);
+            const float4* p1 = s.bvhTris + 3u * (tris.x + k1);
+            const float4 a0 = ldg(p0 + 0), b0 = ldg(p0 + 1), c0 = ldg(p0 + 2);
+            const float4 a1 = ldg(p1 + 0), b1 = ldg(p1 + 1), c1 = ldg(p1 + 2);
+            test(tris.x + k0, a0, b0, c0);
+            if (two)
+                test(tris.x + k1, a1, b1, c1);
+        }
+        return found;
     }
-    // closest hit: two triangles per iteration, both fetched before either is
-    // tested (the second fetch repeats the first when only one is left); tested
-    // in bit order, so the result is that of the one-at-a-time loop
-    while (tris.y != 0u) {
-        const uint32_t k0 = ffs32(tris.y) - 1u;
-        tris.y &= tris.y - 1u;
-        const bool two = tris.y != 0u;
-        const uint32_t k1 = two ? ffs32(tris.y) - 1u : k0;
-        tris.y &= tris.y - 1u;
-        const float4* p0 = s.bvhTris + 3u * (tris.x + k0);
-        const float4* p1 = s.bvhTris + 3u * (tris.x + k1);
-        const float4 a0 = ldg(p0 + 0), b0 = ldg(p0 + 1), c0 = ldg(p0 + 2);
-        const float4 a1 = ldg(p1 + 0), b1 = ldg(p1 + 1), c1 = ldg(p1 + 2);
-        test(tris.x + k0, a0, b0, c0);
-        if (two)
-            test(tris.x + k1, a1, b1, c1);
-    }
-    return found;
 }
 
 // One step: the next hit child node of the current group with the leaf
 // triangles it reports, then a stack pop if the group is exhausted. Returns
 // true when the ray is finished (t.hitSlot, t.tmax, t.u, t.v hold the result;
 // t.ok is false if a bound was exceeded).
-template <bool ANY, bool COUNT>
+template <bool ANY, bool COUNT, int LAYOUT = kLayoutScene>
 TR_HD bool traversal_step(Traversal& t, uint2* stack, const SceneView& s, TraversalCounts* cnt)
 {
     uint2 tris;
-    if (!node_step<COUNT>(t, stack, s.nodes, s.stepLimit, cnt, tris))
+    if (!node_step<COUNT, LAYOUT>(t, stack, s.nodes, s.quantNodes != 0, s.stepLimit, cnt, tris))
         return true;
     if (leaf_triangles<ANY, COUNT, !ANY>(t, tris, s, cnt) == 2)
         return true;
@@ -503,7 +618,8 @@ TR_HD void traversal_begin(TraversalTL& r, const float3& O, const float3& D, flo
     r.hitInst = kNoInstance;
 }
 
-template <bool ANY, bool COUNT>
+// (two levels: the instance BVH has the layout of the mesh BVHs)
+template <bool ANY, bool COUNT, int LAYOUT = kLayoutScene>
 TR_HD bool traversal_step(TraversalTL& r, uint2* stack, const SceneView& s, TraversalCounts* cnt)
 {
     Traversal& t = r.t;
@@ -538,7 +654,8 @@ TR_HD bool traversal_step(TraversalTL& r, uint2* stack, const SceneView& s, Trav
     }
     const bool top = r.inst == kNoInstance;
     uint2 leaves;
-    if (!node_step<COUNT>(t, stack, top ? s.tlasNodes : s.nodes, s.stepLimit, cnt, leaves))
+    if (!node_step<COUNT, LAYOUT>(t, stack, top ? s.tlasNodes : s.nodes, s.quantNodes != 0, s.stepLimit, cnt,
+                                  leaves))
         return true;
     if (top) {
         r.leafGroup = leaves;  // entered one by one in the next steps
