@@ -896,7 +896,7 @@ def main():
             "stage_ms_per_step": {k: round(v, 3) for k, v in stage_ms.items()},
             "accuracy": accuracy,
             "roofline": {
-                "kernel": "extend_kernel (CWBVH closest hit)",
+                "kernel": "extend_kernel (8-wide BVH closest hit)",
                 "bound": "hbm",
                 "achieved": round(achieved, 1),
                 "peak": peak,

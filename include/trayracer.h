@@ -31,7 +31,7 @@
  *                    442-527, Tracer/CUDA/GPU/CudaFwd.h:9-31; the OptiX
  *                    acceleration build (Tracer/Optix/OptixRenderer.cpp:90-123,
  *                    Tracer/Resources/Model.cpp:240-306) is replaced by a host
- *                    built 8-wide compressed BVH
+ *                    built 8-wide BVH
  *   tr_set_camera <- DeviceRenderer::SetCamera, DeviceRenderer.cpp:25-40
  *   tr_set_settings <- KernelSettings, Tracer/Common/CommonStructs.h:145-153
  *   tr_get_statistics <- RenderStatistics::DeviceStatistics,

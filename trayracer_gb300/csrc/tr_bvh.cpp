@@ -1,6 +1,8 @@
 // Host BVH builder: binned SAH over triangle bounds, then a collapse (SAH-optimal
-// or greedy) to an 8-wide compressed BVH (CWBVH) with octant-ordered child slots
-// and 8-bit quantized child boxes (Ylitie, Karras, Laine, HPG 2017).
+// or greedy) to an 8-wide BVH with the child and leaf encoding of the compressed
+// wide BVH (octant-ordered child slots; Ylitie, Karras, Laine, HPG 2017), its
+// child boxes in fp32 (WideNode) and, for BVHs too large for L2, quantized to 8
+// bits (QuantNode, quantize_nodes).
 #include "tr_bvh.h"
 
 #include <algorithm>
@@ -252,9 +254,9 @@ struct SahCollapse {
 
     void node(uint32_t x)
     {
-        // a triangle test weighed as a node visit: with these kernels a node test (80 bytes,
-        // eight slabs) and a triangle test (48 bytes) cost about alike, and this weight gave
-        // the fewest node visits and triangle tests together on the benchmark heightfield
+        // a triangle test weighed as a node visit: with these kernels a node test (eight
+        // slabs) and a triangle test (48 bytes) cost about alike, and this weight gave the
+        // fewest node visits and triangle tests together on the benchmark heightfield
         constexpr float kNode = 1.f, kPrim = 1.f;
         const BinaryNode& b = (*bn)[x];
         const float area = box_area(b.box);

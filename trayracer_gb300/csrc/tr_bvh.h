@@ -1,5 +1,6 @@
-// Host BVH builder: binned-SAH binary BVH, collapsed into an 8-wide
-// compressed BVH (CWBVH) for the extend/connect kernels. Replaces the OptiX
+// Host BVH builder: binned-SAH binary BVH, collapsed into an 8-wide BVH with
+// the compressed wide BVH's child and leaf encoding (fp32 or 8-bit quantized
+// child boxes) for the extend/connect kernels. Replaces the OptiX
 // acceleration-structure build of the reference (Model::Upload,
 // Tracer/Resources/Model.cpp:240-306; OptixRenderer::BuildAccel,
 // Tracer/Optix/OptixRenderer.cpp:90-123).
@@ -53,7 +54,7 @@ BinaryBvh build_binary_bvh(const float* positions, const uint32_t* indices, uint
 // scene).
 BinaryBvh build_binary_bvh_boxes(const Aabb* boxes, uint32_t count, const BvhBuildOptions& options);
 
-// Collapses a binary BVH into the 8-wide compressed layout and packs the
+// Collapses a binary BVH into 8-wide nodes (fp32 child boxes) and packs the
 // traversal triangles (v0, e1 = v1 - v0, e2 = v2 - v0). positions == nullptr
 // (a BVH over boxes): no triangles, triPrim names the primitive of each leaf
 // slot. sahMaxLeaf = 0: greedy collapse (open the largest internal child until

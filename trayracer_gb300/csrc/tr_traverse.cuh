@@ -1,4 +1,5 @@
-// Closest-hit and any-hit traversal of the 8-wide compressed BVH (CWBVH).
+// Closest-hit and any-hit traversal of the 8-wide BVH (the compressed wide BVH's
+// child and leaf encoding, child boxes in fp32 or 8-bit quantized).
 //
 // Replaces optixTrace (Tracer/Optix/GPU/optix.cu:264,308,333) with a software
 // traversal following Ylitie, Karras and Laine (HPG 2017): node groups on a
