@@ -847,6 +847,12 @@ def main():
         except Exception as e:  # the checker is optional; the GPU numbers stand
             cpu = {"value": None, "unavailable": str(e)}
 
+    # the plain workload's renderer and flush buffer are released before the other
+    # configurations, so that their measurements do not run beside its allocations
+    r.close()
+    del flush
+    torch.cuda.empty_cache()
+
     # --- the batched and differentiation configurations, measured in the same process after
     # the plain timed region (their own timed regions, CUDA events, L2 flushed)
     batch = adjoint = large = None
@@ -936,7 +942,6 @@ def main():
             "large": large,
         }
         print(json.dumps(line), flush=True)
-    r.close()
     if ws > 1:
         torch.distributed.destroy_process_group()
 
