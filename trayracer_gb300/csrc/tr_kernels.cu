@@ -297,10 +297,19 @@ __device__ __forceinline__ void primary_ray(const FrameView& f, const Camera& ca
     if (BATCH) {
         // pathIx is the sample id: the item's camera and film, the counter RNG
         // keyed as for one scene
-        const BatchSample bs = batch_sample(f, pathIx);
+        // itemOut (optional) comes in as an item at or before the sample's and
+        // goes out as the sample's item
+        BatchSample bs;
+        if (itemOut) {
+            uint32_t item = *itemOut;
+            while (item + 1u < f.itemCount && __ldg(&f.items[item + 1u].sampleBase) <= pathIx)
+                ++item;
+            *itemOut = item;
+            bs = batch_sample_in(f, pathIx, item);
+        } else {
+            bs = batch_sample(f, pathIx);
+        }
         const BatchItem& it = f.items[bs.item];
-        if (itemOut)
-            *itemOut = bs.item;
         CounterRng rng;
         rng.init(bs.pixel, sc + bs.sample, 0u, st.seed);
         camera_ray(it.camera, it.width, it.height, bs.pixel % it.width, bs.pixel / it.width, rng, false, O, D, T);
@@ -455,13 +464,29 @@ __global__ void __launch_bounds__(128, 8) extend_kernel(SceneView s, FrameView f
             if (lane == leader)
                 base = atomicAdd(work, __popc(idle));
             base = __shfl_sync(kFull, base, leader);
+            // batched: the item of the first new sample of this refill, found by the
+            // whole warp (the first sample ids of 32 items per load and a ballot, in
+            // place of a binary search per lane); the refill's new sample ids are
+            // consecutive, so a lane's own item is at most a few further
+            uint32_t warpItem = 0;
+            if (BATCH && f.itemCount > 1u && base + __popc(idle) > carried && base < count) {
+                const uint32_t firstFresh = freshBase + (base > carried ? base - carried : 0u);
+                for (uint32_t j0 = 1u; j0 < f.itemCount; j0 += 32u) {
+                    const uint32_t j = j0 + lane;
+                    const uint32_t m =
+                        __ballot_sync(kFull, j < f.itemCount && __ldg(&f.items[j].sampleBase) <= firstFresh);
+                    warpItem += __popc(m);
+                    if (m != kFull)
+                        break;  // items are in sample order: none later starts at or before it
+                }
+            }
             if (!alive && more) {
                 const uint32_t i = base + __popc(idle & ((1u << lane) - 1u));
                 if (i < count) {
                     if (BATCH ? i >= carried : PRIMARY) {
                         float3 O, D;
                         float T;
-                        uint32_t item = 0;
+                        uint32_t item = warpItem;
                         const uint32_t pathIx = BATCH ? freshBase + (i - carried) : camera_order(f, i);
                         primary_ray<false, BATCH>(f, cam, st, pathIx, sc, O, D, T, &item);
                         // a batch path keeps its sample id in O.w and item | bounce | flags in D.w
