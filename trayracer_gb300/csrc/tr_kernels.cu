@@ -1005,8 +1005,8 @@ __global__ void __launch_bounds__(128, 5) shade_kernel(SceneView s, FrameView f,
                 const SceneView si = item_scene(s, f.items[bs.item]);
                 CounterRng rng;
                 rng.init(bs.pixel, sc + bs.sample, pathBounce + 1u, st.seed);
-                emitted = shade_path<false, CounterRng, false, true>(si, f, st, pathBounce, sc, O4, D4, T4, hd, rng,
-                                                                     wantExt, ext, wantShadow, sh);
+                emitted = shade_path<false, CounterRng, TEX, true>(si, f, st, pathBounce, sc, O4, D4, T4, hd, rng,
+                                                                   wantExt, ext, wantShadow, sh);
             } else if (REF) {
                 RefRng rng{tea2(st.seed + pathIx, sc + bounce + 1u)};
                 emitted = shade_path<REF, RefRng, TEX>(s, f, st, bounce, sc, O4, D4, T4, hd, rng, wantExt, ext,
@@ -2011,7 +2011,9 @@ cudaError_t launch_shade(const SceneView& s, const FrameView& f, const Settings&
 {
     const bool ref = (st.flags & TR_FLAG_REFERENCE_SAMPLING) != 0;
     const size_t smem = size_t(shape.shadeThreads) * kShadeStageBytes;
-    if (f.batch)
+    if (f.batch && s.texSlots)
+        shade_kernel<false, true, true><<<shape.shadeBlocks, shape.shadeThreads, smem, stream>>>(s, f, st, bounce);
+    else if (f.batch)
         shade_kernel<false, true><<<shape.shadeBlocks, shape.shadeThreads, smem, stream>>>(s, f, st, bounce);
     else if (s.texSlots && ref)
         shade_kernel<true, false, true><<<shape.shadeBlocks, shape.shadeThreads, smem, stream>>>(s, f, st, bounce);
