@@ -380,8 +380,8 @@ tr_status tr_render_frame(void* ctx, void* stream, int32_t use_graph);
  * equals the frame sequence's up to the order of the per-pixel sums (all spp
  * samples summed in sample order, not frame by frame). Allocates 16 B per
  * sample for the per-sample radiance. Where the continuous kernels do not
- * apply (TR_FLAG_REFERENCE_SAMPLING, TR_FLAG_WRITE_AOVS, two-level scenes,
- * other render modes, more than 2^30 samples) it renders the frames. After
+ * apply (TR_FLAG_REFERENCE_SAMPLING, TR_FLAG_WRITE_AOVS, other render modes,
+ * more than 2^30 samples) it renders the frames. After
  * it, tr_get_statistics reports totals: path_count, shadow_ray_count,
  * hit_ray_count, primary_path_count (width * height * spp) and
  * secondary_path_count (every other extend ray), iterations and launches;

@@ -123,15 +123,30 @@ def test_samples_textured_scene():
     assert abs(s["path_count"] - want_rays) <= 1e-3 * want_rays
 
 
-@pytest.mark.parametrize("case", ["instanced", "reference"])
-def test_samples_fall_back_to_frames(case):
-    # two-level scenes and the reference's sampling render the frames themselves
-    scene = tr.instanced_cornell(width=40, height=32) if case == "instanced" else tr.cornell_box(width=40, height=32)
-    st = tr.settings_for(scene, multi_sample=2, reference=case == "reference")
+def test_samples_two_level_scene():
+    """Instanced scenes (two-level traversal) go through the continuous kernels too."""
+    scene = tr.instanced_cornell(width=40, height=32)
+    st = tr.settings_for(scene, multi_sample=2)
+    want, _, want_rays = frames(scene, st, 2)
+    r = renderer(scene, st)
+    r.RenderSamples(4)
+    got = r.ColorBuffer()
+    s = r.Statistics()
+    r.close()
+    assert s["iterations"] > 0 and s["device_error"] == 0
+    np.testing.assert_allclose(got, want, rtol=1e-5, atol=1e-7)
+    assert abs(s["path_count"] - want_rays) <= 1e-3 * want_rays
+
+
+def test_samples_fall_back_to_frames():
+    # the reference's sampling renders the frames themselves
+    scene = tr.cornell_box(width=40, height=32)
+    st = tr.settings_for(scene, multi_sample=2, reference=True)
     want, _, _ = frames(scene, st, 2)
     r = renderer(scene, st)
     r.RenderSamples(4)
     got = r.ColorBuffer()
+    assert r.Statistics()["iterations"] == 0
     r.close()
     np.testing.assert_array_equal(got, want)
 

@@ -1460,8 +1460,7 @@ tr_status tr_render_samples(void* ctx, void* stream, uint32_t spp, int32_t use_g
     const uint64_t samples = wh * spp;
     const uint32_t flags = c->settings.flags;
     const bool continuous = c->renderMode == kModePathTracing &&
-                            (flags & (TR_FLAG_REFERENCE_SAMPLING | TR_FLAG_WRITE_AOVS)) == 0 && !c->scene.tlasNodes &&
-                            samples <= (1ull << 30);
+                            (flags & (TR_FLAG_REFERENCE_SAMPLING | TR_FLAG_WRITE_AOVS)) == 0 && samples <= (1ull << 30);
     if (!continuous) {
         for (uint32_t k = 0; k < spp / ms && st == TR_OK; ++k)
             st = tr_render_frame(ctx, stream, use_graph);

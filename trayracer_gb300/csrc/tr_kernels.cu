@@ -1977,20 +1977,36 @@ void launch_extend_variant(const SceneView& s0, const FrameView& f, const Settin
                 extend_kernel<false, BATCH, PRIMARY, false, kLayoutWide><<<g, b, 0, stream>>>(s, f, st, bounce, cam);
         }
     };
-    if (f.batch) {
-        oneLevel(std::true_type{});
-    } else if (s.tlasNodes && !s.quantNodes) {
-        if (count)
-            extend_kernel<true, false, PRIMARY, true, kLayoutWide><<<g, b, 0, stream>>>(s, f, st, bounce, cam);
+    auto twoLevel = [&](auto batchTag) {
+        constexpr bool BATCH = decltype(batchTag)::value;
+        if (!s.quantNodes) {
+            if (count)
+                extend_kernel<true, BATCH, PRIMARY, true, kLayoutWide><<<g, b, 0, stream>>>(s, f, st, bounce, cam);
+            else
+                extend_kernel<false, BATCH, PRIMARY, true, kLayoutWide><<<g, b, 0, stream>>>(s, f, st, bounce, cam);
+        } else {
+            if (count)
+                extend_kernel<true, BATCH, PRIMARY, true, kLayoutQuant><<<g, b, 0, stream>>>(s, f, st, bounce, cam);
+            else
+                extend_kernel<false, BATCH, PRIMARY, true, kLayoutQuant><<<g, b, 0, stream>>>(s, f, st, bounce, cam);
+        }
+    };
+    // batched paths make their camera rays in the launch from their sample ids,
+    // never from a frame's camera (no PRIMARY variant)
+    if constexpr (PRIMARY) {
+        if (s.tlasNodes)
+            twoLevel(std::false_type{});
         else
-            extend_kernel<false, false, PRIMARY, true, kLayoutWide><<<g, b, 0, stream>>>(s, f, st, bounce, cam);
-    } else if (s.tlasNodes) {
-        if (count)
-            extend_kernel<true, false, PRIMARY, true, kLayoutQuant><<<g, b, 0, stream>>>(s, f, st, bounce, cam);
-        else
-            extend_kernel<false, false, PRIMARY, true, kLayoutQuant><<<g, b, 0, stream>>>(s, f, st, bounce, cam);
+            oneLevel(std::false_type{});
     } else {
-        oneLevel(std::false_type{});
+        if (f.batch && s.tlasNodes)
+            twoLevel(std::true_type{});
+        else if (f.batch)
+            oneLevel(std::true_type{});
+        else if (s.tlasNodes)
+            twoLevel(std::false_type{});
+        else
+            oneLevel(std::false_type{});
     }
 }
 
@@ -2050,21 +2066,28 @@ cudaError_t launch_connect(const SceneView& s0, const FrameView& f, const Settin
                 connect_kernel<false, BATCH, false, kLayoutWide><<<g, b, 0, stream>>>(s, f, st, bounce);
         }
     };
-    if (f.batch) {
+    auto twoLevel = [&](auto batchTag) {
+        constexpr bool BATCH = decltype(batchTag)::value;
+        if (!s.quantNodes) {
+            if (count)
+                connect_kernel<true, BATCH, true, kLayoutWide><<<g, b, 0, stream>>>(s, f, st, bounce);
+            else
+                connect_kernel<false, BATCH, true, kLayoutWide><<<g, b, 0, stream>>>(s, f, st, bounce);
+        } else {
+            if (count)
+                connect_kernel<true, BATCH, true, kLayoutQuant><<<g, b, 0, stream>>>(s, f, st, bounce);
+            else
+                connect_kernel<false, BATCH, true, kLayoutQuant><<<g, b, 0, stream>>>(s, f, st, bounce);
+        }
+    };
+    if (f.batch && s.tlasNodes)
+        twoLevel(std::true_type{});
+    else if (f.batch)
         oneLevel(std::true_type{});
-    } else if (s.tlasNodes && !s.quantNodes) {
-        if (count)
-            connect_kernel<true, false, true, kLayoutWide><<<g, b, 0, stream>>>(s, f, st, bounce);
-        else
-            connect_kernel<false, false, true, kLayoutWide><<<g, b, 0, stream>>>(s, f, st, bounce);
-    } else if (s.tlasNodes) {
-        if (count)
-            connect_kernel<true, false, true, kLayoutQuant><<<g, b, 0, stream>>>(s, f, st, bounce);
-        else
-            connect_kernel<false, false, true, kLayoutQuant><<<g, b, 0, stream>>>(s, f, st, bounce);
-    } else {
+    else if (s.tlasNodes)
+        twoLevel(std::false_type{});
+    else
         oneLevel(std::false_type{});
-    }
     return cudaGetLastError();
 }
 
