@@ -398,7 +398,7 @@ def measure_batch(args, steps, warmup, with_ms1=True):
                 for _ in range(frames):
                     r.RenderFrame(stream=sptr, use_graph=False)
                     total_rays += r.Statistics()["path_count"]
-                n_launch += frames * (3 * st.maxDepth + 3)
+                n_launch += frames * (3 * st.maxDepth + 2)  # kernels: extend, shade, connect per bounce, finalize, advance
         return total_ms, total_rays, n_launch, pclocks.summary()
 
     plain_ms, plain_rays, launches, plain_clocks = per_scene(16)

@@ -610,7 +610,7 @@ typedef struct tr_batch_statistics {
     uint64_t traversal_connect_nodes;
     uint64_t traversal_connect_tris;
     uint32_t iterations;            /* wavefront iterations that traced rays */
-    uint32_t launches;              /* kernels of the last render (4 per iteration, per round 2 + 4) */
+    uint32_t launches;              /* kernels of the last render (4 per iteration, per round 1 + 4) */
 } tr_batch_statistics;
 
 /* Builds and uploads all items (host threads build the BVHs). Items are

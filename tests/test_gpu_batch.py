@@ -77,7 +77,7 @@ def test_batch_equals_single_scene_renders(pool):
             got = b.Image(i)
             np.testing.assert_allclose(got, want, rtol=2e-6, atol=1e-7)
         assert stats["extend_rays"] + stats["shadow_rays"] == rays
-        assert stats["launches"] == 2 + 4 * (stats["iterations"] + 1)
+        assert stats["launches"] == 1 + 4 * (stats["iterations"] + 1)
 
 
 def test_batch_graph_equals_eager():

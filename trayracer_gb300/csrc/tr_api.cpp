@@ -1606,9 +1606,9 @@ tr_status tr_get_statistics(void* ctx, tr_statistics* out)
         s.radiance_updates_connect = trav[5];
         s.hit_ray_count = bs.hitRays;
         s.iterations = bs.iterations;
-        // start, finalize, advance, and plan + connect + extend + shade per iteration (the
-        // last finds nothing to trace)
-        s.launches = 3u + 4u * (bs.iterations + 1u);
+        // kernels: finalize, advance, and plan + connect + extend + shade per iteration (the
+        // last finds nothing to trace); the round-start memset is not a kernel
+        s.launches = 2u + 4u * (bs.iterations + 1u);
         if (c->samplesTimed) {
             const StageTimes& t = c->samplesTimes;
             s.generate_time_ms = t.plan;

@@ -585,7 +585,9 @@ tr_status tr_batch_get_statistics(void* batch, tr_batch_statistics* out)
     }
     // per round: start, finalize, and plan + extend + shade + connect per iteration (the last
     // iteration of a round finds nothing to trace)
-    s.launches = uint32_t(b->rounds.size()) * 2u + 4u * (s.iterations + uint32_t(b->rounds.size()));
+    // kernels: per round its finalize and plan + connect + extend + shade per iteration (the
+    // last finds nothing to trace); the round-start memset is not a kernel
+    s.launches = uint32_t(b->rounds.size()) + 4u * (s.iterations + uint32_t(b->rounds.size()));
     float ms = 0.f;
     cudaEventElapsedTime(&ms, b->evStart, b->evStop);
     s.render_time_ms = ms;
