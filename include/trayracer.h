@@ -614,7 +614,8 @@ typedef struct tr_batch_statistics {
 } tr_batch_statistics;
 
 /* Builds and uploads all items (host threads build the BVHs). Items are
- * one-mesh scenes (instance_count 0). Device memory: 160 B per path slot,
+ * one-mesh scenes (instance_count 0), with or without textures (the batch
+ * owns a copy of each item's textures). Device memory: 160 B per path slot,
  * 16 B per sample of the largest round, 32 B per pixel. TR_ERR_LIMIT when an
  * item has more than 2^30 samples, pool_paths >= 2^28 or count >= 2^24. */
 tr_status tr_batch_create(const tr_config* config, const tr_batch_item* items, uint32_t count, uint64_t pool_paths,

@@ -232,29 +232,16 @@ void release_textures(Context* c)
     c->texSlotsHost.clear();
 }
 
-// Texture::Upload (Texture.cpp:83-139): RGBA binary16 texels in a CUDA array,
-// sampled with bilinear filtering, wrap addressing and normalised coordinates
-// (the same texture description as the reference's, so a texel fetch filters
-// the same way).
+// A context's texture: owned by the context from here on.
 tr_status upload_texture(Context* c, const tr_texture_desc& t)
 {
-    const cudaChannelFormatDesc cd = cudaCreateChannelDescHalf4();
     cudaArray_t arr = nullptr;
-    TR_CUDA(c, cudaMallocArray(&arr, &cd, t.width, t.height));
-    c->texArrays.push_back(arr);
-    const size_t pitch = size_t(t.width) * 4 * sizeof(uint16_t);
-    TR_CUDA(c, cudaMemcpy2DToArray(arr, 0, 0, t.texels, pitch, pitch, t.height, cudaMemcpyHostToDevice));
-    cudaResourceDesc rd{};
-    rd.resType = cudaResourceTypeArray;
-    rd.res.array.array = arr;
-    cudaTextureDesc td{};
-    td.addressMode[0] = cudaAddressModeWrap;
-    td.addressMode[1] = cudaAddressModeWrap;
-    td.filterMode = cudaFilterModeLinear;
-    td.readMode = cudaReadModeElementType;
-    td.normalizedCoords = 1;
     cudaTextureObject_t obj = 0;
-    TR_CUDA(c, cudaCreateTextureObject(&obj, &rd, &td, nullptr));
+    const cudaError_t e = create_texture(t, &arr, &obj);
+    if (arr)
+        c->texArrays.push_back(arr);
+    if (e != cudaSuccess)
+        return cuda_fail(c, e, "create_texture");
     c->texObjects.push_back(obj);
     return TR_OK;
 }
@@ -609,6 +596,38 @@ bool convert_settings(const tr_kernel_settings& s, Settings* out, std::string* e
     return true;
 }
 
+} // namespace tr
+
+namespace tr {
+// Texture::Upload (Texture.cpp:83-139): RGBA binary16 texels in a CUDA array,
+// sampled with bilinear filtering, wrap addressing and normalised coordinates
+// (the same texture description as the reference's, so a texel fetch filters
+// the same way).
+cudaError_t create_texture(const tr_texture_desc& t, cudaArray_t* arrOut, cudaTextureObject_t* objOut)
+{
+    *arrOut = nullptr;
+    *objOut = 0;
+    const cudaChannelFormatDesc cd = cudaCreateChannelDescHalf4();
+    cudaArray_t arr = nullptr;
+    cudaError_t e = cudaMallocArray(&arr, &cd, t.width, t.height);
+    if (e != cudaSuccess)
+        return e;
+    *arrOut = arr;
+    const size_t pitch = size_t(t.width) * 4 * sizeof(uint16_t);
+    e = cudaMemcpy2DToArray(arr, 0, 0, t.texels, pitch, pitch, t.height, cudaMemcpyHostToDevice);
+    if (e != cudaSuccess)
+        return e;
+    cudaResourceDesc rd{};
+    rd.resType = cudaResourceTypeArray;
+    rd.res.array.array = arr;
+    cudaTextureDesc td{};
+    td.addressMode[0] = cudaAddressModeWrap;
+    td.addressMode[1] = cudaAddressModeWrap;
+    td.filterMode = cudaFilterModeLinear;
+    td.readMode = cudaReadModeElementType;
+    td.normalizedCoords = 1;
+    return cudaCreateTextureObject(objOut, &rd, &td, nullptr);
+}
 } // namespace tr
 
 extern "C" {

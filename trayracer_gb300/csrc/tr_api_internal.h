@@ -31,6 +31,11 @@ struct FrameWords {
     unsigned long long* traversal; // 4 counters
 };
 
+// A texture as the kernels sample it (RGBA binary16, bilinear, wrap,
+// normalised coordinates): its CUDA array (set as soon as allocated, so that a
+// caller can free it on an error) and texture object.
+cudaError_t create_texture(const tr_texture_desc& t, cudaArray_t* arr, cudaTextureObject_t* obj);
+
 // TR_OK with the views of a context that has a scene, a camera and a resolution.
 tr_status context_views(void* ctx, ContextViews* out);
 // The context's launch shape (its tuning applied) for `capacity` paths in

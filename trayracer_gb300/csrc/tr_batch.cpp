@@ -70,6 +70,8 @@ struct Batch {
     std::string lastError;
 
     void* sceneArena = nullptr;
+    std::vector<cudaArray_t> texArrays;            // the items' textures
+    std::vector<cudaTextureObject_t> texObjects;
     void* frameArena = nullptr;
     SceneView scene{};
     FrameView frame{};               // pool buffers; items, item count and state set per round
@@ -140,6 +142,10 @@ void release(Batch* b)
         cudaEventDestroy(b->evStop);
     if (b->sceneArena)
         cudaFree(b->sceneArena);
+    for (cudaTextureObject_t t : b->texObjects)
+        cudaDestroyTextureObject(t);
+    for (cudaArray_t a : b->texArrays)
+        cudaFreeArray(a);
     if (b->frameArena)
         cudaFree(b->frameArena);
     if (b->evFork)
@@ -263,8 +269,8 @@ tr_status tr_batch_create(const tr_config* config, const tr_batch_item* items, u
             return TR_ERR_INVALID_ARGUMENT;
         if (uint64_t(it.width) * it.height * it.spp > kRoundSamples)
             return TR_ERR_LIMIT;
-        if (!validate_scene(*it.scene).empty() || it.scene->instance_count || it.scene->material_textures)
-            return TR_ERR_INVALID_ARGUMENT;  // one-mesh untextured scenes only
+        if (!validate_scene(*it.scene).empty() || it.scene->instance_count)
+            return TR_ERR_INVALID_ARGUMENT;  // one-mesh scenes only
         pixels += uint64_t(it.width) * it.height;
         paths += uint64_t(it.width) * it.height * it.spp;
     }
@@ -304,6 +310,10 @@ tr_status tr_batch_create(const tr_config* config, const tr_batch_item* items, u
     std::vector<Material> materials;
     std::vector<LightTri> lights;
     std::vector<AliasEntry> alias;
+    std::vector<TexSlots> texSlots;  // per material, when an item has textures
+    bool anyTextures = false;
+    for (uint32_t i = 0; i < count; ++i)
+        anyTextures |= !built[i].flat.texSlots.empty();
     b->items.resize(count);
     uint64_t pixelBase = 0, triTotal = 0;
     for (uint32_t i = 0; i < count; ++i) {
@@ -332,6 +342,33 @@ tr_status tr_batch_create(const tr_config* config, const tr_batch_item* items, u
         for (uint32_t m : r.flat.matIdx)
             matIdx.push_back(m + matBase);
         materials.insert(materials.end(), r.flat.materials.begin(), r.flat.materials.end());
+        if (anyTextures) {
+            // the item's textures as texture objects; its slots name them (index + 1 before)
+            const size_t texBase = b->texObjects.size();
+            const tr_scene_desc& sd = *items[i].scene;
+            for (uint32_t k = 0; !r.flat.texSlots.empty() && k < sd.texture_count; ++k) {
+                cudaArray_t arr = nullptr;
+                cudaTextureObject_t obj = 0;
+                const cudaError_t te = create_texture(sd.textures[k], &arr, &obj);
+                if (arr)
+                    b->texArrays.push_back(arr);
+                if (te != cudaSuccess) {
+                    cudaGetLastError();
+                    return bail(te == cudaErrorMemoryAllocation ? TR_ERR_OUT_OF_MEMORY : TR_ERR_CUDA);
+                }
+                b->texObjects.push_back(obj);
+            }
+            if (r.flat.texSlots.empty()) {
+                texSlots.resize(texSlots.size() + r.flat.materials.size(), TexSlots{});
+            } else {
+                for (TexSlots slot : r.flat.texSlots) {
+                    for (uint32_t p = 0; p < TR_PROP_COUNT; ++p)
+                        if (slot.tex[p])
+                            slot.tex[p] = b->texObjects[texBase + size_t(slot.tex[p] - 1u)];
+                    texSlots.push_back(slot);
+                }
+            }
+        }
         for (LightTri L : r.flat.lights) {
             L.triIx += int32_t(primBase);
             lights.push_back(L);
@@ -385,6 +422,7 @@ tr_status tr_batch_create(const tr_config* config, const tr_batch_item* items, u
     const size_t oLights = take(lights.size() * sizeof(LightTri));
     const size_t oAlias = take(alias.size() * sizeof(AliasEntry));
     const size_t oXf = take(sizeof(identity));
+    const size_t oTex = take(texSlots.size() * sizeof(TexSlots));
     const size_t sceneBytes = off;
     cudaError_t e = cudaMalloc(&b->sceneArena, sceneBytes);
     if (e != cudaSuccess) {
@@ -404,6 +442,7 @@ tr_status tr_batch_create(const tr_config* config, const tr_batch_item* items, u
         up(oLights, lights.data(), lights.size() * sizeof(LightTri)),
         up(oAlias, alias.data(), alias.size() * sizeof(AliasEntry)),
         up(oXf, identity, sizeof(identity)),
+        up(oTex, texSlots.data(), texSlots.size() * sizeof(TexSlots)),
     };
     for (cudaError_t x : es)
         if (x != cudaSuccess)
@@ -418,6 +457,7 @@ tr_status tr_batch_create(const tr_config* config, const tr_batch_item* items, u
     sv.lights = reinterpret_cast<const LightTri*>(sb + oLights);
     sv.alias = reinterpret_cast<const AliasEntry*>(sb + oAlias);
     sv.invTransforms = reinterpret_cast<const float4*>(sb + oXf);
+    sv.texSlots = texSlots.empty() ? nullptr : reinterpret_cast<const TexSlots*>(sb + oTex);
     sv.nodeCount = uint32_t(nodes.size());
     sv.triCount = uint32_t(tris.size());
 
