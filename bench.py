@@ -335,44 +335,51 @@ def measure_batch(args, steps, warmup, with_ms1=True):
     st = KernelSettings(multiSample=1, maxDepth=6, seed=1, rrStart=3)
     samples = sum(s.width * s.height * s.spp for s in scenes)
 
+    def timed_batch(items):
+        """Median of `steps` graph-launched renders of a batch of `items` (L2 flushed before each),
+        and the batch's build time (BVHs and upload)."""
+        t0 = time.perf_counter()
+        bb = tr.BatchRenderer(items, pool_paths=args.pool_paths)
+        built_s = time.perf_counter() - t0
+        for _ in range(warmup):
+            bb.Render(st, stream=sptr)
+        torch.cuda.synchronize()
+        ts = []
+        with ClockSampler(0) as clk:
+            for _ in range(steps):
+                flush.fill_(1.0)
+                e0 = torch.cuda.Event(enable_timing=True)
+                e1 = torch.cuda.Event(enable_timing=True)
+                e0.record(stream)
+                bb.Render(st, stream=sptr)
+                e1.record(stream)
+                e1.synchronize()
+                ts.append(e0.elapsed_time(e1))
+        stats_, info_ = bb.Statistics(), bb.Info()
+        assert stats_["device_error"] == 0
+        bb.close()
+        return float(statistics.median(ts)), stats_, info_, clk.summary(), built_s
+
     # batched: one continuous wavefront, one graph launch
-    t = time.perf_counter()
-    b = tr.BatchRenderer(scenes, pool_paths=args.pool_paths)
-    build_s = time.perf_counter() - t
-    info = b.Info()
     if args.profile:
+        b = tr.BatchRenderer(scenes, pool_paths=args.pool_paths)
         b.Render(st, stream=sptr, use_graph=False)
         out = {"batch": b.Statistics(), "info": b.Info()}
         b.close()
         return out
-    for _ in range(warmup):
-        b.Render(st, stream=sptr)
-    torch.cuda.synchronize()
-    times = []
-    with ClockSampler(0) as clocks:
-        for _ in range(steps):
-            flush.fill_(1.0)
-            e0 = torch.cuda.Event(enable_timing=True)
-            e1 = torch.cuda.Event(enable_timing=True)
-            e0.record(stream)
-            b.Render(st, stream=sptr)
-            e1.record(stream)
-            e1.synchronize()
-            times.append(e0.elapsed_time(e1))
-    bstats = b.Statistics()
-    info = b.Info()
-    assert bstats["device_error"] == 0
-    batch_ms = float(statistics.median(times))
+    batch_ms, bstats, info, batch_clocks, build_s = timed_batch(scenes)
     rays = bstats["extend_rays"] + bstats["shadow_rays"]
-    b.close()
 
     # per scene: one context, each scene uploaded (untimed) and rendered as spp / ms graph frames,
     # with ms = min(spp, 16) (the reference's largest multi-sample) and with ms = 1 (its default,
     # Renderer.cpp:259)
     r = tr.DeviceRenderer(0)
 
+    per_item_ms = []
+
     def per_scene(max_ms):
         total_ms, total_rays, n_launch = 0.0, 0, 0
+        per_item_ms.clear()
         with ClockSampler(0) as pclocks:
             for s in scenes:
                 ms = min(s.spp, max_ms)
@@ -394,6 +401,7 @@ def measure_batch(args, steps, warmup, with_ms1=True):
                     e1.synchronize()
                     elapsed = e0.elapsed_time(e1)
                 total_ms += elapsed
+                per_item_ms.append(elapsed)
                 r.Reset()
                 for _ in range(frames):
                     r.RenderFrame(stream=sptr, use_graph=False)
@@ -402,6 +410,11 @@ def measure_batch(args, steps, warmup, with_ms1=True):
         return total_ms, total_rays, n_launch, pclocks.summary()
 
     plain_ms, plain_rays, launches, plain_clocks = per_scene(16)
+    # the mix without its 1024^2 items, whose per-scene frames already fill the GPU: a batch of
+    # the smaller items alone against their per-scene frames
+    small = [k for k, s in enumerate(scenes) if s.width * s.height < 1024 * 1024]
+    small_ms, _, small_info, _, _ = timed_batch([scenes[k] for k in small])
+    small_per_scene_ms = float(sum(per_item_ms[k] for k in small))
     out = {
         "iterations": bstats["iterations"],
         "launches": bstats["launches"],
@@ -409,7 +422,11 @@ def measure_batch(args, steps, warmup, with_ms1=True):
         "batch_ms": batch_ms,
         "batch_rays": int(rays),
         "info": info,
-        "clocks": clocks.summary(),
+        "clocks": batch_clocks,
+        "items_below_1024sq": {"count": len(small), "samples": int(small_info["path_count"]),
+                               "batched_ms": round(small_ms, 3), "per_scene_ms": round(small_per_scene_ms, 3),
+                               "batched_over_per_scene": round(small_per_scene_ms / small_ms, 3),
+                               "per_scene_ms_1024sq_items": round(plain_ms - small_per_scene_ms, 3)},
         "per_scene": {"ms": round(plain_ms, 3), "samples_per_s": round(samples / (plain_ms / 1e3), 1),
                       "mrays_per_s": round(plain_rays / (plain_ms / 1e3) / 1e6, 1), "gpu_launches": launches,
                       "clocks": plain_clocks},
@@ -454,7 +471,8 @@ def run_batch(args):
         "mrays_per_s": round(m["batch_rays"] / (batch_ms / 1e3) / 1e6, 1),
         "gpu_launches": m["launches"],
         **{k: m.get(k) for k in ("per_scene", "per_scene_ms1", "speedup_vs_per_scene", "speedup_vs_per_scene_ms1",
-                                 "rays_per_scene", "scene_generation_s", "batch_build_s", "clocks")},
+                                 "items_below_1024sq", "rays_per_scene", "scene_generation_s", "batch_build_s",
+                                 "clocks")},
         "rays_batch": m["batch_rays"],
     }
     print(json.dumps(line), flush=True)
@@ -871,6 +889,7 @@ def main():
             "iterations": m["iterations"],
             "pool_paths": m["info"]["pool_paths"],
             "gpu_launches": m["launches"],
+            "items_below_1024sq": m["items_below_1024sq"],
             "workload": f"{args.batch_count} sphere scenes ({m['info']['triangle_count']} tris, "
                         f"{m['info']['pixel_count']} pixels, 4/16/64 spp, 6 bounces, RR from 3); per scene: "
                         f"tr_render_frame graph frames at multi_sample min(spp, 16)",
