@@ -460,17 +460,17 @@ __global__ void __launch_bounds__(128, 8) extend_kernel(SceneView s, FrameView f
         const uint32_t idle = __ballot_sync(kFull, !alive && more);
         if (idle) {
             const uint32_t leader = __ffs(idle) - 1u;
-            uint32_t base = 0;
+            uint32_t first = 0;
             if (lane == leader)
-                base = atomicAdd(work, __popc(idle));
-            base = __shfl_sync(kFull, base, leader);
+                first = atomicAdd(work, __popc(idle));
+            first = __shfl_sync(kFull, first, leader);
             // batched: the item of the first new sample of this refill, found by the
             // whole warp (the first sample ids of 32 items per load and a ballot, in
             // place of a binary search per lane); the refill's new sample ids are
             // consecutive, so a lane's own item is at most a few further
             uint32_t warpItem = 0;
-            if (BATCH && f.itemCount > 1u && base + __popc(idle) > carried && base < count) {
-                const uint32_t firstFresh = freshBase + (base > carried ? base - carried : 0u);
+            if (BATCH && f.itemCount > 1u && first + __popc(idle) > carried && first < count) {
+                const uint32_t firstFresh = freshBase + (first > carried ? first - carried : 0u);
                 for (uint32_t j0 = 1u; j0 < f.itemCount; j0 += 32u) {
                     const uint32_t j = j0 + lane;
                     const uint32_t m =
@@ -481,7 +481,7 @@ __global__ void __launch_bounds__(128, 8) extend_kernel(SceneView s, FrameView f
                 }
             }
             if (!alive && more) {
-                const uint32_t i = base + __popc(idle & ((1u << lane) - 1u));
+                const uint32_t i = first + __popc(idle & ((1u << lane) - 1u));
                 if (i < count) {
                     if (BATCH ? i >= carried : PRIMARY) {
                         float3 O, D;
