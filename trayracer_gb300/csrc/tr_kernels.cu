@@ -1135,8 +1135,13 @@ __global__ void __launch_bounds__(256) sort_scatter_kernel(FrameView f, SortView
 // Any hit of the bounce's shadow queue over [eps, dist - 2 eps]; an unoccluded
 // ray adds its radiance to its path. Same lane refill as extend_kernel.
 // Blocks of 64 or 128 threads (LaunchShape::traversalThreads): the kernel works per warp.
+// One-level scenes: 56 registers, 9 blocks of 128 threads per SM (the kernel is bound by
+// the latency of its node fetches; 31.3 against 33.1 ms of shadow rays per 1080p, 64 spp
+// heightfield step at 72 registers and 7 blocks). Two-level traversal holds more state and
+// keeps its own register count (it would spill 100-210 bytes at 56).
 template <bool COUNT, bool BATCH, bool TL, int LAYOUT = kLayoutScene>
-__global__ void __launch_bounds__(128) connect_kernel(SceneView s, FrameView f, Settings st, uint32_t bounce)
+__global__ void __launch_bounds__(128, TL ? 1 : 9) connect_kernel(SceneView s, FrameView f, Settings st,
+                                                                   uint32_t bounce)
 {
     const uint32_t count = BATCH ? __ldcg(&f.batch->connectQueue) : __ldcg(f.counters + kShadowCounterBase + bounce);
     const uint32_t cap = f.capacity;
